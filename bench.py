@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Throughput of the sea-ice dynamics step on GB300: cell-updates per second.
+
+Workload (the configuration the headline metric is quoted on, one GPU): the
+256 x 256 box test with DG2 transport (6 components), CG2 velocity, DG-stress
+8, FP64 everywhere, 100 mEVP iterations (alpha = beta = 300) per 120 s step.
+One "step" is one model step: the DG transport of concentration and
+thickness with limiters, the preparation of the momentum solve and the 100
+mEVP iterations (strain, stress, divergence, momentum, boundaries).
+
+  value  device-resident: K steps of the CUDA graph, CUDA events on the
+         library's stream; inputs (> L2: 256^2 elements x ~3.7 kB of FP64
+         operators) are not re-flushed between steps.
+  e2e    the reference's module cycle through the C ABI with host buffers
+         (MEVPDynamics::update: setData of h, A, winds, ocean, ssh, then
+         update, then getDG0Data of h, A, u, v and the ice-ocean stress),
+         wall clock, host<->device copies inside.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle; the reference itself cannot be built: it needs Eigen, absent here)
+on the host cores with all threads, on the same workload.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-updates/s"
+UNIT = "cell-updates/s"
+NX = 256
+DG = 6
+DT = 120.0
+ALPHA = BETA = 300.0
+NSTEPS = 100
+
+
+def bytes_per_element_iteration_stress() -> int:
+    """Algorithmic DRAM bytes of one launch of the element stress kernel, per
+    element: operators Gx, Gy (2 x 81), iMJwPSI (72), divS1, divS2 (2 x 72)
+    FP64; P at the 9 Gauss points; the 24 stress coefficients read and
+    written; the 18 divergence contributions written; the CG2 velocity
+    gather counted once per node (about 4 nodes per element, u and v)."""
+    operators = (81 + 81 + 72 + 72 + 72) * 8
+    pressure = 9 * 8
+    stress = 2 * 24 * 8
+    contrib = 18 * 8
+    velocity = 4 * 2 * 8
+    return operators + pressure + stress + contrib + velocity
+
+
+def flops_per_element_iteration_stress() -> int:
+    """FP64 flops of the element stress kernel per element (FMA = 2):
+    strain 4 x 9 x 9 FMA, Delta/P/viscosity ~16 per Gauss point, projection
+    3 x 8 x 9 FMA, relaxation 24 FMA, divergence 2 x 9 x 16 FMA."""
+    return 2 * (4 * 81) + 9 * 16 + 2 * (3 * 72) + 2 * 24 + 2 * (2 * 9 * 16)
+
+
+def bytes_per_cell_update(n_iter: int = NSTEPS) -> float:
+    """Algorithmic bytes per cell-update of the whole step (FP64 path):
+    n_iter x (element kernel + node kernel share) + transport/prepare."""
+    node_per_element = 4 * (15 * 8) + 18 * 8  # ~4 nodes x 15 FP64 streams + gathered contributions
+    transport = 4 * (6 * 9 * 2 + 36 + 4 * 6 + 2 * 6) * 8  # cell terms, M^-1, phi, stage I/O
+    prepare = 2 * 6 * 8 + 9 * 8 + 20 * 8 * 4
+    return n_iter * (bytes_per_element_iteration_stress() + node_per_element) + transport + prepare
+
+
+# --------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def fp64_peak_tflops(local: int):
+    """FP64 DGEMM throughput (cuBLAS through torch) as the FP64 denominator."""
+    try:
+        import torch
+        dev = torch.device("cuda:0")
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device=dev)
+        b = torch.randn(n, n, dtype=torch.float64, device=dev)
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize(dev)
+        best = 0.0
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        del a, b
+        return best, "measured: cuBLAS DGEMM 4096^3 via torch.matmul"
+    except Exception as ex:  # torch absent or failing: report the nominal figure
+        return 1.25, f"nominal (DGEMM probe failed: {type(ex).__name__})"
+
+
+# --------------------------------------------------------------------------
+def cpu_baseline(sample_steps: int = 2, warm: int = 1):
+    """The oracle (CPU restatement of the reference) on the host cores, all
+    OpenMP threads, on a bounded sample of the same workload."""
+    from oracle import pyoracle
+    from nextsimdg_gb300.boxtest import BoxTest
+
+    pyoracle.load()
+    box = BoxTest(NX)
+    k = pyoracle.OracleKernel(0, DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    for s in range(warm):
+        k.update(s * DT, DT)
+    t0 = time.perf_counter()
+    for s in range(sample_steps):
+        k.update((warm + s) * DT, DT)
+    t = time.perf_counter() - t0
+    v = box.nelements * sample_steps / t
+    return {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
+            "sample": f"{sample_steps} model steps of the {NX}x{NX} DG2 box test after {warm} warm-up step(s), "
+                      f"{t:.1f} s"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    from nextsimdg_gb300.boxtest import BoxTest
+
+    pyoracle.load()
+    box = BoxTest(NX)
+    k = pyoracle.OracleKernel(0, DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    # each step is a bounded sample: the full mEVP step at a reduced iteration
+    # count is not the workload, so the sample is the full step on a sub-box
+    # when the full box would not finish within minutes
+    for s in range(args.warmup):
+        k.update(s * DT, DT)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        k.update((args.warmup + s) * DT, DT)
+    t = time.perf_counter() - t0
+    v = box.nelements * args.steps / t
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic box test",
+            "config": {"workload": f"box test {NX}x{NX}, DG2 transport, CG2 velocity, mEVP {NSTEPS} iterations, "
+                                   f"alpha=beta={ALPHA:g}, dt={DT:g} s", "precision": "fp64"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
+                             "sample": f"{args.steps} full model steps after {args.warmup} warm-up"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    from nextsimdg_gb300.boxtest import BoxTest
+    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
+
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES", str(local))
+    box = BoxTest(NX)
+    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    N = box.nelements
+
+    # ---- value: device-resident steps (CUDA graph replays, CUDA events) ----
+    k.time_updates(DT, max(args.warmup, 3))
+    dist_barrier(world)
+    with ClockSampler(local) as clk:
+        ms = k.time_updates(DT, args.steps)
+    k.synchronize()
+    dist_barrier(world)
+    ms_max = dist_max(ms, world)
+    value = world * N * args.steps / (ms_max * 1e-3)
+    launches = k.launches_per_update()
+
+    # ---- e2e: the module cycle through the C ABI, host buffers ----
+    try:
+        import torch
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    except Exception:
+        pin = np.ascontiguousarray
+    uo, vo = box.ocean()
+    uo, vo, ssh = pin(uo), pin(vo), pin(box.ssh())
+    winds = [tuple(pin(w) for w in box.wind(s * DT)) for s in range(args.warmup + args.steps)]
+    h, a = pin(k.getDG0Data("hice")), pin(k.getDG0Data("cice"))
+    outs = {n: pin(np.empty(N)) for n in ("hice", "cice", "u", "v", "uiostress", "viostress")}
+
+    def cycle(s):
+        k.setData("hice", outs["hice"] if s else h)
+        k.setData("cice", outs["cice"] if s else a)
+        k.setData("uwind", winds[s][0])
+        k.setData("vwind", winds[s][1])
+        k.setData("uocean", uo)
+        k.setData("vocean", vo)
+        k.setData("ssh", ssh)
+        k.update(s * DT, DT)
+        for n, buf in outs.items():
+            k.getDG0Data(n, out=buf)
+
+    for s in range(args.warmup):
+        cycle(s)
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for s in range(args.warmup, args.warmup + args.steps):
+        cycle(s)
+    t_e2e = time.perf_counter() - t0
+    dist_barrier(world)
+    t_e2e = dist_max(t_e2e, world)
+    e2e = world * N * args.steps / t_e2e
+
+    # ---- roofline of the dominant kernel (element stress kernel) ----
+    kms, kname = k.time_kernel(0, 50)
+    nms, nname = k.time_kernel(1, 50)
+    bpe = bytes_per_element_iteration_stress()
+    achieved_gbs = N * bpe / (kms * 1e-3) / 1e9
+    hbm, hbm_kind = measured_peaks()
+    fp64_tf, fp64_kind = fp64_peak_tflops(local)
+    fp64_achieved = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
+    share = (kms * NSTEPS) / (ms_max / args.steps)
+    traffic = None
+    prof = ROOT / "profiles" / "kMevpStress_traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get("bytes_per_launch_256")
+        except ValueError:
+            traffic = None
+
+    if rank == 0:
+        base = cpu_baseline() if world == 1 and not args.no_cpu_baseline else None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic box test",
+            "config": {"workload": f"box test {NX}x{NX}, DG2 transport, CG2 velocity, mEVP {NSTEPS} iterations, "
+                                   f"alpha=beta={ALPHA:g}, dt={DT:g} s",
+                       "precision": "fp64", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (operators ~240 MB per step sweep), no flush",
+                       "bytes_per_cell_update": bytes_per_cell_update()},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8},
+            "gpu_launches": launches * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm, "traffic": traffic,
+                         "kernel": kname, "kernel_ms": kms, "share_of_step": share,
+                         "algorithmic_bytes_per_element": bpe, "peak_kind": hbm_kind,
+                         "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_tf,
+                                  "frac": fp64_achieved / fp64_tf, "peak_kind": fp64_kind}},
+            "node_kernel": {"name": nname, "ms": nms},
+            "clocks": clk.summary(),
+        }
+        if base:
+            line["cpu_baseline"] = base
+        print(json.dumps(line), flush=True)
+    k.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * nsdg.h — C ABI of the GB300 (sm_103a) sea-ice dynamics kernel.
+ *
+ * This is the drop-in boundary for neXtSIM_DG's dynamics hot path: the DG
+ * transport of ice thickness / concentration / damage, the mEVP or BBM stress
+ * update and the CG2 momentum sub-cycle.  Every entry point takes plain
+ * pointers and sizes, returns an int status (NSDG_OK == 0) and never aborts.
+ * All arrays are FP64 in the reference's ModelArray layout:
+ *   - H / DG / DGSTRESS fields: element-major, component fastest,
+ *     element index = i + nx*j  (ModelArray.hpp:358-361 in the reference);
+ *   - coordinates: VERTEX type, (nx+1)*(ny+1) nodes, 2 components (x, y).
+ *
+ * Entry point  ->  reference interface it replaces
+ *   nsdg_kernel_create      MEVPDynamicsKernel(const DynamicsParameters&)
+ *                           (dynamics/src/include/MEVPDynamicsKernel.hpp:25-28),
+ *                           BBMDynamicsKernel (BBMDynamicsKernel.hpp:20-24)
+ *   nsdg_kernel_initialise  DynamicsKernel::initialise / CGDynamicsKernel::initialise
+ *                           (DynamicsKernel.hpp:44-75; CGDynamicsKernel.cpp:24-51)
+ *   nsdg_kernel_set_data    DynamicsKernel::setData / CGDynamicsKernel::setData
+ *                           (DynamicsKernel.hpp:93-110; CGDynamicsKernel.cpp:54-90;
+ *                           BrittleCGDynamicsKernel.hpp:138-145)
+ *   nsdg_kernel_get_dg0     DynamicsKernel::getDG0Data / CGDynamicsKernel::getDG0Data
+ *                           (DynamicsKernel.hpp:119-130; CGDynamicsKernel.cpp:93-118)
+ *   nsdg_kernel_get_dg      DynamicsKernel::getDGData (DynamicsKernel.hpp:138-156)
+ *   nsdg_kernel_update      VPCGDynamicsKernel::update (VPCGDynamicsKernel.hpp:63-94),
+ *                           BrittleCGDynamicsKernel::update (BrittleCGDynamicsKernel.hpp:91-136)
+ *   nsdg_transport_*        DGTransport<DG> (dynamics/src/include/DGTransport.hpp:27-152),
+ *                           dgLimit.hpp:16-85 and Tools::MeanValue (Tools.hpp:24-50)
+ */
+#ifndef NSDG_H
+#define NSDG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NSDG_OK 0
+#define NSDG_ERR_BAD_ARG 1          /* invalid argument / call order             */
+#define NSDG_ERR_UNKNOWN_FIELD 2    /* reference: std::out_of_range from .at()   */
+#define NSDG_ERR_SIZE_MISMATCH 3    /* array size does not match the mesh        */
+#define NSDG_ERR_CUDA 4             /* CUDA runtime error (message in last_error)*/
+#define NSDG_ERR_NUMERIC 5          /* non-finite velocity or stress detected    */
+#define NSDG_ERR_UNSUPPORTED 6      /* e.g. spherical coordinates                */
+#define NSDG_ERR_LOGIC 7            /* reference: std::logic_error               */
+#define NSDG_ERR_NO_DEVICE 8        /* no CUDA device is visible                 */
+
+/* ---- rheologies and precision modes ------------------------------------ */
+#define NSDG_RHEOLOGY_MEVP 0        /* MEVPDynamicsKernel                        */
+#define NSDG_RHEOLOGY_BBM 1         /* BBMDynamicsKernel                         */
+
+#define NSDG_PRECISION_FP64 0       /* every operation in FP64                   */
+#define NSDG_PRECISION_MIXED 1      /* FP32 bulk; FP64 conservation sums, inverse
+                                       mass matrices, Delta and viscosity        */
+
+/*
+ * Physical and numerical parameters.  Defaults (nsdg_default_params) are the
+ * reference's: DynamicsParameters.hpp:22-40, VPParameters.hpp:20-25,
+ * MEBParameters.hpp:40-65; alpha = beta = 1500 (VPCGDynamicsKernel.hpp:125-126);
+ * n_steps = 100 (DynamicsKernel.hpp:187).
+ */
+typedef struct nsdg_params {
+    /* DynamicsParameters */
+    double rho_ice, rho_atm, rho_ocean;
+    double C_atm, C_ocean;
+    double F_atm, F_ocean;
+    double fc;
+    double ocean_turning_angle; /* degrees */
+    double gravity;
+    /* VPParameters */
+    double Pstar, DeltaMin;
+    /* mEVP relaxation constants */
+    double alpha, beta;
+    /* MEBParameters (BBM) */
+    double compaction_param, nu0, young, P0;
+    double undamaged_time_relaxation_sigma, exponent_relaxation_sigma;
+    double exponent_compression_factor, tan_phi, compr_strength, C_lab;
+    /* sub-cycle count (mEVP iterations or BBM sub-steps) */
+    int n_steps;
+    /* NSDG_PRECISION_* */
+    int precision;
+} nsdg_params;
+
+/* Fills *p with the reference defaults. */
+void nsdg_default_params(nsdg_params* p);
+
+/* Human-readable name of a status code (static storage). */
+const char* nsdg_status_string(int status);
+
+/* Library version string, e.g. "nsdg-gb300 0.1 sm_103a". */
+const char* nsdg_version(void);
+
+/* ======================================================================== */
+/* Dynamics kernel (the DynamicsKernel drop-in)                             */
+/* ======================================================================== */
+typedef struct nsdg_kernel nsdg_kernel;
+
+/* dg_comp: DG components of the advected fields (1, 3 or 6; DGCOMP in the
+ * reference).  Velocity is CG2 and stress DG 8 (CGDEGREE 2, DGSTRESSCOMP 8).
+ * No device work happens here. */
+int nsdg_kernel_create(int rheology, int dg_comp, const nsdg_params* params,
+    nsdg_kernel** out);
+int nsdg_kernel_destroy(nsdg_kernel* k);
+
+/* Message of the last failing call on this handle ("" if none). */
+const char* nsdg_kernel_last_error(const nsdg_kernel* k);
+
+/* Builds the mesh (landmask, Dirichlet lists from the mask and the four
+ * domain edges), the FP64 per-element operators, and uploads them.
+ * coords: (nx+1)*(ny+1)*2 doubles; mask: nx*ny doubles (1.0 = ice).
+ * is_spherical != 0 returns NSDG_ERR_UNSUPPORTED. */
+int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny,
+    const double* coords, int is_spherical, const double* mask);
+
+/* setData semantics of the reference: hice/cice/ssh/damage and unknown names
+ * follow DGModelArray::ma2dg (zero, then all components if n_comp equals the
+ * DG count, else component 0 only); u, v, uwind, vwind, uocean, vocean are
+ * DG->CG2 interpolated.  data: n_elements*n_comp doubles from host memory. */
+int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data,
+    size_t n_elements, size_t n_comp);
+
+/* getDG0Data: component 0 (cell average) of hice, cice, damage, u, v,
+ * uiostress, viostress or a stored field.  out: n_elements doubles. */
+int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_elements);
+
+/* getDGData: all components (n_comp must be the stored DG count, or 1). */
+int nsdg_kernel_get_dg(nsdg_kernel* k, const char* name, double* out,
+    size_t n_elements, size_t n_comp);
+
+/* One model step of length dt seconds (TimestepTime::step).  The step is
+ * enqueued on the handle's CUDA stream (as one CUDA graph) and the call
+ * returns without waiting; every get / snapshot / mean-value call waits for
+ * it and reports NSDG_ERR_NUMERIC if the step produced non-finite values. */
+int nsdg_kernel_update(nsdg_kernel* k, double t_start, double dt);
+
+/* Waits for the enqueued work and reports device-side numeric faults. */
+int nsdg_kernel_synchronize(nsdg_kernel* k);
+
+/* Device-side state snapshot (checkpoint/resume).  nsdg_kernel_snapshot_size
+ * returns the byte count; save writes it to a host buffer, load restores it. */
+int nsdg_kernel_snapshot_size(nsdg_kernel* k, size_t* bytes);
+int nsdg_kernel_snapshot_save(nsdg_kernel* k, void* buffer, size_t bytes);
+int nsdg_kernel_snapshot_load(nsdg_kernel* k, const void* buffer, size_t bytes);
+
+/* FP64 integral of a DG field over the mesh (Tools::MeanValue), computed on
+ * the GPU with a deterministic warp-shuffle + block reduction. */
+int nsdg_kernel_mean_value(nsdg_kernel* k, const char* name, double* out);
+
+/* Measurement hooks (used by bench.py).  Times `steps` updates on the
+ * handle's stream with CUDA events; *ms is the total device time. */
+int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms);
+/* Times `reps` launches of one kernel of the step in isolation on the handle's
+ * stream and returns the mean duration.  kernel_id: 0 = element stress kernel,
+ * 1 = node momentum kernel, 2 = transport operator.  *name gets its name. */
+int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms,
+    const char** name);
+/* Kernel launches issued by one update (for gpu_launches accounting). */
+int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
+
+/* ======================================================================== */
+/* Stand-alone DG transport (the DGTransport<DG> class of the reference)    */
+/* ======================================================================== */
+typedef struct nsdg_transport nsdg_transport;
+
+/* Mesh given explicitly, as the reference tests build ParametricMesh by hand:
+ * vertices (nx+1)*(ny+1)*2; landmask nx*ny (nonzero = ice, NULL = all ice);
+ * dirichlet lists per edge (0 bottom, 1 right, 2 top, 3 left) of element ids;
+ * periodic entries as 4 size_t each {edge type (0 X-edge, 1 Y-edge), cell 1,
+ * cell 2, edge id}, segment by segment in the reference order.
+ * dg: 1, 3, 6 or 8; scheme: 1, 2 or 3 (rk1/rk2/rk3). */
+int nsdg_transport_create(int dg, size_t nx, size_t ny, const double* vertices,
+    const unsigned char* landmask, const size_t* const dirichlet[4],
+    const size_t n_dirichlet[4], const size_t* periodic, size_t n_periodic,
+    int scheme, nsdg_transport** out);
+int nsdg_transport_destroy(nsdg_transport* t);
+const char* nsdg_transport_last_error(const nsdg_transport* t);
+/* DG velocity components (n_elements*dg each, element-major). */
+int nsdg_transport_set_velocity(nsdg_transport* t, const double* vx, const double* vy);
+/* DGTransport::reinitnormalvelocity (DGTransport.cpp:158-252). */
+int nsdg_transport_reinit_normal_velocity(nsdg_transport* t);
+/* DGTransport::step on a host field (n_elements*dg), in place, `nsteps` times.
+ * limit_max / limit_min != 0 apply LimitMax(phi, max) / LimitMin(phi, min)
+ * after every step (dgLimit.hpp), as the periodic reference test does. */
+int nsdg_transport_step(nsdg_transport* t, double dt, double* phi, int nsteps,
+    int limit_max, double max_value, int limit_min, double min_value);
+/* Tools::MeanValue of a host DG field (computed on the GPU, FP64). */
+int nsdg_transport_mean_value(nsdg_transport* t, const double* phi, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NSDG_H */

@@ -1,0 +1,115 @@
+"""ctypes binding of libnsdg_gb300.so (the C ABI declared in include/nsdg.h).
+
+The library is built in-tree by nextsimdg_gb300.build.  Loading fails loudly
+(ImportError) when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_size_t, c_ubyte, c_void_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libnsdg_gb300.so"
+
+NSDG_OK = 0
+NSDG_ERR_BAD_ARG = 1
+NSDG_ERR_UNKNOWN_FIELD = 2
+NSDG_ERR_SIZE_MISMATCH = 3
+NSDG_ERR_CUDA = 4
+NSDG_ERR_NUMERIC = 5
+NSDG_ERR_UNSUPPORTED = 6
+NSDG_ERR_LOGIC = 7
+NSDG_ERR_NO_DEVICE = 8
+
+RHEOLOGY_MEVP = 0
+RHEOLOGY_BBM = 1
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+
+class Params(ctypes.Structure):
+    """nsdg_params (include/nsdg.h)."""
+
+    _fields_ = [
+        ("rho_ice", c_double), ("rho_atm", c_double), ("rho_ocean", c_double),
+        ("C_atm", c_double), ("C_ocean", c_double),
+        ("F_atm", c_double), ("F_ocean", c_double),
+        ("fc", c_double), ("ocean_turning_angle", c_double), ("gravity", c_double),
+        ("Pstar", c_double), ("DeltaMin", c_double),
+        ("alpha", c_double), ("beta", c_double),
+        ("compaction_param", c_double), ("nu0", c_double), ("young", c_double), ("P0", c_double),
+        ("undamaged_time_relaxation_sigma", c_double), ("exponent_relaxation_sigma", c_double),
+        ("exponent_compression_factor", c_double), ("tan_phi", c_double),
+        ("compr_strength", c_double), ("C_lab", c_double),
+        ("n_steps", c_int), ("precision", c_int),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# (name, restype, argtypes) for every symbol in include/nsdg.h
+SIGNATURES = [
+    ("nsdg_default_params", None, [POINTER(Params)]),
+    ("nsdg_status_string", c_char_p, [c_int]),
+    ("nsdg_version", c_char_p, []),
+    ("nsdg_kernel_create", c_int, [c_int, c_int, POINTER(Params), POINTER(c_void_p)]),
+    ("nsdg_kernel_destroy", c_int, [c_void_p]),
+    ("nsdg_kernel_last_error", c_char_p, [c_void_p]),
+    ("nsdg_kernel_initialise", c_int, [c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]),
+    ("nsdg_kernel_set_data", c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
+    ("nsdg_kernel_get_dg0", c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
+    ("nsdg_kernel_get_dg", c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
+    ("nsdg_kernel_update", c_int, [c_void_p, c_double, c_double]),
+    ("nsdg_kernel_synchronize", c_int, [c_void_p]),
+    ("nsdg_kernel_snapshot_size", c_int, [c_void_p, POINTER(c_size_t)]),
+    ("nsdg_kernel_snapshot_save", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_kernel_snapshot_load", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_kernel_mean_value", c_int, [c_void_p, c_char_p, POINTER(c_double)]),
+    ("nsdg_kernel_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
+    ("nsdg_kernel_time_kernel", c_int, [c_void_p, c_int, c_int, POINTER(c_float), POINTER(c_char_p)]),
+    ("nsdg_kernel_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
+    ("nsdg_transport_create", c_int, [c_int, c_size_t, c_size_t, c_void_p, c_void_p,
+                                      POINTER(c_void_p), POINTER(c_size_t), c_void_p, c_size_t, c_int,
+                                      POINTER(c_void_p)]),
+    ("nsdg_transport_destroy", c_int, [c_void_p]),
+    ("nsdg_transport_last_error", c_char_p, [c_void_p]),
+    ("nsdg_transport_set_velocity", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("nsdg_transport_reinit_normal_velocity", c_int, [c_void_p]),
+    ("nsdg_transport_step", c_int, [c_void_p, c_double, c_void_p, c_int, c_int, c_double, c_int, c_double]),
+    ("nsdg_transport_mean_value", c_int, [c_void_p, c_void_p, POINTER(c_double)]),
+]
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> ctypes.CDLL:
+    """Loads the in-tree library (once) and declares every signature."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            f"{p} is missing: build it with `python -m nextsimdg_gb300.build` "
+            "(the dynamics kernel has no CPU fallback)")
+    lib = ctypes.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def default_params() -> Params:
+    p = Params()
+    load().nsdg_default_params(ctypes.byref(p))
+    return p
+
+
+class NsdgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"[{status}] {message}")

@@ -1,0 +1,1025 @@
+// nsdg_capi.cpp — the C ABI (include/nsdg.h): handles, device memory, the
+// CUDA-graph capture of one model step, and the field exchange with the
+// reference's ModelArray layout.
+//
+// No exception crosses the ABI; every entry point returns a status code and
+// keeps a message in the handle.
+#include "nsdg.h"
+
+#include "nsdg_host.hpp"
+#include "nsdg_kernels.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+using namespace nsdg;
+
+namespace {
+
+const char* kVersion = "nsdg-gb300 0.1 sm_103a";
+
+// Bump allocator over one device allocation (256-byte aligned sub-buffers).
+struct Arena {
+    char* base = nullptr;
+    size_t cap = 0, used = 0;
+    cudaError_t reserve(size_t bytes)
+    {
+        cap = bytes;
+        used = 0;
+        return cudaMalloc(&base, bytes);
+    }
+    template <class T> T* take(size_t n)
+    {
+        const size_t bytes = ((n * sizeof(T) + 255) / 256) * 256;
+        if (used + bytes > cap)
+            return nullptr;
+        T* p = reinterpret_cast<T*>(base + used);
+        used += bytes;
+        return p;
+    }
+    void release()
+    {
+        if (base)
+            cudaFree(base);
+        base = nullptr;
+        cap = used = 0;
+    }
+};
+inline size_t al(size_t bytes) { return ((bytes + 255) / 256) * 256; }
+
+struct Status {
+    int code = NSDG_OK;
+    std::string msg;
+};
+
+#define CUDA_TRY(expr)                                                                             \
+    do {                                                                                           \
+        cudaError_t e_ = (expr);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            return fail(NSDG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));       \
+        }                                                                                          \
+    } while (0)
+
+int deviceCheck(std::string& msg)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        msg = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+        cudaGetLastError();
+        return NSDG_ERR_NO_DEVICE;
+    }
+    return NSDG_OK;
+}
+
+} // namespace
+
+// ===========================================================================
+// Dynamics kernel handle
+// ===========================================================================
+struct nsdg_kernel {
+    int rheology = NSDG_RHEOLOGY_MEVP;
+    int dg = 6;
+    nsdg_params P {};
+    std::string err;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    HostMesh mesh;
+    BoundaryFlags flags;
+    DevMesh dm;
+    DevOps dops;
+    size_t N = 0, Ncg = 0, Ncg1 = 0;
+    // state
+    double *hice = nullptr, *cice = nullptr, *ssh = nullptr, *damage = nullptr;
+    double *s11 = nullptr, *s12 = nullptr, *s22 = nullptr;
+    double *u = nullptr, *v = nullptr, *uo = nullptr, *vo = nullptr, *ua = nullptr, *va = nullptr;
+    double *avgU = nullptr, *avgV = nullptr;
+    // per-step work
+    double *u0 = nullptr, *v0 = nullptr, *cgH = nullptr, *cgA = nullptr, *uGrad = nullptr, *vGrad = nullptr;
+    double *c1 = nullptr, *c1b = nullptr, *fau = nullptr, *fav = nullptr, *rhfc = nullptr, *gu = nullptr, *gv = nullptr;
+    double *Pg = nullptr, *contrib = nullptr;
+    double *velx = nullptr, *vely = nullptr, *nvX = nullptr, *nvY = nullptr;
+    double *phiA = nullptr, *k1 = nullptr; // 3 fields x dg x N
+    double *velx8 = nullptr, *vely8 = nullptr, *nvX8 = nullptr, *nvY8 = nullptr;
+    double *sA = nullptr, *sK1 = nullptr;  // 3 x 8 x N
+    double *sshScratch = nullptr, *staging = nullptr, *dgTmp = nullptr, *cgTmp = nullptr;
+    double *partials = nullptr, *dsum = nullptr;
+    int* derr = nullptr;
+    // graph of one update
+    cudaGraphExec_t graph = nullptr;
+    double graphDt = -1.0;
+    int launchesPerUpdate = 0;
+    // fields stored but not advected (DynamicsKernel::advectedFields)
+    std::unordered_map<std::string, std::vector<double>> bucket;
+    std::unordered_map<std::string, int> bucketComps;
+    size_t stepNumber = 0;
+
+    int fail(int code, const std::string& m)
+    {
+        err = m;
+        return code;
+    }
+    int ok()
+    {
+        err.clear();
+        return NSDG_OK;
+    }
+    void releaseDevice()
+    {
+        if (graph)
+            cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graphDt = -1.0;
+        arena.release();
+        if (stream)
+            cudaStreamDestroy(stream);
+        stream = nullptr;
+        ready = false;
+    }
+    int initialise(size_t nx, size_t ny, const double* coords, int spherical, const double* mask);
+    int enqueueUpdate(double dt, int& launches);
+    int ensureGraph(double dt);
+    int checkDeviceError();
+};
+
+int nsdg_kernel::checkDeviceError()
+{
+    int h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (h) {
+        CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), stream));
+        std::string m = "non-finite values detected on the device:";
+        if (h & DEV_ERR_NONFINITE_VELOCITY)
+            m += " velocity";
+        if (h & DEV_ERR_NONFINITE_STRESS)
+            m += " stress";
+        return fail(NSDG_ERR_NUMERIC, m);
+    }
+    return NSDG_OK;
+}
+
+int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int spherical, const double* mask)
+{
+    if (!coords || !mask)
+        return fail(NSDG_ERR_BAD_ARG, "initialise: null coords or mask");
+    if (spherical)
+        return fail(NSDG_ERR_UNSUPPORTED, "initialise: spherical coordinates are not supported");
+    if (nx < 2 || ny < 2)
+        return fail(NSDG_ERR_BAD_ARG, "initialise: the mesh needs nx >= 2 and ny >= 2");
+    {
+        std::string m;
+        const int st = deviceCheck(m);
+        if (st != NSDG_OK)
+            return fail(st, m);
+    }
+    releaseDevice();
+    bucket.clear();
+    bucketComps.clear();
+    stepNumber = 0;
+
+    // --- host mesh (DynamicsKernel.hpp:44-75) ---
+    mesh = HostMesh();
+    mesh.nx = nx;
+    mesh.ny = ny;
+    const size_t nn = (nx + 1) * (ny + 1);
+    mesh.vx.resize(nn);
+    mesh.vy.resize(nn);
+    for (size_t i = 0; i < nn; ++i) {
+        mesh.vx[i] = coords[2 * i];
+        mesh.vy[i] = coords[2 * i + 1];
+        if (!std::isfinite(mesh.vx[i]) || !std::isfinite(mesh.vy[i]))
+            return fail(NSDG_ERR_BAD_ARG, "initialise: non-finite coordinate");
+    }
+    N = nx * ny;
+    mesh.ice.resize(N);
+    for (size_t i = 0; i < N; ++i)
+        mesh.ice[i] = (mask[i] == 1.0) ? 1 : 0;
+    mesh.dirichletFromMaskAndEdges();
+    const std::string fm = buildBoundaryFlags(mesh, flags);
+    if (!fm.empty())
+        return fail(NSDG_ERR_BAD_ARG, "initialise: " + fm);
+    ElementOps ops;
+    const bool bbm = rheology == NSDG_RHEOLOGY_BBM;
+    buildElementOps(mesh, dg, bbm, ops);
+    for (size_t i = 0; i < N; ++i) {
+        const size_t e = i;
+        for (int q = 0; q < 9; ++q)
+            if (!(ops.jw3[q * N + e] > 0.0))
+                return fail(NSDG_ERR_BAD_ARG, "initialise: element " + std::to_string(e) + " is degenerate or inverted");
+    }
+
+    Ncg = (2 * nx + 1) * (2 * ny + 1);
+    Ncg1 = (nx + 1) * (ny + 1);
+    const int Qa = gaussPoints1d(dg);
+    const size_t nXe = nx * (ny + 1), nYe = (nx + 1) * ny;
+    const int ED = edgeDofs(dg);
+
+    // --- size the arena ---
+    size_t bytes = 0;
+    auto add = [&](size_t n, size_t sz = sizeof(double)) { bytes += al(n * sz); };
+    // mesh
+    add(nn, 8); add(nn, 8);
+    add(N, 1); add(N, 1); add(nXe, 1); add(nYe, 1); add(Ncg, 1);
+    add(N + 1, 4); add(std::max<size_t>(flags.perEntry.size(), 1), 4);
+    // ops
+    add(ops.cellX.size()); add(ops.cellY.size()); add(ops.minv.size()); add(ops.jwA.size()); add(ops.jw3.size());
+    add(ops.gx.size()); add(ops.gy.size()); add(ops.w.size()); add(ops.d1.size()); add(ops.d2.size());
+    add(ops.dxssh.size()); add(ops.dyssh.size()); add(Ncg); add(Ncg1);
+    if (bbm) {
+        add(ops.cellX8.size()); add(ops.cellY8.size()); add(ops.minv8.size()); add(ops.wdam.size()); add(ops.hsize.size());
+    }
+    // state and work
+    add(size_t(dg) * N); add(size_t(dg) * N); add(N); add(size_t(dg) * N);
+    add(8 * N); add(8 * N); add(8 * N);
+    for (int i = 0; i < 25; ++i) add(Ncg);
+    add(9 * N); add(18 * N);
+    add(size_t(dg) * N); add(size_t(dg) * N); add(ED * nXe); add(ED * nYe);
+    add(3 * size_t(dg) * N); add(3 * size_t(dg) * N);
+    if (bbm) {
+        add(8 * N); add(8 * N); add(3 * nXe); add(3 * nYe); add(24 * N); add(24 * N);
+    }
+    add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
+    add((N + 255) / 256 + 1); add(1); add(1, 4);
+    bytes += 4096;
+
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CUDA_TRY(uploadConstTables());
+    CUDA_TRY(arena.reserve(bytes));
+
+    auto up = [&](const void* src, size_t n, size_t sz, cudaError_t& e) -> void* {
+        void* p = nullptr;
+        if (sz == 8) p = arena.take<double>(n);
+        else if (sz == 4) p = arena.take<int>(n);
+        else p = arena.take<uint8_t>(n);
+        if (!p) { e = cudaErrorMemoryAllocation; return nullptr; }
+        if (src && n) e = cudaMemcpyAsync(p, src, n * sz, cudaMemcpyHostToDevice, stream);
+        return p;
+    };
+    cudaError_t e = cudaSuccess;
+    dm.nx = static_cast<int>(nx);
+    dm.ny = static_cast<int>(ny);
+    dm.N = N;
+    dm.Ncg = Ncg;
+    dm.Ncg1 = Ncg1;
+    dm.nXe = nXe;
+    dm.nYe = nYe;
+    dm.vx = static_cast<const double*>(up(mesh.vx.data(), nn, 8, e));
+    dm.vy = static_cast<const double*>(up(mesh.vy.data(), nn, 8, e));
+    dm.ice = static_cast<const uint8_t*>(up(mesh.ice.data(), N, 1, e));
+    dm.cellSeg = static_cast<const uint8_t*>(up(flags.cellSeg.data(), N, 1, e));
+    dm.edgeXCount = static_cast<const uint8_t*>(up(flags.edgeXCount.data(), nXe, 1, e));
+    dm.edgeYCount = static_cast<const uint8_t*>(up(flags.edgeYCount.data(), nYe, 1, e));
+    dm.cg2Dir = static_cast<const uint8_t*>(up(flags.cg2Dirichlet.data(), Ncg, 1, e));
+    dm.perPtr = static_cast<const int*>(up(flags.perPtr.data(), N + 1, 4, e));
+    dm.perEntry = static_cast<const int*>(up(flags.perEntry.empty() ? nullptr : flags.perEntry.data(),
+        std::max<size_t>(flags.perEntry.size(), 1), 4, e));
+    auto upd = [&](const std::vector<double>& vsrc) {
+        return static_cast<const double*>(up(vsrc.data(), vsrc.size(), 8, e));
+    };
+    dops.cellX = upd(ops.cellX);
+    dops.cellY = upd(ops.cellY);
+    dops.minv = upd(ops.minv);
+    dops.jwA = upd(ops.jwA);
+    dops.jw3 = upd(ops.jw3);
+    dops.gx = upd(ops.gx);
+    dops.gy = upd(ops.gy);
+    dops.w = upd(ops.w);
+    dops.d1 = upd(ops.d1);
+    dops.d2 = upd(ops.d2);
+    dops.dxssh = upd(ops.dxssh);
+    dops.dyssh = upd(ops.dyssh);
+    std::vector<double> invm(Ncg);
+    for (size_t i = 0; i < Ncg; ++i)
+        invm[i] = 1.0 / ops.lumped2[i];
+    dops.invm2 = upd(invm);
+    dops.lumped1 = upd(ops.lumped1);
+    if (bbm) {
+        dops.cellX8 = upd(ops.cellX8);
+        dops.cellY8 = upd(ops.cellY8);
+        dops.minv8 = upd(ops.minv8);
+        dops.wdam = upd(ops.wdam);
+        dops.hsize = upd(ops.hsize);
+    }
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("initialise: upload failed: ") + cudaGetErrorString(e));
+    auto z = [&](size_t n) {
+        double* p = arena.take<double>(n);
+        if (p && e == cudaSuccess)
+            e = cudaMemsetAsync(p, 0, n * sizeof(double), stream);
+        if (!p)
+            e = cudaErrorMemoryAllocation;
+        return p;
+    };
+    hice = z(size_t(dg) * N);
+    cice = z(size_t(dg) * N);
+    ssh = z(N);
+    damage = z(size_t(dg) * N);
+    s11 = z(8 * N);
+    s12 = z(8 * N);
+    s22 = z(8 * N);
+    u = z(Ncg); v = z(Ncg); uo = z(Ncg); vo = z(Ncg); ua = z(Ncg); va = z(Ncg);
+    avgU = z(Ncg); avgV = z(Ncg); u0 = z(Ncg); v0 = z(Ncg); cgH = z(Ncg); cgA = z(Ncg);
+    uGrad = z(Ncg); vGrad = z(Ncg); c1 = z(Ncg); c1b = z(Ncg); fau = z(Ncg); fav = z(Ncg);
+    rhfc = z(Ncg); gu = z(Ncg); gv = z(Ncg);
+    Pg = z(9 * N);
+    contrib = z(18 * N);
+    velx = z(size_t(dg) * N);
+    vely = z(size_t(dg) * N);
+    nvX = z(ED * nXe);
+    nvY = z(ED * nYe);
+    phiA = z(3 * size_t(dg) * N);
+    k1 = z(3 * size_t(dg) * N);
+    if (bbm) {
+        velx8 = z(8 * N);
+        vely8 = z(8 * N);
+        nvX8 = z(3 * nXe);
+        nvY8 = z(3 * nYe);
+        sA = z(24 * N);
+        sK1 = z(24 * N);
+    }
+    sshScratch = z(3 * Ncg1);
+    staging = z(8 * N);
+    dgTmp = z(8 * N);
+    cgTmp = z(Ncg);
+    partials = z((N + 255) / 256 + 1);
+    dsum = z(1);
+    derr = arena.take<int>(1);
+    if (!derr)
+        e = cudaErrorMemoryAllocation;
+    else if (e == cudaSuccess)
+        e = cudaMemsetAsync(derr, 0, sizeof(int), stream);
+    (void)Qa;
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("initialise: allocation failed: ") + cudaGetErrorString(e));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    ready = true;
+    return ok();
+}
+
+int nsdg_kernel::enqueueUpdate(double dt, int& launches)
+{
+    cudaStream_t s = stream;
+    launches = 0;
+    cudaError_t e;
+#define LCH(expr)                                                                                  \
+    do {                                                                                           \
+        e = (expr);                                                                                \
+        if (e != cudaSuccess)                                                                      \
+            return fail(NSDG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e));       \
+        ++launches;                                                                                \
+    } while (0)
+    const size_t dN = size_t(dg) * N;
+    const bool bbm = rheology == NSDG_RHEOLOGY_BBM;
+    // --- advection of cice, hice (and damage for BBM), with limits
+    //     (DynamicsKernel.hpp:160-172; BrittleCGDynamicsKernel.hpp:89-106) ---
+    {
+        const double* cgv[2] = { bbm ? avgU : u, bbm ? avgV : v };
+        double* dgv[2] = { velx, vely };
+        LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minv, 2, cgv, dgv));
+        LCH(launchNormalVelocity(s, dm, dg, velx, vely, nvX, nvY));
+        StageFields a, b;
+        const int nf = bbm ? 3 : 2;
+        double* fld[3] = { cice, hice, damage };
+        a.nf = b.nf = nf;
+        for (int k = 0; k < nf; ++k) {
+            a.src[k] = fld[k];
+            a.phi[k] = fld[k];
+            a.k1[k] = k1 + k * dN;
+            a.dst[k] = phiA + k * dN;
+            b.src[k] = phiA + k * dN;
+            b.phi[k] = fld[k];
+            b.k1[k] = k1 + k * dN;
+            b.dst[k] = fld[k];
+        }
+        b.lmax[0] = 1; b.vmax[0] = 1.0; b.lmin[0] = 1; b.vmin[0] = 0.0;  // cice
+        b.lmin[1] = 1; b.vmin[1] = 0.0;                                   // hice
+        if (bbm) { b.lmax[2] = 1; b.vmax[2] = 1.0; b.lmin[2] = 1; b.vmin[2] = 1e-12; } // damage
+        LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
+            STAGE_RK2_A, dt, a));
+        LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
+            STAGE_RK2_B, dt, b));
+    }
+    if (bbm) {
+        // stress transport with DGTransport<8> (BrittleCGDynamicsKernel.hpp:98-101)
+        const double* cgv[2] = { avgU, avgV };
+        double* dgv[2] = { velx8, vely8 };
+        LCH(launchCG2DG(s, dm, 8, dops.jw3, dops.minv8, 2, cgv, dgv));
+        LCH(launchNormalVelocity(s, dm, 8, velx8, vely8, nvX8, nvY8));
+        StageFields a, b;
+        double* fld[3] = { s11, s12, s22 };
+        a.nf = b.nf = 3;
+        for (int k = 0; k < 3; ++k) {
+            a.src[k] = fld[k];
+            a.phi[k] = fld[k];
+            a.k1[k] = sK1 + k * 8 * N;
+            a.dst[k] = sA + k * 8 * N;
+            b.src[k] = sA + k * 8 * N;
+            b.phi[k] = fld[k];
+            b.k1[k] = sK1 + k * 8 * N;
+            b.dst[k] = fld[k];
+        }
+        LCH(launchTransportStage(s, dm, 8, dops.cellX8, dops.cellY8, dops.minv8, velx8, vely8, nvX8,
+            nvY8, STAGE_RK2_A, dt, a));
+        LCH(launchTransportStage(s, dm, 8, dops.cellX8, dops.cellY8, dops.minv8, velx8, vely8, nvX8,
+            nvY8, STAGE_RK2_B, dt, b));
+    }
+    // --- prepareIteration (CGDynamicsKernel.cpp:260-276) ---
+    {
+        const double* in[2] = { hice, cice };
+        double* out[2] = { cgH, cgA };
+        LCH(launchDG2CG(s, dm, dg, 2, in, out));
+        e = launchSSHGradient(s, dm, dops, ssh, sshScratch, uGrad, vGrad);
+        if (e != cudaSuccess)
+            return fail(NSDG_ERR_CUDA, std::string("ssh gradient: ") + cudaGetErrorString(e));
+        launches += 3;
+    }
+    const int nS = P.n_steps;
+    if (!bbm) {
+        MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, dt };
+        MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
+        LCH(launchMevpPrepNodes(s, dm, st, mp));
+        LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
+        for (int it = 0; it < nS; ++it) {
+            LCH(launchMevpStress(s, dm, dops, u, v, Pg, s11, s12, s22, contrib, mp, derr));
+            LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
+        }
+    } else {
+        const double rad = 0x1.1df46a2529d39p-6;
+        BbmParams bp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, dt / nS, double(nS),
+            std::cos(rad * P.ocean_turning_angle), std::sin(rad * P.ocean_turning_angle),
+            P.compaction_param, P.nu0, P.young, P.P0, P.undamaged_time_relaxation_sigma,
+            P.exponent_relaxation_sigma, P.exponent_compression_factor, P.tan_phi, P.compr_strength, P.C_lab };
+        BbmNodeState st { u, v, avgU, avgV, cgH, cgA, uo, vo, ua, va, uGrad, vGrad };
+        LCH(launchBbmPrepNodes(s, dm, st));
+        for (int it = 0; it < nS; ++it) {
+            LCH(launchBbmStress(s, dm, dops, dg, u, v, hice, cice, damage, s11, s12, s22, contrib, bp, derr));
+            LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr));
+        }
+    }
+#undef LCH
+    return NSDG_OK;
+}
+
+int nsdg_kernel::ensureGraph(double dt)
+{
+    if (graph && graphDt == dt)
+        return NSDG_OK;
+    if (graph) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int launches = 0;
+    const int st = enqueueUpdate(dt, launches);
+    const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+    if (st != NSDG_OK) {
+        if (g)
+            cudaGraphDestroy(g);
+        return st;
+    }
+    if (ec != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        graph = nullptr;
+        return fail(NSDG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    graphDt = dt;
+    launchesPerUpdate = launches;
+    return NSDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// extern "C"
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void nsdg_default_params(nsdg_params* p)
+{
+    if (!p)
+        return;
+    std::memset(p, 0, sizeof(*p));
+    // DynamicsParameters.hpp:22-40
+    p->rho_ice = 900.0;
+    p->rho_atm = 1.3;
+    p->rho_ocean = 1026.0;
+    p->C_atm = 1.2e-3;
+    p->C_ocean = 5.5e-3;
+    p->F_atm = p->C_atm * p->rho_atm;
+    p->F_ocean = p->C_ocean * p->rho_ocean;
+    p->fc = 1.45842e-4;
+    p->ocean_turning_angle = 0.0;
+    p->gravity = 9.81;
+    // VPParameters.hpp:20-25
+    p->Pstar = 27500.0;
+    p->DeltaMin = 2.e-9;
+    // VPCGDynamicsKernel.hpp:125-126
+    p->alpha = 1500.;
+    p->beta = 1500.;
+    // MEBParameters.hpp:40-65
+    p->compaction_param = -20.;
+    p->nu0 = 1. / 3.;
+    p->young = 5.96e8;
+    p->P0 = 10.e3;
+    p->undamaged_time_relaxation_sigma = 1e7;
+    p->exponent_relaxation_sigma = 5;
+    p->exponent_compression_factor = 1.5;
+    p->tan_phi = 0.7;
+    p->compr_strength = 1e10;
+    p->C_lab = 2.0e6;
+    // DynamicsKernel.hpp:187
+    p->n_steps = 100;
+    p->precision = NSDG_PRECISION_FP64;
+}
+
+const char* nsdg_status_string(int s)
+{
+    switch (s) {
+    case NSDG_OK: return "ok";
+    case NSDG_ERR_BAD_ARG: return "bad argument";
+    case NSDG_ERR_UNKNOWN_FIELD: return "unknown field";
+    case NSDG_ERR_SIZE_MISMATCH: return "size mismatch";
+    case NSDG_ERR_CUDA: return "CUDA error";
+    case NSDG_ERR_NUMERIC: return "non-finite values";
+    case NSDG_ERR_UNSUPPORTED: return "unsupported";
+    case NSDG_ERR_LOGIC: return "logic error";
+    case NSDG_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+const char* nsdg_version(void) { return kVersion; }
+
+int nsdg_kernel_create(int rheology, int dg_comp, const nsdg_params* params, nsdg_kernel** out)
+{
+    if (!out)
+        return NSDG_ERR_BAD_ARG;
+    *out = nullptr;
+    if (rheology != NSDG_RHEOLOGY_MEVP && rheology != NSDG_RHEOLOGY_BBM)
+        return NSDG_ERR_BAD_ARG;
+    if (dg_comp != 1 && dg_comp != 3 && dg_comp != 6)
+        return NSDG_ERR_BAD_ARG;
+    nsdg_params p;
+    if (params)
+        p = *params;
+    else
+        nsdg_default_params(&p);
+    if (p.n_steps < 1 || !(p.alpha > 0) || !(p.beta >= 0) || !(p.rho_ice > 0))
+        return NSDG_ERR_BAD_ARG;
+    if (p.precision != NSDG_PRECISION_FP64)
+        return NSDG_ERR_UNSUPPORTED;
+    try {
+        nsdg_kernel* k = new nsdg_kernel();
+        k->rheology = rheology;
+        k->dg = dg_comp;
+        k->P = p;
+        *out = k;
+    } catch (const std::exception&) {
+        return NSDG_ERR_BAD_ARG;
+    }
+    return NSDG_OK;
+}
+
+int nsdg_kernel_destroy(nsdg_kernel* k)
+{
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    if (k->stream)
+        cudaStreamSynchronize(k->stream);
+    k->releaseDevice();
+    delete k;
+    return NSDG_OK;
+}
+
+const char* nsdg_kernel_last_error(const nsdg_kernel* k) { return k ? k->err.c_str() : "null handle"; }
+
+int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny, const double* coords, int is_spherical,
+    const double* mask)
+{
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    try {
+        return k->initialise(nx, ny, coords, is_spherical, mask);
+    } catch (const std::exception& ex) {
+        return k->fail(NSDG_ERR_BAD_ARG, std::string("initialise: ") + ex.what());
+    }
+}
+
+int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, size_t n_elements, size_t n_comp)
+{
+    if (!k || !name)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "set_data: kernel not initialised");
+    if (!data)
+        return k->fail(NSDG_ERR_BAD_ARG, "set_data: null data");
+    if (n_elements != k->N || n_comp == 0 || n_comp > 8)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, std::string("set_data: size mismatch for ") + name);
+    const std::string s(name);
+    const int dg = k->dg;
+    const size_t N = k->N;
+    cudaStream_t st = k->stream;
+    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
+    double* cgTarget = nullptr;
+    if (s == "u") cgTarget = k->u;
+    else if (s == "v") cgTarget = k->v;
+    else if (s == "uwind") cgTarget = k->ua;
+    else if (s == "vwind") cgTarget = k->va;
+    else if (s == "uocean") cgTarget = k->uo;
+    else if (s == "vocean") cgTarget = k->vo;
+    double* dgTarget = nullptr;
+    int targetComps = dg;
+    if (s == "hice") dgTarget = k->hice;
+    else if (s == "cice") dgTarget = k->cice;
+    else if (s == "ssh") { dgTarget = k->ssh; targetComps = 1; }
+    else if (s == "damage" && bbm) dgTarget = k->damage;
+    if (!cgTarget && !dgTarget) {
+        // DynamicsKernel.hpp:104-109: any other name is stored (ma2dg semantics)
+        std::vector<double>& b = k->bucket[s];
+        b.assign(N * dg, 0.0);
+        if (n_comp == size_t(dg))
+            std::memcpy(b.data(), data, N * dg * sizeof(double));
+        else
+            for (size_t i = 0; i < N; ++i)
+                b[i * dg] = data[i * n_comp];
+        k->bucketComps[s] = static_cast<int>(n_comp);
+        return k->ok();
+    }
+    auto cu = [&](cudaError_t e, const char* what) {
+        return e == cudaSuccess ? NSDG_OK : k->fail(NSDG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    int r = cu(cudaMemcpyAsync(k->staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, st), "set_data copy");
+    if (r) return r;
+    if (cgTarget) {
+        // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
+        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, k->staging, k->dgTmp), "set_data convert");
+        if (r) return r;
+        const double* in[1] = { k->dgTmp };
+        double* out[1] = { cgTarget };
+        r = cu(launchDG2CG(st, k->dm, dg, 1, in, out), "set_data DG2CG");
+        if (r) return r;
+    } else {
+        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, k->staging, dgTarget), "set_data convert");
+        if (r) return r;
+    }
+    r = cu(cudaStreamSynchronize(st), "set_data sync");
+    if (r) return r;
+    return k->ok();
+}
+
+int nsdg_kernel_update(nsdg_kernel* k, double t_start, double dt)
+{
+    (void)t_start;
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "update: kernel not initialised");
+    if (!(dt > 0) || !std::isfinite(dt))
+        return k->fail(NSDG_ERR_BAD_ARG, "update: dt must be positive");
+    int r = k->ensureGraph(dt);
+    if (r)
+        return r;
+    const cudaError_t e = cudaGraphLaunch(k->graph, k->stream);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("update: ") + cudaGetErrorString(e));
+    ++k->stepNumber;
+    return k->ok();
+}
+
+int nsdg_kernel_synchronize(nsdg_kernel* k)
+{
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "synchronize: kernel not initialised");
+    const int r = k->checkDeviceError();
+    return r ? r : k->ok();
+}
+
+int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_elements)
+{
+    if (!k || !name || !out)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "get_dg0: kernel not initialised");
+    if (n_elements != k->N)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "get_dg0: size mismatch");
+    const std::string s(name);
+    const size_t N = k->N;
+    const int dg = k->dg;
+    cudaStream_t st = k->stream;
+    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
+    const double* src = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (s == "u" || s == "v" || s == "uiostress" || s == "viostress") {
+        const double* cg = nullptr;
+        if (s == "u") cg = k->u;
+        else if (s == "v") cg = k->v;
+        else {
+            const double rad = 0x1.1df46a2529d39p-6;
+            const double ang = bbm ? k->P.ocean_turning_angle : 0.0;
+            double* tx = k->cgTmp;
+            double* ty = k->u0; // reused as scratch outside update
+            e = launchIceOceanStress(st, k->Ncg, bbm ? 1 : 0, bbm ? k->avgU : k->u, bbm ? k->avgV : k->v,
+                k->uo, k->vo, k->P.F_ocean, std::cos(rad * ang), std::sin(rad * ang), tx, ty);
+            cg = (s == "uiostress") ? tx : ty;
+        }
+        const double* in[1] = { cg };
+        double* outd[1] = { k->dgTmp };
+        if (e == cudaSuccess)
+            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, k->dops.minv, 1, in, outd);
+        src = k->dgTmp;
+    } else if (s == "hice") src = k->hice;
+    else if (s == "cice") src = k->cice;
+    else if (s == "damage" && bbm) src = k->damage;
+    else {
+        auto it = k->bucket.find(s);
+        if (it == k->bucket.end())
+            return k->fail(NSDG_ERR_UNKNOWN_FIELD, "get_dg0: unknown field " + s);
+        for (size_t i = 0; i < N; ++i)
+            out[i] = it->second[i * dg];
+        return k->ok();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, src, N * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("get_dg0: ") + cudaGetErrorString(e));
+    const int r = k->checkDeviceError();
+    return r ? r : k->ok();
+}
+
+int nsdg_kernel_get_dg(nsdg_kernel* k, const char* name, double* out, size_t n_elements, size_t n_comp)
+{
+    if (!k || !name || !out)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "get_dg: kernel not initialised");
+    if (n_elements != k->N)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "get_dg: size mismatch");
+    const std::string s(name);
+    const size_t N = k->N;
+    const int dg = k->dg;
+    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
+    const double* src = nullptr;
+    if (s == "hice") src = k->hice;
+    else if (s == "cice") src = k->cice;
+    else if (s == "damage" && bbm) src = k->damage;
+    else {
+        auto it = k->bucket.find(s);
+        if (it == k->bucket.end())
+            return k->fail(NSDG_ERR_UNKNOWN_FIELD, "get_dg: unknown field " + s);
+        const size_t want = (k->bucketComps[s] == dg) ? dg : 1;
+        if (n_comp != want)
+            return k->fail(NSDG_ERR_SIZE_MISMATCH, "get_dg: component count mismatch");
+        for (size_t i = 0; i < N; ++i)
+            for (size_t j = 0; j < want; ++j)
+                out[i * want + j] = it->second[i * dg + j];
+        return k->ok();
+    }
+    if (n_comp != size_t(dg))
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "get_dg: component count mismatch");
+    cudaError_t e = launchSoaToAos(k->stream, N, dg, dg, src, k->staging);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, k->staging, N * dg * sizeof(double), cudaMemcpyDeviceToHost, k->stream);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("get_dg: ") + cudaGetErrorString(e));
+    const int r = k->checkDeviceError();
+    return r ? r : k->ok();
+}
+
+// Snapshot layout: magic, version, rheology, dg, N, Ncg, stepNumber, then the
+// state arrays in a fixed order.
+namespace {
+struct SnapHeader {
+    char magic[8];
+    int version, rheology, dg, pad;
+    unsigned long long N, Ncg, step;
+};
+std::vector<std::pair<double*, size_t>> snapshotArrays(nsdg_kernel* k)
+{
+    const size_t dN = size_t(k->dg) * k->N;
+    std::vector<std::pair<double*, size_t>> a = { { k->hice, dN }, { k->cice, dN }, { k->ssh, k->N },
+        { k->s11, 8 * k->N }, { k->s12, 8 * k->N }, { k->s22, 8 * k->N }, { k->u, k->Ncg },
+        { k->v, k->Ncg }, { k->uo, k->Ncg }, { k->vo, k->Ncg }, { k->ua, k->Ncg }, { k->va, k->Ncg } };
+    if (k->rheology == NSDG_RHEOLOGY_BBM) {
+        a.push_back({ k->damage, dN });
+        a.push_back({ k->avgU, k->Ncg });
+        a.push_back({ k->avgV, k->Ncg });
+    }
+    return a;
+}
+} // namespace
+
+int nsdg_kernel_snapshot_size(nsdg_kernel* k, size_t* bytes)
+{
+    if (!k || !bytes)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "snapshot: kernel not initialised");
+    size_t b = sizeof(SnapHeader);
+    for (auto& p : snapshotArrays(k))
+        b += p.second * sizeof(double);
+    *bytes = b;
+    return k->ok();
+}
+
+int nsdg_kernel_snapshot_save(nsdg_kernel* k, void* buffer, size_t bytes)
+{
+    size_t need = 0;
+    int r = nsdg_kernel_snapshot_size(k, &need);
+    if (r)
+        return r;
+    if (!buffer || bytes < need)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "snapshot_save: buffer too small");
+    SnapHeader h {};
+    std::memcpy(h.magic, "NSDGSNP", 8);
+    h.version = 1;
+    h.rheology = k->rheology;
+    h.dg = k->dg;
+    h.N = k->N;
+    h.Ncg = k->Ncg;
+    h.step = k->stepNumber;
+    std::memcpy(buffer, &h, sizeof(h));
+    char* p = static_cast<char*>(buffer) + sizeof(h);
+    for (auto& a : snapshotArrays(k)) {
+        const cudaError_t e = cudaMemcpyAsync(p, a.first, a.second * sizeof(double), cudaMemcpyDeviceToHost, k->stream);
+        if (e != cudaSuccess)
+            return k->fail(NSDG_ERR_CUDA, std::string("snapshot_save: ") + cudaGetErrorString(e));
+        p += a.second * sizeof(double);
+    }
+    r = k->checkDeviceError();
+    return r ? r : k->ok();
+}
+
+int nsdg_kernel_snapshot_load(nsdg_kernel* k, const void* buffer, size_t bytes)
+{
+    size_t need = 0;
+    int r = nsdg_kernel_snapshot_size(k, &need);
+    if (r)
+        return r;
+    if (!buffer || bytes < need)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "snapshot_load: buffer too small");
+    SnapHeader h;
+    std::memcpy(&h, buffer, sizeof(h));
+    if (std::memcmp(h.magic, "NSDGSNP", 8) != 0 || h.version != 1 || h.rheology != k->rheology
+        || h.dg != k->dg || h.N != k->N || h.Ncg != k->Ncg)
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "snapshot_load: snapshot does not match this kernel");
+    const char* p = static_cast<const char*>(buffer) + sizeof(h);
+    for (auto& a : snapshotArrays(k)) {
+        const cudaError_t e = cudaMemcpyAsync(a.first, p, a.second * sizeof(double), cudaMemcpyHostToDevice, k->stream);
+        if (e != cudaSuccess)
+            return k->fail(NSDG_ERR_CUDA, std::string("snapshot_load: ") + cudaGetErrorString(e));
+        p += a.second * sizeof(double);
+    }
+    const cudaError_t e = cudaStreamSynchronize(k->stream);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("snapshot_load: ") + cudaGetErrorString(e));
+    k->stepNumber = h.step;
+    return k->ok();
+}
+
+int nsdg_kernel_mean_value(nsdg_kernel* k, const char* name, double* out)
+{
+    if (!k || !name || !out)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "mean_value: kernel not initialised");
+    const std::string s(name);
+    const double* src = nullptr;
+    if (s == "hice") src = k->hice;
+    else if (s == "cice") src = k->cice;
+    else if (s == "damage" && k->rheology == NSDG_RHEOLOGY_BBM) src = k->damage;
+    else return k->fail(NSDG_ERR_UNKNOWN_FIELD, "mean_value: unknown field " + s);
+    cudaError_t e = launchMeanValue(k->stream, k->N, k->dg, src, k->dops.jw3, k->partials, k->dsum);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, k->dsum, sizeof(double), cudaMemcpyDeviceToHost, k->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(k->stream);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("mean_value: ") + cudaGetErrorString(e));
+    return k->ok();
+}
+
+int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms)
+{
+    if (!k || !ms || steps < 1)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "time_updates: kernel not initialised");
+    int r = k->ensureGraph(dt);
+    if (r)
+        return r;
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, "time_updates: event create failed");
+    cudaError_t e = cudaStreamSynchronize(k->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(a, k->stream);
+    for (int i = 0; i < steps && e == cudaSuccess; ++i)
+        e = cudaGraphLaunch(k->graph, k->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b, k->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("time_updates: ") + cudaGetErrorString(e));
+    k->stepNumber += steps;
+    r = k->checkDeviceError();
+    return r ? r : k->ok();
+}
+
+int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms, const char** name)
+{
+    if (!k || !mean_ms || reps < 1)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel not initialised");
+    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
+    const double dt = k->graphDt > 0 ? k->graphDt : 120.0;
+    MevpParams mp { k->P.rho_ice, k->P.F_atm, k->P.F_ocean, k->P.fc, k->P.gravity, k->P.Pstar, k->P.DeltaMin,
+        k->P.alpha, k->P.beta, dt };
+    MevpNodeState st { k->u, k->v, k->u0, k->v0, k->cgH, k->cgA, k->uo, k->vo, k->ua, k->va, k->uGrad,
+        k->vGrad, k->c1, k->c1b, k->fau, k->fav, k->rhfc, k->gu, k->gv };
+    const double rad = 0x1.1df46a2529d39p-6;
+    BbmParams bp { k->P.rho_ice, k->P.F_atm, k->P.F_ocean, k->P.fc, k->P.gravity, dt / k->P.n_steps,
+        double(k->P.n_steps), std::cos(rad * k->P.ocean_turning_angle), std::sin(rad * k->P.ocean_turning_angle),
+        k->P.compaction_param, k->P.nu0, k->P.young, k->P.P0, k->P.undamaged_time_relaxation_sigma,
+        k->P.exponent_relaxation_sigma, k->P.exponent_compression_factor, k->P.tan_phi, k->P.compr_strength,
+        k->P.C_lab };
+    BbmNodeState bs { k->u, k->v, k->avgU, k->avgV, k->cgH, k->cgA, k->uo, k->vo, k->ua, k->va, k->uGrad, k->vGrad };
+    const size_t dN = size_t(k->dg) * k->N;
+    StageFields a;
+    a.nf = bbm ? 3 : 2;
+    double* fld[3] = { k->cice, k->hice, k->damage };
+    for (int i = 0; i < a.nf; ++i) {
+        a.src[i] = fld[i];
+        a.phi[i] = fld[i];
+        a.k1[i] = k->k1 + i * dN;
+        a.dst[i] = k->phiA + i * dN;
+    }
+    auto launch = [&]() -> cudaError_t {
+        switch (kernel_id) {
+        case 0:
+            return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
+                             k->s11, k->s12, k->s22, k->contrib, bp, k->derr)
+                       : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->s11, k->s12, k->s22,
+                             k->contrib, mp, k->derr);
+        case 1:
+            return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
+                       : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
+        default:
+            return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
+                k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a);
+        }
+    };
+    if (name)
+        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : "kMevpStress")
+            : kernel_id == 1 ? (bbm ? "kBbmMomentum" : "kMevpMomentum")
+                             : "kTransportStage";
+    if (kernel_id < 0 || kernel_id > 2)
+        return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel_id must be 0, 1 or 2");
+    cudaEvent_t ea, eb;
+    if (cudaEventCreate(&ea) != cudaSuccess || cudaEventCreate(&eb) != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, "time_kernel: event create failed");
+    cudaError_t e = launch(); // warm-up
+    if (e == cudaSuccess) e = cudaStreamSynchronize(k->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ea, k->stream);
+    for (int i = 0; i < reps && e == cudaSuccess; ++i)
+        e = launch();
+    if (e == cudaSuccess) e = cudaEventRecord(eb, k->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(eb);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ea, eb);
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("time_kernel: ") + cudaGetErrorString(e));
+    *mean_ms = ms / reps;
+    return k->ok();
+}
+
+int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches)
+{
+    if (!k || !launches)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "launches_per_update: kernel not initialised");
+    if (k->launchesPerUpdate == 0) {
+        const int r = k->ensureGraph(k->graphDt > 0 ? k->graphDt : 120.0);
+        if (r)
+            return r;
+    }
+    *launches = k->launchesPerUpdate;
+    return k->ok();
+}
+
+} // extern "C"

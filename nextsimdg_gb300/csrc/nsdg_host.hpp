@@ -1,0 +1,120 @@
+// nsdg_host.hpp — host-side FP64 precompute for the GB300 dynamics kernel.
+//
+// The reference builds its geometry once per initialise on the CPU
+// (ParametricMesh, ParametricTransportMap, ParametricMomentumMap:
+// dynamics/src/ParametricMap.cpp:13-356, dynamics/src/include/ParametricTools.hpp:73-181).
+// This file does the same work, in FP64, but emits the per-element operators
+// directly in the device layout: structure-of-arrays, one contiguous
+// N-element array per matrix entry ("entry-major"), so that thread e of a
+// warp reads entry k of element e at base + k*N + e (coalesced).
+#pragma once
+
+#include <array>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace nsdg {
+
+// Quadrature (Gauss-Legendre on [0,1]) and the DG / CG2 basis functions the
+// reference generates in dynamics/codegeneration/{gaussquadrature,basisfunctions}.py.
+struct Basis {
+    double gp[5][4] = {};
+    double gw[5][4] = {};
+    Basis();
+    static double dg(int j, double x, double y);
+    static double dgdx(int j, double x, double y);
+    static double dgdy(int j, double x, double y);
+    static double edge(int j, double t);
+    static double cg1d(int deg, int j, double x);
+    static double cg1ddx(int deg, int j, double x);
+    // tables with Gauss point q = gy*Q + gx
+    double psi(int j, int Q, int q) const { return dg(j, gp[Q][q % Q], gp[Q][q / Q]); }
+    double psix(int j, int Q, int q) const { return dgdx(j, gp[Q][q % Q], gp[Q][q / Q]); }
+    double psiy(int j, int Q, int q) const { return dgdy(j, gp[Q][q % Q], gp[Q][q / Q]); }
+    double weight(int Q, int q) const { return gw[Q][q % Q] * gw[Q][q / Q]; }
+    double phi(int deg, int j, int Q, int q) const;
+    double phix(int deg, int j, int Q, int q) const;
+    double phiy(int deg, int j, int Q, int q) const;
+    double psiEdgeW(int j, int G, int E, int g) const; // PSIe_w
+    double psiLagrange(int j, int G, int q) const;     // PSILagrange
+};
+const Basis& basis();
+
+inline int gaussPoints1d(int dg) { return (dg == 8 || dg == 6) ? 3 : (dg == 3 ? 2 : 1); }
+inline int edgeDofs(int dg) { return dg == 1 ? 1 : (dg == 3 ? 2 : 3); }
+
+// Constant tables uploaded to __constant__ memory (layout shared with the
+// device code in nsdg_common.cuh).
+struct ConstTables {
+    double psi[4][8][16];     // [Q][j][q]    DG basis at the Q x Q Gauss points
+    double psix[4][8][16];    // unused on device, kept for completeness of the table set
+    double psiLag3[8][9];     // PSILagrange<DG,3>[j][q]
+    double psie[4][3][3];     // [G][j][g]    edge basis at G Gauss points
+    double psiew[4][4][3][8]; // [G][E][g][j] weighted edge traces (PSIe_w)
+    double phi2[4][9][16];    // [Q][j][q]    CG2 basis at Q x Q Gauss points
+    double gw[5][16];         // [Q][q]       tensor Gauss weights
+};
+void fillConstTables(ConstTables& t);
+
+// The structured quad mesh with arbitrary vertex positions (ParametricMesh).
+struct HostMesh {
+    size_t nx = 0, ny = 0;
+    std::vector<double> vx, vy;               // (nx+1)*(ny+1) vertices
+    std::vector<uint8_t> ice;                 // nx*ny, 1 = ice
+    std::array<std::vector<size_t>, 4> dirichlet;  // bottom, right, top, left
+    std::vector<std::array<size_t, 4>> periodic;   // {type, c1, c2, edge}
+    size_t nelements() const { return nx * ny; }
+    // ParametricMesh::dirichletFromMask / dirichletFromEdge (ParametricMesh.cpp:228-272)
+    void dirichletFromMaskAndEdges();
+    void elementCoords(size_t e, double c[4][2]) const;
+    double area(size_t e) const; // ParametricMesh.hpp:276-295
+};
+
+// Element operators in SoA layout (entry-major: [entry][N]).
+struct ElementOps {
+    int dg = 0;
+    size_t N = 0;
+    // DG transport of the advected fields (DG comps) and of the stress (8 comps)
+    std::vector<double> cellX, cellY, minv;      // dg*Qa^2, dg*Qa^2, dg*dg
+    std::vector<double> jwA;                     // Qa^2   J*w at the advection Gauss points
+    std::vector<double> cellX8, cellY8, minv8;   // 8*9, 8*9, 64 (BBM stress transport)
+    std::vector<double> jw3;                     // 9      J*w at the 3x3 Gauss points
+    // momentum (CG2 / DG-stress 8)
+    std::vector<double> gx, gy;                  // 81: strain at Gauss points from CG2 nodes
+    std::vector<double> w;                       // 72: iMJwPSI[k][q]
+    std::vector<double> d1, d2;                  // 72: divS1[j][k], divS2[j][k]
+    std::vector<double> wdam;                    // dg*9: iMJwPSI_dam (BBM)
+    std::vector<double> dxssh, dyssh;            // 16: dX_SSH[i][j], dY_SSH[i][j]
+    std::vector<double> hsize;                   // 1: sqrt(area)  (BBM)
+    // node arrays
+    std::vector<double> lumped2;                 // (2nx+1)(2ny+1)
+    std::vector<double> lumped1;                 // (nx+1)(ny+1)
+};
+
+// Builds every operator the device needs.  `stressTransport` adds the DG8
+// transport operators and damage projection used by the BBM rheology.
+// Work is split across `threads` host threads (0 = hardware concurrency).
+void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps& ops,
+    unsigned threads = 0);
+
+// Builds only the transport operators (cellX/Y, minv, jwA, jw3) for a DG
+// degree (used by the stand-alone transport handle).
+void buildTransportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads = 0);
+
+// Node / edge / element flags derived from the Dirichlet and periodic lists.
+struct BoundaryFlags {
+    std::vector<uint8_t> cellSeg;      // nx*ny: bit s set if the cell is in dirichlet[s]
+    std::vector<uint8_t> edgeXCount;   // nx*(ny+1): times the X-edge is doubled
+    std::vector<uint8_t> edgeYCount;   // (nx+1)*ny: times the Y-edge is doubled
+    std::vector<uint8_t> cg2Dirichlet; // (2nx+1)(2ny+1): node zeroed by dirichletZero
+    // periodic entries, CSR by cell: for cell c, entries [ptr[c], ptr[c+1]) of
+    // {type, c1, c2, edge} in the reference's processing order
+    std::vector<int> perPtr;
+    std::vector<int> perEntry;         // 4 ints per entry
+};
+// Returns "" on success, else a message (e.g. duplicate Dirichlet entry).
+std::string buildBoundaryFlags(const HostMesh& m, BoundaryFlags& f);
+
+} // namespace nsdg

@@ -1,0 +1,1456 @@
+// nsdg_kernels.cu — sm_103a kernels of the sea-ice dynamics hot path (FP64).
+//
+// One thread per element (element kernels) or per CG2 node (node kernels);
+// every accumulation into a node or an element is a gather in a fixed order,
+// so results are bitwise reproducible from run to run (no atomics on data).
+#include <cmath>
+
+#include "nsdg_host.hpp"
+
+namespace nsdg {
+__constant__ ConstTables cT;
+}
+
+#include "nsdg_common.cuh"
+#include "nsdg_kernels.hpp"
+
+namespace nsdg {
+
+cudaError_t uploadConstTables()
+{
+    static ConstTables host;
+    static bool filled = false;
+    if (!filled) {
+        fillConstTables(host);
+        filled = true;
+    }
+    return cudaMemcpyToSymbol(cT, &host, sizeof(ConstTables));
+}
+
+namespace {
+
+constexpr int kBlock = 128;
+inline unsigned blocksFor(size_t n, int b = kBlock) { return static_cast<unsigned>((n + b - 1) / b); }
+
+// ===========================================================================
+// CG2 -> DG projection   (Interpolations.cpp:74-122, Cartesian)
+//   val(q) = sum_j PHI_j(q) cg_j ; t(q) = (J w)(q) val(q) ;
+//   r_i = sum_q PSI_i(q) t(q) ;  dg = M^{-1} r
+// ===========================================================================
+template <int DG, int NF>
+__global__ void __launch_bounds__(kBlock) kCG2DG(int nx, size_t N, const double* __restrict__ jw,
+    const double* __restrict__ minv, const double* __restrict__ cg0, const double* __restrict__ cg1,
+    double* __restrict__ out0, double* __restrict__ out1)
+{
+    constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q;
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    const size_t s2 = 2 * size_t(nx) + 1;
+    const size_t ix = e % nx, iy = e / nx;
+    const size_t base = 2 * s2 * iy + 2 * ix;
+    const double* cg[2] = { cg0, cg1 };
+    double* out[2] = { out0, out1 };
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        double loc[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+            loc[j] = cg[f][base + (j % 3) + (j / 3) * s2];
+        double t[QQ];
+#pragma unroll
+        for (int q = 0; q < QQ; ++q) {
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < 9; ++j)
+                v += cT.phi2[Q][j][q] * loc[j];
+            t[q] = jw[q * N + e] * v;
+        }
+        double r[DG];
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            double a = 0.0;
+#pragma unroll
+            for (int q = 0; q < QQ; ++q)
+                a += cT.psi[Q][i][q] * t[q];
+            r[i] = a;
+        }
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            double a = 0.0;
+#pragma unroll
+            for (int k = 0; k < DG; ++k)
+                a += minv[(i * DG + k) * N + e] * r[k];
+            out[f][i * N + e] = a;
+        }
+    }
+}
+
+// ===========================================================================
+// Edge normal velocities  (DGTransport.cpp:158-252)
+// X-edge (ix,iy), iy in [0,ny]: first the cell below contributes through its
+// top trace, then the cell above through its bottom trace; Y-edge (ix,iy):
+// left cell (right trace) then right cell (left trace).  Land cells are
+// skipped; Dirichlet edges are doubled.
+// ===========================================================================
+template <int DG>
+__global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const double* __restrict__ velx,
+    const double* __restrict__ vely, double* __restrict__ nvX, double* __restrict__ nvY)
+{
+    constexpr int ED = DGTraits<DG>::ED;
+    const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    const size_t N = m.N;
+    const int nx = m.nx, ny = m.ny;
+    const size_t sv = size_t(nx) + 1;
+    if (t < m.nXe) {
+        const size_t ix = t % nx, iy = t / nx;
+        const size_t n0 = iy * sv + ix;
+        const double t0 = m.vx[n0 + 1] - m.vx[n0], t1 = m.vy[n0 + 1] - m.vy[n0];
+        double acc[ED];
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            acc[k] = 0.0;
+        double cx[DG], cy[DG], tx[ED], ty[ED];
+        if (iy >= 1) {
+            const size_t c = (iy - 1) * nx + ix;
+            if (m.ice[c]) {
+#pragma unroll
+                for (int j = 0; j < DG; ++j) {
+                    cx[j] = velx[j * N + c];
+                    cy[j] = vely[j * N + c];
+                }
+                traceTop<DG>(cx, tx);
+                traceTop<DG>(cy, ty);
+#pragma unroll
+                for (int k = 0; k < ED; ++k)
+                    acc[k] += 0.5 * (-t1 * tx[k] + t0 * ty[k]);
+            }
+        }
+        if (iy < size_t(ny)) {
+            const size_t c = iy * nx + ix;
+            if (m.ice[c]) {
+#pragma unroll
+                for (int j = 0; j < DG; ++j) {
+                    cx[j] = velx[j * N + c];
+                    cy[j] = vely[j * N + c];
+                }
+                traceBottom<DG>(cx, tx);
+                traceBottom<DG>(cy, ty);
+#pragma unroll
+                for (int k = 0; k < ED; ++k)
+                    acc[k] += 0.5 * (-t1 * tx[k] + t0 * ty[k]);
+            }
+        }
+        for (int r = 0; r < m.edgeXCount[t]; ++r)
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                acc[k] *= 2.0;
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            nvX[k * m.nXe + t] = acc[k];
+        return;
+    }
+    const size_t u = t - m.nXe;
+    if (u >= m.nYe)
+        return;
+    const size_t ix = u % sv, iy = u / sv;
+    const size_t n0 = iy * sv + ix;
+    const double t0 = m.vx[n0 + sv] - m.vx[n0], t1 = m.vy[n0 + sv] - m.vy[n0];
+    double acc[ED];
+#pragma unroll
+    for (int k = 0; k < ED; ++k)
+        acc[k] = 0.0;
+    double cx[DG], cy[DG], tx[ED], ty[ED];
+    if (ix >= 1) {
+        const size_t c = iy * nx + ix - 1;
+        if (m.ice[c]) {
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                cx[j] = velx[j * N + c];
+                cy[j] = vely[j * N + c];
+            }
+            traceRight<DG>(cx, tx);
+            traceRight<DG>(cy, ty);
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                acc[k] += 0.5 * (t1 * tx[k] - t0 * ty[k]);
+        }
+    }
+    if (ix < size_t(nx)) {
+        const size_t c = iy * nx + ix;
+        if (m.ice[c]) {
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                cx[j] = velx[j * N + c];
+                cy[j] = vely[j * N + c];
+            }
+            traceLeft<DG>(cx, tx);
+            traceLeft<DG>(cy, ty);
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                acc[k] += 0.5 * (t1 * tx[k] - t0 * ty[k]);
+        }
+    }
+    for (int r = 0; r < m.edgeYCount[u]; ++r)
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            acc[k] *= 2.0;
+#pragma unroll
+    for (int k = 0; k < ED; ++k)
+        nvY[k * m.nYe + u] = acc[k];
+}
+
+// ===========================================================================
+// DG transport operator + Runge-Kutta stage  (DGTransport.cpp:278-566)
+// ===========================================================================
+template <int DG> struct Cell {
+    double c[DG];
+};
+
+// upwind flux at the ED edge Gauss points between trace 1 (cell 1: bottom /
+// left) and trace 2 (cell 2: top / right)
+template <int DG>
+__device__ __forceinline__ void upwind(const double* nv, const double* t1, const double* t2, double* tmp)
+{
+    constexpr int ED = DGTraits<DG>::ED;
+    double vg[ED], g1[ED], g2[ED];
+    edgeGauss<ED>(nv, vg);
+    edgeGauss<ED>(t1, g1);
+    edgeGauss<ED>(t2, g2);
+#pragma unroll
+    for (int g = 0; g < ED; ++g)
+        tmp[g] = fmax(vg[g], 0.0) * g1[g] + fmin(vg[g], 0.0) * g2[g];
+}
+// acc += sdt * sum_g tmp(g) PSIe_w<DG,ED,E>(g, :)
+template <int DG>
+__device__ __forceinline__ void addEdge(double* acc, double sdt, const double* tmp, int E)
+{
+    constexpr int ED = DGTraits<DG>::ED;
+#pragma unroll
+    for (int j = 0; j < DG; ++j) {
+        double s = 0.0;
+#pragma unroll
+        for (int g = 0; g < ED; ++g)
+            s += tmp[g] * cT.psiew[ED][E][g][j];
+        acc[j] += sdt * s;
+    }
+}
+
+template <int DG>
+__device__ __forceinline__ void loadCell(const double* __restrict__ p, size_t N, size_t c, double* out)
+{
+#pragma unroll
+    for (int j = 0; j < DG; ++j)
+        out[j] = p[j * N + c];
+}
+
+template <int DG> __device__ __forceinline__ void limitMax(double* r, double mx)
+{
+    if constexpr (DG == 1) {
+        r[0] = fmin(r[0], mx);
+    } else if constexpr (DG == 3) {
+        r[0] = fmin(mx, r[0]);
+        const double l0 = 2.0 * fmax(fabs(r[1] + r[2]), fabs(r[1] - r[2]));
+        if (l0 != 0.0 && r[0] + l0 - mx > 0) {
+            r[1] *= (mx - r[0]) / l0;
+            r[2] *= (mx - r[0]) / l0;
+        }
+    } else if constexpr (DG == 6) {
+        r[0] = fmin(mx, r[0]);
+        double mv = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < 6; ++j)
+                s += r[j] * cT.psi[3][j][q];
+            mv = fmax(mv, s);
+        }
+        if (mv > mx) {
+            const double f = (mx - r[0]) / (mv - r[0]);
+#pragma unroll
+            for (int j = 1; j < 6; ++j)
+                r[j] *= f;
+        }
+    }
+}
+template <int DG> __device__ __forceinline__ void limitMin(double* r, double mn)
+{
+    if constexpr (DG == 1) {
+        r[0] = fmax(r[0], mn);
+    } else if constexpr (DG == 3) {
+        r[0] = fmax(mn, r[0]);
+        const double l0 = 2.0 * fmax(fabs(r[1] + r[2]), fabs(r[1] - r[2]));
+        if (l0 != 0.0 && r[0] - l0 - mn < 0) {
+            r[1] *= (r[0] - mn) / l0;
+            r[2] *= (r[0] - mn) / l0;
+        }
+    } else if constexpr (DG == 6) {
+        r[0] = fmax(mn, r[0]);
+        double mv = INFINITY;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < 6; ++j)
+                s += r[j] * cT.psi[3][j][q];
+            mv = fmin(mv, s);
+        }
+        if (mv < mn) {
+            const double f = (r[0] - mn) / (mv - r[0]);
+#pragma unroll
+            for (int j = 1; j < 6; ++j)
+                r[j] *= f;
+        }
+    }
+}
+
+struct TransportArgs {
+    DevMesh m;
+    const double* cellX;
+    const double* cellY;
+    const double* minv;
+    const double* velx;
+    const double* vely;
+    const double* nvX;
+    const double* nvY;
+    double dt;
+    int mode;
+};
+
+template <int DG, int NF>
+__global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, StageFields f)
+{
+    constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q, ED = DGTraits<DG>::ED;
+    const size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    const DevMesh& m = a.m;
+    const size_t N = m.N;
+    if (c >= N)
+        return;
+    const int nx = m.nx, ny = m.ny;
+    const int ix = static_cast<int>(c % nx), iy = static_cast<int>(c / nx);
+    const double dt = a.dt;
+    const bool ice = m.ice[c] != 0;
+
+    double own[NF][DG], acc[NF][DG];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        loadCell<DG>(f.src[k], N, c, own[k]);
+#pragma unroll
+        for (int j = 0; j < DG; ++j)
+            acc[k][j] = 0.0;
+    }
+
+    // cell term: dt * sum_q (cellX_iq vx(q) + cellY_iq vy(q)) phi(q)
+    if constexpr (DG > 1) {
+        if (ice) {
+            double vxg[QQ], vyg[QQ], pg[NF][QQ];
+            double vx[DG], vy[DG];
+            loadCell<DG>(a.velx, N, c, vx);
+            loadCell<DG>(a.vely, N, c, vy);
+#pragma unroll
+            for (int q = 0; q < QQ; ++q) {
+                double sx = 0.0, sy = 0.0;
+#pragma unroll
+                for (int j = 0; j < DG; ++j) {
+                    sx += vx[j] * cT.psi[Q][j][q];
+                    sy += vy[j] * cT.psi[Q][j][q];
+                }
+                vxg[q] = sx;
+                vyg[q] = sy;
+#pragma unroll
+                for (int k = 0; k < NF; ++k) {
+                    double sp = 0.0;
+#pragma unroll
+                    for (int j = 0; j < DG; ++j)
+                        sp += own[k][j] * cT.psi[Q][j][q];
+                    pg[k][q] = sp;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < DG; ++i) {
+                double t[NF];
+#pragma unroll
+                for (int k = 0; k < NF; ++k)
+                    t[k] = 0.0;
+#pragma unroll
+                for (int q = 0; q < QQ; ++q) {
+                    const double mq = a.cellX[(i * QQ + q) * N + c] * vxg[q] + a.cellY[(i * QQ + q) * N + c] * vyg[q];
+#pragma unroll
+                    for (int k = 0; k < NF; ++k)
+                        t[k] += mq * pg[k][q];
+                }
+#pragma unroll
+                for (int k = 0; k < NF; ++k)
+                    acc[k][i] += dt * t[k];
+            }
+        }
+    }
+
+    double nv[ED], t1[ED], t2[ED], tmp[ED], nb[DG];
+    // left Y-edge (this cell is "cell 2"), interior edges only
+    if (ix >= 1) {
+        const size_t c1 = c - 1;
+        if (ice && m.ice[c1]) {
+            const size_t e = size_t(iy) * (nx + 1) + ix;
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                nv[k] = a.nvY[k * m.nYe + e];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                loadCell<DG>(f.src[k], N, c1, nb);
+                traceRight<DG>(nb, t1);
+                traceLeft<DG>(own[k], t2);
+                upwind<DG>(nv, t1, t2, tmp);
+                addEdge<DG>(acc[k], dt, tmp, 3);
+            }
+        }
+    }
+    // right Y-edge (this cell is "cell 1")
+    if (ix + 1 <= nx - 1) {
+        const size_t c2 = c + 1;
+        if (ice && m.ice[c2]) {
+            const size_t e = size_t(iy) * (nx + 1) + ix + 1;
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                nv[k] = a.nvY[k * m.nYe + e];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                loadCell<DG>(f.src[k], N, c2, nb);
+                traceRight<DG>(own[k], t1);
+                traceLeft<DG>(nb, t2);
+                upwind<DG>(nv, t1, t2, tmp);
+                addEdge<DG>(acc[k], -dt, tmp, 1);
+            }
+        }
+    }
+    // bottom X-edge (this cell is "cell 2")
+    if (iy >= 1) {
+        const size_t c1 = c - nx;
+        if (ice && m.ice[c1]) {
+            const size_t e = size_t(iy) * nx + ix;
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                nv[k] = a.nvX[k * m.nXe + e];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                loadCell<DG>(f.src[k], N, c1, nb);
+                traceTop<DG>(nb, t1);
+                traceBottom<DG>(own[k], t2);
+                upwind<DG>(nv, t1, t2, tmp);
+                addEdge<DG>(acc[k], dt, tmp, 0);
+            }
+        }
+    }
+    // top X-edge (this cell is "cell 1")
+    if (iy + 1 <= ny - 1) {
+        const size_t c2 = c + nx;
+        if (ice && m.ice[c2]) {
+            const size_t e = size_t(iy + 1) * nx + ix;
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                nv[k] = a.nvX[k * m.nXe + e];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                loadCell<DG>(f.src[k], N, c2, nb);
+                traceTop<DG>(own[k], t1);
+                traceBottom<DG>(nb, t2);
+                upwind<DG>(nv, t1, t2, tmp);
+                addEdge<DG>(acc[k], -dt, tmp, 2);
+            }
+        }
+    }
+    // periodic edges touching this cell, in list order
+    for (int p = m.perPtr[c]; p < m.perPtr[c + 1]; ++p) {
+        const int type = m.perEntry[4 * p], p1 = m.perEntry[4 * p + 1], p2 = m.perEntry[4 * p + 2];
+        const size_t e = static_cast<size_t>(m.perEntry[4 * p + 3]);
+        if (!m.ice[p1] || !m.ice[p2])
+            continue;
+        const double* nvp = type == 0 ? a.nvX : a.nvY;
+        const size_t ne = type == 0 ? m.nXe : m.nYe;
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            nv[k] = nvp[k * ne + e];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            double b1[DG], b2[DG];
+            loadCell<DG>(f.src[k], N, p1, b1);
+            loadCell<DG>(f.src[k], N, p2, b2);
+            if (type == 0) {
+                traceTop<DG>(b1, t1);
+                traceBottom<DG>(b2, t2);
+            } else {
+                traceRight<DG>(b1, t1);
+                traceLeft<DG>(b2, t2);
+            }
+            upwind<DG>(nv, t1, t2, tmp);
+            if (size_t(p1) == c)
+                addEdge<DG>(acc[k], -dt, tmp, type == 0 ? 2 : 1);
+            if (size_t(p2) == c)
+                addEdge<DG>(acc[k], dt, tmp, type == 0 ? 0 : 3);
+        }
+    }
+    // Dirichlet (closed) boundaries: outflow only (DGTransport.cpp:306-351)
+    const int seg = m.cellSeg[c];
+    if (seg) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            if (!(seg & (1 << s)))
+                continue;
+            size_t e;
+            const double* nvp;
+            size_t ne;
+            if (s == 0) { e = size_t(iy) * nx + ix; nvp = a.nvX; ne = m.nXe; }
+            else if (s == 1) { e = size_t(iy) * (nx + 1) + ix + 1; nvp = a.nvY; ne = m.nYe; }
+            else if (s == 2) { e = size_t(iy + 1) * nx + ix; nvp = a.nvX; ne = m.nXe; }
+            else { e = size_t(iy) * (nx + 1) + ix; nvp = a.nvY; ne = m.nYe; }
+            double vg[ED];
+#pragma unroll
+            for (int k = 0; k < ED; ++k)
+                nv[k] = nvp[k * ne + e];
+            edgeGauss<ED>(nv, vg);
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                if (s == 0) traceBottom<DG>(own[k], t1);
+                else if (s == 1) traceRight<DG>(own[k], t1);
+                else if (s == 2) traceTop<DG>(own[k], t1);
+                else traceLeft<DG>(own[k], t1);
+                double tg[ED];
+                edgeGauss<ED>(t1, tg);
+#pragma unroll
+                for (int g = 0; g < ED; ++g)
+                    tmp[g] = tg[g] * ((s == 0 || s == 3) ? fmax(-vg[g], 0.0) : fmax(vg[g], 0.0));
+                addEdge<DG>(acc[k], -dt, tmp, s);
+            }
+        }
+    }
+    // inverse mass and the Runge-Kutta combination
+    double Mi[DG * DG];
+#pragma unroll
+    for (int i = 0; i < DG * DG; ++i)
+        Mi[i] = a.minv[i * N + c];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        double r[DG], out[DG];
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                s += Mi[i * DG + j] * acc[k][j];
+            r[i] = s;
+        }
+        switch (a.mode) {
+        case STAGE_RK1:
+#pragma unroll
+            for (int i = 0; i < DG; ++i)
+                out[i] = own[k][i] + r[i];
+            break;
+        case STAGE_RK2_A:
+#pragma unroll
+            for (int i = 0; i < DG; ++i) {
+                f.k1[k][i * N + c] = r[i];
+                out[i] = f.phi[k][i * N + c] + r[i];
+            }
+            break;
+        case STAGE_RK2_B:
+#pragma unroll
+            for (int i = 0; i < DG; ++i)
+                out[i] = own[k][i] + 0.5 * (r[i] - f.k1[k][i * N + c]);
+            break;
+        case STAGE_RK3_A:
+#pragma unroll
+            for (int i = 0; i < DG; ++i)
+                out[i] = r[i] + f.phi[k][i * N + c];
+            break;
+        case STAGE_RK3_B:
+#pragma unroll
+            for (int i = 0; i < DG; ++i)
+                out[i] = (r[i] + own[k][i]) * 0.25 + 0.75 * f.phi[k][i * N + c];
+            break;
+        default: // STAGE_RK3_C
+#pragma unroll
+            for (int i = 0; i < DG; ++i)
+                out[i] = f.phi[k][i * N + c] * (1.0 / 3.0) + 2.0 / 3.0 * (r[i] + own[k][i]);
+            break;
+        }
+        if (f.lmax[k])
+            limitMax<DG>(out, f.vmax[k]);
+        if (f.lmin[k])
+            limitMin<DG>(out, f.vmin[k]);
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            f.dst[k][i * N + c] = out[i];
+    }
+}
+
+// ===========================================================================
+// DG -> CG2 (Interpolations.cpp:144-204): per node, contributions of the (up
+// to four) cells around it, odd cell rows first then even rows (the
+// reference's reversed-parity stripes), cells in ascending x; then the
+// boundary rows and columns are doubled.
+// ===========================================================================
+__device__ __forceinline__ int nodeCandidates(int i2, int n, int* cell, int* loc)
+{
+    // cells along one direction touching CG2 index i2 (0..2n), ascending
+    int k = 0;
+    if (i2 & 1) {
+        cell[k] = (i2 - 1) / 2;
+        loc[k++] = 1;
+    } else {
+        if (i2 >= 2) {
+            cell[k] = i2 / 2 - 1;
+            loc[k++] = 2;
+        }
+        if (i2 / 2 < n) {
+            cell[k] = i2 / 2;
+            loc[k++] = 0;
+        }
+    }
+    return k;
+}
+
+template <int DG, int NF>
+__global__ void __launch_bounds__(kBlock) kDG2CG(DevMesh m, const double* __restrict__ in0,
+    const double* __restrict__ in1, double* __restrict__ out0, double* __restrict__ out1)
+{
+    const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (t >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(t % s2), j2 = static_cast<int>(t / s2);
+    int cxs[2], lxs[2], cys[2], lys[2];
+    const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
+    const int nyc = nodeCandidates(j2, m.ny, cys, lys);
+    // odd rows first
+    int order[2] = { 0, 1 };
+    if (nyc == 2 && (cys[0] % 2) == 0) {
+        order[0] = 1;
+        order[1] = 0;
+    }
+    const double* in[2] = { in0, in1 };
+    double acc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+        acc[f] = 0.0;
+    for (int r = 0; r < nyc; ++r) {
+        const int cy = cys[order[r]], ly = lys[order[r]];
+        for (int k = 0; k < nxc; ++k) {
+            const int cx = cxs[k], lx = lxs[k];
+            const size_t c = size_t(cy) * m.nx + cx;
+            const int q = lx + 3 * ly;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                double at = 0.0;
+#pragma unroll
+                for (int j = 0; j < DG; ++j)
+                    at += in[f][j * m.N + c] * cT.psiLag3[j][q];
+                if (q == 4)
+                    acc[f] += at;
+                else if (q == 1 || q == 3 || q == 5 || q == 7)
+                    acc[f] += 0.5 * at;
+                else
+                    acc[f] += 0.25 * at;
+            }
+        }
+    }
+    double scale = 1.0;
+    if (j2 == 0 || j2 == 2 * m.ny)
+        scale *= 2.0;
+    if (i2 == 0 || i2 == 2 * m.nx)
+        scale *= 2.0;
+    out0[t] = acc[0] * scale;
+    if constexpr (NF > 1)
+        out1[t] = acc[1] * scale;
+}
+
+// ===========================================================================
+// Sea-surface-height gradient (CGDynamicsKernel.cpp:126-258)
+// ===========================================================================
+// CG1 Lagrange average of the DG0 ssh (reversed parity: odd rows first)
+__global__ void __launch_bounds__(kBlock) kSSHToCG1(DevMesh m, const double* __restrict__ ssh, double* __restrict__ cg1)
+{
+    const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (t >= m.Ncg1)
+        return;
+    const int s1 = m.nx + 1;
+    const int i1 = static_cast<int>(t % s1), j1 = static_cast<int>(t / s1);
+    int rows[2], nr = 0;
+    if (j1 >= 1) rows[nr++] = j1 - 1;
+    if (j1 < m.ny) rows[nr++] = j1;
+    if (nr == 2 && (rows[0] % 2) == 0) {
+        const int tmp = rows[0];
+        rows[0] = rows[1];
+        rows[1] = tmp;
+    }
+    double acc = 0.0;
+    for (int r = 0; r < nr; ++r)
+        for (int cx = i1 - 1; cx <= i1; ++cx) {
+            if (cx < 0 || cx >= m.nx)
+                continue;
+            acc += 0.25 * ssh[size_t(rows[r]) * m.nx + cx];
+        }
+    double scale = 1.0;
+    if (j1 == 0 || j1 == m.ny)
+        scale *= 2.0;
+    if (i1 == 0 || i1 == m.nx)
+        scale *= 2.0;
+    cg1[t] = acc * scale;
+}
+// CG1 gradient by element gather (even rows first), divided by the lumped mass
+__global__ void __launch_bounds__(kBlock) kSSHGrad1(DevMesh m, DevOps o, const double* __restrict__ cg1,
+    double* __restrict__ ug, double* __restrict__ vg)
+{
+    const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (t >= m.Ncg1)
+        return;
+    const int s1 = m.nx + 1;
+    const int i1 = static_cast<int>(t % s1), j1 = static_cast<int>(t / s1);
+    int rows[2], lys[2], nr = 0;
+    if (j1 >= 1) { rows[nr] = j1 - 1; lys[nr++] = 1; }
+    if (j1 < m.ny) { rows[nr] = j1; lys[nr++] = 0; }
+    if (nr == 2 && (rows[0] % 2) == 1) {
+        int a = rows[0]; rows[0] = rows[1]; rows[1] = a;
+        a = lys[0]; lys[0] = lys[1]; lys[1] = a;
+    }
+    double au = 0.0, av = 0.0;
+    const size_t N = m.N;
+    for (int r = 0; r < nr; ++r)
+        for (int lx = 1; lx >= 0; --lx) {
+            const int cx = i1 - lx;
+            if (cx < 0 || cx >= m.nx)
+                continue;
+            const int cy = rows[r], ly = lys[r];
+            const size_t e = size_t(cy) * m.nx + cx;
+            const size_t n0 = size_t(cy) * s1 + cx;
+            const double loc[4] = { cg1[n0], cg1[n0 + 1], cg1[n0 + s1], cg1[n0 + s1 + 1] };
+            const int k = lx + 2 * ly;
+            double tx = 0.0, ty = 0.0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                tx += o.dxssh[(k * 4 + j) * N + e] * loc[j];
+                ty += o.dyssh[(k * 4 + j) * N + e] * loc[j];
+            }
+            au -= tx;
+            av -= ty;
+        }
+    ug[t] = au / o.lumped1[t];
+    vg[t] = av / o.lumped1[t];
+}
+// boundary extension of the CG1 gradient (the value a boundary node copies
+// from the neighbouring interior node) followed by CG1 -> CG2 interpolation
+__device__ __forceinline__ size_t sshSource(int i1, int j1, int nx, int ny)
+{
+    int si = i1, sj = j1;
+    if (i1 == 0) si = 1;
+    if (i1 == nx) si = nx - 1;
+    if (j1 == 0) sj = 1;
+    if (j1 == ny) sj = ny - 1;
+    return size_t(sj) * (nx + 1) + si;
+}
+__global__ void __launch_bounds__(kBlock) kSSHToCG2(DevMesh m, const double* __restrict__ ug,
+    const double* __restrict__ vg, double* __restrict__ uGrad, double* __restrict__ vGrad)
+{
+    const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (t >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(t % s2), j2 = static_cast<int>(t / s2);
+    const int nx = m.nx, ny = m.ny;
+    const int ix = i2 / 2, iy = j2 / 2;
+    double u, v;
+    if (!(i2 & 1) && !(j2 & 1)) {
+        const size_t a = sshSource(ix, iy, nx, ny);
+        u = ug[a];
+        v = vg[a];
+    } else if ((i2 & 1) && !(j2 & 1)) {
+        const size_t a = sshSource(ix, iy, nx, ny), b = sshSource(ix + 1, iy, nx, ny);
+        u = 0.5 * (ug[a] + ug[b]);
+        v = 0.5 * (vg[a] + vg[b]);
+    } else if (!(i2 & 1) && (j2 & 1)) {
+        const size_t a = sshSource(ix, iy, nx, ny), b = sshSource(ix, iy + 1, nx, ny);
+        u = 0.5 * (ug[a] + ug[b]);
+        v = 0.5 * (vg[a] + vg[b]);
+    } else {
+        const size_t a = sshSource(ix, iy, nx, ny), b = sshSource(ix + 1, iy, nx, ny);
+        const size_t c = sshSource(ix, iy + 1, nx, ny), d = sshSource(ix + 1, iy + 1, nx, ny);
+        u = 0.25 * (ug[a] + ug[b] + ug[c] + ug[d]);
+        v = 0.25 * (vg[a] + vg[b] + vg[c] + vg[d]);
+    }
+    uGrad[t] = u;
+    vGrad[t] = v;
+}
+
+// ===========================================================================
+// mEVP
+// ===========================================================================
+__global__ void __launch_bounds__(kBlock) kMevpPrepNodes(size_t n, MevpNodeState st, MevpParams p)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    // clamps of prepareIteration (CGDynamicsKernel.cpp:273-275)
+    const double A = fmax(fmin(st.cgA[i], 1.0), 1.e-4);
+    const double H = fmax(st.cgH[i], 1.e-4);
+    st.cgA[i] = A;
+    st.cgH[i] = H;
+    st.u0[i] = st.u[i];
+    st.v0[i] = st.v[i];
+    const double rhoH = p.rho_ice * H;
+    const double c1 = rhoH / p.dt;
+    st.c1[i] = c1;
+    st.c1b[i] = c1 * (1.0 + p.beta);
+    const double ua = st.ua[i], va = st.va[i];
+    const double absatm = sqrt(ua * ua + va * va);
+    st.fau[i] = p.F_atm * absatm * ua;
+    st.fav[i] = p.F_atm * absatm * va;
+    st.rhfc[i] = rhoH * p.fc;
+    st.gu[i] = rhoH * p.gravity * st.uGrad[i];
+    st.gv[i] = rhoH * p.gravity * st.vGrad[i];
+}
+
+template <int DG>
+__global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const double* __restrict__ h,
+    const double* __restrict__ a, double* __restrict__ Pg, double Pstar)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    double hc[DG], ac[DG];
+    loadCell<DG>(h, N, e, hc);
+    loadCell<DG>(a, N, e, ac);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        double hs = 0.0, as = 0.0;
+#pragma unroll
+        for (int j = 0; j < DG; ++j) {
+            hs += hc[j] * cT.psi[3][j][q];
+            as += ac[j] * cT.psi[3][j][q];
+        }
+        const double hq = fmax(hs, 0.0);
+        const double aq = fmin(fmax(as, 0.0), 1.0);
+        Pg[q * N + e] = Pstar * hq * exp(-20.0 * (1.0 - aq));
+    }
+}
+
+// One mEVP iteration, element part.  Per element: the strain at the 3x3 Gauss
+// points straight from the 9 CG2 velocity nodes (composite operator
+// G = psi^T M^{-1} divS^T), Delta, the relaxed stress update projected with
+// iMJwPSI, and the element's share of the stress divergence at its 9 nodes,
+// written to contrib[18][N] for the node kernel to gather.
+__global__ void __launch_bounds__(kBlock) kMevpStress(DevMesh m, DevOps o, const double* __restrict__ u,
+    const double* __restrict__ v, const double* __restrict__ Pg, double* __restrict__ s11,
+    double* __restrict__ s12, double* __restrict__ s22, double* __restrict__ contrib, MevpParams p,
+    int* __restrict__ err)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    const size_t N = m.N;
+    if (e >= N)
+        return;
+    const bool ice = m.ice[e] != 0;
+    const size_t s2 = 2 * size_t(m.nx) + 1;
+    const size_t ix = e % m.nx, iy = e / m.nx;
+    const size_t base = 2 * s2 * iy + 2 * ix;
+    double ul[9], vl[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const size_t nd = base + (j % 3) + (j / 3) * s2;
+        ul[j] = ice ? u[nd] : 0.0;
+        vl[j] = ice ? v[nd] : 0.0;
+    }
+    const double inva = 1.0 / p.alpha;
+    const double dmin2 = p.DeltaMin * p.DeltaMin;
+    double a11[8], a12[8], a22[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        a11[k] = a12[k] = a22[k] = 0.0;
+#pragma unroll 1
+    for (int q = 0; q < 9; ++q) {
+        double ex = 0.0, ey = 0.0, exv = 0.0, eyu = 0.0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const double gxq = o.gx[(q * 9 + j) * N + e];
+            const double gyq = o.gy[(q * 9 + j) * N + e];
+            ex = fma(gxq, ul[j], ex);
+            ey = fma(gyq, vl[j], ey);
+            exv = fma(gxq, vl[j], exv);
+            eyu = fma(gyq, ul[j], eyu);
+        }
+        const double e11 = ex, e22 = ey, e12 = 0.5 * (exv + eyu);
+        const double d2 = dmin2 + 1.25 * (e11 * e11 + e22 * e22) + 1.50 * e11 * e22 + e12 * e12;
+        const double rdelta = rsqrt(d2);
+        const double P = Pg[q * N + e];
+        const double t = P * rdelta;
+        const double f11 = inva * (0.125 * t * (5.0 * e11 + 3.0 * e22) - 0.5 * P);
+        const double f12 = inva * (0.25 * t * e12);
+        const double f22 = inva * (0.125 * t * (5.0 * e22 + 3.0 * e11) - 0.5 * P);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const double wk = o.w[(k * 9 + q) * N + e];
+            a11[k] = fma(wk, f11, a11[k]);
+            a12[k] = fma(wk, f12, a12[k]);
+            a22[k] = fma(wk, f22, a22[k]);
+        }
+    }
+    const double keep = 1.0 - inva;
+    double t11[8], t12[8], t22[8];
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        t11[k] = s11[k * N + e] * keep + a11[k];
+        t12[k] = s12[k * N + e] * keep + a12[k];
+        t22[k] = s22[k * N + e] * keep + a22[k];
+        s11[k * N + e] = t11[k];
+        s12[k * N + e] = t12[k];
+        s22[k * N + e] = t22[k];
+        finite = finite && isfinite(t11[k]) && isfinite(t12[k]) && isfinite(t22[k]);
+    }
+    if (!finite)
+        atomicOr(err, DEV_ERR_NONFINITE_STRESS);
+    // stress divergence contributions: tx = divS1 s11 + divS2 s12,
+    // ty = divS1 s12 + divS2 s22 (CGDynamicsKernel.cpp:340-363)
+#pragma unroll 1
+    for (int j = 0; j < 9; ++j) {
+        double tx = 0.0, ty = 0.0;
+        if (ice) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const double d1 = o.d1[(j * 8 + k) * N + e];
+                const double d2v = o.d2[(j * 8 + k) * N + e];
+                tx = fma(d1, t11[k], fma(d2v, t12[k], tx));
+                ty = fma(d1, t12[k], fma(d2v, t22[k], ty));
+            }
+        }
+        contrib[j * N + e] = tx;
+        contrib[(9 + j) * N + e] = ty;
+    }
+}
+
+// Gathers the divergence contributions of the (up to four) ice cells around
+// a CG2 node in the reference's scatter order (even cell rows first, then
+// odd; ascending x) and returns -sum.
+__device__ __forceinline__ void gatherDivergence(const DevMesh& m, int i2, int j2,
+    const double* __restrict__ contrib, double& dx, double& dy)
+{
+    int cxs[2], lxs[2], cys[2], lys[2];
+    const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
+    const int nyc = nodeCandidates(j2, m.ny, cys, lys);
+    int order[2] = { 0, 1 };
+    if (nyc == 2 && (cys[0] % 2) == 1) {
+        order[0] = 1;
+        order[1] = 0;
+    }
+    const size_t N = m.N;
+    double ax = 0.0, ay = 0.0;
+    for (int r = 0; r < nyc; ++r) {
+        const int cy = cys[order[r]], ly = lys[order[r]];
+        for (int k = 0; k < nxc; ++k) {
+            const size_t c = size_t(cy) * m.nx + cxs[k];
+            const int j = lxs[k] + 3 * ly;
+            ax -= contrib[j * N + c];
+            ay -= contrib[(9 + j) * N + c];
+        }
+    }
+    dx = ax;
+    dy = ay;
+}
+
+__global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, MevpNodeState st,
+    const double* __restrict__ contrib, MevpParams p, int* __restrict__ err)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    const bool dir = m.cg2Dir[i] != 0;
+    double dSx = 0.0, dSy = 0.0;
+    if (!dir)
+        gatherDivergence(m, i2, j2, contrib, dSx, dSy);
+    const double u = st.u[i], v = st.v[i];
+    const double uo = st.uo[i], vo = st.vo[i];
+    const double uOcnRel = uo - u, vOcnRel = v - vo;
+    const double absocn = sqrt(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
+    const double A = st.cgA[i];
+    const double c1 = st.c1[i];
+    const double invm = o.invm2[i];
+    const double rden = 1.0 / (st.c1b[i] + A * p.F_ocean * absocn);
+    const double focn = p.F_ocean * absocn;
+    double un = rden * (c1 * (p.beta * u + st.u0[i]) + A * (st.fau[i] + focn * uo) - st.rhfc[i] * u
+        - st.gu[i] + dSx * invm);
+    double vn = rden * (c1 * (p.beta * v + st.v0[i]) + A * (st.fav[i] + focn * vo) + st.rhfc[i] * v
+        - st.gv[i] + dSy * invm);
+    if (!isfinite(un) || !isfinite(vn))
+        atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
+    if (dir) {
+        un = 0.0;
+        vn = 0.0;
+    }
+    st.u[i] = un;
+    st.v[i] = vn;
+}
+
+// ===========================================================================
+// BBM (BBMStressUpdateStep.hpp:31-195, BrittleCGDynamicsKernel.hpp:206-254)
+// ===========================================================================
+__global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState st)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    st.cgA[i] = fmax(fmin(st.cgA[i], 1.0), 1.e-4);
+    st.cgH[i] = fmax(st.cgH[i], 1.e-4);
+    st.avgU[i] = 0.0;
+    st.avgV[i] = 0.0;
+}
+
+template <int DG>
+__global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, DevOps o, const double* __restrict__ u,
+    const double* __restrict__ v, const double* __restrict__ h, const double* __restrict__ a,
+    double* __restrict__ damage, double* __restrict__ s11, double* __restrict__ s12,
+    double* __restrict__ s22, double* __restrict__ contrib, BbmParams p, int* __restrict__ err)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    const size_t N = m.N;
+    if (e >= N)
+        return;
+    const bool ice = m.ice[e] != 0;
+    const size_t s2 = 2 * size_t(m.nx) + 1;
+    const size_t ix = e % m.nx, iy = e / m.nx;
+    const size_t base = 2 * s2 * iy + 2 * ix;
+    double ul[9], vl[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const size_t nd = base + (j % 3) + (j / 3) * s2;
+        ul[j] = ice ? u[nd] : 0.0;
+        vl[j] = ice ? v[nd] : 0.0;
+    }
+    double hc[DG], ac[DG], dc[DG], c11[8], c12[8], c22[8];
+    loadCell<DG>(h, N, e, hc);
+    loadCell<DG>(a, N, e, ac);
+    loadCell<DG>(damage, N, e, dc);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        c11[k] = s11[k * N + e];
+        c12[k] = s12[k * N + e];
+        c22[k] = s22[k * N + e];
+    }
+    const double dt = p.dt;
+    const double hi = o.hsize[e];
+    const double scale_coef = sqrt(0.1 / hi);
+    const double tdScale = hi * sqrt(2. * (1. + p.nu0) * p.rho_ice);
+    double n11[8], n12[8], n22[8], nd[DG];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        n11[k] = n12[k] = n22[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < DG; ++k)
+        nd[k] = 0.0;
+#pragma unroll 1
+    for (int q = 0; q < 9; ++q) {
+        double hs = 0.0, as = 0.0, ds = 0.0;
+#pragma unroll
+        for (int j = 0; j < DG; ++j) {
+            hs += hc[j] * cT.psi[3][j][q];
+            as += ac[j] * cT.psi[3][j][q];
+            ds += dc[j] * cT.psi[3][j][q];
+        }
+        const double hG = fmax(hs, 0.0);
+        const double aG = fmin(fmax(as, 0.0), 1.0);
+        double dG = fmin(fmax(ds, 1e-12), 1.0);
+        double ex = 0.0, ey = 0.0, exv = 0.0, eyu = 0.0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const double gxq = o.gx[(q * 9 + j) * N + e];
+            const double gyq = o.gy[(q * 9 + j) * N + e];
+            ex = fma(gxq, ul[j], ex);
+            ey = fma(gyq, vl[j], ey);
+            exv = fma(gxq, vl[j], exv);
+            eyu = fma(gyq, ul[j], eyu);
+        }
+        const double e11 = ex, e22 = ey, e12 = 0.5 * (exv + eyu);
+        double g11 = 0.0, g12 = 0.0, g22 = 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            g11 += c11[k] * cT.psi[3][k][q];
+            g12 += c12[k] * cT.psi[3][k][q];
+            g22 += c22[k] * cT.psi[3][k][q];
+        }
+        double sigma_n = 0.5 * (g11 + g22);
+        const double expC = exp(p.compaction_param * (1.0 - aG));
+        const double powalphaexpC = pow(dG * expC, p.exponent_relaxation_sigma - 1);
+        const double time_viscous = p.lambda * powalphaexpC;
+        const double Pmax = p.P0 * pow(hG, p.exponent_compression_factor + 1.) * expC;
+        const double tildeP = (sigma_n < 0.0) ? fmin(-Pmax / sigma_n, 1.0) : 0.;
+        const double multiplicator = time_viscous / (time_viscous + (1. - tildeP) * dt);
+        const double elasticity = hG * p.young * dG * expC;
+        const double Dunit_factor = dt * elasticity / (1. - (p.nu0 * p.nu0));
+        g11 += Dunit_factor * (e11 + p.nu0 * e22);
+        g22 += Dunit_factor * (p.nu0 * e11 + e22);
+        g12 += Dunit_factor * e12 * (1. - p.nu0);
+        g11 *= multiplicator;
+        g22 *= multiplicator;
+        g12 *= multiplicator;
+        sigma_n = 0.5 * (g11 + g22);
+        const double dd = g11 - g22;
+        const double tau = sqrt(0.25 * (dd * dd) + g12 * g12);
+        const double cohesion = p.C_lab * scale_coef * hG;
+        const double compr = p.compr_strength * scale_coef * hG;
+        double dcrit = (tau + p.tan_phi * sigma_n > 0.) ? cohesion / (tau + p.tan_phi * sigma_n) : 1.;
+        dcrit = (sigma_n < -compr) ? -compr / sigma_n : dcrit;
+        dcrit = fmin(dcrit, 1.0);
+        const double td = tdScale / sqrt(elasticity);
+        const double relax = (1. - dcrit) * dt / td;
+        dG -= dG * relax;
+        g11 -= g11 * relax;
+        g12 -= g12 * relax;
+        g22 -= g22 * relax;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const double wk = o.w[(k * 9 + q) * N + e];
+            n11[k] = fma(wk, g11, n11[k]);
+            n12[k] = fma(wk, g12, n12[k]);
+            n22[k] = fma(wk, g22, n22[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < DG; ++k)
+            nd[k] = fma(o.wdam[(k * 9 + q) * N + e], dG, nd[k]);
+    }
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        s11[k * N + e] = n11[k];
+        s12[k * N + e] = n12[k];
+        s22[k * N + e] = n22[k];
+        finite = finite && isfinite(n11[k]) && isfinite(n12[k]) && isfinite(n22[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < DG; ++k)
+        damage[k * N + e] = nd[k];
+    if (!finite)
+        atomicOr(err, DEV_ERR_NONFINITE_STRESS);
+#pragma unroll 1
+    for (int j = 0; j < 9; ++j) {
+        double tx = 0.0, ty = 0.0;
+        if (ice) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const double d1 = o.d1[(j * 8 + k) * N + e];
+                const double d2v = o.d2[(j * 8 + k) * N + e];
+                tx = fma(d1, n11[k], fma(d2v, n12[k], tx));
+                ty = fma(d1, n12[k], fma(d2v, n22[k], ty));
+            }
+        }
+        contrib[j * N + e] = tx;
+        contrib[(9 + j) * N + e] = ty;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) kBbmMomentum(DevMesh m, DevOps o, BbmNodeState st,
+    const double* __restrict__ contrib, BbmParams p, int* __restrict__ err)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    const bool dir = m.cg2Dir[i] != 0;
+    double dSx = 0.0, dSy = 0.0;
+    if (!dir)
+        gatherDivergence(m, i2, j2, contrib, dSx, dSy);
+    const double H = st.cgH[i], A = st.cgA[i];
+    const double dteOverMass = p.dt / (p.rho_ice * H);
+    const double uIce = st.u[i], vIce = st.v[i];
+    const double uo = st.uo[i], vo = st.vo[i], ua = st.ua[i], va = st.va[i];
+    const double cPrime = A * p.F_ocean * hypot(uo - uIce, vo - vIce);
+    const double alpha = 1 + dteOverMass * (cPrime * p.cosA);
+    const double beta = p.dt * p.fc + dteOverMass * cPrime * p.sinA;
+    const double rDenom = 1 / (alpha * alpha + beta * beta);
+    const double dragAtm = A * p.F_atm * hypot(ua, va);
+    const double tauX = dragAtm * ua + cPrime * (uo * p.cosA - vo * p.sinA);
+    const double tauY = dragAtm * va + cPrime * (vo * p.cosA + uo * p.sinA);
+    const double invm = o.invm2[i];
+    const double gradX = dSx * invm - p.rho_ice * H * p.gravity * st.uGrad[i];
+    const double gradY = dSy * invm - p.rho_ice * H * p.gravity * st.vGrad[i];
+    double un = alpha * uIce + beta * vIce + dteOverMass * (alpha * (gradX + tauX) + beta * (gradY + tauY));
+    un *= rDenom;
+    double vn = alpha * vIce - beta * uIce + dteOverMass * (alpha * (gradY + tauY) + beta * (gradX + tauX));
+    vn *= rDenom;
+    if (!isfinite(un) || !isfinite(vn))
+        atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
+    st.avgU[i] += un / p.nSteps;
+    st.avgV[i] += vn / p.nSteps;
+    if (dir) {
+        un = 0.0;
+        vn = 0.0;
+    }
+    st.u[i] = un;
+    st.v[i] = vn;
+}
+
+// ===========================================================================
+// Misc
+// ===========================================================================
+__global__ void kIceOceanStress(size_t n, int brittle, const double* __restrict__ u,
+    const double* __restrict__ v, const double* __restrict__ uo, const double* __restrict__ vo,
+    double Fo, double ca, double sa, double* __restrict__ tx, double* __restrict__ ty)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    if (!brittle) {
+        const double ur = u[i] - uo[i], vr = v[i] - vo[i];
+        const double a = sqrt(ur * ur + vr * vr);
+        tx[i] = Fo * a * ur;
+        ty[i] = Fo * a * vr;
+    } else {
+        const double ur = uo[i] - u[i], vr = vo[i] - v[i];
+        const double cp = Fo * hypot(ur, vr);
+        tx[i] = cp * (ur * ca - vr * sa);
+        ty[i] = cp * (vr * ca + ur * sa);
+    }
+}
+
+__global__ void kAosToSoa(size_t N, int nin, int dg, const double* __restrict__ aos, double* __restrict__ soa)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    if (nin == dg) {
+        for (int j = 0; j < dg; ++j)
+            soa[j * N + e] = aos[e * dg + j];
+    } else {
+        soa[e] = aos[e * nin];
+        for (int j = 1; j < dg; ++j)
+            soa[j * N + e] = 0.0;
+    }
+}
+__global__ void kSoaToAos(size_t N, int dg, int nout, const double* __restrict__ soa, double* __restrict__ aos)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    for (int j = 0; j < nout; ++j)
+        aos[e * nout + j] = soa[j * N + e];
+}
+
+// Per-element masses summed by a fixed-shape tree: warp shuffles, then the
+// block's warps, then one block over the per-block partials.
+template <int DG>
+__global__ void __launch_bounds__(256) kMeanValuePartial(size_t N, const double* __restrict__ phi,
+    const double* __restrict__ jw3, double* __restrict__ partials)
+{
+    __shared__ double ws[8];
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    double s = 0.0;
+    if (e < N) {
+        double c[DG];
+        loadCell<DG>(phi, N, e, c);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                v += c[j] * cT.psi[3][j][q];
+            s += v * jw3[q * N + e];
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < 8 ? ws[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            t += __shfl_down_sync(0xffffffffu, t, off);
+        if (threadIdx.x == 0)
+            partials[blockIdx.x] = t;
+    }
+}
+__global__ void __launch_bounds__(1024) kReduceFinal(size_t n, const double* __restrict__ partials, double* __restrict__ out)
+{
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x)
+        s += partials[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = ws[threadIdx.x];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            t += __shfl_down_sync(0xffffffffu, t, off);
+        if (threadIdx.x == 0)
+            *out = t;
+    }
+}
+
+} // namespace
+
+// ===========================================================================
+// Launchers
+// ===========================================================================
+#define NSDG_DG_SWITCH(dg, CALL)                                                                  \
+    switch (dg) {                                                                                  \
+    case 1: { constexpr int D = 1; CALL; } break;                                                  \
+    case 3: { constexpr int D = 3; CALL; } break;                                                  \
+    case 6: { constexpr int D = 6; CALL; } break;                                                  \
+    case 8: { constexpr int D = 8; CALL; } break;                                                  \
+    default: return cudaErrorInvalidValue;                                                         \
+    }
+
+cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* jw, const double* minv,
+    int nf, const double* const* cg, double* const* out)
+{
+    const unsigned g = blocksFor(m.N);
+    if (nf == 1) {
+        NSDG_DG_SWITCH(dg, (kCG2DG<D, 1><<<g, kBlock, 0, s>>>(m.nx, m.N, jw, minv, cg[0], nullptr, out[0], nullptr)));
+    } else {
+        NSDG_DG_SWITCH(dg, (kCG2DG<D, 2><<<g, kBlock, 0, s>>>(m.nx, m.N, jw, minv, cg[0], cg[1], out[0], out[1])));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
+    const double* vely, double* nvX, double* nvY)
+{
+    const unsigned g = blocksFor(m.nXe + m.nYe);
+    NSDG_DG_SWITCH(dg, (kNormalVelocity<D><<<g, kBlock, 0, s>>>(m, velx, vely, nvX, nvY)));
+    return cudaGetLastError();
+}
+
+cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const double* cellX,
+    const double* cellY, const double* minv, const double* velx, const double* vely,
+    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f)
+{
+    TransportArgs a { m, cellX, cellY, minv, velx, vely, nvX, nvY, dt, mode };
+    const unsigned g = blocksFor(m.N);
+    switch (f.nf) {
+    case 1: NSDG_DG_SWITCH(dg, (kTransportStage<D, 1><<<g, kBlock, 0, s>>>(a, f))); break;
+    case 2: NSDG_DG_SWITCH(dg, (kTransportStage<D, 2><<<g, kBlock, 0, s>>>(a, f))); break;
+    case 3: NSDG_DG_SWITCH(dg, (kTransportStage<D, 3><<<g, kBlock, 0, s>>>(a, f))); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchDG2CG(cudaStream_t s, const DevMesh& m, int dg, int nf, const double* const* dgIn,
+    double* const* cgOut)
+{
+    const unsigned g = blocksFor(m.Ncg);
+    if (nf == 1) {
+        NSDG_DG_SWITCH(dg, (kDG2CG<D, 1><<<g, kBlock, 0, s>>>(m, dgIn[0], nullptr, cgOut[0], nullptr)));
+    } else {
+        NSDG_DG_SWITCH(dg, (kDG2CG<D, 2><<<g, kBlock, 0, s>>>(m, dgIn[0], dgIn[1], cgOut[0], cgOut[1])));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchSSHGradient(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* ssh,
+    double* scratch, double* uGrad, double* vGrad)
+{
+    double* cg1 = scratch;
+    double* ug = scratch + m.Ncg1;
+    double* vg = scratch + 2 * m.Ncg1;
+    kSSHToCG1<<<blocksFor(m.Ncg1), kBlock, 0, s>>>(m, ssh, cg1);
+    kSSHGrad1<<<blocksFor(m.Ncg1), kBlock, 0, s>>>(m, o, cg1, ug, vg);
+    kSSHToCG2<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, ug, vg, uGrad, vGrad);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st, const MevpParams& p)
+{
+    kMevpPrepNodes<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
+    const double* a, double* Pg, const MevpParams& p)
+{
+    const unsigned g = blocksFor(m.N);
+    switch (dg) {
+    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
+    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
+    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
+    const double* v, const double* Pg, double* s11, double* s12, double* s22, double* contrib,
+    const MevpParams& p, int* err)
+{
+    kMevpStress<<<blocksFor(m.N), kBlock, 0, s>>>(m, o, u, v, Pg, s11, s12, s22, contrib, p, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o, const MevpNodeState& st,
+    const double* contrib, const MevpParams& p, int* err)
+{
+    kMevpMomentum<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const double* u, const double* v,
+    const double* uo, const double* vo, double F_ocean, double cosA, double sinA, double* tx, double* ty)
+{
+    kIceOceanStress<<<blocksFor(n), kBlock, 0, s>>>(n, brittle, u, v, uo, vo, F_ocean, cosA, sinA, tx, ty);
+    return cudaGetLastError();
+}
+
+cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st)
+{
+    kBbmPrepNodes<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg, const double* u,
+    const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,
+    double* s22, double* contrib, const BbmParams& p, int* err)
+{
+    const unsigned g = blocksFor(m.N);
+    switch (dg) {
+    case 1: kBbmStress<1><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    case 3: kBbmStress<3><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    case 6: kBbmStress<6><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o, const BbmNodeState& st,
+    const double* contrib, const BbmParams& p, int* err)
+{
+    kBbmMomentum<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchAosToSoa(cudaStream_t s, size_t N, int nin, int dg, const double* aos, double* soa)
+{
+    kAosToSoa<<<blocksFor(N), kBlock, 0, s>>>(N, nin, dg, aos, soa);
+    return cudaGetLastError();
+}
+cudaError_t launchSoaToAos(cudaStream_t s, size_t N, int dg, int nout, const double* soa, double* aos)
+{
+    kSoaToAos<<<blocksFor(N), kBlock, 0, s>>>(N, dg, nout, soa, aos);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMeanValue(cudaStream_t s, size_t N, int dg, const double* phi, const double* jw3,
+    double* partials, double* out)
+{
+    const unsigned g = blocksFor(N, 256);
+    NSDG_DG_SWITCH(dg, (kMeanValuePartial<D><<<g, 256, 0, s>>>(N, phi, jw3, partials)));
+    kReduceFinal<<<1, 1024, 0, s>>>(g, partials, out);
+    return cudaGetLastError();
+}
+
+} // namespace nsdg

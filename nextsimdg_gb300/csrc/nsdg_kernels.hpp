@@ -1,0 +1,187 @@
+// nsdg_kernels.hpp — host-callable launchers for the sm_103a kernels.
+//
+// Pure C++ declarations (no CUDA syntax) so the C-ABI layer can be compiled
+// by the host compiler.  Every launcher enqueues on `stream` and returns the
+// cudaError_t of the launch.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nsdg_host.hpp"
+
+namespace nsdg {
+
+// Device copy of the mesh connectivity and boundary flags.
+struct DevMesh {
+    int nx = 0, ny = 0;
+    size_t N = 0;      // elements
+    size_t Ncg = 0;    // CG2 nodes (2nx+1)(2ny+1)
+    size_t Ncg1 = 0;   // CG1 nodes (nx+1)(ny+1)
+    size_t nXe = 0;    // X-edges nx(ny+1)
+    size_t nYe = 0;    // Y-edges (nx+1)ny
+    const double* vx = nullptr;
+    const double* vy = nullptr;
+    const uint8_t* ice = nullptr;
+    const uint8_t* cellSeg = nullptr;
+    const uint8_t* edgeXCount = nullptr;
+    const uint8_t* edgeYCount = nullptr;
+    const uint8_t* cg2Dir = nullptr;
+    const int* perPtr = nullptr;
+    const int* perEntry = nullptr;
+};
+
+// Device copy of the element operators (entry-major SoA, see nsdg_host.hpp).
+struct DevOps {
+    const double* cellX = nullptr;
+    const double* cellY = nullptr;
+    const double* minv = nullptr;
+    const double* jwA = nullptr;
+    const double* jw3 = nullptr;
+    const double* cellX8 = nullptr;
+    const double* cellY8 = nullptr;
+    const double* minv8 = nullptr;
+    const double* gx = nullptr;
+    const double* gy = nullptr;
+    const double* w = nullptr;
+    const double* d1 = nullptr;
+    const double* d2 = nullptr;
+    const double* wdam = nullptr;
+    const double* dxssh = nullptr;
+    const double* dyssh = nullptr;
+    const double* hsize = nullptr;
+    const double* invm2 = nullptr;   // 1 / lumped CG2 mass
+    const double* lumped1 = nullptr; // lumped CG1 mass
+};
+
+// Status bits written by kernels into the handle's device error word.
+enum DeviceError : int {
+    DEV_ERR_NONFINITE_VELOCITY = 1,
+    DEV_ERR_NONFINITE_STRESS = 2,
+};
+
+cudaError_t uploadConstTables();
+
+// --- transport ---------------------------------------------------------
+enum StageMode { STAGE_RK1 = 0, STAGE_RK2_A, STAGE_RK2_B, STAGE_RK3_A, STAGE_RK3_B, STAGE_RK3_C };
+struct StageFields {
+    int nf = 1;
+    const double* src[3] = {};
+    const double* phi[3] = {};
+    double* k1[3] = {};
+    double* dst[3] = {};
+    int lmax[3] = {};
+    int lmin[3] = {};
+    double vmax[3] = {};
+    double vmin[3] = {};
+};
+// CG2 -> DG projection of nf (<=2) node fields (Interpolations.cpp:74-122).
+// Uses jw/minv for `dg` components (jwA/minv, or jw3/minv8 for dg == 8).
+cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* jw,
+    const double* minv, int nf, const double* const* cg, double* const* out);
+// Edge normal velocities (DGTransport.cpp:158-252).
+cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
+    const double* vely, double* nvX, double* nvY);
+// One Runge-Kutta stage of the DG transport operator for nf fields sharing a
+// velocity (DGTransport.cpp:435-566).
+cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const double* cellX,
+    const double* cellY, const double* minv, const double* velx, const double* vely,
+    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f);
+
+// --- interpolation / preparation ----------------------------------------
+// DG -> CG2 Lagrange averaging of nf (<=2) DG fields (Interpolations.cpp:144-204).
+cudaError_t launchDG2CG(cudaStream_t s, const DevMesh& m, int dg, int nf,
+    const double* const* dgIn, double* const* cgOut);
+// Gradient of the sea-surface height on CG2 (CGDynamicsKernel.cpp:126-258);
+// scratch needs 3*Ncg1 doubles.
+cudaError_t launchSSHGradient(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* ssh,
+    double* scratch, double* uGrad, double* vGrad);
+
+// mEVP per-step node constants (CGDynamicsKernel.cpp:260-276 clamps plus the
+// loop-invariant parts of VPCGDynamicsKernel.hpp:132-172).
+struct MevpNodeState {
+    double* u;
+    double* v;
+    double* u0;
+    double* v0;
+    double* cgH;     // in: DG2CG(h) ; out: clamped
+    double* cgA;     // in: DG2CG(A) ; out: clamped
+    const double* uo;
+    const double* vo;
+    const double* ua;
+    const double* va;
+    const double* uGrad;
+    const double* vGrad;
+    double* c1;      // rho H / dt
+    double* c1b;     // rho H / dt * (1 + beta)
+    double* fau;     // F_atm |wind| uwind
+    double* fav;
+    double* rhfc;    // rho H fc
+    double* gu;      // rho H g dxSSH
+    double* gv;
+};
+struct MevpParams {
+    double rho_ice, F_atm, F_ocean, fc, gravity, Pstar, DeltaMin, alpha, beta, dt;
+};
+cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st,
+    const MevpParams& p);
+// P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298).
+cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
+    const double* a, double* Pg, const MevpParams& p);
+// Strain at the Gauss points, mEVP stress update and the per-element stress
+// divergence contributions (CGDynamicsKernel.cpp:300-398, MEVPStressUpdateStep.hpp).
+cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
+    const double* v, const double* Pg, double* s11, double* s12, double* s22, double* contrib,
+    const MevpParams& p, int* err);
+// Node gather of the divergence, Dirichlet zero, implicit velocity update and
+// boundary zero (CGDynamicsKernel.cpp:365-444, VPCGDynamicsKernel.hpp:132-172).
+cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
+    const MevpNodeState& st, const double* contrib, const MevpParams& p, int* err);
+
+// Ice-ocean stress on CG2 nodes (VPCGDynamicsKernel.hpp:96-120 / BrittleCGDynamicsKernel.hpp:168-192).
+cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const double* u,
+    const double* v, const double* uo, const double* vo, double F_ocean, double cosA, double sinA,
+    double* tx, double* ty);
+
+// --- BBM -----------------------------------------------------------------
+struct BbmParams {
+    double rho_ice, F_atm, F_ocean, fc, gravity, dt, nSteps, cosA, sinA;
+    double compaction_param, nu0, young, P0, lambda, exponent_relaxation_sigma,
+        exponent_compression_factor, tan_phi, compr_strength, C_lab;
+};
+struct BbmNodeState {
+    double* u;
+    double* v;
+    double* avgU;
+    double* avgV;
+    double* cgH;
+    double* cgA;
+    const double* uo;
+    const double* vo;
+    const double* ua;
+    const double* va;
+    const double* uGrad;
+    const double* vGrad;
+};
+cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st);
+// Per-step Gauss-point constants of the BBM update from h and A:
+// 0 hG, 1 expC, 2 Pmax, 3 elasticity, 4 Dunit_factor / dt ... (9 x 5 per element)
+cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg,
+    const double* u, const double* v, const double* h, const double* a, double* damage,
+    double* s11, double* s12, double* s22, double* contrib, const BbmParams& p, int* err);
+cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
+    const BbmNodeState& st, const double* contrib, const BbmParams& p, int* err);
+
+// --- layout conversion, reductions ---------------------------------------
+// host ModelArray layout (AoS, nin comps) -> device SoA with `dg` comps,
+// following DGModelArray::ma2dg (zero, then all or component 0 only).
+cudaError_t launchAosToSoa(cudaStream_t s, size_t N, int nin, int dg, const double* aos, double* soa);
+// device SoA -> AoS with `nout` comps (all, or component 0 only)
+cudaError_t launchSoaToAos(cudaStream_t s, size_t N, int dg, int nout, const double* soa, double* aos);
+// Tools::MeanValue: writes partial sums per block into `partials` and the
+// final FP64 sum into *out (device).  partials needs ceil(N/256) doubles.
+cudaError_t launchMeanValue(cudaStream_t s, size_t N, int dg, const double* phi, const double* jw3,
+    double* partials, double* out);
+
+} // namespace nsdg

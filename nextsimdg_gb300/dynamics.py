@@ -1,0 +1,264 @@
+"""Python mirror of the reference's dynamics-kernel interface, over the C ABI.
+
+Class and method names follow the reference so that tests and callers read
+like the reference's own code:
+
+  MEVPDynamicsKernel / BBMDynamicsKernel
+      dynamics/src/include/MEVPDynamicsKernel.hpp, BBMDynamicsKernel.hpp
+      initialise(coords, isSpherical, mask)   DynamicsKernel.hpp:44-75
+      setData(name, data)                     DynamicsKernel.hpp:93-110,
+                                              CGDynamicsKernel.cpp:54-90
+      getDG0Data(name) / getDGData(name)      DynamicsKernel.hpp:119-156,
+                                              CGDynamicsKernel.cpp:93-118
+      update(tst)                             VPCGDynamicsKernel.hpp:63-94
+  DGTransport                                 dynamics/src/include/DGTransport.hpp:27-152
+
+Arrays use the ModelArray layout: H fields have shape (N,), DG fields
+(N, ncomp) with the element index i + nx*j, coordinates ((nx+1)*(ny+1), 2).
+Errors map to the exception types the reference throws: an unknown field
+name raises KeyError (std::out_of_range from .at()), other failures raise
+NsdgError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_char_p, c_double, c_float, c_int, c_size_t, c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import NsdgError, Params
+
+__all__ = ["TimestepTime", "MEVPDynamicsKernel", "BBMDynamicsKernel", "DGTransport", "Params",
+           "NsdgError", "default_params"]
+
+default_params = _lib.default_params
+
+
+@dataclass
+class TimestepTime:
+    """core/src/include/Time.hpp:265-268 (start and step, in seconds)."""
+
+    start: float
+    step: float
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a: np.ndarray) -> c_void_p:
+    return a.ctypes.data_as(c_void_p)
+
+
+class _KernelBase:
+    rheology = _lib.RHEOLOGY_MEVP
+
+    def __init__(self, dg_comp: int = 6, params: Params | None = None, **overrides):
+        self._l = _lib.load()
+        p = params if params is not None else _lib.default_params()
+        for k, v in overrides.items():
+            if not hasattr(p, k):
+                raise AttributeError(f"unknown parameter {k}")
+            setattr(p, k, v)
+        self.params = p
+        self.dg = dg_comp
+        h = c_void_p()
+        st = self._l.nsdg_kernel_create(self.rheology, dg_comp, byref(p), byref(h))
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, f"nsdg_kernel_create: {self._l.nsdg_status_string(st).decode()}")
+        self._h = h
+        self.nx = self.ny = 0
+
+    # -- error handling ------------------------------------------------------
+    def _check(self, st: int):
+        if st == _lib.NSDG_OK:
+            return
+        msg = self._l.nsdg_kernel_last_error(self._h).decode()
+        if st == _lib.NSDG_ERR_UNKNOWN_FIELD:
+            raise KeyError(msg)
+        raise NsdgError(st, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.nsdg_kernel_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- the reference interface ---------------------------------------------
+    @property
+    def nelements(self) -> int:
+        return self.nx * self.ny
+
+    def initialise(self, coords, isSpherical: bool, mask, nx: int | None = None, ny: int | None = None):
+        """coords: ((nx+1)*(ny+1), 2) vertices; mask: (nx*ny,) with 1.0 = ice.
+
+        The reference takes nx and ny from the ModelArray dimensions; here they
+        come from the mask shape (ny, nx) or the explicit arguments."""
+        mask = np.asarray(mask, dtype=np.float64)
+        if nx is None or ny is None:
+            if mask.ndim != 2:
+                raise ValueError("pass a (ny, nx) mask or explicit nx, ny")
+            ny, nx = mask.shape
+        coords = _f64(coords).reshape(-1, 2)
+        m = _f64(mask).reshape(-1)
+        self._check(self._l.nsdg_kernel_initialise(self._h, nx, ny, _ptr(coords), int(bool(isSpherical)), _ptr(m)))
+        self.nx, self.ny = nx, ny
+
+    def setData(self, name: str, data):
+        a = _f64(data)
+        n = self.nelements
+        ncomp = 1 if a.ndim == 1 else a.shape[-1]
+        if a.size != n * ncomp:
+            raise NsdgError(_lib.NSDG_ERR_SIZE_MISMATCH, f"setData: {name} has {a.size} values, mesh has {n} elements")
+        self._check(self._l.nsdg_kernel_set_data(self._h, name.encode(), _ptr(a), n, ncomp))
+
+    def getDG0Data(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.nelements)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self.nelements:
+            raise ValueError("out must be a contiguous float64 array with one value per element")
+        self._check(self._l.nsdg_kernel_get_dg0(self._h, name.encode(), _ptr(out), self.nelements))
+        return out
+
+    def getDGData(self, name: str, ncomp: int | None = None) -> np.ndarray:
+        nc = self.dg if ncomp is None else ncomp
+        out = np.empty((self.nelements, nc))
+        self._check(self._l.nsdg_kernel_get_dg(self._h, name.encode(), _ptr(out), self.nelements, nc))
+        return out if nc > 1 else out[:, 0]
+
+    def update(self, tst: TimestepTime | float, dt: float | None = None):
+        if isinstance(tst, TimestepTime):
+            start, step = tst.start, tst.step
+        else:
+            start, step = float(tst), float(dt)
+        self._check(self._l.nsdg_kernel_update(self._h, start, step))
+
+    # -- extras ----------------------------------------------------------------
+    def synchronize(self):
+        self._check(self._l.nsdg_kernel_synchronize(self._h))
+
+    def snapshot(self) -> bytes:
+        n = c_size_t()
+        self._check(self._l.nsdg_kernel_snapshot_size(self._h, byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        self._check(self._l.nsdg_kernel_snapshot_save(self._h, buf, n.value))
+        return buf.raw
+
+    def restore(self, blob: bytes):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        self._check(self._l.nsdg_kernel_snapshot_load(self._h, buf, len(blob)))
+
+    def meanValue(self, name: str) -> float:
+        out = c_double()
+        self._check(self._l.nsdg_kernel_mean_value(self._h, name.encode(), byref(out)))
+        return out.value
+
+    def time_updates(self, dt: float, steps: int) -> float:
+        ms = c_float()
+        self._check(self._l.nsdg_kernel_time_updates(self._h, dt, steps, byref(ms)))
+        return ms.value
+
+    def time_kernel(self, kernel_id: int, reps: int):
+        ms = c_float()
+        name = c_char_p()
+        self._check(self._l.nsdg_kernel_time_kernel(self._h, kernel_id, reps, byref(ms), byref(name)))
+        return ms.value, name.value.decode()
+
+    def launches_per_update(self) -> int:
+        n = c_int()
+        self._check(self._l.nsdg_kernel_launches_per_update(self._h, byref(n)))
+        return n.value
+
+
+class MEVPDynamicsKernel(_KernelBase):
+    """mEVP rheology (MEVPDynamicsKernel.hpp, VPCGDynamicsKernel.hpp)."""
+
+    rheology = _lib.RHEOLOGY_MEVP
+
+
+class BBMDynamicsKernel(_KernelBase):
+    """Brittle BBM rheology (BBMDynamicsKernel.hpp, BrittleCGDynamicsKernel.hpp)."""
+
+    rheology = _lib.RHEOLOGY_BBM
+
+
+class DGTransport:
+    """Stand-alone DG transport (DGTransport<DG>) on an explicitly described mesh.
+
+    vertices: ((nx+1)*(ny+1), 2); landmask: (nx*ny,) nonzero = ice or None;
+    dirichlet: four lists of element ids (bottom, right, top, left);
+    periodic: list of (type, cell1, cell2, edge) with type 0 for X-edges and 1
+    for Y-edges; scheme: "rk1", "rk2" or "rk3".
+    """
+
+    def __init__(self, dg, nx, ny, vertices, dirichlet, periodic=(), landmask=None, scheme="rk2"):
+        self._l = _lib.load()
+        self.dg, self.nx, self.ny = dg, nx, ny
+        v = _f64(vertices).reshape(-1, 2)
+        self._keep = [v]
+        lm = None
+        if landmask is not None:
+            lm = np.ascontiguousarray(landmask, dtype=np.uint8)
+            self._keep.append(lm)
+        arrs = [np.ascontiguousarray(np.asarray(d, dtype=np.uint64).reshape(-1)) for d in dirichlet]
+        self._keep += arrs
+        ptrs = (c_void_p * 4)(*[a.ctypes.data if a.size else None for a in arrs])
+        counts = (c_size_t * 4)(*[a.size for a in arrs])
+        per = np.ascontiguousarray(np.asarray(periodic, dtype=np.uint64).reshape(-1))
+        self._keep.append(per)
+        h = c_void_p()
+        sch = {"rk1": 1, "rk2": 2, "rk3": 3}[scheme]
+        st = self._l.nsdg_transport_create(dg, nx, ny, _ptr(v), _ptr(lm) if lm is not None else None,
+                                           ptrs, counts, _ptr(per) if per.size else None, per.size // 4,
+                                           sch, byref(h))
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, f"nsdg_transport_create: {self._l.nsdg_status_string(st).decode()}")
+        self._h = h
+
+    def _check(self, st):
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, self._l.nsdg_transport_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.nsdg_transport_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setVelocity(self, vx, vy):
+        a, b = _f64(vx), _f64(vy)
+        self._check(self._l.nsdg_transport_set_velocity(self._h, _ptr(a), _ptr(b)))
+
+    def reinitnormalvelocity(self):
+        self._check(self._l.nsdg_transport_reinit_normal_velocity(self._h))
+
+    def step(self, dt, phi, nsteps=1, limit_max=None, limit_min=None) -> np.ndarray:
+        a = _f64(phi).copy()
+        self._check(self._l.nsdg_transport_step(
+            self._h, dt, _ptr(a), nsteps, int(limit_max is not None), 0.0 if limit_max is None else limit_max,
+            int(limit_min is not None), 0.0 if limit_min is None else limit_min))
+        return a
+
+    def meanValue(self, phi) -> float:
+        a = _f64(phi)
+        out = c_double()
+        self._check(self._l.nsdg_transport_mean_value(self._h, _ptr(a), byref(out)))
+        return out.value

@@ -1,0 +1,74 @@
+"""The C-ABI library loads and exports every entry point of include/nsdg.h;
+host-side argument validation works without touching a GPU."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from nextsimdg_gb300 import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "nsdg.h"
+
+
+def header_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nsdg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    fns = header_functions()
+    for required in ("nsdg_kernel_create", "nsdg_kernel_initialise", "nsdg_kernel_set_data",
+                     "nsdg_kernel_get_dg0", "nsdg_kernel_get_dg", "nsdg_kernel_update",
+                     "nsdg_transport_step"):
+        assert required in fns
+
+
+def test_library_exports_every_header_symbol(nsdg_lib):
+    missing = [f for f in header_functions() if not hasattr(nsdg_lib, f)]
+    assert not missing, missing
+    declared = {name for name, _, _ in _lib.SIGNATURES}
+    assert set(header_functions()) == declared
+
+
+def test_version_and_status_strings(nsdg_lib):
+    assert b"sm_103a" in nsdg_lib.nsdg_version()
+    assert nsdg_lib.nsdg_status_string(_lib.NSDG_ERR_UNKNOWN_FIELD) == b"unknown field"
+
+
+def test_default_params_equal_oracle(nsdg_lib, oracle):
+    p = _lib.default_params()
+    q = oracle.default_params()
+    for name, _ in _lib.Params._fields_:
+        assert getattr(p, name) == getattr(q, name), name
+
+
+def test_create_validates_arguments(nsdg_lib):
+    h = ctypes.c_void_p()
+    p = _lib.default_params()
+    assert nsdg_lib.nsdg_kernel_create(7, 6, ctypes.byref(p), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
+    assert nsdg_lib.nsdg_kernel_create(0, 5, ctypes.byref(p), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
+    bad = _lib.default_params()
+    bad.n_steps = 0
+    assert nsdg_lib.nsdg_kernel_create(0, 6, ctypes.byref(bad), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
+    mixed = _lib.default_params()
+    mixed.precision = 7
+    assert nsdg_lib.nsdg_kernel_create(0, 6, ctypes.byref(mixed), ctypes.byref(h)) == _lib.NSDG_ERR_UNSUPPORTED
+    assert nsdg_lib.nsdg_kernel_create(0, 6, ctypes.byref(p), ctypes.byref(h)) == _lib.NSDG_OK
+    # calls before initialise fail cleanly, with a message
+    buf = (ctypes.c_double * 4)()
+    assert nsdg_lib.nsdg_kernel_set_data(h, b"hice", buf, 4, 1) == _lib.NSDG_ERR_BAD_ARG
+    assert b"not initialised" in nsdg_lib.nsdg_kernel_last_error(h)
+    assert nsdg_lib.nsdg_kernel_update(h, 0.0, 120.0) == _lib.NSDG_ERR_BAD_ARG
+    assert nsdg_lib.nsdg_kernel_destroy(h) == _lib.NSDG_OK
+
+
+def test_python_mirror_raises(nsdg_lib):
+    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel, NsdgError
+    with pytest.raises(NsdgError):
+        MEVPDynamicsKernel(dg_comp=4)
+    k = MEVPDynamicsKernel(dg_comp=6)
+    with pytest.raises(NsdgError):
+        k.update(0.0, 120.0)
+    k.close()

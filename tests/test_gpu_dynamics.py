@@ -1,0 +1,180 @@
+"""The GPU dynamics kernel (mEVP and BBM) against the CPU oracle, through the C ABI.
+
+Parity bar for the FP64 path: max |gpu - oracle| <= 1e-10 * max |oracle| for
+thickness, concentration, damage (all DG components), velocity and ice-ocean
+stress (DG0 read-out) after several full model steps of the box test.
+"""
+import numpy as np
+import pytest
+
+from nextsimdg_gb300.boxtest import BoxTest
+from nextsimdg_gb300.dynamics import BBMDynamicsKernel, MEVPDynamicsKernel, NsdgError
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _make(cls_or_oracle, box, dg, rheology, **params):
+    k = cls_or_oracle(dg_comp=dg, **params) if rheology is None else cls_or_oracle(rheology, dg, **params)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    return k
+
+
+def _advance(k, box, steps, start=0):
+    for s in range(start, start + steps):
+        uw, vw = box.wind(s * box.dt)
+        k.setData("uwind", uw)
+        k.setData("vwind", vw)
+        k.update(s * box.dt, box.dt)
+
+
+def _rel(a, b):
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / scale
+
+
+def _compare(g, o, names, dg):
+    worst = {}
+    for n in names:
+        if n in ("hice", "cice", "damage") and dg > 1:
+            a, b = g.getDGData(n), o.getDGData(n)
+        else:
+            a, b = g.getDG0Data(n), o.getDG0Data(n)
+        assert np.all(np.isfinite(a)), n
+        worst[n] = _rel(a, b)
+    return worst
+
+
+MEVP_CASES = [(12, 6, 3), (17, 3, 3), (16, 1, 2), (32, 6, 4)]
+
+
+@pytest.mark.parametrize("n,dg,steps", MEVP_CASES)
+def test_mevp_matches_oracle(gpu, oracle, n, dg, steps):
+    box = BoxTest(n, n + (1 if n == 17 else 0))
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, dg, None, **prm)
+    o = _make(oracle.OracleKernel, box, dg, 0, **prm)
+    _advance(g, box, steps)
+    _advance(o, box, steps)
+    worst = _compare(g, o, ["hice", "cice", "u", "v", "uiostress", "viostress"], dg)
+    assert all(v <= TOL for v in worst.values()), worst
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3  # the test moves the ice
+
+
+def test_mevp_land_holes_matches_oracle(gpu, oracle):
+    box = BoxTest(20, 15)
+    m = box.mask()
+    rng = np.random.default_rng(5)
+    for _ in range(12):
+        m[rng.integers(1, 14), rng.integers(1, 19)] = 0.0
+    box.mask = lambda m=m: m
+    prm = dict(alpha=1500.0, beta=1500.0, n_steps=60)
+    g = _make(MEVPDynamicsKernel, box, 6, None, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    _advance(g, box, 3)
+    _advance(o, box, 3)
+    worst = _compare(g, o, ["hice", "cice", "u", "v"], 6)
+    assert all(v <= TOL for v in worst.values()), worst
+
+
+def test_bbm_matches_oracle(gpu, oracle):
+    box = BoxTest(14)
+    prm = dict(n_steps=50)
+    g = _make(BBMDynamicsKernel, box, 6, None, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 1, **prm)
+    for k in (g, o):
+        k.setData("damage", box.damage())
+    _advance(g, box, 3)
+    _advance(o, box, 3)
+    worst = _compare(g, o, ["hice", "cice", "damage", "u", "v", "uiostress"], 6)
+    assert all(v <= TOL for v in worst.values()), worst
+
+
+def test_full_size_one_step_matches_oracle(gpu, oracle):
+    """256 x 256 DG2 box test (the benchmark configuration), two full steps."""
+    box = BoxTest(256)
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, 6, None, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    _advance(g, box, 2)
+    _advance(o, box, 2)
+    worst = _compare(g, o, ["hice", "cice", "u", "v"], 6)
+    assert all(v <= TOL for v in worst.values()), worst
+
+
+def test_bitwise_reproducible(gpu):
+    box = BoxTest(24)
+    outs = []
+    for _ in range(2):
+        g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=50)
+        _advance(g, box, 3)
+        outs.append(np.concatenate([g.getDG0Data("u"), g.getDGData("hice").ravel()]))
+        g.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("cls,extra", [(MEVPDynamicsKernel, {}), (BBMDynamicsKernel, {"damage": True})])
+def test_snapshot_resume_is_bitwise(gpu, cls, extra):
+    box = BoxTest(16)
+    a = _make(cls, box, 6, None, n_steps=30)
+    if extra:
+        a.setData("damage", box.damage())
+    _advance(a, box, 4)
+    ref = a.getDG0Data("u"), a.getDGData("hice")
+    b = _make(cls, box, 6, None, n_steps=30)
+    if extra:
+        b.setData("damage", box.damage())
+    _advance(b, box, 2)
+    blob = b.snapshot()
+    c = cls(dg_comp=6, n_steps=30)
+    c.initialise(box.coords(), False, box.mask())
+    c.restore(blob)
+    _advance(c, box, 2, start=2)
+    np.testing.assert_array_equal(c.getDG0Data("u"), ref[0])
+    np.testing.assert_array_equal(c.getDGData("hice"), ref[1])
+
+
+def test_mean_value_matches_oracle(gpu, oracle):
+    box = BoxTest(20)
+    g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=20)
+    o = _make(oracle.OracleKernel, box, 6, 0, n_steps=20)
+    _advance(g, box, 2)
+    _advance(o, box, 2)
+    assert g.meanValue("hice") == pytest.approx(o.meanValue("hice"), rel=1e-12)
+
+
+def test_errors_surface_and_gpu_stays_usable(gpu):
+    box = BoxTest(10)
+    g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=10)
+    with pytest.raises(KeyError):
+        g.getDG0Data("no_such_field")
+    with pytest.raises(NsdgError):
+        g.setData("hice", np.ones(7))
+    # a non-finite forcing is reported as a numeric fault, not a crash
+    bad = np.full(box.nelements, np.nan)
+    g.setData("uwind", bad)
+    g.update(0.0, box.dt)
+    with pytest.raises(NsdgError) as ei:
+        g.getDG0Data("u")
+    assert ei.value.status == 5
+    # the same handle is re-initialised and runs normally afterwards
+    g.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        g.setData(name, arr)
+    _advance(g, box, 1)
+    assert np.all(np.isfinite(g.getDG0Data("u")))
+    with pytest.raises(NsdgError):
+        g.initialise(box.coords(), True, box.mask())  # spherical: unsupported
+
+
+def test_other_fields_are_stored_not_advected(gpu):
+    box = BoxTest(8)
+    g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=5)
+    tracer = np.arange(box.nelements, dtype=float)
+    g.setData("tracer", tracer)
+    _advance(g, box, 1)
+    np.testing.assert_array_equal(g.getDG0Data("tracer"), tracer)
+    np.testing.assert_array_equal(g.getDGData("tracer", ncomp=1), tracer)
