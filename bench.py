@@ -360,6 +360,24 @@ def run_ours(args, world, rank, local):
     k.close()
 
 
+def run_profile(args):
+    """Setup plus warm-up and K device-resident steps, nothing else."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
+
+    box = BoxTest(NX)
+    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    for s in range(args.warmup + args.steps):
+        k.update(s * DT, DT)
+    k.synchronize()
+    print(json.dumps({"profile": True, "steps": args.steps, "warmup": args.warmup,
+                      "launches_per_step": k.launches_per_update()}))
+    k.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,10 +385,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the device-resident steps (for ncu captures): no e2e, no baselines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_ours(args, world, rank, local)
