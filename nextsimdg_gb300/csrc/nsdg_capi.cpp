@@ -230,7 +230,10 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     add(N + 1, 4); add(std::max<size_t>(flags.perEntry.size(), 1), 4);
     // ops
     add(ops.cellX.size()); add(ops.cellY.size()); add(ops.minv.size()); add(ops.jwA.size()); add(ops.jw3.size());
-    add(ops.gx.size()); add(ops.gy.size()); add(ops.w.size()); add(ops.d1.size()); add(ops.d2.size());
+    add(ops.gx.size()); add(ops.gy.size()); add(ops.a1.size()); add(ops.a2.size());
+    if (bbm) {
+        add(ops.w.size()); add(ops.d1.size()); add(ops.d2.size());
+    }
     add(ops.dxssh.size()); add(ops.dyssh.size()); add(Ncg); add(Ncg1);
     if (bbm) {
         add(ops.cellX8.size()); add(ops.cellY8.size()); add(ops.minv8.size()); add(ops.wdam.size()); add(ops.hsize.size());
@@ -290,9 +293,13 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     dops.jw3 = upd(ops.jw3);
     dops.gx = upd(ops.gx);
     dops.gy = upd(ops.gy);
-    dops.w = upd(ops.w);
-    dops.d1 = upd(ops.d1);
-    dops.d2 = upd(ops.d2);
+    dops.a1 = upd(ops.a1);
+    dops.a2 = upd(ops.a2);
+    if (bbm) {
+        dops.w = upd(ops.w);
+        dops.d1 = upd(ops.d1);
+        dops.d2 = upd(ops.d2);
+    }
     dops.dxssh = upd(ops.dxssh);
     dops.dyssh = upd(ops.dyssh);
     std::vector<double> invm(Ncg);
@@ -447,7 +454,7 @@ int nsdg_kernel::enqueueUpdate(double dt, int& launches)
         LCH(launchMevpPrepNodes(s, dm, st, mp));
         LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
         for (int it = 0; it < nS; ++it) {
-            LCH(launchMevpStress(s, dm, dops, u, v, Pg, s11, s12, s22, contrib, mp, derr));
+            LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
             LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
         }
     } else {
@@ -808,9 +815,15 @@ std::vector<std::pair<double*, size_t>> snapshotArrays(nsdg_kernel* k)
 {
     const size_t dN = size_t(k->dg) * k->N;
     std::vector<std::pair<double*, size_t>> a = { { k->hice, dN }, { k->cice, dN }, { k->ssh, k->N },
-        { k->s11, 8 * k->N }, { k->s12, 8 * k->N }, { k->s22, 8 * k->N }, { k->u, k->Ncg },
-        { k->v, k->Ncg }, { k->uo, k->Ncg }, { k->vo, k->Ncg }, { k->ua, k->Ncg }, { k->va, k->Ncg } };
-    if (k->rheology == NSDG_RHEOLOGY_BBM) {
+        { k->u, k->Ncg }, { k->v, k->Ncg }, { k->uo, k->Ncg }, { k->vo, k->Ncg }, { k->ua, k->Ncg },
+        { k->va, k->Ncg } };
+    if (k->rheology == NSDG_RHEOLOGY_MEVP) {
+        // the mEVP stress lives in divergence space (see kMevpStress)
+        a.push_back({ k->contrib, 18 * k->N });
+    } else {
+        a.push_back({ k->s11, 8 * k->N });
+        a.push_back({ k->s12, 8 * k->N });
+        a.push_back({ k->s22, 8 * k->N });
         a.push_back({ k->damage, dN });
         a.push_back({ k->avgU, k->Ncg });
         a.push_back({ k->avgV, k->Ncg });
@@ -971,8 +984,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 0:
             return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
                              k->s11, k->s12, k->s22, k->contrib, bp, k->derr)
-                       : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->s11, k->s12, k->s22,
-                             k->contrib, mp, k->derr);
+                       : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);

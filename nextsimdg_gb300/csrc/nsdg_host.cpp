@@ -406,6 +406,8 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
     ops.gx.assign(81 * N, 0.0);
     ops.gy.assign(81 * N, 0.0);
     ops.w.assign(72 * N, 0.0);
+    ops.a1.assign(81 * N, 0.0);
+    ops.a2.assign(81 * N, 0.0);
     ops.d1.assign(72 * N, 0.0);
     ops.d2.assign(72 * N, 0.0);
     ops.dxssh.assign(16 * N, 0.0);
@@ -489,12 +491,25 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
                     ops.gy[(q * 9 + j) * N + e] = s2;
                 }
             // iMJwPSI = M8^{-1} (psi_k(q) w_q J_q)   (8 x 9)
+            double W[8][9];
             for (int k = 0; k < 8; ++k)
                 for (int q = 0; q < 9; ++q) {
                     double s = 0;
                     for (int mm = 0; mm < 8; ++mm)
                         s += im8[k * 8 + mm] * (b.psi(mm, 3, q) * (b.weight(3, q) * g.J[q]));
+                    W[k][q] = s;
                     ops.w[(k * 9 + q) * N + e] = s;
+                }
+            // divergence of a Gauss-point stress increment: A = divS iMJwPSI (9 x 9)
+            for (int j = 0; j < 9; ++j)
+                for (int q = 0; q < 9; ++q) {
+                    double s1 = 0, s2 = 0;
+                    for (int k = 0; k < 8; ++k) {
+                        s1 += D1[j][k] * W[k][q];
+                        s2 += D2[j][k] * W[k][q];
+                    }
+                    ops.a1[(j * 9 + q) * N + e] = s1;
+                    ops.a2[(j * 9 + q) * N + e] = s2;
                 }
             if (stressTransport) {
                 cellTerms(g, 8, N, e, ops.cellX8, ops.cellY8);

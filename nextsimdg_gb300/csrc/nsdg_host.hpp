@@ -84,6 +84,7 @@ struct ElementOps {
     // momentum (CG2 / DG-stress 8)
     std::vector<double> gx, gy;                  // 81: strain at Gauss points from CG2 nodes
     std::vector<double> w;                       // 72: iMJwPSI[k][q]
+    std::vector<double> a1, a2;                  // 81: divS1 iMJwPSI, divS2 iMJwPSI [j][q]
     std::vector<double> d1, d2;                  // 72: divS1[j][k], divS2[j][k]
     std::vector<double> wdam;                    // dg*9: iMJwPSI_dam (BBM)
     std::vector<double> dxssh, dyssh;            // 16: dX_SSH[i][j], dY_SSH[i][j]

@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes(size_t n, MevpNodeState
 
 template <int DG>
 __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const double* __restrict__ h,
-    const double* __restrict__ a, double* __restrict__ Pg, double Pstar)
+    const double* __restrict__ a, double* __restrict__ Pg, double Pstar, double invAlpha)
 {
     const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (e >= N)
@@ -829,100 +829,100 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const doub
         }
         const double hq = fmax(hs, 0.0);
         const double aq = fmin(fmax(as, 0.0), 1.0);
-        Pg[q * N + e] = Pstar * hq * exp(-20.0 * (1.0 - aq));
+        Pg[q * N + e] = Pstar * hq * exp(-20.0 * (1.0 - aq)) * invAlpha;
     }
 }
 
-// One mEVP iteration, element part.  Per element: the strain at the 3x3 Gauss
-// points straight from the 9 CG2 velocity nodes (composite operator
-// G = psi^T M^{-1} divS^T), Delta, the relaxed stress update projected with
-// iMJwPSI, and the element's share of the stress divergence at its 9 nodes,
-// written to contrib[18][N] for the node kernel to gather.
-__global__ void __launch_bounds__(kBlock) kMevpStress(DevMesh m, DevOps o, const double* __restrict__ u,
-    const double* __restrict__ v, const double* __restrict__ Pg, double* __restrict__ s11,
-    double* __restrict__ s12, double* __restrict__ s22, double* __restrict__ contrib, MevpParams p,
-    int* __restrict__ err)
+// One mEVP iteration, element part, carried in divergence space.
+//
+// The reference updates the stress coefficients s (8 per component,
+// MEVPStressUpdateStep.hpp:301-337) and then forms the element's share of the
+// stress divergence at its 9 CG2 nodes, divS1 s11 + divS2 s12 and
+// divS1 s12 + divS2 s22 (CGDynamicsKernel.cpp:340-363).  In the mEVP solver s
+// is observed only through that divergence, and the update is linear in s:
+//   s' = (1 - 1/alpha) s + iMJwPSI f    =>   divS s' = (1 - 1/alpha) divS s + (divS iMJwPSI) f
+// so each element keeps its 18 divergence coefficients tdiv instead of the 24
+// stress coefficients and applies the 9 x 9 operators A = divS iMJwPSI,
+// precomputed in FP64 on the host.  This drops the separate projection and
+// divergence products (216 + 288 FMA) for 324 FMA on an FP64-issue-bound
+// kernel.  The strain at the Gauss points comes straight from the 9 velocity
+// nodes through G = psi^T iMgrad (9 x 9), so the strain coefficients are not
+// formed either.  Land cells keep tdiv = 0 (the reference's divergence skips
+// them).  Pg holds P/alpha at the 9 Gauss points.
+//
+// Thread layout: three threads per element (kStressParts), 64 elements per
+// block.  Phase 1: thread `part` computes the strain, Delta and the stress
+// increments at Gauss points 3*part .. 3*part+2 and leaves them in shared
+// memory.  Phase 2: the same thread updates the divergence coefficients of
+// nodes 3*part .. 3*part+2.  Same FP64 work as one thread per element, three
+// times the warps to hide the operator loads.
+constexpr int kStressElems = 64;
+constexpr int kStressParts = 3;
+
+__global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMesh m, DevOps o,
+    const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ Pg,
+    double* __restrict__ tdiv, MevpParams p)
 {
-    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    __shared__ double fs[3][9][kStressElems];
+    const int le = threadIdx.x % kStressElems;
+    const int part = threadIdx.x / kStressElems; // warp-uniform
     const size_t N = m.N;
-    if (e >= N)
-        return;
-    const bool ice = m.ice[e] != 0;
-    const size_t s2 = 2 * size_t(m.nx) + 1;
-    const size_t ix = e % m.nx, iy = e / m.nx;
-    const size_t base = 2 * s2 * iy + 2 * ix;
-    double ul[9], vl[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        const size_t nd = base + (j % 3) + (j / 3) * s2;
-        ul[j] = ice ? u[nd] : 0.0;
-        vl[j] = ice ? v[nd] : 0.0;
-    }
-    const double inva = 1.0 / p.alpha;
-    const double dmin2 = p.DeltaMin * p.DeltaMin;
-    double a11[8], a12[8], a22[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        a11[k] = a12[k] = a22[k] = 0.0;
-#pragma unroll 1
-    for (int q = 0; q < 9; ++q) {
-        double ex = 0.0, ey = 0.0, exv = 0.0, eyu = 0.0;
+    const size_t e = blockIdx.x * size_t(kStressElems) + le;
+    const bool active = e < N && m.ice[e];
+    if (active) {
+        const size_t s2 = 2 * size_t(m.nx) + 1;
+        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t base = 2 * s2 * iy + 2 * ix;
+        double ul[9], vl[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-            const double gxq = o.gx[(q * 9 + j) * N + e];
-            const double gyq = o.gy[(q * 9 + j) * N + e];
-            ex = fma(gxq, ul[j], ex);
-            ey = fma(gyq, vl[j], ey);
-            exv = fma(gxq, vl[j], exv);
-            eyu = fma(gyq, ul[j], eyu);
+            const size_t nd = base + (j % 3) + (j / 3) * s2;
+            ul[j] = u[nd];
+            vl[j] = v[nd];
         }
-        const double e11 = ex, e22 = ey, e12 = 0.5 * (exv + eyu);
-        const double d2 = dmin2 + 1.25 * (e11 * e11 + e22 * e22) + 1.50 * e11 * e22 + e12 * e12;
-        const double rdelta = rsqrt(d2);
-        const double P = Pg[q * N + e];
-        const double t = P * rdelta;
-        const double f11 = inva * (0.125 * t * (5.0 * e11 + 3.0 * e22) - 0.5 * P);
-        const double f12 = inva * (0.25 * t * e12);
-        const double f22 = inva * (0.125 * t * (5.0 * e22 + 3.0 * e11) - 0.5 * P);
+        const double dmin2 = p.DeltaMin * p.DeltaMin;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const double wk = o.w[(k * 9 + q) * N + e];
-            a11[k] = fma(wk, f11, a11[k]);
-            a12[k] = fma(wk, f12, a12[k]);
-            a22[k] = fma(wk, f22, a22[k]);
-        }
-    }
-    const double keep = 1.0 - inva;
-    double t11[8], t12[8], t22[8];
-    bool finite = true;
+        for (int qq = 0; qq < 3; ++qq) {
+            const int q = 3 * part + qq;
+            double ex = 0.0, ey = 0.0, exv = 0.0, eyu = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        t11[k] = s11[k * N + e] * keep + a11[k];
-        t12[k] = s12[k * N + e] * keep + a12[k];
-        t22[k] = s22[k * N + e] * keep + a22[k];
-        s11[k * N + e] = t11[k];
-        s12[k * N + e] = t12[k];
-        s22[k * N + e] = t22[k];
-        finite = finite && isfinite(t11[k]) && isfinite(t12[k]) && isfinite(t22[k]);
-    }
-    if (!finite)
-        atomicOr(err, DEV_ERR_NONFINITE_STRESS);
-    // stress divergence contributions: tx = divS1 s11 + divS2 s12,
-    // ty = divS1 s12 + divS2 s22 (CGDynamicsKernel.cpp:340-363)
-#pragma unroll 1
-    for (int j = 0; j < 9; ++j) {
-        double tx = 0.0, ty = 0.0;
-        if (ice) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const double d1 = o.d1[(j * 8 + k) * N + e];
-                const double d2v = o.d2[(j * 8 + k) * N + e];
-                tx = fma(d1, t11[k], fma(d2v, t12[k], tx));
-                ty = fma(d1, t12[k], fma(d2v, t22[k], ty));
+            for (int j = 0; j < 9; ++j) {
+                const double gxq = o.gx[(q * 9 + j) * N + e];
+                const double gyq = o.gy[(q * 9 + j) * N + e];
+                ex = fma(gxq, ul[j], ex);
+                ey = fma(gyq, vl[j], ey);
+                exv = fma(gxq, vl[j], exv);
+                eyu = fma(gyq, ul[j], eyu);
             }
+            // e11 = ex, e22 = ey, e12 = (exv + eyu) / 2
+            const double sxy = exv + eyu;
+            const double d2 = dmin2 + 1.25 * (ex * ex + ey * ey) + 1.50 * ex * ey + 0.25 * sxy * sxy;
+            const double Pa = Pg[q * N + e];
+            const double z8 = 0.125 * Pa * rsqrt(d2); // P / (8 alpha Delta)
+            const double hP = 0.5 * Pa;
+            fs[0][q][le] = fma(z8, fma(5.0, ex, 3.0 * ey), -hP);
+            fs[1][q][le] = z8 * sxy; // P / (4 alpha Delta) e12
+            fs[2][q][le] = fma(z8, fma(5.0, ey, 3.0 * ex), -hP);
         }
-        contrib[j * N + e] = tx;
-        contrib[(9 + j) * N + e] = ty;
+    }
+    __syncthreads();
+    if (!active)
+        return;
+    const double keep = 1.0 - 1.0 / p.alpha;
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) {
+        const int j = 3 * part + jj;
+        double ax = 0.0, ay = 0.0;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const double a1 = o.a1[(j * 9 + q) * N + e];
+            const double a2 = o.a2[(j * 9 + q) * N + e];
+            const double f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
+            ax = fma(a1, f11, fma(a2, f12, ax));
+            ay = fma(a1, f12, fma(a2, f22, ay));
+        }
+        tdiv[j * N + e] = fma(tdiv[j * N + e], keep, ax);
+        tdiv[(9 + j) * N + e] = fma(tdiv[(9 + j) * N + e], keep, ay);
     }
 }
 
@@ -1376,19 +1376,18 @@ cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, con
 {
     const unsigned g = blocksFor(m.N);
     switch (dg) {
-    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
-    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
-    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar); break;
+    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
+    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
+    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
-    const double* v, const double* Pg, double* s11, double* s12, double* s22, double* contrib,
-    const MevpParams& p, int* err)
+    const double* v, const double* Pg, double* tdiv, const MevpParams& p)
 {
-    kMevpStress<<<blocksFor(m.N), kBlock, 0, s>>>(m, o, u, v, Pg, s11, s12, s22, contrib, p, err);
+    kMevpStress<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
     return cudaGetLastError();
 }
 

@@ -45,6 +45,8 @@ struct DevOps {
     const double* gx = nullptr;
     const double* gy = nullptr;
     const double* w = nullptr;
+    const double* a1 = nullptr;
+    const double* a2 = nullptr;
     const double* d1 = nullptr;
     const double* d2 = nullptr;
     const double* wdam = nullptr;
@@ -129,11 +131,13 @@ cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNode
 // P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298).
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
     const double* a, double* Pg, const MevpParams& p);
-// Strain at the Gauss points, mEVP stress update and the per-element stress
-// divergence contributions (CGDynamicsKernel.cpp:300-398, MEVPStressUpdateStep.hpp).
+// One mEVP iteration, element part, carried in divergence space: the strain at
+// the Gauss points, Delta, and the relaxed update of the element's stress
+// divergence contributions tdiv[18][N] = (divS1 s11 + divS2 s12, divS1 s12 +
+// divS2 s22) at its 9 CG2 nodes (CGDynamicsKernel.cpp:300-398,
+// MEVPStressUpdateStep.hpp:251-339).  Pg holds P/alpha at the Gauss points.
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
-    const double* v, const double* Pg, double* s11, double* s12, double* s22, double* contrib,
-    const MevpParams& p, int* err);
+    const double* v, const double* Pg, double* tdiv, const MevpParams& p);
 // Node gather of the divergence, Dirichlet zero, implicit velocity update and
 // boundary zero (CGDynamicsKernel.cpp:365-444, VPCGDynamicsKernel.hpp:132-172).
 cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,

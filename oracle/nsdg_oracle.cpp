@@ -1982,6 +1982,16 @@ void oracle_transport_step(void* tp, double dt, double* phi, int nsteps, int lma
     }
     std::memcpy(phi, d.a.data(), d.a.size() * sizeof(double));
 }
+// LimitMax / LimitMin of a host field (dgLimit.hpp:16-85)
+void oracle_transport_limit(void* tp, double* phi, int lmax, double maxv, int lmin, double minv)
+{
+    OTransport* t = static_cast<OTransport*>(tp);
+    DG d(t->mesh.nelements, t->tr.dg);
+    std::memcpy(d.a.data(), phi, d.a.size() * sizeof(double));
+    if (lmax) LimitMax(d, maxv);
+    if (lmin) LimitMin(d, minv);
+    std::memcpy(phi, d.a.data(), d.a.size() * sizeof(double));
+}
 double oracle_transport_mean_value(void* tp, const double* phi)
 {
     OTransport* t = static_cast<OTransport*>(tp);

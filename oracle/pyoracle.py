@@ -81,6 +81,7 @@ def load() -> ctypes.CDLL:
             "oracle_transport_step": (None, [c_void_p, c_double, c_void_p, c_int, c_int, c_double, c_int,
                                              c_double]),
             "oracle_transport_mean_value": (c_double, [c_void_p, c_void_p]),
+            "oracle_transport_limit": (None, [c_void_p, c_void_p, c_int, c_double, c_int, c_double]),
             "oracle_transport_function2dg": (None, [c_void_p, c_int, c_double, c_void_p]),
             "oracle_transport_l2error": (c_double, [c_void_p, c_int, c_double, c_void_p]),
             "oracle_advection_golden": (c_double, [c_int, c_double, c_int, POINTER(c_double)]),
@@ -237,6 +238,13 @@ class OracleTransport:
     def meanValue(self, phi):
         a = _f64(phi)
         return self._l.oracle_transport_mean_value(self._h, _p(a))
+
+    def limit(self, phi, limit_max=None, limit_min=None):
+        a = _f64(phi).copy()
+        self._l.oracle_transport_limit(self._h, _p(a), int(limit_max is not None),
+                                       0.0 if limit_max is None else limit_max, int(limit_min is not None),
+                                       0.0 if limit_min is None else limit_min)
+        return a
 
     def function2dg(self, fn: int, param: float):
         out = np.empty((self.nx * self.ny, self.dg))

@@ -18,7 +18,7 @@ def _run_golden(oracle, dg, verts, dirichlet, periodic, nx, ny, fn_phi, fn_vx, f
     o = oracle.OracleTransport(dg, nx, ny, verts, dirichlet, periodic)
     phi = o.function2dg(fn_phi, param)
     if limit:  # LimitMax(phi, 1.0) after the initial projection
-        phi = o.step(0.0, phi, 0, limit_max=1.0)
+        phi = o.limit(phi, limit_max=1.0)
     vx, vy = o.function2dg(fn_vx, param), o.function2dg(fn_vy, param)
     t = DGTransport(dg, nx, ny, verts, dirichlet, periodic, scheme="rk2" if dg < 3 else "rk3")
     t.setVelocity(vx, vy)
