@@ -49,31 +49,30 @@ ALPHA = BETA = 300.0
 NSTEPS = 100
 
 
-def bytes_per_element_iteration_stress() -> int:
-    """Algorithmic DRAM bytes of one launch of the element stress kernel, per
-    element: operators Gx, Gy (2 x 81), iMJwPSI (72), divS1, divS2 (2 x 72)
-    FP64; P at the 9 Gauss points; the 24 stress coefficients read and
-    written; the 18 divergence contributions written; the CG2 velocity
-    gather counted once per node (about 4 nodes per element, u and v)."""
-    operators = (81 + 81 + 72 + 72 + 72) * 8
+def bytes_per_element_iteration_stress(word: int = 8) -> int:
+    """Algorithmic DRAM bytes of one launch of the element stress kernel
+    (kMevpStress), per element: the strain operators G_x, G_y and the
+    divergence operators A_1, A_2 (4 x 81 words), P/alpha at the 9 Gauss
+    points (FP64), the 18 divergence coefficients read and written, and the
+    CG2 velocity counted once per node (about 4 nodes per element, u and v)."""
+    operators = 4 * 81 * word
     pressure = 9 * 8
-    stress = 2 * 24 * 8
-    contrib = 18 * 8
-    velocity = 4 * 2 * 8
-    return operators + pressure + stress + contrib + velocity
+    tdiv = 2 * 18 * word
+    velocity = 4 * 2 * word
+    return operators + pressure + tdiv + velocity
 
 
 def flops_per_element_iteration_stress() -> int:
-    """FP64 flops of the element stress kernel per element (FMA = 2):
-    strain 4 x 9 x 9 FMA, Delta/P/viscosity ~16 per Gauss point, projection
-    3 x 8 x 9 FMA, relaxation 24 FMA, divergence 2 x 9 x 16 FMA."""
-    return 2 * (4 * 81) + 9 * 16 + 2 * (3 * 72) + 2 * 24 + 2 * (2 * 9 * 16)
+    """Flops of kMevpStress per element (FMA = 2): strain 4 x 81 FMA, Delta,
+    viscosity and stress increments ~12 per Gauss point, divergence update
+    4 x 81 FMA + 18."""
+    return 2 * (4 * 81) + 9 * 12 + 2 * (4 * 81) + 2 * 18
 
 
 def bytes_per_cell_update(n_iter: int = NSTEPS) -> float:
     """Algorithmic bytes per cell-update of the whole step (FP64 path):
     n_iter x (element kernel + node kernel share) + transport/prepare."""
-    node_per_element = 4 * (15 * 8) + 18 * 8  # ~4 nodes x 15 FP64 streams + gathered contributions
+    node_per_element = 4 * (15 * 8) + 18 * 8  # ~4 nodes x 15 FP64 streams + gathered divergence coefficients
     transport = 4 * (6 * 9 * 2 + 36 + 4 * 6 + 2 * 6) * 8  # cell terms, M^-1, phi, stage I/O
     prepare = 2 * 6 * 8 + 9 * 8 + 20 * 8 * 4
     return n_iter * (bytes_per_element_iteration_stress() + node_per_element) + transport + prepare
@@ -198,14 +197,14 @@ def fp64_peak_tflops(local: int):
 
 
 # --------------------------------------------------------------------------
-def cpu_baseline(sample_steps: int = 2, warm: int = 1):
+def cpu_baseline(nx: int = NX, sample_steps: int = 2, warm: int = 1):
     """The oracle (CPU restatement of the reference) on the host cores, all
     OpenMP threads, on a bounded sample of the same workload."""
     from oracle import pyoracle
     from nextsimdg_gb300.boxtest import BoxTest
 
     pyoracle.load()
-    box = BoxTest(NX)
+    box = BoxTest(nx)
     k = pyoracle.OracleKernel(0, DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
@@ -218,7 +217,7 @@ def cpu_baseline(sample_steps: int = 2, warm: int = 1):
     t = time.perf_counter() - t0
     v = box.nelements * sample_steps / t
     return {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
-            "sample": f"{sample_steps} model steps of the {NX}x{NX} DG2 box test after {warm} warm-up step(s), "
+            "sample": f"{sample_steps} model steps of the {nx}x{nx} DG2 box test after {warm} warm-up step(s), "
                       f"{t:.1f} s"}
 
 
@@ -229,7 +228,7 @@ def run_reference(args, world, rank):
     from nextsimdg_gb300.boxtest import BoxTest
 
     pyoracle.load()
-    box = BoxTest(NX)
+    box = BoxTest(args.nx)
     k = pyoracle.OracleKernel(0, DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
@@ -246,9 +245,10 @@ def run_reference(args, world, rank):
     v = box.nelements * args.steps / t
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic box test",
-            "config": {"workload": f"box test {NX}x{NX}, DG2 transport, CG2 velocity, mEVP {NSTEPS} iterations, "
-                                   f"alpha=beta={ALPHA:g}, dt={DT:g} s", "precision": "fp64"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic box test",
+            "config": {"workload": f"box test {args.nx}x{args.nx}, DG2 transport, CG2 velocity, mEVP {NSTEPS} "
+                                   f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s", "precision": args.precision},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
                              "sample": f"{args.steps} full model steps after {args.warmup} warm-up"},
@@ -262,8 +262,9 @@ def run_ours(args, world, rank, local):
 
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES", str(local))
-    box = BoxTest(NX)
-    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    prec = 1 if args.precision == "mixed" else 0
+    box = BoxTest(args.nx)
+    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=prec)
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
         k.setData(name, arr)
@@ -318,29 +319,49 @@ def run_ours(args, world, rank, local):
     # ---- roofline of the dominant kernel (element stress kernel) ----
     kms, kname = k.time_kernel(0, 50)
     nms, nname = k.time_kernel(1, 50)
-    bpe = bytes_per_element_iteration_stress()
+    bpe = bytes_per_element_iteration_stress(4 if prec else 8)
     achieved_gbs = N * bpe / (kms * 1e-3) / 1e9
     hbm, hbm_kind = measured_peaks()
     fp64_tf, fp64_kind = fp64_peak_tflops(local)
     fp64_achieved = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
     share = (kms * NSTEPS) / (ms_max / args.steps)
     traffic = None
-    prof = ROOT / "profiles" / "kMevpStress_traffic.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("bytes_per_launch_256")
-        except ValueError:
-            traffic = None
+    prof = ROOT / "profiles" / "kMevpStress_box256_fp64.md"
+    if prof.exists() and args.nx == 256 and prec == 0:
+        for line in prof.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch_256:"):
+                traffic = int(line.split(":")[1])
+
+    k.close()
+    variants = {}
+    if not args.no_variants and prec == 0:
+        # the mixed-precision path on the same grid, device-resident
+        km = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=1)
+        km.initialise(box.coords(), False, box.mask())
+        for name, arr in box.initial_fields().items():
+            km.setData(name, arr)
+        km.time_updates(DT, 3)
+        mms = km.time_updates(DT, args.steps)
+        km.synchronize()
+        sms, _ = km.time_kernel(0, 50)
+        nms2, _ = km.time_kernel(1, 50)
+        mval = N * args.steps / (mms * 1e-3)
+        variants["mixed_fp32"] = {"value": mval, "unit": UNIT, "ms_per_step": mms / args.steps,
+                                  "speedup_vs_fp64": mval / (N * args.steps / (ms_max * 1e-3)),
+                                  "kMevpStress32_ms": sms, "kMevpMomentum32_ms": nms2,
+                                  "stress_GBps": N * bytes_per_element_iteration_stress(4) / (sms * 1e-3) / 1e9}
+        km.close()
 
     if rank == 0:
-        base = cpu_baseline() if world == 1 and not args.no_cpu_baseline else None
+        base = cpu_baseline(args.nx) if world == 1 and not args.no_cpu_baseline else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic box test",
-            "config": {"workload": f"box test {NX}x{NX}, DG2 transport, CG2 velocity, mEVP {NSTEPS} iterations, "
-                                   f"alpha=beta={ALPHA:g}, dt={DT:g} s",
-                       "precision": "fp64", "parallelism": "replicas" if world > 1 else "single",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == 0 else "f32+f64",
+            "data": "synthetic box test",
+            "config": {"workload": f"box test {args.nx}x{args.nx}, DG2 transport, CG2 velocity, mEVP {NSTEPS} "
+                                   f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s",
+                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (operators ~240 MB per step sweep), no flush",
                        "bytes_per_cell_update": bytes_per_cell_update()},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8},
@@ -356,8 +377,9 @@ def run_ours(args, world, rank, local):
         }
         if base:
             line["cpu_baseline"] = base
+        if variants:
+            line["variants"] = variants
         print(json.dumps(line), flush=True)
-    k.close()
 
 
 def run_profile(args):
@@ -365,8 +387,9 @@ def run_profile(args):
     from nextsimdg_gb300.boxtest import BoxTest
     from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
 
-    box = BoxTest(NX)
-    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS)
+    box = BoxTest(args.nx)
+    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS,
+                           precision=1 if args.precision == "mixed" else 0)
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
         k.setData(name, arr)
@@ -385,6 +408,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="fp64: every operation FP64 (the reference's arithmetic); mixed: FP32 bulk")
+    ap.add_argument("--nx", type=int, default=NX, help="box side in cells (256 is the benchmark grid)")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident steps (for ncu captures): no e2e, no baselines")
     args = ap.parse_args()

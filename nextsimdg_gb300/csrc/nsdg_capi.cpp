@@ -109,6 +109,11 @@ struct nsdg_kernel {
     double *velx8 = nullptr, *vely8 = nullptr, *nvX8 = nullptr, *nvY8 = nullptr;
     double *sA = nullptr, *sK1 = nullptr;  // 3 x 8 x N
     double *sshScratch = nullptr, *staging = nullptr, *dgTmp = nullptr, *cgTmp = nullptr;
+    // mixed precision (NSDG_PRECISION_MIXED)
+    DevOps32 dops32;
+    float* tdiv32 = nullptr;
+    MevpNodeState32 st32 {};
+    bool mixed() const { return P.precision == NSDG_PRECISION_MIXED; }
     double *partials = nullptr, *dsum = nullptr;
     int* derr = nullptr;
     // graph of one update
@@ -249,6 +254,11 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(8 * N); add(8 * N); add(3 * nXe); add(3 * nYe); add(24 * N); add(24 * N);
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
+    if (P.precision == NSDG_PRECISION_MIXED) {
+        for (int i = 0; i < 4; ++i) add(81 * N, 4);
+        add(18 * N, 4);
+        for (int i = 0; i < 14; ++i) add(Ncg, 4);
+    }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
 
@@ -357,6 +367,30 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     cgTmp = z(Ncg);
     partials = z((N + 255) / 256 + 1);
     dsum = z(1);
+    if (mixed()) {
+        auto upf = [&](const std::vector<double>& src) {
+            std::vector<float> tmp(src.begin(), src.end());
+            float* p = arena.take<float>(tmp.size());
+            if (!p) { e = cudaErrorMemoryAllocation; return p; }
+            if (e == cudaSuccess) e = cudaMemcpy(p, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice);
+            return p;
+        };
+        dops32.gx = upf(ops.gx);
+        dops32.gy = upf(ops.gy);
+        dops32.a1 = upf(ops.a1);
+        dops32.a2 = upf(ops.a2);
+        auto zf = [&](size_t n) {
+            float* p = arena.take<float>(n);
+            if (!p) { e = cudaErrorMemoryAllocation; return p; }
+            if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, n * sizeof(float), stream);
+            return p;
+        };
+        tdiv32 = zf(18 * N);
+        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.A, &st32.uo, &st32.vo, &st32.c1,
+            &st32.c1b, &st32.fau, &st32.fav, &st32.rhfc, &st32.gu, &st32.gv };
+        for (float** q : f32)
+            *q = zf(Ncg);
+    }
     derr = arena.take<int>(1);
     if (!derr)
         e = cudaErrorMemoryAllocation;
@@ -453,9 +487,18 @@ int nsdg_kernel::enqueueUpdate(double dt, int& launches)
         MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
         LCH(launchMevpPrepNodes(s, dm, st, mp));
         LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
-        for (int it = 0; it < nS; ++it) {
-            LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
-            LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
+        if (!mixed()) {
+            for (int it = 0; it < nS; ++it) {
+                LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
+                LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
+            }
+        } else {
+            LCH(launchMevpPrepNodes32(s, dm, st, st32));
+            for (int it = 0; it < nS; ++it) {
+                LCH(launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp));
+                LCH(launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, derr));
+            }
+            LCH(launchWidenVelocity(s, Ncg, st32.u, st32.v, u, v));
         }
     } else {
         const double rad = 0x1.1df46a2529d39p-6;
@@ -582,7 +625,9 @@ int nsdg_kernel_create(int rheology, int dg_comp, const nsdg_params* params, nsd
         nsdg_default_params(&p);
     if (p.n_steps < 1 || !(p.alpha > 0) || !(p.beta >= 0) || !(p.rho_ice > 0))
         return NSDG_ERR_BAD_ARG;
-    if (p.precision != NSDG_PRECISION_FP64)
+    if (p.precision != NSDG_PRECISION_FP64 && p.precision != NSDG_PRECISION_MIXED)
+        return NSDG_ERR_UNSUPPORTED;
+    if (p.precision == NSDG_PRECISION_MIXED && rheology != NSDG_RHEOLOGY_MEVP)
         return NSDG_ERR_UNSUPPORTED;
     try {
         nsdg_kernel* k = new nsdg_kernel();
@@ -811,22 +856,26 @@ struct SnapHeader {
     int version, rheology, dg, pad;
     unsigned long long N, Ncg, step;
 };
-std::vector<std::pair<double*, size_t>> snapshotArrays(nsdg_kernel* k)
+// (device pointer, bytes) of every array that carries state across steps
+std::vector<std::pair<void*, size_t>> snapshotArrays(nsdg_kernel* k)
 {
-    const size_t dN = size_t(k->dg) * k->N;
-    std::vector<std::pair<double*, size_t>> a = { { k->hice, dN }, { k->cice, dN }, { k->ssh, k->N },
-        { k->u, k->Ncg }, { k->v, k->Ncg }, { k->uo, k->Ncg }, { k->vo, k->Ncg }, { k->ua, k->Ncg },
-        { k->va, k->Ncg } };
+    const size_t dN = size_t(k->dg) * k->N * sizeof(double);
+    const size_t cg = k->Ncg * sizeof(double);
+    std::vector<std::pair<void*, size_t>> a = { { k->hice, dN }, { k->cice, dN }, { k->ssh, k->N * sizeof(double) },
+        { k->u, cg }, { k->v, cg }, { k->uo, cg }, { k->vo, cg }, { k->ua, cg }, { k->va, cg } };
     if (k->rheology == NSDG_RHEOLOGY_MEVP) {
         // the mEVP stress lives in divergence space (see kMevpStress)
-        a.push_back({ k->contrib, 18 * k->N });
+        if (k->mixed())
+            a.push_back({ k->tdiv32, 18 * k->N * sizeof(float) });
+        else
+            a.push_back({ k->contrib, 18 * k->N * sizeof(double) });
     } else {
-        a.push_back({ k->s11, 8 * k->N });
-        a.push_back({ k->s12, 8 * k->N });
-        a.push_back({ k->s22, 8 * k->N });
+        a.push_back({ k->s11, 8 * k->N * sizeof(double) });
+        a.push_back({ k->s12, 8 * k->N * sizeof(double) });
+        a.push_back({ k->s22, 8 * k->N * sizeof(double) });
         a.push_back({ k->damage, dN });
-        a.push_back({ k->avgU, k->Ncg });
-        a.push_back({ k->avgV, k->Ncg });
+        a.push_back({ k->avgU, cg });
+        a.push_back({ k->avgV, cg });
     }
     return a;
 }
@@ -840,7 +889,7 @@ int nsdg_kernel_snapshot_size(nsdg_kernel* k, size_t* bytes)
         return k->fail(NSDG_ERR_BAD_ARG, "snapshot: kernel not initialised");
     size_t b = sizeof(SnapHeader);
     for (auto& p : snapshotArrays(k))
-        b += p.second * sizeof(double);
+        b += p.second;
     *bytes = b;
     return k->ok();
 }
@@ -858,16 +907,17 @@ int nsdg_kernel_snapshot_save(nsdg_kernel* k, void* buffer, size_t bytes)
     h.version = 1;
     h.rheology = k->rheology;
     h.dg = k->dg;
+    h.pad = k->P.precision;
     h.N = k->N;
     h.Ncg = k->Ncg;
     h.step = k->stepNumber;
     std::memcpy(buffer, &h, sizeof(h));
     char* p = static_cast<char*>(buffer) + sizeof(h);
     for (auto& a : snapshotArrays(k)) {
-        const cudaError_t e = cudaMemcpyAsync(p, a.first, a.second * sizeof(double), cudaMemcpyDeviceToHost, k->stream);
+        const cudaError_t e = cudaMemcpyAsync(p, a.first, a.second, cudaMemcpyDeviceToHost, k->stream);
         if (e != cudaSuccess)
             return k->fail(NSDG_ERR_CUDA, std::string("snapshot_save: ") + cudaGetErrorString(e));
-        p += a.second * sizeof(double);
+        p += a.second;
     }
     r = k->checkDeviceError();
     return r ? r : k->ok();
@@ -884,14 +934,14 @@ int nsdg_kernel_snapshot_load(nsdg_kernel* k, const void* buffer, size_t bytes)
     SnapHeader h;
     std::memcpy(&h, buffer, sizeof(h));
     if (std::memcmp(h.magic, "NSDGSNP", 8) != 0 || h.version != 1 || h.rheology != k->rheology
-        || h.dg != k->dg || h.N != k->N || h.Ncg != k->Ncg)
+        || h.dg != k->dg || h.pad != k->P.precision || h.N != k->N || h.Ncg != k->Ncg)
         return k->fail(NSDG_ERR_SIZE_MISMATCH, "snapshot_load: snapshot does not match this kernel");
     const char* p = static_cast<const char*>(buffer) + sizeof(h);
     for (auto& a : snapshotArrays(k)) {
-        const cudaError_t e = cudaMemcpyAsync(a.first, p, a.second * sizeof(double), cudaMemcpyHostToDevice, k->stream);
+        const cudaError_t e = cudaMemcpyAsync(a.first, p, a.second, cudaMemcpyHostToDevice, k->stream);
         if (e != cudaSuccess)
             return k->fail(NSDG_ERR_CUDA, std::string("snapshot_load: ") + cudaGetErrorString(e));
-        p += a.second * sizeof(double);
+        p += a.second;
     }
     const cudaError_t e = cudaStreamSynchronize(k->stream);
     if (e != cudaSuccess)
@@ -982,10 +1032,14 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
     auto launch = [&]() -> cudaError_t {
         switch (kernel_id) {
         case 0:
+            if (!bbm && k->mixed())
+                return launchMevpStress32(k->stream, k->dm, k->dops32, k->st32.u, k->st32.v, k->Pg, k->tdiv32, mp);
             return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
                              k->s11, k->s12, k->s22, k->contrib, bp, k->derr)
                        : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
+            if (!bbm && k->mixed())
+                return launchMevpMomentum32(k->stream, k->dm, k->dops, k->st32, k->tdiv32, mp, k->derr);
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
         default:
@@ -994,8 +1048,8 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         }
     };
     if (name)
-        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : "kMevpStress")
-            : kernel_id == 1 ? (bbm ? "kBbmMomentum" : "kMevpMomentum")
+        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : (k->mixed() ? "kMevpStress32" : "kMevpStress"))
+            : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
                              : "kTransportStage";
     if (kernel_id < 0 || kernel_id > 2)
         return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel_id must be 0, 1 or 2");

@@ -991,6 +991,167 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
 }
 
 // ===========================================================================
+// mEVP, mixed precision
+// ===========================================================================
+__global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const float u = static_cast<float>(st.u[i]), v = static_cast<float>(st.v[i]);
+    f.u[i] = u;
+    f.v[i] = v;
+    f.u0[i] = u;
+    f.v0[i] = v;
+    f.A[i] = static_cast<float>(st.cgA[i]);
+    f.uo[i] = static_cast<float>(st.uo[i]);
+    f.vo[i] = static_cast<float>(st.vo[i]);
+    f.c1[i] = static_cast<float>(st.c1[i]);
+    f.c1b[i] = static_cast<float>(st.c1b[i]);
+    f.fau[i] = static_cast<float>(st.fau[i]);
+    f.fav[i] = static_cast<float>(st.fav[i]);
+    f.rhfc[i] = static_cast<float>(st.rhfc[i]);
+    f.gu[i] = static_cast<float>(st.gu[i]);
+    f.gv[i] = static_cast<float>(st.gv[i]);
+}
+
+// The FP64 kernel kMevpStress with FP32 operators and state.  The strain
+// invariant 1.25(e11^2+e22^2) + 1.5 e11 e22 + e12^2 is formed in FP32 from the
+// FP32 strain (it is a positive-definite quadratic form: no cancellation);
+// Delta = sqrt(invariant + DeltaMin^2) and the viscosity P/(8 alpha Delta) are
+// evaluated in FP64; the stress increments and the divergence update are FP32.
+__global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(DevMesh m, DevOps32 o,
+    const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
+    float* __restrict__ tdiv, MevpParams p)
+{
+    __shared__ float fs[3][9][kStressElems];
+    const int le = threadIdx.x % kStressElems;
+    const int part = threadIdx.x / kStressElems;
+    const size_t N = m.N;
+    const size_t e = blockIdx.x * size_t(kStressElems) + le;
+    const bool active = e < N && m.ice[e];
+    if (active) {
+        const size_t s2 = 2 * size_t(m.nx) + 1;
+        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t base = 2 * s2 * iy + 2 * ix;
+        float ul[9], vl[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const size_t nd = base + (j % 3) + (j / 3) * s2;
+            ul[j] = u[nd];
+            vl[j] = v[nd];
+        }
+        const double dmin2 = p.DeltaMin * p.DeltaMin;
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+            const int q = 3 * part + qq;
+            float ex = 0.f, ey = 0.f, exv = 0.f, eyu = 0.f;
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const float gxq = o.gx[(q * 9 + j) * N + e];
+                const float gyq = o.gy[(q * 9 + j) * N + e];
+                ex = fmaf(gxq, ul[j], ex);
+                ey = fmaf(gyq, vl[j], ey);
+                exv = fmaf(gxq, vl[j], exv);
+                eyu = fmaf(gyq, ul[j], eyu);
+            }
+            const float sxy = exv + eyu;
+            const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
+            const double Pa = Pg[q * N + e];
+            const float z8 = static_cast<float>(0.125 * Pa * rsqrt(static_cast<double>(inv) + dmin2));
+            const float hP = static_cast<float>(0.5 * Pa);
+            fs[0][q][le] = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP);
+            fs[1][q][le] = z8 * sxy;
+            fs[2][q][le] = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP);
+        }
+    }
+    __syncthreads();
+    if (!active)
+        return;
+    const float keep = static_cast<float>(1.0 - 1.0 / p.alpha);
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) {
+        const int j = 3 * part + jj;
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float a1 = o.a1[(j * 9 + q) * N + e];
+            const float a2 = o.a2[(j * 9 + q) * N + e];
+            const float f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
+            ax = fmaf(a1, f11, fmaf(a2, f12, ax));
+            ay = fmaf(a1, f12, fmaf(a2, f22, ay));
+        }
+        tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
+        tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, MevpNodeState32 st,
+    const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    const bool dir = m.cg2Dir[i] != 0;
+    float dSx = 0.f, dSy = 0.f;
+    if (!dir) {
+        int cxs[2], lxs[2], cys[2], lys[2];
+        const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
+        const int nyc = nodeCandidates(j2, m.ny, cys, lys);
+        int order[2] = { 0, 1 };
+        if (nyc == 2 && (cys[0] % 2) == 1) {
+            order[0] = 1;
+            order[1] = 0;
+        }
+        const size_t N = m.N;
+        for (int r = 0; r < nyc; ++r) {
+            const int cy = cys[order[r]], ly = lys[order[r]];
+            for (int k = 0; k < nxc; ++k) {
+                const size_t c = size_t(cy) * m.nx + cxs[k];
+                const int j = lxs[k] + 3 * ly;
+                dSx -= tdiv[j * N + c];
+                dSy -= tdiv[(9 + j) * N + c];
+            }
+        }
+    }
+    // divided by the lumped mass in FP64
+    const double invm = o.invm2[i];
+    const float mx = static_cast<float>(static_cast<double>(dSx) * invm);
+    const float my = static_cast<float>(static_cast<double>(dSy) * invm);
+    const float u = st.u[i], v = st.v[i];
+    const float uo = st.uo[i], vo = st.vo[i];
+    const float uOcnRel = uo - u, vOcnRel = v - vo;
+    const float absocn = sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
+    const float A = st.A[i];
+    const float Fo = static_cast<float>(p.F_ocean), beta = static_cast<float>(p.beta);
+    const float focn = Fo * absocn;
+    const float rden = 1.0f / (st.c1b[i] + A * focn);
+    const float c1 = st.c1[i];
+    float un = rden * (c1 * (beta * u + st.u0[i]) + A * (st.fau[i] + focn * uo) - st.rhfc[i] * u - st.gu[i] + mx);
+    float vn = rden * (c1 * (beta * v + st.v0[i]) + A * (st.fav[i] + focn * vo) + st.rhfc[i] * v - st.gv[i] + my);
+    if (!isfinite(un) || !isfinite(vn))
+        atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
+    if (dir) {
+        un = 0.f;
+        vn = 0.f;
+    }
+    st.u[i] = un;
+    st.v[i] = vn;
+}
+
+__global__ void kWidenVelocity(size_t n, const float* __restrict__ u32, const float* __restrict__ v32,
+    double* __restrict__ u, double* __restrict__ v)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    u[i] = u32[i];
+    v[i] = v32[i];
+}
+
+// ===========================================================================
 // BBM (BBMStressUpdateStep.hpp:31-195, BrittleCGDynamicsKernel.hpp:206-254)
 // ===========================================================================
 __global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState st)
@@ -1395,6 +1556,30 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
     const double* contrib, const MevpParams& p, int* err)
 {
     kMevpMomentum<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
+    const MevpNodeState32& st32)
+{
+    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32);
+    return cudaGetLastError();
+}
+cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
+    const float* v, const double* Pg, float* tdiv, const MevpParams& p)
+{
+    kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
+    return cudaGetLastError();
+}
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o, const MevpNodeState32& st,
+    const float* tdiv, const MevpParams& p, int* err)
+{
+    kMevpMomentum32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, tdiv, p, err);
+    return cudaGetLastError();
+}
+cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, const float* v32, double* u, double* v)
+{
+    kWidenVelocity<<<blocksFor(n), kBlock, 0, s>>>(n, u32, v32, u, v);
     return cudaGetLastError();
 }
 

@@ -143,6 +143,43 @@ cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, 
 cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
     const MevpNodeState& st, const double* contrib, const MevpParams& p, int* err);
 
+// --- mEVP, mixed precision (NSDG_PRECISION_MIXED) ----------------------
+// FP32 operators, velocities, divergence coefficients and momentum
+// arithmetic; FP64 for Delta = sqrt(strain invariant + DeltaMin^2), the
+// viscosity P/(2 Delta), and the lumped-mass inverse.
+struct DevOps32 {
+    const float* gx = nullptr;
+    const float* gy = nullptr;
+    const float* a1 = nullptr;
+    const float* a2 = nullptr;
+};
+struct MevpNodeState32 {
+    float* u;
+    float* v;
+    float* u0;
+    float* v0;
+    float* A;
+    float* uo;
+    float* vo;
+    float* c1;
+    float* c1b;
+    float* fau;
+    float* fav;
+    float* rhfc;
+    float* gu;
+    float* gv;
+};
+// after launchMevpPrepNodes: FP32 copies of the per-step node constants
+cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
+    const MevpNodeState32& st32);
+cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
+    const float* v, const double* Pg, float* tdiv, const MevpParams& p);
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o,
+    const MevpNodeState32& st, const float* tdiv, const MevpParams& p, int* err);
+// u, v (FP64) from the FP32 iterate at the end of the sub-cycle
+cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, const float* v32, double* u,
+    double* v);
+
 // Ice-ocean stress on CG2 nodes (VPCGDynamicsKernel.hpp:96-120 / BrittleCGDynamicsKernel.hpp:168-192).
 cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const double* u,
     const double* v, const double* uo, const double* vo, double F_ocean, double cosA, double sinA,

@@ -201,3 +201,36 @@ def test_other_fields_are_stored_not_advected(gpu):
     _advance(g, box, 1)
     np.testing.assert_array_equal(g.getDG0Data("tracer"), tracer)
     np.testing.assert_array_equal(g.getDGData("tracer", ncomp=1), tracer)
+
+
+@pytest.mark.parametrize("n,steps", [(32, 5), (64, 3)])
+def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
+    """FP32 bulk with FP64 Delta/viscosity, lumped-mass inverse and
+    conservation sums: RMS error against the FP64 oracle, stated bars."""
+    box = BoxTest(n)
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    _advance(g, box, steps)
+    _advance(o, box, steps)
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
+    du = rms(g.getDG0Data("u"), o.getDG0Data("u"))
+    dv = rms(g.getDG0Data("v"), o.getDG0Data("v"))
+    dh = rms(g.getDG0Data("hice"), o.getDG0Data("hice"))
+    da = rms(g.getDG0Data("cice"), o.getDG0Data("cice"))
+    assert max(du, dv) <= 1e-5, (du, dv)       # m/s
+    assert dh <= 1e-6 and da <= 1e-6, (dh, da)  # m, fraction
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
+
+
+def test_mixed_precision_snapshot_and_reproducible(gpu):
+    box = BoxTest(16)
+    a = _make(MEVPDynamicsKernel, box, 6, None, precision=1, n_steps=30)
+    _advance(a, box, 2)
+    blob = a.snapshot()
+    _advance(a, box, 2, start=2)
+    b = MEVPDynamicsKernel(dg_comp=6, precision=1, n_steps=30)
+    b.initialise(box.coords(), False, box.mask())
+    b.restore(blob)
+    _advance(b, box, 2, start=2)
+    np.testing.assert_array_equal(a.getDG0Data("u"), b.getDG0Data("u"))
