@@ -188,6 +188,26 @@ int nsdg_transport_step(nsdg_transport* t, double dt, double* phi, int nsteps,
 /* Tools::MeanValue of a host DG field (computed on the GPU, FP64). */
 int nsdg_transport_mean_value(nsdg_transport* t, const double* phi, double* out);
 
+/* ======================================================================== */
+/* Allocation-free entry point                                               */
+/* ======================================================================== */
+/* No counterpart in the reference.  Tools::MeanValue (the FP64 mesh integral
+ * of a DG field) for callers that cannot allocate device memory: a host model
+ * whose pool allocator owns the GPU memory, or a time-critical loop that may
+ * not pay cudaMalloc's implicit synchronisation.  phi: device array
+ * double[dg][n_elements] (component-major); jw: device array
+ * double[9][n_elements], Jacobian times Gauss weight at the 3x3 Gauss points;
+ * out: one device double; stream: a cudaStream_t (NULL = legacy default).
+ * The reduction's scratch is a fixed array inside the library, held on every
+ * GPU that loads it until the process exits; n_elements above
+ * NSDG_NOALLOC_MAX_ELEMENTS returns NSDG_ERR_SIZE_MISMATCH.  The first call on
+ * a device looks up that array's address with the device current (make it
+ * before any stream capture that would record a later call).  Calls share the
+ * array: calls that overlap on the GPU race.  Nothing is allocated. */
+#define NSDG_NOALLOC_MAX_ELEMENTS (1u << 24)
+int nsdg_mean_value_noalloc(int dg, size_t n_elements, const double* phi, const double* jw,
+    double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

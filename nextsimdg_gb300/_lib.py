@@ -78,6 +78,7 @@ SIGNATURES = [
     ("nsdg_transport_reinit_normal_velocity", c_int, [c_void_p]),
     ("nsdg_transport_step", c_int, [c_void_p, c_double, c_void_p, c_int, c_int, c_double, c_int, c_double]),
     ("nsdg_transport_mean_value", c_int, [c_void_p, c_void_p, POINTER(c_double)]),
+    ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 
 _lib = None
