@@ -382,6 +382,64 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def ensemble_boxes(n_members: int, seed: int = 2024):
+    """32-member ensemble of the box test: square sides drawn uniformly from
+    {64, 128, 192, 256, 384}; cyclone start perturbed by up to +-50 km and
+    speed 8-12 m/s; seeded Gaussian noise on h with sigma 0.02 m."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    rng = np.random.default_rng(seed)
+    sides = rng.choice([64, 128, 192, 256, 384], size=n_members)
+    boxes = []
+    for i, n in enumerate(sides):
+        L = 512e3
+        start = (0.5 * L + rng.uniform(-50e3, 50e3), 0.5 * L + rng.uniform(-50e3, 50e3))
+        boxes.append(BoxTest(int(n), seed=int(seed + i), h_noise=0.02, start=start,
+                             wind_speed=float(rng.uniform(8.0, 12.0))))
+    return boxes
+
+
+def run_ensemble(args):
+    """Batched ensemble (one graph per step for all members) against the same
+    members stepped one after another, each with its own graph."""
+    from nextsimdg_gb300.dynamics import Ensemble, MEVPDynamicsKernel
+
+    boxes = ensemble_boxes(args.ensemble)
+    members = []
+    for b in boxes:
+        k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=1)
+        k.initialise(b.coords(), False, b.mask())
+        for name, arr in b.initial_fields().items():
+            k.setData(name, arr)
+        members.append(k)
+    cells = sum(b.nelements for b in boxes)
+    ens = Ensemble(members)
+    ens.time_updates(DT, max(args.warmup, 3))
+    with ClockSampler(0) as clk:
+        ms = ens.time_updates(DT, args.steps)
+    # the same members one by one (each its own graph, same stream order)
+    t_seq = 0.0
+    for k in members:
+        k.time_updates(DT, 1)
+        t_seq += k.time_updates(DT, args.steps)
+    tiles = {}
+    for i, b in enumerate(boxes):
+        tiles[f"{b.nx}"] = "x".join(map(str, ens.tile(i)))
+    line = {"metric": METRIC, "value": cells * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic box-test ensemble",
+            "config": {"workload": f"ensemble of {len(boxes)} box tests, sides "
+                                   f"{sorted(set(int(b.nx) for b in boxes))}, {cells} cells, DG2, mEVP {NSTEPS} "
+                                   f"iterations, mixed precision", "members": len(boxes)},
+            "sequential_members": {"value": cells * args.steps / (t_seq * 1e-3), "ms_per_step": t_seq / args.steps},
+            "autotuned_tiles": tiles, "gpu_launches": ens.launches_per_update() * args.steps,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ens.close()
+    for k in members:
+        k.close()
+
+
 def run_profile(args):
     """Setup plus warm-up and K device-resident steps, nothing else."""
     from nextsimdg_gb300.boxtest import BoxTest
@@ -409,6 +467,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--ensemble", type=int, default=0,
+                    help="time a batched ensemble of this many box tests (mixed precision) instead")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="fp64: every operation FP64 (the reference's arithmetic); mixed: FP32 bulk")
     ap.add_argument("--nx", type=int, default=NX, help="box side in cells (256 is the benchmark grid)")
@@ -417,7 +477,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
-    if args.profile:
+    if args.ensemble:
+        run_ensemble(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args, world, rank)

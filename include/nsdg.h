@@ -160,6 +160,28 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
 int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
 
 /* ======================================================================== */
+/* Batched ensembles                                                         */
+/* ======================================================================== */
+/* Several independent dynamics kernels (ensemble members, uneven grids) stepped
+ * together: one CUDA graph per step runs each member's transport and
+ * preparation and then the mEVP sub-cycle of all members as one element launch
+ * and one node launch per iteration.  No reference counterpart: the reference
+ * runs one model (one kernel) per process.  Members must be initialised
+ * mEVP kernels in NSDG_PRECISION_MIXED with the same parameters; they keep
+ * their own setData / getDG0Data, which are ordered after the ensemble's
+ * update.  The element tile shape of every grid size is chosen at creation by
+ * timing the candidates on the GPU (nsdg_ensemble_tile reports the choice). */
+typedef struct nsdg_ensemble nsdg_ensemble;
+int nsdg_ensemble_create(nsdg_kernel* const* members, int n_members, nsdg_ensemble** out);
+int nsdg_ensemble_destroy(nsdg_ensemble* ens);
+const char* nsdg_ensemble_last_error(const nsdg_ensemble* ens);
+int nsdg_ensemble_update(nsdg_ensemble* ens, double t_start, double dt);
+int nsdg_ensemble_synchronize(nsdg_ensemble* ens);
+int nsdg_ensemble_time_updates(nsdg_ensemble* ens, double dt, int steps, float* ms);
+int nsdg_ensemble_tile(nsdg_ensemble* ens, int member, int* tile_w, int* tile_h);
+int nsdg_ensemble_launches_per_update(nsdg_ensemble* ens, int* launches);
+
+/* ======================================================================== */
 /* Stand-alone DG transport (the DGTransport<DG> class of the reference)    */
 /* ======================================================================== */
 typedef struct nsdg_transport nsdg_transport;

@@ -78,6 +78,14 @@ SIGNATURES = [
     ("nsdg_transport_reinit_normal_velocity", c_int, [c_void_p]),
     ("nsdg_transport_step", c_int, [c_void_p, c_double, c_void_p, c_int, c_int, c_double, c_int, c_double]),
     ("nsdg_transport_mean_value", c_int, [c_void_p, c_void_p, POINTER(c_double)]),
+    ("nsdg_ensemble_create", c_int, [POINTER(c_void_p), c_int, POINTER(c_void_p)]),
+    ("nsdg_ensemble_destroy", c_int, [c_void_p]),
+    ("nsdg_ensemble_last_error", c_char_p, [c_void_p]),
+    ("nsdg_ensemble_update", c_int, [c_void_p, c_double, c_double]),
+    ("nsdg_ensemble_synchronize", c_int, [c_void_p]),
+    ("nsdg_ensemble_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
+    ("nsdg_ensemble_tile", c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int)]),
+    ("nsdg_ensemble_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 

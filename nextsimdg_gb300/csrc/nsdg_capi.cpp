@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <exception>
+#include <map>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -148,7 +150,12 @@ struct nsdg_kernel {
         ready = false;
     }
     int initialise(size_t nx, size_t ny, const double* coords, int spherical, const double* mask);
-    int enqueueUpdate(double dt, int& launches);
+    // Phases of one model step: everything before the sub-cycle, the
+    // sub-cycle, and what follows it (the ensemble runs the sub-cycle of all
+    // its members as batched launches between the other two).
+    enum Phase { PHASE_PREP = 1, PHASE_LOOP = 2, PHASE_FINISH = 4, PHASE_ALL = 7 };
+    int enqueuePhases(cudaStream_t s, double dt, int phases, int& launches);
+    int enqueueUpdate(double dt, int& launches) { return enqueuePhases(stream, dt, PHASE_ALL, launches); }
     int ensureGraph(double dt);
     int checkDeviceError();
 };
@@ -404,9 +411,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     return ok();
 }
 
-int nsdg_kernel::enqueueUpdate(double dt, int& launches)
+int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launches)
 {
-    cudaStream_t s = stream;
     launches = 0;
     cudaError_t e;
 #define LCH(expr)                                                                                  \
@@ -418,6 +424,9 @@ int nsdg_kernel::enqueueUpdate(double dt, int& launches)
     } while (0)
     const size_t dN = size_t(dg) * N;
     const bool bbm = rheology == NSDG_RHEOLOGY_BBM;
+    const bool prep = (phases & PHASE_PREP) != 0, loop = (phases & PHASE_LOOP) != 0;
+    const bool finish = (phases & PHASE_FINISH) != 0;
+    if (prep) {
     // --- advection of cice, hice (and damage for BBM), with limits
     //     (DynamicsKernel.hpp:160-172; BrittleCGDynamicsKernel.hpp:89-106) ---
     {
@@ -481,26 +490,31 @@ int nsdg_kernel::enqueueUpdate(double dt, int& launches)
             return fail(NSDG_ERR_CUDA, std::string("ssh gradient: ") + cudaGetErrorString(e));
         launches += 3;
     }
+    } // prep
     const int nS = P.n_steps;
     if (!bbm) {
         MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, dt };
         MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
-        LCH(launchMevpPrepNodes(s, dm, st, mp));
-        LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
-        if (!mixed()) {
-            for (int it = 0; it < nS; ++it) {
-                LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
-                LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
-            }
-        } else {
-            LCH(launchMevpPrepNodes32(s, dm, st, st32));
-            for (int it = 0; it < nS; ++it) {
-                LCH(launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp));
-                LCH(launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, derr));
-            }
-            LCH(launchWidenVelocity(s, Ncg, st32.u, st32.v, u, v));
+        if (prep) {
+            LCH(launchMevpPrepNodes(s, dm, st, mp));
+            LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
+            if (mixed())
+                LCH(launchMevpPrepNodes32(s, dm, st, st32));
         }
-    } else {
+        if (loop) {
+            for (int it = 0; it < nS; ++it) {
+                if (!mixed()) {
+                    LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
+                    LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
+                } else {
+                    LCH(launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp));
+                    LCH(launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, derr));
+                }
+            }
+        }
+        if (finish && mixed())
+            LCH(launchWidenVelocity(s, Ncg, st32.u, st32.v, u, v));
+    } else if (phases == PHASE_ALL) {
         const double rad = 0x1.1df46a2529d39p-6;
         BbmParams bp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, dt / nS, double(nS),
             std::cos(rad * P.ocean_turning_angle), std::sin(rad * P.ocean_turning_angle),
@@ -1086,6 +1100,391 @@ int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches)
     }
     *launches = k->launchesPerUpdate;
     return k->ok();
+}
+
+} // extern "C"
+
+// ===========================================================================
+// Batched ensembles (nsdg_ensemble_*)
+// ===========================================================================
+struct nsdg_ensemble {
+    std::vector<nsdg_kernel*> members;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    void* dmem = nullptr;
+    EnsembleMember* dMembers = nullptr;
+    uint16_t* dStressMap = nullptr;
+    uint16_t* dNodeMap = nullptr;
+    int* derr = nullptr;
+    int stressBlocks = 0, nodeBlocks = 0;
+    std::vector<int> tileW;
+    cudaGraphExec_t graph = nullptr;
+    double graphDt = -1.0;
+    int launches = 0;
+    cudaEvent_t done = nullptr;
+
+    int fail(int code, const std::string& m)
+    {
+        err = m;
+        return code;
+    }
+    ~nsdg_ensemble()
+    {
+        if (stream)
+            cudaStreamSynchronize(stream);
+        if (graph)
+            cudaGraphExecDestroy(graph);
+        if (done)
+            cudaEventDestroy(done);
+        if (dmem)
+            cudaFree(dmem);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+    EnsembleMember describe(nsdg_kernel* k, int tw) const
+    {
+        EnsembleMember d {};
+        d.nx = k->dm.nx;
+        d.ny = k->dm.ny;
+        d.N = k->N;
+        d.Ncg = k->Ncg;
+        d.ice = k->dm.ice;
+        d.cg2Dir = k->dm.cg2Dir;
+        d.invm2 = k->dops.invm2;
+        d.o = k->dops32;
+        d.st = k->st32;
+        d.Pg = k->Pg;
+        d.tdiv = k->tdiv32;
+        d.tileW = tw;
+        d.tileH = stressElementsPerBlock() / tw;
+        d.tilesX = (d.nx + tw - 1) / tw;
+        return d;
+    }
+    static int stressBlocksOf(const EnsembleMember& d) { return d.tilesX * ((d.ny + d.tileH - 1) / d.tileH); }
+    static int nodeBlocksOf(const EnsembleMember& d)
+    {
+        return static_cast<int>((d.Ncg + nodesPerBlock() - 1) / nodesPerBlock());
+    }
+    int autotune();
+    int build();
+    int ensureGraph(double dt);
+};
+
+// Project-written autotuner: for every grid size in the ensemble, times the
+// batched element kernel on that member alone for each tile shape
+// (tileW x tileH, tileW * tileH = elements per block) and keeps the fastest.
+// The divergence coefficients of the timing runs go to a scratch buffer, so
+// the members' state is not touched.
+int nsdg_ensemble::autotune()
+{
+    const int E = stressElementsPerBlock();
+    std::vector<int> candidates;
+    for (int w = E; w >= 8; w /= 2)
+        candidates.push_back(w);
+    size_t maxN = 0;
+    for (auto* k : members)
+        maxN = std::max(maxN, k->N);
+    void* scratch = nullptr;
+    EnsembleMember* dOne = nullptr;
+    uint16_t* dMap = nullptr;
+    size_t mapLen = 1;
+    for (auto* k : members)
+        for (int w : candidates)
+            mapLen = std::max(mapLen, static_cast<size_t>(stressBlocksOf(describe(k, w))));
+    if (cudaMalloc(&scratch, 18 * maxN * sizeof(float)) != cudaSuccess
+        || cudaMalloc(&dOne, sizeof(EnsembleMember)) != cudaSuccess
+        || cudaMalloc(&dMap, mapLen * sizeof(uint16_t)) != cudaSuccess) {
+        cudaFree(scratch);
+        cudaFree(dOne);
+        return fail(NSDG_ERR_CUDA, "ensemble autotune: allocation failed");
+    }
+    cudaMemsetAsync(dMap, 0, mapLen * sizeof(uint16_t), stream);
+    cudaMemsetAsync(scratch, 0, 18 * maxN * sizeof(float), stream);
+    std::map<std::pair<int, int>, int> best;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const nsdg_params& P = members[0]->P;
+    MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, 120.0 };
+    cudaError_t e = cudaSuccess;
+    for (size_t mi = 0; mi < members.size() && e == cudaSuccess; ++mi) {
+        nsdg_kernel* k = members[mi];
+        const auto key = std::make_pair(k->dm.nx, k->dm.ny);
+        if (best.count(key))
+            continue;
+        float bestMs = 1e30f;
+        int bestW = E;
+        for (int w : candidates) {
+            EnsembleMember d = describe(k, w);
+            d.tdiv = static_cast<float*>(scratch);
+            d.stressBlock0 = 0;
+            const int blocks = stressBlocksOf(d);
+            e = cudaMemcpyAsync(dOne, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
+            for (int r = 0; r < 3 && e == cudaSuccess; ++r) // warm-up
+                e = launchMevpStress32Batched(stream, dOne, dMap, blocks, mp);
+            if (e == cudaSuccess) e = cudaEventRecord(a, stream);
+            for (int r = 0; r < 10 && e == cudaSuccess; ++r)
+                e = launchMevpStress32Batched(stream, dOne, dMap, blocks, mp);
+            if (e == cudaSuccess) e = cudaEventRecord(b, stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (e == cudaSuccess && ms < bestMs) {
+                bestMs = ms;
+                bestW = w;
+            }
+        }
+        best[key] = bestW;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamSynchronize(stream);
+    cudaFree(scratch);
+    cudaFree(dOne);
+    cudaFree(dMap);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("ensemble autotune: ") + cudaGetErrorString(e));
+    tileW.clear();
+    for (auto* k : members)
+        tileW.push_back(best[std::make_pair(k->dm.nx, k->dm.ny)]);
+    return NSDG_OK;
+}
+
+int nsdg_ensemble::build()
+{
+    std::vector<EnsembleMember> table;
+    std::vector<uint16_t> smap, nmap;
+    for (size_t mi = 0; mi < members.size(); ++mi) {
+        EnsembleMember d = describe(members[mi], tileW[mi]);
+        d.stressBlock0 = static_cast<int>(smap.size());
+        d.nodeBlock0 = static_cast<int>(nmap.size());
+        smap.insert(smap.end(), stressBlocksOf(d), static_cast<uint16_t>(mi));
+        nmap.insert(nmap.end(), nodeBlocksOf(d), static_cast<uint16_t>(mi));
+        table.push_back(d);
+    }
+    stressBlocks = static_cast<int>(smap.size());
+    nodeBlocks = static_cast<int>(nmap.size());
+    const size_t bytes = al(table.size() * sizeof(EnsembleMember)) + al(smap.size() * 2) + al(nmap.size() * 2) + al(4);
+    if (cudaMalloc(&dmem, bytes) != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, "ensemble: allocation failed");
+    char* p = static_cast<char*>(dmem);
+    dMembers = reinterpret_cast<EnsembleMember*>(p);
+    p += al(table.size() * sizeof(EnsembleMember));
+    dStressMap = reinterpret_cast<uint16_t*>(p);
+    p += al(smap.size() * 2);
+    dNodeMap = reinterpret_cast<uint16_t*>(p);
+    p += al(nmap.size() * 2);
+    derr = reinterpret_cast<int*>(p);
+    cudaError_t e = cudaMemcpy(dMembers, table.data(), table.size() * sizeof(EnsembleMember), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dStressMap, smap.data(), smap.size() * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dNodeMap, nmap.data(), nmap.size() * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("ensemble: upload failed: ") + cudaGetErrorString(e));
+    return NSDG_OK;
+}
+
+int nsdg_ensemble::ensureGraph(double dt)
+{
+    if (graph && graphDt == dt)
+        return NSDG_OK;
+    if (graph) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    const nsdg_params& P = members[0]->P;
+    MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, dt };
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(e));
+    int total = 0, st = NSDG_OK;
+    for (auto* k : members) {
+        int l = 0;
+        st = k->enqueuePhases(stream, dt, nsdg_kernel::PHASE_PREP, l);
+        total += l;
+        if (st) {
+            err = k->err;
+            break;
+        }
+    }
+    for (int it = 0; it < P.n_steps && st == NSDG_OK; ++it) {
+        e = launchMevpStress32Batched(stream, dMembers, dStressMap, stressBlocks, mp);
+        if (e == cudaSuccess)
+            e = launchMevpMomentum32Batched(stream, dMembers, dNodeMap, nodeBlocks, mp, derr);
+        if (e != cudaSuccess)
+            st = fail(NSDG_ERR_CUDA, std::string("ensemble sub-cycle: ") + cudaGetErrorString(e));
+        total += 2;
+    }
+    for (auto* k : members) {
+        if (st)
+            break;
+        int l = 0;
+        st = k->enqueuePhases(stream, dt, nsdg_kernel::PHASE_FINISH, l);
+        total += l;
+        if (st)
+            err = k->err;
+    }
+    const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+    if (st) {
+        if (g)
+            cudaGraphDestroy(g);
+        return st;
+    }
+    if (ec != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ec));
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        graph = nullptr;
+        return fail(NSDG_ERR_CUDA, std::string("ensemble instantiate: ") + cudaGetErrorString(e));
+    }
+    graphDt = dt;
+    launches = total;
+    return NSDG_OK;
+}
+
+extern "C" {
+
+int nsdg_ensemble_create(nsdg_kernel* const* members, int n_members, nsdg_ensemble** out)
+{
+    if (!out || !members || n_members < 1 || n_members > 65535)
+        return NSDG_ERR_BAD_ARG;
+    *out = nullptr;
+    const nsdg_params& P0 = members[0] ? members[0]->P : nsdg_params {};
+    for (int i = 0; i < n_members; ++i) {
+        const nsdg_kernel* k = members[i];
+        if (!k || !k->ready || k->rheology != NSDG_RHEOLOGY_MEVP || !k->mixed())
+            return NSDG_ERR_UNSUPPORTED; // initialised mEVP kernels in mixed precision only
+        const nsdg_params& P = k->P;
+        if (P.n_steps != P0.n_steps || P.alpha != P0.alpha || P.beta != P0.beta || P.rho_ice != P0.rho_ice
+            || P.F_ocean != P0.F_ocean || P.F_atm != P0.F_atm || P.fc != P0.fc || P.gravity != P0.gravity
+            || P.Pstar != P0.Pstar || P.DeltaMin != P0.DeltaMin)
+            return NSDG_ERR_BAD_ARG; // the batched launches share one parameter set
+        for (int j = 0; j < i; ++j)
+            if (members[j] == k)
+                return NSDG_ERR_BAD_ARG;
+    }
+    nsdg_ensemble* ens = new nsdg_ensemble();
+    ens->members.assign(members, members + n_members);
+    if (cudaStreamCreateWithFlags(&ens->stream, cudaStreamNonBlocking) != cudaSuccess
+        || cudaEventCreateWithFlags(&ens->done, cudaEventDisableTiming) != cudaSuccess) {
+        delete ens;
+        return NSDG_ERR_CUDA;
+    }
+    for (auto* k : ens->members)
+        cudaStreamSynchronize(k->stream);
+    if (ens->autotune() != NSDG_OK || ens->build() != NSDG_OK) {
+        delete ens;
+        return NSDG_ERR_CUDA;
+    }
+    *out = ens;
+    return NSDG_OK;
+}
+
+int nsdg_ensemble_destroy(nsdg_ensemble* ens)
+{
+    if (!ens)
+        return NSDG_ERR_BAD_ARG;
+    delete ens;
+    return NSDG_OK;
+}
+
+const char* nsdg_ensemble_last_error(const nsdg_ensemble* ens) { return ens ? ens->err.c_str() : "null handle"; }
+
+int nsdg_ensemble_update(nsdg_ensemble* ens, double t_start, double dt)
+{
+    (void)t_start;
+    if (!ens)
+        return NSDG_ERR_BAD_ARG;
+    if (!(dt > 0) || !std::isfinite(dt))
+        return ens->fail(NSDG_ERR_BAD_ARG, "update: dt must be positive");
+    int r = ens->ensureGraph(dt);
+    if (r)
+        return r;
+    // order the graph after the members' own streams, and their later reads after the graph
+    for (auto* k : ens->members) {
+        cudaEvent_t ev;
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        cudaEventRecord(ev, k->stream);
+        cudaStreamWaitEvent(ens->stream, ev, 0);
+        cudaEventDestroy(ev);
+    }
+    cudaError_t e = cudaGraphLaunch(ens->graph, ens->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ens->done, ens->stream);
+    for (auto* k : ens->members) {
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(k->stream, ens->done, 0);
+        ++k->stepNumber;
+    }
+    if (e != cudaSuccess)
+        return ens->fail(NSDG_ERR_CUDA, std::string("update: ") + cudaGetErrorString(e));
+    ens->err.clear();
+    return NSDG_OK;
+}
+
+int nsdg_ensemble_synchronize(nsdg_ensemble* ens)
+{
+    if (!ens)
+        return NSDG_ERR_BAD_ARG;
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, ens->derr, sizeof(int), cudaMemcpyDeviceToHost, ens->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ens->stream);
+    if (e != cudaSuccess)
+        return ens->fail(NSDG_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+    if (h) {
+        cudaMemsetAsync(ens->derr, 0, sizeof(int), ens->stream);
+        return ens->fail(NSDG_ERR_NUMERIC, "non-finite velocity in an ensemble member");
+    }
+    return NSDG_OK;
+}
+
+int nsdg_ensemble_time_updates(nsdg_ensemble* ens, double dt, int steps, float* ms)
+{
+    if (!ens || !ms || steps < 1)
+        return NSDG_ERR_BAD_ARG;
+    int r = ens->ensureGraph(dt);
+    if (r)
+        return r;
+    for (auto* k : ens->members)
+        cudaStreamSynchronize(k->stream);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaError_t e = cudaEventRecord(a, ens->stream);
+    for (int i = 0; i < steps && e == cudaSuccess; ++i)
+        e = cudaGraphLaunch(ens->graph, ens->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b, ens->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess)
+        return ens->fail(NSDG_ERR_CUDA, std::string("time_updates: ") + cudaGetErrorString(e));
+    for (auto* k : ens->members)
+        k->stepNumber += steps;
+    return nsdg_ensemble_synchronize(ens);
+}
+
+int nsdg_ensemble_tile(nsdg_ensemble* ens, int member, int* tile_w, int* tile_h)
+{
+    if (!ens || !tile_w || !tile_h || member < 0 || member >= static_cast<int>(ens->members.size()))
+        return NSDG_ERR_BAD_ARG;
+    *tile_w = ens->tileW[member];
+    *tile_h = stressElementsPerBlock() / ens->tileW[member];
+    return NSDG_OK;
+}
+
+int nsdg_ensemble_launches_per_update(nsdg_ensemble* ens, int* launches)
+{
+    if (!ens || !launches)
+        return NSDG_ERR_BAD_ARG;
+    if (!ens->graph) {
+        const int r = ens->ensureGraph(120.0);
+        if (r)
+            return r;
+    }
+    *launches = ens->launches;
+    return NSDG_OK;
 }
 
 } // extern "C"

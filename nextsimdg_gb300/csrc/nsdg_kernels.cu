@@ -1020,19 +1020,16 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeSta
 // FP32 strain (it is a positive-definite quadratic form: no cancellation);
 // Delta = sqrt(invariant + DeltaMin^2) and the viscosity P/(8 alpha Delta) are
 // evaluated in FP64; the stress increments and the divergence update are FP32.
-__global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(DevMesh m, DevOps32 o,
-    const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
-    float* __restrict__ tdiv, MevpParams p)
+// Body of the mixed-precision element kernel for element e handled by thread
+// (le, part) of a block of kStressElems x kStressParts threads; shared by the
+// single-grid and the batched (ensemble) kernels.
+__device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool active, size_t e, int le, int part,
+    const DevOps32& o, const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
+    float* __restrict__ tdiv, const MevpParams& p, float (*fs)[9][kStressElems])
 {
-    __shared__ float fs[3][9][kStressElems];
-    const int le = threadIdx.x % kStressElems;
-    const int part = threadIdx.x / kStressElems;
-    const size_t N = m.N;
-    const size_t e = blockIdx.x * size_t(kStressElems) + le;
-    const bool active = e < N && m.ice[e];
     if (active) {
-        const size_t s2 = 2 * size_t(m.nx) + 1;
-        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t s2 = 2 * size_t(nx) + 1;
+        const size_t ix = e % nx, iy = e / nx;
         const size_t base = 2 * s2 * iy + 2 * ix;
         float ul[9], vl[9];
 #pragma unroll
@@ -1086,30 +1083,45 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(Dev
     }
 }
 
-__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, MevpNodeState32 st,
-    const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
+// The FP64 kernel kMevpStress with FP32 operators and state.  The strain
+// invariant 1.25(e11^2+e22^2) + 1.5 e11 e22 + e12^2 is formed in FP32 from the
+// FP32 strain (it is a positive-definite quadratic form: no cancellation);
+// Delta = sqrt(invariant + DeltaMin^2) and the viscosity P/(8 alpha Delta) are
+// evaluated in FP64; the stress increments and the divergence update are FP32.
+__global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(DevMesh m, DevOps32 o,
+    const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
+    float* __restrict__ tdiv, MevpParams p)
 {
-    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-    if (i >= m.Ncg)
-        return;
-    const int s2 = 2 * m.nx + 1;
+    __shared__ float fs[3][9][kStressElems];
+    const int le = threadIdx.x % kStressElems;
+    const int part = threadIdx.x / kStressElems;
+    const size_t e = blockIdx.x * size_t(kStressElems) + le;
+    const bool active = e < m.N && m.ice[e];
+    mevpStress32Element(m.nx, m.N, active, e, le, part, o, u, v, Pg, tdiv, p, fs);
+}
+
+// Body of the mixed-precision node kernel for CG2 node i.
+__device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, size_t i, const uint8_t* __restrict__ cg2Dir,
+    const double* __restrict__ invm2, const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p,
+    int* __restrict__ err)
+{
+    const int s2 = 2 * nx + 1;
     const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
-    const bool dir = m.cg2Dir[i] != 0;
+    const bool dir = cg2Dir[i] != 0;
     float dSx = 0.f, dSy = 0.f;
     if (!dir) {
         int cxs[2], lxs[2], cys[2], lys[2];
-        const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
-        const int nyc = nodeCandidates(j2, m.ny, cys, lys);
+        const int nxc = nodeCandidates(i2, nx, cxs, lxs);
+        const int nyc = nodeCandidates(j2, ny, cys, lys);
         int order[2] = { 0, 1 };
         if (nyc == 2 && (cys[0] % 2) == 1) {
             order[0] = 1;
             order[1] = 0;
         }
-        const size_t N = m.N;
         for (int r = 0; r < nyc; ++r) {
             const int cy = cys[order[r]], ly = lys[order[r]];
             for (int k = 0; k < nxc; ++k) {
-                const size_t c = size_t(cy) * m.nx + cxs[k];
+                const size_t c = size_t(cy) * nx + cxs[k];
                 const int j = lxs[k] + 3 * ly;
                 dSx -= tdiv[j * N + c];
                 dSy -= tdiv[(9 + j) * N + c];
@@ -1117,7 +1129,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, M
         }
     }
     // divided by the lumped mass in FP64
-    const double invm = o.invm2[i];
+    const double invm = invm2[i];
     const float mx = static_cast<float>(static_cast<double>(dSx) * invm);
     const float my = static_cast<float>(static_cast<double>(dSy) * invm);
     const float u = st.u[i], v = st.v[i];
@@ -1139,6 +1151,48 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, M
     }
     st.u[i] = un;
     st.v[i] = vn;
+}
+
+__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, MevpNodeState32 st,
+    const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= m.Ncg)
+        return;
+    mevpMomentum32Node(m.nx, m.ny, m.N, i, m.cg2Dir, o.invm2, st, tdiv, p, err);
+}
+
+// ---------------------------------------------------------------------------
+// Batched ensemble: one launch covers the elements (nodes) of every member.
+// Block b belongs to member blockMember[b]; within the member, stress blocks
+// map to 2D tiles of tileW x tileH elements (tileW * tileH = kStressElems,
+// chosen per grid size by the ensemble's autotuner) and node blocks to
+// consecutive runs of kBlock CG2 nodes.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32Batched(
+    const EnsembleMember* __restrict__ members, const uint16_t* __restrict__ blockMember, MevpParams p)
+{
+    __shared__ float fs[3][9][kStressElems];
+    const EnsembleMember& M = members[blockMember[blockIdx.x]];
+    const int b = static_cast<int>(blockIdx.x) - M.stressBlock0;
+    const int le = threadIdx.x % kStressElems;
+    const int part = threadIdx.x / kStressElems;
+    const int tx = b % M.tilesX, ty = b / M.tilesX;
+    const int ix = tx * M.tileW + le % M.tileW, iy = ty * M.tileH + le / M.tileW;
+    const bool inside = ix < M.nx && iy < M.ny;
+    const size_t e = inside ? size_t(iy) * M.nx + ix : 0;
+    const bool active = inside && M.ice[e];
+    mevpStress32Element(M.nx, M.N, active, e, le, part, M.o, M.st.u, M.st.v, M.Pg, M.tdiv, p, fs);
+}
+
+__global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
+    const uint16_t* __restrict__ blockMember, MevpParams p, int* __restrict__ err)
+{
+    const EnsembleMember& M = members[blockMember[blockIdx.x]];
+    const size_t i = (static_cast<size_t>(blockIdx.x) - M.nodeBlock0) * kBlock + threadIdx.x;
+    if (i >= M.Ncg)
+        return;
+    mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.invm2, M.st, M.tdiv, p, err);
 }
 
 __global__ void kWidenVelocity(size_t n, const float* __restrict__ u32, const float* __restrict__ v32,
@@ -1577,6 +1631,21 @@ cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps&
     kMevpMomentum32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, tdiv, p, err);
     return cudaGetLastError();
 }
+cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
+    int blocks, const MevpParams& p)
+{
+    kMevpStress32Batched<<<blocks, kStressElems * kStressParts, 0, s>>>(members, blockMember, p);
+    return cudaGetLastError();
+}
+cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
+    int blocks, const MevpParams& p, int* err)
+{
+    kMevpMomentum32Batched<<<blocks, kBlock, 0, s>>>(members, blockMember, p, err);
+    return cudaGetLastError();
+}
+int stressElementsPerBlock() { return kStressElems; }
+int nodesPerBlock() { return kBlock; }
+
 cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, const float* v32, double* u, double* v)
 {
     kWidenVelocity<<<blocksFor(n), kBlock, 0, s>>>(n, u32, v32, u, v);

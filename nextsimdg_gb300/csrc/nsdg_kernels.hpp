@@ -176,6 +176,28 @@ cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32&
     const float* v, const double* Pg, float* tdiv, const MevpParams& p);
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o,
     const MevpNodeState32& st, const float* tdiv, const MevpParams& p, int* err);
+// One member of a batched ensemble (device-resident table entry).
+struct EnsembleMember {
+    int nx, ny;
+    size_t N, Ncg;
+    const uint8_t* ice;
+    const uint8_t* cg2Dir;
+    const double* invm2;
+    DevOps32 o;
+    MevpNodeState32 st;
+    const double* Pg;
+    float* tdiv;
+    int tileW, tileH, tilesX;
+    int stressBlock0, nodeBlock0;
+};
+// One launch each for the element and the node phase of every member.
+cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
+    int blocks, const MevpParams& p);
+cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
+    int blocks, const MevpParams& p, int* err);
+int stressElementsPerBlock();
+int nodesPerBlock();
+
 // u, v (FP64) from the FP32 iterate at the end of the sub-cycle
 cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, const float* v32, double* u,
     double* v);

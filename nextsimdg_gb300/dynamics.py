@@ -30,7 +30,7 @@ import numpy as np
 from . import _lib
 from ._lib import NsdgError, Params
 
-__all__ = ["TimestepTime", "MEVPDynamicsKernel", "BBMDynamicsKernel", "DGTransport", "Params",
+__all__ = ["TimestepTime", "MEVPDynamicsKernel", "BBMDynamicsKernel", "Ensemble", "DGTransport", "Params",
            "NsdgError", "default_params"]
 
 default_params = _lib.default_params
@@ -193,6 +193,60 @@ class BBMDynamicsKernel(_KernelBase):
     """Brittle BBM rheology (BBMDynamicsKernel.hpp, BrittleCGDynamicsKernel.hpp)."""
 
     rheology = _lib.RHEOLOGY_BBM
+
+
+class Ensemble:
+    """Several mEVP kernels (mixed precision, possibly uneven grids) stepped
+    together: per step one CUDA graph, with the mEVP sub-cycle of all members
+    in one element launch and one node launch per iteration.  The members keep
+    their own setData / getDG0Data."""
+
+    def __init__(self, members):
+        self._l = _lib.load()
+        self.members = list(members)
+        arr = (c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        h = c_void_p()
+        st = self._l.nsdg_ensemble_create(arr, len(self.members), byref(h))
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, f"nsdg_ensemble_create: {self._l.nsdg_status_string(st).decode()}")
+        self._h = h
+
+    def _check(self, st):
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, self._l.nsdg_ensemble_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.nsdg_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update(self, tst, dt=None):
+        start, step = (tst.start, tst.step) if isinstance(tst, TimestepTime) else (float(tst), float(dt))
+        self._check(self._l.nsdg_ensemble_update(self._h, start, step))
+
+    def synchronize(self):
+        self._check(self._l.nsdg_ensemble_synchronize(self._h))
+
+    def time_updates(self, dt, steps):
+        ms = c_float()
+        self._check(self._l.nsdg_ensemble_time_updates(self._h, dt, steps, byref(ms)))
+        return ms.value
+
+    def tile(self, member):
+        w, h = c_int(), c_int()
+        self._check(self._l.nsdg_ensemble_tile(self._h, member, byref(w), byref(h)))
+        return w.value, h.value
+
+    def launches_per_update(self):
+        n = c_int()
+        self._check(self._l.nsdg_ensemble_launches_per_update(self._h, byref(n)))
+        return n.value
 
 
 class DGTransport:
