@@ -211,6 +211,32 @@ int nsdg_transport_step(nsdg_transport* t, double dt, double* phi, int nsteps,
 int nsdg_transport_mean_value(nsdg_transport* t, const double* phi, double* out);
 
 /* ======================================================================== */
+/* Warm-start network (no counterpart in the reference)                      */
+/* ======================================================================== */
+/* A stack of 3x3 convolutions (ReLU between layers) on the cell grid, trained
+ * and evaluated on the GPU with BF16 tensor-core kernels accumulating in FP32.
+ * channels: n_layers+1 counts, each 16, 32 or 48; the first `used_outputs`
+ * output channels enter the masked mean-squared-error loss.  Parameters are
+ * one FP32 vector: per layer the weights W[co][3*dy+dx][ci] then the biases. */
+typedef struct nsdg_net nsdg_net;
+int nsdg_net_create(int n_layers, const int* channels, int height, int width, int max_batch,
+    int used_outputs, unsigned long long seed, nsdg_net** out);
+int nsdg_net_destroy(nsdg_net* net);
+const char* nsdg_net_last_error(const nsdg_net* net);
+int nsdg_net_param_count(nsdg_net* net, size_t* n);
+int nsdg_net_get_params(nsdg_net* net, float* host, size_t n);
+int nsdg_net_set_params(nsdg_net* net, const float* host, size_t n);
+int nsdg_net_get_grads(nsdg_net* net, float* host, size_t n);
+/* host input [batch][h][w][ch0] (rounded to BF16), target [batch][h][w][chL],
+ * mask [batch][h][w]; target and mask may be NULL */
+int nsdg_net_set_batch(nsdg_net* net, int batch, const float* input, const float* target,
+    const float* mask);
+int nsdg_net_forward(nsdg_net* net, int batch, float* out_host);
+/* loss and gradients of the last forward pass (gradients stay on the device) */
+int nsdg_net_loss_backward(nsdg_net* net, int batch, float* loss);
+int nsdg_net_adam_step(nsdg_net* net, float lr, float beta1, float beta2, float eps);
+
+/* ======================================================================== */
 /* Allocation-free entry point                                               */
 /* ======================================================================== */
 /* No counterpart in the reference.  Tools::MeanValue (the FP64 mesh integral

@@ -86,6 +86,18 @@ SIGNATURES = [
     ("nsdg_ensemble_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
     ("nsdg_ensemble_tile", c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int)]),
     ("nsdg_ensemble_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
+    ("nsdg_net_create", c_int, [c_int, POINTER(c_int), c_int, c_int, c_int, c_int, ctypes.c_ulonglong,
+                                POINTER(c_void_p)]),
+    ("nsdg_net_destroy", c_int, [c_void_p]),
+    ("nsdg_net_last_error", c_char_p, [c_void_p]),
+    ("nsdg_net_param_count", c_int, [c_void_p, POINTER(c_size_t)]),
+    ("nsdg_net_get_params", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_net_set_params", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_net_get_grads", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_net_set_batch", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    ("nsdg_net_forward", c_int, [c_void_p, c_int, c_void_p]),
+    ("nsdg_net_loss_backward", c_int, [c_void_p, c_int, POINTER(c_float)]),
+    ("nsdg_net_adam_step", c_int, [c_void_p, c_float, c_float, c_float, c_float]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 

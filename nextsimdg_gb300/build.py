@@ -23,7 +23,7 @@ LIB = PKG / "libnsdg_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
-CU_SOURCES = ["nsdg_kernels.cu", "nsdg_noalloc.cu"]
+CU_SOURCES = ["nsdg_kernels.cu", "nsdg_noalloc.cu", "nsdg_surrogate.cu"]
 CXX_SOURCES = ["nsdg_host.cpp", "nsdg_capi.cpp", "nsdg_transport_capi.cpp"]
 
 

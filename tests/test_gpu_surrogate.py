@@ -1,0 +1,59 @@
+"""GPU network kernels (BF16 mma.sync, FP32 accumulate) against the numpy oracle:
+forward output, loss, weight and bias gradients; and a short training run."""
+import numpy as np
+import pytest
+
+from oracle import cnn_oracle as co
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
+
+
+@pytest.mark.parametrize("chans,H,W,B,used", [([16, 32, 32, 16], 10, 13, 2, 12), ([48, 48, 32], 9, 70, 1, 26)])
+def test_net_gradients_match_oracle(gpu, chans, H, W, B, used):
+    from nextsimdg_gb300.surrogate import Net
+    rng = np.random.default_rng(11)
+    net = Net(chans, H, W, max_batch=B, used_outputs=used, seed=5)
+    p = net.get_params()
+    p[:] = (rng.standard_normal(p.size) * 0.2).astype(np.float32)  # nonzero biases too
+    net.set_params(p)
+    Ws, bs = net.unpack(p)
+    x = rng.standard_normal((B, H, W, chans[0])).astype(np.float32)
+    t = np.zeros((B, H, W, chans[-1]), dtype=np.float32)
+    t[..., :used] = rng.standard_normal((B, H, W, used))
+    m = (rng.random((B, H, W)) > 0.2).astype(np.float32)
+    net.set_batch(x, t, m)
+    out = net.forward()
+    loss_g = net.loss_backward()
+    g = net.get_grads()
+    gWs, gbs = net.unpack(g)
+    loss_o, gWo, gbo, out_o = co.loss_and_grads_bf16(x.astype(np.float64), t[..., :used].astype(np.float64),
+                                                      m.astype(np.float64), Ws, bs)
+    assert _rel(out, out_o) < 1e-3
+    assert abs(loss_g - loss_o) <= 1e-3 * loss_o
+    for l in range(len(Ws)):
+        assert _rel(gWs[l], gWo[l]) < 2e-2, l
+        assert _rel(gbs[l], gbo[l]) < 2e-2, l
+
+
+def test_net_training_reduces_loss(gpu):
+    """Fit a smooth target map (a fixed random 3x3 linear filter of the input)."""
+    from nextsimdg_gb300.surrogate import Net
+    rng = np.random.default_rng(2)
+    H = W = 24
+    net = Net([16, 32, 32, 16], H, W, max_batch=4, used_outputs=4, seed=1)
+    K = rng.standard_normal((3, 3, 16, 16)) * 0.1
+    x = rng.standard_normal((4, H, W, 16))
+    t = co.conv3x3(x, K, np.zeros(16)).astype(np.float32)
+    t[..., 4:] = 0
+    m = np.ones((4, H, W), dtype=np.float32)
+    net.set_batch(x, t, m)
+    losses = []
+    for _ in range(300):
+        net.forward()
+        losses.append(net.loss_backward())
+        net.adam_step(lr=3e-3)
+    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
