@@ -215,7 +215,7 @@ int nsdg_transport_mean_value(nsdg_transport* t, const double* phi, double* out)
 /* ======================================================================== */
 /* A stack of 3x3 convolutions (ReLU between layers) on the cell grid, trained
  * and evaluated on the GPU with BF16 tensor-core kernels accumulating in FP32.
- * channels: n_layers+1 counts, each 16, 32 or 48; the first `used_outputs`
+ * channels: n_layers+1 counts, each 16, 32, 48 or 64; the first `used_outputs`
  * output channels enter the masked mean-squared-error loss.  Parameters are
  * one FP32 vector: per layer the weights W[co][3*dy+dx][ci] then the biases. */
 typedef struct nsdg_net nsdg_net;
@@ -235,6 +235,64 @@ int nsdg_net_forward(nsdg_net* net, int batch, float* out_host);
 /* loss and gradients of the last forward pass (gradients stay on the device) */
 int nsdg_net_loss_backward(nsdg_net* net, int batch, float* loss);
 int nsdg_net_adam_step(nsdg_net* net, float lr, float beta1, float beta2, float eps);
+
+/* ---- learned warm start of the mEVP sub-cycle ----------------------------
+ * No counterpart in the reference, which always runs the fixed mEVP count
+ * (VPCGDynamicsKernel.hpp:76, DynamicsKernel.hpp:187: nSteps = 100).  The
+ * network maps, per cell, NSDG_WARM_FEATURES features of the state at the
+ * start of the sub-cycle (h, A, sea mask, u and v at the four CG2 nodes the
+ * cell owns, wind and ocean velocity, the 18 stress-divergence entries
+ * carried from the last sub-cycle, and the change of those u, v and
+ * divergence values since the start of the previous sub-cycle) to the
+ * increments of u, v and divergence that the plain sub-cycle reaches after
+ * n_steps - K iterations; the warm sub-cycle adds them and runs K iterations.
+ * Such a network has NSDG_WARM_FEATURES input channels, NSDG_WARM_TARGETS
+ * output channels and NSDG_WARM_USED used outputs; its height/width are the
+ * grid's ny/nx. */
+#define NSDG_WARM_FEATURES 64
+#define NSDG_WARM_TARGETS 32
+#define NSDG_WARM_USED 26
+#define NSDG_NET_NORM_FLOATS 192 /* feature mean[64], 1/std[64], target mean[32], std[32] */
+/* Device dataset of `capacity` samples (features, targets, mask per cell). */
+int nsdg_net_dataset_reserve(nsdg_net* net, int capacity);
+/* Per-channel mean/std of the first `count` samples over sea cells; the
+ * network normalises its inputs and outputs with them. */
+int nsdg_net_dataset_normalise(nsdg_net* net, int count);
+/* `iterations` Adam steps on random batches drawn (seeded) from the first
+ * `count` samples; *loss = mean loss of the last 20 steps. */
+int nsdg_net_train(nsdg_net* net, int count, int iterations, int batch, float lr,
+    unsigned long long seed, float* loss);
+int nsdg_net_get_normalisation(nsdg_net* net, float* host, size_t n);
+int nsdg_net_set_normalisation(nsdg_net* net, const float* host, size_t n);
+/* One plain model step, as nsdg_kernel_update (mEVP, mixed precision), that
+ * also writes dataset sample `slot` (slot < 0: none): the features at the
+ * start of the sub-cycle and the increments after n_steps - k_iters
+ * iterations.  *plain_ratio = |u^n - u^(n-1)| / |u^n - u^0| of the plain
+ * sub-cycle's last iteration (RMS over CG2 nodes: the warm-start residual). */
+int nsdg_kernel_warm_sample(nsdg_kernel* k, double t_start, double dt, int k_iters,
+    nsdg_net* net, int slot, double* plain_ratio);
+/* Attaches (net != NULL) or detaches the warm start.  Each later update runs
+ * network + k_iters iterations and accepts the result when the warm start is
+ * enabled, the attempt produced only finite values and its residual (as
+ * above) is at most `kappa`; otherwise it restores the state at the start of
+ * the sub-cycle and runs the plain n_steps iterations.  With judge_every > 0,
+ * the first update and every judge_every-th after it are judged: the warm
+ * attempt and the plain sub-cycle both run from the same start, the plain
+ * result is kept, and the warm start stays enabled until the next judgement
+ * only if |warm - plain| / |plain - start| (RMS over CG2 nodes) <= judge_tol.
+ * All decisions are taken on the device, inside the update's CUDA graphs.
+ * The net must stay alive while attached.  mEVP in mixed precision only
+ * (NSDG_ERR_UNSUPPORTED otherwise). */
+int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, double kappa,
+    int judge_every, double judge_tol);
+typedef struct nsdg_warm_stats {
+    long long accepted, fallbacks;       /* warm updates accepted / fallen back   */
+    long long judged, judge_rejected;    /* judged updates / judgements that disabled it */
+    double last_ratio, last_judged_error;
+    int enabled;                         /* current judgement                     */
+    int launches_warm, launches_judged, launches_fallback; /* kernels per graph    */
+} nsdg_warm_stats;
+int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
 
 /* ======================================================================== */
 /* Allocation-free entry point                                               */

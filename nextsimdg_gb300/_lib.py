@@ -26,6 +26,11 @@ RHEOLOGY_BBM = 1
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+WARM_FEATURES = 64
+WARM_TARGETS = 32
+WARM_USED = 26
+NET_NORM_FLOATS = 192
+
 
 class Params(ctypes.Structure):
     """nsdg_params (include/nsdg.h)."""
@@ -42,6 +47,20 @@ class Params(ctypes.Structure):
         ("exponent_compression_factor", c_double), ("tan_phi", c_double),
         ("compr_strength", c_double), ("C_lab", c_double),
         ("n_steps", c_int), ("precision", c_int),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class WarmStats(ctypes.Structure):
+    """nsdg_warm_stats (include/nsdg.h)."""
+
+    _fields_ = [
+        ("accepted", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
+        ("judged", ctypes.c_longlong), ("judge_rejected", ctypes.c_longlong),
+        ("last_ratio", c_double), ("last_judged_error", c_double),
+        ("enabled", c_int), ("launches_warm", c_int), ("launches_judged", c_int), ("launches_fallback", c_int),
     ]
 
     def as_dict(self):
@@ -98,6 +117,14 @@ SIGNATURES = [
     ("nsdg_net_forward", c_int, [c_void_p, c_int, c_void_p]),
     ("nsdg_net_loss_backward", c_int, [c_void_p, c_int, POINTER(c_float)]),
     ("nsdg_net_adam_step", c_int, [c_void_p, c_float, c_float, c_float, c_float]),
+    ("nsdg_net_dataset_reserve", c_int, [c_void_p, c_int]),
+    ("nsdg_net_dataset_normalise", c_int, [c_void_p, c_int]),
+    ("nsdg_net_train", c_int, [c_void_p, c_int, c_int, c_int, c_float, ctypes.c_ulonglong, POINTER(c_float)]),
+    ("nsdg_net_get_normalisation", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_net_set_normalisation", c_int, [c_void_p, c_void_p, c_size_t]),
+    ("nsdg_kernel_warm_sample", c_int, [c_void_p, c_double, c_double, c_int, c_void_p, c_int, POINTER(c_double)]),
+    ("nsdg_kernel_set_warm_start", c_int, [c_void_p, c_void_p, c_int, c_double, c_int, c_double]),
+    ("nsdg_kernel_warm_stats", c_int, [c_void_p, c_void_p]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 

@@ -8,6 +8,7 @@
 
 #include "nsdg_host.hpp"
 #include "nsdg_kernels.hpp"
+#include "nsdg_surrogate.hpp"
 
 #include <cmath>
 #include <cstdio>
@@ -115,6 +116,9 @@ struct nsdg_kernel {
     DevOps32 dops32;
     float* tdiv32 = nullptr;
     MevpNodeState32 st32 {};
+    // FP32 u, v and divergence at the start of the previous sub-cycle (the
+    // warm-start features), refreshed by every mixed-precision mEVP update
+    float *uLast = nullptr, *vLast = nullptr, *tdivLast = nullptr;
     bool mixed() const { return P.precision == NSDG_PRECISION_MIXED; }
     double *partials = nullptr, *dsum = nullptr;
     int* derr = nullptr;
@@ -126,6 +130,24 @@ struct nsdg_kernel {
     std::unordered_map<std::string, std::vector<double>> bucket;
     std::unordered_map<std::string, int> bucketComps;
     size_t stepNumber = 0;
+    // learned warm start (mixed-precision mEVP): the attached network, the
+    // iteration count after it, the acceptance bound, the judgement schedule,
+    // backups of the sub-cycle's starting state, the previous sub-cycle's
+    // starting state (features) and the device-side decision record
+    NetImpl* warmNet = nullptr;
+    int warmK = 0;
+    double warmKappa = 0.0;
+    int judgeEvery = 0;
+    double judgeTol = 0.0;
+    long long warmSteps = 0;   // updates since attaching
+    void* warmMem = nullptr;
+    float *bu = nullptr, *bv = nullptr, *btdiv = nullptr, *uPrev = nullptr, *vPrev = nullptr;
+    float* wbase = nullptr;
+    double *wPart = nullptr, *wRes = nullptr;
+    WarmRecord rec {};
+    cudaGraphExec_t judgeGraph = nullptr;
+    int judgeLaunches = 0;
+    int warmBodyLaunches = 0;
 
     int fail(int code, const std::string& m)
     {
@@ -137,8 +159,30 @@ struct nsdg_kernel {
         err.clear();
         return NSDG_OK;
     }
+    void dropGraphs()
+    {
+        if (graph)
+            cudaGraphExecDestroy(graph);
+        if (judgeGraph)
+            cudaGraphExecDestroy(judgeGraph);
+        graph = judgeGraph = nullptr;
+        graphDt = -1.0;
+        launchesPerUpdate = 0;
+    }
+    void releaseWarm()
+    {
+        if (warmMem)
+            cudaFree(warmMem);
+        warmMem = nullptr;
+        warmNet = nullptr;
+        warmK = 0;
+    }
     void releaseDevice()
     {
+        releaseWarm();
+        if (judgeGraph)
+            cudaGraphExecDestroy(judgeGraph);
+        judgeGraph = nullptr;
         if (graph)
             cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -157,6 +201,19 @@ struct nsdg_kernel {
     int enqueuePhases(cudaStream_t s, double dt, int phases, int& launches);
     int enqueueUpdate(double dt, int& launches) { return enqueuePhases(stream, dt, PHASE_ALL, launches); }
     int ensureGraph(double dt);
+    MevpParams mevpParams(double dt) const
+    {
+        return MevpParams { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, dt };
+    }
+    // `count` mixed-precision mEVP iterations, numeric faults to `errWord`
+    int mixedIterations(cudaStream_t s, double dt, int count, int* errWord, int& launches);
+    WarmState warmState() const;
+    int allocWarm();
+    int saveLast(cudaStream_t s, float* bu_, float* bv_, float* btdiv_);
+    int enqueueWarmFront(cudaStream_t s, double dt, int& launches);
+    int captureWarmGraph(double dt, cudaGraph_t& g, int& launches);
+    int captureJudgeGraph(double dt, cudaGraph_t& g, int& launches);
+    int launchStep(double dt);
     int checkDeviceError();
 };
 
@@ -265,6 +322,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         for (int i = 0; i < 4; ++i) add(81 * N, 4);
         add(18 * N, 4);
         for (int i = 0; i < 14; ++i) add(Ncg, 4);
+        add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -397,6 +455,9 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             &st32.c1b, &st32.fau, &st32.fav, &st32.rhfc, &st32.gu, &st32.gv };
         for (float** q : f32)
             *q = zf(Ncg);
+        tdivLast = zf(18 * N);
+        uLast = zf(Ncg);
+        vLast = zf(Ncg);
     }
     derr = arena.take<int>(1);
     if (!derr)
@@ -493,13 +554,19 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
     } // prep
     const int nS = P.n_steps;
     if (!bbm) {
-        MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, dt };
+        const MevpParams mp = mevpParams(dt);
         MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
         if (prep) {
             LCH(launchMevpPrepNodes(s, dm, st, mp));
             LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
             if (mixed())
                 LCH(launchMevpPrepNodes32(s, dm, st, st32));
+        }
+        if (loop && mixed()) {
+            const int sv = saveLast(s, nullptr, nullptr, nullptr);
+            if (sv != NSDG_OK)
+                return sv;
+            launches += 3;
         }
         if (loop) {
             for (int it = 0; it < nS; ++it) {
@@ -531,17 +598,269 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
     return NSDG_OK;
 }
 
+int nsdg_kernel::mixedIterations(cudaStream_t s, double dt, int count, int* errWord, int& launches)
+{
+    const MevpParams mp = mevpParams(dt);
+    for (int it = 0; it < count; ++it) {
+        cudaError_t e = launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp);
+        if (e == cudaSuccess)
+            e = launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, errWord);
+        if (e != cudaSuccess)
+            return fail(NSDG_ERR_CUDA, std::string("mEVP iteration: ") + cudaGetErrorString(e));
+        launches += 2;
+    }
+    return NSDG_OK;
+}
+
+WarmState nsdg_kernel::warmState() const
+{
+    WarmState w {};
+    w.nx = dm.nx;
+    w.ny = dm.ny;
+    w.N = N;
+    w.hice = hice; // component 0 of [dg][N] is the cell average
+    w.cice = cice;
+    w.ice = dm.ice;
+    w.cg2Dir = dm.cg2Dir;
+    w.u = st32.u;
+    w.v = st32.v;
+    w.ua = ua;
+    w.va = va;
+    w.uo = uo;
+    w.vo = vo;
+    w.tdiv = tdiv32;
+    w.uLast = uLast;
+    w.vLast = vLast;
+    w.tdivLast = tdivLast;
+    return w;
+}
+
+int nsdg_kernel::allocWarm()
+{
+    if (warmMem)
+        return NSDG_OK;
+    auto a = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t nPart = warmResidualPartials(Ncg);
+    const size_t bytes = 4 * a(Ncg * 4) + a(18 * N * 4) + a(N * kWarmUsed * 4) + a(nPart * 8) + a(2 * 8)
+        + a(4 * 8) + 2 * a(4) + 2 * a(8);
+    cudaError_t e = cudaMalloc(&warmMem, bytes);
+    if (e != cudaSuccess) {
+        warmMem = nullptr;
+        return fail(NSDG_ERR_CUDA, std::string("warm start: allocation failed: ") + cudaGetErrorString(e));
+    }
+    char* p = static_cast<char*>(warmMem);
+    auto take = [&](size_t b) { void* r = p; p += a(b); return r; };
+    bu = static_cast<float*>(take(Ncg * 4));
+    bv = static_cast<float*>(take(Ncg * 4));
+    uPrev = static_cast<float*>(take(Ncg * 4));
+    vPrev = static_cast<float*>(take(Ncg * 4));
+    btdiv = static_cast<float*>(take(18 * N * 4));
+    wbase = static_cast<float*>(take(N * kWarmUsed * 4));
+    wPart = static_cast<double*>(take(nPart * 8));
+    wRes = static_cast<double*>(take(2 * 8));
+    rec.counts = static_cast<long long*>(take(4 * 8));
+    rec.warmErr = static_cast<int*>(take(4));
+    rec.enabled = static_cast<int*>(take(4));
+    rec.lastRatio = static_cast<double*>(take(8));
+    rec.lastError = static_cast<double*>(take(8));
+    e = cudaMemset(warmMem, 0, bytes);
+    if (e == cudaSuccess) {
+        const int one = 1;
+        e = cudaMemcpy(rec.enabled, &one, sizeof(int), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm start: ") + cudaGetErrorString(e));
+    return NSDG_OK;
+}
+
+// (uLast, vLast, tdivLast) := the current sub-cycle's start, also copied to
+// the backups when given
+int nsdg_kernel::saveLast(cudaStream_t s, float* bu_, float* bv_, float* btdiv_)
+{
+    cudaError_t e = launchWarmSave(s, Ncg, st32.u, uLast, bu_);
+    if (e == cudaSuccess) e = launchWarmSave(s, Ncg, st32.v, vLast, bv_);
+    if (e == cudaSuccess) e = launchWarmSave(s, 18 * N, tdiv32, tdivLast, btdiv_);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("save sub-cycle start: ") + cudaGetErrorString(e));
+    return NSDG_OK;
+}
+
+// prep phase; features (network input); back up the sub-cycle's start into
+// (bu, bv, btdiv) and (uLast, vLast, tdivLast); network; increments; K
+// iterations with the warm error word, keeping the iterate before the last
+int nsdg_kernel::enqueueWarmFront(cudaStream_t s, double dt, int& launches)
+{
+    int l = 0;
+    int st = enqueuePhases(s, dt, PHASE_PREP, l);
+    launches += l;
+    if (st != NSDG_OK)
+        return st;
+    const WarmState ws = warmState();
+    cudaError_t e = launchWarmFeaturesNet(s, ws, warmNet);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm start: ") + cudaGetErrorString(e));
+    st = saveLast(s, bu, bv, btdiv);
+    if (st != NSDG_OK)
+        return st;
+    e = netForward(warmNet, s, 1);
+    if (e == cudaSuccess) e = launchWarmApply(s, ws, warmNet);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm start: ") + cudaGetErrorString(e));
+    launches += 5 + netLayers(warmNet);
+    st = mixedIterations(s, dt, warmK - 1, rec.warmErr, launches);
+    if (st != NSDG_OK)
+        return st;
+    e = launchWarmSave(s, Ncg, st32.u, uPrev, nullptr);
+    if (e == cudaSuccess) e = launchWarmSave(s, Ncg, st32.v, vPrev, nullptr);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm start: ") + cudaGetErrorString(e));
+    launches += 2;
+    return mixedIterations(s, dt, 1, rec.warmErr, launches);
+}
+
+// One update with the warm start, as a graph with a device-side fallback:
+//   A: warm front; residual; decision (sets the conditional)
+//   IF (fallback): restore u, v, tdiv; n_steps iterations
+//   C: finish phase
+int nsdg_kernel::captureWarmGraph(double dt, cudaGraph_t& g, int& launches)
+{
+    launches = 0;
+    g = nullptr;
+    CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm graph: conditional handle: ") + cudaGetErrorString(e));
+    std::vector<cudaGraphNode_t> tail;
+    int st = NSDG_OK;
+    // ---- part A
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    {
+        st = enqueueWarmFront(stream, dt, launches);
+        if (st == NSDG_OK) {
+            cudaError_t ee = launchWarmResidual(stream, Ncg, st32.u, st32.v, uPrev, vPrev, st32.u0, st32.v0, wPart,
+                wRes);
+            if (ee == cudaSuccess) ee = launchWarmDecide(stream, h, wRes, warmKappa, rec);
+            if (ee != cudaSuccess)
+                st = fail(NSDG_ERR_CUDA, std::string("warm graph: decision: ") + cudaGetErrorString(ee));
+            launches += 3;
+        }
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        if (e == cudaSuccess)
+            tail.assign(deps, deps + nd);
+        cudaGraph_t gg = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(stream, &gg);
+        if (st != NSDG_OK)
+            return st;
+        if (e != cudaSuccess || ec != cudaSuccess)
+            return fail(NSDG_ERR_CUDA, std::string("warm graph capture: ")
+                    + cudaGetErrorString(e != cudaSuccess ? e : ec));
+    }
+    // ---- the conditional fallback
+    cudaGraphNodeParams cp {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    e = cudaGraphAddNode(&cn, g, tail.data(), nullptr, tail.size(), &cp);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("warm graph: conditional node: ") + cudaGetErrorString(e));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    {
+        int l = 3;
+        cudaError_t ee = launchWarmSave(stream, Ncg, bu, st32.u, nullptr);
+        if (ee == cudaSuccess) ee = launchWarmSave(stream, Ncg, bv, st32.v, nullptr);
+        if (ee == cudaSuccess) ee = launchWarmSave(stream, 18 * N, btdiv, tdiv32, nullptr);
+        if (ee != cudaSuccess)
+            st = fail(NSDG_ERR_CUDA, std::string("warm graph: restore: ") + cudaGetErrorString(ee));
+        if (st == NSDG_OK)
+            st = mixedIterations(stream, dt, P.n_steps, derr, l);
+        warmBodyLaunches = l;
+        cudaGraph_t bb = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(stream, &bb);
+        if (st != NSDG_OK)
+            return st;
+        if (ec != cudaSuccess)
+            return fail(NSDG_ERR_CUDA, std::string("warm graph: fallback capture: ") + cudaGetErrorString(ec));
+    }
+    // ---- part C
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(stream, g, &cn, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+    {
+        int l = 0;
+        st = enqueuePhases(stream, dt, PHASE_FINISH, l);
+        launches += l;
+        cudaGraph_t gg = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(stream, &gg);
+        if (st != NSDG_OK)
+            return st;
+        if (ec != cudaSuccess)
+            return fail(NSDG_ERR_CUDA, std::string("warm graph: finish capture: ") + cudaGetErrorString(ec));
+    }
+    return NSDG_OK;
+}
+
+// A judged update: the warm attempt, then the plain sub-cycle from the same
+// start (its result is kept), and the relative distance between the two
+// decides whether the following updates may accept warm sub-cycles.
+int nsdg_kernel::captureJudgeGraph(double dt, cudaGraph_t& g, int& launches)
+{
+    launches = 0;
+    g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int st = enqueueWarmFront(stream, dt, launches);
+    if (st == NSDG_OK) {
+        cudaError_t e = launchWarmSave(stream, Ncg, st32.u, uPrev, nullptr); // the warm result
+        if (e == cudaSuccess) e = launchWarmSave(stream, Ncg, st32.v, vPrev, nullptr);
+        if (e == cudaSuccess) e = launchWarmSave(stream, Ncg, bu, st32.u, nullptr);
+        if (e == cudaSuccess) e = launchWarmSave(stream, Ncg, bv, st32.v, nullptr);
+        if (e == cudaSuccess) e = launchWarmSave(stream, 18 * N, btdiv, tdiv32, nullptr);
+        if (e != cudaSuccess)
+            st = fail(NSDG_ERR_CUDA, std::string("judge graph: ") + cudaGetErrorString(e));
+        launches += 5;
+    }
+    if (st == NSDG_OK)
+        st = mixedIterations(stream, dt, P.n_steps, derr, launches);
+    if (st == NSDG_OK) {
+        cudaError_t e = launchWarmResidual(stream, Ncg, st32.u, st32.v, uPrev, vPrev, st32.u0, st32.v0, wPart, wRes);
+        if (e == cudaSuccess) e = launchWarmJudge(stream, wRes, judgeTol, rec);
+        if (e != cudaSuccess)
+            st = fail(NSDG_ERR_CUDA, std::string("judge graph: ") + cudaGetErrorString(e));
+        launches += 3;
+    }
+    if (st == NSDG_OK) {
+        int l = 0;
+        st = enqueuePhases(stream, dt, PHASE_FINISH, l);
+        launches += l;
+    }
+    const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+    if (st != NSDG_OK)
+        return st;
+    if (ec != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("judge graph capture: ") + cudaGetErrorString(ec));
+    return NSDG_OK;
+}
+
 int nsdg_kernel::ensureGraph(double dt)
 {
     if (graph && graphDt == dt)
         return NSDG_OK;
-    if (graph) {
-        cudaGraphExecDestroy(graph);
-        graph = nullptr;
-    }
+    dropGraphs();
     cudaGraph_t g = nullptr;
-    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int launches = 0;
+    if (warmNet) {
+        const int st = captureWarmGraph(dt, g, launches);
+        if (st != NSDG_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return st;
+        }
+    } else {
+    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int st = enqueueUpdate(dt, launches);
     const cudaError_t ec = cudaStreamEndCapture(stream, &g);
     if (st != NSDG_OK) {
@@ -551,6 +870,7 @@ int nsdg_kernel::ensureGraph(double dt)
     }
     if (ec != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    }
     const cudaError_t ei = cudaGraphInstantiate(&graph, g, 0);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
@@ -559,6 +879,40 @@ int nsdg_kernel::ensureGraph(double dt)
     }
     graphDt = dt;
     launchesPerUpdate = launches;
+    if (warmNet && judgeEvery > 0) {
+        cudaGraph_t gj = nullptr;
+        const int st = captureJudgeGraph(dt, gj, judgeLaunches);
+        if (st != NSDG_OK) {
+            if (gj)
+                cudaGraphDestroy(gj);
+            return st;
+        }
+        const cudaError_t ej = cudaGraphInstantiate(&judgeGraph, gj, 0);
+        cudaGraphDestroy(gj);
+        if (ej != cudaSuccess) {
+            judgeGraph = nullptr;
+            return fail(NSDG_ERR_CUDA, std::string("judge graph instantiate: ") + cudaGetErrorString(ej));
+        }
+    }
+    return NSDG_OK;
+}
+
+// Launches the update graph of the next step: with a warm start attached and
+// judging on, every judgeEvery-th update (the first included) is a judged one.
+int nsdg_kernel::launchStep(double dt)
+{
+    int r = ensureGraph(dt);
+    if (r)
+        return r;
+    cudaGraphExec_t gx = graph;
+    if (warmNet && judgeEvery > 0 && warmSteps % judgeEvery == 0)
+        gx = judgeGraph;
+    const cudaError_t e = cudaGraphLaunch(gx, stream);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("update: ") + cudaGetErrorString(e));
+    if (warmNet)
+        ++warmSteps;
+    ++stepNumber;
     return NSDG_OK;
 }
 
@@ -751,14 +1105,8 @@ int nsdg_kernel_update(nsdg_kernel* k, double t_start, double dt)
         return k->fail(NSDG_ERR_BAD_ARG, "update: kernel not initialised");
     if (!(dt > 0) || !std::isfinite(dt))
         return k->fail(NSDG_ERR_BAD_ARG, "update: dt must be positive");
-    int r = k->ensureGraph(dt);
-    if (r)
-        return r;
-    const cudaError_t e = cudaGraphLaunch(k->graph, k->stream);
-    if (e != cudaSuccess)
-        return k->fail(NSDG_ERR_CUDA, std::string("update: ") + cudaGetErrorString(e));
-    ++k->stepNumber;
-    return k->ok();
+    const int r = k->launchStep(dt);
+    return r ? r : k->ok();
 }
 
 int nsdg_kernel_synchronize(nsdg_kernel* k)
@@ -879,8 +1227,12 @@ std::vector<std::pair<void*, size_t>> snapshotArrays(nsdg_kernel* k)
         { k->u, cg }, { k->v, cg }, { k->uo, cg }, { k->vo, cg }, { k->ua, cg }, { k->va, cg } };
     if (k->rheology == NSDG_RHEOLOGY_MEVP) {
         // the mEVP stress lives in divergence space (see kMevpStress)
-        if (k->mixed())
+        if (k->mixed()) {
             a.push_back({ k->tdiv32, 18 * k->N * sizeof(float) });
+            a.push_back({ k->tdivLast, 18 * k->N * sizeof(float) });
+            a.push_back({ k->uLast, k->Ncg * sizeof(float) });
+            a.push_back({ k->vLast, k->Ncg * sizeof(float) });
+        }
         else
             a.push_back({ k->contrib, 18 * k->N * sizeof(double) });
     } else {
@@ -1000,16 +1352,17 @@ int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms)
         return k->fail(NSDG_ERR_CUDA, "time_updates: event create failed");
     cudaError_t e = cudaStreamSynchronize(k->stream);
     if (e == cudaSuccess) e = cudaEventRecord(a, k->stream);
-    for (int i = 0; i < steps && e == cudaSuccess; ++i)
-        e = cudaGraphLaunch(k->graph, k->stream);
+    for (int i = 0; i < steps && e == cudaSuccess && r == NSDG_OK; ++i)
+        r = k->launchStep(dt);
     if (e == cudaSuccess) e = cudaEventRecord(b, k->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    if (r)
+        return r;
     if (e != cudaSuccess)
         return k->fail(NSDG_ERR_CUDA, std::string("time_updates: ") + cudaGetErrorString(e));
-    k->stepNumber += steps;
     r = k->checkDeviceError();
     return r ? r : k->ok();
 }
@@ -1099,6 +1452,160 @@ int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches)
             return r;
     }
     *launches = k->launchesPerUpdate;
+    return k->ok();
+}
+
+#define CUDA_TRY_K(expr)                                                                           \
+    do {                                                                                           \
+        cudaError_t e_ = (expr);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return k->fail(NSDG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));    \
+    } while (0)
+
+int nsdg_kernel_warm_sample(nsdg_kernel* k, double t_start, double dt, int k_iters, nsdg_net* net, int slot,
+    double* plain_ratio)
+{
+    (void)t_start;
+    if (!k || !net)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "warm_sample: kernel not initialised");
+    if (k->rheology != NSDG_RHEOLOGY_MEVP || !k->mixed())
+        return k->fail(NSDG_ERR_UNSUPPORTED, "warm_sample: mEVP in mixed precision only");
+    if (!(dt > 0) || !std::isfinite(dt))
+        return k->fail(NSDG_ERR_BAD_ARG, "warm_sample: dt must be positive");
+    NetImpl* n = netImplOf(net);
+    if (!netIsWarmShaped(n, k->dm.nx, k->dm.ny))
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "warm_sample: the network does not match the grid / warm-start layout");
+    if (slot >= netDatasetCapacity(n))
+        return k->fail(NSDG_ERR_BAD_ARG, "warm_sample: slot outside the reserved dataset");
+    if (k_iters < 1 || k_iters > k->P.n_steps)
+        return k->fail(NSDG_ERR_BAD_ARG, "warm_sample: k_iters must be in [1, n_steps]");
+    int r = k->allocWarm();
+    if (r)
+        return r;
+    cudaStream_t s = k->stream;
+    const bool record = slot >= 0;
+    int l = 0;
+    r = k->enqueuePhases(s, dt, nsdg_kernel::PHASE_PREP, l);
+    if (r)
+        return r;
+    const WarmState ws = k->warmState();
+    cudaError_t e = cudaSuccess;
+    if (record) {
+        e = launchWarmFeaturesRaw(s, ws, netDatasetFeatures(n, slot));
+        if (e == cudaSuccess) e = launchWarmBase(s, ws, k->wbase, netDatasetMask(n, slot));
+        if (e != cudaSuccess)
+            return k->fail(NSDG_ERR_CUDA, std::string("warm_sample: ") + cudaGetErrorString(e));
+    }
+    r = k->saveLast(s, nullptr, nullptr, nullptr);
+    if (r)
+        return r;
+    r = k->mixedIterations(s, dt, k->P.n_steps - k_iters, k->derr, l);
+    if (r)
+        return r;
+    if (record) {
+        e = launchWarmTargets(s, ws, k->wbase, netDatasetTargets(n, slot));
+        if (e != cudaSuccess)
+            return k->fail(NSDG_ERR_CUDA, std::string("warm_sample: ") + cudaGetErrorString(e));
+    }
+    r = k->mixedIterations(s, dt, k_iters - 1, k->derr, l);
+    if (r)
+        return r;
+    e = launchWarmSave(s, k->Ncg, k->st32.u, k->uPrev, nullptr);
+    if (e == cudaSuccess) e = launchWarmSave(s, k->Ncg, k->st32.v, k->vPrev, nullptr);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("warm_sample: ") + cudaGetErrorString(e));
+    r = k->mixedIterations(s, dt, 1, k->derr, l);
+    if (r)
+        return r;
+    e = launchWarmResidual(s, k->Ncg, k->st32.u, k->st32.v, k->uPrev, k->vPrev, k->st32.u0, k->st32.v0, k->wPart,
+        k->wRes);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("warm_sample: ") + cudaGetErrorString(e));
+    r = k->enqueuePhases(s, dt, nsdg_kernel::PHASE_FINISH, l);
+    if (r)
+        return r;
+    double res[2] = { 0, 0 };
+    e = cudaMemcpyAsync(res, k->wRes, sizeof(res), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("warm_sample: ") + cudaGetErrorString(e));
+    r = k->checkDeviceError();
+    if (r)
+        return r;
+    ++k->stepNumber;
+    if (plain_ratio)
+        *plain_ratio = res[1] > 0 ? std::sqrt(res[0] / res[1]) : 0.0;
+    return k->ok();
+}
+
+int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, double kappa, int judge_every,
+    double judge_tol)
+{
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: kernel not initialised");
+    if (k->stream)
+        cudaStreamSynchronize(k->stream);
+    if (!net) {
+        k->dropGraphs();
+        k->warmNet = nullptr;
+        k->warmK = 0;
+        return k->ok();
+    }
+    if (k->rheology != NSDG_RHEOLOGY_MEVP || !k->mixed())
+        return k->fail(NSDG_ERR_UNSUPPORTED, "set_warm_start: mEVP in mixed precision only");
+    NetImpl* n = netImplOf(net);
+    if (!netIsWarmShaped(n, k->dm.nx, k->dm.ny))
+        return k->fail(NSDG_ERR_SIZE_MISMATCH, "set_warm_start: the network does not match the grid / warm-start layout");
+    if (k_iters < 1 || k_iters > k->P.n_steps)
+        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: k_iters must be in [1, n_steps]");
+    if (!(kappa >= 0) || !std::isfinite(kappa))
+        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: kappa must be finite and non-negative");
+    if (judge_every < 0 || (judge_every > 0 && (!(judge_tol >= 0) || !std::isfinite(judge_tol))))
+        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: judge_every >= 0 and a finite judge_tol >= 0 needed");
+    k->dropGraphs();
+    const int r = k->allocWarm();
+    if (r)
+        return r;
+    const int one = 1;
+    CUDA_TRY_K(cudaMemsetAsync(k->rec.counts, 0, 4 * sizeof(long long), k->stream));
+    CUDA_TRY_K(cudaMemcpyAsync(k->rec.enabled, &one, sizeof(int), cudaMemcpyHostToDevice, k->stream));
+    CUDA_TRY_K(cudaStreamSynchronize(k->stream));
+    k->warmNet = n;
+    k->warmK = k_iters;
+    k->warmKappa = kappa;
+    k->judgeEvery = judge_every;
+    k->judgeTol = judge_tol;
+    k->warmSteps = 0;
+    return k->ok();
+}
+
+int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out)
+{
+    if (!k || !out)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready || !k->warmMem)
+        return k->fail(NSDG_ERR_BAD_ARG, "warm_stats: no warm start attached");
+    long long c[4] = { 0, 0, 0, 0 };
+    double last[2] = { 0, 0 };
+    int enabled = 0;
+    CUDA_TRY_K(cudaMemcpyAsync(c, k->rec.counts, sizeof(c), cudaMemcpyDeviceToHost, k->stream));
+    CUDA_TRY_K(cudaMemcpyAsync(&last[0], k->rec.lastRatio, sizeof(double), cudaMemcpyDeviceToHost, k->stream));
+    CUDA_TRY_K(cudaMemcpyAsync(&last[1], k->rec.lastError, sizeof(double), cudaMemcpyDeviceToHost, k->stream));
+    CUDA_TRY_K(cudaMemcpyAsync(&enabled, k->rec.enabled, sizeof(int), cudaMemcpyDeviceToHost, k->stream));
+    CUDA_TRY_K(cudaStreamSynchronize(k->stream));
+    out->accepted = c[0];
+    out->fallbacks = c[1];
+    out->judged = c[2];
+    out->judge_rejected = c[3];
+    out->last_ratio = last[0];
+    out->last_judged_error = last[1];
+    out->enabled = enabled;
+    out->launches_warm = k->launchesPerUpdate;
+    out->launches_judged = k->judgeLaunches;
+    out->launches_fallback = k->warmBodyLaunches;
     return k->ok();
 }
 

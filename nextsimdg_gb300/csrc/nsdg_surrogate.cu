@@ -261,10 +261,11 @@ __global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, f
 // Masked MSE: gz = 2 m (out - target) / denom for the first `used` channels
 // (BF16, zero in the padding), per-block partial losses.
 __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const float* __restrict__ out,
-    const float* __restrict__ target, const float* __restrict__ mask, float invDenom, __nv_bfloat16* __restrict__ gz,
-    float* __restrict__ partial)
+    const float* __restrict__ target, const float* __restrict__ mask, const float* __restrict__ invDenomPtr,
+    __nv_bfloat16* __restrict__ gz, float* __restrict__ partial)
 {
     __shared__ float ws[8];
+    const float invDenom = *invDenomPtr;
     const long m = blockIdx.x * long(blockDim.x) + threadIdx.x;
     float s = 0.f;
     if (m < M) {
@@ -289,6 +290,27 @@ __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const floa
         for (int w = 0; w < 8; ++w)
             t += ws[w];
         partial[blockIdx.x] = t * invDenom;
+    }
+}
+
+// 1 / (sum of the mask * used channels), one block, fixed summation order
+__global__ void __launch_bounds__(1024) kInvDenom(long M, int used, const float* __restrict__ mask,
+    float* __restrict__ invDenom)
+{
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (long m = threadIdx.x; m < M; m += blockDim.x)
+        s += mask[m];
+    for (int off = 16; off > 0; off >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 32; ++w)
+            t += ws[w];
+        *invDenom = t > 0.0 ? static_cast<float>(1.0 / (t * used)) : 0.f;
     }
 }
 
@@ -338,12 +360,13 @@ cudaError_t conv(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src, 
     return cudaGetLastError();
 }
 
-// channel counts supported by the instantiations: 16, 32, 48
+// channel counts supported by the instantiations: 16, 32, 48, 64
 #define NSDG_CH_SWITCH(c, D, CALL)                                                                 \
     switch (c) {                                                                                   \
     case 16: { constexpr int D = 16; CALL; } break;                                                \
     case 32: { constexpr int D = 32; CALL; } break;                                                \
     case 48: { constexpr int D = 48; CALL; } break;                                                \
+    case 64: { constexpr int D = 64; CALL; } break;                                                \
     default: return cudaErrorInvalidValue;                                                         \
     }
 
@@ -372,6 +395,13 @@ struct NetImpl {
     size_t partFloats = 0;
     int adamStep = 0;
     std::string err;
+    // dataset (raw FP32) and normalisation
+    void* dsMem = nullptr;
+    int dsCap = 0;
+    float *dsX = nullptr, *dsY = nullptr, *dsM = nullptr;
+    float* stats = nullptr; // device: featShift[kWarmFeat], featInv[kWarmFeat], tgtShift[kWarmTgt], tgtScale[kWarmTgt]
+    int* dIdx = nullptr;    // batch sample indices
+    double* dPart = nullptr;
 };
 
 namespace {
@@ -386,8 +416,8 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
         return NSDG_ERR_BAD_ARG;
     }
     for (int l = 0; l <= L; ++l)
-        if (channels[l] != 16 && channels[l] != 32 && channels[l] != 48) {
-            err = "channel counts must be 16, 32 or 48";
+        if (channels[l] != 16 && channels[l] != 32 && channels[l] != 48 && channels[l] != 64) {
+            err = "channel counts must be 16, 32, 48 or 64";
             return NSDG_ERR_BAD_ARG;
         }
     if (used < 1 || used > channels[L]) {
@@ -418,11 +448,12 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     for (int l = 0; l < L; ++l)
         wmax = std::max(wmax, size_t(n->ch[l + 1]) * 9 * n->ch[l]);
     n->partFloats = size_t(nChunks) * wmax;
-    size_t bytes = 4 * a256(n->nParams * 4) + 2 * a256(n->nParams * 2);
+    size_t bytes = 4 * a256(n->nParams * 4) + 2 * a256(n->nParams * 2) + a256(kWarmNorm * 4)
+        + a256(size_t(maxB) * 4);
     for (int l = 0; l < L; ++l)
         bytes += a256(size_t(M) * n->ch[l] * 2);
     bytes += 2 * a256(size_t(M) * n->ch[L] * 4) + a256(size_t(M) * 4) + 2 * a256(size_t(M) * cmax * 2)
-        + a256(n->partFloats * 4) + a256(size_t((M + 255) / 256 + 1) * 4);
+        + a256(n->partFloats * 4) + a256(size_t((M + 255) / 256 + 2) * 4);
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess
         || cudaMalloc(&n->mem, bytes) != cudaSuccess) {
         err = "network: device allocation failed";
@@ -451,7 +482,9 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     n->gA = static_cast<__nv_bfloat16*>(take(size_t(M) * cmax * 2));
     n->gB = static_cast<__nv_bfloat16*>(take(size_t(M) * cmax * 2));
     n->part = static_cast<float*>(take(n->partFloats * 4));
-    n->lossPart = static_cast<float*>(take(size_t((M + 255) / 256 + 1) * 4));
+    n->lossPart = static_cast<float*>(take(size_t((M + 255) / 256 + 2) * 4));
+    n->stats = static_cast<float*>(take(kWarmNorm * 4));
+    n->dIdx = static_cast<int*>(take(size_t(maxB) * 4));
     // He-normal initial weights, zero biases (host RNG: reproducible)
     std::vector<float> w(n->nParams, 0.f);
     std::mt19937_64 rng(seed);
@@ -466,6 +499,15 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     if (e == cudaSuccess) e = cudaMemset(n->m2, 0, n->nParams * 4);
     if (e == cudaSuccess) e = cudaMemset(n->mask, 0, size_t(M) * 4);
     if (e == cudaSuccess) e = cudaMemset(n->target, 0, size_t(M) * n->ch[L] * 4);
+    if (e == cudaSuccess) {
+        // identity normalisation until a dataset sets it
+        std::vector<float> st(kWarmNorm, 0.f);
+        for (int c = 0; c < kWarmFeat; ++c)
+            st[kWarmFeat + c] = 1.f;
+        for (int c = 0; c < kWarmTgt; ++c)
+            st[2 * kWarmFeat + kWarmTgt + c] = 1.f;
+        e = cudaMemcpy(n->stats, st.data(), st.size() * 4, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = netRefresh(n);
     if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
     if (e != cudaSuccess) {
@@ -483,6 +525,8 @@ void netDestroy(NetImpl* n)
         return;
     if (n->stream)
         cudaStreamSynchronize(n->stream);
+    if (n->dsMem)
+        cudaFree(n->dsMem);
     if (n->mem)
         cudaFree(n->mem);
     if (n->stream)
@@ -537,16 +581,10 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
     cudaStream_t s = n->stream;
     const long M = long(B) * n->H * n->W;
     const int CL = n->ch[n->L];
-    // denominator: sum of the mask times the used channels (host-side sum of the device mask)
-    std::vector<float> hm(M);
-    cudaError_t e = cudaMemcpyAsync(hm.data(), n->mask, M * 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess)
-        return e;
-    double msum = 0;
-    for (float v : hm)
-        msum += v;
-    const float invDenom = msum > 0 ? static_cast<float>(1.0 / (msum * n->used)) : 0.f;
+    // denominator: sum of the mask times the used channels
+    cudaError_t e = cudaSuccess;
+    float* invDenom = n->lossPart + (long(n->maxB) * n->H * n->W + 255) / 256 + 1;
+    kInvDenom<<<1, 1024, 0, s>>>(M, n->used, n->mask, invDenom);
     const unsigned lb = static_cast<unsigned>((M + 255) / 256);
     kLoss<<<lb, 256, 0, s>>>(M, CL, n->used, n->out, n->target, n->mask, invDenom, n->gA, n->lossPart);
     kSumChunks<<<1, 1, 0, s>>>(static_cast<int>(lb), 1, n->lossPart, lossDev);
@@ -592,6 +630,498 @@ cudaError_t netInputFromFloat(NetImpl* n, long count, const float* dev)
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Warm start: features, targets, increments, residual
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ size_t ownedNode(int nx, int i, int j, int q)
+{
+    const int i2 = 2 * i + 1 + (q & 1), j2 = 2 * j + 1 + (q >> 1);
+    return size_t(j2) * (2 * nx + 1) + i2;
+}
+
+__device__ __forceinline__ void warmFeature(const WarmState& w, size_t e, float* f)
+{
+    const int i = static_cast<int>(e % w.nx), j = static_cast<int>(e / w.nx);
+    f[0] = static_cast<float>(w.hice[e]);
+    f[1] = static_cast<float>(w.cice[e]);
+    f[2] = w.ice[e] ? 1.f : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const size_t nd = ownedNode(w.nx, i, j, q);
+        const float u = w.u[nd], v = w.v[nd];
+        f[3 + q] = u;
+        f[7 + q] = v;
+        f[33 + q] = u - w.uLast[nd];
+        f[37 + q] = v - w.vLast[nd];
+    }
+    const size_t c = ownedNode(w.nx, i, j, 0);
+    f[11] = static_cast<float>(w.ua[c]);
+    f[12] = static_cast<float>(w.va[c]);
+    f[13] = static_cast<float>(w.uo[c]);
+    f[14] = static_cast<float>(w.vo[c]);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+        const float t = w.tdiv[k * w.N + e];
+        f[15 + k] = t;
+        f[41 + k] = t - w.tdivLast[k * w.N + e];
+    }
+#pragma unroll
+    for (int k = 59; k < kWarmFeat; ++k)
+        f[k] = 0.f;
+}
+
+__global__ void kWarmFeaturesRaw(WarmState w, float* __restrict__ out)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= w.N)
+        return;
+    float f[kWarmFeat];
+    warmFeature(w, e, f);
+#pragma unroll
+    for (int k = 0; k < kWarmFeat; ++k)
+        out[e * kWarmFeat + k] = f[k];
+}
+
+__global__ void kWarmFeaturesNet(WarmState w, const float* __restrict__ stats, __nv_bfloat16* __restrict__ in)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= w.N)
+        return;
+    float f[kWarmFeat];
+    warmFeature(w, e, f);
+#pragma unroll
+    for (int k = 0; k < kWarmFeat; ++k)
+        in[e * kWarmFeat + k] = __float2bfloat16_rn((f[k] - stats[k]) * stats[kWarmFeat + k]);
+}
+
+__device__ __forceinline__ void warmCurrent(const WarmState& w, size_t e, float* t)
+{
+    const int i = static_cast<int>(e % w.nx), j = static_cast<int>(e / w.nx);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const size_t nd = ownedNode(w.nx, i, j, q);
+        t[q] = w.u[nd];
+        t[4 + q] = w.v[nd];
+    }
+#pragma unroll
+    for (int k = 0; k < 18; ++k)
+        t[8 + k] = w.tdiv[k * w.N + e];
+}
+
+__global__ void kWarmBase(WarmState w, float* __restrict__ base, float* __restrict__ mask)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= w.N)
+        return;
+    mask[e] = w.ice[e] ? 1.f : 0.f;
+    float t[kWarmUsed];
+    warmCurrent(w, e, t);
+#pragma unroll
+    for (int k = 0; k < kWarmUsed; ++k)
+        base[e * kWarmUsed + k] = t[k];
+}
+
+__global__ void kWarmTargets(WarmState w, const float* __restrict__ base, float* __restrict__ out)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= w.N)
+        return;
+    float t[kWarmUsed];
+    warmCurrent(w, e, t);
+#pragma unroll
+    for (int k = 0; k < kWarmTgt; ++k)
+        out[e * kWarmTgt + k] = k < kWarmUsed ? t[k] - base[e * kWarmUsed + k] : 0.f;
+}
+
+__global__ void kWarmApply(WarmState w, const float* __restrict__ netOut, const float* __restrict__ stats)
+{
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= w.N)
+        return;
+    const float* tShift = stats + 2 * kWarmFeat;
+    const float* tScale = tShift + kWarmTgt;
+    const int i = static_cast<int>(e % w.nx), j = static_cast<int>(e / w.nx);
+    const float* o = netOut + e * kWarmTgt;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const size_t nd = ownedNode(w.nx, i, j, q);
+        if (!w.cg2Dir[nd]) {
+            w.u[nd] += o[q] * tScale[q] + tShift[q];
+            w.v[nd] += o[4 + q] * tScale[4 + q] + tShift[4 + q];
+        }
+    }
+    if (w.ice[e]) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k)
+            w.tdiv[k * w.N + e] += o[8 + k] * tScale[8 + k] + tShift[8 + k];
+    }
+}
+
+__global__ void __launch_bounds__(256) kWarmResidualPartial(size_t n, const float* __restrict__ u,
+    const float* __restrict__ v, const float* __restrict__ up, const float* __restrict__ vp,
+    const float* __restrict__ u0, const float* __restrict__ v0, double* __restrict__ partial)
+{
+    __shared__ double ws[2][8];
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    double r = 0.0, d = 0.0;
+    if (i < n) {
+        const double a = double(u[i]) - up[i], b = double(v[i]) - vp[i];
+        const double c = double(u[i]) - u0[i], dd = double(v[i]) - v0[i];
+        r = a * a + b * b;
+        d = c * c + dd * dd;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        r += __shfl_down_sync(0xffffffffu, r, off);
+        d += __shfl_down_sync(0xffffffffu, d, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ws[0][threadIdx.x >> 5] = r;
+        ws[1][threadIdx.x >> 5] = d;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sr = 0.0, sd = 0.0;
+        for (int k = 0; k < 8; ++k) {
+            sr += ws[0][k];
+            sd += ws[1][k];
+        }
+        partial[2 * blockIdx.x] = sr;
+        partial[2 * blockIdx.x + 1] = sd;
+    }
+}
+__global__ void kWarmResidualFinal(size_t nb, const double* __restrict__ partial, double* __restrict__ out)
+{
+    double sr = 0.0, sd = 0.0;
+    for (size_t b = 0; b < nb; ++b) {
+        sr += partial[2 * b];
+        sd += partial[2 * b + 1];
+    }
+    out[0] = sr;
+    out[1] = sd;
+}
+
+// dataset -> network batch (normalised)
+__global__ void kGatherBatch(long N, int B, const int* __restrict__ idx, const float* __restrict__ X,
+    const float* __restrict__ Y, const float* __restrict__ M, const float* __restrict__ stats,
+    __nv_bfloat16* __restrict__ in, float* __restrict__ tgt, float* __restrict__ mask)
+{
+    const long t = blockIdx.x * long(blockDim.x) + threadIdx.x;
+    if (t >= long(B) * N)
+        return;
+    const int b = static_cast<int>(t / N);
+    const long p = t - long(b) * N;
+    const long src = long(idx[b]) * N + p;
+#pragma unroll 4
+    for (int k = 0; k < kWarmFeat; ++k)
+        in[t * kWarmFeat + k] = __float2bfloat16_rn((X[src * kWarmFeat + k] - stats[k]) * stats[kWarmFeat + k]);
+    const float* tShift = stats + 2 * kWarmFeat;
+    const float* tScale = tShift + kWarmTgt;
+#pragma unroll 4
+    for (int k = 0; k < kWarmTgt; ++k)
+        tgt[t * kWarmTgt + k] = k < kWarmUsed ? (Y[src * kWarmTgt + k] - tShift[k]) / tScale[k] : 0.f;
+    mask[t] = M[src];
+}
+
+// per-channel sums and sums of squares over `rows` rows of `C` channels (masked
+// rows only), one partial per block
+__global__ void kChannelMoments(long rows, int C, const float* __restrict__ a, const float* __restrict__ maskRows,
+    double* __restrict__ partial)
+{
+    const int c = blockIdx.y;
+    double s = 0.0, s2 = 0.0;
+    for (long r = blockIdx.x * long(blockDim.x) + threadIdx.x; r < rows; r += long(gridDim.x) * blockDim.x) {
+        if (maskRows[r] == 0.f)
+            continue;
+        const double v = a[r * C + c];
+        s += v;
+        s2 += v * v;
+    }
+    __shared__ double ws[2][8];
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        s2 += __shfl_down_sync(0xffffffffu, s2, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ws[0][threadIdx.x >> 5] = s;
+        ws[1][threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a0 = 0, a1 = 0;
+        for (int k = 0; k < 8; ++k) {
+            a0 += ws[0][k];
+            a1 += ws[1][k];
+        }
+        partial[(long(c) * gridDim.x + blockIdx.x) * 2] = a0;
+        partial[(long(c) * gridDim.x + blockIdx.x) * 2 + 1] = a1;
+    }
+}
+
+__global__ void kWarmDecide(cudaGraphConditionalHandle h, const double* __restrict__ res, double kappa,
+    WarmRecord rec)
+{
+    const double r = res[0], d = res[1];
+    const double ratio = d > 0.0 ? sqrt(r / d) : (r > 0.0 ? INFINITY : 0.0);
+    const bool ok = *rec.enabled != 0 && *rec.warmErr == 0 && isfinite(r) && isfinite(d) && ratio <= kappa;
+    *rec.lastRatio = ratio;
+    rec.counts[ok ? 0 : 1] += 1;
+    *rec.warmErr = 0;
+    cudaGraphSetConditional(h, ok ? 0u : 1u);
+}
+
+__global__ void kWarmJudge(const double* __restrict__ res, double tol, WarmRecord rec)
+{
+    const double r = res[0], d = res[1];
+    const double err = d > 0.0 ? sqrt(r / d) : (r > 0.0 ? INFINITY : 0.0);
+    const bool ok = *rec.warmErr == 0 && isfinite(r) && isfinite(d) && err <= tol;
+    *rec.lastError = err;
+    *rec.enabled = ok ? 1 : 0;
+    rec.counts[2] += 1;
+    if (!ok)
+        rec.counts[3] += 1;
+    *rec.warmErr = 0;
+}
+
+__global__ void kWarmSave(size_t n, const float* __restrict__ src, float* __restrict__ d1, float* __restrict__ d2)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i < n) {
+        const float x = src[i];
+        d1[i] = x;
+        if (d2)
+            d2[i] = x;
+    }
+}
+
+__global__ void kNarrow(size_t n, const double* __restrict__ src, float* __restrict__ dst)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i < n)
+        dst[i] = static_cast<float>(src[i]);
+}
+
+__global__ void kCopyF32(size_t n, const float* __restrict__ src, float* __restrict__ dst)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i < n)
+        dst[i] = src[i];
+}
+
+unsigned gridOf(size_t n) { return static_cast<unsigned>((n + 255) / 256); }
+
+} // namespace
+
+cudaError_t launchWarmDecide(cudaStream_t s, cudaGraphConditionalHandle h, const double* res, double kappa,
+    const WarmRecord& rec)
+{
+    kWarmDecide<<<1, 1, 0, s>>>(h, res, kappa, rec);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmJudge(cudaStream_t s, const double* res, double tol, const WarmRecord& rec)
+{
+    kWarmJudge<<<1, 1, 0, s>>>(res, tol, rec);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmSave(cudaStream_t s, size_t n, const float* src, float* dst1, float* dst2)
+{
+    kWarmSave<<<gridOf(n), 256, 0, s>>>(n, src, dst1, dst2);
+    return cudaGetLastError();
+}
+cudaError_t launchNarrow(cudaStream_t s, size_t n, const double* src, float* dst)
+{
+    kNarrow<<<gridOf(n), 256, 0, s>>>(n, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launchCopyF32(cudaStream_t s, size_t n, const float* src, float* dst)
+{
+    kCopyF32<<<gridOf(n), 256, 0, s>>>(n, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launchWarmFeaturesRaw(cudaStream_t s, const WarmState& w, float* out)
+{
+    kWarmFeaturesRaw<<<gridOf(w.N), 256, 0, s>>>(w, out);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmFeaturesNet(cudaStream_t s, const WarmState& w, NetImpl* net)
+{
+    kWarmFeaturesNet<<<gridOf(w.N), 256, 0, s>>>(w, net->stats, net->act[0]);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmBase(cudaStream_t s, const WarmState& w, float* base, float* mask)
+{
+    kWarmBase<<<gridOf(w.N), 256, 0, s>>>(w, base, mask);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmTargets(cudaStream_t s, const WarmState& w, const float* base, float* out)
+{
+    kWarmTargets<<<gridOf(w.N), 256, 0, s>>>(w, base, out);
+    return cudaGetLastError();
+}
+cudaError_t launchWarmApply(cudaStream_t s, const WarmState& w, NetImpl* net)
+{
+    kWarmApply<<<gridOf(w.N), 256, 0, s>>>(w, net->out, net->stats);
+    return cudaGetLastError();
+}
+size_t warmResidualPartials(size_t n) { return 2 * gridOf(n); }
+cudaError_t launchWarmResidual(cudaStream_t s, size_t n, const float* u, const float* v, const float* uPrev,
+    const float* vPrev, const float* u0, const float* v0, double* partial, double* out)
+{
+    kWarmResidualPartial<<<gridOf(n), 256, 0, s>>>(n, u, v, uPrev, vPrev, u0, v0, partial);
+    kWarmResidualFinal<<<1, 1, 0, s>>>(gridOf(n), partial, out);
+    return cudaGetLastError();
+}
+
+bool netIsWarmShaped(NetImpl* n, int nx, int ny)
+{
+    return n && n->W == nx && n->H == ny && n->ch[0] == kWarmFeat && n->ch[n->L] == kWarmTgt
+        && n->used == kWarmUsed;
+}
+
+int netDatasetReserve(NetImpl* n, int capacity, std::string& err)
+{
+    if (capacity < 1) {
+        err = "dataset capacity must be positive";
+        return NSDG_ERR_BAD_ARG;
+    }
+    if (n->ch[0] != kWarmFeat || n->ch[n->L] != kWarmTgt) {
+        err = "the dataset needs a network with the warm-start input and output channel counts";
+        return NSDG_ERR_BAD_ARG;
+    }
+    const size_t N = size_t(n->H) * n->W;
+    const size_t bytes = a256(size_t(capacity) * N * kWarmFeat * 4) + a256(size_t(capacity) * N * kWarmTgt * 4)
+        + a256(size_t(capacity) * N * 4) + a256(size_t(2) * 80 * 1024 * 8);
+    if (n->dsMem)
+        cudaFree(n->dsMem);
+    n->dsMem = nullptr;
+    if (cudaMalloc(&n->dsMem, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        err = "dataset: device allocation failed";
+        return NSDG_ERR_CUDA;
+    }
+    char* p = static_cast<char*>(n->dsMem);
+    n->dsX = reinterpret_cast<float*>(p);
+    p += a256(size_t(capacity) * N * kWarmFeat * 4);
+    n->dsY = reinterpret_cast<float*>(p);
+    p += a256(size_t(capacity) * N * kWarmTgt * 4);
+    n->dsM = reinterpret_cast<float*>(p);
+    p += a256(size_t(capacity) * N * 4);
+    n->dPart = reinterpret_cast<double*>(p);
+    n->dsCap = capacity;
+    return NSDG_OK;
+}
+float* netDatasetFeatures(NetImpl* n, int slot) { return n->dsX + size_t(slot) * n->H * n->W * kWarmFeat; }
+float* netDatasetTargets(NetImpl* n, int slot) { return n->dsY + size_t(slot) * n->H * n->W * kWarmTgt; }
+float* netDatasetMask(NetImpl* n, int slot) { return n->dsM + size_t(slot) * n->H * n->W; }
+int netDatasetCapacity(NetImpl* n) { return n->dsCap; }
+
+int netDatasetNormalise(NetImpl* n, int count, std::string& err)
+{
+    if (count < 1 || count > n->dsCap) {
+        err = "normalise: bad sample count";
+        return NSDG_ERR_BAD_ARG;
+    }
+    const long rows = long(count) * n->H * n->W;
+    const int blocks = 80;
+    std::vector<float> st(2 * kWarmFeat + 2 * kWarmTgt, 0.f);
+    // number of sea cells: the mask's own masked sum
+    double msum = 0;
+    {
+        kChannelMoments<<<dim3(blocks, 1), 256, 0, n->stream>>>(rows, 1, n->dsM, n->dsM, n->dPart);
+        std::vector<double> part(size_t(2) * blocks);
+        cudaError_t e = cudaMemcpyAsync(part.data(), n->dPart, part.size() * 8, cudaMemcpyDeviceToHost, n->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+        if (e != cudaSuccess) {
+            err = std::string("normalise: ") + cudaGetErrorString(e);
+            return NSDG_ERR_CUDA;
+        }
+        for (int b = 0; b < blocks; ++b)
+            msum += part[2 * b];
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        const int C = pass == 0 ? kWarmFeat : kWarmTgt;
+        const float* a = pass == 0 ? n->dsX : n->dsY;
+        kChannelMoments<<<dim3(blocks, C), 256, 0, n->stream>>>(rows, C, a, n->dsM, n->dPart);
+        std::vector<double> part(size_t(2) * blocks * C);
+        cudaError_t e = cudaMemcpyAsync(part.data(), n->dPart, part.size() * 8, cudaMemcpyDeviceToHost, n->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+        if (e != cudaSuccess) {
+            err = std::string("normalise: ") + cudaGetErrorString(e);
+            return NSDG_ERR_CUDA;
+        }
+        for (int c = 0; c < C; ++c) {
+            double s = 0, s2 = 0;
+            for (int b = 0; b < blocks; ++b) {
+                s += part[(size_t(c) * blocks + b) * 2];
+                s2 += part[(size_t(c) * blocks + b) * 2 + 1];
+            }
+            const double mean = msum > 0 ? s / msum : 0.0;
+            const double var = msum > 0 ? std::max(s2 / msum - mean * mean, 0.0) : 0.0;
+            const double sd = std::sqrt(var);
+            if (pass == 0) {
+                st[c] = static_cast<float>(mean);
+                st[kWarmFeat + c] = sd > 1e-30 ? static_cast<float>(1.0 / sd) : 0.f;
+            } else {
+                st[2 * kWarmFeat + c] = static_cast<float>(mean);
+                st[2 * kWarmFeat + kWarmTgt + c] = sd > 1e-30 ? static_cast<float>(sd) : 1.f;
+            }
+        }
+    }
+    if (cudaMemcpy(n->stats, st.data(), st.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        err = "normalise: upload failed";
+        return NSDG_ERR_CUDA;
+    }
+    return NSDG_OK;
+}
+
+int netTrain(NetImpl* n, int count, int iterations, int batch, float lr, unsigned long long seed, float* loss,
+    std::string& err)
+{
+    if (count < 1 || count > n->dsCap || batch < 1 || batch > n->maxB || iterations < 1) {
+        err = "train: bad arguments";
+        return NSDG_ERR_BAD_ARG;
+    }
+    std::mt19937_64 rng(seed);
+    std::uniform_int_distribution<int> pick(0, count - 1);
+    const long N = long(n->H) * n->W;
+    std::vector<int> idx(batch);
+    float* lossDev = n->lossPart + (N * n->maxB + 255) / 256; // one spare float after the loss partials
+    std::vector<float> last;
+    for (int it = 0; it < iterations; ++it) {
+        for (int& i : idx)
+            i = pick(rng);
+        cudaError_t e = cudaMemcpyAsync(n->dIdx, idx.data(), batch * 4, cudaMemcpyHostToDevice, n->stream);
+        if (e == cudaSuccess) {
+            const long T = long(batch) * N;
+            kGatherBatch<<<static_cast<unsigned>((T + 255) / 256), 256, 0, n->stream>>>(N, batch, n->dIdx, n->dsX,
+                n->dsY, n->dsM, n->stats, n->act[0], n->target, n->mask);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = netForward(n, n->stream, batch);
+        if (e == cudaSuccess) e = netLossBackward(n, batch, lossDev);
+        if (e == cudaSuccess) e = netAdam(n, lr, 0.9f, 0.999f, 1e-8f);
+        float l = 0.f;
+        if (e == cudaSuccess && it + 20 >= iterations) {
+            e = cudaMemcpyAsync(&l, lossDev, 4, cudaMemcpyDeviceToHost, n->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+            last.push_back(l);
+        }
+        if (e != cudaSuccess) {
+            err = std::string("train: ") + cudaGetErrorString(e);
+            return NSDG_ERR_CUDA;
+        }
+    }
+    double s = 0;
+    for (float v : last)
+        s += v;
+    if (loss)
+        *loss = static_cast<float>(s / std::max<size_t>(1, last.size()));
+    return NSDG_OK;
+}
+
 } // namespace nsdg
 
 // ===========================================================================
@@ -604,6 +1134,8 @@ struct nsdg_net {
     size_t stagingFloats = 0;
     float* lossDev = nullptr;
 };
+
+nsdg::NetImpl* nsdg::netImplOf(nsdg_net* h) { return h ? h->impl : nullptr; }
 
 using namespace nsdg;
 
@@ -749,6 +1281,60 @@ int nsdg_net_loss_backward(nsdg_net* h, int batch, float* loss)
     if (loss)
         return netCopy(h, loss, h->lossDev, 4, cudaMemcpyDeviceToHost);
     return NSDG_OK;
+}
+
+int nsdg_net_get_normalisation(nsdg_net* h, float* host, size_t n)
+{
+    if (!h || !host)
+        return NSDG_ERR_BAD_ARG;
+    if (n != NSDG_NET_NORM_FLOATS) {
+        h->err = "normalisation: expected NSDG_NET_NORM_FLOATS floats";
+        return NSDG_ERR_SIZE_MISMATCH;
+    }
+    const cudaError_t e = cudaMemcpy(host, h->impl->stats, n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        h->err = std::string("normalisation: ") + cudaGetErrorString(e);
+        return NSDG_ERR_CUDA;
+    }
+    return NSDG_OK;
+}
+
+int nsdg_net_set_normalisation(nsdg_net* h, const float* host, size_t n)
+{
+    if (!h || !host)
+        return NSDG_ERR_BAD_ARG;
+    if (n != NSDG_NET_NORM_FLOATS) {
+        h->err = "normalisation: expected NSDG_NET_NORM_FLOATS floats";
+        return NSDG_ERR_SIZE_MISMATCH;
+    }
+    cudaError_t e = cudaStreamSynchronize(h->impl->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(h->impl->stats, host, n * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        h->err = std::string("normalisation: ") + cudaGetErrorString(e);
+        return NSDG_ERR_CUDA;
+    }
+    return NSDG_OK;
+}
+
+int nsdg_net_dataset_reserve(nsdg_net* h, int capacity)
+{
+    if (!h)
+        return NSDG_ERR_BAD_ARG;
+    return netDatasetReserve(h->impl, capacity, h->err);
+}
+
+int nsdg_net_dataset_normalise(nsdg_net* h, int count)
+{
+    if (!h)
+        return NSDG_ERR_BAD_ARG;
+    return netDatasetNormalise(h->impl, count, h->err);
+}
+
+int nsdg_net_train(nsdg_net* h, int count, int iterations, int batch, float lr, unsigned long long seed, float* loss)
+{
+    if (!h)
+        return NSDG_ERR_BAD_ARG;
+    return netTrain(h->impl, count, iterations, batch, lr, seed, loss, h->err);
 }
 
 int nsdg_net_adam_step(nsdg_net* h, float lr, float beta1, float beta2, float eps)

@@ -182,6 +182,33 @@ class _KernelBase:
         self._check(self._l.nsdg_kernel_launches_per_update(self._h, byref(n)))
         return n.value
 
+    # -- learned warm start (mEVP, mixed precision) ------------------------------
+    def warm_sample(self, tst, dt, k_iters: int, net, slot: int) -> float:
+        """One plain update that also records dataset sample `slot` of `net`;
+        returns the plain sub-cycle's last-iteration ratio."""
+        ratio = c_double()
+        self._check(self._l.nsdg_kernel_warm_sample(self._h, float(tst), float(dt), int(k_iters), net._h,
+                                                    int(slot), byref(ratio)))
+        return ratio.value
+
+    def set_warm_start(self, net, k_iters: int = 0, kappa: float = 0.0, judge_every: int = 0,
+                       judge_tol: float = 0.0):
+        """Attaches `net` (None detaches); later updates run the network plus
+        `k_iters` iterations, falling back to the full count when the
+        last-iteration ratio exceeds `kappa`; every `judge_every`-th update
+        also runs the plain sub-cycle and keeps the warm start enabled only
+        while the warm result is within `judge_tol` (relative) of it."""
+        self._check(self._l.nsdg_kernel_set_warm_start(self._h, None if net is None else net._h,
+                                                       int(k_iters), float(kappa), int(judge_every),
+                                                       float(judge_tol)))
+        self._warm_net = net  # keeps the network alive while attached
+
+    def warm_stats(self) -> dict:
+        """Counters of the attached warm start (nsdg_warm_stats as a dict)."""
+        st = _lib.WarmStats()
+        self._check(self._l.nsdg_kernel_warm_stats(self._h, byref(st)))
+        return st.as_dict()
+
 
 class MEVPDynamicsKernel(_KernelBase):
     """mEVP rheology (MEVPDynamicsKernel.hpp, VPCGDynamicsKernel.hpp)."""

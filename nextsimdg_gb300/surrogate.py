@@ -93,3 +93,64 @@ class Net:
 
     def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         self._check(self._l.nsdg_net_adam_step(self._h, lr, beta1, beta2, eps))
+
+    # -- warm-start dataset and training (all on the device) -------------------
+    def dataset_reserve(self, capacity: int):
+        self._check(self._l.nsdg_net_dataset_reserve(self._h, int(capacity)))
+        self.capacity = int(capacity)
+
+    def dataset_normalise(self, count: int):
+        self._check(self._l.nsdg_net_dataset_normalise(self._h, int(count)))
+
+    def train(self, count: int, iterations: int, batch: int = 1, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = c_float()
+        self._check(self._l.nsdg_net_train(self._h, int(count), int(iterations), int(batch), float(lr),
+                                           int(seed), byref(loss)))
+        return loss.value
+
+    def get_normalisation(self) -> np.ndarray:
+        out = np.empty(_lib.NET_NORM_FLOATS, dtype=np.float32)
+        self._check(self._l.nsdg_net_get_normalisation(self._h, out.ctypes.data_as(c_void_p), out.size))
+        return out
+
+    def set_normalisation(self, stats):
+        a = np.ascontiguousarray(stats, dtype=np.float32)
+        self._check(self._l.nsdg_net_set_normalisation(self._h, a.ctypes.data_as(c_void_p), a.size))
+
+
+WARM_CHANNELS = (_lib.WARM_FEATURES, 48, 48, 48, 48, 48, _lib.WARM_TARGETS)
+
+
+def warm_net(nx: int, ny: int, max_batch: int = 1, seed: int = 0, channels=WARM_CHANNELS) -> Net:
+    """A network shaped for the warm start of an nx x ny grid."""
+    return Net(channels, ny, nx, max_batch=max_batch, used_outputs=_lib.WARM_USED, seed=seed)
+
+
+def train_warm_start(kernel, forcing, samples: int, k_iters: int, dt: float, net: Net | None = None,
+                     stride: int = 1, iterations: int = 2000, batch: int = 1,
+                     schedule=((0.4, 1e-3), (0.3, 3e-4), (0.3, 1e-4)), seed: int = 0, t0: float = 0.0,
+                     nx: int | None = None, ny: int | None = None):
+    """Runs the plain sub-cycle of `kernel` for samples * stride steps
+    (forcing(kernel, step) sets each step's inputs), recording every
+    stride-th step as a training sample; then normalises and trains with
+    Adam over `schedule` ((fraction of the iterations, learning rate), ...).
+    Returns (net, kappa, loss): kappa is the largest last-iteration ratio of
+    the plain sub-cycle over the recorded steps."""
+    if net is None:
+        net = warm_net(nx, ny, max_batch=batch, seed=seed)
+    net.dataset_reserve(samples)
+    ratios = []
+    step = 0
+    for j in range(samples):
+        for i in range(stride):
+            forcing(kernel, step)
+            slot = j if i == stride - 1 else -1
+            r = kernel.warm_sample(t0 + step * dt, dt, k_iters, net, slot)
+            if slot >= 0:
+                ratios.append(r)
+            step += 1
+    net.dataset_normalise(samples)
+    loss = float("nan")
+    for i, (frac, lr) in enumerate(schedule):
+        loss = net.train(samples, max(1, int(iterations * frac)), batch=batch, lr=lr, seed=seed + i)
+    return net, float(max(ratios)), loss
