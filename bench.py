@@ -2,19 +2,30 @@
 """Throughput of the sea-ice dynamics step on GB300: cell-updates per second.
 
 Workload (the configuration the headline metric is quoted on, one GPU): the
-256 x 256 box test with DG2 transport (6 components), CG2 velocity, DG-stress
-8, FP64 everywhere, 100 mEVP iterations (alpha = beta = 300) per 120 s step.
+512 x 512 box test with DG2 transport (6 components), CG2 velocity, DG-stress
+8, 100 mEVP iterations (alpha = beta = 300) per 120 s step, in the mixed
+precision mode (FP32 stress/momentum arithmetic and state; FP64 for the
+conservation sums, the inverse mass matrices, Delta and the viscosity).
 One "step" is one model step: the DG transport of concentration and
 thickness with limiters, the preparation of the momentum solve and the 100
 mEVP iterations (strain, stress, divergence, momentum, boundaries).
 
   value  device-resident: K steps of the CUDA graph, CUDA events on the
-         library's stream; inputs (> L2: 256^2 elements x ~3.7 kB of FP64
-         operators) are not re-flushed between steps.
+         library's stream; inputs (the per-iteration operator sweep, 405 MB
+         FP32 at 512^2, is larger than L2) are not re-flushed between steps.
   e2e    the reference's module cycle through the C ABI with host buffers
          (MEVPDynamics::update: setData of h, A, winds, ocean, ssh, then
          update, then getDG0Data of h, A, u, v and the ice-ocean stress),
          wall clock, host<->device copies inside.
+  variants.plain_fp64     the FP64 path (the reference's arithmetic) on the
+                          same grid, with its own roofline;
+  variants.learned_fp32   the learned warm start: data generation and
+                          training on the GPU, then the warm update with and
+                          without judgement against the plain sub-cycle;
+  velocity_error_vs_fp64  one simulated day: FP32 path vs FP64 path, next to
+                          the FP64 path's own response to h x (1 + 1e-14).
+
+--precision fp64 --nx 256 gives the FP64 drop-in path on the 256^2 grid.
 
 --impl reference times the CPU restatement of the reference algorithm (the
 oracle; the reference itself cannot be built: it needs Eigen, absent here)
@@ -42,7 +53,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "cell-updates/s"
 UNIT = "cell-updates/s"
-NX = 256
+NX = 512
 DG = 6
 DT = 120.0
 ALPHA = BETA = 300.0
@@ -50,13 +61,14 @@ NSTEPS = 100
 
 
 def bytes_per_element_iteration_stress(word: int = 8) -> int:
-    """Algorithmic DRAM bytes of one launch of the element stress kernel
-    (kMevpStress), per element: the strain operators G_x, G_y and the
-    divergence operators A_1, A_2 (4 x 81 words), P/alpha at the 9 Gauss
-    points (FP64), the 18 divergence coefficients read and written, and the
-    CG2 velocity counted once per node (about 4 nodes per element, u and v)."""
+    """Algorithmic DRAM bytes of one launch of the element stress kernel, per
+    element: the strain operators G_x, G_y and the divergence operators A_1,
+    A_2 (4 x 81 words), the pressure terms at the 9 Gauss points (FP64 P/alpha;
+    in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha)), the 18
+    divergence coefficients read and written, and the CG2 velocity counted
+    once per node (about 4 nodes per element, u and v)."""
     operators = 4 * 81 * word
-    pressure = 9 * 8
+    pressure = 9 * 8 + (9 * 4 if word == 4 else 0)
     tdiv = 2 * 18 * word
     velocity = 4 * 2 * word
     return operators + pressure + tdiv + velocity
@@ -69,13 +81,13 @@ def flops_per_element_iteration_stress() -> int:
     return 2 * (4 * 81) + 9 * 12 + 2 * (4 * 81) + 2 * 18
 
 
-def bytes_per_cell_update(n_iter: int = NSTEPS) -> float:
-    """Algorithmic bytes per cell-update of the whole step (FP64 path):
-    n_iter x (element kernel + node kernel share) + transport/prepare."""
-    node_per_element = 4 * (15 * 8) + 18 * 8  # ~4 nodes x 15 FP64 streams + gathered divergence coefficients
+def bytes_per_cell_update(n_iter: int = NSTEPS, word: int = 8) -> float:
+    """Algorithmic bytes per cell-update of the whole step: n_iter x (element
+    kernel + node kernel share) + transport/prepare (FP64 in both paths)."""
+    node_per_element = 4 * (15 * word) + 18 * word  # ~4 nodes x 15 streams + gathered divergence coefficients
     transport = 4 * (6 * 9 * 2 + 36 + 4 * 6 + 2 * 6) * 8  # cell terms, M^-1, phi, stage I/O
     prepare = 2 * 6 * 8 + 9 * 8 + 20 * 8 * 4
-    return n_iter * (bytes_per_element_iteration_stress() + node_per_element) + transport + prepare
+    return n_iter * (bytes_per_element_iteration_stress(word) + node_per_element) + transport + prepare
 
 
 # --------------------------------------------------------------------------
@@ -245,10 +257,10 @@ def run_reference(args, world, rank):
     v = box.nelements * args.steps / t
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic box test",
             "config": {"workload": f"box test {args.nx}x{args.nx}, DG2 transport, CG2 velocity, mEVP {NSTEPS} "
-                                   f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s", "precision": args.precision},
+                                   f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s", "precision": "fp64 (oracle)"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
                              "sample": f"{args.steps} full model steps after {args.warmup} warm-up"},
@@ -256,18 +268,112 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def make_kernel(box, precision: int, n_steps: int = NSTEPS, scale_h: float = 1.0):
+    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
+    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=n_steps, precision=precision)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr * scale_h if name == "hice" else arr)
+    return k
+
+
+def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
+    """Roofline of the dominant kernel (the element stress kernel), timed alone
+    with CUDA events on the library's stream."""
+    kms, kname = k.time_kernel(0, 50)
+    nms, nname = k.time_kernel(1, 50)
+    bpe = bytes_per_element_iteration_stress(4 if prec else 8)
+    achieved = N * bpe / (kms * 1e-3) / 1e9
+    hbm, hbm_kind = measured_peaks()
+    traffic = None
+    prof = ROOT / "profiles" / (f"kMevpStress32_box{nx}_fp32.md" if prec else f"kMevpStress_box{nx}_fp64.md")
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith(f"traffic_bytes_per_launch_{nx}:"):
+                traffic = int(line.split(":")[1])
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": traffic, "kernel": kname, "kernel_ms": kms, "share_of_step": kms * NSTEPS / ms_step,
+            "algorithmic_bytes_per_element": bpe, "peak_kind": hbm_kind}
+    if prec:
+        # both FP32 stress kernels (the library keeps the faster at initialise)
+        roof["stress_kernel_ms"] = {k.time_kernel(i, 50)[1]: k.time_kernel(i, 50)[0] for i in (3, 4)}
+    if prec == 0:
+        fp64_tf, fp64_kind = fp64_peak_tflops(local)
+        ach = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
+        roof["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_tf, "frac": ach / fp64_tf,
+                        "peak_kind": fp64_kind}
+    return roof, {"name": nname, "ms": nms}
+
+
+def learned_variant(args, box_eval, N: int, plain_ms: float):
+    """The learned warm start: samples from a perturbed trajectory (other h
+    phases, cyclone start and speed), training on the GPU, then (a) the warm
+    update without judgement and (b) judged every 10th update against the
+    plain sub-cycle with a relative tolerance of 0.1, on the evaluation box."""
+    from nextsimdg_gb300 import surrogate
+    from nextsimdg_gb300.boxtest import BoxTest, step_forcing
+
+    K = args.warm_iters
+    tb = BoxTest(args.nx, seed=1, start=(0.45 * 512e3, 0.47 * 512e3), wind_speed=9.0, h_noise=0.02)
+    kt = make_kernel(tb, 1)
+    t0 = time.perf_counter()
+    net, kappa, loss = surrogate.train_warm_start(
+        kt, lambda k, s: step_forcing(k, tb, s), args.warm_samples, K, DT, stride=3,
+        iterations=args.warm_train_iters, batch=1, nx=args.nx, ny=args.nx, seed=1)
+    t_train = time.perf_counter() - t0
+    kt.close()
+    out = {"k_iters": K, "samples": args.warm_samples, "train_iterations": args.warm_train_iters,
+           "train_loss": loss, "data_and_training_s": t_train, "kappa": kappa * 1.5}
+    res = {}
+    for name, je, jt in (("unjudged", 0, 0.0), ("judged_every_10_tol_0.1", 10, 0.1)):
+        k = make_kernel(box_eval, 1)
+        k.set_warm_start(net, K, kappa * 1.5, je, jt)
+        for s in range(args.warmup):
+            step_forcing(k, box_eval, s)
+            k.update(s * DT, DT)
+        ms = k.time_updates(DT, args.steps) / args.steps
+        st = k.warm_stats()
+        res[name] = {"value": N / (ms * 1e-3), "ms_per_step": ms, "speedup_vs_plain_fp32": plain_ms / ms,
+                     "accepted": st["accepted"], "fallbacks": st["fallbacks"], "judged": st["judged"],
+                     "judge_rejected": st["judge_rejected"], "last_judged_rel_error": st["last_judged_error"]}
+        k.close()
+    out.update(res)
+    net.close()
+    return out
+
+
+def day_error(args, box, steps: int):
+    """Velocity / thickness / concentration RMS after `steps` model steps: the
+    headline precision path and the FP64 path with h scaled by (1 + 1e-14),
+    both against the FP64 path."""
+    from nextsimdg_gb300.boxtest import step_forcing
+    ks = {"fp64": make_kernel(box, 0), "fp64_h_times_1p1e-14": make_kernel(box, 0, scale_h=1 + 1e-14),
+          "fp32": make_kernel(box, 1)}
+    for s in range(steps):
+        for k in ks.values():
+            step_forcing(k, box, s)
+            k.update(s * DT, DT)
+    r = {n: {f: k.getDG0Data(f) for f in ("u", "v", "hice", "cice")} for n, k in ks.items()}
+    ref = r["fp64"]
+    rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+    out = {"steps": steps, "simulated_hours": steps * DT / 3600.0}
+    for n in ("fp32", "fp64_h_times_1p1e-14"):
+        x = r[n]
+        out[n] = {"u_v_rms_m_per_s": rms(np.hypot(x["u"] - ref["u"], x["v"] - ref["v"])),
+                  "h_rms_m": rms(x["hice"] - ref["hice"]), "A_rms": rms(x["cice"] - ref["cice"])}
+    for k in ks.values():
+        k.close()
+    return out
+
+
 def run_ours(args, world, rank, local):
     from nextsimdg_gb300.boxtest import BoxTest
-    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
 
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES", str(local))
     prec = 1 if args.precision == "mixed" else 0
     box = BoxTest(args.nx)
-    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=prec)
-    k.initialise(box.coords(), False, box.mask())
-    for name, arr in box.initial_fields().items():
-        k.setData(name, arr)
+    k = make_kernel(box, prec)
     N = box.nelements
 
     # ---- value: device-resident steps (CUDA graph replays, CUDA events) ----
@@ -316,41 +422,24 @@ def run_ours(args, world, rank, local):
     t_e2e = dist_max(t_e2e, world)
     e2e = world * N * args.steps / t_e2e
 
-    # ---- roofline of the dominant kernel (element stress kernel) ----
-    kms, kname = k.time_kernel(0, 50)
-    nms, nname = k.time_kernel(1, 50)
-    bpe = bytes_per_element_iteration_stress(4 if prec else 8)
-    achieved_gbs = N * bpe / (kms * 1e-3) / 1e9
-    hbm, hbm_kind = measured_peaks()
-    fp64_tf, fp64_kind = fp64_peak_tflops(local)
-    fp64_achieved = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
-    share = (kms * NSTEPS) / (ms_max / args.steps)
-    traffic = None
-    prof = ROOT / "profiles" / "kMevpStress_box256_fp64.md"
-    if prof.exists() and args.nx == 256 and prec == 0:
-        for line in prof.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_launch_256:"):
-                traffic = int(line.split(":")[1])
-
+    roof, node = stress_roofline(k, N, prec, ms_max / args.steps, local, args.nx)
     k.close()
+
     variants = {}
-    if not args.no_variants and prec == 0:
-        # the mixed-precision path on the same grid, device-resident
-        km = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=1)
-        km.initialise(box.coords(), False, box.mask())
-        for name, arr in box.initial_fields().items():
-            km.setData(name, arr)
-        km.time_updates(DT, 3)
-        mms = km.time_updates(DT, args.steps)
-        km.synchronize()
-        sms, _ = km.time_kernel(0, 50)
-        nms2, _ = km.time_kernel(1, 50)
-        mval = N * args.steps / (mms * 1e-3)
-        variants["mixed_fp32"] = {"value": mval, "unit": UNIT, "ms_per_step": mms / args.steps,
-                                  "speedup_vs_fp64": mval / (N * args.steps / (ms_max * 1e-3)),
-                                  "kMevpStress32_ms": sms, "kMevpMomentum32_ms": nms2,
-                                  "stress_GBps": N * bytes_per_element_iteration_stress(4) / (sms * 1e-3) / 1e9}
-        km.close()
+    if not args.no_variants and world == 1:
+        other = 0 if prec else 1
+        ko = make_kernel(box, other)
+        ko.time_updates(DT, 3)
+        oms = ko.time_updates(DT, args.steps) / args.steps
+        ko.synchronize()
+        oroof, _ = stress_roofline(ko, N, other, oms, local, args.nx)
+        ko.close()
+        variants["plain_fp64" if prec else "mixed_fp32"] = {
+            "value": N / (oms * 1e-3), "unit": UNIT, "ms_per_step": oms,
+            "headline_speedup_over_this": oms / (ms_max / args.steps), "roofline": oroof}
+        if prec and args.warm_train_iters > 0:
+            variants["learned_fp32"] = learned_variant(args, box, N, ms_max / args.steps)
+    err = day_error(args, box, args.error_steps) if (prec and args.error_steps > 0 and world == 1) else None
 
     if rank == 0:
         base = cpu_baseline(args.nx) if world == 1 and not args.no_cpu_baseline else None
@@ -361,20 +450,21 @@ def run_ours(args, world, rank, local):
             "data": "synthetic box test",
             "config": {"workload": f"box test {args.nx}x{args.nx}, DG2 transport, CG2 velocity, mEVP {NSTEPS} "
                                    f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s",
-                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (operators ~240 MB per step sweep), no flush",
-                       "bytes_per_cell_update": bytes_per_cell_update()},
+                       "precision": args.precision,
+                       "method": ("FP32 bulk (FP64: conservation sums, inverse mass matrices, Delta, viscosity); "
+                                  "the learned warm start is measured in variants.learned_fp32, not enabled here"
+                                  if prec else "FP64 throughout (the reference's arithmetic)"),
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (per-step operator sweep well above 129 MB), no flush",
+                       "bytes_per_cell_update": bytes_per_cell_update(word=4 if prec else 8)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8},
             "gpu_launches": launches * args.steps,
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm, "traffic": traffic,
-                         "kernel": kname, "kernel_ms": kms, "share_of_step": share,
-                         "algorithmic_bytes_per_element": bpe, "peak_kind": hbm_kind,
-                         "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_tf,
-                                  "frac": fp64_achieved / fp64_tf, "peak_kind": fp64_kind}},
-            "node_kernel": {"name": nname, "ms": nms},
+            "roofline": roof,
+            "node_kernel": node,
             "clocks": clk.summary(),
         }
+        if err:
+            line["velocity_error_vs_fp64"] = err
         if base:
             line["cpu_baseline"] = base
         if variants:
@@ -469,9 +559,14 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time a batched ensemble of this many box tests (mixed precision) instead")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="fp64: every operation FP64 (the reference's arithmetic); mixed: FP32 bulk")
-    ap.add_argument("--nx", type=int, default=NX, help="box side in cells (256 is the benchmark grid)")
+    ap.add_argument("--nx", type=int, default=NX, help="box side in cells (512: the mixed-precision benchmark grid)")
+    ap.add_argument("--error-steps", type=int, default=720,
+                    help="model steps of the FP32-vs-FP64 velocity error check (720 = one day; 0: skip)")
+    ap.add_argument("--warm-iters", type=int, default=40, help="mEVP iterations after the learned warm start")
+    ap.add_argument("--warm-samples", type=int, default=120, help="training samples (every 3rd step)")
+    ap.add_argument("--warm-train-iters", type=int, default=2000, help="Adam steps (0: skip the learned variant)")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident steps (for ncu captures): no e2e, no baselines")
     args = ap.parse_args()

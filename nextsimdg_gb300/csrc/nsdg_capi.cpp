@@ -114,6 +114,16 @@ struct nsdg_kernel {
     double *sshScratch = nullptr, *staging = nullptr, *dgTmp = nullptr, *cgTmp = nullptr;
     // mixed precision (NSDG_PRECISION_MIXED)
     DevOps32 dops32;
+    StressMaps maps32 {};
+    float* hP32 = nullptr; // P/(2 alpha) at the Gauss points (mixed precision)
+    bool tmaStress = true; // which FP32 stress kernel the updates use (chosen by timing at initialise)
+    cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1)
+    {
+        const bool tma = variant < 0 ? tmaStress : variant == 1;
+        return tma ? launchMevpStress32Tma(s, dm, maps32, st32.u, st32.v, Pg, hP32, tdiv32, mp, errWord)
+                   : launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, hP32, tdiv32, mp);
+    }
+    int chooseStress32();
     float* tdiv32 = nullptr;
     MevpNodeState32 st32 {};
     // FP32 u, v and divergence at the start of the previous sub-cycle (the
@@ -229,6 +239,8 @@ int nsdg_kernel::checkDeviceError()
             m += " velocity";
         if (h & DEV_ERR_NONFINITE_STRESS)
             m += " stress";
+        if (h & DEV_ERR_TIMEOUT)
+            return fail(NSDG_ERR_CUDA, "a bounded wait for an asynchronous copy ran out on the device");
         return fail(NSDG_ERR_NUMERIC, m);
     }
     return NSDG_OK;
@@ -319,10 +331,11 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
     if (P.precision == NSDG_PRECISION_MIXED) {
-        for (int i = 0; i < 4; ++i) add(81 * N, 4);
+        add(324 * ops32Ld(N), 4);
         add(18 * N, 4);
         for (int i = 0; i < 14; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
+        add(9 * N, 4);                            // P/(2 alpha)
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -440,10 +453,28 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             if (e == cudaSuccess) e = cudaMemcpy(p, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice);
             return p;
         };
-        dops32.gx = upf(ops.gx);
-        dops32.gy = upf(ops.gy);
-        dops32.a1 = upf(ops.a1);
-        dops32.a2 = upf(ops.a2);
+        {
+            // one [324][ld] block (G_x, G_y, A_1, A_2), rows padded to ld
+            const size_t ld = ops32Ld(N);
+            std::vector<float> blk(324 * ld, 0.f);
+            const std::vector<double>* src[4] = { &ops.gx, &ops.gy, &ops.a1, &ops.a2 };
+            for (int b = 0; b < 4; ++b)
+                for (size_t r = 0; r < 81; ++r)
+                    for (size_t el = 0; el < N; ++el)
+                        blk[(81 * b + r) * ld + el] = static_cast<float>((*src[b])[r * N + el]);
+            float* p = arena.take<float>(blk.size());
+            if (!p)
+                e = cudaErrorMemoryAllocation;
+            else if (e == cudaSuccess)
+                e = cudaMemcpy(p, blk.data(), blk.size() * sizeof(float), cudaMemcpyHostToDevice);
+            dops32.ld = ld;
+            dops32.gx = p;
+            dops32.gy = p ? p + 81 * ld : nullptr;
+            dops32.a1 = p ? p + 162 * ld : nullptr;
+            dops32.a2 = p ? p + 243 * ld : nullptr;
+            if (e == cudaSuccess)
+                e = makeStressMaps(dops32, &maps32);
+        }
         auto zf = [&](size_t n) {
             float* p = arena.take<float>(n);
             if (!p) { e = cudaErrorMemoryAllocation; return p; }
@@ -458,6 +489,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         tdivLast = zf(18 * N);
         uLast = zf(Ncg);
         vLast = zf(Ncg);
+        hP32 = zf(9 * N);
     }
     derr = arena.take<int>(1);
     if (!derr)
@@ -468,8 +500,45 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("initialise: allocation failed: ") + cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(stream));
+    if (mixed() && rheology == NSDG_RHEOLOGY_MEVP) {
+        const int r = chooseStress32();
+        if (r)
+            return r;
+    }
     ready = true;
     return ok();
+}
+
+// Times the two FP32 stress kernels (operators through TMA into shared
+// memory, or read directly from global memory) on this mesh and keeps the
+// faster one: which wins depends on the grid size and the number of
+// resident blocks.  Both compute the same values.
+int nsdg_kernel::chooseStress32()
+{
+    const MevpParams mp = mevpParams(120.0);
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, "initialise: event create failed");
+    float best[2] = { 0, 0 };
+    cudaError_t e = cudaSuccess;
+    for (int variant = 0; variant < 2 && e == cudaSuccess; ++variant) {
+        e = launchStress32(stream, mp, derr, variant);
+        if (e == cudaSuccess) e = cudaEventRecord(a, stream);
+        for (int r = 0; r < 10 && e == cudaSuccess; ++r)
+            e = launchStress32(stream, mp, derr, variant);
+        if (e == cudaSuccess) e = cudaEventRecord(b, stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&best[variant], a, b);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    // the timing launches updated the divergence of the (zero) initial state: reset it
+    if (e == cudaSuccess) e = cudaMemsetAsync(tdiv32, 0, 18 * N * sizeof(float), stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("initialise: stress kernel timing: ") + cudaGetErrorString(e));
+    tmaStress = best[1] <= best[0];
+    return NSDG_OK;
 }
 
 int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launches)
@@ -558,7 +627,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
         if (prep) {
             LCH(launchMevpPrepNodes(s, dm, st, mp));
-            LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp));
+            LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp, mixed() ? hP32 : nullptr));
             if (mixed())
                 LCH(launchMevpPrepNodes32(s, dm, st, st32));
         }
@@ -574,7 +643,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
                     LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
                     LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
                 } else {
-                    LCH(launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp));
+                    LCH(launchStress32(s, mp, derr));
                     LCH(launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, derr));
                 }
             }
@@ -602,7 +671,7 @@ int nsdg_kernel::mixedIterations(cudaStream_t s, double dt, int count, int* errW
 {
     const MevpParams mp = mevpParams(dt);
     for (int it = 0; it < count; ++it) {
-        cudaError_t e = launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, tdiv32, mp);
+        cudaError_t e = launchStress32(s, mp, errWord);
         if (e == cudaSuccess)
             e = launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, errWord);
         if (e != cudaSuccess)
@@ -1400,7 +1469,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         switch (kernel_id) {
         case 0:
             if (!bbm && k->mixed())
-                return launchMevpStress32(k->stream, k->dm, k->dops32, k->st32.u, k->st32.v, k->Pg, k->tdiv32, mp);
+                return k->launchStress32(k->stream, mp, k->derr);
             return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
                              k->s11, k->s12, k->s22, k->contrib, bp, k->derr)
                        : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
@@ -1409,17 +1478,24 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                 return launchMevpMomentum32(k->stream, k->dm, k->dops, k->st32, k->tdiv32, mp, k->derr);
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
+        case 3:
+        case 4:
+            return k->launchStress32(k->stream, mp, k->derr, kernel_id == 4 ? 1 : 0);
         default:
             return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
                 k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a);
         }
     };
+    if (kernel_id < 0 || kernel_id > 4 || (kernel_id >= 3 && (bbm || !k->mixed())))
+        return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP)");
     if (name)
-        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : (k->mixed() ? "kMevpStress32" : "kMevpStress"))
+        *name = kernel_id == 0 ? (bbm ? "kBbmStress"
+                                      : (k->mixed() ? (k->tmaStress ? "kMevpStress32Tma" : "kMevpStress32")
+                                                    : "kMevpStress"))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
-                             : "kTransportStage";
-    if (kernel_id < 0 || kernel_id > 2)
-        return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel_id must be 0, 1 or 2");
+            : kernel_id == 2 ? "kTransportStage"
+            : kernel_id == 3 ? "kMevpStress32"
+                             : "kMevpStress32Tma";
     cudaEvent_t ea, eb;
     if (cudaEventCreate(&ea) != cudaSuccess || cudaEventCreate(&eb) != cudaSuccess)
         return k->fail(NSDG_ERR_CUDA, "time_kernel: event create failed");
@@ -1661,6 +1737,7 @@ struct nsdg_ensemble {
         d.o = k->dops32;
         d.st = k->st32;
         d.Pg = k->Pg;
+        d.hP = k->hP32;
         d.tdiv = k->tdiv32;
         d.tileW = tw;
         d.tileH = stressElementsPerBlock() / tw;

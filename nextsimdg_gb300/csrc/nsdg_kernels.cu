@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes(size_t n, MevpNodeState
 
 template <int DG>
 __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const double* __restrict__ h,
-    const double* __restrict__ a, double* __restrict__ Pg, double Pstar, double invAlpha)
+    const double* __restrict__ a, double* __restrict__ Pg, double Pstar, double invAlpha, float* __restrict__ hP32)
 {
     const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (e >= N)
@@ -829,7 +829,13 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const doub
         }
         const double hq = fmax(hs, 0.0);
         const double aq = fmin(fmax(as, 0.0), 1.0);
-        Pg[q * N + e] = Pstar * hq * exp(-20.0 * (1.0 - aq)) * invAlpha;
+        const double pa = Pstar * hq * exp(-20.0 * (1.0 - aq)) * invAlpha;
+        if (hP32) {
+            Pg[q * N + e] = 0.125 * pa;
+            hP32[q * N + e] = static_cast<float>(0.5 * pa);
+        } else {
+            Pg[q * N + e] = pa;
+        }
     }
 }
 
@@ -1019,13 +1025,14 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeSta
 // invariant 1.25(e11^2+e22^2) + 1.5 e11 e22 + e12^2 is formed in FP32 from the
 // FP32 strain (it is a positive-definite quadratic form: no cancellation);
 // Delta = sqrt(invariant + DeltaMin^2) and the viscosity P/(8 alpha Delta) are
-// evaluated in FP64; the stress increments and the divergence update are FP32.
+// evaluated in FP64 (Pg holds P/(8 alpha), hP = P/(2 alpha) in FP32); the
+// stress increments and the divergence update are FP32.
 // Body of the mixed-precision element kernel for element e handled by thread
 // (le, part) of a block of kStressElems x kStressParts threads; shared by the
 // single-grid and the batched (ensemble) kernels.
 __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool active, size_t e, int le, int part,
     const DevOps32& o, const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
-    float* __restrict__ tdiv, const MevpParams& p, float (*fs)[9][kStressElems])
+    const float* __restrict__ hPg, float* __restrict__ tdiv, const MevpParams& p, float (*fs)[9][kStressElems])
 {
     if (active) {
         const size_t s2 = 2 * size_t(nx) + 1;
@@ -1045,8 +1052,8 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
             float ex = 0.f, ey = 0.f, exv = 0.f, eyu = 0.f;
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
-                const float gxq = o.gx[(q * 9 + j) * N + e];
-                const float gyq = o.gy[(q * 9 + j) * N + e];
+                const float gxq = o.gx[(q * 9 + j) * o.ld + e];
+                const float gyq = o.gy[(q * 9 + j) * o.ld + e];
                 ex = fmaf(gxq, ul[j], ex);
                 ey = fmaf(gyq, vl[j], ey);
                 exv = fmaf(gxq, vl[j], exv);
@@ -1054,9 +1061,8 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
             }
             const float sxy = exv + eyu;
             const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
-            const double Pa = Pg[q * N + e];
-            const float z8 = static_cast<float>(0.125 * Pa * rsqrt(static_cast<double>(inv) + dmin2));
-            const float hP = static_cast<float>(0.5 * Pa);
+            const float z8 = static_cast<float>(Pg[q * N + e] * rsqrt(static_cast<double>(inv) + dmin2));
+            const float hP = hPg[q * N + e];
             fs[0][q][le] = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP);
             fs[1][q][le] = z8 * sxy;
             fs[2][q][le] = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP);
@@ -1072,8 +1078,8 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
         float ax = 0.f, ay = 0.f;
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            const float a1 = o.a1[(j * 9 + q) * N + e];
-            const float a2 = o.a2[(j * 9 + q) * N + e];
+            const float a1 = o.a1[(j * 9 + q) * o.ld + e];
+            const float a2 = o.a2[(j * 9 + q) * o.ld + e];
             const float f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
             ax = fmaf(a1, f11, fmaf(a2, f12, ax));
             ay = fmaf(a1, f12, fmaf(a2, f22, ay));
@@ -1090,14 +1096,183 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
 // evaluated in FP64; the stress increments and the divergence update are FP32.
 __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(DevMesh m, DevOps32 o,
     const float* __restrict__ u, const float* __restrict__ v, const double* __restrict__ Pg,
-    float* __restrict__ tdiv, MevpParams p)
+    const float* __restrict__ hP, float* __restrict__ tdiv, MevpParams p)
 {
     __shared__ float fs[3][9][kStressElems];
     const int le = threadIdx.x % kStressElems;
     const int part = threadIdx.x / kStressElems;
     const size_t e = blockIdx.x * size_t(kStressElems) + le;
     const bool active = e < m.N && m.ice[e];
-    mevpStress32Element(m.nx, m.N, active, e, le, part, o, u, v, Pg, tdiv, p, fs);
+    mevpStress32Element(m.nx, m.N, active, e, le, part, o, u, v, Pg, hP, tdiv, p, fs);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged FP32 stress kernel
+// ---------------------------------------------------------------------------
+// The arithmetic of mevpStress32Element, with the operator entries of a
+// block's 32 elements brought into shared memory by 2-D TMA copies that
+// complete on mbarriers: first the strain rows (G_x, G_y: box {32 elements,
+// 162 rows}, 20.7 KB), then, into the same buffer once the strain phase has
+// read it, the divergence rows (A_1, A_2).  One 24 KB buffer per block keeps
+// nine blocks (27 warps) resident per SM, each with a 20.7 KB copy in
+// flight; the velocity gathers and P/alpha loads are issued while the first
+// copy lands.  Waits are bounded: a copy that has not landed after kTmaSpin
+// polls sets DEV_ERR_TIMEOUT and the block returns after a second bounded
+// wait for the copy it issued.
+namespace {
+constexpr int kTmaRows = 162;
+constexpr unsigned kTmaTileBytes = kTmaRows * kTmaElems * 4;
+constexpr long kTmaSpin = 1L << 26;
+
+__device__ __forceinline__ unsigned smemAddr(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbarInit(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint64_t* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, unsigned parity)
+{
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smemAddr(bar)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbarWaitBounded(uint64_t* bar, unsigned parity)
+{
+    for (long i = 0; i < kTmaSpin; ++i)
+        if (mbarTryWait(bar, parity))
+            return true;
+    return false;
+}
+__device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(smemAddr(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smemAddr(bar))
+                 : "memory");
+}
+} // namespace
+
+__global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(const __grid_constant__ CUtensorMap mapG,
+    const __grid_constant__ CUtensorMap mapA, DevMesh m, const float* __restrict__ u, const float* __restrict__ v,
+    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p,
+    int* __restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* sT = reinterpret_cast<float*>(smem);                      // [162][32]: G_x|G_y, then A_1|A_2
+    float (*fs)[9][kTmaElems] = reinterpret_cast<float (*)[9][kTmaElems]>(sT + kTmaRows * kTmaElems);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(fs[3]);             // 2 mbarriers, one per copy
+    const int le = threadIdx.x % kTmaElems;
+    const int part = threadIdx.x / kTmaElems;
+    const int x0 = blockIdx.x * kTmaElems;
+    if (threadIdx.x == 0) {
+        mbarInit(&bars[0], 1);
+        mbarInit(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbarExpectTx(&bars[0], kTmaTileBytes);
+        tmaLoad2d(sT, &mapG, x0, 0, &bars[0]);
+    }
+    const size_t N = m.N;
+    const size_t e = size_t(x0) + le;
+    const bool active = e < N && m.ice[e];
+    // the 9 CG2 velocities of the element and P/alpha (loaded while the copy lands)
+    float ul[9], vl[9];
+    double Pa[3];
+    float hP[3];
+    if (active) {
+        const size_t s2 = 2 * size_t(m.nx) + 1;
+        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t base = 2 * s2 * iy + 2 * ix;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const size_t nd = base + (j % 3) + (j / 3) * s2;
+            ul[j] = u[nd];
+            vl[j] = v[nd];
+        }
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+            Pa[qq] = Pg[(3 * part + qq) * N + e];
+            hP[qq] = hPg[(3 * part + qq) * N + e];
+        }
+    }
+    __syncthreads(); // the barriers are initialised before anyone polls them
+    bool ok = mbarWaitBounded(&bars[0], 0);
+    if (ok && active) {
+        const double dmin2 = p.DeltaMin * p.DeltaMin;
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+            const int q = 3 * part + qq;
+            float ex = 0.f, ey = 0.f, exv = 0.f, eyu = 0.f;
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const float gxq = sT[(q * 9 + j) * kTmaElems + le];
+                const float gyq = sT[(81 + q * 9 + j) * kTmaElems + le];
+                ex = fmaf(gxq, ul[j], ex);
+                ey = fmaf(gyq, vl[j], ey);
+                exv = fmaf(gxq, vl[j], exv);
+                eyu = fmaf(gyq, ul[j], eyu);
+            }
+            const float sxy = exv + eyu;
+            const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
+            const float z8 = static_cast<float>(Pa[qq] * rsqrt(static_cast<double>(inv) + dmin2));
+            fs[0][q][le] = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP[qq]);
+            fs[1][q][le] = z8 * sxy;
+            fs[2][q][le] = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP[qq]);
+        }
+    }
+    // every thread has finished reading the strain rows (and written its
+    // stress terms): the buffer may take the divergence rows
+    if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) {
+            atomicOr(err, DEV_ERR_TIMEOUT);
+            mbarWaitBounded(&bars[0], 0);
+        }
+        __syncthreads();
+        return;
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbarExpectTx(&bars[1], kTmaTileBytes);
+        tmaLoad2d(sT, &mapA, x0, 0, &bars[1]);
+    }
+    ok = mbarWaitBounded(&bars[1], 0);
+    if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) {
+            atomicOr(err, DEV_ERR_TIMEOUT);
+            mbarWaitBounded(&bars[1], 0);
+        }
+        __syncthreads();
+        return;
+    }
+    if (!active)
+        return;
+    const float keep = static_cast<float>(1.0 - 1.0 / p.alpha);
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) {
+        const int j = 3 * part + jj;
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float a1 = sT[(j * 9 + q) * kTmaElems + le];
+            const float a2 = sT[(81 + j * 9 + q) * kTmaElems + le];
+            const float f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
+            ax = fmaf(a1, f11, fmaf(a2, f12, ax));
+            ay = fmaf(a1, f12, fmaf(a2, f22, ay));
+        }
+        tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
+        tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
+    }
 }
 
 // Body of the mixed-precision node kernel for CG2 node i.
@@ -1182,7 +1357,7 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32Batc
     const bool inside = ix < M.nx && iy < M.ny;
     const size_t e = inside ? size_t(iy) * M.nx + ix : 0;
     const bool active = inside && M.ice[e];
-    mevpStress32Element(M.nx, M.N, active, e, le, part, M.o, M.st.u, M.st.v, M.Pg, M.tdiv, p, fs);
+    mevpStress32Element(M.nx, M.N, active, e, le, part, M.o, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, fs);
 }
 
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
@@ -1587,13 +1762,13 @@ cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNode
 }
 
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
-    const double* a, double* Pg, const MevpParams& p)
+    const double* a, double* Pg, const MevpParams& p, float* hP32)
 {
     const unsigned g = blocksFor(m.N);
     switch (dg) {
-    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
-    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
-    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha); break;
+    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
+    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
+    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1619,10 +1794,57 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
     kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32);
     return cudaGetLastError();
 }
-cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
-    const float* v, const double* Pg, float* tdiv, const MevpParams& p)
+namespace {
+constexpr size_t kTmaSmem = size_t(kTmaTileBytes) + 3 * 9 * kTmaElems * 4 + 2 * 8;
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+} // namespace
+
+cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
 {
-    kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
+    static EncodeTiledFn encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        const cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return e != cudaSuccess ? e : cudaErrorNotSupported;
+        encode = reinterpret_cast<EncodeTiledFn>(fn);
+    }
+    // the four operator blocks are rows of one [324][ld] array; ld * 4 bytes
+    // is a multiple of 128 and the base is 256-byte aligned
+    const cuuint64_t dims[2] = { o.ld, kTmaRows };
+    const cuuint64_t strides[1] = { o.ld * sizeof(float) };
+    const cuuint32_t box[2] = { kTmaElems, kTmaRows };
+    const cuuint32_t estr[2] = { 1, 1 };
+    const float* rows[2] = { o.gx, o.a1 };
+    CUtensorMap* maps[2] = { &out->g, &out->a };
+    for (int i = 0; i < 2; ++i) {
+        const CUresult r = encode(maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(rows[i]), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    // dynamic shared memory of the kernel (24 KB: one operator tile, the
+    // stress terms, two mbarriers), set once
+    return cudaFuncSetAttribute(kMevpStress32Tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        static_cast<int>(kTmaSmem));
+}
+
+cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err)
+{
+    kMevpStress32Tma<<<blocksFor(m.N, kTmaElems), kTmaElems * kStressParts, kTmaSmem, s>>>(maps.g, maps.a, m, u, v,
+        Pg, hP, tdiv, p, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p)
+{
+    kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, hP, tdiv, p);
     return cudaGetLastError();
 }
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o, const MevpNodeState32& st,

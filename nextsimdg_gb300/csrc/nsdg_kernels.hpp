@@ -7,6 +7,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "nsdg_host.hpp"
@@ -61,6 +62,7 @@ struct DevOps {
 enum DeviceError : int {
     DEV_ERR_NONFINITE_VELOCITY = 1,
     DEV_ERR_NONFINITE_STRESS = 2,
+    DEV_ERR_TIMEOUT = 4,            // a bounded wait on an asynchronous copy ran out
 };
 
 cudaError_t uploadConstTables();
@@ -128,9 +130,11 @@ struct MevpParams {
 };
 cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st,
     const MevpParams& p);
-// P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298).
+// P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298):
+// Pg = P/alpha, or, for the mixed-precision kernels (hP32 given),
+// Pg = P/(8 alpha) (FP64, the viscosity numerator) and hP32 = P/(2 alpha).
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
-    const double* a, double* Pg, const MevpParams& p);
+    const double* a, double* Pg, const MevpParams& p, float* hP32 = nullptr);
 // One mEVP iteration, element part, carried in divergence space: the strain at
 // the Gauss points, Delta, and the relaxed update of the element's stress
 // divergence contributions tdiv[18][N] = (divS1 s11 + divS2 s12, divS1 s12 +
@@ -147,12 +151,27 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 // FP32 operators, velocities, divergence coefficients and momentum
 // arithmetic; FP64 for Delta = sqrt(strain invariant + DeltaMin^2), the
 // viscosity P/(2 Delta), and the lumped-mass inverse.
+// FP32 element operators, one [324][ld] block: rows 0..80 G_x, 81..161 G_y,
+// 162..242 A_1, 243..323 A_2; ld = N rounded up to kTmaElems (padding zero).
 struct DevOps32 {
     const float* gx = nullptr;
     const float* gy = nullptr;
     const float* a1 = nullptr;
     const float* a2 = nullptr;
+    size_t ld = 0;
 };
+constexpr int kTmaElems = 32;   // elements per block of the TMA-staged stress kernel
+inline size_t ops32Ld(size_t N) { return (N + kTmaElems - 1) / kTmaElems * kTmaElems; }
+// TMA descriptors of the strain rows (G_x, G_y) and the divergence rows
+// (A_1, A_2) of a DevOps32 block: 2-D, inner dimension the element index.
+struct alignas(64) StressMaps {
+    CUtensorMap g;
+    CUtensorMap a;
+};
+cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out);
+// kMevpStress32 with the operator tiles staged in shared memory by TMA.
+cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err);
 struct MevpNodeState32 {
     float* u;
     float* v;
@@ -173,7 +192,7 @@ struct MevpNodeState32 {
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
     const MevpNodeState32& st32);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
-    const float* v, const double* Pg, float* tdiv, const MevpParams& p);
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o,
     const MevpNodeState32& st, const float* tdiv, const MevpParams& p, int* err);
 // One member of a batched ensemble (device-resident table entry).
@@ -186,6 +205,7 @@ struct EnsembleMember {
     DevOps32 o;
     MevpNodeState32 st;
     const double* Pg;
+    const float* hP;
     float* tdiv;
     int tileW, tileH, tilesX;
     int stressBlock0, nodeBlock0;
