@@ -116,6 +116,7 @@ struct nsdg_kernel {
     DevOps32 dops32;
     StressMaps maps32 {};
     float* hP32 = nullptr; // P/(2 alpha) at the Gauss points (mixed precision)
+    float *cellX32 = nullptr, *cellY32 = nullptr; // FP32 transport cell operators (mixed precision)
     bool tmaStress = true; // which FP32 stress kernel the updates use (chosen by timing at initialise)
     cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1)
     {
@@ -336,6 +337,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         for (int i = 0; i < 14; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
+        add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -490,6 +492,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         uLast = zf(Ncg);
         vLast = zf(Ncg);
         hP32 = zf(9 * N);
+        cellX32 = upf(ops.cellX);
+        cellY32 = upf(ops.cellY);
     }
     derr = arena.take<int>(1);
     if (!derr)
@@ -581,10 +585,12 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         b.lmax[0] = 1; b.vmax[0] = 1.0; b.lmin[0] = 1; b.vmin[0] = 0.0;  // cice
         b.lmin[1] = 1; b.vmin[1] = 0.0;                                   // hice
         if (bbm) { b.lmax[2] = 1; b.vmax[2] = 1.0; b.lmin[2] = 1; b.vmin[2] = 1e-12; } // damage
+        const float* cx32 = mixed() ? cellX32 : nullptr;
+        const float* cy32 = mixed() ? cellY32 : nullptr;
         LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
-            STAGE_RK2_A, dt, a));
+            STAGE_RK2_A, dt, a, cx32, cy32));
         LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
-            STAGE_RK2_B, dt, b));
+            STAGE_RK2_B, dt, b, cx32, cy32));
     }
     if (bbm) {
         // stress transport with DGTransport<8> (BrittleCGDynamicsKernel.hpp:98-101)
@@ -1483,7 +1489,8 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
             return k->launchStress32(k->stream, mp, k->derr, kernel_id == 4 ? 1 : 0);
         default:
             return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
-                k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a);
+                k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a, k->mixed() ? k->cellX32 : nullptr,
+                k->mixed() ? k->cellY32 : nullptr);
         }
     };
     if (kernel_id < 0 || kernel_id > 4 || (kernel_id >= 3 && (bbm || !k->mixed())))

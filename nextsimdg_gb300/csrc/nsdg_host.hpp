@@ -57,6 +57,12 @@ struct ConstTables {
     double gw[5][16];         // [Q][q]       tensor Gauss weights
 };
 void fillConstTables(ConstTables& t);
+// FP32 copies of the tables the FP32 transport reads (same layout)
+struct ConstTables32 {
+    float psi[4][8][16];
+    float psie[4][3][3];
+    float psiew[4][4][3][8];
+};
 
 // The structured quad mesh with arbitrary vertex positions (ParametricMesh).
 struct HostMesh {

@@ -1,4 +1,4 @@
-// nsdg_kernels.cu — sm_103a kernels of the sea-ice dynamics hot path (FP64).
+// nsdg_kernels.cu — sm_103a kernels of the sea-ice dynamics hot path.
 //
 // One thread per element (element kernels) or per CG2 node (node kernels);
 // every accumulation into a node or an element is a gather in a fixed order,
@@ -9,6 +9,7 @@
 
 namespace nsdg {
 __constant__ ConstTables cT;
+__constant__ ConstTables32 cT32;
 }
 
 #include "nsdg_common.cuh"
@@ -19,12 +20,27 @@ namespace nsdg {
 cudaError_t uploadConstTables()
 {
     static ConstTables host;
+    static ConstTables32 host32;
     static bool filled = false;
     if (!filled) {
         fillConstTables(host);
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 8; ++b)
+                for (int c = 0; c < 16; ++c)
+                    host32.psi[a][b][c] = static_cast<float>(host.psi[a][b][c]);
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int c = 0; c < 3; ++c)
+                    host32.psie[a][b][c] = static_cast<float>(host.psie[a][b][c]);
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b)
+                for (int c = 0; c < 3; ++c)
+                    for (int d = 0; d < 8; ++d)
+                        host32.psiew[a][b][c][d] = static_cast<float>(host.psiew[a][b][c][d]);
         filled = true;
     }
-    return cudaMemcpyToSymbol(cT, &host, sizeof(ConstTables));
+    const cudaError_t e = cudaMemcpyToSymbol(cT, &host, sizeof(ConstTables));
+    return e != cudaSuccess ? e : cudaMemcpyToSymbol(cT32, &host32, sizeof(ConstTables32));
 }
 
 namespace {
@@ -209,29 +225,29 @@ template <int DG> struct Cell {
 
 // upwind flux at the ED edge Gauss points between trace 1 (cell 1: bottom /
 // left) and trace 2 (cell 2: top / right)
-template <int DG>
-__device__ __forceinline__ void upwind(const double* nv, const double* t1, const double* t2, double* tmp)
+template <int DG, typename T = double>
+__device__ __forceinline__ void upwind(const T* nv, const T* t1, const T* t2, T* tmp)
 {
     constexpr int ED = DGTraits<DG>::ED;
-    double vg[ED], g1[ED], g2[ED];
-    edgeGauss<ED>(nv, vg);
-    edgeGauss<ED>(t1, g1);
-    edgeGauss<ED>(t2, g2);
+    T vg[ED], g1[ED], g2[ED];
+    edgeGauss<ED, T>(nv, vg);
+    edgeGauss<ED, T>(t1, g1);
+    edgeGauss<ED, T>(t2, g2);
 #pragma unroll
     for (int g = 0; g < ED; ++g)
-        tmp[g] = fmax(vg[g], 0.0) * g1[g] + fmin(vg[g], 0.0) * g2[g];
+        tmp[g] = fmax(vg[g], T(0)) * g1[g] + fmin(vg[g], T(0)) * g2[g];
 }
 // acc += sdt * sum_g tmp(g) PSIe_w<DG,ED,E>(g, :)
-template <int DG>
-__device__ __forceinline__ void addEdge(double* acc, double sdt, const double* tmp, int E)
+template <int DG, typename T = double>
+__device__ __forceinline__ void addEdge(T* acc, T sdt, const T* tmp, int E)
 {
     constexpr int ED = DGTraits<DG>::ED;
 #pragma unroll
     for (int j = 0; j < DG; ++j) {
-        double s = 0.0;
+        T s = T(0);
 #pragma unroll
         for (int g = 0; g < ED; ++g)
-            s += tmp[g] * cT.psiew[ED][E][g][j];
+            s += tmp[g] * tab<T>::psiew(ED, E, g, j);
         acc[j] += sdt * s;
     }
 }
@@ -316,9 +332,16 @@ struct TransportArgs {
     const double* nvY;
     double dt;
     int mode;
+    const float* cellX32; // FP32 copies of cellX / cellY (T = float)
+    const float* cellY32;
 };
 
-template <int DG, int NF>
+// One Runge-Kutta stage of DGTransport for NF fields.  T is the type of the
+// flux arithmetic (cell term, edge traces, upwind fluxes, the accumulated
+// right-hand side): double reproduces the reference's arithmetic; float is
+// the mixed-precision transport, whose fields, inverse mass matrices and
+// Runge-Kutta combination stay FP64.
+template <int DG, int NF, typename T>
 __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, StageFields f)
 {
     constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q, ED = DGTraits<DG>::ED;
@@ -329,53 +352,68 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         return;
     const int nx = m.nx, ny = m.ny;
     const int ix = static_cast<int>(c % nx), iy = static_cast<int>(c / nx);
-    const double dt = a.dt;
+    const T dt = static_cast<T>(a.dt);
     const bool ice = m.ice[c] != 0;
+    const T* cellX;
+    const T* cellY;
+    if constexpr (sizeof(T) == 4) {
+        cellX = a.cellX32;
+        cellY = a.cellY32;
+    } else {
+        cellX = a.cellX;
+        cellY = a.cellY;
+    }
 
-    double own[NF][DG], acc[NF][DG];
+    double own[NF][DG];
+    T ownT[NF][DG], acc[NF][DG];
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
         loadCell<DG>(f.src[k], N, c, own[k]);
 #pragma unroll
-        for (int j = 0; j < DG; ++j)
-            acc[k][j] = 0.0;
+        for (int j = 0; j < DG; ++j) {
+            ownT[k][j] = static_cast<T>(own[k][j]);
+            acc[k][j] = T(0);
+        }
     }
 
     // cell term: dt * sum_q (cellX_iq vx(q) + cellY_iq vy(q)) phi(q)
     if constexpr (DG > 1) {
         if (ice) {
-            double vxg[QQ], vyg[QQ], pg[NF][QQ];
-            double vx[DG], vy[DG];
-            loadCell<DG>(a.velx, N, c, vx);
-            loadCell<DG>(a.vely, N, c, vy);
+            T vxg[QQ], vyg[QQ], pg[NF][QQ];
+            T vx[DG], vy[DG];
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                vx[j] = static_cast<T>(a.velx[j * N + c]);
+                vy[j] = static_cast<T>(a.vely[j * N + c]);
+            }
 #pragma unroll
             for (int q = 0; q < QQ; ++q) {
-                double sx = 0.0, sy = 0.0;
+                T sx = T(0), sy = T(0);
 #pragma unroll
                 for (int j = 0; j < DG; ++j) {
-                    sx += vx[j] * cT.psi[Q][j][q];
-                    sy += vy[j] * cT.psi[Q][j][q];
+                    sx += vx[j] * tab<T>::psi(Q, j, q);
+                    sy += vy[j] * tab<T>::psi(Q, j, q);
                 }
                 vxg[q] = sx;
                 vyg[q] = sy;
 #pragma unroll
                 for (int k = 0; k < NF; ++k) {
-                    double sp = 0.0;
+                    T sp = T(0);
 #pragma unroll
                     for (int j = 0; j < DG; ++j)
-                        sp += own[k][j] * cT.psi[Q][j][q];
+                        sp += ownT[k][j] * tab<T>::psi(Q, j, q);
                     pg[k][q] = sp;
                 }
             }
 #pragma unroll
             for (int i = 0; i < DG; ++i) {
-                double t[NF];
+                T t[NF];
 #pragma unroll
                 for (int k = 0; k < NF; ++k)
-                    t[k] = 0.0;
+                    t[k] = T(0);
 #pragma unroll
                 for (int q = 0; q < QQ; ++q) {
-                    const double mq = a.cellX[(i * QQ + q) * N + c] * vxg[q] + a.cellY[(i * QQ + q) * N + c] * vyg[q];
+                    const T mq = cellX[(i * QQ + q) * N + c] * vxg[q] + cellY[(i * QQ + q) * N + c] * vyg[q];
 #pragma unroll
                     for (int k = 0; k < NF; ++k)
                         t[k] += mq * pg[k][q];
@@ -387,22 +425,29 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         }
     }
 
-    double nv[ED], t1[ED], t2[ED], tmp[ED], nb[DG];
+    T nv[ED], t1[ED], t2[ED], tmp[ED], nb[DG];
+    auto loadNb = [&](const double* src, size_t cc) {
+#pragma unroll
+        for (int j = 0; j < DG; ++j)
+            nb[j] = static_cast<T>(src[j * N + cc]);
+    };
+    auto loadNv = [&](const double* nvp, size_t ne, size_t e) {
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            nv[k] = static_cast<T>(nvp[k * ne + e]);
+    };
     // left Y-edge (this cell is "cell 2"), interior edges only
     if (ix >= 1) {
         const size_t c1 = c - 1;
         if (ice && m.ice[c1]) {
-            const size_t e = size_t(iy) * (nx + 1) + ix;
-#pragma unroll
-            for (int k = 0; k < ED; ++k)
-                nv[k] = a.nvY[k * m.nYe + e];
+            loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix);
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
-                loadCell<DG>(f.src[k], N, c1, nb);
-                traceRight<DG>(nb, t1);
-                traceLeft<DG>(own[k], t2);
-                upwind<DG>(nv, t1, t2, tmp);
-                addEdge<DG>(acc[k], dt, tmp, 3);
+                loadNb(f.src[k], c1);
+                traceRight<DG, T>(nb, t1);
+                traceLeft<DG, T>(ownT[k], t2);
+                upwind<DG, T>(nv, t1, t2, tmp);
+                addEdge<DG, T>(acc[k], dt, tmp, 3);
             }
         }
     }
@@ -410,17 +455,14 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
     if (ix + 1 <= nx - 1) {
         const size_t c2 = c + 1;
         if (ice && m.ice[c2]) {
-            const size_t e = size_t(iy) * (nx + 1) + ix + 1;
-#pragma unroll
-            for (int k = 0; k < ED; ++k)
-                nv[k] = a.nvY[k * m.nYe + e];
+            loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix + 1);
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
-                loadCell<DG>(f.src[k], N, c2, nb);
-                traceRight<DG>(own[k], t1);
-                traceLeft<DG>(nb, t2);
-                upwind<DG>(nv, t1, t2, tmp);
-                addEdge<DG>(acc[k], -dt, tmp, 1);
+                loadNb(f.src[k], c2);
+                traceRight<DG, T>(ownT[k], t1);
+                traceLeft<DG, T>(nb, t2);
+                upwind<DG, T>(nv, t1, t2, tmp);
+                addEdge<DG, T>(acc[k], -dt, tmp, 1);
             }
         }
     }
@@ -428,17 +470,14 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
     if (iy >= 1) {
         const size_t c1 = c - nx;
         if (ice && m.ice[c1]) {
-            const size_t e = size_t(iy) * nx + ix;
-#pragma unroll
-            for (int k = 0; k < ED; ++k)
-                nv[k] = a.nvX[k * m.nXe + e];
+            loadNv(a.nvX, m.nXe, size_t(iy) * nx + ix);
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
-                loadCell<DG>(f.src[k], N, c1, nb);
-                traceTop<DG>(nb, t1);
-                traceBottom<DG>(own[k], t2);
-                upwind<DG>(nv, t1, t2, tmp);
-                addEdge<DG>(acc[k], dt, tmp, 0);
+                loadNb(f.src[k], c1);
+                traceTop<DG, T>(nb, t1);
+                traceBottom<DG, T>(ownT[k], t2);
+                upwind<DG, T>(nv, t1, t2, tmp);
+                addEdge<DG, T>(acc[k], dt, tmp, 0);
             }
         }
     }
@@ -446,17 +485,14 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
     if (iy + 1 <= ny - 1) {
         const size_t c2 = c + nx;
         if (ice && m.ice[c2]) {
-            const size_t e = size_t(iy + 1) * nx + ix;
-#pragma unroll
-            for (int k = 0; k < ED; ++k)
-                nv[k] = a.nvX[k * m.nXe + e];
+            loadNv(a.nvX, m.nXe, size_t(iy + 1) * nx + ix);
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
-                loadCell<DG>(f.src[k], N, c2, nb);
-                traceTop<DG>(own[k], t1);
-                traceBottom<DG>(nb, t2);
-                upwind<DG>(nv, t1, t2, tmp);
-                addEdge<DG>(acc[k], -dt, tmp, 2);
+                loadNb(f.src[k], c2);
+                traceTop<DG, T>(ownT[k], t1);
+                traceBottom<DG, T>(nb, t2);
+                upwind<DG, T>(nv, t1, t2, tmp);
+                addEdge<DG, T>(acc[k], -dt, tmp, 2);
             }
         }
     }
@@ -466,28 +502,27 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         const size_t e = static_cast<size_t>(m.perEntry[4 * p + 3]);
         if (!m.ice[p1] || !m.ice[p2])
             continue;
-        const double* nvp = type == 0 ? a.nvX : a.nvY;
-        const size_t ne = type == 0 ? m.nXe : m.nYe;
-#pragma unroll
-        for (int k = 0; k < ED; ++k)
-            nv[k] = nvp[k * ne + e];
+        loadNv(type == 0 ? a.nvX : a.nvY, type == 0 ? m.nXe : m.nYe, e);
 #pragma unroll
         for (int k = 0; k < NF; ++k) {
-            double b1[DG], b2[DG];
-            loadCell<DG>(f.src[k], N, p1, b1);
-            loadCell<DG>(f.src[k], N, p2, b2);
-            if (type == 0) {
-                traceTop<DG>(b1, t1);
-                traceBottom<DG>(b2, t2);
-            } else {
-                traceRight<DG>(b1, t1);
-                traceLeft<DG>(b2, t2);
+            T b1[DG], b2[DG];
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                b1[j] = static_cast<T>(f.src[k][j * N + p1]);
+                b2[j] = static_cast<T>(f.src[k][j * N + p2]);
             }
-            upwind<DG>(nv, t1, t2, tmp);
+            if (type == 0) {
+                traceTop<DG, T>(b1, t1);
+                traceBottom<DG, T>(b2, t2);
+            } else {
+                traceRight<DG, T>(b1, t1);
+                traceLeft<DG, T>(b2, t2);
+            }
+            upwind<DG, T>(nv, t1, t2, tmp);
             if (size_t(p1) == c)
-                addEdge<DG>(acc[k], -dt, tmp, type == 0 ? 2 : 1);
+                addEdge<DG, T>(acc[k], -dt, tmp, type == 0 ? 2 : 1);
             if (size_t(p2) == c)
-                addEdge<DG>(acc[k], dt, tmp, type == 0 ? 0 : 3);
+                addEdge<DG, T>(acc[k], dt, tmp, type == 0 ? 0 : 3);
         }
     }
     // Dirichlet (closed) boundaries: outflow only (DGTransport.cpp:306-351)
@@ -497,34 +532,28 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         for (int s = 0; s < 4; ++s) {
             if (!(seg & (1 << s)))
                 continue;
-            size_t e;
-            const double* nvp;
-            size_t ne;
-            if (s == 0) { e = size_t(iy) * nx + ix; nvp = a.nvX; ne = m.nXe; }
-            else if (s == 1) { e = size_t(iy) * (nx + 1) + ix + 1; nvp = a.nvY; ne = m.nYe; }
-            else if (s == 2) { e = size_t(iy + 1) * nx + ix; nvp = a.nvX; ne = m.nXe; }
-            else { e = size_t(iy) * (nx + 1) + ix; nvp = a.nvY; ne = m.nYe; }
-            double vg[ED];
-#pragma unroll
-            for (int k = 0; k < ED; ++k)
-                nv[k] = nvp[k * ne + e];
-            edgeGauss<ED>(nv, vg);
+            if (s == 0) loadNv(a.nvX, m.nXe, size_t(iy) * nx + ix);
+            else if (s == 1) loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix + 1);
+            else if (s == 2) loadNv(a.nvX, m.nXe, size_t(iy + 1) * nx + ix);
+            else loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix);
+            T vg[ED];
+            edgeGauss<ED, T>(nv, vg);
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
-                if (s == 0) traceBottom<DG>(own[k], t1);
-                else if (s == 1) traceRight<DG>(own[k], t1);
-                else if (s == 2) traceTop<DG>(own[k], t1);
-                else traceLeft<DG>(own[k], t1);
-                double tg[ED];
-                edgeGauss<ED>(t1, tg);
+                if (s == 0) traceBottom<DG, T>(ownT[k], t1);
+                else if (s == 1) traceRight<DG, T>(ownT[k], t1);
+                else if (s == 2) traceTop<DG, T>(ownT[k], t1);
+                else traceLeft<DG, T>(ownT[k], t1);
+                T tg[ED];
+                edgeGauss<ED, T>(t1, tg);
 #pragma unroll
                 for (int g = 0; g < ED; ++g)
-                    tmp[g] = tg[g] * ((s == 0 || s == 3) ? fmax(-vg[g], 0.0) : fmax(vg[g], 0.0));
-                addEdge<DG>(acc[k], -dt, tmp, s);
+                    tmp[g] = tg[g] * ((s == 0 || s == 3) ? fmax(-vg[g], T(0)) : fmax(vg[g], T(0)));
+                addEdge<DG, T>(acc[k], -dt, tmp, s);
             }
         }
     }
-    // inverse mass and the Runge-Kutta combination
+    // inverse mass (FP64) and the Runge-Kutta combination (FP64)
     double Mi[DG * DG];
 #pragma unroll
     for (int i = 0; i < DG * DG; ++i)
@@ -537,7 +566,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
             double s = 0.0;
 #pragma unroll
             for (int j = 0; j < DG; ++j)
-                s += Mi[i * DG + j] * acc[k][j];
+                s += Mi[i * DG + j] * static_cast<double>(acc[k][j]);
             r[i] = s;
         }
         switch (a.mode) {
@@ -1718,14 +1747,24 @@ cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const
 
 cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const double* cellX,
     const double* cellY, const double* minv, const double* velx, const double* vely,
-    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f)
+    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f, const float* cellX32,
+    const float* cellY32)
 {
-    TransportArgs a { m, cellX, cellY, minv, velx, vely, nvX, nvY, dt, mode };
+    TransportArgs a { m, cellX, cellY, minv, velx, vely, nvX, nvY, dt, mode, cellX32, cellY32 };
     const unsigned g = blocksFor(m.N);
+    if (cellX32 && cellY32) {
+        switch (f.nf) {
+        case 1: NSDG_DG_SWITCH(dg, (kTransportStage<D, 1, float><<<g, kBlock, 0, s>>>(a, f))); break;
+        case 2: NSDG_DG_SWITCH(dg, (kTransportStage<D, 2, float><<<g, kBlock, 0, s>>>(a, f))); break;
+        case 3: NSDG_DG_SWITCH(dg, (kTransportStage<D, 3, float><<<g, kBlock, 0, s>>>(a, f))); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (f.nf) {
-    case 1: NSDG_DG_SWITCH(dg, (kTransportStage<D, 1><<<g, kBlock, 0, s>>>(a, f))); break;
-    case 2: NSDG_DG_SWITCH(dg, (kTransportStage<D, 2><<<g, kBlock, 0, s>>>(a, f))); break;
-    case 3: NSDG_DG_SWITCH(dg, (kTransportStage<D, 3><<<g, kBlock, 0, s>>>(a, f))); break;
+    case 1: NSDG_DG_SWITCH(dg, (kTransportStage<D, 1, double><<<g, kBlock, 0, s>>>(a, f))); break;
+    case 2: NSDG_DG_SWITCH(dg, (kTransportStage<D, 2, double><<<g, kBlock, 0, s>>>(a, f))); break;
+    case 3: NSDG_DG_SWITCH(dg, (kTransportStage<D, 3, double><<<g, kBlock, 0, s>>>(a, f))); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

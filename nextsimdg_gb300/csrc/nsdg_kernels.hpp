@@ -88,10 +88,13 @@ cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* 
 cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
     const double* vely, double* nvX, double* nvY);
 // One Runge-Kutta stage of the DG transport operator for nf fields sharing a
-// velocity (DGTransport.cpp:435-566).
+// velocity (DGTransport.cpp:435-566).  With FP32 copies of the cell
+// operators (cellX32, cellY32) the flux arithmetic is FP32; the fields, the
+// inverse mass matrices and the stage combination stay FP64.
 cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const double* cellX,
     const double* cellY, const double* minv, const double* velx, const double* vely,
-    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f);
+    const double* nvX, const double* nvY, int mode, double dt, const StageFields& f,
+    const float* cellX32 = nullptr, const float* cellY32 = nullptr);
 
 // --- interpolation / preparation ----------------------------------------
 // DG -> CG2 Lagrange averaging of nf (<=2) DG fields (Interpolations.cpp:144-204).
