@@ -334,7 +334,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (P.precision == NSDG_PRECISION_MIXED) {
         add(324 * ops32Ld(N), 4);
         add(18 * N, 4);
-        for (int i = 0; i < 14; ++i) add(Ncg, 4);
+        for (int i = 0; i < 12; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
@@ -484,8 +484,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             return p;
         };
         tdiv32 = zf(18 * N);
-        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.A, &st32.uo, &st32.vo, &st32.c1,
-            &st32.c1b, &st32.fau, &st32.fav, &st32.rhfc, &st32.gu, &st32.gv };
+        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.A, &st32.uo, &st32.vo, &st32.c1b,
+            &st32.rhfc, &st32.c1beta, &st32.ku, &st32.kv };
         for (float** q : f32)
             *q = zf(Ncg);
         tdivLast = zf(18 * N);
@@ -635,7 +635,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
             LCH(launchMevpPrepNodes(s, dm, st, mp));
             LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp, mixed() ? hP32 : nullptr));
             if (mixed())
-                LCH(launchMevpPrepNodes32(s, dm, st, st32));
+                LCH(launchMevpPrepNodes32(s, dm, st, st32, P.beta));
         }
         if (loop && mixed()) {
             const int sv = saveLast(s, nullptr, nullptr, nullptr);

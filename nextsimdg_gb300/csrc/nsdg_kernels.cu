@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
 // ===========================================================================
 // mEVP, mixed precision
 // ===========================================================================
-__global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f)
+__global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f, double beta)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
@@ -1041,13 +1041,12 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeSta
     f.A[i] = static_cast<float>(st.cgA[i]);
     f.uo[i] = static_cast<float>(st.uo[i]);
     f.vo[i] = static_cast<float>(st.vo[i]);
-    f.c1[i] = static_cast<float>(st.c1[i]);
     f.c1b[i] = static_cast<float>(st.c1b[i]);
-    f.fau[i] = static_cast<float>(st.fau[i]);
-    f.fav[i] = static_cast<float>(st.fav[i]);
     f.rhfc[i] = static_cast<float>(st.rhfc[i]);
-    f.gu[i] = static_cast<float>(st.gu[i]);
-    f.gv[i] = static_cast<float>(st.gv[i]);
+    // the iteration-independent parts of the momentum update, formed in FP64
+    f.c1beta[i] = static_cast<float>(st.c1[i] * beta);
+    f.ku[i] = static_cast<float>(st.c1[i] * st.u[i] + st.cgA[i] * st.fau[i] - st.gu[i]);
+    f.kv[i] = static_cast<float>(st.c1[i] * st.v[i] + st.cgA[i] * st.fav[i] - st.gv[i]);
 }
 
 // The FP64 kernel kMevpStress with FP32 operators and state.  The strain
@@ -1341,12 +1340,14 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     const float uOcnRel = uo - u, vOcnRel = v - vo;
     const float absocn = sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
     const float A = st.A[i];
-    const float Fo = static_cast<float>(p.F_ocean), beta = static_cast<float>(p.beta);
+    const float Fo = static_cast<float>(p.F_ocean);
     const float focn = Fo * absocn;
     const float rden = 1.0f / (st.c1b[i] + A * focn);
-    const float c1 = st.c1[i];
-    float un = rden * (c1 * (beta * u + st.u0[i]) + A * (st.fau[i] + focn * uo) - st.rhfc[i] * u - st.gu[i] + mx);
-    float vn = rden * (c1 * (beta * v + st.v0[i]) + A * (st.fav[i] + focn * vo) + st.rhfc[i] * v - st.gv[i] + my);
+    const float c1beta = st.c1beta[i], rhfc = st.rhfc[i], Afocn = A * focn;
+    // c1 (beta u + u0) + A (fau + focn uo) - rhfc u - gu + mx, with the
+    // iteration-independent part ku = c1 u0 + A fau - gu formed once per step
+    float un = rden * (c1beta * u + st.ku[i] + Afocn * uo - rhfc * u + mx);
+    float vn = rden * (c1beta * v + st.kv[i] + Afocn * vo + rhfc * v + my);
     if (!isfinite(un) || !isfinite(vn))
         atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
     if (dir) {
@@ -1828,9 +1829,9 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 }
 
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32)
+    const MevpNodeState32& st32, double beta)
 {
-    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32);
+    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, beta);
     return cudaGetLastError();
 }
 namespace {

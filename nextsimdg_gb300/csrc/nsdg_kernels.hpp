@@ -183,17 +183,15 @@ struct MevpNodeState32 {
     float* A;
     float* uo;
     float* vo;
-    float* c1;
-    float* c1b;
-    float* fau;
-    float* fav;
-    float* rhfc;
-    float* gu;
-    float* gv;
+    float* c1b;     // rho H / dt (1 + beta)
+    float* rhfc;    // rho H fc
+    float* c1beta;  // rho H / dt * beta
+    float* ku;      // rho H / dt u0 + A F_atm |wind| uwind - rho H g dxSSH (formed in FP64)
+    float* kv;
 };
 // after launchMevpPrepNodes: FP32 copies of the per-step node constants
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32);
+    const MevpNodeState32& st32, double beta);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o,
