@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <exception>
@@ -519,6 +520,14 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
 // resident blocks.  Both compute the same values.
 int nsdg_kernel::chooseStress32()
 {
+    // NSDG_STRESS_KERNEL=tma|global fixes the choice (for profilers, whose
+    // serialised launches make the timing below meaningless)
+    if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
+        if (std::strcmp(env, "tma") == 0 || std::strcmp(env, "global") == 0) {
+            tmaStress = std::strcmp(env, "tma") == 0;
+            return NSDG_OK;
+        }
+    }
     const MevpParams mp = mevpParams(120.0);
     cudaEvent_t a, b;
     if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
