@@ -118,6 +118,7 @@ struct nsdg_kernel {
     StressMaps maps32 {};
     float* hP32 = nullptr; // P/(2 alpha) at the Gauss points (mixed precision)
     float *cellX32 = nullptr, *cellY32 = nullptr; // FP32 transport cell operators (mixed precision)
+    float2* invmHL = nullptr; // inverse lumped CG2 mass as {hi, lo} floats (mixed precision)
     bool tmaStress = true; // which FP32 stress kernel the updates use (chosen by timing at initialise)
     cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1)
     {
@@ -339,6 +340,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
+        add(Ncg, 8);                                        // inverse lumped mass {hi, lo}
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -495,6 +497,18 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         hP32 = zf(9 * N);
         cellX32 = upf(ops.cellX);
         cellY32 = upf(ops.cellY);
+        {
+            std::vector<float2> hl(Ncg);
+            for (size_t i = 0; i < Ncg; ++i) {
+                const float hi = static_cast<float>(invm[i]);
+                hl[i] = make_float2(hi, static_cast<float>(invm[i] - static_cast<double>(hi)));
+            }
+            invmHL = arena.take<float2>(Ncg);
+            if (!invmHL)
+                e = cudaErrorMemoryAllocation;
+            else if (e == cudaSuccess)
+                e = cudaMemcpy(invmHL, hl.data(), Ncg * sizeof(float2), cudaMemcpyHostToDevice);
+        }
     }
     derr = arena.take<int>(1);
     if (!derr)
@@ -659,7 +673,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
                     LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
                 } else {
                     LCH(launchStress32(s, mp, derr));
-                    LCH(launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, derr));
+                    LCH(launchMevpMomentum32(s, dm, invmHL, st32, tdiv32, mp, derr));
                 }
             }
         }
@@ -688,7 +702,7 @@ int nsdg_kernel::mixedIterations(cudaStream_t s, double dt, int count, int* errW
     for (int it = 0; it < count; ++it) {
         cudaError_t e = launchStress32(s, mp, errWord);
         if (e == cudaSuccess)
-            e = launchMevpMomentum32(s, dm, dops, st32, tdiv32, mp, errWord);
+            e = launchMevpMomentum32(s, dm, invmHL, st32, tdiv32, mp, errWord);
         if (e != cudaSuccess)
             return fail(NSDG_ERR_CUDA, std::string("mEVP iteration: ") + cudaGetErrorString(e));
         launches += 2;
@@ -1490,7 +1504,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                        : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
             if (!bbm && k->mixed())
-                return launchMevpMomentum32(k->stream, k->dm, k->dops, k->st32, k->tdiv32, mp, k->derr);
+                return launchMevpMomentum32(k->stream, k->dm, k->invmHL, k->st32, k->tdiv32, mp, k->derr);
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
         case 3:
@@ -1750,6 +1764,7 @@ struct nsdg_ensemble {
         d.ice = k->dm.ice;
         d.cg2Dir = k->dm.cg2Dir;
         d.invm2 = k->dops.invm2;
+        d.invmHL = k->invmHL;
         d.o = k->dops32;
         d.st = k->st32;
         d.Pg = k->Pg;

@@ -1214,10 +1214,21 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
     const size_t N = m.N;
     const size_t e = size_t(x0) + le;
     const bool active = e < N && m.ice[e];
-    // the 9 CG2 velocities of the element and P/alpha (loaded while the copy lands)
+    // P/(8 alpha), P/(2 alpha) (fixed during the sub-cycle) are loaded while the
+    // copy lands; launched as a programmatic dependent of the previous
+    // kernel, everything up to here overlaps that kernel's tail, and the
+    // velocities and divergence it wrote are read only after the wait
     float ul[9], vl[9];
     double Pa[3];
     float hP[3];
+    if (active) {
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+            Pa[qq] = Pg[(3 * part + qq) * N + e];
+            hP[qq] = hPg[(3 * part + qq) * N + e];
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (active) {
         const size_t s2 = 2 * size_t(m.nx) + 1;
         const size_t ix = e % m.nx, iy = e / m.nx;
@@ -1227,11 +1238,6 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
             const size_t nd = base + (j % 3) + (j / 3) * s2;
             ul[j] = u[nd];
             vl[j] = v[nd];
-        }
-#pragma unroll
-        for (int qq = 0; qq < 3; ++qq) {
-            Pa[qq] = Pg[(3 * part + qq) * N + e];
-            hP[qq] = hPg[(3 * part + qq) * N + e];
         }
     }
     __syncthreads(); // the barriers are initialised before anyone polls them
@@ -1305,12 +1311,18 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
 
 // Body of the mixed-precision node kernel for CG2 node i.
 __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, size_t i, const uint8_t* __restrict__ cg2Dir,
-    const double* __restrict__ invm2, const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p,
+    const float2* __restrict__ invmHL, const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p,
     int* __restrict__ err)
 {
     const int s2 = 2 * nx + 1;
     const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
     const bool dir = cg2Dir[i] != 0;
+    // per-step constants first (a programmatic dependent launch overlaps
+    // them with the stress kernel's tail), then the wait for its results
+    const float2 im = invmHL[i];
+    const float uo = st.uo[i], vo = st.vo[i], A = st.A[i];
+    const float c1b = st.c1b[i], c1beta = st.c1beta[i], rhfc = st.rhfc[i], ku = st.ku[i], kv = st.kv[i];
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     float dSx = 0.f, dSy = 0.f;
     if (!dir) {
         int cxs[2], lxs[2], cys[2], lys[2];
@@ -1331,23 +1343,21 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
             }
         }
     }
-    // divided by the lumped mass in FP64
-    const double invm = invm2[i];
-    const float mx = static_cast<float>(static_cast<double>(dSx) * invm);
-    const float my = static_cast<float>(static_cast<double>(dSy) * invm);
+    // divided by the lumped mass: its FP64 inverse held as the unevaluated sum
+    // hi + lo of two floats (48 significant bits), applied with FP32 FMAs
+    const float mx = fmaf(dSx, im.y, dSx * im.x);
+    const float my = fmaf(dSy, im.y, dSy * im.x);
     const float u = st.u[i], v = st.v[i];
-    const float uo = st.uo[i], vo = st.vo[i];
     const float uOcnRel = uo - u, vOcnRel = v - vo;
     const float absocn = sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
-    const float A = st.A[i];
     const float Fo = static_cast<float>(p.F_ocean);
     const float focn = Fo * absocn;
-    const float rden = 1.0f / (st.c1b[i] + A * focn);
-    const float c1beta = st.c1beta[i], rhfc = st.rhfc[i], Afocn = A * focn;
+    const float rden = 1.0f / (c1b + A * focn);
+    const float Afocn = A * focn;
     // c1 (beta u + u0) + A (fau + focn uo) - rhfc u - gu + mx, with the
     // iteration-independent part ku = c1 u0 + A fau - gu formed once per step
-    float un = rden * (c1beta * u + st.ku[i] + Afocn * uo - rhfc * u + mx);
-    float vn = rden * (c1beta * v + st.kv[i] + Afocn * vo + rhfc * v + my);
+    float un = rden * (c1beta * u + ku + Afocn * uo - rhfc * u + mx);
+    float vn = rden * (c1beta * v + kv + Afocn * vo + rhfc * v + my);
     if (!isfinite(un) || !isfinite(vn))
         atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
     if (dir) {
@@ -1358,13 +1368,13 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     st.v[i] = vn;
 }
 
-__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, DevOps o, MevpNodeState32 st,
-    const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
+__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, const float2* __restrict__ invmHL,
+    MevpNodeState32 st, const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= m.Ncg)
         return;
-    mevpMomentum32Node(m.nx, m.ny, m.N, i, m.cg2Dir, o.invm2, st, tdiv, p, err);
+    mevpMomentum32Node(m.nx, m.ny, m.N, i, m.cg2Dir, invmHL, st, tdiv, p, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1397,7 +1407,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleM
     const size_t i = (static_cast<size_t>(blockIdx.x) - M.nodeBlock0) * kBlock + threadIdx.x;
     if (i >= M.Ncg)
         return;
-    mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.invm2, M.st, M.tdiv, p, err);
+    mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.invmHL, M.st, M.tdiv, p, err);
 }
 
 __global__ void kWidenVelocity(size_t n, const float* __restrict__ u32, const float* __restrict__ v32,
@@ -1876,9 +1886,17 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
 cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err)
 {
-    kMevpStress32Tma<<<blocksFor(m.N, kTmaElems), kTmaElems * kStressParts, kTmaSmem, s>>>(maps.g, maps.a, m, u, v,
-        Pg, hP, tdiv, p, err);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocksFor(m.N, kTmaElems));
+    cfg.blockDim = dim3(kTmaElems * kStressParts);
+    cfg.dynamicSmemBytes = kTmaSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kMevpStress32Tma, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
 }
 
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
@@ -1887,11 +1905,19 @@ cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32&
     kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, hP, tdiv, p);
     return cudaGetLastError();
 }
-cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o, const MevpNodeState32& st,
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2* invmHL, const MevpNodeState32& st,
     const float* tdiv, const MevpParams& p, int* err)
 {
-    kMevpMomentum32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, tdiv, p, err);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocksFor(m.Ncg));
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kMevpMomentum32, m, invmHL, st, tdiv, p, err);
 }
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& p)

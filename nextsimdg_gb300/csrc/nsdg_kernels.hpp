@@ -194,7 +194,8 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
     const MevpNodeState32& st32, double beta);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
-cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const DevOps& o,
+// invmHL: the FP64 inverse lumped mass as float2 {hi, lo}, hi + lo = 1/m to 48 bits
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2* invmHL,
     const MevpNodeState32& st, const float* tdiv, const MevpParams& p, int* err);
 // One member of a batched ensemble (device-resident table entry).
 struct EnsembleMember {
@@ -203,6 +204,7 @@ struct EnsembleMember {
     const uint8_t* ice;
     const uint8_t* cg2Dir;
     const double* invm2;
+    const float2* invmHL;
     DevOps32 o;
     MevpNodeState32 st;
     const double* Pg;
