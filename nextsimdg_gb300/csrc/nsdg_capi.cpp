@@ -119,6 +119,8 @@ struct nsdg_kernel {
     float* hP32 = nullptr; // P/(2 alpha) at the Gauss points (mixed precision)
     float *cellX32 = nullptr, *cellY32 = nullptr; // FP32 transport cell operators (mixed precision)
     float2* invmHL = nullptr; // inverse lumped CG2 mass as {hi, lo} floats (mixed precision)
+    BbmOps32 bbm32 {};        // FP32 BBM operators (mixed precision BBM)
+    float *cellX8_32 = nullptr, *cellY8_32 = nullptr; // FP32 DG8 stress-transport operators
     bool tmaStress = true; // which FP32 stress kernel the updates use (chosen by timing at initialise)
     cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1)
     {
@@ -333,14 +335,20 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(8 * N); add(8 * N); add(3 * nXe); add(3 * nYe); add(24 * N); add(24 * N);
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
-    if (P.precision == NSDG_PRECISION_MIXED) {
+    if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
         add(324 * ops32Ld(N), 4);
         add(18 * N, 4);
         for (int i = 0; i < 12; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
+        add(Ncg, 8);                              // inverse lumped mass {hi, lo}
+    }
+    if (P.precision == NSDG_PRECISION_MIXED) {
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
-        add(Ncg, 8);                                        // inverse lumped mass {hi, lo}
+    }
+    if (P.precision == NSDG_PRECISION_MIXED && bbm) {
+        add(ops.gx.size(), 4); add(ops.gy.size(), 4); add(ops.w.size(), 4); add(ops.wdam.size(), 4);
+        add(ops.d1.size(), 4); add(ops.d2.size(), 4); add(ops.cellX8.size(), 4); add(ops.cellY8.size(), 4);
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -450,14 +458,28 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     cgTmp = z(Ncg);
     partials = z((N + 255) / 256 + 1);
     dsum = z(1);
+    auto upf = [&](const std::vector<double>& src) {
+        std::vector<float> tmp(src.begin(), src.end());
+        float* p = arena.take<float>(tmp.size());
+        if (!p) { e = cudaErrorMemoryAllocation; return p; }
+        if (e == cudaSuccess) e = cudaMemcpy(p, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice);
+        return p;
+    };
     if (mixed()) {
-        auto upf = [&](const std::vector<double>& src) {
-            std::vector<float> tmp(src.begin(), src.end());
-            float* p = arena.take<float>(tmp.size());
-            if (!p) { e = cudaErrorMemoryAllocation; return p; }
-            if (e == cudaSuccess) e = cudaMemcpy(p, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice);
-            return p;
-        };
+        cellX32 = upf(ops.cellX);
+        cellY32 = upf(ops.cellY);
+    }
+    if (mixed() && bbm) {
+        bbm32.gx = upf(ops.gx);
+        bbm32.gy = upf(ops.gy);
+        bbm32.w = upf(ops.w);
+        bbm32.wdam = upf(ops.wdam);
+        bbm32.d1 = upf(ops.d1);
+        bbm32.d2 = upf(ops.d2);
+        cellX8_32 = upf(ops.cellX8);
+        cellY8_32 = upf(ops.cellY8);
+    }
+    if (mixed() && !bbm) {
         {
             // one [324][ld] block (G_x, G_y, A_1, A_2), rows padded to ld
             const size_t ld = ops32Ld(N);
@@ -495,8 +517,6 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         uLast = zf(Ncg);
         vLast = zf(Ncg);
         hP32 = zf(9 * N);
-        cellX32 = upf(ops.cellX);
-        cellY32 = upf(ops.cellY);
         {
             std::vector<float2> hl(Ncg);
             for (size_t i = 0; i < Ncg; ++i) {
@@ -634,10 +654,12 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
             b.k1[k] = sK1 + k * 8 * N;
             b.dst[k] = fld[k];
         }
+        const float* cx8 = mixed() ? cellX8_32 : nullptr;
+        const float* cy8 = mixed() ? cellY8_32 : nullptr;
         LCH(launchTransportStage(s, dm, 8, dops.cellX8, dops.cellY8, dops.minv8, velx8, vely8, nvX8,
-            nvY8, STAGE_RK2_A, dt, a));
+            nvY8, STAGE_RK2_A, dt, a, cx8, cy8));
         LCH(launchTransportStage(s, dm, 8, dops.cellX8, dops.cellY8, dops.minv8, velx8, vely8, nvX8,
-            nvY8, STAGE_RK2_B, dt, b));
+            nvY8, STAGE_RK2_B, dt, b, cx8, cy8));
     }
     // --- prepareIteration (CGDynamicsKernel.cpp:260-276) ---
     {
@@ -688,7 +710,8 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         BbmNodeState st { u, v, avgU, avgV, cgH, cgA, uo, vo, ua, va, uGrad, vGrad };
         LCH(launchBbmPrepNodes(s, dm, st));
         for (int it = 0; it < nS; ++it) {
-            LCH(launchBbmStress(s, dm, dops, dg, u, v, hice, cice, damage, s11, s12, s22, contrib, bp, derr));
+            LCH(launchBbmStress(s, dm, dops, dg, u, v, hice, cice, damage, s11, s12, s22, contrib, bp, derr,
+                mixed() ? &bbm32 : nullptr));
             LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr));
         }
     }
@@ -1092,8 +1115,6 @@ int nsdg_kernel_create(int rheology, int dg_comp, const nsdg_params* params, nsd
     if (p.n_steps < 1 || !(p.alpha > 0) || !(p.beta >= 0) || !(p.rho_ice > 0))
         return NSDG_ERR_BAD_ARG;
     if (p.precision != NSDG_PRECISION_FP64 && p.precision != NSDG_PRECISION_MIXED)
-        return NSDG_ERR_UNSUPPORTED;
-    if (p.precision == NSDG_PRECISION_MIXED && rheology != NSDG_RHEOLOGY_MEVP)
         return NSDG_ERR_UNSUPPORTED;
     try {
         nsdg_kernel* k = new nsdg_kernel();
@@ -1500,7 +1521,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
             if (!bbm && k->mixed())
                 return k->launchStress32(k->stream, mp, k->derr);
             return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
-                             k->s11, k->s12, k->s22, k->contrib, bp, k->derr)
+                             k->s11, k->s12, k->s22, k->contrib, bp, k->derr, k->mixed() ? &k->bbm32 : nullptr)
                        : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
             if (!bbm && k->mixed())

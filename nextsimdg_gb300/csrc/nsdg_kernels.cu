@@ -1434,8 +1434,23 @@ __global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState s
     st.avgV[i] = 0.0;
 }
 
-template <int DG>
-__global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, DevOps o, const double* __restrict__ u,
+// Element operators of the BBM stress kernel in the compute type T.
+template <typename T> struct BbmOps {
+    const T* gx;
+    const T* gy;
+    const T* w;
+    const T* wdam;
+    const T* d1;
+    const T* d2;
+    const double* hsize;
+};
+
+// BBM stress, damage and divergence for one element.  T = double is the
+// reference's arithmetic; T = float is the mixed-precision kernel (FP32
+// operators and arithmetic, including exp/pow/sqrt; the stress, damage and
+// divergence are stored FP64 for the FP64 transport of the stress fields).
+template <int DG, typename T>
+__global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, const double* __restrict__ u,
     const double* __restrict__ v, const double* __restrict__ h, const double* __restrict__ a,
     double* __restrict__ damage, double* __restrict__ s11, double* __restrict__ s12,
     double* __restrict__ s22, double* __restrict__ contrib, BbmParams p, int* __restrict__ err)
@@ -1448,96 +1463,101 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, DevOps o, const 
     const size_t s2 = 2 * size_t(m.nx) + 1;
     const size_t ix = e % m.nx, iy = e / m.nx;
     const size_t base = 2 * s2 * iy + 2 * ix;
-    double ul[9], vl[9];
+    T ul[9], vl[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
         const size_t nd = base + (j % 3) + (j / 3) * s2;
-        ul[j] = ice ? u[nd] : 0.0;
-        vl[j] = ice ? v[nd] : 0.0;
+        ul[j] = ice ? static_cast<T>(u[nd]) : T(0);
+        vl[j] = ice ? static_cast<T>(v[nd]) : T(0);
     }
-    double hc[DG], ac[DG], dc[DG], c11[8], c12[8], c22[8];
-    loadCell<DG>(h, N, e, hc);
-    loadCell<DG>(a, N, e, ac);
-    loadCell<DG>(damage, N, e, dc);
+    T hc[DG], ac[DG], dc[DG], c11[8], c12[8], c22[8];
+#pragma unroll
+    for (int j = 0; j < DG; ++j) {
+        hc[j] = static_cast<T>(h[j * N + e]);
+        ac[j] = static_cast<T>(a[j * N + e]);
+        dc[j] = static_cast<T>(damage[j * N + e]);
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        c11[k] = s11[k * N + e];
-        c12[k] = s12[k * N + e];
-        c22[k] = s22[k * N + e];
+        c11[k] = static_cast<T>(s11[k * N + e]);
+        c12[k] = static_cast<T>(s12[k * N + e]);
+        c22[k] = static_cast<T>(s22[k * N + e]);
     }
-    const double dt = p.dt;
-    const double hi = o.hsize[e];
-    const double scale_coef = sqrt(0.1 / hi);
-    const double tdScale = hi * sqrt(2. * (1. + p.nu0) * p.rho_ice);
-    double n11[8], n12[8], n22[8], nd[DG];
+    const T dt = static_cast<T>(p.dt);
+    const T nu0 = static_cast<T>(p.nu0);
+    const T hi = static_cast<T>(o.hsize[e]);
+    const T scale_coef = sqrt(T(0.1) / hi);
+    const T tdScale = hi * sqrt(T(2.) * (T(1.) + nu0) * static_cast<T>(p.rho_ice));
+    T n11[8], n12[8], n22[8], nd[DG];
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        n11[k] = n12[k] = n22[k] = 0.0;
+        n11[k] = n12[k] = n22[k] = T(0);
 #pragma unroll
     for (int k = 0; k < DG; ++k)
-        nd[k] = 0.0;
+        nd[k] = T(0);
 #pragma unroll 1
     for (int q = 0; q < 9; ++q) {
-        double hs = 0.0, as = 0.0, ds = 0.0;
+        T hs = T(0), as = T(0), ds = T(0);
 #pragma unroll
         for (int j = 0; j < DG; ++j) {
-            hs += hc[j] * cT.psi[3][j][q];
-            as += ac[j] * cT.psi[3][j][q];
-            ds += dc[j] * cT.psi[3][j][q];
+            hs += hc[j] * tab<T>::psi(3, j, q);
+            as += ac[j] * tab<T>::psi(3, j, q);
+            ds += dc[j] * tab<T>::psi(3, j, q);
         }
-        const double hG = fmax(hs, 0.0);
-        const double aG = fmin(fmax(as, 0.0), 1.0);
-        double dG = fmin(fmax(ds, 1e-12), 1.0);
-        double ex = 0.0, ey = 0.0, exv = 0.0, eyu = 0.0;
+        const T hG = fmax(hs, T(0));
+        const T aG = fmin(fmax(as, T(0)), T(1));
+        T dG = fmin(fmax(ds, T(1e-12)), T(1));
+        T ex = T(0), ey = T(0), exv = T(0), eyu = T(0);
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-            const double gxq = o.gx[(q * 9 + j) * N + e];
-            const double gyq = o.gy[(q * 9 + j) * N + e];
+            const T gxq = o.gx[(q * 9 + j) * N + e];
+            const T gyq = o.gy[(q * 9 + j) * N + e];
             ex = fma(gxq, ul[j], ex);
             ey = fma(gyq, vl[j], ey);
             exv = fma(gxq, vl[j], exv);
             eyu = fma(gyq, ul[j], eyu);
         }
-        const double e11 = ex, e22 = ey, e12 = 0.5 * (exv + eyu);
-        double g11 = 0.0, g12 = 0.0, g22 = 0.0;
+        const T e11 = ex, e22 = ey, e12 = T(0.5) * (exv + eyu);
+        T g11 = T(0), g12 = T(0), g22 = T(0);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            g11 += c11[k] * cT.psi[3][k][q];
-            g12 += c12[k] * cT.psi[3][k][q];
-            g22 += c22[k] * cT.psi[3][k][q];
+            g11 += c11[k] * tab<T>::psi(3, k, q);
+            g12 += c12[k] * tab<T>::psi(3, k, q);
+            g22 += c22[k] * tab<T>::psi(3, k, q);
         }
-        double sigma_n = 0.5 * (g11 + g22);
-        const double expC = exp(p.compaction_param * (1.0 - aG));
-        const double powalphaexpC = pow(dG * expC, p.exponent_relaxation_sigma - 1);
-        const double time_viscous = p.lambda * powalphaexpC;
-        const double Pmax = p.P0 * pow(hG, p.exponent_compression_factor + 1.) * expC;
-        const double tildeP = (sigma_n < 0.0) ? fmin(-Pmax / sigma_n, 1.0) : 0.;
-        const double multiplicator = time_viscous / (time_viscous + (1. - tildeP) * dt);
-        const double elasticity = hG * p.young * dG * expC;
-        const double Dunit_factor = dt * elasticity / (1. - (p.nu0 * p.nu0));
-        g11 += Dunit_factor * (e11 + p.nu0 * e22);
-        g22 += Dunit_factor * (p.nu0 * e11 + e22);
-        g12 += Dunit_factor * e12 * (1. - p.nu0);
+        T sigma_n = T(0.5) * (g11 + g22);
+        const T expC = exp(static_cast<T>(p.compaction_param) * (T(1.0) - aG));
+        const T powalphaexpC = pow(dG * expC, static_cast<T>(p.exponent_relaxation_sigma) - T(1));
+        const T time_viscous = static_cast<T>(p.lambda) * powalphaexpC;
+        const T Pmax = static_cast<T>(p.P0) * pow(hG, static_cast<T>(p.exponent_compression_factor) + T(1.)) * expC;
+        const T tildeP = (sigma_n < T(0)) ? fmin(-Pmax / sigma_n, T(1.0)) : T(0);
+        const T multiplicator = time_viscous / (time_viscous + (T(1.) - tildeP) * dt);
+        const T elasticity = hG * static_cast<T>(p.young) * dG * expC;
+        const T Dunit_factor = dt * elasticity / (T(1.) - (nu0 * nu0));
+        g11 += Dunit_factor * (e11 + nu0 * e22);
+        g22 += Dunit_factor * (nu0 * e11 + e22);
+        g12 += Dunit_factor * e12 * (T(1.) - nu0);
         g11 *= multiplicator;
         g22 *= multiplicator;
         g12 *= multiplicator;
-        sigma_n = 0.5 * (g11 + g22);
-        const double dd = g11 - g22;
-        const double tau = sqrt(0.25 * (dd * dd) + g12 * g12);
-        const double cohesion = p.C_lab * scale_coef * hG;
-        const double compr = p.compr_strength * scale_coef * hG;
-        double dcrit = (tau + p.tan_phi * sigma_n > 0.) ? cohesion / (tau + p.tan_phi * sigma_n) : 1.;
+        sigma_n = T(0.5) * (g11 + g22);
+        const T dd = g11 - g22;
+        const T tau = sqrt(T(0.25) * (dd * dd) + g12 * g12);
+        const T tan_phi = static_cast<T>(p.tan_phi);
+        const T cohesion = static_cast<T>(p.C_lab) * scale_coef * hG;
+        const T compr = static_cast<T>(p.compr_strength) * scale_coef * hG;
+        T dcrit = (tau + tan_phi * sigma_n > T(0)) ? cohesion / (tau + tan_phi * sigma_n) : T(1.);
         dcrit = (sigma_n < -compr) ? -compr / sigma_n : dcrit;
-        dcrit = fmin(dcrit, 1.0);
-        const double td = tdScale / sqrt(elasticity);
-        const double relax = (1. - dcrit) * dt / td;
+        dcrit = fmin(dcrit, T(1.0));
+        const T td = tdScale / sqrt(elasticity);
+        const T relax = (T(1.) - dcrit) * dt / td;
         dG -= dG * relax;
         g11 -= g11 * relax;
         g12 -= g12 * relax;
         g22 -= g22 * relax;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const double wk = o.w[(k * 9 + q) * N + e];
+            const T wk = o.w[(k * 9 + q) * N + e];
             n11[k] = fma(wk, g11, n11[k]);
             n12[k] = fma(wk, g12, n12[k]);
             n22[k] = fma(wk, g22, n22[k]);
@@ -1561,12 +1581,12 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, DevOps o, const 
         atomicOr(err, DEV_ERR_NONFINITE_STRESS);
 #pragma unroll 1
     for (int j = 0; j < 9; ++j) {
-        double tx = 0.0, ty = 0.0;
+        T tx = T(0), ty = T(0);
         if (ice) {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const double d1 = o.d1[(j * 8 + k) * N + e];
-                const double d2v = o.d2[(j * 8 + k) * N + e];
+                const T d1 = o.d1[(j * 8 + k) * N + e];
+                const T d2v = o.d2[(j * 8 + k) * N + e];
                 tx = fma(d1, n11[k], fma(d2v, n12[k], tx));
                 ty = fma(d1, n12[k], fma(d2v, n22[k], ty));
             }
@@ -1955,13 +1975,24 @@ cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeSt
 
 cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg, const double* u,
     const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,
-    double* s22, double* contrib, const BbmParams& p, int* err)
+    double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32)
 {
     const unsigned g = blocksFor(m.N);
+    if (o32) {
+        const BbmOps<float> of { o32->gx, o32->gy, o32->w, o32->wdam, o32->d1, o32->d2, o.hsize };
+        switch (dg) {
+        case 1: kBbmStress<1, float><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        case 3: kBbmStress<3, float><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        case 6: kBbmStress<6, float><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
+    const BbmOps<double> od { o.gx, o.gy, o.w, o.wdam, o.d1, o.d2, o.hsize };
     switch (dg) {
-    case 1: kBbmStress<1><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
-    case 3: kBbmStress<3><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
-    case 6: kBbmStress<6><<<g, kBlock, 0, s>>>(m, o, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    case 1: kBbmStress<1, double><<<g, kBlock, 0, s>>>(m, od, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    case 3: kBbmStress<3, double><<<g, kBlock, 0, s>>>(m, od, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+    case 6: kBbmStress<6, double><<<g, kBlock, 0, s>>>(m, od, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -253,9 +253,18 @@ struct BbmNodeState {
 cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st);
 // Per-step Gauss-point constants of the BBM update from h and A:
 // 0 hG, 1 expC, 2 Pmax, 3 elasticity, 4 Dunit_factor / dt ... (9 x 5 per element)
-cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg,
-    const double* u, const double* v, const double* h, const double* a, double* damage,
-    double* s11, double* s12, double* s22, double* contrib, const BbmParams& p, int* err);
+// FP32 copies of the BBM element operators (mixed precision)
+struct BbmOps32 {
+    const float* gx;
+    const float* gy;
+    const float* w;
+    const float* wdam;
+    const float* d1;
+    const float* d2;
+};
+cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg, const double* u,
+    const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,
+    double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32 = nullptr);
 cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
     const BbmNodeState& st, const double* contrib, const BbmParams& p, int* err);
 

@@ -106,6 +106,50 @@ def test_full_size_matches_oracle(gpu, oracle):
     assert all(v <= TOL for v in worst.values()), worst
 
 
+@pytest.mark.parametrize("dg,alpha,steps", [(3, 300.0, 30), (6, 300.0, 30), (6, 1500.0, 100)])
+def test_long_horizon_matches_oracle(gpu, oracle, dg, alpha, steps):
+    """64 x 64 box test over the longest horizons on which the oracle's own
+    sensitivity to h x (1 + 1e-14) stays near 1e-13 (30 steps at alpha = 300:
+    between steps 35 and 40 a clamp/limiter switch amplifies it to 4e-5;
+    100 steps at alpha = 1500): FP64 parity 1e-10 for h, A (all DG
+    components), u, v and the ice-ocean stress."""
+    box = BoxTest(64)
+    prm = dict(alpha=alpha, beta=alpha, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, dg, None, **prm)
+    o = _make(oracle.OracleKernel, box, dg, 0, **prm)
+    _advance(g, box, steps)
+    _advance(o, box, steps)
+    worst = _compare(g, o, ["hice", "cice", "u", "v", "uiostress", "viostress"], dg)
+    assert all(v <= TOL for v in worst.values()), worst
+    assert np.abs(o.getDG0Data("u")).max() > 1e-2
+
+
+@pytest.mark.parametrize("dg", [3, 6])
+def test_one_day_64_matches_oracle(gpu, oracle, dg):
+    """The CPU-runnable box test for a full simulated day: 64 x 64 cells,
+    DG1 (3 components) or DG2 transport, CG2 velocity, 100 mEVP iterations,
+    alpha = beta = 300, 720 steps of 120 s, the oracle on the same inputs.
+    The bar is 1e-10 relative where the oracle's own sensitivity (to h scaled
+    by 1 + 1e-14) stays below 1e-11; otherwise 10x that sensitivity (over a
+    day it is ~1e-4 for u: see test_long_horizon_matches_oracle)."""
+    box = BoxTest(64)
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, dg, None, **prm)
+    o = _make(oracle.OracleKernel, box, dg, 0, **prm)
+    o2 = oracle.OracleKernel(0, dg, **prm)
+    o2.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        o2.setData(name, arr * (1.0 + 1e-14) if name == "hice" else arr)
+    for k in (g, o, o2):
+        _advance(k, box, 720)
+    worst = _compare(g, o, ["hice", "cice", "u", "v", "uiostress", "viostress"], dg)
+    sens = max(_compare(o2, o, ["hice", "cice", "u", "v"], dg).values())
+    bar = TOL if sens < 1e-11 else 10.0 * sens
+    print(f"one day 64x64 DG{dg}: gpu vs oracle {worst}, oracle sensitivity {sens:.3e}, bar {bar:.1e}")
+    assert all(v <= bar for v in worst.values()), (worst, sens)
+    assert np.abs(o.getDG0Data("u")).max() > 1e-2
+
+
 def test_full_size_alpha300_within_oracle_sensitivity(gpu, oracle):
     """With alpha = beta = 300 on 2 km cells the mEVP iteration amplifies
     rounding (alpha*beta is far below its stability bound), so no 1e-10 bar
@@ -220,6 +264,28 @@ def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
     da = rms(g.getDG0Data("cice"), o.getDG0Data("cice"))
     assert max(du, dv) <= 1e-5, (du, dv)       # m/s
     assert dh <= 1e-6 and da <= 1e-6, (dh, da)  # m, fraction
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
+
+
+@pytest.mark.parametrize("n,steps", [(14, 3), (48, 3)])
+def test_bbm_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
+    """BBM in the mixed mode (FP32 stress/damage arithmetic and transport
+    fluxes, FP64 fields, inverse mass matrices and momentum): RMS error
+    against the FP64 oracle, stated bars."""
+    box = BoxTest(n)
+    prm = dict(n_steps=50)
+    g = _make(BBMDynamicsKernel, box, 6, None, precision=1, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 1, **prm)
+    for k in (g, o):
+        k.setData("damage", box.damage())
+    _advance(g, box, steps)
+    _advance(o, box, steps)
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
+    err = {f: rms(g.getDG0Data(f), o.getDG0Data(f)) for f in ("u", "v", "hice", "cice", "damage")}
+    print(f"BBM mixed {n}x{n}, {steps} steps: RMS vs oracle {err}")
+    assert max(err["u"], err["v"]) <= 1e-5, err           # m/s
+    assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
+    assert err["damage"] <= 1e-5, err
     assert np.abs(o.getDG0Data("u")).max() > 1e-3
 
 
