@@ -342,6 +342,58 @@ def learned_variant(args, box_eval, N: int, plain_ms: float):
     return out
 
 
+def bbm_variant(args, box, N: int, err_steps: int = 10):
+    """The BBM rheology (damage, DG8 stress transport) on the same box with
+    damage = 1, FP64 and mixed precision: throughput, and the velocity and
+    damage RMS after `err_steps` steps of the FP32 path and of the FP64 path
+    with h x (1 + 1e-14), both against the FP64 path."""
+    from nextsimdg_gb300._lib import NsdgError
+    from nextsimdg_gb300.boxtest import setup_kernel, step_forcing
+    from nextsimdg_gb300.dynamics import BBMDynamicsKernel
+    # the explicit elastic sub-steps must resolve the elastic wave: dt / n <=
+    # dx / (2 sqrt(E / rho)) (813 m/s with the default Young's modulus)
+    dx = box.L / box.nx
+    sub = max(NSTEPS, int(math.ceil(DT / (0.5 * dx / math.sqrt(5.9467e8 / 900.0)))))
+    sub = int(math.ceil(sub / 50.0)) * 50
+    out = {"sub_steps": sub, "damage_init": 1.0}
+    ks = {}
+    for name, prec, scale in (("fp64", 0, 1.0), ("fp64_h_times_1p1e-14", 0, 1.0 + 1e-14), ("fp32", 1, 1.0)):
+        k = BBMDynamicsKernel(dg_comp=DG, n_steps=sub, precision=prec)
+        k.initialise(box.coords(), False, box.mask())
+        for fname, arr in box.initial_fields().items():
+            k.setData(fname, arr * scale if fname == "hice" else arr)
+        k.setData("damage", box.damage())
+        ks[name] = k
+    try:
+        for s in range(err_steps):
+            for k in ks.values():
+                step_forcing(k, box, s)
+                k.update(s * DT, DT)
+        r = {n: {f: k.getDG0Data(f) for f in ("u", "v", "damage", "hice")} for n, k in ks.items()}
+        ref = r["fp64"]
+        rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+        out["error_vs_fp64"] = {"steps": err_steps}
+        for n in ("fp32", "fp64_h_times_1p1e-14"):
+            x = r[n]
+            out["error_vs_fp64"][n] = {"u_v_rms_m_per_s": rms(np.hypot(x["u"] - ref["u"], x["v"] - ref["v"])),
+                                       "damage_rms": rms(x["damage"] - ref["damage"]),
+                                       "h_rms_m": rms(x["hice"] - ref["hice"])}
+        for name in ("fp64", "fp32"):
+            k = ks[name]
+            steps = 3
+            ms = k.time_updates(DT, steps) / steps
+            sms, sname = k.time_kernel(0, 10)
+            mms, mname = k.time_kernel(1, 10)
+            out[name] = {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, sname + "_ms": sms,
+                         mname + "_ms": mms}
+        out["fp32_speedup"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
+    except NsdgError as ex:
+        out["error"] = str(ex)
+    for k in ks.values():
+        k.close()
+    return out
+
+
 def day_error(args, box, steps: int):
     """Velocity / thickness / concentration RMS after `steps` model steps: the
     headline precision path and the FP64 path with h scaled by (1 + 1e-14),
@@ -439,6 +491,8 @@ def run_ours(args, world, rank, local):
             "headline_speedup_over_this": oms / (ms_max / args.steps), "roofline": oroof}
         if prec and args.warm_train_iters > 0:
             variants["learned_fp32"] = learned_variant(args, box, N, ms_max / args.steps)
+        if prec and not args.no_bbm:
+            variants["bbm"] = bbm_variant(args, box, N)
     err = day_error(args, box, args.error_steps) if (prec and args.error_steps > 0 and world == 1) else None
 
     if rank == 0:
@@ -567,6 +621,7 @@ def main():
     ap.add_argument("--warm-iters", type=int, default=40, help="mEVP iterations after the learned warm start")
     ap.add_argument("--warm-samples", type=int, default=120, help="training samples (every 3rd step)")
     ap.add_argument("--warm-train-iters", type=int, default=2000, help="Adam steps (0: skip the learned variant)")
+    ap.add_argument("--no-bbm", action="store_true", help="skip the BBM variant")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident steps (for ncu captures): no e2e, no baselines")
     args = ap.parse_args()

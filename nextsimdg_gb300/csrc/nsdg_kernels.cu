@@ -1527,11 +1527,25 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         }
         T sigma_n = T(0.5) * (g11 + g22);
         const T expC = exp(static_cast<T>(p.compaction_param) * (T(1.0) - aG));
-        const T powalphaexpC = pow(dG * expC, static_cast<T>(p.exponent_relaxation_sigma) - T(1));
-        const T time_viscous = static_cast<T>(p.lambda) * powalphaexpC;
         const T Pmax = static_cast<T>(p.P0) * pow(hG, static_cast<T>(p.exponent_compression_factor) + T(1.)) * expC;
         const T tildeP = (sigma_n < T(0)) ? fmin(-Pmax / sigma_n, T(1.0)) : T(0);
-        const T multiplicator = time_viscous / (time_viscous + (T(1.) - tildeP) * dt);
+        T multiplicator;
+        if constexpr (sizeof(T) == 8) {
+            const T powalphaexpC = pow(dG * expC, static_cast<T>(p.exponent_relaxation_sigma) - T(1));
+            const T time_viscous = static_cast<T>(p.lambda) * powalphaexpC;
+            multiplicator = time_viscous / (time_viscous + (T(1.) - tildeP) * dt);
+        } else {
+            // lambda (d e^{C(1-A)})^(n-1) underflows FP32 in open water and
+            // 0 / (0 + 0) would follow where tildeP = 1: the same quantity as
+            // 1 / (1 + (1 - tildeP) dt / time_viscous) with the relaxation
+            // time taken in log space
+            const T logTv = log(static_cast<T>(p.lambda))
+                + (static_cast<T>(p.exponent_relaxation_sigma) - T(1))
+                    * (log(dG) + static_cast<T>(p.compaction_param) * (T(1.0) - aG));
+            const T open = T(1.) - tildeP;
+            const T ratio = open > T(0) ? open * dt * exp(-logTv) : T(0);
+            multiplicator = T(1) / (T(1) + ratio);
+        }
         const T elasticity = hG * static_cast<T>(p.young) * dG * expC;
         const T Dunit_factor = dt * elasticity / (T(1.) - (nu0 * nu0));
         g11 += Dunit_factor * (e11 + nu0 * e22);
