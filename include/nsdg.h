@@ -170,7 +170,10 @@ int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
  * mEVP kernels in NSDG_PRECISION_MIXED with the same parameters; they keep
  * their own setData / getDG0Data, which are ordered after the ensemble's
  * update.  The element tile shape of every grid size is chosen at creation by
- * timing the candidates on the GPU (nsdg_ensemble_tile reports the choice). */
+ * timing the candidates on the GPU; then the whole element phase is timed with
+ * those tiles and with the TMA-staged kernel (32 consecutive elements per
+ * block, 32 x 1) and the faster is kept (nsdg_ensemble_tile reports the
+ * choice; NSDG_STRESS_KERNEL=tma|global in the environment fixes it). */
 typedef struct nsdg_ensemble nsdg_ensemble;
 int nsdg_ensemble_create(nsdg_kernel* const* members, int n_members, nsdg_ensemble** out);
 int nsdg_ensemble_destroy(nsdg_ensemble* ens);

@@ -1749,8 +1749,10 @@ struct nsdg_ensemble {
     EnsembleMember* dMembers = nullptr;
     uint16_t* dStressMap = nullptr;
     uint16_t* dNodeMap = nullptr;
+    uint16_t* dTmaMap = nullptr;
     int* derr = nullptr;
-    int stressBlocks = 0, nodeBlocks = 0;
+    int stressBlocks = 0, nodeBlocks = 0, tmaBlocks = 0;
+    bool useTma = false; // element phase: TMA-staged batched kernel (else the tiled global-load one)
     std::vector<int> tileW;
     cudaGraphExec_t graph = nullptr;
     double graphDt = -1.0;
@@ -1791,6 +1793,7 @@ struct nsdg_ensemble {
         d.Pg = k->Pg;
         d.hP = k->hP32;
         d.tdiv = k->tdiv32;
+        d.maps = k->maps32;
         d.tileW = tw;
         d.tileH = stressElementsPerBlock() / tw;
         d.tilesX = (d.nx + tw - 1) / tw;
@@ -1801,6 +1804,8 @@ struct nsdg_ensemble {
     {
         return static_cast<int>((d.Ncg + nodesPerBlock() - 1) / nodesPerBlock());
     }
+    static int tmaBlocksOf(const EnsembleMember& d) { return static_cast<int>((d.N + kTmaElems - 1) / kTmaElems); }
+    int chooseElementKernel();
     int autotune();
     int build();
     int ensureGraph(double dt);
@@ -1889,18 +1894,22 @@ int nsdg_ensemble::autotune()
 int nsdg_ensemble::build()
 {
     std::vector<EnsembleMember> table;
-    std::vector<uint16_t> smap, nmap;
+    std::vector<uint16_t> smap, nmap, tmap;
     for (size_t mi = 0; mi < members.size(); ++mi) {
         EnsembleMember d = describe(members[mi], tileW[mi]);
         d.stressBlock0 = static_cast<int>(smap.size());
         d.nodeBlock0 = static_cast<int>(nmap.size());
+        d.tmaBlock0 = static_cast<int>(tmap.size());
         smap.insert(smap.end(), stressBlocksOf(d), static_cast<uint16_t>(mi));
         nmap.insert(nmap.end(), nodeBlocksOf(d), static_cast<uint16_t>(mi));
+        tmap.insert(tmap.end(), tmaBlocksOf(d), static_cast<uint16_t>(mi));
         table.push_back(d);
     }
     stressBlocks = static_cast<int>(smap.size());
     nodeBlocks = static_cast<int>(nmap.size());
-    const size_t bytes = al(table.size() * sizeof(EnsembleMember)) + al(smap.size() * 2) + al(nmap.size() * 2) + al(4);
+    tmaBlocks = static_cast<int>(tmap.size());
+    const size_t bytes = al(table.size() * sizeof(EnsembleMember)) + al(smap.size() * 2) + al(nmap.size() * 2)
+        + al(tmap.size() * 2) + al(4);
     if (cudaMalloc(&dmem, bytes) != cudaSuccess)
         return fail(NSDG_ERR_CUDA, "ensemble: allocation failed");
     char* p = static_cast<char*>(dmem);
@@ -1910,13 +1919,77 @@ int nsdg_ensemble::build()
     p += al(smap.size() * 2);
     dNodeMap = reinterpret_cast<uint16_t*>(p);
     p += al(nmap.size() * 2);
+    dTmaMap = reinterpret_cast<uint16_t*>(p);
+    p += al(tmap.size() * 2);
     derr = reinterpret_cast<int*>(p);
     cudaError_t e = cudaMemcpy(dMembers, table.data(), table.size() * sizeof(EnsembleMember), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dStressMap, smap.data(), smap.size() * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dNodeMap, nmap.data(), nmap.size() * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dTmaMap, tmap.data(), tmap.size() * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("ensemble: upload failed: ") + cudaGetErrorString(e));
+    return chooseElementKernel();
+}
+
+// Times the element phase of the whole ensemble with the tiled global-load
+// kernel (autotuned tiles) and with the TMA-staged kernel, the divergence
+// redirected to scratch so that no member's state changes, and keeps the
+// faster.
+int nsdg_ensemble::chooseElementKernel()
+{
+    size_t total = 0;
+    for (auto* k : members)
+        total += 18 * k->N;
+    std::vector<EnsembleMember> table;
+    void* scratch = nullptr;
+    EnsembleMember* dT = nullptr;
+    if (cudaMalloc(&scratch, total * sizeof(float)) != cudaSuccess
+        || cudaMalloc(&dT, members.size() * sizeof(EnsembleMember)) != cudaSuccess) {
+        cudaFree(scratch);
+        return fail(NSDG_ERR_CUDA, "ensemble: timing allocation failed");
+    }
+    std::vector<EnsembleMember> host(members.size());
+    cudaError_t e = cudaMemcpy(host.data(), dMembers, host.size() * sizeof(EnsembleMember), cudaMemcpyDeviceToHost);
+    size_t off = 0;
+    for (size_t mi = 0; mi < host.size(); ++mi) {
+        host[mi].tdiv = static_cast<float*>(scratch) + off;
+        off += 18 * members[mi]->N;
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(dT, host.data(), host.size() * sizeof(EnsembleMember), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(scratch, 0, total * sizeof(float));
+    const nsdg_params& P = members[0]->P;
+    MevpParams mp { P.rho_ice, P.F_atm, P.F_ocean, P.fc, P.gravity, P.Pstar, P.DeltaMin, P.alpha, P.beta, 120.0 };
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float ms[2] = { 0, 0 };
+    for (int variant = 0; variant < 2 && e == cudaSuccess; ++variant) {
+        auto launch = [&]() {
+            return variant == 0 ? launchMevpStress32Batched(stream, dT, dStressMap, stressBlocks, mp)
+                                : launchMevpStress32TmaBatched(stream, dT, dTmaMap, tmaBlocks, mp, derr);
+        };
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r)
+            e = launch();
+        if (e == cudaSuccess) e = cudaEventRecord(a, stream);
+        for (int r = 0; r < 10 && e == cudaSuccess; ++r)
+            e = launch();
+        if (e == cudaSuccess) e = cudaEventRecord(b, stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[variant], a, b);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamSynchronize(stream);
+    cudaFree(scratch);
+    cudaFree(dT);
+    if (e != cudaSuccess)
+        return fail(NSDG_ERR_CUDA, std::string("ensemble: element kernel timing: ") + cudaGetErrorString(e));
+    useTma = ms[1] <= ms[0];
+    if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
+        if (std::strcmp(env, "tma") == 0) useTma = true;
+        if (std::strcmp(env, "global") == 0) useTma = false;
+    }
     return NSDG_OK;
 }
 
@@ -1945,7 +2018,8 @@ int nsdg_ensemble::ensureGraph(double dt)
         }
     }
     for (int it = 0; it < P.n_steps && st == NSDG_OK; ++it) {
-        e = launchMevpStress32Batched(stream, dMembers, dStressMap, stressBlocks, mp);
+        e = useTma ? launchMevpStress32TmaBatched(stream, dMembers, dTmaMap, tmaBlocks, mp, derr)
+                   : launchMevpStress32Batched(stream, dMembers, dStressMap, stressBlocks, mp);
         if (e == cudaSuccess)
             e = launchMevpMomentum32Batched(stream, dMembers, dNodeMap, nodeBlocks, mp, derr);
         if (e != cudaSuccess)
@@ -2105,8 +2179,13 @@ int nsdg_ensemble_tile(nsdg_ensemble* ens, int member, int* tile_w, int* tile_h)
 {
     if (!ens || !tile_w || !tile_h || member < 0 || member >= static_cast<int>(ens->members.size()))
         return NSDG_ERR_BAD_ARG;
-    *tile_w = ens->tileW[member];
-    *tile_h = stressElementsPerBlock() / ens->tileW[member];
+    if (ens->useTma) {
+        *tile_w = kTmaElems; // consecutive elements, operators staged by TMA
+        *tile_h = 1;
+    } else {
+        *tile_w = ens->tileW[member];
+        *tile_h = stressElementsPerBlock() / ens->tileW[member];
+    }
     return NSDG_OK;
 }
 

@@ -1192,28 +1192,27 @@ __device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int
 }
 } // namespace
 
-__global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(const __grid_constant__ CUtensorMap mapG,
-    const __grid_constant__ CUtensorMap mapA, DevMesh m, const float* __restrict__ u, const float* __restrict__ v,
-    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p,
-    int* __restrict__ err)
+// One block of the TMA-staged stress kernel: elements x0 .. x0+31 of a grid
+// (shared by the single-grid and the batched ensemble kernels).
+__device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const CUtensorMap* mapA, int nx, size_t N,
+    const uint8_t* __restrict__ ice, const float* __restrict__ u, const float* __restrict__ v,
+    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, const MevpParams& p,
+    int* __restrict__ err, int x0, unsigned char* smem)
 {
-    extern __shared__ __align__(128) unsigned char smem[];
     float* sT = reinterpret_cast<float*>(smem);                      // [162][32]: G_x|G_y, then A_1|A_2
     float (*fs)[9][kTmaElems] = reinterpret_cast<float (*)[9][kTmaElems]>(sT + kTmaRows * kTmaElems);
     uint64_t* bars = reinterpret_cast<uint64_t*>(fs[3]);             // 2 mbarriers, one per copy
     const int le = threadIdx.x % kTmaElems;
     const int part = threadIdx.x / kTmaElems;
-    const int x0 = blockIdx.x * kTmaElems;
     if (threadIdx.x == 0) {
         mbarInit(&bars[0], 1);
         mbarInit(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbarExpectTx(&bars[0], kTmaTileBytes);
-        tmaLoad2d(sT, &mapG, x0, 0, &bars[0]);
+        tmaLoad2d(sT, mapG, x0, 0, &bars[0]);
     }
-    const size_t N = m.N;
     const size_t e = size_t(x0) + le;
-    const bool active = e < N && m.ice[e];
+    const bool active = e < N && ice[e];
     // P/(8 alpha), P/(2 alpha) (fixed during the sub-cycle) are loaded while the
     // copy lands; launched as a programmatic dependent of the previous
     // kernel, everything up to here overlaps that kernel's tail, and the
@@ -1230,8 +1229,8 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (active) {
-        const size_t s2 = 2 * size_t(m.nx) + 1;
-        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t s2 = 2 * size_t(nx) + 1;
+        const size_t ix = e % nx, iy = e / nx;
         const size_t base = 2 * s2 * iy + 2 * ix;
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
@@ -1278,7 +1277,7 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
     if (threadIdx.x == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbarExpectTx(&bars[1], kTmaTileBytes);
-        tmaLoad2d(sT, &mapA, x0, 0, &bars[1]);
+        tmaLoad2d(sT, mapA, x0, 0, &bars[1]);
     }
     ok = mbarWaitBounded(&bars[1], 0);
     if (!__syncthreads_and(ok)) {
@@ -1307,6 +1306,15 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
         tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
         tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
     }
+}
+
+__global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(const __grid_constant__ CUtensorMap mapG,
+    const __grid_constant__ CUtensorMap mapA, DevMesh m, const float* __restrict__ u, const float* __restrict__ v,
+    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p,
+    int* __restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    stress32TmaBlock(&mapG, &mapA, m.nx, m.N, m.ice, u, v, Pg, hPg, tdiv, p, err, blockIdx.x * kTmaElems, smem);
 }
 
 // Body of the mixed-precision node kernel for CG2 node i.
@@ -1398,6 +1406,16 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32Batc
     const size_t e = inside ? size_t(iy) * M.nx + ix : 0;
     const bool active = inside && M.ice[e];
     mevpStress32Element(M.nx, M.N, active, e, le, part, M.o, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, fs);
+}
+
+__global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32TmaBatched(
+    const EnsembleMember* __restrict__ members, const uint16_t* __restrict__ blockMember, MevpParams p,
+    int* __restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const EnsembleMember& M = members[blockMember[blockIdx.x]];
+    const int x0 = (static_cast<int>(blockIdx.x) - M.tmaBlock0) * kTmaElems;
+    stress32TmaBlock(&M.maps.g, &M.maps.a, M.nx, M.N, M.ice, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, err, x0, smem);
 }
 
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
@@ -1913,8 +1931,11 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
     }
     // dynamic shared memory of the kernel (24 KB: one operator tile, the
     // stress terms, two mbarriers), set once
-    return cudaFuncSetAttribute(kMevpStress32Tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const cudaError_t e = cudaFuncSetAttribute(kMevpStress32Tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
         static_cast<int>(kTmaSmem));
+    return e != cudaSuccess ? e
+                            : cudaFuncSetAttribute(kMevpStress32TmaBatched,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmem));
 }
 
 cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
@@ -1962,8 +1983,31 @@ cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* memb
 cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& p, int* err)
 {
-    kMevpMomentum32Batched<<<blocks, kBlock, 0, s>>>(members, blockMember, p, err);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kMevpMomentum32Batched, members, blockMember, p, err);
+}
+cudaError_t launchMevpStress32TmaBatched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
+    int blocks, const MevpParams& p, int* err)
+{
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kTmaElems * kStressParts);
+    cfg.dynamicSmemBytes = kTmaSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kMevpStress32TmaBatched, members, blockMember, p, err);
 }
 int stressElementsPerBlock() { return kStressElems; }
 int nodesPerBlock() { return kBlock; }

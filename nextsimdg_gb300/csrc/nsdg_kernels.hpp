@@ -212,12 +212,18 @@ struct EnsembleMember {
     float* tdiv;
     int tileW, tileH, tilesX;
     int stressBlock0, nodeBlock0;
+    int tmaBlock0;   // first block of this member in the TMA-staged batched launch
+    StressMaps maps; // the member's tensor maps (64-byte aligned inside the device table)
 };
 // One launch each for the element and the node phase of every member.
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& p);
 cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& p, int* err);
+// The element phase of every member with the TMA-staged kernel: blocks of
+// kTmaElems consecutive elements, tensor maps read from the member table.
+cudaError_t launchMevpStress32TmaBatched(cudaStream_t s, const EnsembleMember* members,
+    const uint16_t* blockMember, int blocks, const MevpParams& p, int* err);
 int stressElementsPerBlock();
 int nodesPerBlock();
 

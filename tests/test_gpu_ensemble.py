@@ -52,8 +52,41 @@ def test_ensemble_members_match_single_runs(gpu):
             np.testing.assert_array_equal(a.getDG0Data(name), b.getDG0Data(name))
     for i in range(len(boxes)):
         w, h = ens.tile(i)
-        assert w * h == 64 and w in (64, 32, 16, 8)
+        # an autotuned 2-D tile of 64 elements, or 32 consecutive elements
+        # for the TMA-staged element kernel
+        assert (w * h == 64 and w in (64, 32, 16, 8)) or (w, h) == (32, 1)
     assert ens.launches_per_update() < 2 * PRM["n_steps"] + 20 * len(boxes)
+
+
+@pytest.mark.parametrize("kernel", ["tma", "global"])
+def test_ensemble_both_element_kernels_match_single_runs(gpu, kernel, monkeypatch):
+    """Each element kernel of the batched sub-cycle, forced through
+    NSDG_STRESS_KERNEL, reproduces the members' single runs bitwise."""
+    monkeypatch.setenv("NSDG_STRESS_KERNEL", kernel)
+    boxes = [BoxTest(24, seed=1), BoxTest(40, 33, seed=2)]
+    ens_members = [_member(b) for b in boxes]
+    solo = [_member(b) for b in boxes]
+    ens = Ensemble(ens_members)
+    for s in range(2):
+        for k, b in zip(ens_members, boxes):
+            uw, vw = b.wind(s * b.dt)
+            k.setData("uwind", uw)
+            k.setData("vwind", vw)
+        ens.update(s * 120.0, 120.0)
+        for k, b in zip(solo, boxes):
+            uw, vw = b.wind(s * b.dt)
+            k.setData("uwind", uw)
+            k.setData("vwind", vw)
+            k.update(s * 120.0, 120.0)
+    ens.synchronize()
+    for a, b in zip(ens_members, solo):
+        for name in ("u", "v", "hice", "cice"):
+            np.testing.assert_array_equal(a.getDG0Data(name), b.getDG0Data(name))
+    w, h = ens.tile(0)
+    if kernel == "tma":
+        assert (w, h) == (32, 1)
+    else:
+        assert w * h == 64
 
 
 def test_ensemble_rejects_fp64_members(gpu):
