@@ -110,7 +110,10 @@ const char* nsdg_kernel_last_error(const nsdg_kernel* k);
 /* Builds the mesh (landmask, Dirichlet lists from the mask and the four
  * domain edges), the FP64 per-element operators, and uploads them.
  * coords: (nx+1)*(ny+1)*2 doubles; mask: nx*ny doubles (1.0 = ice).
- * is_spherical != 0 returns NSDG_ERR_UNSUPPORTED. */
+ * is_spherical != 0: coords are (lon, lat) in radians; the mesh is rotated
+ * so that its poles lie in Greenland / Antarctica and the operators carry the
+ * spherical metric terms (DynamicsKernel.hpp:44-58, ParametricMap.cpp:298-353,
+ * CGDynamicsKernel.cpp:331-351). */
 int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny,
     const double* coords, int is_spherical, const double* mask);
 
@@ -167,7 +170,7 @@ int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
  * preparation and then the mEVP sub-cycle of all members as one element launch
  * and one node launch per iteration.  No reference counterpart: the reference
  * runs one model (one kernel) per process.  Members must be initialised
- * mEVP kernels in NSDG_PRECISION_MIXED with the same parameters; they keep
+ * Cartesian mEVP kernels in NSDG_PRECISION_MIXED with the same parameters; they keep
  * their own setData / getDG0Data, which are ordered after the ensemble's
  * update.  The element tile shape of every grid size is chosen at creation by
  * timing the candidates on the GPU; then the whole element phase is timed with

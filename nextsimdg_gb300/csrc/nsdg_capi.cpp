@@ -255,8 +255,12 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
 {
     if (!coords || !mask)
         return fail(NSDG_ERR_BAD_ARG, "initialise: null coords or mask");
-    if (spherical)
-        return fail(NSDG_ERR_UNSUPPORTED, "initialise: spherical coordinates are not supported");
+    if (spherical && rheology == NSDG_RHEOLOGY_BBM)
+        // the BBM's element size is sqrt(area) of the raw vertex coordinates
+        // (ParametricMesh.hpp:276-299, BBMStressUpdateStep.hpp:134,158): in
+        // radians on a sphere, which makes its relaxation times meaningless
+        return fail(NSDG_ERR_UNSUPPORTED, "initialise: BBM on spherical coordinates is not supported "
+                                          "(its element size would be in radians)");
     if (nx < 2 || ny < 2)
         return fail(NSDG_ERR_BAD_ARG, "initialise: the mesh needs nx >= 2 and ny >= 2");
     {
@@ -272,6 +276,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
 
     // --- host mesh (DynamicsKernel.hpp:44-75) ---
     mesh = HostMesh();
+    mesh.spherical = spherical != 0;
     mesh.nx = nx;
     mesh.ny = ny;
     const size_t nn = (nx + 1) * (ny + 1);
@@ -283,6 +288,10 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         if (!std::isfinite(mesh.vx[i]) || !std::isfinite(mesh.vy[i]))
             return fail(NSDG_ERR_BAD_ARG, "initialise: non-finite coordinate");
     }
+    // spherical meshes: (lon, lat) in radians, poles moved to Greenland /
+    // Antarctica as DynamicsKernel::initialise does (DynamicsKernel.hpp:49-51)
+    if (mesh.spherical)
+        mesh.rotatePoleToGreenland();
     N = nx * ny;
     mesh.ice.resize(N);
     for (size_t i = 0; i < N; ++i)
@@ -321,6 +330,10 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(ops.w.size()); add(ops.d1.size()); add(ops.d2.size());
     }
     add(ops.dxssh.size()); add(ops.dyssh.size()); add(Ncg); add(Ncg1);
+    if (mesh.spherical) {
+        add(ops.gm.size()); add(ops.a3.size() + 1); add(ops.dm.size() + 1);
+        add(ops.minvP.size()); add(ops.minv8P.size() + 1);
+    }
     if (bbm) {
         add(ops.cellX8.size()); add(ops.cellY8.size()); add(ops.minv8.size()); add(ops.wdam.size()); add(ops.hsize.size());
     }
@@ -336,7 +349,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
     if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
-        add(324 * ops32Ld(N), 4);
+        add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
         add(18 * N, 4);
         for (int i = 0; i < 12; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
@@ -349,6 +362,9 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (P.precision == NSDG_PRECISION_MIXED && bbm) {
         add(ops.gx.size(), 4); add(ops.gy.size(), 4); add(ops.w.size(), 4); add(ops.wdam.size(), 4);
         add(ops.d1.size(), 4); add(ops.d2.size(), 4); add(ops.cellX8.size(), 4); add(ops.cellY8.size(), 4);
+        if (mesh.spherical) {
+            add(ops.gm.size(), 4); add(ops.dm.size(), 4);
+        }
     }
     add((N + 255) / 256 + 1); add(1); add(1, 4);
     bytes += 4096;
@@ -369,6 +385,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     cudaError_t e = cudaSuccess;
     dm.nx = static_cast<int>(nx);
     dm.ny = static_cast<int>(ny);
+    dm.spherical = mesh.spherical ? 1 : 0;
     dm.N = N;
     dm.Ncg = Ncg;
     dm.Ncg1 = Ncg1;
@@ -400,6 +417,16 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         dops.w = upd(ops.w);
         dops.d1 = upd(ops.d1);
         dops.d2 = upd(ops.d2);
+    }
+    if (mesh.spherical) {
+        dops.minvP = upd(ops.minvP);
+        if (bbm)
+            dops.minv8P = upd(ops.minv8P);
+        dops.gm = upd(ops.gm);
+        if (bbm)
+            dops.dm = upd(ops.dm);
+        else
+            dops.a3 = upd(ops.a3);
     }
     dops.dxssh = upd(ops.dxssh);
     dops.dyssh = upd(ops.dyssh);
@@ -476,29 +503,41 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         bbm32.wdam = upf(ops.wdam);
         bbm32.d1 = upf(ops.d1);
         bbm32.d2 = upf(ops.d2);
+        bbm32.gm = mesh.spherical ? upf(ops.gm) : nullptr;
+        bbm32.dm = mesh.spherical ? upf(ops.dm) : nullptr;
         cellX8_32 = upf(ops.cellX8);
         cellY8_32 = upf(ops.cellY8);
     }
     if (mixed() && !bbm) {
         {
-            // one [324][ld] block (G_x, G_y, A_1, A_2), rows padded to ld
+            // one block of 81-row operators, rows padded to ld: G_x, G_y, A_1, A_2
+            // ([324][ld]); on a sphere G_x, G_y, G_m, A_1, A_2, A_3 ([486][ld])
             const size_t ld = ops32Ld(N);
-            std::vector<float> blk(324 * ld, 0.f);
-            const std::vector<double>* src[4] = { &ops.gx, &ops.gy, &ops.a1, &ops.a2 };
-            for (int b = 0; b < 4; ++b)
+            const bool sph = mesh.spherical;
+            const int nb = sph ? 6 : 4;
+            std::vector<float> blk(size_t(81) * nb * ld, 0.f);
+            const std::vector<double>* src4[4] = { &ops.gx, &ops.gy, &ops.a1, &ops.a2 };
+            const std::vector<double>* src6[6] = { &ops.gx, &ops.gy, &ops.gm, &ops.a1, &ops.a2, &ops.a3 };
+            for (int b = 0; b < nb; ++b) {
+                const std::vector<double>& o = sph ? *src6[b] : *src4[b];
                 for (size_t r = 0; r < 81; ++r)
                     for (size_t el = 0; el < N; ++el)
-                        blk[(81 * b + r) * ld + el] = static_cast<float>((*src[b])[r * N + el]);
+                        blk[(81 * b + r) * ld + el] = static_cast<float>(o[r * N + el]);
+            }
             float* p = arena.take<float>(blk.size());
             if (!p)
                 e = cudaErrorMemoryAllocation;
             else if (e == cudaSuccess)
                 e = cudaMemcpy(p, blk.data(), blk.size() * sizeof(float), cudaMemcpyHostToDevice);
+            const size_t gRows = sph ? 243 : 162;
             dops32.ld = ld;
+            dops32.rowsG = static_cast<int>(gRows);
             dops32.gx = p;
             dops32.gy = p ? p + 81 * ld : nullptr;
-            dops32.a1 = p ? p + 162 * ld : nullptr;
-            dops32.a2 = p ? p + 243 * ld : nullptr;
+            dops32.gm = (p && sph) ? p + 162 * ld : nullptr;
+            dops32.a1 = p ? p + gRows * ld : nullptr;
+            dops32.a2 = p ? p + (gRows + 81) * ld : nullptr;
+            dops32.a3 = (p && sph) ? p + (gRows + 162) * ld : nullptr;
             if (e == cudaSuccess)
                 e = makeStressMaps(dops32, &maps32);
         }
@@ -609,7 +648,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
     {
         const double* cgv[2] = { bbm ? avgU : u, bbm ? avgV : v };
         double* dgv[2] = { velx, vely };
-        LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minv, 2, cgv, dgv));
+        LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minvP ? dops.minvP : dops.minv, 2, cgv, dgv));
         LCH(launchNormalVelocity(s, dm, dg, velx, vely, nvX, nvY));
         StageFields a, b;
         const int nf = bbm ? 3 : 2;
@@ -639,7 +678,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         // stress transport with DGTransport<8> (BrittleCGDynamicsKernel.hpp:98-101)
         const double* cgv[2] = { avgU, avgV };
         double* dgv[2] = { velx8, vely8 };
-        LCH(launchCG2DG(s, dm, 8, dops.jw3, dops.minv8, 2, cgv, dgv));
+        LCH(launchCG2DG(s, dm, 8, dops.jw3, dops.minv8P ? dops.minv8P : dops.minv8, 2, cgv, dgv));
         LCH(launchNormalVelocity(s, dm, 8, velx8, vely8, nvX8, nvY8));
         StageFields a, b;
         double* fld[3] = { s11, s12, s22 };
@@ -1269,7 +1308,7 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
         const double* in[1] = { cg };
         double* outd[1] = { k->dgTmp };
         if (e == cudaSuccess)
-            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, k->dops.minv, 1, in, outd);
+            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, k->dops.minvP ? k->dops.minvP : k->dops.minv, 1, in, outd);
         src = k->dgTmp;
     } else if (s == "hice") src = k->hice;
     else if (s == "cice") src = k->cice;
@@ -2064,8 +2103,8 @@ int nsdg_ensemble_create(nsdg_kernel* const* members, int n_members, nsdg_ensemb
     const nsdg_params& P0 = members[0] ? members[0]->P : nsdg_params {};
     for (int i = 0; i < n_members; ++i) {
         const nsdg_kernel* k = members[i];
-        if (!k || !k->ready || k->rheology != NSDG_RHEOLOGY_MEVP || !k->mixed())
-            return NSDG_ERR_UNSUPPORTED; // initialised mEVP kernels in mixed precision only
+        if (!k || !k->ready || k->rheology != NSDG_RHEOLOGY_MEVP || !k->mixed() || k->mesh.spherical)
+            return NSDG_ERR_UNSUPPORTED; // initialised Cartesian mEVP kernels in mixed precision only
         const nsdg_params& P = k->P;
         if (P.n_steps != P0.n_steps || P.alpha != P0.alpha || P.beta != P0.beta || P.rho_ice != P0.rho_ice
             || P.F_ocean != P0.F_ocean || P.F_atm != P0.F_atm || P.fc != P0.fc || P.gravity != P0.gravity

@@ -186,6 +186,36 @@ void HostMesh::elementCoords(size_t e, double c[4][2]) const
         c[k][0] = vx[id[k]];
         c[k][1] = vy[id[k]];
     }
+    if (spherical) {
+        // no longitude jump across the element (ParametricMesh.hpp:196-209)
+        bool jump = false;
+        for (int k = 1; k < 4; ++k)
+            jump = jump || std::fabs(c[0][0] - c[k][0]) > 2.0 / 3.0 * M_PI;
+        if (jump)
+            for (int k = 0; k < 4; ++k)
+                if (c[k][0] < 0)
+                    c[k][0] += 2.0 * M_PI;
+    }
+}
+
+// The singular poles of the lon/lat grid moved to Greenland (75N 40W) and
+// Antarctica: rotation by 40 degrees about z, then 15 degrees about y.
+void HostMesh::rotatePoleToGreenland()
+{
+    const double aw = 40.0 * M_PI / 180.0, bw = 15.0 * M_PI / 180.0;
+    for (size_t i = 0; i < vx.size(); ++i) {
+        const double x = std::cos(vy[i]) * std::cos(vx[i]);
+        const double y = std::cos(vy[i]) * std::sin(vx[i]);
+        const double z = std::sin(vy[i]);
+        const double x1 = std::cos(aw) * x - std::sin(aw) * y;
+        const double y1 = std::sin(aw) * x + std::cos(aw) * y;
+        const double z1 = z;
+        const double x2 = std::cos(bw) * x1 - std::sin(bw) * z1;
+        const double y2 = y1;
+        const double z2 = std::sin(bw) * x1 + std::cos(bw) * z1;
+        vy[i] = std::asin(z2);
+        vx[i] = std::atan2(y2, x2);
+    }
 }
 
 // Bretschneider's formula for the quadrilateral area (ParametricMesh.hpp:276-295).
@@ -282,13 +312,21 @@ bool luInverse(int n, const double* A, double* out)
 // map T (dT/dxi in rows 0..1 of dxi, dT/deta in dxe) and J = det(dT).
 struct Geom {
     double dxi[2][16], deta[2][16], J[16];
+    double cl[16], sl[16]; // cos / sin of the latitude at the Gauss points (spherical)
+    bool spherical;
 };
 void geometry(const HostMesh& m, size_t e, int Q, Geom& g)
 {
     const Basis& b = basis();
     double c[4][2];
     m.elementCoords(e, c);
+    g.spherical = m.spherical;
     for (int q = 0; q < Q * Q; ++q) {
+        double lat = 0;
+        for (int k = 0; k < 4; ++k)
+            lat += c[k][1] * b.phi(1, k, Q, q);
+        g.cl[q] = std::cos(lat);
+        g.sl[q] = std::sin(lat);
         for (int r = 0; r < 2; ++r) {
             double sx = 0, sy = 0;
             for (int k = 0; k < 4; ++k) {
@@ -302,7 +340,8 @@ void geometry(const HostMesh& m, size_t e, int Q, Geom& g)
     }
 }
 
-// Inverse of the DG mass matrix M_ij = sum_q psi_i psi_j w_q J_q.
+// Inverse of the DG mass matrix M_ij = sum_q psi_i psi_j w_q J_q (times
+// cos(lat_q) on a spherical mesh: ParametricTools.hpp:109-153, 189-202).
 void inverseMass(const Geom& g, int dg, double* inv)
 {
     const Basis& b = basis();
@@ -312,7 +351,8 @@ void inverseMass(const Geom& g, int dg, double* inv)
         for (int j = 0; j < dg; ++j) {
             double s = 0;
             for (int q = 0; q < Q * Q; ++q)
-                s += (b.psi(i, Q, q) * (b.weight(Q, q) * g.J[q])) * b.psi(j, Q, q);
+                s += g.spherical ? (b.psi(i, Q, q) * (b.weight(Q, q) * g.J[q] * g.cl[q])) * b.psi(j, Q, q)
+                                 : (b.psi(i, Q, q) * (b.weight(Q, q) * g.J[q])) * b.psi(j, Q, q);
             M[i * dg + j] = s;
         }
     if (!luInverse(dg, M, inv))
@@ -364,6 +404,10 @@ void transportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads)
     ops.cellX.assign(size_t(dg) * QQ * N, 0.0);
     ops.cellY.assign(size_t(dg) * QQ * N, 0.0);
     ops.minv.assign(size_t(dg) * dg * N, 0.0);
+    if (m.spherical)
+        ops.minvP.assign(size_t(dg) * dg * N, 0.0);
+    else
+        ops.minvP.clear();
     ops.jwA.assign(size_t(QQ) * N, 0.0);
     ops.jw3.assign(9 * N, 0.0);
     const Basis& b = basis();
@@ -374,13 +418,16 @@ void transportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads)
             geometry(m, e, Q, g);
             cellTerms(g, dg, N, e, ops.cellX, ops.cellY);
             inverseMass(g, dg, inv);
-            for (int k = 0; k < dg * dg; ++k)
-                ops.minv[k * N + e] = inv[k];
-            for (int q = 0; q < QQ; ++q)
-                ops.jwA[q * N + e] = g.J[q] * b.weight(Q, q);
+            for (int k = 0; k < dg * dg; ++k) { // transport: M^{-1} / R on a sphere (ParametricMap.cpp:74-79)
+                ops.minv[k * N + e] = m.spherical ? inv[k] / kEarthRadius : inv[k];
+                if (m.spherical)
+                    ops.minvP[k * N + e] = inv[k];
+            }
+            for (int q = 0; q < QQ; ++q) // CG2DG weights (Interpolations.cpp:100-110)
+                ops.jwA[q * N + e] = m.spherical ? g.J[q] * b.weight(Q, q) * g.cl[q] : g.J[q] * b.weight(Q, q);
             geometry(m, e, 3, g3);
-            for (int q = 0; q < 9; ++q)
-                ops.jw3[q * N + e] = g3.J[q] * b.weight(3, q);
+            for (int q = 0; q < 9; ++q) // MeanValue / DG8 CG2DG weights (Tools.hpp:28-36)
+                ops.jw3[q * N + e] = m.spherical ? g3.J[q] * b.weight(3, q) * g3.cl[q] : g3.J[q] * b.weight(3, q);
         }
     });
 }
@@ -412,10 +459,22 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
     ops.d2.assign(72 * N, 0.0);
     ops.dxssh.assign(16 * N, 0.0);
     ops.dyssh.assign(16 * N, 0.0);
+    const bool sph = m.spherical;
+    if (sph) {
+        ops.gm.assign(81 * N, 0.0);
+        ops.a3.assign(81 * N, 0.0);
+        ops.dm.assign(72 * N, 0.0);
+    } else {
+        ops.gm.clear();
+        ops.a3.clear();
+        ops.dm.clear();
+    }
     if (stressTransport) {
         ops.cellX8.assign(72 * N, 0.0);
         ops.cellY8.assign(72 * N, 0.0);
         ops.minv8.assign(64 * N, 0.0);
+        if (sph)
+            ops.minv8P.assign(64 * N, 0.0);
         ops.wdam.assign(size_t(dg) * 9 * N, 0.0);
         ops.hsize.assign(N, 0.0);
     }
@@ -440,14 +499,25 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
                     dy1[j][q] = b.phiy(1, j, 3, q) * xi0 - b.phix(1, j, 3, q) * et0;
                 }
             }
-            // divS1/divS2 (9 x 8): (grad phi_j, psi_k)
-            double D1[9][8], D2[9][8];
+            // divS1/divS2 (9 x 8): (grad phi_j, psi_k).  On a sphere
+            // (ParametricMap.cpp:298-347) the lat-derivative carries cos(lat),
+            // divM = (phi_j, J sin(lat) w psi_k) is added and all is / R.
+            double D1[9][8], D2[9][8], DM[9][8];
             for (int j = 0; j < 9; ++j)
                 for (int k = 0; k < 8; ++k) {
                     double s1 = 0, s2 = 0;
                     for (int q = 0; q < 9; ++q) {
                         s1 += dx2[j][q] * b.psi(k, 3, q);
-                        s2 += dy2[j][q] * b.psi(k, 3, q);
+                        s2 += (sph ? dy2[j][q] * g.cl[q] : dy2[j][q]) * b.psi(k, 3, q);
+                    }
+                    if (sph) {
+                        s1 /= kEarthRadius;
+                        s2 /= kEarthRadius;
+                        double s3 = 0;
+                        for (int q = 0; q < 9; ++q)
+                            s3 += (b.phi(2, j, 3, q) * (g.J[q] * g.sl[q] * b.weight(3, q))) * b.psi(k, 3, q);
+                        DM[j][k] = s3 / kEarthRadius;
+                        ops.dm[(j * 8 + k) * N + e] = DM[j][k];
                     }
                     D1[j][k] = s1;
                     D2[j][k] = s2;
@@ -460,35 +530,42 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
                     double s1 = 0, s2 = 0;
                     for (int q = 0; q < 9; ++q) {
                         s1 += dx1[i][q] * b.phi(1, j, 3, q);
-                        s2 += dy1[i][q] * b.phi(1, j, 3, q);
+                        s2 += (sph ? dy1[i][q] * g.cl[q] : dy1[i][q]) * b.phi(1, j, 3, q);
                     }
-                    ops.dxssh[(i * 4 + j) * N + e] = s1;
-                    ops.dyssh[(i * 4 + j) * N + e] = s2;
+                    ops.dxssh[(i * 4 + j) * N + e] = sph ? s1 / kEarthRadius : s1;
+                    ops.dyssh[(i * 4 + j) * N + e] = sph ? s2 / kEarthRadius : s2;
                 }
             inverseMass(g, 8, im8);
             // iMgrad = M8^{-1} divS^T (8 x 9); the strain at the Gauss points
             // is psi(q)^T iMgrad u, so the device stores the composite
             // G(q, j) = sum_k psi_k(q) iMgrad(k, j) (9 x 9).
-            double iGx[8][9], iGy[8][9];
+            double iGx[8][9], iGy[8][9], iGm[8][9];
             for (int k = 0; k < 8; ++k)
                 for (int j = 0; j < 9; ++j) {
-                    double s1 = 0, s2 = 0;
+                    double s1 = 0, s2 = 0, s3 = 0;
                     for (int mm = 0; mm < 8; ++mm) {
                         s1 += im8[k * 8 + mm] * D1[j][mm];
                         s2 += im8[k * 8 + mm] * D2[j][mm];
+                        if (sph)
+                            s3 += im8[k * 8 + mm] * DM[j][mm];
                     }
                     iGx[k][j] = s1;
                     iGy[k][j] = s2;
+                    iGm[k][j] = s3; // iMM = M8^{-1} divM^T (spherical strain term)
                 }
             for (int q = 0; q < 9; ++q)
                 for (int j = 0; j < 9; ++j) {
-                    double s1 = 0, s2 = 0;
+                    double s1 = 0, s2 = 0, s3 = 0;
                     for (int k = 0; k < 8; ++k) {
                         s1 += b.psi(k, 3, q) * iGx[k][j];
                         s2 += b.psi(k, 3, q) * iGy[k][j];
+                        if (sph)
+                            s3 += b.psi(k, 3, q) * iGm[k][j];
                     }
                     ops.gx[(q * 9 + j) * N + e] = s1;
                     ops.gy[(q * 9 + j) * N + e] = s2;
+                    if (sph)
+                        ops.gm[(q * 9 + j) * N + e] = s3;
                 }
             // iMJwPSI = M8^{-1} (psi_k(q) w_q J_q)   (8 x 9)
             double W[8][9];
@@ -503,18 +580,25 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
             // divergence of a Gauss-point stress increment: A = divS iMJwPSI (9 x 9)
             for (int j = 0; j < 9; ++j)
                 for (int q = 0; q < 9; ++q) {
-                    double s1 = 0, s2 = 0;
+                    double s1 = 0, s2 = 0, s3 = 0;
                     for (int k = 0; k < 8; ++k) {
                         s1 += D1[j][k] * W[k][q];
                         s2 += D2[j][k] * W[k][q];
+                        if (sph)
+                            s3 += DM[j][k] * W[k][q];
                     }
                     ops.a1[(j * 9 + q) * N + e] = s1;
                     ops.a2[(j * 9 + q) * N + e] = s2;
+                    if (sph)
+                        ops.a3[(j * 9 + q) * N + e] = s3;
                 }
             if (stressTransport) {
                 cellTerms(g, 8, N, e, ops.cellX8, ops.cellY8);
-                for (int k = 0; k < 64; ++k)
-                    ops.minv8[k * N + e] = im8[k];
+                for (int k = 0; k < 64; ++k) { // the DG8 stress transport's M^{-1} (/ R on a sphere)
+                    ops.minv8[k * N + e] = sph ? im8[k] / kEarthRadius : im8[k];
+                    if (sph)
+                        ops.minv8P[k * N + e] = im8[k];
+                }
                 // iMJwPSI_dam = M_dg^{-1} (psi_k(q) w_q J_q) at the 3x3 rule
                 Geom ga;
                 geometry(m, e, gaussPoints1d(dg), ga);
@@ -546,7 +630,7 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
                 for (int j = 0; j < 9; ++j) {
                     double s = 0;
                     for (int q = 0; q < 16; ++q)
-                        s += b.phi(2, j, 4, q) * (g4.J[q] * b.weight(4, q));
+                        s += b.phi(2, j, 4, q) * (sph ? g4.J[q] * b.weight(4, q) * g4.cl[q] : g4.J[q] * b.weight(4, q));
                     ops.lumped2[n0 + (j % 3) + (j / 3) * s2] += s;
                 }
             }
@@ -559,7 +643,7 @@ void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps
                 for (int j = 0; j < 4; ++j) {
                     double s = 0;
                     for (int q = 0; q < 4; ++q)
-                        s += b.phi(1, j, 2, q) * (g2.J[q] * b.weight(2, q));
+                        s += b.phi(1, j, 2, q) * (sph ? g2.J[q] * b.weight(2, q) * g2.cl[q] : g2.J[q] * b.weight(2, q));
                     ops.lumped1[n0 + (j % 2) + (j / 2) * s1] += s;
                 }
             }

@@ -65,7 +65,10 @@ struct ConstTables32 {
 };
 
 // The structured quad mesh with arbitrary vertex positions (ParametricMesh).
+constexpr double kEarthRadius = 6371000.0; // NextsimDynamics.hpp:34
+
 struct HostMesh {
+    bool spherical = false;                   // x = lon, y = lat (radians); else Cartesian
     size_t nx = 0, ny = 0;
     std::vector<double> vx, vy;               // (nx+1)*(ny+1) vertices
     std::vector<uint8_t> ice;                 // nx*ny, 1 = ice
@@ -74,8 +77,9 @@ struct HostMesh {
     size_t nelements() const { return nx * ny; }
     // ParametricMesh::dirichletFromMask / dirichletFromEdge (ParametricMesh.cpp:228-272)
     void dirichletFromMaskAndEdges();
-    void elementCoords(size_t e, double c[4][2]) const;
+    void elementCoords(size_t e, double c[4][2]) const; // longitudes made continuous (spherical)
     double area(size_t e) const; // ParametricMesh.hpp:276-295
+    void rotatePoleToGreenland(); // ParametricMesh.hpp:137-157
 };
 
 // Element operators in SoA layout (entry-major: [entry][N]).
@@ -87,6 +91,9 @@ struct ElementOps {
     std::vector<double> jwA;                     // Qa^2   J*w at the advection Gauss points
     std::vector<double> cellX8, cellY8, minv8;   // 8*9, 8*9, 64 (BBM stress transport)
     std::vector<double> jw3;                     // 9      J*w at the 3x3 Gauss points
+    // spherical meshes: the transport's M^{-1} carries 1 / R, the CG2DG
+    // projection's does not (Interpolations.cpp:100-110)
+    std::vector<double> minvP, minv8P;           // dg*dg, 64 (empty on Cartesian meshes)
     // momentum (CG2 / DG-stress 8)
     std::vector<double> gx, gy;                  // 81: strain at Gauss points from CG2 nodes
     std::vector<double> w;                       // 72: iMJwPSI[k][q]
@@ -95,6 +102,10 @@ struct ElementOps {
     std::vector<double> wdam;                    // dg*9: iMJwPSI_dam (BBM)
     std::vector<double> dxssh, dyssh;            // 16: dX_SSH[i][j], dY_SSH[i][j]
     std::vector<double> hsize;                   // 1: sqrt(area)  (BBM)
+    // spherical metric terms (empty on Cartesian meshes)
+    std::vector<double> gm;                      // 81: the iMM strain term at Gauss points [q][j]
+    std::vector<double> a3;                      // 81: divM iMJwPSI [j][q]
+    std::vector<double> dm;                      // 72: divM[j][k] (BBM)
     // node arrays
     std::vector<double> lumped2;                 // (2nx+1)(2ny+1)
     std::vector<double> lumped1;                 // (nx+1)(ny+1)

@@ -109,6 +109,19 @@ __global__ void __launch_bounds__(kBlock) kCG2DG(int nx, size_t N, const double*
 // left cell (right trace) then right cell (left trace).  Land cells are
 // skipped; Dirichlet edges are doubled.
 // ===========================================================================
+// Longitude difference of an edge vector on a spherical mesh, with the jump
+// at +-Pi removed (ParametricMesh.hpp:381-397).
+__device__ __forceinline__ double wrapLon(const DevMesh& m, double d)
+{
+    if (m.spherical) {
+        if (d > 0.5 * M_PI)
+            d -= 2.0 * M_PI;
+        if (d < -0.5 * M_PI)
+            d += 2.0 * M_PI;
+    }
+    return d;
+}
+
 template <int DG>
 __global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const double* __restrict__ velx,
     const double* __restrict__ vely, double* __restrict__ nvX, double* __restrict__ nvY)
@@ -121,7 +134,7 @@ __global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const doubl
     if (t < m.nXe) {
         const size_t ix = t % nx, iy = t / nx;
         const size_t n0 = iy * sv + ix;
-        const double t0 = m.vx[n0 + 1] - m.vx[n0], t1 = m.vy[n0 + 1] - m.vy[n0];
+        const double t0 = wrapLon(m, m.vx[n0 + 1] - m.vx[n0]), t1 = m.vy[n0 + 1] - m.vy[n0];
         double acc[ED];
 #pragma unroll
         for (int k = 0; k < ED; ++k)
@@ -171,7 +184,7 @@ __global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const doubl
         return;
     const size_t ix = u % sv, iy = u / sv;
     const size_t n0 = iy * sv + ix;
-    const double t0 = m.vx[n0 + sv] - m.vx[n0], t1 = m.vy[n0 + sv] - m.vy[n0];
+    const double t0 = wrapLon(m, m.vx[n0 + sv] - m.vx[n0]), t1 = m.vy[n0 + sv] - m.vy[n0];
     double acc[ED];
 #pragma unroll
     for (int k = 0; k < ED; ++k)
@@ -894,6 +907,10 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const doub
 constexpr int kStressElems = 64;
 constexpr int kStressParts = 3;
 
+// SPH: spherical metric terms (CGDynamicsKernel.cpp:331-334, 348-351): the
+// strain gains e11 -= iMM v, e12 += iMM u / 2 (through the composite G_m),
+// the divergence gains +divM s12 (x) and -divM s11 (y) (through A_3).
+template <bool SPH>
 __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMesh m, DevOps o,
     const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ Pg,
     double* __restrict__ tdiv, MevpParams p)
@@ -929,6 +946,17 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMe
                 exv = fma(gxq, vl[j], exv);
                 eyu = fma(gyq, ul[j], eyu);
             }
+            if constexpr (SPH) {
+                double mu = 0.0, mv = 0.0;
+#pragma unroll
+                for (int j = 0; j < 9; ++j) {
+                    const double gmq = o.gm[(q * 9 + j) * N + e];
+                    mu = fma(gmq, ul[j], mu);
+                    mv = fma(gmq, vl[j], mv);
+                }
+                ex -= mv;
+                eyu += mu;
+            }
             // e11 = ex, e22 = ey, e12 = (exv + eyu) / 2
             const double sxy = exv + eyu;
             const double d2 = dmin2 + 1.25 * (ex * ex + ey * ey) + 1.50 * ex * ey + 0.25 * sxy * sxy;
@@ -955,6 +983,11 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMe
             const double f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
             ax = fma(a1, f11, fma(a2, f12, ax));
             ay = fma(a1, f12, fma(a2, f22, ay));
+            if constexpr (SPH) {
+                const double a3 = o.a3[(j * 9 + q) * N + e];
+                ax = fma(a3, f12, ax);
+                ay = fma(-a3, f11, ay);
+            }
         }
         tdiv[j * N + e] = fma(tdiv[j * N + e], keep, ax);
         tdiv[(9 + j) * N + e] = fma(tdiv[(9 + j) * N + e], keep, ay);
@@ -1087,6 +1120,17 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
                 exv = fmaf(gxq, vl[j], exv);
                 eyu = fmaf(gyq, ul[j], eyu);
             }
+            if (o.gm) { // spherical metric term
+                float mu = 0.f, mv = 0.f;
+#pragma unroll
+                for (int j = 0; j < 9; ++j) {
+                    const float gmq = o.gm[(q * 9 + j) * o.ld + e];
+                    mu = fmaf(gmq, ul[j], mu);
+                    mv = fmaf(gmq, vl[j], mv);
+                }
+                ex -= mv;
+                eyu += mu;
+            }
             const float sxy = exv + eyu;
             const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
             const float z8 = static_cast<float>(Pg[q * N + e] * rsqrt(static_cast<double>(inv) + dmin2));
@@ -1111,6 +1155,11 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
             const float f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
             ax = fmaf(a1, f11, fmaf(a2, f12, ax));
             ay = fmaf(a1, f12, fmaf(a2, f22, ay));
+            if (o.a3) {
+                const float a3 = o.a3[(j * 9 + q) * o.ld + e];
+                ax = fmaf(a3, f12, ax);
+                ay = fmaf(-a3, f11, ay);
+            }
         }
         tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
         tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
@@ -1148,8 +1197,10 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(Dev
 // polls sets DEV_ERR_TIMEOUT and the block returns after a second bounded
 // wait for the copy it issued.
 namespace {
-constexpr int kTmaRows = 162;
-constexpr unsigned kTmaTileBytes = kTmaRows * kTmaElems * 4;
+constexpr int kTmaRows = 162;                           // G_x | G_y  (A_1 | A_2)
+constexpr int kTmaRowsSph = 243;                        // G_x | G_y | G_m  (A_1 | A_2 | A_3)
+template <bool SPH> __host__ __device__ constexpr int tmaRows() { return SPH ? kTmaRowsSph : kTmaRows; }
+template <bool SPH> __host__ __device__ constexpr unsigned tmaTileBytes() { return tmaRows<SPH>() * kTmaElems * 4; }
 constexpr long kTmaSpin = 1L << 26;
 
 __device__ __forceinline__ unsigned smemAddr(const void* p)
@@ -1194,13 +1245,14 @@ __device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int
 
 // One block of the TMA-staged stress kernel: elements x0 .. x0+31 of a grid
 // (shared by the single-grid and the batched ensemble kernels).
+template <bool SPH>
 __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const CUtensorMap* mapA, int nx, size_t N,
     const uint8_t* __restrict__ ice, const float* __restrict__ u, const float* __restrict__ v,
     const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, const MevpParams& p,
     int* __restrict__ err, int x0, unsigned char* smem)
 {
     float* sT = reinterpret_cast<float*>(smem);                      // [162][32]: G_x|G_y, then A_1|A_2
-    float (*fs)[9][kTmaElems] = reinterpret_cast<float (*)[9][kTmaElems]>(sT + kTmaRows * kTmaElems);
+    float (*fs)[9][kTmaElems] = reinterpret_cast<float (*)[9][kTmaElems]>(sT + tmaRows<SPH>() * kTmaElems);
     uint64_t* bars = reinterpret_cast<uint64_t*>(fs[3]);             // 2 mbarriers, one per copy
     const int le = threadIdx.x % kTmaElems;
     const int part = threadIdx.x / kTmaElems;
@@ -1208,7 +1260,7 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
         mbarInit(&bars[0], 1);
         mbarInit(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        mbarExpectTx(&bars[0], kTmaTileBytes);
+        mbarExpectTx(&bars[0], tmaTileBytes<SPH>());
         tmaLoad2d(sT, mapG, x0, 0, &bars[0]);
     }
     const size_t e = size_t(x0) + le;
@@ -1256,6 +1308,17 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
                 exv = fmaf(gxq, vl[j], exv);
                 eyu = fmaf(gyq, ul[j], eyu);
             }
+            if constexpr (SPH) {
+                float mu = 0.f, mv = 0.f;
+#pragma unroll
+                for (int j = 0; j < 9; ++j) {
+                    const float gmq = sT[(162 + q * 9 + j) * kTmaElems + le];
+                    mu = fmaf(gmq, ul[j], mu);
+                    mv = fmaf(gmq, vl[j], mv);
+                }
+                ex -= mv;
+                eyu += mu;
+            }
             const float sxy = exv + eyu;
             const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
             const float z8 = static_cast<float>(Pa[qq] * rsqrt(static_cast<double>(inv) + dmin2));
@@ -1276,7 +1339,7 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
     }
     if (threadIdx.x == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbarExpectTx(&bars[1], kTmaTileBytes);
+        mbarExpectTx(&bars[1], tmaTileBytes<SPH>());
         tmaLoad2d(sT, mapA, x0, 0, &bars[1]);
     }
     ok = mbarWaitBounded(&bars[1], 0);
@@ -1302,19 +1365,25 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
             const float f11 = fs[0][q][le], f12 = fs[1][q][le], f22 = fs[2][q][le];
             ax = fmaf(a1, f11, fmaf(a2, f12, ax));
             ay = fmaf(a1, f12, fmaf(a2, f22, ay));
+            if constexpr (SPH) {
+                const float a3 = sT[(162 + j * 9 + q) * kTmaElems + le];
+                ax = fmaf(a3, f12, ax);
+                ay = fmaf(-a3, f11, ay);
+            }
         }
         tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
         tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
     }
 }
 
+template <bool SPH>
 __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(const __grid_constant__ CUtensorMap mapG,
     const __grid_constant__ CUtensorMap mapA, DevMesh m, const float* __restrict__ u, const float* __restrict__ v,
     const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p,
     int* __restrict__ err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    stress32TmaBlock(&mapG, &mapA, m.nx, m.N, m.ice, u, v, Pg, hPg, tdiv, p, err, blockIdx.x * kTmaElems, smem);
+    stress32TmaBlock<SPH>(&mapG, &mapA, m.nx, m.N, m.ice, u, v, Pg, hPg, tdiv, p, err, blockIdx.x * kTmaElems, smem);
 }
 
 // Body of the mixed-precision node kernel for CG2 node i.
@@ -1415,7 +1484,8 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32TmaBatc
     extern __shared__ __align__(128) unsigned char smem[];
     const EnsembleMember& M = members[blockMember[blockIdx.x]];
     const int x0 = (static_cast<int>(blockIdx.x) - M.tmaBlock0) * kTmaElems;
-    stress32TmaBlock(&M.maps.g, &M.maps.a, M.nx, M.N, M.ice, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, err, x0, smem);
+    stress32TmaBlock<false>(&M.maps.g, &M.maps.a, M.nx, M.N, M.ice, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, err, x0,
+        smem);
 }
 
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
@@ -1461,6 +1531,8 @@ template <typename T> struct BbmOps {
     const T* d1;
     const T* d2;
     const double* hsize;
+    const T* gm; // spherical metric terms (null on Cartesian meshes)
+    const T* dm;
 };
 
 // BBM stress, damage and divergence for one element.  T = double is the
@@ -1534,6 +1606,17 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
             ey = fma(gyq, vl[j], ey);
             exv = fma(gxq, vl[j], exv);
             eyu = fma(gyq, ul[j], eyu);
+        }
+        if (o.gm) { // spherical: e11 -= iMM v, e12 += iMM u / 2 (CGDynamicsKernel.cpp:331-334)
+            T mu = T(0), mv = T(0);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const T gmq = o.gm[(q * 9 + j) * N + e];
+                mu = fma(gmq, ul[j], mu);
+                mv = fma(gmq, vl[j], mv);
+            }
+            ex -= mv;
+            eyu += mu;
         }
         const T e11 = ex, e22 = ey, e12 = T(0.5) * (exv + eyu);
         T g11 = T(0), g12 = T(0), g22 = T(0);
@@ -1621,6 +1704,11 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
                 const T d2v = o.d2[(j * 8 + k) * N + e];
                 tx = fma(d1, n11[k], fma(d2v, n12[k], tx));
                 ty = fma(d1, n12[k], fma(d2v, n22[k], ty));
+                if (o.dm) { // spherical: +divM s12, -divM s11 (CGDynamicsKernel.cpp:348-351)
+                    const T dmv = o.dm[(j * 8 + k) * N + e];
+                    tx = fma(dmv, n12[k], tx);
+                    ty = fma(-dmv, n11[k], ty);
+                }
             }
         }
         contrib[j * N + e] = tx;
@@ -1879,7 +1967,10 @@ cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, con
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
     const double* v, const double* Pg, double* tdiv, const MevpParams& p)
 {
-    kMevpStress<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
+    if (o.gm)
+        kMevpStress<true><<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
+    else
+        kMevpStress<false><<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
     return cudaGetLastError();
 }
 
@@ -1897,7 +1988,8 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
     return cudaGetLastError();
 }
 namespace {
-constexpr size_t kTmaSmem = size_t(kTmaTileBytes) + 3 * 9 * kTmaElems * 4 + 2 * 8;
+template <bool SPH> constexpr size_t tmaSmem() { return size_t(tmaTileBytes<SPH>()) + 3 * 9 * kTmaElems * 4 + 2 * 8; }
+constexpr size_t kTmaSmem = tmaSmem<false>();
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
     CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1916,9 +2008,9 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
     }
     // the four operator blocks are rows of one [324][ld] array; ld * 4 bytes
     // is a multiple of 128 and the base is 256-byte aligned
-    const cuuint64_t dims[2] = { o.ld, kTmaRows };
+    const cuuint64_t dims[2] = { o.ld, static_cast<cuuint64_t>(o.rowsG) };
     const cuuint64_t strides[1] = { o.ld * sizeof(float) };
-    const cuuint32_t box[2] = { kTmaElems, kTmaRows };
+    const cuuint32_t box[2] = { kTmaElems, static_cast<cuuint32_t>(o.rowsG) };
     const cuuint32_t estr[2] = { 1, 1 };
     const float* rows[2] = { o.gx, o.a1 };
     CUtensorMap* maps[2] = { &out->g, &out->a };
@@ -1931,8 +2023,11 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
     }
     // dynamic shared memory of the kernel (24 KB: one operator tile, the
     // stress terms, two mbarriers), set once
-    const cudaError_t e = cudaFuncSetAttribute(kMevpStress32Tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        static_cast<int>(kTmaSmem));
+    cudaError_t e = cudaFuncSetAttribute(kMevpStress32Tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        static_cast<int>(tmaSmem<false>()));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kMevpStress32Tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            static_cast<int>(tmaSmem<true>()));
     return e != cudaSuccess ? e
                             : cudaFuncSetAttribute(kMevpStress32TmaBatched,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmem));
@@ -1944,14 +2039,16 @@ cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const Stress
     cudaLaunchConfig_t cfg {};
     cfg.gridDim = dim3(blocksFor(m.N, kTmaElems));
     cfg.blockDim = dim3(kTmaElems * kStressParts);
-    cfg.dynamicSmemBytes = kTmaSmem;
+    cfg.dynamicSmemBytes = m.spherical ? tmaSmem<true>() : tmaSmem<false>();
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kMevpStress32Tma, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
+    if (m.spherical)
+        return cudaLaunchKernelEx(&cfg, kMevpStress32Tma<true>, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
+    return cudaLaunchKernelEx(&cfg, kMevpStress32Tma<false>, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
 }
 
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
@@ -2037,7 +2134,7 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
 {
     const unsigned g = blocksFor(m.N);
     if (o32) {
-        const BbmOps<float> of { o32->gx, o32->gy, o32->w, o32->wdam, o32->d1, o32->d2, o.hsize };
+        const BbmOps<float> of { o32->gx, o32->gy, o32->w, o32->wdam, o32->d1, o32->d2, o.hsize, o32->gm, o32->dm };
         switch (dg) {
         case 1: kBbmStress<1, float><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
         case 3: kBbmStress<3, float><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
@@ -2046,7 +2143,7 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
         }
         return cudaGetLastError();
     }
-    const BbmOps<double> od { o.gx, o.gy, o.w, o.wdam, o.d1, o.d2, o.hsize };
+    const BbmOps<double> od { o.gx, o.gy, o.w, o.wdam, o.d1, o.d2, o.hsize, o.gm, o.dm };
     switch (dg) {
     case 1: kBbmStress<1, double><<<g, kBlock, 0, s>>>(m, od, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
     case 3: kBbmStress<3, double><<<g, kBlock, 0, s>>>(m, od, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;

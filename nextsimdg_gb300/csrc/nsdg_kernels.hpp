@@ -17,6 +17,7 @@ namespace nsdg {
 // Device copy of the mesh connectivity and boundary flags.
 struct DevMesh {
     int nx = 0, ny = 0;
+    int spherical = 0; // x = lon, y = lat (radians): edge tangents wrap in longitude
     size_t N = 0;      // elements
     size_t Ncg = 0;    // CG2 nodes (2nx+1)(2ny+1)
     size_t Ncg1 = 0;   // CG1 nodes (nx+1)(ny+1)
@@ -56,6 +57,12 @@ struct DevOps {
     const double* hsize = nullptr;
     const double* invm2 = nullptr;   // 1 / lumped CG2 mass
     const double* lumped1 = nullptr; // lumped CG1 mass
+    // spherical metric terms (null on Cartesian meshes)
+    const double* gm = nullptr;      // strain term iMM at the Gauss points [q][j]
+    const double* minvP = nullptr;   // CG2DG inverse mass (the transport's minv carries 1 / R)
+    const double* minv8P = nullptr;
+    const double* a3 = nullptr;      // divM iMJwPSI [j][q]
+    const double* dm = nullptr;      // divM [j][k] (BBM)
 };
 
 // Status bits written by kernels into the handle's device error word.
@@ -154,14 +161,18 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 // FP32 operators, velocities, divergence coefficients and momentum
 // arithmetic; FP64 for Delta = sqrt(strain invariant + DeltaMin^2), the
 // viscosity P/(2 Delta), and the lumped-mass inverse.
-// FP32 element operators, one [324][ld] block: rows 0..80 G_x, 81..161 G_y,
-// 162..242 A_1, 243..323 A_2; ld = N rounded up to kTmaElems (padding zero).
+// FP32 element operators, one [rows][ld] block: G_x, G_y (and G_m on a
+// sphere), then A_1, A_2 (and A_3), 81 rows each; ld = N rounded up to
+// kTmaElems (padding zero).
 struct DevOps32 {
     const float* gx = nullptr;
     const float* gy = nullptr;
     const float* a1 = nullptr;
     const float* a2 = nullptr;
+    const float* gm = nullptr; // spherical only
+    const float* a3 = nullptr; // spherical only
     size_t ld = 0;
+    int rowsG = 162;           // rows of the strain (and of the divergence) part: 162, or 243 on a sphere
 };
 constexpr int kTmaElems = 32;   // elements per block of the TMA-staged stress kernel
 inline size_t ops32Ld(size_t N) { return (N + kTmaElems - 1) / kTmaElems * kTmaElems; }
@@ -212,7 +223,7 @@ struct EnsembleMember {
     float* tdiv;
     int tileW, tileH, tilesX;
     int stressBlock0, nodeBlock0;
-    int tmaBlock0;   // first block of this member in the TMA-staged batched launch
+    int tmaBlock0;   // first block of this member in the TMA-staged batched launch (Cartesian members)
     StressMaps maps; // the member's tensor maps (64-byte aligned inside the device table)
 };
 // One launch each for the element and the node phase of every member.
@@ -267,6 +278,8 @@ struct BbmOps32 {
     const float* wdam;
     const float* d1;
     const float* d2;
+    const float* gm; // spherical only
+    const float* dm; // spherical only
 };
 cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg, const double* u,
     const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,

@@ -239,13 +239,31 @@ static bool invert(int n, const double* A, double* inv)
 /* ------------------------------------------------------------------------ */
 /* ParametricMesh (dynamics/src/include/ParametricMesh.hpp:42-442)          */
 /* ------------------------------------------------------------------------ */
+// NextsimDynamics.hpp:34
+static constexpr double kEarthRadius = 6371000.0;
+
 struct Mesh {
+    bool spherical = false; // COORDINATES: SPHERICAL (x = lon, y = lat, radians) or CARTESIAN
     size_t nx = 0, ny = 0, nnodes = 0, nelements = 0;
     std::vector<double> vx, vy; // vertices
     std::vector<char> landmask; // 1 = ice
     std::array<std::vector<size_t>, 4> dirichlet;
     std::vector<std::vector<std::array<size_t, 4>>> periodic;
 
+    // ParametricMesh.hpp:196-209: no longitude jump (Pi -> -Pi) inside one element
+    static void correctLongitude(double c[][2], int n)
+    {
+        bool problem = false;
+        for (int i = 1; i < n; ++i)
+            if (std::fabs(c[0][0] - c[i][0]) > 2.0 / 3.0 * M_PI) {
+                problem = true;
+                break;
+            }
+        if (problem)
+            for (int i = 0; i < n; ++i)
+                if (c[i][0] < 0)
+                    c[i][0] += 2.0 * M_PI;
+    }
     // ParametricMesh.hpp:218-232
     void coordinatesOfElement(size_t eid, double c[4][2]) const
     {
@@ -254,6 +272,27 @@ struct Mesh {
         for (int k = 0; k < 4; ++k) {
             c[k][0] = vx[ids[k]];
             c[k][1] = vy[ids[k]];
+        }
+        if (spherical)
+            correctLongitude(c, 4);
+    }
+    // ParametricMesh.hpp:137-157: the poles moved to Greenland / Antarctica
+    void rotatePoleToGreenland()
+    {
+        for (size_t i = 0; i < nnodes; ++i) {
+            const double x = std::cos(vy[i]) * std::cos(vx[i]);
+            const double y = std::cos(vy[i]) * std::sin(vx[i]);
+            const double z = std::sin(vy[i]);
+            const double aw = 40.0 * M_PI / 180.0;
+            const double x1 = std::cos(aw) * x - std::sin(aw) * y;
+            const double y1 = std::sin(aw) * x + std::cos(aw) * y;
+            const double z1 = z;
+            const double bw = 15.0 * M_PI / 180.0;
+            const double x2 = std::cos(bw) * x1 - std::sin(bw) * z1;
+            const double y2 = y1;
+            const double z2 = std::sin(bw) * x1 + std::cos(bw) * z1;
+            vy[i] = std::asin(z2);
+            vx[i] = std::atan2(y2, x2);
         }
     }
     // ParametricMesh.hpp:276-299
@@ -274,11 +313,17 @@ struct Mesh {
         return 0.25 * std::sqrt(4.0 * e * f - t * t);
     }
     double h(size_t eid) const { return std::sqrt(area(eid)); }
-    // ParametricMesh.hpp:381-397 (Cartesian)
+    // ParametricMesh.hpp:381-397
     void edgevector(size_t n1, size_t n2, double t[2]) const
     {
         t[0] = vx[n2] - vx[n1];
         t[1] = vy[n2] - vy[n1];
+        if (spherical) {
+            if (t[0] > 0.5 * M_PI)
+                t[0] -= 2.0 * M_PI;
+            if (t[0] < -0.5 * M_PI)
+                t[0] += 2.0 * M_PI;
+        }
     }
     void sortDirichlet(int edge) { std::sort(dirichlet[edge].begin(), dirichlet[edge].end()); }
     // ParametricMesh.cpp:228-252
@@ -352,17 +397,31 @@ static void gaussPointsInElement(const Mesh& m, size_t eid, int Q, double gp[2][
             gp[r][q] = s;
         }
 }
-// ParametricTools.hpp:109-153: M_ij = sum_q PSI_iq (w_q J_q) PSI_jq
+// cos / sin of the latitude at the Q x Q Gauss points of an element
+static void latTrig(const Mesh& m, size_t eid, int Q, double* cl, double* sl)
+{
+    double gp[2][16];
+    gaussPointsInElement(m, eid, Q, gp);
+    for (int q = 0; q < Q * Q; ++q) {
+        if (cl) cl[q] = std::cos(gp[1][q]);
+        if (sl) sl[q] = std::sin(gp[1][q]);
+    }
+}
+// ParametricTools.hpp:109-153: M_ij = sum_q PSI_iq (w_q J_q) PSI_jq;
+// SphericalTools::massMatrix (ParametricTools.hpp:189-202) adds cos(lat_q)
 static void massMatrix(const Mesh& m, size_t eid, int DG, double* M)
 {
     const int Q = gauss1d(DG);
-    double J[16];
+    double J[16], cl[16];
     jacobian(m, eid, Q, J);
+    if (m.spherical)
+        latTrig(m, eid, Q, cl, nullptr);
     for (int i = 0; i < DG; ++i)
         for (int j = 0; j < DG; ++j) {
             double s = 0;
             for (int q = 0; q < Q * Q; ++q)
-                s += (PSI(i, Q, q) * (GW(Q, q) * J[q])) * PSI(j, Q, q);
+                s += m.spherical ? (PSI(i, Q, q) * (GW(Q, q) * J[q] * cl[q])) * PSI(j, Q, q)
+                                 : (PSI(i, Q, q) * (GW(Q, q) * J[q])) * PSI(j, Q, q);
             M[i * DG + j] = s;
         }
 }
@@ -464,6 +523,9 @@ struct Transport {
                     cellY[(e * dg + i) * QQ + q] = PSIy(i, Q, q) * dxT[0][q] - PSIx(i, Q, q) * dyT[0][q];
                 }
             inverseMass(m, e, dg, &minv[e * dg * dg]);
+            if (m.spherical) // ParametricMap.cpp:74-79
+                for (int k = 0; k < dg * dg; ++k)
+                    minv[e * dg * dg + k] /= kEarthRadius;
         }
     }
 
@@ -815,7 +877,9 @@ static void Function2DG(const Mesh& m, DG& phi, Function f, const double* fp)
         inverseMass(m, e, dg, Minv);
         for (int i = 0; i < dg; ++i) {
             double s = 0;
-            for (int q = 0; q < QQ; ++q) s += (PSI(i, Q, q) * (J[q] * GW(Q, q))) * fg[q];
+            for (int q = 0; q < QQ; ++q)
+                s += m.spherical ? (PSI(i, Q, q) * (J[q] * GW(Q, q) * std::cos(gp[1][q]))) * fg[q]
+                                 : (PSI(i, Q, q) * (J[q] * GW(Q, q))) * fg[q];
             r[i] = s;
         }
         for (int i = 0; i < dg; ++i) {
@@ -840,7 +904,7 @@ static double L2ErrorFunctionDG(const Mesh& m, const DG& src, Function f, const 
             double v = 0;
             for (int j = 0; j < dg; ++j) v += src.row(e)[j] * PSI(j, Q, q);
             const double d = v - f(gp[0][q], gp[1][q], fp);
-            s += J[q] * GW(Q, q) * (d * d);
+            s += m.spherical ? std::cos(gp[1][q]) * J[q] * GW(Q, q) * (d * d) : J[q] * GW(Q, q) * (d * d);
         }
         err += s;
     }
@@ -851,13 +915,15 @@ static double MeanValue(const Mesh& m, const DG& phi)
 {
     double mass = 0;
     for (size_t e = 0; e < m.nelements; ++e) {
-        double J[16];
+        double J[16], cl[16];
         jacobian(m, e, 3, J);
+        if (m.spherical)
+            latTrig(m, e, 3, cl, nullptr);
         double s = 0;
         for (int q = 0; q < 9; ++q) {
             double v = 0;
             for (int j = 0; j < phi.n; ++j) v += phi.row(e)[j] * PSI(j, 3, q);
-            s += v * (J[q] * GW(3, q));
+            s += m.spherical ? v * cl[q] * (J[q] * GW(3, q)) : v * (J[q] * GW(3, q));
         }
         mass += s;
     }
@@ -877,9 +943,12 @@ struct CG2DGOp {
         jw.assign(m.nelements * QQ, 0.0);
 #pragma omp parallel for schedule(static)
         for (long e = 0; e < static_cast<long>(m.nelements); ++e) {
-            double J[16];
+            double J[16], cl[16];
             jacobian(m, e, Q, J);
-            for (int q = 0; q < QQ; ++q) jw[e * QQ + q] = J[q] * GW(Q, q);
+            if (m.spherical)
+                latTrig(m, e, Q, cl, nullptr);
+            for (int q = 0; q < QQ; ++q)
+                jw[e * QQ + q] = m.spherical ? J[q] * GW(Q, q) * cl[q] : J[q] * GW(Q, q);
             inverseMass(m, e, dg, &minv[e * dg * dg]);
         }
     }
@@ -993,6 +1062,7 @@ struct MomentumMap {
     std::vector<double> iMJwPSI;          // N x 8 x 9
     std::vector<double> iMJwPSI_dam;      // N x dg x 9
     std::vector<double> dX_SSH, dY_SSH;   // N x 4 x 4
+    std::vector<double> divM, iMM;        // spherical metric terms: N x 9 x 8, N x 8 x 9
     int dg = 0;
 
     void init(const Mesh& m, int DGadv)
@@ -1005,9 +1075,13 @@ struct MomentumMap {
             for (size_t iy = p; iy < m.ny; iy += 2)
                 for (size_t ix = 0; ix < m.nx; ++ix) {
                     const size_t eid = m.nx * iy + ix;
-                    double J[16], Meid[9];
+                    double J[16], Meid[9], cl[16];
                     jacobian(m, eid, 4, J);
-                    for (int q = 0; q < 16; ++q) J[q] = J[q] * GW(4, q);
+                    if (m.spherical) {
+                        latTrig(m, eid, 4, cl, nullptr);
+                        for (int q = 0; q < 16; ++q) J[q] = J[q] * GW(4, q) * cl[q];
+                    } else
+                        for (int q = 0; q < 16; ++q) J[q] = J[q] * GW(4, q);
                     for (int j = 0; j < 9; ++j) {
                         double s = 0;
                         for (int q = 0; q < 16; ++q) s += PHI(2, j, 4, q) * J[q];
@@ -1021,9 +1095,13 @@ struct MomentumMap {
             for (size_t iy = p; iy < m.ny; iy += 2)
                 for (size_t ix = 0; ix < m.nx; ++ix) {
                     const size_t eid = m.nx * iy + ix;
-                    double J[16], Meid[4];
+                    double J[16], Meid[4], cl[16];
                     jacobian(m, eid, 2, J);
-                    for (int q = 0; q < 4; ++q) J[q] = J[q] * GW(2, q);
+                    if (m.spherical) {
+                        latTrig(m, eid, 2, cl, nullptr);
+                        for (int q = 0; q < 4; ++q) J[q] = J[q] * GW(2, q) * cl[q];
+                    } else
+                        for (int q = 0; q < 4; ++q) J[q] = J[q] * GW(2, q);
                     for (int j = 0; j < 4; ++j) {
                         double s = 0;
                         for (int q = 0; q < 4; ++q) s += PHI(1, j, 2, q) * J[q];
@@ -1044,6 +1122,10 @@ struct MomentumMap {
         iMJwPSI_dam.assign(N * dg * 9, 0.0);
         dX_SSH.assign(N * 16, 0.0);
         dY_SSH.assign(N * 16, 0.0);
+        if (m.spherical) {
+            divM.assign(N * 72, 0.0);
+            iMM.assign(N * 72, 0.0);
+        }
 #pragma omp parallel for schedule(static)
         for (long e = 0; e < static_cast<long>(N); ++e) {
             double Fx[2][16], Fy[2][16], J[16];
@@ -1067,39 +1149,57 @@ struct MomentumMap {
             jacobian(m, e, 3, J);
             double* d1 = &divS1[e * 72];
             double* d2 = &divS2[e * 72];
+            // spherical (ParametricMap.cpp:298-347): (x, y) = (lon, lat); the
+            // lat-derivative carries cos(lat), a divM term carries sin(lat),
+            // and everything is divided by the Earth radius
+            double cl[16], sl[16];
+            if (m.spherical)
+                latTrig(m, e, 3, cl, sl);
             for (int j = 0; j < 9; ++j)
                 for (int k = 0; k < 8; ++k) {
                     double a = 0, b = 0;
                     for (int q = 0; q < 9; ++q) {
                         a += dx2[j][q] * PSI(k, 3, q);
-                        b += dy2[j][q] * PSI(k, 3, q);
+                        b += (m.spherical ? dy2[j][q] * cl[q] : dy2[j][q]) * PSI(k, 3, q);
                     }
-                    d1[j * 8 + k] = a;
-                    d2[j * 8 + k] = b;
+                    d1[j * 8 + k] = m.spherical ? a / kEarthRadius : a;
+                    d2[j * 8 + k] = m.spherical ? b / kEarthRadius : b;
                 }
+            if (m.spherical)
+                for (int j = 0; j < 9; ++j)
+                    for (int k = 0; k < 8; ++k) {
+                        double a = 0;
+                        for (int q = 0; q < 9; ++q)
+                            a += (PHI(2, j, 3, q) * (J[q] * sl[q] * GW(3, q))) * PSI(k, 3, q);
+                        divM[e * 72 + j * 8 + k] = a / kEarthRadius;
+                    }
             for (int i = 0; i < 4; ++i)
                 for (int j = 0; j < 4; ++j) {
                     double a = 0, b = 0;
                     for (int q = 0; q < 9; ++q) {
                         a += dx1[i][q] * PHI(1, j, 3, q);
-                        b += dy1[i][q] * PHI(1, j, 3, q);
+                        b += (m.spherical ? dy1[i][q] * cl[q] : dy1[i][q]) * PHI(1, j, 3, q);
                     }
-                    dX_SSH[e * 16 + i * 4 + j] = a;
-                    dY_SSH[e * 16 + i * 4 + j] = b;
+                    dX_SSH[e * 16 + i * 4 + j] = m.spherical ? a / kEarthRadius : a;
+                    dY_SSH[e * 16 + i * 4 + j] = m.spherical ? b / kEarthRadius : b;
                 }
             double imass[64];
             inverseMass(m, e, 8, imass);
             for (int i = 0; i < 8; ++i)
                 for (int j = 0; j < 9; ++j) {
-                    double a = 0, b = 0, c = 0;
+                    double a = 0, b = 0, c = 0, d = 0;
                     for (int k = 0; k < 8; ++k) {
                         a += imass[i * 8 + k] * d1[j * 8 + k];
                         b += imass[i * 8 + k] * d2[j * 8 + k];
                         c += imass[i * 8 + k] * (PSI(k, 3, j) * (GW(3, j) * J[j]));
+                        if (m.spherical)
+                            d += imass[i * 8 + k] * divM[e * 72 + j * 8 + k];
                     }
                     iMgradX[e * 72 + i * 9 + j] = a;
                     iMgradY[e * 72 + i * 9 + j] = b;
                     iMJwPSI[e * 72 + i * 9 + j] = c;
+                    if (m.spherical)
+                        iMM[e * 72 + i * 9 + j] = d;
                 }
             double imd[64];
             inverseMass(m, e, dg, imd);
@@ -1140,10 +1240,12 @@ struct Kernel {
     size_t Ncg() const { return (2 * mesh.nx + 1) * (2 * mesh.ny + 1); }
 
     // DynamicsKernel.hpp:44-75, CGDynamicsKernel.cpp:24-51, BrittleCGDynamicsKernel.hpp:72-86
-    int initialise(size_t nx, size_t ny, const double* coords, const double* mask)
+    // DynamicsKernel.hpp:44-58
+    int initialise(size_t nx, size_t ny, const double* coords, const double* mask, bool spherical = false)
     {
         Mesh& m = mesh;
         m = Mesh();
+        m.spherical = spherical;
         m.nx = nx;
         m.ny = ny;
         m.nelements = nx * ny;
@@ -1154,6 +1256,8 @@ struct Kernel {
             m.vx[i] = coords[2 * i];
             m.vy[i] = coords[2 * i + 1];
         }
+        if (spherical)
+            m.rotatePoleToGreenland();
         m.landmask.resize(m.nelements);
         for (size_t i = 0; i < m.nelements; ++i) m.landmask[i] = (mask[i] == 1.) ? 1 : 0;
         m.dirichletFromMask();
@@ -1412,6 +1516,18 @@ struct Kernel {
                     e22.row(dgi)[i] = b;
                     e12.row(dgi)[i] = 0.5 * (c + d);
                 }
+                if (m.spherical) { // CGDynamicsKernel.cpp:331-334
+                    const double* MM = &pmap.iMM[dgi * 72];
+                    for (int i = 0; i < 8; ++i) {
+                        double mu = 0, mv = 0;
+                        for (int j = 0; j < 9; ++j) {
+                            mv += MM[i * 9 + j] * vl[j];
+                            mu += MM[i * 9 + j] * ul[j];
+                        }
+                        e11.row(dgi)[i] -= mv;
+                        e12.row(dgi)[i] += 0.5 * mu;
+                    }
+                }
             }
         }
     }
@@ -1597,9 +1713,20 @@ struct Kernel {
                             cc += D1[j * 8 + k] * s12.row(c)[k];
                             d += D2[j * 8 + k] * s22.row(c)[k];
                         }
+                        double tx = a + b, ty = cc + d;
+                        if (m.spherical) { // CGDynamicsKernel.cpp:348-351
+                            const double* DM = &pmap.divM[c * 72];
+                            double e1 = 0, e2 = 0;
+                            for (int k = 0; k < 8; ++k) {
+                                e1 += DM[j * 8 + k] * s12.row(c)[k];
+                                e2 += DM[j * 8 + k] * s11.row(c)[k];
+                            }
+                            tx += e1;
+                            ty -= e2;
+                        }
                         const size_t node = cg_i + (j % 3) + (j / 3) * cgRow;
-                        dSx[node] -= (a + b);
-                        dSy[node] -= (cc + d);
+                        dSx[node] -= tx;
+                        dSy[node] -= ty;
                     }
                 }
             }
@@ -1856,6 +1983,11 @@ const char* oracle_kernel_last_error(void* k) { return static_cast<Kernel*>(k)->
 int oracle_kernel_initialise(void* k, size_t nx, size_t ny, const double* coords, const double* mask)
 {
     return static_cast<Kernel*>(k)->initialise(nx, ny, coords, mask);
+}
+int oracle_kernel_initialise_spherical(void* k, size_t nx, size_t ny, const double* coords, int spherical,
+    const double* mask)
+{
+    return static_cast<Kernel*>(k)->initialise(nx, ny, coords, mask, spherical != 0);
 }
 int oracle_kernel_set_data(void* k, const char* name, const double* d, size_t n, size_t nc)
 {

@@ -62,6 +62,7 @@ def load() -> ctypes.CDLL:
             "oracle_kernel_destroy": (None, [c_void_p]),
             "oracle_kernel_last_error": (c_char_p, [c_void_p]),
             "oracle_kernel_initialise": (c_int, [c_void_p, c_size_t, c_size_t, c_void_p, c_void_p]),
+            "oracle_kernel_initialise_spherical": (c_int, [c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]),
             "oracle_kernel_set_data": (c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
             "oracle_kernel_get_dg0": (c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
             "oracle_kernel_get_dg": (c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
@@ -156,7 +157,8 @@ class OracleKernel:
             ny, nx = mask.shape
         c = _f64(coords).reshape(-1, 2)
         m = _f64(mask).reshape(-1)
-        self._check(self._l.oracle_kernel_initialise(self._h, nx, ny, _p(c), _p(m)))
+        self._check(self._l.oracle_kernel_initialise_spherical(self._h, nx, ny, _p(c), int(bool(isSpherical)),
+                                                               _p(m)))
         self.nx, self.ny = nx, ny
 
     def setData(self, name, data):

@@ -234,7 +234,7 @@ def test_errors_surface_and_gpu_stays_usable(gpu):
     _advance(g, box, 1)
     assert np.all(np.isfinite(g.getDG0Data("u")))
     with pytest.raises(NsdgError):
-        g.initialise(box.coords(), True, box.mask())  # spherical: unsupported
+        g.initialise(box.coords() * np.nan, False, box.mask())  # non-finite coordinates
 
 
 def test_other_fields_are_stored_not_advected(gpu):
@@ -300,3 +300,92 @@ def test_mixed_precision_snapshot_and_reproducible(gpu):
     b.restore(blob)
     _advance(b, box, 2, start=2)
     np.testing.assert_array_equal(a.getDG0Data("u"), b.getDG0Data("u"))
+
+
+# ---------------------------------------------------------------------------
+# Spherical coordinates (x = lon, y = lat in radians; the poles are moved to
+# Greenland / Antarctica by the kernel, as DynamicsKernel::initialise does)
+# ---------------------------------------------------------------------------
+def _sphere_case(nx=20, ny=16, lon=(-0.3, 0.3), lat=(1.0, 1.3), seed=3):
+    lo = np.linspace(lon[0], lon[1], nx + 1)
+    la = np.linspace(lat[0], lat[1], ny + 1)
+    X, Y = np.meshgrid(lo, la)
+    coords = np.stack([X.ravel(), Y.ravel()], 1)
+    mask = np.ones((ny, nx))
+    mask[0, :] = mask[-1, :] = 0
+    mask[:, 0] = mask[:, -1] = 0
+    rng = np.random.default_rng(seed)
+    N = nx * ny
+    cx = 0.5 * (lo[:-1] + lo[1:])
+    cy = 0.5 * (la[:-1] + la[1:])
+    CX, CY = np.meshgrid(cx, cy)
+    fields = {
+        "hice": (0.3 + 0.05 * np.sin(9 * CX) * np.cos(7 * CY)).ravel() + 0.01 * rng.standard_normal(N),
+        "cice": np.full(N, 0.95), "u": np.zeros(N), "v": np.zeros(N),
+        "uocean": 0.05 * np.cos(5 * CY).ravel(), "vocean": np.zeros(N),
+        "ssh": np.zeros(N),
+    }
+    wind = lambda s: (12.0 * np.cos(4 * CY + 0.01 * s).ravel(), 6.0 * np.sin(3 * CX - 0.02 * s).ravel())  # noqa: E731
+    return coords, mask, fields, wind
+
+
+def _sphere_make(k, case, damage=False):
+    coords, mask, fields, _ = case
+    k.initialise(coords, True, mask)
+    for name, arr in fields.items():
+        k.setData(name, arr)
+    if damage:
+        k.setData("damage", np.ones(mask.size))
+    return k
+
+
+def _sphere_advance(k, case, steps):
+    wind = case[3]
+    for s in range(steps):
+        uw, vw = wind(s)
+        k.setData("uwind", uw)
+        k.setData("vwind", vw)
+        k.update(s * 120.0, 120.0)
+
+
+@pytest.mark.parametrize("dg", [3, 6])
+def test_spherical_mevp_matches_oracle(gpu, oracle, dg):
+    case = _sphere_case()
+    prm = dict(alpha=1500.0, beta=1500.0, n_steps=100)
+    g = _sphere_make(MEVPDynamicsKernel(dg_comp=dg, **prm), case)
+    o = _sphere_make(oracle.OracleKernel(0, dg, **prm), case)
+    _sphere_advance(g, case, 3)
+    _sphere_advance(o, case, 3)
+    worst = _compare(g, o, ["hice", "cice", "u", "v", "uiostress", "viostress"], dg)
+    assert all(v <= TOL for v in worst.values()), worst
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
+    assert abs(g.meanValue("hice") - o.meanValue("hice")) <= 1e-12 * abs(o.meanValue("hice"))
+
+
+def test_spherical_bbm_is_refused(gpu):
+    """The BBM's element size (sqrt of the area of the raw vertex coordinates)
+    would be in radians on a sphere; the oracle restated from the reference
+    diverges in its first step there.  The library refuses the combination."""
+    case = _sphere_case(14, 12)
+    with pytest.raises(NsdgError) as e:
+        _sphere_make(BBMDynamicsKernel(dg_comp=6, n_steps=50), case, damage=True)
+    assert e.value.status == 6  # NSDG_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("rheology,kernel", [("mevp", "tma"), ("mevp", "global")])
+def test_spherical_mixed_precision_close_to_oracle(gpu, oracle, rheology, kernel, monkeypatch):
+    """Both FP32 element kernels (NSDG_STRESS_KERNEL forces the choice)."""
+    monkeypatch.setenv("NSDG_STRESS_KERNEL", kernel)
+    case = _sphere_case(24, 18)
+    bbm = rheology == "bbm"
+    prm = dict(n_steps=50) if bbm else dict(alpha=1500.0, beta=1500.0, n_steps=100)
+    cls = BBMDynamicsKernel if bbm else MEVPDynamicsKernel
+    g = _sphere_make(cls(dg_comp=6, precision=1, **prm), case, damage=bbm)
+    o = _sphere_make(oracle.OracleKernel(1 if bbm else 0, 6, **prm), case, damage=bbm)
+    _sphere_advance(g, case, 3)
+    _sphere_advance(o, case, 3)
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
+    err = {f: rms(g.getDG0Data(f), o.getDG0Data(f)) for f in ("u", "v", "hice", "cice")}
+    print(f"spherical {rheology} mixed ({kernel} element kernel): RMS vs oracle {err}")
+    assert max(err["u"], err["v"]) <= 1e-5, err
+    assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
