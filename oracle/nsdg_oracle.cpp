@@ -19,6 +19,10 @@
  *   - The mEVP / BBM stress updates, strain, stress divergence, momentum and
  *     the full kernel update are restated from the sources; no reference test
  *     exercises them, so that half is "parity unpinned".
+ *   - Spherical meshes (pole rotation, longitude continuity, cos(lat) weights,
+ *     the divM / iMM metric terms) have no reference test either; the
+ *     geometry is checked against the exact area of a lon/lat rectangle on
+ *     the unit sphere (tests/test_oracle_spherical.py).
  *
  * Arithmetic: FP64 throughout, compiled with -ffp-contract=off so x86-64 and
  * aarch64 give identical results.  Sums run in the order the reference's
