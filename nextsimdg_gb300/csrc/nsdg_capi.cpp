@@ -354,10 +354,10 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         for (int i = 0; i < 12; ++i) add(Ncg, 4);
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
-        add(Ncg, 8);                              // inverse lumped mass {hi, lo}
     }
     if (P.precision == NSDG_PRECISION_MIXED) {
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
+        add(Ncg, 8);                                        // inverse lumped mass {hi, lo}
     }
     if (P.precision == NSDG_PRECISION_MIXED && bbm) {
         add(ops.gx.size(), 4); add(ops.gy.size(), 4); add(ops.w.size(), 4); add(ops.wdam.size(), 4);
@@ -495,6 +495,16 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (mixed()) {
         cellX32 = upf(ops.cellX);
         cellY32 = upf(ops.cellY);
+        std::vector<float2> hl(Ncg);
+        for (size_t i = 0; i < Ncg; ++i) {
+            const float hi = static_cast<float>(invm[i]);
+            hl[i] = make_float2(hi, static_cast<float>(invm[i] - static_cast<double>(hi)));
+        }
+        invmHL = arena.take<float2>(Ncg);
+        if (!invmHL)
+            e = cudaErrorMemoryAllocation;
+        else if (e == cudaSuccess)
+            e = cudaMemcpy(invmHL, hl.data(), Ncg * sizeof(float2), cudaMemcpyHostToDevice);
     }
     if (mixed() && bbm) {
         bbm32.gx = upf(ops.gx);
@@ -556,18 +566,6 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         uLast = zf(Ncg);
         vLast = zf(Ncg);
         hP32 = zf(9 * N);
-        {
-            std::vector<float2> hl(Ncg);
-            for (size_t i = 0; i < Ncg; ++i) {
-                const float hi = static_cast<float>(invm[i]);
-                hl[i] = make_float2(hi, static_cast<float>(invm[i] - static_cast<double>(hi)));
-            }
-            invmHL = arena.take<float2>(Ncg);
-            if (!invmHL)
-                e = cudaErrorMemoryAllocation;
-            else if (e == cudaSuccess)
-                e = cudaMemcpy(invmHL, hl.data(), Ncg * sizeof(float2), cudaMemcpyHostToDevice);
-        }
     }
     derr = arena.take<int>(1);
     if (!derr)
@@ -751,7 +749,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         for (int it = 0; it < nS; ++it) {
             LCH(launchBbmStress(s, dm, dops, dg, u, v, hice, cice, damage, s11, s12, s22, contrib, bp, derr,
                 mixed() ? &bbm32 : nullptr));
-            LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr));
+            LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr, mixed() ? invmHL : nullptr));
         }
     }
 #undef LCH
@@ -1565,7 +1563,8 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 1:
             if (!bbm && k->mixed())
                 return launchMevpMomentum32(k->stream, k->dm, k->invmHL, k->st32, k->tdiv32, mp, k->derr);
-            return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr)
+            return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr,
+                             k->mixed() ? k->invmHL : nullptr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
         case 3:
         case 4:

@@ -1716,8 +1716,13 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
     }
 }
 
+// BBM momentum per CG2 node.  T = double is the reference's arithmetic; T =
+// float is the mixed-precision kernel: FP32 arithmetic on the FP64 state, the
+// inverse lumped mass as a hi/lo float pair, the sub-step averages of the
+// velocity accumulated in FP64.
+template <typename T>
 __global__ void __launch_bounds__(kBlock) kBbmMomentum(DevMesh m, DevOps o, BbmNodeState st,
-    const double* __restrict__ contrib, BbmParams p, int* __restrict__ err)
+    const double* __restrict__ contrib, BbmParams p, int* __restrict__ err, const float2* __restrict__ invmHL)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= m.Ncg)
@@ -1728,31 +1733,49 @@ __global__ void __launch_bounds__(kBlock) kBbmMomentum(DevMesh m, DevOps o, BbmN
     double dSx = 0.0, dSy = 0.0;
     if (!dir)
         gatherDivergence(m, i2, j2, contrib, dSx, dSy);
-    const double H = st.cgH[i], A = st.cgA[i];
-    const double dteOverMass = p.dt / (p.rho_ice * H);
-    const double uIce = st.u[i], vIce = st.v[i];
-    const double uo = st.uo[i], vo = st.vo[i], ua = st.ua[i], va = st.va[i];
-    const double cPrime = A * p.F_ocean * hypot(uo - uIce, vo - vIce);
-    const double alpha = 1 + dteOverMass * (cPrime * p.cosA);
-    const double beta = p.dt * p.fc + dteOverMass * cPrime * p.sinA;
-    const double rDenom = 1 / (alpha * alpha + beta * beta);
-    const double dragAtm = A * p.F_atm * hypot(ua, va);
-    const double tauX = dragAtm * ua + cPrime * (uo * p.cosA - vo * p.sinA);
-    const double tauY = dragAtm * va + cPrime * (vo * p.cosA + uo * p.sinA);
-    const double invm = o.invm2[i];
-    const double gradX = dSx * invm - p.rho_ice * H * p.gravity * st.uGrad[i];
-    const double gradY = dSy * invm - p.rho_ice * H * p.gravity * st.vGrad[i];
-    double un = alpha * uIce + beta * vIce + dteOverMass * (alpha * (gradX + tauX) + beta * (gradY + tauY));
+    const T H = static_cast<T>(st.cgH[i]), A = static_cast<T>(st.cgA[i]);
+    const T dt = static_cast<T>(p.dt), rho = static_cast<T>(p.rho_ice);
+    const T cosA = static_cast<T>(p.cosA), sinA = static_cast<T>(p.sinA);
+    const T dteOverMass = dt / (rho * H);
+    const T uIce = static_cast<T>(st.u[i]), vIce = static_cast<T>(st.v[i]);
+    const T uo = static_cast<T>(st.uo[i]), vo = static_cast<T>(st.vo[i]);
+    const T ua = static_cast<T>(st.ua[i]), va = static_cast<T>(st.va[i]);
+    const T cPrime = A * static_cast<T>(p.F_ocean) * hypot(uo - uIce, vo - vIce);
+    const T alpha = 1 + dteOverMass * (cPrime * cosA);
+    const T beta = dt * static_cast<T>(p.fc) + dteOverMass * cPrime * sinA;
+    const T rDenom = 1 / (alpha * alpha + beta * beta);
+    const T dragAtm = A * static_cast<T>(p.F_atm) * hypot(ua, va);
+    const T tauX = dragAtm * ua + cPrime * (uo * cosA - vo * sinA);
+    const T tauY = dragAtm * va + cPrime * (vo * cosA + uo * sinA);
+    T gradX, gradY;
+    if constexpr (sizeof(T) == 8) {
+        const double invm = o.invm2[i];
+        gradX = dSx * invm - p.rho_ice * H * p.gravity * st.uGrad[i];
+        gradY = dSy * invm - p.rho_ice * H * p.gravity * st.vGrad[i];
+    } else {
+        const float2 im = invmHL[i];
+        const float fx = static_cast<float>(dSx), fy = static_cast<float>(dSy);
+        const float rhoHg = rho * H * static_cast<float>(p.gravity);
+        gradX = fmaf(fx, im.y, fx * im.x) - rhoHg * static_cast<float>(st.uGrad[i]);
+        gradY = fmaf(fy, im.y, fy * im.x) - rhoHg * static_cast<float>(st.vGrad[i]);
+    }
+    T un = alpha * uIce + beta * vIce + dteOverMass * (alpha * (gradX + tauX) + beta * (gradY + tauY));
     un *= rDenom;
-    double vn = alpha * vIce - beta * uIce + dteOverMass * (alpha * (gradY + tauY) + beta * (gradX + tauX));
+    T vn = alpha * vIce - beta * uIce + dteOverMass * (alpha * (gradY + tauY) + beta * (gradX + tauX));
     vn *= rDenom;
     if (!isfinite(un) || !isfinite(vn))
         atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
-    st.avgU[i] += un / p.nSteps;
-    st.avgV[i] += vn / p.nSteps;
+    if constexpr (sizeof(T) == 8) {
+        st.avgU[i] += un / p.nSteps;
+        st.avgV[i] += vn / p.nSteps;
+    } else {
+        const double invSteps = 1.0 / p.nSteps;
+        st.avgU[i] += static_cast<double>(un) * invSteps;
+        st.avgV[i] += static_cast<double>(vn) * invSteps;
+    }
     if (dir) {
-        un = 0.0;
-        vn = 0.0;
+        un = T(0);
+        vn = T(0);
     }
     st.u[i] = un;
     st.v[i] = vn;
@@ -2154,9 +2177,12 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
 }
 
 cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o, const BbmNodeState& st,
-    const double* contrib, const BbmParams& p, int* err)
+    const double* contrib, const BbmParams& p, int* err, const float2* invmHL)
 {
-    kBbmMomentum<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err);
+    if (invmHL)
+        kBbmMomentum<float><<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err, invmHL);
+    else
+        kBbmMomentum<double><<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err, nullptr);
     return cudaGetLastError();
 }
 

@@ -285,7 +285,8 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
     const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,
     double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32 = nullptr);
 cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
-    const BbmNodeState& st, const double* contrib, const BbmParams& p, int* err);
+    const BbmNodeState& st, const double* contrib, const BbmParams& p, int* err,
+    const float2* invmHL = nullptr);
 
 // --- layout conversion, reductions ---------------------------------------
 // host ModelArray layout (AoS, nin comps) -> device SoA with `dg` comps,
