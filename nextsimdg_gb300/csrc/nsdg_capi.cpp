@@ -744,6 +744,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
             std::cos(rad * P.ocean_turning_angle), std::sin(rad * P.ocean_turning_angle),
             P.compaction_param, P.nu0, P.young, P.P0, P.undamaged_time_relaxation_sigma,
             P.exponent_relaxation_sigma, P.exponent_compression_factor, P.tan_phi, P.compr_strength, P.C_lab };
+        bbmPowModes(bp);
         BbmNodeState st { u, v, avgU, avgV, cgH, cgA, uo, vo, ua, va, uGrad, vGrad };
         LCH(launchBbmPrepNodes(s, dm, st));
         for (int it = 0; it < nS; ++it) {
@@ -1541,6 +1542,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         k->P.compaction_param, k->P.nu0, k->P.young, k->P.P0, k->P.undamaged_time_relaxation_sigma,
         k->P.exponent_relaxation_sigma, k->P.exponent_compression_factor, k->P.tan_phi, k->P.compr_strength,
         k->P.C_lab };
+    bbmPowModes(bp);
     BbmNodeState bs { k->u, k->v, k->avgU, k->avgV, k->cgH, k->cgA, k->uo, k->vo, k->ua, k->va, k->uGrad, k->vGrad };
     const size_t dN = size_t(k->dg) * k->N;
     StageFields a;

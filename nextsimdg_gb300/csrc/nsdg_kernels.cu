@@ -1522,6 +1522,19 @@ __global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState s
     st.avgV[i] = 0.0;
 }
 
+// x^y for x >= 0: by multiplication when y is a small integer (mode 1), times
+// sqrt(x) when it is a small half-integer (mode 2), else pow().  Differs from
+// pow() by a few ulps.
+template <typename T> __device__ __forceinline__ T powByMode(T x, T y, int mode, int k)
+{
+    if (mode == 0)
+        return pow(x, y);
+    T r = T(1);
+    for (int i = 0; i < k; ++i)
+        r *= x;
+    return mode == 2 ? r * sqrt(x) : r;
+}
+
 // Element operators of the BBM stress kernel in the compute type T.
 template <typename T> struct BbmOps {
     const T* gx;
@@ -1628,11 +1641,13 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         }
         T sigma_n = T(0.5) * (g11 + g22);
         const T expC = exp(static_cast<T>(p.compaction_param) * (T(1.0) - aG));
-        const T Pmax = static_cast<T>(p.P0) * pow(hG, static_cast<T>(p.exponent_compression_factor) + T(1.)) * expC;
+        const T Pmax = static_cast<T>(p.P0)
+            * powByMode(hG, static_cast<T>(p.exponent_compression_factor) + T(1.), p.powCmode, p.powCk) * expC;
         const T tildeP = (sigma_n < T(0)) ? fmin(-Pmax / sigma_n, T(1.0)) : T(0);
         T multiplicator;
         if constexpr (sizeof(T) == 8) {
-            const T powalphaexpC = pow(dG * expC, static_cast<T>(p.exponent_relaxation_sigma) - T(1));
+            const T powalphaexpC
+                = powByMode(dG * expC, static_cast<T>(p.exponent_relaxation_sigma) - T(1), p.powRmode, p.powRk);
             const T time_viscous = static_cast<T>(p.lambda) * powalphaexpC;
             multiplicator = time_viscous / (time_viscous + (T(1.) - tildeP) * dt);
         } else {

@@ -252,7 +252,32 @@ struct BbmParams {
     double rho_ice, F_atm, F_ocean, fc, gravity, dt, nSteps, cosA, sinA;
     double compaction_param, nu0, young, P0, lambda, exponent_relaxation_sigma,
         exponent_compression_factor, tan_phi, compr_strength, C_lab;
+    // how the kernels evaluate d^(n-1) (relaxation) and h^(m+1) (compression):
+    // mode 1 = integer power k by multiplication, 2 = x^k sqrt(x), 0 = pow()
+    int powRmode = 0, powRk = 0, powCmode = 0, powCk = 0;
 };
+// Sets the power modes of p from its exponents (integers and half-integers up to 8).
+inline void bbmPowModes(BbmParams& p)
+{
+    auto classify = [](double y, int& mode, int& k) {
+        mode = 0;
+        k = 0;
+        for (int n = 0; n <= 8; ++n) {
+            if (y == n) {
+                mode = 1;
+                k = n;
+                return;
+            }
+            if (y == n + 0.5) {
+                mode = 2;
+                k = n;
+                return;
+            }
+        }
+    };
+    classify(p.exponent_relaxation_sigma - 1, p.powRmode, p.powRk);
+    classify(p.exponent_compression_factor + 1., p.powCmode, p.powCk);
+}
 struct BbmNodeState {
     double* u;
     double* v;
