@@ -60,14 +60,14 @@ ALPHA = BETA = 300.0
 NSTEPS = 100
 
 
-def bytes_per_element_iteration_stress(word: int = 8) -> int:
+def bytes_per_element_iteration_stress(word: int = 8, spherical: bool = False) -> int:
     """Algorithmic DRAM bytes of one launch of the element stress kernel, per
     element: the strain operators G_x, G_y and the divergence operators A_1,
     A_2 (4 x 81 words), the pressure terms at the 9 Gauss points (FP64 P/alpha;
     in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha)), the 18
     divergence coefficients read and written, and the CG2 velocity counted
     once per node (about 4 nodes per element, u and v)."""
-    operators = 4 * 81 * word
+    operators = (6 if spherical else 4) * 81 * word  # + G_m, A_3 on a sphere
     pressure = 9 * 8 + (9 * 4 if word == 4 else 0)
     tdiv = 2 * 18 * word
     velocity = 4 * 2 * word
@@ -394,6 +394,42 @@ def bbm_variant(args, box, N: int, err_steps: int = 10):
     return out
 
 
+def spherical_variant(args, N: int, local: int):
+    """The same step on a spherical (lon, lat) mesh of the same size: a
+    patch from 57 to 74 degrees north, 34 degrees of longitude, land ring,
+    constant thickness and concentration, a spatially varying wind; FP32 and
+    FP64.  The FP32 element kernel streams 6 operator blocks instead of 4."""
+    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
+    n = args.nx
+    lo = np.linspace(-0.3, 0.3, n + 1)
+    la = np.linspace(1.0, 1.3, n + 1)
+    X, Y = np.meshgrid(lo, la)
+    coords = np.stack([X.ravel(), Y.ravel()], 1)
+    mask = np.ones((n, n))
+    mask[0, :] = mask[-1, :] = 0
+    mask[:, 0] = mask[:, -1] = 0
+    cx, cy = np.meshgrid(0.5 * (lo[:-1] + lo[1:]), 0.5 * (la[:-1] + la[1:]))
+    fields = {"hice": np.full(N, 0.3), "cice": np.full(N, 0.95), "u": np.zeros(N), "v": np.zeros(N),
+              "uocean": np.zeros(N), "vocean": np.zeros(N), "ssh": np.zeros(N),
+              "uwind": (12.0 * np.cos(4 * cy)).ravel(), "vwind": (6.0 * np.sin(3 * cx)).ravel()}
+    out = {"mesh": f"{n}x{n} lon/lat cells, lon -0.3..0.3 rad, lat 1.0..1.3 rad"}
+    for name, prec in (("fp64", 0), ("fp32", 1)):
+        k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=prec)
+        k.initialise(coords, True, mask)
+        for f, arr in fields.items():
+            k.setData(f, arr)
+        k.time_updates(DT, 3)
+        steps = max(3, args.steps // 2)
+        ms = k.time_updates(DT, steps) / steps
+        kms, kname = k.time_kernel(0, 30)
+        bpe = bytes_per_element_iteration_stress(4 if prec else 8, spherical=True)
+        out[name] = {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "stress_kernel": kname,
+                     "stress_kernel_ms": kms, "stress_GBps": N * bpe / (kms * 1e-3) / 1e9,
+                     "algorithmic_bytes_per_element": bpe}
+        k.close()
+    return out
+
+
 def day_error(args, box, steps: int):
     """Velocity / thickness / concentration RMS after `steps` model steps: the
     headline precision path and the FP64 path with h scaled by (1 + 1e-14),
@@ -493,6 +529,8 @@ def run_ours(args, world, rank, local):
             variants["learned_fp32"] = learned_variant(args, box, N, ms_max / args.steps)
         if prec and not args.no_bbm:
             variants["bbm"] = bbm_variant(args, box, N)
+        if prec:
+            variants["spherical"] = spherical_variant(args, N, local)
     err = day_error(args, box, args.error_steps) if (prec and args.error_steps > 0 and world == 1) else None
 
     if rank == 0:

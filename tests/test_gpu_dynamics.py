@@ -247,14 +247,14 @@ def test_other_fields_are_stored_not_advected(gpu):
     np.testing.assert_array_equal(g.getDGData("tracer", ncomp=1), tracer)
 
 
-@pytest.mark.parametrize("n,steps", [(32, 5), (64, 3)])
-def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
+@pytest.mark.parametrize("n,steps,dg", [(32, 5, 6), (64, 3, 6), (32, 5, 3), (32, 5, 1)])
+def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps, dg):
     """FP32 bulk with FP64 Delta/viscosity, lumped-mass inverse and
     conservation sums: RMS error against the FP64 oracle, stated bars."""
     box = BoxTest(n)
     prm = dict(alpha=300.0, beta=300.0, n_steps=100)
-    g = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
-    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    g = _make(MEVPDynamicsKernel, box, dg, None, precision=1, **prm)
+    o = _make(oracle.OracleKernel, box, dg, 0, **prm)
     _advance(g, box, steps)
     _advance(o, box, steps)
     rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
