@@ -301,6 +301,16 @@ typedef struct nsdg_warm_stats {
 int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
 
 /* ======================================================================== */
+/* Failure-detection self-test                                               */
+/* ======================================================================== */
+/* No counterpart in the reference.  The only waits in the library's kernels
+ * (the TMA stress kernel's mbarrier waits) are bounded in time; this runs one
+ * such wait on an mbarrier that nothing completes, with a limit of
+ * limit_seconds (0 < limit <= 2), and reports *timed_out = 1 when the wait ran
+ * out and the kernel returned as it must.  The GPU context stays usable. */
+int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
+
+/* ======================================================================== */
 /* Allocation-free entry point                                               */
 /* ======================================================================== */
 /* No counterpart in the reference.  Tools::MeanValue (the FP64 mesh integral

@@ -125,6 +125,7 @@ SIGNATURES = [
     ("nsdg_kernel_warm_sample", c_int, [c_void_p, c_double, c_double, c_int, c_void_p, c_int, POINTER(c_double)]),
     ("nsdg_kernel_set_warm_start", c_int, [c_void_p, c_void_p, c_int, c_double, c_int, c_double]),
     ("nsdg_kernel_warm_stats", c_int, [c_void_p, c_void_p]),
+    ("nsdg_selftest_bounded_wait", c_int, [c_double, POINTER(c_int)]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 

@@ -2242,4 +2242,31 @@ int nsdg_ensemble_launches_per_update(nsdg_ensemble* ens, int* launches)
     return NSDG_OK;
 }
 
+int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out)
+{
+    if (!timed_out || !(limit_seconds > 0.0) || limit_seconds > 2.0)
+        return NSDG_ERR_BAD_ARG;
+    std::string m;
+    const int st = deviceCheck(m);
+    if (st != NSDG_OK)
+        return st;
+    int* d = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0xff, sizeof(int), s);
+    if (e == cudaSuccess) e = launchBoundedWaitSelfTest(s, limit_seconds, d);
+    int h = -1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (d)
+        cudaFree(d);
+    if (s)
+        cudaStreamDestroy(s);
+    if (e != cudaSuccess)
+        return NSDG_ERR_CUDA;
+    *timed_out = h;
+    return NSDG_OK;
+}
+
 } // extern "C"

@@ -1193,15 +1193,17 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32(Dev
 // read it, the divergence rows (A_1, A_2).  One 24 KB buffer per block keeps
 // nine blocks (27 warps) resident per SM, each with a 20.7 KB copy in
 // flight; the velocity gathers and P/alpha loads are issued while the first
-// copy lands.  Waits are bounded: a copy that has not landed after kTmaSpin
-// polls sets DEV_ERR_TIMEOUT and the block returns after a second bounded
-// wait for the copy it issued.
+// copy lands.  Waits are bounded in time (kWaitNs of the GPU's global timer,
+// and at most kTmaSpin polls): a copy that has not landed by then sets
+// DEV_ERR_TIMEOUT and the block returns after a second bounded wait for the
+// copy it issued.
 namespace {
 constexpr int kTmaRows = 162;                           // G_x | G_y  (A_1 | A_2)
 constexpr int kTmaRowsSph = 243;                        // G_x | G_y | G_m  (A_1 | A_2 | A_3)
 template <bool SPH> __host__ __device__ constexpr int tmaRows() { return SPH ? kTmaRowsSph : kTmaRows; }
 template <bool SPH> __host__ __device__ constexpr unsigned tmaTileBytes() { return tmaRows<SPH>() * kTmaElems * 4; }
 constexpr long kTmaSpin = 1L << 26;
+constexpr unsigned long long kWaitNs = 1000000000ull; // 1 s
 
 __device__ __forceinline__ unsigned smemAddr(const void* p)
 {
@@ -1227,11 +1229,22 @@ __device__ __forceinline__ bool mbarTryWait(uint64_t* bar, unsigned parity)
                  : "memory");
     return done != 0;
 }
-__device__ __forceinline__ bool mbarWaitBounded(uint64_t* bar, unsigned parity)
+__device__ __forceinline__ unsigned long long globalTimerNs()
 {
-    for (long i = 0; i < kTmaSpin; ++i)
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ bool mbarWaitBounded(uint64_t* bar, unsigned parity,
+    unsigned long long limitNs = kWaitNs)
+{
+    const unsigned long long t0 = globalTimerNs();
+    for (long i = 0; i < kTmaSpin; ++i) {
         if (mbarTryWait(bar, parity))
             return true;
+        if ((i & 63) == 63 && globalTimerNs() - t0 > limitNs)
+            break;
+    }
     return false;
 }
 __device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
@@ -1475,6 +1488,19 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress32Batc
     const size_t e = inside ? size_t(iy) * M.nx + ix : 0;
     const bool active = inside && M.ice[e];
     mevpStress32Element(M.nx, M.N, active, e, le, part, M.o, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, fs);
+}
+
+// Self-test of the bounded wait: one thread waits on an mbarrier that nothing
+// will complete (expected arrivals 1, none made), records whether the wait
+// ran out, and the barrier is left behind with the block.
+__global__ void kBoundedWaitSelfTest(unsigned long long limitNs, int* __restrict__ timedOut)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbarInit(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *timedOut = mbarWaitBounded(&bar, 0, limitNs) ? 0 : 1;
+    }
 }
 
 __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32TmaBatched(
@@ -2032,6 +2058,13 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
     CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 } // namespace
+
+cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* timedOut)
+{
+    const double ns = limitSeconds * 1e9;
+    kBoundedWaitSelfTest<<<1, 32, 0, s>>>(static_cast<unsigned long long>(ns < 0 ? 0 : ns), timedOut);
+    return cudaGetLastError();
+}
 
 cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
 {

@@ -183,6 +183,9 @@ struct alignas(64) StressMaps {
     CUtensorMap a;
 };
 cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out);
+// One block waits (bounded) on an mbarrier nothing completes; *timedOut = 1
+// when the wait ran out as it must.
+cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* timedOut);
 // kMevpStress32 with the operator tiles staged in shared memory by TMA.
 cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err);

@@ -389,3 +389,37 @@ def test_spherical_mixed_precision_close_to_oracle(gpu, oracle, rheology, kernel
     print(f"spherical {rheology} mixed ({kernel} element kernel): RMS vs oracle {err}")
     assert max(err["u"], err["v"]) <= 1e-5, err
     assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
+
+
+def test_bounded_wait_runs_out_and_the_gpu_stays_usable(gpu):
+    """Failure detection without a GPU fault: a device wait on an mbarrier
+    that nothing completes gives up after its time limit and reports it."""
+    import ctypes
+    import time
+    from nextsimdg_gb300 import _lib
+    lib = _lib.load()
+    flag = ctypes.c_int(-1)
+    t0 = time.perf_counter()
+    assert lib.nsdg_selftest_bounded_wait(0.02, ctypes.byref(flag)) == _lib.NSDG_OK
+    assert flag.value == 1
+    assert time.perf_counter() - t0 < 10.0
+    assert lib.nsdg_selftest_bounded_wait(0.0, ctypes.byref(flag)) == _lib.NSDG_ERR_BAD_ARG
+    box = BoxTest(8)
+    g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=5, precision=1)
+    _advance(g, box, 1)
+    assert np.all(np.isfinite(g.getDG0Data("u")))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_zero_thickness_is_handled(gpu, precision):
+    """Open water everywhere (h = 0, A = 0): the clamps of prepareIteration
+    (H, A >= 1e-4) keep the momentum finite; nothing is flagged."""
+    box = BoxTest(12)
+    g = _make(MEVPDynamicsKernel, box, 6, None, n_steps=20, precision=precision)
+    g.setData("hice", np.zeros(box.nelements))
+    g.setData("cice", np.zeros(box.nelements))
+    _advance(g, box, 2)
+    g.synchronize()
+    for f in ("u", "v", "hice", "cice"):
+        assert np.all(np.isfinite(g.getDG0Data(f))), f
+    assert np.all(g.getDG0Data("hice") == 0.0)
