@@ -293,7 +293,9 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
                 traffic = int(line.split(":")[1])
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": traffic, "kernel": kname, "kernel_ms": kms, "share_of_step": kms * NSTEPS / ms_step,
-            "algorithmic_bytes_per_element": bpe, "peak_kind": hbm_kind}
+            "algorithmic_bytes_per_element": bpe, "peak_kind": hbm_kind,
+            "kernel_timing": "CUDA events on the library's stream around 50 back-to-back launches of the kernel "
+                             "on the workload's state, right after the timed steps"}
     if prec:
         # both FP32 stress kernels (the library keeps the faster at initialise)
         roof["stress_kernel_ms"] = {k.time_kernel(i, 50)[1]: k.time_kernel(i, 50)[0] for i in (3, 4)}
