@@ -145,6 +145,10 @@ struct nsdg_kernel {
     std::unordered_map<std::string, std::vector<double>> bucket;
     std::unordered_map<std::string, int> bucketComps;
     size_t stepNumber = 0;
+    // read-out projections kept until the state changes: bit 1 = u, v in
+    // (velx, vely), bit 2 = the ice-ocean stress in phiA (work arrays that are
+    // free outside an update)
+    int readCache = 0;
     // learned warm start (mixed-precision mEVP): the attached network, the
     // iteration count after it, the acceptance bound, the judgement schedule,
     // backups of the sub-cycle's starting state, the previous sub-cycle's
@@ -273,6 +277,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     bucket.clear();
     bucketComps.clear();
     stepNumber = 0;
+    readCache = 0;
 
     // --- host mesh (DynamicsKernel.hpp:44-75) ---
     mesh = HostMesh();
@@ -1072,6 +1077,7 @@ int nsdg_kernel::launchStep(double dt)
     if (warmNet)
         ++warmSteps;
     ++stepNumber;
+    readCache = 0;
     return NSDG_OK;
 }
 
@@ -1201,6 +1207,7 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
         return k->fail(NSDG_ERR_BAD_ARG, "set_data: null data");
     if (n_elements != k->N || n_comp == 0 || n_comp > 8)
         return k->fail(NSDG_ERR_SIZE_MISMATCH, std::string("set_data: size mismatch for ") + name);
+    k->readCache = 0;
     const std::string s(name);
     const int dg = k->dg;
     const size_t N = k->N;
@@ -1236,7 +1243,15 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
     };
     int r = cu(cudaMemcpyAsync(k->staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, st), "set_data copy");
     if (r) return r;
-    if (cgTarget) {
+    if (cgTarget && n_comp != size_t(dg)) {
+        // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so DG2CG
+        // of the one-component field gives the same node values (the higher
+        // components' contributions are exact zeros)
+        const double* in[1] = { k->staging };
+        double* out[1] = { cgTarget };
+        r = cu(launchDG2CG(st, k->dm, 1, 1, in, out), "set_data DG2CG");
+        if (r) return r;
+    } else if (cgTarget) {
         // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
         r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, k->staging, k->dgTmp), "set_data convert");
         if (r) return r;
@@ -1291,24 +1306,33 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
     const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
     const double* src = nullptr;
     cudaError_t e = cudaSuccess;
-    if (s == "u" || s == "v" || s == "uiostress" || s == "viostress") {
-        const double* cg = nullptr;
-        if (s == "u") cg = k->u;
-        else if (s == "v") cg = k->v;
-        else {
+    const double* minvP = k->dops.minvP ? k->dops.minvP : k->dops.minv;
+    if (s == "u" || s == "v") {
+        // both components are projected on the first read after a state change
+        if (!(k->readCache & 1)) {
+            const double* in[2] = { k->u, k->v };
+            double* outd[2] = { k->velx, k->vely };
+            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+            if (e == cudaSuccess)
+                k->readCache |= 1;
+        }
+        src = (s == "u") ? k->velx : k->vely;
+    } else if (s == "uiostress" || s == "viostress") {
+        if (!(k->readCache & 2)) {
             const double rad = 0x1.1df46a2529d39p-6;
             const double ang = bbm ? k->P.ocean_turning_angle : 0.0;
             double* tx = k->cgTmp;
             double* ty = k->u0; // reused as scratch outside update
             e = launchIceOceanStress(st, k->Ncg, bbm ? 1 : 0, bbm ? k->avgU : k->u, bbm ? k->avgV : k->v,
                 k->uo, k->vo, k->P.F_ocean, std::cos(rad * ang), std::sin(rad * ang), tx, ty);
-            cg = (s == "uiostress") ? tx : ty;
+            const double* in[2] = { tx, ty };
+            double* outd[2] = { k->phiA, k->phiA + size_t(dg) * N };
+            if (e == cudaSuccess)
+                e = launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+            if (e == cudaSuccess)
+                k->readCache |= 2;
         }
-        const double* in[1] = { cg };
-        double* outd[1] = { k->dgTmp };
-        if (e == cudaSuccess)
-            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, k->dops.minvP ? k->dops.minvP : k->dops.minv, 1, in, outd);
-        src = k->dgTmp;
+        src = (s == "uiostress") ? k->phiA : k->phiA + size_t(dg) * N;
     } else if (s == "hice") src = k->hice;
     else if (s == "cice") src = k->cice;
     else if (s == "damage" && bbm) src = k->damage;
@@ -1448,6 +1472,8 @@ int nsdg_kernel_snapshot_save(nsdg_kernel* k, void* buffer, size_t bytes)
 
 int nsdg_kernel_snapshot_load(nsdg_kernel* k, const void* buffer, size_t bytes)
 {
+    if (k)
+        k->readCache = 0;
     size_t need = 0;
     int r = nsdg_kernel_snapshot_size(k, &need);
     if (r)
@@ -1526,6 +1552,8 @@ int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms)
 
 int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms, const char** name)
 {
+    if (k)
+        k->readCache = 0; // the timed kernels change the state
     if (!k || !mean_ms || reps < 1)
         return NSDG_ERR_BAD_ARG;
     if (!k->ready)
@@ -1632,6 +1660,8 @@ int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches)
 int nsdg_kernel_warm_sample(nsdg_kernel* k, double t_start, double dt, int k_iters, nsdg_net* net, int slot,
     double* plain_ratio)
 {
+    if (k)
+        k->readCache = 0;
     (void)t_start;
     if (!k || !net)
         return NSDG_ERR_BAD_ARG;
@@ -2144,6 +2174,9 @@ const char* nsdg_ensemble_last_error(const nsdg_ensemble* ens) { return ens ? en
 
 int nsdg_ensemble_update(nsdg_ensemble* ens, double t_start, double dt)
 {
+    if (ens)
+        for (auto* m : ens->members)
+            m->readCache = 0;
     (void)t_start;
     if (!ens)
         return NSDG_ERR_BAD_ARG;
@@ -2190,6 +2223,9 @@ int nsdg_ensemble_synchronize(nsdg_ensemble* ens)
 
 int nsdg_ensemble_time_updates(nsdg_ensemble* ens, double dt, int steps, float* ms)
 {
+    if (ens)
+        for (auto* m : ens->members)
+            m->readCache = 0;
     if (!ens || !ms || steps < 1)
         return NSDG_ERR_BAD_ARG;
     int r = ens->ensureGraph(dt);
