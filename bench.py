@@ -21,7 +21,7 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
                           same grid, with its own roofline;
   variants.learned_fp32   the learned warm start: data generation and
                           training on the GPU, then the warm update with and
-                          without judgement against the plain sub-cycle;
+                          without audit against the plain sub-cycle;
   velocity_error_vs_fp64  one simulated day: FP32 path vs FP64 path, next to
                           the FP64 path's own response to h x (1 + 1e-14).
 
@@ -310,7 +310,7 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
 def learned_variant(args, box_eval, N: int, plain_ms: float):
     """The learned warm start: samples from a perturbed trajectory (other h
     phases, cyclone start and speed), training on the GPU, then (a) the warm
-    update without judgement and (b) judged every 10th update against the
+    update without audit and (b) audited every 10th update against the
     plain sub-cycle with a relative tolerance of 0.1, on the evaluation box."""
     from nextsimdg_gb300 import surrogate
     from nextsimdg_gb300.boxtest import BoxTest, step_forcing
@@ -327,7 +327,7 @@ def learned_variant(args, box_eval, N: int, plain_ms: float):
     out = {"k_iters": K, "samples": args.warm_samples, "train_iterations": args.warm_train_iters,
            "train_loss": loss, "data_and_training_s": t_train, "kappa": kappa * 1.5}
     res = {}
-    for name, je, jt in (("unjudged", 0, 0.0), ("judged_every_10_tol_0.1", 10, 0.1)):
+    for name, je, jt in (("unaudited", 0, 0.0), ("audited_every_10_tol_0.1", 10, 0.1)):
         k = make_kernel(box_eval, 1)
         k.set_warm_start(net, K, kappa * 1.5, je, jt)
         for s in range(args.warmup):
@@ -336,8 +336,8 @@ def learned_variant(args, box_eval, N: int, plain_ms: float):
         ms = k.time_updates(DT, args.steps) / args.steps
         st = k.warm_stats()
         res[name] = {"value": N / (ms * 1e-3), "ms_per_step": ms, "speedup_vs_plain_fp32": plain_ms / ms,
-                     "accepted": st["accepted"], "fallbacks": st["fallbacks"], "judged": st["judged"],
-                     "judge_rejected": st["judge_rejected"], "last_judged_rel_error": st["last_judged_error"]}
+                     "accepted": st["accepted"], "fallbacks": st["fallbacks"], "audited": st["audited"],
+                     "audit_rejected": st["audit_rejected"], "last_audit_rel_error": st["last_audit_error"]}
         k.close()
     out.update(res)
     net.close()

@@ -281,22 +281,22 @@ int nsdg_kernel_warm_sample(nsdg_kernel* k, double t_start, double dt, int k_ite
  * network + k_iters iterations and accepts the result when the warm start is
  * enabled, the attempt produced only finite values and its residual (as
  * above) is at most `kappa`; otherwise it restores the state at the start of
- * the sub-cycle and runs the plain n_steps iterations.  With judge_every > 0,
- * the first update and every judge_every-th after it are judged: the warm
+ * the sub-cycle and runs the plain n_steps iterations.  With audit_every > 0,
+ * the first update and every audit_every-th after it are audited: the warm
  * attempt and the plain sub-cycle both run from the same start, the plain
- * result is kept, and the warm start stays enabled until the next judgement
- * only if |warm - plain| / |plain - start| (RMS over CG2 nodes) <= judge_tol.
+ * result is kept, and the warm start stays enabled until the next audit
+ * only if |warm - plain| / |plain - start| (RMS over CG2 nodes) <= audit_tol.
  * All decisions are taken on the device, inside the update's CUDA graphs.
  * The net must stay alive while attached.  mEVP in mixed precision only
  * (NSDG_ERR_UNSUPPORTED otherwise). */
 int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, double kappa,
-    int judge_every, double judge_tol);
+    int audit_every, double audit_tol);
 typedef struct nsdg_warm_stats {
     long long accepted, fallbacks;       /* warm updates accepted / fallen back   */
-    long long judged, judge_rejected;    /* judged updates / judgements that disabled it */
-    double last_ratio, last_judged_error;
-    int enabled;                         /* current judgement                     */
-    int launches_warm, launches_judged, launches_fallback; /* kernels per graph    */
+    long long audited, audit_rejected;    /* audited updates / audits that disabled it */
+    double last_ratio, last_audit_error;
+    int enabled;                         /* current audit                     */
+    int launches_warm, launches_audited, launches_fallback; /* kernels per graph    */
 } nsdg_warm_stats;
 int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
 

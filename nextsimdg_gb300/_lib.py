@@ -58,9 +58,9 @@ class WarmStats(ctypes.Structure):
 
     _fields_ = [
         ("accepted", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
-        ("judged", ctypes.c_longlong), ("judge_rejected", ctypes.c_longlong),
-        ("last_ratio", c_double), ("last_judged_error", c_double),
-        ("enabled", c_int), ("launches_warm", c_int), ("launches_judged", c_int), ("launches_fallback", c_int),
+        ("audited", ctypes.c_longlong), ("audit_rejected", ctypes.c_longlong),
+        ("last_ratio", c_double), ("last_audit_error", c_double),
+        ("enabled", c_int), ("launches_warm", c_int), ("launches_audited", c_int), ("launches_fallback", c_int),
     ]
 
     def as_dict(self):

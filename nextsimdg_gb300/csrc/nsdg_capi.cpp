@@ -150,22 +150,22 @@ struct nsdg_kernel {
     // free outside an update)
     int readCache = 0;
     // learned warm start (mixed-precision mEVP): the attached network, the
-    // iteration count after it, the acceptance bound, the judgement schedule,
+    // iteration count after it, the acceptance bound, the audit schedule,
     // backups of the sub-cycle's starting state, the previous sub-cycle's
     // starting state (features) and the device-side decision record
     NetImpl* warmNet = nullptr;
     int warmK = 0;
     double warmKappa = 0.0;
-    int judgeEvery = 0;
-    double judgeTol = 0.0;
+    int auditEvery = 0;
+    double auditTol = 0.0;
     long long warmSteps = 0;   // updates since attaching
     void* warmMem = nullptr;
     float *bu = nullptr, *bv = nullptr, *btdiv = nullptr, *uPrev = nullptr, *vPrev = nullptr;
     float* wbase = nullptr;
     double *wPart = nullptr, *wRes = nullptr;
     WarmRecord rec {};
-    cudaGraphExec_t judgeGraph = nullptr;
-    int judgeLaunches = 0;
+    cudaGraphExec_t auditGraph = nullptr;
+    int auditLaunches = 0;
     int warmBodyLaunches = 0;
 
     int fail(int code, const std::string& m)
@@ -182,9 +182,9 @@ struct nsdg_kernel {
     {
         if (graph)
             cudaGraphExecDestroy(graph);
-        if (judgeGraph)
-            cudaGraphExecDestroy(judgeGraph);
-        graph = judgeGraph = nullptr;
+        if (auditGraph)
+            cudaGraphExecDestroy(auditGraph);
+        graph = auditGraph = nullptr;
         graphDt = -1.0;
         launchesPerUpdate = 0;
     }
@@ -199,9 +199,9 @@ struct nsdg_kernel {
     void releaseDevice()
     {
         releaseWarm();
-        if (judgeGraph)
-            cudaGraphExecDestroy(judgeGraph);
-        judgeGraph = nullptr;
+        if (auditGraph)
+            cudaGraphExecDestroy(auditGraph);
+        auditGraph = nullptr;
         if (graph)
             cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -231,7 +231,7 @@ struct nsdg_kernel {
     int saveLast(cudaStream_t s, float* bu_, float* bv_, float* btdiv_);
     int enqueueWarmFront(cudaStream_t s, double dt, int& launches);
     int captureWarmGraph(double dt, cudaGraph_t& g, int& launches);
-    int captureJudgeGraph(double dt, cudaGraph_t& g, int& launches);
+    int captureAuditGraph(double dt, cudaGraph_t& g, int& launches);
     int launchStep(double dt);
     int checkDeviceError();
 };
@@ -968,10 +968,10 @@ int nsdg_kernel::captureWarmGraph(double dt, cudaGraph_t& g, int& launches)
     return NSDG_OK;
 }
 
-// A judged update: the warm attempt, then the plain sub-cycle from the same
+// A audited update: the warm attempt, then the plain sub-cycle from the same
 // start (its result is kept), and the relative distance between the two
 // decides whether the following updates may accept warm sub-cycles.
-int nsdg_kernel::captureJudgeGraph(double dt, cudaGraph_t& g, int& launches)
+int nsdg_kernel::captureAuditGraph(double dt, cudaGraph_t& g, int& launches)
 {
     launches = 0;
     g = nullptr;
@@ -984,16 +984,16 @@ int nsdg_kernel::captureJudgeGraph(double dt, cudaGraph_t& g, int& launches)
         if (e == cudaSuccess) e = launchWarmSave(stream, Ncg, bv, st32.v, nullptr);
         if (e == cudaSuccess) e = launchWarmSave(stream, 18 * N, btdiv, tdiv32, nullptr);
         if (e != cudaSuccess)
-            st = fail(NSDG_ERR_CUDA, std::string("judge graph: ") + cudaGetErrorString(e));
+            st = fail(NSDG_ERR_CUDA, std::string("audit graph: ") + cudaGetErrorString(e));
         launches += 5;
     }
     if (st == NSDG_OK)
         st = mixedIterations(stream, dt, P.n_steps, derr, launches);
     if (st == NSDG_OK) {
         cudaError_t e = launchWarmResidual(stream, Ncg, st32.u, st32.v, uPrev, vPrev, st32.u0, st32.v0, wPart, wRes);
-        if (e == cudaSuccess) e = launchWarmJudge(stream, wRes, judgeTol, rec);
+        if (e == cudaSuccess) e = launchWarmAudit(stream, wRes, auditTol, rec);
         if (e != cudaSuccess)
-            st = fail(NSDG_ERR_CUDA, std::string("judge graph: ") + cudaGetErrorString(e));
+            st = fail(NSDG_ERR_CUDA, std::string("audit graph: ") + cudaGetErrorString(e));
         launches += 3;
     }
     if (st == NSDG_OK) {
@@ -1005,7 +1005,7 @@ int nsdg_kernel::captureJudgeGraph(double dt, cudaGraph_t& g, int& launches)
     if (st != NSDG_OK)
         return st;
     if (ec != cudaSuccess)
-        return fail(NSDG_ERR_CUDA, std::string("judge graph capture: ") + cudaGetErrorString(ec));
+        return fail(NSDG_ERR_CUDA, std::string("audit graph capture: ") + cudaGetErrorString(ec));
     return NSDG_OK;
 }
 
@@ -1043,34 +1043,34 @@ int nsdg_kernel::ensureGraph(double dt)
     }
     graphDt = dt;
     launchesPerUpdate = launches;
-    if (warmNet && judgeEvery > 0) {
+    if (warmNet && auditEvery > 0) {
         cudaGraph_t gj = nullptr;
-        const int st = captureJudgeGraph(dt, gj, judgeLaunches);
+        const int st = captureAuditGraph(dt, gj, auditLaunches);
         if (st != NSDG_OK) {
             if (gj)
                 cudaGraphDestroy(gj);
             return st;
         }
-        const cudaError_t ej = cudaGraphInstantiate(&judgeGraph, gj, 0);
+        const cudaError_t ej = cudaGraphInstantiate(&auditGraph, gj, 0);
         cudaGraphDestroy(gj);
         if (ej != cudaSuccess) {
-            judgeGraph = nullptr;
-            return fail(NSDG_ERR_CUDA, std::string("judge graph instantiate: ") + cudaGetErrorString(ej));
+            auditGraph = nullptr;
+            return fail(NSDG_ERR_CUDA, std::string("audit graph instantiate: ") + cudaGetErrorString(ej));
         }
     }
     return NSDG_OK;
 }
 
 // Launches the update graph of the next step: with a warm start attached and
-// judging on, every judgeEvery-th update (the first included) is a judged one.
+// auditing on, every auditEvery-th update (the first included) is a audited one.
 int nsdg_kernel::launchStep(double dt)
 {
     int r = ensureGraph(dt);
     if (r)
         return r;
     cudaGraphExec_t gx = graph;
-    if (warmNet && judgeEvery > 0 && warmSteps % judgeEvery == 0)
-        gx = judgeGraph;
+    if (warmNet && auditEvery > 0 && warmSteps % auditEvery == 0)
+        gx = auditGraph;
     const cudaError_t e = cudaGraphLaunch(gx, stream);
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("update: ") + cudaGetErrorString(e));
@@ -1736,8 +1736,8 @@ int nsdg_kernel_warm_sample(nsdg_kernel* k, double t_start, double dt, int k_ite
     return k->ok();
 }
 
-int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, double kappa, int judge_every,
-    double judge_tol)
+int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, double kappa, int audit_every,
+    double audit_tol)
 {
     if (!k)
         return NSDG_ERR_BAD_ARG;
@@ -1760,8 +1760,8 @@ int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, doubl
         return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: k_iters must be in [1, n_steps]");
     if (!(kappa >= 0) || !std::isfinite(kappa))
         return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: kappa must be finite and non-negative");
-    if (judge_every < 0 || (judge_every > 0 && (!(judge_tol >= 0) || !std::isfinite(judge_tol))))
-        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: judge_every >= 0 and a finite judge_tol >= 0 needed");
+    if (audit_every < 0 || (audit_every > 0 && (!(audit_tol >= 0) || !std::isfinite(audit_tol))))
+        return k->fail(NSDG_ERR_BAD_ARG, "set_warm_start: audit_every >= 0 and a finite audit_tol >= 0 needed");
     k->dropGraphs();
     const int r = k->allocWarm();
     if (r)
@@ -1773,8 +1773,8 @@ int nsdg_kernel_set_warm_start(nsdg_kernel* k, nsdg_net* net, int k_iters, doubl
     k->warmNet = n;
     k->warmK = k_iters;
     k->warmKappa = kappa;
-    k->judgeEvery = judge_every;
-    k->judgeTol = judge_tol;
+    k->auditEvery = audit_every;
+    k->auditTol = audit_tol;
     k->warmSteps = 0;
     return k->ok();
 }
@@ -1795,13 +1795,13 @@ int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out)
     CUDA_TRY_K(cudaStreamSynchronize(k->stream));
     out->accepted = c[0];
     out->fallbacks = c[1];
-    out->judged = c[2];
-    out->judge_rejected = c[3];
+    out->audited = c[2];
+    out->audit_rejected = c[3];
     out->last_ratio = last[0];
-    out->last_judged_error = last[1];
+    out->last_audit_error = last[1];
     out->enabled = enabled;
     out->launches_warm = k->launchesPerUpdate;
-    out->launches_judged = k->judgeLaunches;
+    out->launches_audited = k->auditLaunches;
     out->launches_fallback = k->warmBodyLaunches;
     return k->ok();
 }

@@ -871,7 +871,7 @@ __global__ void kWarmDecide(cudaGraphConditionalHandle h, const double* __restri
     cudaGraphSetConditional(h, ok ? 0u : 1u);
 }
 
-__global__ void kWarmJudge(const double* __restrict__ res, double tol, WarmRecord rec)
+__global__ void kWarmAudit(const double* __restrict__ res, double tol, WarmRecord rec)
 {
     const double r = res[0], d = res[1];
     const double err = d > 0.0 ? sqrt(r / d) : (r > 0.0 ? INFINITY : 0.0);
@@ -919,9 +919,9 @@ cudaError_t launchWarmDecide(cudaStream_t s, cudaGraphConditionalHandle h, const
     kWarmDecide<<<1, 1, 0, s>>>(h, res, kappa, rec);
     return cudaGetLastError();
 }
-cudaError_t launchWarmJudge(cudaStream_t s, const double* res, double tol, const WarmRecord& rec)
+cudaError_t launchWarmAudit(cudaStream_t s, const double* res, double tol, const WarmRecord& rec)
 {
-    kWarmJudge<<<1, 1, 0, s>>>(res, tol, rec);
+    kWarmAudit<<<1, 1, 0, s>>>(res, tol, rec);
     return cudaGetLastError();
 }
 cudaError_t launchWarmSave(cudaStream_t s, size_t n, const float* src, float* dst1, float* dst2)

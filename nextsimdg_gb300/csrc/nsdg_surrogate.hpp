@@ -100,12 +100,12 @@ int netDatasetNormalise(NetImpl* n, int count, std::string& err);
 int netTrain(NetImpl* n, int count, int iterations, int batch, float lr, unsigned long long seed, float* loss,
     std::string& err);
 bool netIsWarmShaped(NetImpl* n, int nx, int ny);
-// Device-side record of the warm start (counts: accepted, fallbacks, judged,
-// judged-and-rejected sub-cycles).
+// Device-side record of the warm start (counts: accepted, fallbacks, audited,
+// audited-and-rejected sub-cycles).
 struct WarmRecord {
     long long* counts;  // [4]
     int* warmErr;       // numeric fault of the warm attempt (private to it)
-    int* enabled;       // 1 while the last judgement allows warm sub-cycles
+    int* enabled;       // 1 while the last audit allows warm sub-cycles
     double* lastRatio;
     double* lastError;
 };
@@ -116,10 +116,10 @@ struct WarmRecord {
 // the warm error word.
 cudaError_t launchWarmDecide(cudaStream_t s, cudaGraphConditionalHandle h, const double* res, double kappa,
     const WarmRecord& rec);
-// Judgement against the plain sub-cycle: err = sqrt(res[0] / res[1]) with
+// Audit against the plain sub-cycle: err = sqrt(res[0] / res[1]) with
 // res from launchWarmResidual(plain result, warm result, start); enables the
 // warm start when the warm attempt raised no device error and err <= tol.
-cudaError_t launchWarmJudge(cudaStream_t s, const double* res, double tol, const WarmRecord& rec);
+cudaError_t launchWarmAudit(cudaStream_t s, const double* res, double tol, const WarmRecord& rec);
 // dst1 = dst2 = src (dst2 may be null)
 cudaError_t launchWarmSave(cudaStream_t s, size_t n, const float* src, float* dst1, float* dst2);
 // dst = (float) src

@@ -191,16 +191,16 @@ class _KernelBase:
                                                     int(slot), byref(ratio)))
         return ratio.value
 
-    def set_warm_start(self, net, k_iters: int = 0, kappa: float = 0.0, judge_every: int = 0,
-                       judge_tol: float = 0.0):
+    def set_warm_start(self, net, k_iters: int = 0, kappa: float = 0.0, audit_every: int = 0,
+                       audit_tol: float = 0.0):
         """Attaches `net` (None detaches); later updates run the network plus
         `k_iters` iterations, falling back to the full count when the
-        last-iteration ratio exceeds `kappa`; every `judge_every`-th update
+        last-iteration ratio exceeds `kappa`; every `audit_every`-th update
         also runs the plain sub-cycle and keeps the warm start enabled only
-        while the warm result is within `judge_tol` (relative) of it."""
+        while the warm result is within `audit_tol` (relative) of it."""
         self._check(self._l.nsdg_kernel_set_warm_start(self._h, None if net is None else net._h,
-                                                       int(k_iters), float(kappa), int(judge_every),
-                                                       float(judge_tol)))
+                                                       int(k_iters), float(kappa), int(audit_every),
+                                                       float(audit_tol)))
         self._warm_net = net  # keeps the network alive while attached
 
     def warm_stats(self) -> dict:

@@ -1,6 +1,6 @@
 """Learned warm start of the mixed-precision mEVP sub-cycle, through the C ABI.
 
-The plain sub-cycle (100 iterations) is the judge: a warm sub-cycle (network
+The plain sub-cycle (100 iterations) is the audit: a warm sub-cycle (network
 + K iterations) is compared with it from the same state, next to the cold
 sub-cycle with the same K iterations and no network.  The fallback (restore
 the state at the start of the sub-cycle, run the full count) must reproduce
@@ -152,35 +152,35 @@ def test_nonfinite_network_falls_back(trained):
     assert (st["accepted"], st["fallbacks"]) == (0, 2)
 
 
-def test_judged_updates_keep_the_plain_result(trained):
-    """judge_every = 1: every update runs warm and plain from the same start
+def test_audited_updates_keep_the_plain_result(trained):
+    """audit_every = 1: every update runs warm and plain from the same start
     and keeps the plain result (bitwise the plain update)."""
     net, kappa, _, _ = trained
     box = _box()
     a, b = _kernel(box), _kernel(box)
-    b.set_warm_start(net, K, kappa * 10.0, judge_every=1, judge_tol=1.0)
+    b.set_warm_start(net, K, kappa * 10.0, audit_every=1, audit_tol=1.0)
     _run(a, box, 3)
     _run(b, box, 3)
     for f in ("u", "v", "hice", "cice"):
         np.testing.assert_array_equal(a.getDG0Data(f), b.getDG0Data(f))
     st = b.warm_stats()
-    assert st["judged"] == 3 and st["judge_rejected"] == 0 and st["enabled"] == 1
-    assert 0 < st["last_judged_error"] < 1.0
+    assert st["audited"] == 3 and st["audit_rejected"] == 0 and st["enabled"] == 1
+    assert 0 < st["last_audit_error"] < 1.0
 
 
-def test_failed_judgement_disables_warm_start(trained):
-    """judge_tol = 0 fails the first judgement: the next updates fall back
-    (plain result) until the next judgement."""
+def test_failed_audit_disables_warm_start(trained):
+    """audit_tol = 0 fails the first audit: the next updates fall back
+    (plain result) until the next audit."""
     net, kappa, _, _ = trained
     box = _box()
     a, b = _kernel(box), _kernel(box)
-    b.set_warm_start(net, K, kappa * 10.0, judge_every=3, judge_tol=0.0)
+    b.set_warm_start(net, K, kappa * 10.0, audit_every=3, audit_tol=0.0)
     _run(a, box, 3)
     _run(b, box, 3)
     for f in ("u", "v", "hice", "cice"):
         np.testing.assert_array_equal(a.getDG0Data(f), b.getDG0Data(f))
     st = b.warm_stats()
-    assert (st["judged"], st["judge_rejected"], st["accepted"], st["fallbacks"], st["enabled"]) == (1, 1, 0, 2, 0)
+    assert (st["audited"], st["audit_rejected"], st["accepted"], st["fallbacks"], st["enabled"]) == (1, 1, 0, 2, 0)
 
 
 def test_detach_restores_plain_graph(trained):
