@@ -451,3 +451,34 @@ def test_sea_surface_height_gradient_matches_oracle(gpu, oracle, precision):
     o2 = _make(oracle.OracleKernel, box, 6, 0, **prm)
     _advance(o2, box, 3)
     assert np.abs(o2.getDG0Data("u") - o.getDG0Data("u")).max() > 1e-4
+
+
+
+@pytest.mark.parametrize("precision,alpha", [(0, 1500.0), (0, 300.0), (1, 300.0)])
+def test_full_size_512_within_oracle_sensitivity(gpu, oracle, precision, alpha):
+    """The 512 x 512 DG2 box test (1 km cells; the mixed-precision benchmark
+    grid), two full steps, FP64 or mixed precision, against the oracle on the
+    same inputs.  On 1 km cells both relaxations amplify rounding within two
+    steps (the oracle's own response to h x (1 + 1e-14) reaches ~1e-6 in u),
+    so the bar per field is 10x that response (h and A follow through
+    advection by the perturbed velocity); 1e-10 where the response stays
+    below 1e-11, and never below 1e-6 for the mixed-precision path."""
+    box = BoxTest(512)
+    prm = dict(alpha=alpha, beta=alpha, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, 6, None, precision=precision, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    o2 = oracle.OracleKernel(0, 6, **prm)
+    o2.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        o2.setData(name, arr * (1.0 + 1e-14) if name == "hice" else arr)
+    for k in (g, o, o2):
+        _advance(k, box, 2)
+    names = ["hice", "cice", "u", "v"]
+    worst = _compare(g, o, names, 6)
+    sens = _compare(o2, o, names, 6)
+    floor = 1e-6 if precision else TOL
+    print(f"512x512 precision {precision} alpha {alpha}: gpu vs oracle {worst}, oracle sensitivity {sens}")
+    for n in names:
+        bar = TOL if sens[n] < 1e-11 else 10.0 * sens[n]
+        assert worst[n] <= max(bar, floor), (n, worst, sens)
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
