@@ -60,14 +60,15 @@ ALPHA = BETA = 300.0
 NSTEPS = 100
 
 
-def bytes_per_element_iteration_stress(word: int = 8, spherical: bool = False) -> int:
+def bytes_per_element_iteration_stress(word: int = 8, spherical: bool = False, parallelogram: bool = False) -> int:
     """Algorithmic DRAM bytes of one launch of the element stress kernel, per
     element: the strain operators G_x, G_y and the divergence operators A_1,
-    A_2 (4 x 81 words), the pressure terms at the 9 Gauss points (FP64 P/alpha;
-    in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha)), the 18
-    divergence coefficients read and written, and the CG2 velocity counted
+    A_2 (4 x 81 words; on a parallelogram mesh the FP32 kernel reads 5 FP32
+    coefficients instead), the pressure terms at the 9 Gauss points (FP64
+    P/alpha; in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha)), the
+    18 divergence coefficients read and written, and the CG2 velocity counted
     once per node (about 4 nodes per element, u and v)."""
-    operators = (6 if spherical else 4) * 81 * word  # + G_m, A_3 on a sphere
+    operators = 5 * 4 if parallelogram else (6 if spherical else 4) * 81 * word  # + G_m, A_3 on a sphere
     pressure = 9 * 8 + (9 * 4 if word == 4 else 0)
     tdiv = 2 * 18 * word
     velocity = 4 * 2 * word
@@ -282,11 +283,13 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
     with CUDA events on the library's stream."""
     kms, kname = k.time_kernel(0, 50)
     nms, nname = k.time_kernel(1, 50)
-    bpe = bytes_per_element_iteration_stress(4 if prec else 8)
+    kind, mismatch = k.stress_variant()
+    affine = kind == "affine"
+    bpe = bytes_per_element_iteration_stress(4 if prec else 8, parallelogram=affine)
     achieved = N * bpe / (kms * 1e-3) / 1e9
     hbm, hbm_kind = measured_peaks()
     traffic = None
-    prof = ROOT / "profiles" / (f"kMevpStress32_box{nx}_fp32.md" if prec else f"kMevpStress_box{nx}_fp64.md")
+    prof = ROOT / "profiles" / (f"{kname}_box{nx}_fp32.md" if prec else f"kMevpStress_box{nx}_fp64.md")
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.startswith(f"traffic_bytes_per_launch_{nx}:"):
@@ -297,8 +300,13 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
             "kernel_timing": "CUDA events on the library's stream around 50 back-to-back launches of the kernel "
                              "on the workload's state, right after the timed steps"}
     if prec:
-        # both FP32 stress kernels (the library keeps the faster at initialise)
-        roof["stress_kernel_ms"] = {k.time_kernel(i, 50)[1]: k.time_kernel(i, 50)[0] for i in (3, 4)}
+        # every FP32 stress kernel on this mesh: the operator-streaming ones
+        # (global loads, TMA tiles) and, on a parallelogram mesh, the
+        # coefficient kernel with each FP64 viscosity form
+        names = {3: "global", 4: "tma", 5: "affine_rsqrt_f64", 6: "affine_newton_f64", 7: "affine_newton_f64_intcvt"}
+        roof["stress_kernel_ms"] = {names[i]: k.time_kernel(i, 50)[0] for i in ((3, 4, 5, 6, 7) if affine else (3, 4))}
+        roof["stress_kernel"] = kind
+        roof["parallelogram_mismatch"] = mismatch
     if prec == 0:
         fp64_tf, fp64_kind = fp64_peak_tflops(local)
         ach = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
@@ -436,19 +444,35 @@ def day_error(args, box, steps: int):
     """Velocity / thickness / concentration RMS after `steps` model steps: the
     headline precision path and the FP64 path with h scaled by (1 + 1e-14),
     both against the FP64 path."""
+    from nextsimdg_gb300._lib import NsdgError
     from nextsimdg_gb300.boxtest import step_forcing
     ks = {"fp64": make_kernel(box, 0), "fp64_h_times_1p1e-14": make_kernel(box, 0, scale_h=1 + 1e-14),
           "fp32": make_kernel(box, 1)}
+    # on 1 km cells with alpha = beta = 300 a trajectory can go unstable (the
+    # library flags non-finite velocities): such a run is reported with the
+    # 60-step window in which it was flagged, not measured
+    failed = {}
     for s in range(steps):
-        for k in ks.values():
-            step_forcing(k, box, s)
-            k.update(s * DT, DT)
-    r = {n: {f: k.getDG0Data(f) for f in ("u", "v", "hice", "cice")} for n, k in ks.items()}
-    ref = r["fp64"]
+        for n, k in ks.items():
+            if n not in failed:
+                step_forcing(k, box, s)
+                k.update(s * DT, DT)
+        if (s + 1) % 60 == 0 or s == steps - 1:
+            for n, k in ks.items():
+                if n not in failed:
+                    try:
+                        k.synchronize()
+                    except NsdgError:
+                        failed[n] = s + 1
+    r = {n: {f: k.getDG0Data(f) for f in ("u", "v", "hice", "cice")} for n, k in ks.items() if n not in failed}
     rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
     out = {"steps": steps, "simulated_hours": steps * DT / 3600.0}
     for n in ("fp32", "fp64_h_times_1p1e-14"):
-        x = r[n]
+        if n in failed or "fp64" in failed:
+            out[n] = {"non_finite_by_step": failed.get(n, failed.get("fp64")),
+                      "run": n if n in failed else "fp64"}
+            continue
+        x, ref = r[n], r["fp64"]
         out[n] = {"u_v_rms_m_per_s": rms(np.hypot(x["u"] - ref["u"], x["v"] - ref["v"])),
                   "h_rms_m": rms(x["hice"] - ref["hice"]), "A_rms": rms(x["cice"] - ref["cice"])}
     for k in ks.values():

@@ -156,9 +156,20 @@ int nsdg_kernel_mean_value(nsdg_kernel* k, const char* name, double* out);
 int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms);
 /* Times `reps` launches of one kernel of the step in isolation on the handle's
  * stream and returns the mean duration.  kernel_id: 0 = element stress kernel,
- * 1 = node momentum kernel, 2 = transport operator.  *name gets its name. */
+ * 1 = node momentum kernel, 2 = transport operator; for mixed-precision mEVP
+ * also 3 = stress kernel with operators by global loads, 4 = with operator
+ * tiles by TMA, and on parallelogram meshes 5, 6, 7 = the coefficient kernel
+ * with FP64 viscosity form 0, 1, 2 (see nsdg_selftest_viscosity).  *name gets
+ * its name. */
 int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms,
     const char** name);
+/* Which mixed-precision mEVP stress kernel the updates use: *kind 0 =
+ * operators by global loads, 1 = operator tiles by TMA, 2 = parallelogram
+ * coefficients (chosen by timing at initialise; NSDG_STRESS_KERNEL =
+ * global|tma|affine fixes it); *mismatch = the largest relative difference,
+ * in FP64, between the exact operators and those rebuilt from parallelogram
+ * coefficients (-1 when not evaluated, e.g. spherical or FP64 handles). */
+int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch);
 /* Kernel launches issued by one update (for gpu_launches accounting). */
 int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
 
@@ -308,6 +319,18 @@ int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
  * such wait on an mbarrier that nothing completes, with a limit of
  * limit_seconds (0 < limit <= 2), and reports *timed_out = 1 when the wait ran
  * out and the kernel returned as it must.  The GPU context stays usable. */
+/* Host only (no GPU): the largest relative FP64 difference between the exact
+ * mEVP stress operators of a Cartesian mesh (coords as for
+ * nsdg_kernel_initialise) and those rebuilt from parallelogram coefficients.
+ * Mixed-precision handles use the parallelogram stress kernel when it is at
+ * most 1e-9. */
+int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords, int dg_comp, double* mismatch);
+/* P / (8 alpha Delta), Delta = sqrt(inv + delta_min^2), for n host values by
+ * the three FP64 forms of the mixed-precision stress kernels: out[k n + i]
+ * for form k = 0 (CUDA's rsqrt(double)), 1 (one Newton-Raphson step in FP64
+ * from an FP32 rsqrtf seed), 2 (the same with float/double conversions on
+ * the integer pipe).  Inputs: inv >= 0, Pa >= 0. */
+int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
 
 /* ======================================================================== */

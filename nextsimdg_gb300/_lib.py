@@ -88,6 +88,7 @@ SIGNATURES = [
     ("nsdg_kernel_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
     ("nsdg_kernel_time_kernel", c_int, [c_void_p, c_int, c_int, POINTER(c_float), POINTER(c_char_p)]),
     ("nsdg_kernel_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
+    ("nsdg_kernel_stress_variant", c_int, [c_void_p, POINTER(c_int), POINTER(c_double)]),
     ("nsdg_transport_create", c_int, [c_int, c_size_t, c_size_t, c_void_p, c_void_p,
                                       POINTER(c_void_p), POINTER(c_size_t), c_void_p, c_size_t, c_int,
                                       POINTER(c_void_p)]),
@@ -126,6 +127,8 @@ SIGNATURES = [
     ("nsdg_kernel_set_warm_start", c_int, [c_void_p, c_void_p, c_int, c_double, c_int, c_double]),
     ("nsdg_kernel_warm_stats", c_int, [c_void_p, c_void_p]),
     ("nsdg_selftest_bounded_wait", c_int, [c_double, POINTER(c_int)]),
+    ("nsdg_selftest_viscosity", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
+    ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
 ]
 

@@ -121,12 +121,23 @@ struct nsdg_kernel {
     float2* invmHL = nullptr; // inverse lumped CG2 mass as {hi, lo} floats (mixed precision)
     BbmOps32 bbm32 {};        // FP32 BBM operators (mixed precision BBM)
     float *cellX8_32 = nullptr, *cellY8_32 = nullptr; // FP32 DG8 stress-transport operators
-    bool tmaStress = true; // which FP32 stress kernel the updates use (chosen by timing at initialise)
-    cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1)
+    // which FP32 stress kernel the updates use (chosen by timing at
+    // initialise): 0 operators by global loads, 1 operator tiles by TMA,
+    // 2 parallelogram coefficients (when the mesh allows it)
+    int stressKind = 1;
+    int viscMode = 2;                // FP64 viscosity form of the parallelogram kernel
+    float* affCoef = nullptr;        // [5][ld] parallelogram coefficients (null: not a parallelogram mesh)
+    size_t affLd = 0;
+    double affWorst = -1;            // largest relative mismatch of the rebuilt operators (FP64)
+    cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1,
+        int vm = -1)
     {
-        const bool tma = variant < 0 ? tmaStress : variant == 1;
-        return tma ? launchMevpStress32Tma(s, dm, maps32, st32.u, st32.v, Pg, hP32, tdiv32, mp, errWord)
-                   : launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, hP32, tdiv32, mp);
+        const int kind = variant < 0 ? stressKind : variant;
+        if (kind == 2 && affCoef)
+            return launchMevpStress32Affine(s, dm, affCoef, affLd, st32.u, st32.v, Pg, hP32, tdiv32, mp,
+                vm < 0 ? viscMode : vm);
+        return kind == 1 ? launchMevpStress32Tma(s, dm, maps32, st32.u, st32.v, Pg, hP32, tdiv32, mp, errWord)
+                         : launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, hP32, tdiv32, mp);
     }
     int chooseStress32();
     float* tdiv32 = nullptr;
@@ -556,6 +567,24 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             if (e == cudaSuccess)
                 e = makeStressMaps(dops32, &maps32);
         }
+        if (!mesh.spherical) {
+            // parallelogram meshes: 5 coefficients per element replace the
+            // operator block (the rebuilt operators must match the exact
+            // ones far below FP32 rounding)
+            AffineStressOps aff;
+            const size_t ld = ops32Ld(N);
+            if (buildAffineStressOps(mesh, ops, ld, 1e-9, aff)) {
+                affCoef = arena.take<float>(aff.coef.size());
+                if (!affCoef)
+                    e = cudaErrorMemoryAllocation;
+                else if (e == cudaSuccess)
+                    e = cudaMemcpy(affCoef, aff.coef.data(), aff.coef.size() * sizeof(float), cudaMemcpyHostToDevice);
+                if (e == cudaSuccess)
+                    e = uploadAffineReference(aff.ref);
+                affLd = ld;
+            }
+            affWorst = aff.worst;
+        }
         auto zf = [&](size_t n) {
             float* p = arena.take<float>(n);
             if (!p) { e = cudaErrorMemoryAllocation; return p; }
@@ -590,27 +619,38 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     return ok();
 }
 
-// Times the two FP32 stress kernels (operators through TMA into shared
-// memory, or read directly from global memory) on this mesh and keeps the
-// faster one: which wins depends on the grid size and the number of
-// resident blocks.  Both compute the same values.
+// Picks the FP32 stress kernel.  A parallelogram mesh takes the coefficient
+// kernel (5 coefficients instead of 324 operator entries per element; its
+// results differ from the others' by FP32 rounding only, and ensembles of
+// such members take it too, so a member's single run and its ensemble run
+// agree bit for bit).  Otherwise the two operator kernels (tiles through TMA
+// into shared memory, or direct global loads), which compute identical
+// values, are timed on this mesh and the faster is kept: which wins depends
+// on the grid size and the number of resident blocks.
 int nsdg_kernel::chooseStress32()
 {
-    // NSDG_STRESS_KERNEL=tma|global fixes the choice (for profilers, whose
-    // serialised launches make the timing below meaningless)
+    // NSDG_STRESS_KERNEL=global|tma|affine fixes the choice (for profilers,
+    // whose serialised launches make the timing below meaningless)
     if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
-        if (std::strcmp(env, "tma") == 0 || std::strcmp(env, "global") == 0) {
-            tmaStress = std::strcmp(env, "tma") == 0;
-            return NSDG_OK;
-        }
+        const char* names[3] = { "global", "tma", "affine" };
+        for (int i = 0; i < 3; ++i)
+            if (std::strcmp(env, names[i]) == 0 && (i < 2 || affCoef)) {
+                stressKind = i;
+                return NSDG_OK;
+            }
+    }
+    if (affCoef) {
+        stressKind = 2;
+        return NSDG_OK;
     }
     const MevpParams mp = mevpParams(120.0);
     cudaEvent_t a, b;
     if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
         return fail(NSDG_ERR_CUDA, "initialise: event create failed");
     float best[2] = { 0, 0 };
+    const int kinds = 2;
     cudaError_t e = cudaSuccess;
-    for (int variant = 0; variant < 2 && e == cudaSuccess; ++variant) {
+    for (int variant = 0; variant < kinds && e == cudaSuccess; ++variant) {
         e = launchStress32(stream, mp, derr, variant);
         if (e == cudaSuccess) e = cudaEventRecord(a, stream);
         for (int r = 0; r < 10 && e == cudaSuccess; ++r)
@@ -626,7 +666,10 @@ int nsdg_kernel::chooseStress32()
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("initialise: stress kernel timing: ") + cudaGetErrorString(e));
-    tmaStress = best[1] <= best[0];
+    stressKind = 0;
+    for (int variant = 1; variant < kinds; ++variant)
+        if (best[variant] <= best[stressKind])
+            stressKind = variant;
     return NSDG_OK;
 }
 
@@ -1599,22 +1642,26 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 3:
         case 4:
             return k->launchStress32(k->stream, mp, k->derr, kernel_id == 4 ? 1 : 0);
+        case 5:
+        case 6:
+        case 7:
+            return k->launchStress32(k->stream, mp, k->derr, 2, kernel_id - 5);
         default:
             return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
                 k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a, k->mixed() ? k->cellX32 : nullptr,
                 k->mixed() ? k->cellY32 : nullptr);
         }
     };
-    if (kernel_id < 0 || kernel_id > 4 || (kernel_id >= 3 && (bbm || !k->mixed())))
-        return k->fail(NSDG_ERR_BAD_ARG, "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP)");
+    if (kernel_id < 0 || kernel_id > 7 || (kernel_id >= 3 && (bbm || !k->mixed()))
+        || (kernel_id >= 5 && !k->affCoef))
+        return k->fail(NSDG_ERR_BAD_ARG,
+            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-7: on parallelogram meshes)");
+    static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
-        *name = kernel_id == 0 ? (bbm ? "kBbmStress"
-                                      : (k->mixed() ? (k->tmaStress ? "kMevpStress32Tma" : "kMevpStress32")
-                                                    : "kMevpStress"))
+        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : (k->mixed() ? kStress32Names[k->stressKind] : "kMevpStress"))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
             : kernel_id == 2 ? "kTransportStage"
-            : kernel_id == 3 ? "kMevpStress32"
-                             : "kMevpStress32Tma";
+            : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3];
     cudaEvent_t ea, eb;
     if (cudaEventCreate(&ea) != cudaSuccess || cudaEventCreate(&eb) != cudaSuccess)
         return k->fail(NSDG_ERR_CUDA, "time_kernel: event create failed");
@@ -1632,6 +1679,17 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
     if (e != cudaSuccess)
         return k->fail(NSDG_ERR_CUDA, std::string("time_kernel: ") + cudaGetErrorString(e));
     *mean_ms = ms / reps;
+    return k->ok();
+}
+
+int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch)
+{
+    if (!k || !kind || !mismatch)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "stress_variant: kernel not initialised");
+    *kind = k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP ? k->stressKind : -1;
+    *mismatch = k->affWorst;
     return k->ok();
 }
 
@@ -1822,7 +1880,17 @@ struct nsdg_ensemble {
     uint16_t* dTmaMap = nullptr;
     int* derr = nullptr;
     int stressBlocks = 0, nodeBlocks = 0, tmaBlocks = 0;
-    bool useTma = false; // element phase: TMA-staged batched kernel (else the tiled global-load one)
+    // element phase: 0 tiled global-load kernel, 1 TMA-staged, 2 parallelogram
+    // coefficients (every member a parallelogram mesh)
+    int elementKind = 0;
+    int viscMode = 2;
+    cudaError_t launchElements(cudaStream_t s, const EnsembleMember* table, const MevpParams& mp)
+    {
+        if (elementKind == 2)
+            return launchMevpStress32AffineBatched(s, table, dTmaMap, tmaBlocks, mp, viscMode);
+        return elementKind == 1 ? launchMevpStress32TmaBatched(s, table, dTmaMap, tmaBlocks, mp, derr)
+                                : launchMevpStress32Batched(s, table, dStressMap, stressBlocks, mp);
+    }
     std::vector<int> tileW;
     cudaGraphExec_t graph = nullptr;
     double graphDt = -1.0;
@@ -1864,6 +1932,8 @@ struct nsdg_ensemble {
         d.hP = k->hP32;
         d.tdiv = k->tdiv32;
         d.maps = k->maps32;
+        d.affCoef = k->affCoef;
+        d.affLd = k->affLd;
         d.tileW = tw;
         d.tileH = stressElementsPerBlock() / tw;
         d.tilesX = (d.nx + tw - 1) / tw;
@@ -2055,10 +2125,20 @@ int nsdg_ensemble::chooseElementKernel()
     cudaFree(dT);
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("ensemble: element kernel timing: ") + cudaGetErrorString(e));
-    useTma = ms[1] <= ms[0];
+    elementKind = ms[1] <= ms[0] ? 1 : 0;
+    // parallelogram members take the coefficient kernel (as their single
+    // runs do), when every member has coefficients
+    bool allAffine = true;
+    for (auto* k : members)
+        allAffine = allAffine && k->affCoef != nullptr;
+    if (allAffine) {
+        elementKind = 2;
+        viscMode = members[0]->viscMode;
+    }
     if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
-        if (std::strcmp(env, "tma") == 0) useTma = true;
-        if (std::strcmp(env, "global") == 0) useTma = false;
+        if (std::strcmp(env, "tma") == 0) elementKind = 1;
+        if (std::strcmp(env, "global") == 0) elementKind = 0;
+        if (std::strcmp(env, "affine") == 0 && allAffine) elementKind = 2;
     }
     return NSDG_OK;
 }
@@ -2088,8 +2168,7 @@ int nsdg_ensemble::ensureGraph(double dt)
         }
     }
     for (int it = 0; it < P.n_steps && st == NSDG_OK; ++it) {
-        e = useTma ? launchMevpStress32TmaBatched(stream, dMembers, dTmaMap, tmaBlocks, mp, derr)
-                   : launchMevpStress32Batched(stream, dMembers, dStressMap, stressBlocks, mp);
+        e = launchElements(stream, dMembers, mp);
         if (e == cudaSuccess)
             e = launchMevpMomentum32Batched(stream, dMembers, dNodeMap, nodeBlocks, mp, derr);
         if (e != cudaSuccess)
@@ -2255,8 +2334,8 @@ int nsdg_ensemble_tile(nsdg_ensemble* ens, int member, int* tile_w, int* tile_h)
 {
     if (!ens || !tile_w || !tile_h || member < 0 || member >= static_cast<int>(ens->members.size()))
         return NSDG_ERR_BAD_ARG;
-    if (ens->useTma) {
-        *tile_w = kTmaElems; // consecutive elements, operators staged by TMA
+    if (ens->elementKind != 0) {
+        *tile_w = kTmaElems; // consecutive elements (operators staged by TMA, or parallelogram coefficients)
         *tile_h = 1;
     } else {
         *tile_w = ens->tileW[member];
@@ -2276,6 +2355,59 @@ int nsdg_ensemble_launches_per_update(nsdg_ensemble* ens, int* launches)
     }
     *launches = ens->launches;
     return NSDG_OK;
+}
+
+int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords, int dg_comp, double* mismatch)
+{
+    if (!coords || !mismatch || nx < 1 || ny < 1 || (dg_comp != 1 && dg_comp != 3 && dg_comp != 6))
+        return NSDG_ERR_BAD_ARG;
+    HostMesh m;
+    m.nx = nx;
+    m.ny = ny;
+    const size_t nn = (nx + 1) * (ny + 1);
+    m.vx.resize(nn);
+    m.vy.resize(nn);
+    for (size_t i = 0; i < nn; ++i) {
+        m.vx[i] = coords[2 * i];
+        m.vy[i] = coords[2 * i + 1];
+        if (!std::isfinite(m.vx[i]) || !std::isfinite(m.vy[i]))
+            return NSDG_ERR_BAD_ARG;
+    }
+    m.ice.assign(nx * ny, 1);
+    ElementOps ops;
+    buildElementOps(m, dg_comp, false, ops);
+    AffineStressOps aff;
+    buildAffineStressOps(m, ops, m.nelements(), 0.0, aff);
+    *mismatch = aff.worst;
+    return NSDG_OK;
+}
+
+int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
+{
+    if (!inv || !Pa || !out || n == 0 || n > (size_t(1) << 26) || !(delta_min > 0.0))
+        return NSDG_ERR_BAD_ARG;
+    std::string m;
+    const int st = deviceCheck(m);
+    if (st != NSDG_OK)
+        return st;
+    float *dInv = nullptr, *dOut = nullptr;
+    double* dPa = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&dInv, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dPa, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dOut, 3 * n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dInv, inv, n * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dPa, Pa, n * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launchViscositySelfTest(s, n, dInv, dPa, delta_min, dOut);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dOut, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (void* p : { static_cast<void*>(dInv), static_cast<void*>(dPa), static_cast<void*>(dOut) })
+        if (p)
+            cudaFree(p);
+    if (s)
+        cudaStreamDestroy(s);
+    return e == cudaSuccess ? NSDG_OK : NSDG_ERR_CUDA;
 }
 
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out)

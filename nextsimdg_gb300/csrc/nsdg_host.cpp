@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <thread>
 
 namespace nsdg {
@@ -433,6 +434,62 @@ void transportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads)
 }
 
 } // namespace
+
+bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, double tol,
+    AffineStressOps& out, unsigned threads)
+{
+    const size_t N = m.nelements();
+    if (m.spherical || N == 0 || ops.gx.size() != 81 * N || ld < N)
+        return false;
+    // the unit-square operators: one element with vertices (0,0) (1,0) (0,1) (1,1)
+    HostMesh u;
+    u.nx = u.ny = 1;
+    u.vx = { 0.0, 1.0, 0.0, 1.0 };
+    u.vy = { 0.0, 0.0, 1.0, 1.0 };
+    u.ice = { 1 };
+    ElementOps uo;
+    buildElementOps(u, ops.dg, false, uo, 1);
+    for (int r = 0; r < 81; ++r) {
+        out.ref[0][r] = uo.gx[r];
+        out.ref[1][r] = uo.gy[r];
+        out.ref[2][r] = uo.a1[r];
+        out.ref[3][r] = uo.a2[r];
+    }
+    out.ld = ld;
+    out.coef.assign(5 * ld, 0.f);
+    std::mutex mu;
+    out.worst = 0;
+    parallelFor(N, threads, [&](size_t lo, size_t hi) {
+        double worst = 0;
+        Geom g;
+        for (size_t e = lo; e < hi; ++e) {
+            geometry(m, e, 3, g);
+            const int qc = 4; // the element centre
+            const double J = g.J[qc];
+            const double c[5] = { g.deta[1][qc], -g.dxi[1][qc], -g.deta[0][qc], g.dxi[0][qc], 1.0 / J };
+            const std::vector<double>* exact[4] = { &ops.gx, &ops.gy, &ops.a1, &ops.a2 };
+            for (int b = 0; b < 4; ++b) {
+                const double s = b < 2 ? c[4] : 1.0;
+                const double k0 = (b % 2 == 0) ? c[0] : c[2], k1 = (b % 2 == 0) ? c[1] : c[3];
+                const int r0 = b < 2 ? 0 : 2;
+                double mx = 0, diff = 0;
+                for (int r = 0; r < 81; ++r) {
+                    const double x = (*exact[b])[size_t(r) * N + e];
+                    const double y = s * (k0 * out.ref[r0][r] + k1 * out.ref[r0 + 1][r]);
+                    mx = std::max(mx, std::fabs(x));
+                    diff = std::max(diff, std::fabs(x - y));
+                }
+                if (mx > 0)
+                    worst = std::max(worst, diff / mx);
+            }
+            for (int k = 0; k < 5; ++k)
+                out.coef[k * ld + e] = static_cast<float>(c[k]);
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        out.worst = std::max(out.worst, worst);
+    });
+    return out.worst <= tol;
+}
 
 void buildTransportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads)
 {

@@ -117,6 +117,30 @@ struct ElementOps {
 void buildElementOps(const HostMesh& m, int dg, bool stressTransport, ElementOps& ops,
     unsigned threads = 0);
 
+// Parallelogram (affine) elements.  When every element is a parallelogram,
+// its Jacobian is constant and the mEVP stress operators are fixed linear
+// combinations of the unit-square ones: with (x_xi, y_xi, x_eta, y_eta) the
+// Jacobian entries, J its determinant and
+//   c = (y_eta, -y_xi, -x_eta, x_xi, 1/J),
+//   G_x = c4 (c0 G_xi + c1 G_eta),   G_y = c4 (c2 G_xi + c3 G_eta),
+//   A_1 = c0 A_xi + c1 A_eta,        A_2 = c2 A_xi + c3 A_eta,
+// because the transformed gradients are c0 d_xi + c1 d_eta (times 1/J), the
+// mass matrix is J M_ref and iMJwPSI does not depend on J
+// (ParametricMap.cpp:232-263, ParametricTools.hpp:109-153).  The mixed
+// precision path then streams 5 coefficients per element instead of 324
+// operator entries.
+struct AffineStressOps {
+    double ref[4][81] {};          // G_xi [q][j], G_eta [q][j], A_xi [j][q], A_eta [j][q]
+    std::vector<float> coef;       // [5][ld]: c0 .. c4 per element (ld >= N, zero padded)
+    size_t ld = 0;
+    double worst = 0;              // max over elements of |rebuilt - exact| / max |exact| (FP64)
+};
+// Fills `out` and returns true if the mesh is Cartesian and every element's
+// operators, rebuilt from its coefficients in FP64, match `ops` (from
+// buildElementOps) within `tol` relative to each operator's largest entry.
+bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, double tol,
+    AffineStressOps& out, unsigned threads = 0);
+
 // Builds only the transport operators (cellX/Y, minv, jwA, jw3) for a DG
 // degree (used by the stand-alone transport handle).
 void buildTransportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads = 0);

@@ -971,7 +971,7 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMe
     __syncthreads();
     if (!active)
         return;
-    const double keep = 1.0 - 1.0 / p.alpha;
+    const double keep = p.keepd;
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj) {
         const int j = 3 * part + jj;
@@ -1097,7 +1097,8 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
 {
     if (active) {
         const size_t s2 = 2 * size_t(nx) + 1;
-        const size_t ix = e % nx, iy = e / nx;
+        const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx);
+        const size_t iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
         const size_t base = 2 * s2 * iy + 2 * ix;
         float ul[9], vl[9];
 #pragma unroll
@@ -1106,7 +1107,7 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
             ul[j] = u[nd];
             vl[j] = v[nd];
         }
-        const double dmin2 = p.DeltaMin * p.DeltaMin;
+        const double dmin = p.DeltaMin; // Delta^2 = inv + DeltaMin^2 with one rounding (FMA)
 #pragma unroll
         for (int qq = 0; qq < 3; ++qq) {
             const int q = 3 * part + qq;
@@ -1133,7 +1134,7 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
             }
             const float sxy = exv + eyu;
             const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
-            const float z8 = static_cast<float>(Pg[q * N + e] * rsqrt(static_cast<double>(inv) + dmin2));
+            const float z8 = static_cast<float>(Pg[q * N + e] * rsqrt(fma(dmin, dmin, static_cast<double>(inv))));
             const float hP = hPg[q * N + e];
             fs[0][q][le] = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP);
             fs[1][q][le] = z8 * sxy;
@@ -1143,7 +1144,7 @@ __device__ __forceinline__ void mevpStress32Element(int nx, size_t N, bool activ
     __syncthreads();
     if (!active)
         return;
-    const float keep = static_cast<float>(1.0 - 1.0 / p.alpha);
+    const float keep = p.keep;
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj) {
         const int j = 3 * part + jj;
@@ -1295,7 +1296,8 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (active) {
         const size_t s2 = 2 * size_t(nx) + 1;
-        const size_t ix = e % nx, iy = e / nx;
+        const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx);
+        const size_t iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
         const size_t base = 2 * s2 * iy + 2 * ix;
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
@@ -1307,7 +1309,7 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
     __syncthreads(); // the barriers are initialised before anyone polls them
     bool ok = mbarWaitBounded(&bars[0], 0);
     if (ok && active) {
-        const double dmin2 = p.DeltaMin * p.DeltaMin;
+        const double dmin = p.DeltaMin; // Delta^2 = inv + DeltaMin^2 with one rounding (FMA)
 #pragma unroll
         for (int qq = 0; qq < 3; ++qq) {
             const int q = 3 * part + qq;
@@ -1334,7 +1336,7 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
             }
             const float sxy = exv + eyu;
             const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
-            const float z8 = static_cast<float>(Pa[qq] * rsqrt(static_cast<double>(inv) + dmin2));
+            const float z8 = static_cast<float>(Pa[qq] * rsqrt(fma(dmin, dmin, static_cast<double>(inv))));
             fs[0][q][le] = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP[qq]);
             fs[1][q][le] = z8 * sxy;
             fs[2][q][le] = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP[qq]);
@@ -1366,7 +1368,7 @@ __device__ __forceinline__ void stress32TmaBlock(const CUtensorMap* mapG, const 
     }
     if (!active)
         return;
-    const float keep = static_cast<float>(1.0 - 1.0 / p.alpha);
+    const float keep = p.keep;
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj) {
         const int j = 3 * part + jj;
@@ -1399,13 +1401,226 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32Tma(con
     stress32TmaBlock<SPH>(&mapG, &mapA, m.nx, m.N, m.ice, u, v, Pg, hPg, tdiv, p, err, blockIdx.x * kTmaElems, smem);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 stress kernel for parallelogram meshes
+// ---------------------------------------------------------------------------
+// On a mesh of parallelograms every element's operators are combinations of
+// the unit-square ones with 5 coefficients per element (c0..c3 the Jacobian
+// entries, c4 = 1/J; the host derives them and checks the rebuilt operators
+// against the exact ones).  The unit-square operators sit in constant memory
+// and each warp handles a fixed third of the Gauss points and nodes, so their
+// entries are compile-time constant-bank operands; per element-iteration the
+// kernel streams 5 coefficients, P/(8 alpha), P/(2 alpha), the divergence and
+// the velocities instead of 324 operator entries.
+namespace {
+constexpr int kAffElems = 32;
+__constant__ float cAff[4][81]; // G_xi [q][j], G_eta [q][j], A_xi [j][q], A_eta [j][q]
+
+// float <-> double by exponent rebiasing on the integer pipe (GB300 executes
+// FP64 at about 1/60 of its FP32 rate): exact for positive normal
+// floats; a value below the smallest normal float maps to zero.
+__device__ __forceinline__ double widenPos(float f)
+{
+    const unsigned long long b = (static_cast<unsigned long long>(__float_as_uint(f)) << 29) + (896ull << 52);
+    return __longlong_as_double(static_cast<long long>(b));
+}
+// f / 2 for a positive normal float f (exact)
+__device__ __forceinline__ double widenHalfPos(float f)
+{
+    const unsigned long long b = (static_cast<unsigned long long>(__float_as_uint(f)) << 29) + (895ull << 52);
+    return __longlong_as_double(static_cast<long long>(b));
+}
+__device__ __forceinline__ double widenNonneg(float f)
+{
+    return __float_as_uint(f) >= 0x00800000u ? widenPos(f) : 0.0;
+}
+// d >= 0 and below 2^128: nearest float (ties away from zero); 0 below the
+// smallest normal float
+__device__ __forceinline__ float narrowPos(double d)
+{
+    const long long b = __double_as_longlong(d);
+    const long long r = (b - (896ll << 52) + (1ll << 28)) >> 29;
+    return b >= (897ll << 52) ? __uint_as_float(static_cast<unsigned>(r)) : 0.f;
+}
+} // namespace
+
+// P/(8 alpha Delta) with Delta = sqrt(t), t = inv + DeltaMin^2 formed in FP64
+// with one rounding (FMA), evaluated in FP64.  VM 0: CUDA's rsqrt(double).
+// VM 1 and 2: one Newton-Raphson step for the reciprocal square root,
+// y1 = y0 + y0 (1 - t y0^2) / 2, in FP64 from the FP32 seed
+// y0 = rsqrtf(inv + DeltaMin^2) (relative error of y1: 1.5 e0^2 + FP64
+// rounding, e0 <= 2^-21 for the seed and its FP32 argument, i.e. below
+// 1e-12); VM 2 converts between float and double on the integer pipe (y0/2
+// by the exponent bias).  Five FP64 instructions per Gauss point in VM 2.
+template <int VM>
+__device__ __forceinline__ float viscosity8(float inv, double Pa, double dmin, float dmin2f)
+{
+    const double td = VM == 2 ? widenNonneg(inv) : static_cast<double>(inv);
+    const double t = fma(dmin, dmin, td);
+    if constexpr (VM == 0) {
+        return static_cast<float>(Pa * rsqrt(t));
+    } else {
+        const float y0 = rsqrtf(inv + dmin2f);
+        const double yd = VM == 1 ? static_cast<double>(y0) : widenPos(y0);
+        const double yh = VM == 1 ? 0.5 * yd : widenHalfPos(y0);
+        const double h = t * yd;
+        const double e2 = fma(-h, yh, 0.5); // (1 - t y0^2) / 2
+        const double z = Pa * yd;
+        const double z8 = fma(z, e2, z);
+        return VM == 1 ? static_cast<float>(z8) : narrowPos(z8);
+    }
+}
+
+template <int PART, int VM>
+__device__ __forceinline__ void affineStrain(const float (&ul)[9], const float (&vl)[9], const float (&c)[5],
+    const double (&Pa)[3], const float (&hP)[3], double dmin, float dmin2f,
+    float (*fs)[9][kAffElems], int le)
+{
+#pragma unroll
+    for (int qq = 0; qq < 3; ++qq) {
+        constexpr int q0 = 3 * PART;
+        const int q = q0 + qq;
+        float ux = 0.f, ue = 0.f, vx = 0.f, ve = 0.f;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const float gx = cAff[0][q * 9 + j], ge = cAff[1][q * 9 + j];
+            ux = fmaf(gx, ul[j], ux);
+            ue = fmaf(ge, ul[j], ue);
+            vx = fmaf(gx, vl[j], vx);
+            ve = fmaf(ge, vl[j], ve);
+        }
+        const float ex = c[4] * fmaf(c[0], ux, c[1] * ue);  // G_x u
+        const float ey = c[4] * fmaf(c[2], vx, c[3] * ve);  // G_y v
+        const float exv = c[4] * fmaf(c[0], vx, c[1] * ve); // G_x v
+        const float eyu = c[4] * fmaf(c[2], ux, c[3] * ue); // G_y u
+        const float sxy = exv + eyu;
+        const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
+        const float z8 = viscosity8<VM>(inv, Pa[qq], dmin, dmin2f);
+        const float f11 = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP[qq]);
+        const float f12 = z8 * sxy;
+        const float f22 = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP[qq]);
+        // the Gauss-point weights of A_xi and A_eta in A_1 f11 + A_2 f12 and
+        // A_1 f12 + A_2 f22
+        fs[0][q][le] = fmaf(c[0], f11, c[2] * f12);
+        fs[1][q][le] = fmaf(c[1], f11, c[3] * f12);
+        fs[2][q][le] = fmaf(c[0], f12, c[2] * f22);
+        fs[3][q][le] = fmaf(c[1], f12, c[3] * f22);
+    }
+}
+
+template <int PART>
+__device__ __forceinline__ void affineDivergence(float (*fs)[9][kAffElems], int le, size_t e, size_t N,
+    float* __restrict__ tdiv, float keep)
+{
+    float w[4][9];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int q = 0; q < 9; ++q)
+            w[k][q] = fs[k][q][le];
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) {
+        const int j = 3 * PART + jj;
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float axi = cAff[2][j * 9 + q], aet = cAff[3][j * 9 + q];
+            ax = fmaf(axi, w[0][q], fmaf(aet, w[1][q], ax));
+            ay = fmaf(axi, w[2][q], fmaf(aet, w[3][q], ay));
+        }
+        tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
+        tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
+    }
+}
+
+// One block of the parallelogram stress kernel: elements x0 .. x0+31 of a
+// grid (shared by the single-grid and the batched ensemble kernels).
+template <int VM>
+__device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __restrict__ ice,
+    const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
+    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, const MevpParams& p,
+    size_t x0, float (*fs)[9][kAffElems])
+{
+    const int le = threadIdx.x % kAffElems;
+    const int part = threadIdx.x / kAffElems; // one warp per third of the Gauss points / nodes
+    const size_t e = x0 + le;
+    const bool active = e < N && ice[e];
+    // step constants first: a programmatic dependent launch overlaps them
+    // with the previous kernel's tail
+    float c[5], ul[9], vl[9], hP[3];
+    double Pa[3];
+    if (active) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            c[k] = coef[k * ld + e];
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+            Pa[qq] = Pg[(3 * part + qq) * N + e];
+            hP[qq] = hPg[(3 * part + qq) * N + e];
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (active) {
+        const size_t s2 = 2 * size_t(nx) + 1;
+        const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx);
+        const size_t iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
+        const size_t base = 2 * s2 * iy + 2 * ix;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const size_t nd = base + (j % 3) + (j / 3) * s2;
+            ul[j] = u[nd];
+            vl[j] = v[nd];
+        }
+        const double dmin = p.DeltaMin;
+        const float dmin2f = p.dmin2f;
+        switch (part) {
+        case 0: affineStrain<0, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
+        case 1: affineStrain<1, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
+        default: affineStrain<2, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
+        }
+    }
+    __syncthreads();
+    if (!active)
+        return;
+    const float keep = p.keep;
+    switch (part) {
+    case 0: affineDivergence<0>(fs, le, e, N, tdiv, keep); break;
+    case 1: affineDivergence<1>(fs, le, e, N, tdiv, keep); break;
+    default: affineDivergence<2>(fs, le, e, N, tdiv, keep); break;
+    }
+}
+
+template <int VM>
+__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32Affine(DevMesh m,
+    const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
+    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p)
+{
+    __shared__ float fs[4][9][kAffElems];
+    affineBlock<VM>(m.nx, m.N, m.ice, coef, ld, u, v, Pg, hPg, tdiv, p, blockIdx.x * size_t(kAffElems), fs);
+}
+
+// Self-test of the FP64 viscosity forms: out[3 n] = P/(8 alpha Delta) for
+// every VM (0, 1, 2) at each (inv, Pa).
+__global__ void kViscositySelfTest(size_t n, const float* __restrict__ inv, const double* __restrict__ Pa,
+    double dmin, float* __restrict__ out)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const float dmin2f = static_cast<float>(dmin * dmin);
+    out[i] = viscosity8<0>(inv[i], Pa[i], dmin, dmin2f);
+    out[n + i] = viscosity8<1>(inv[i], Pa[i], dmin, dmin2f);
+    out[2 * n + i] = viscosity8<2>(inv[i], Pa[i], dmin, dmin2f);
+}
+
 // Body of the mixed-precision node kernel for CG2 node i.
 __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, size_t i, const uint8_t* __restrict__ cg2Dir,
     const float2* __restrict__ invmHL, const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p,
     int* __restrict__ err)
 {
-    const int s2 = 2 * nx + 1;
-    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    // 32-bit index arithmetic (node counts stay far below 2^31)
+    const unsigned s2 = 2u * static_cast<unsigned>(nx) + 1u;
+    const int i2 = static_cast<int>(static_cast<unsigned>(i) % s2), j2 = static_cast<int>(static_cast<unsigned>(i) / s2);
     const bool dir = cg2Dir[i] != 0;
     // per-step constants first (a programmatic dependent launch overlaps
     // them with the stress kernel's tail), then the wait for its results
@@ -1440,8 +1655,7 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     const float u = st.u[i], v = st.v[i];
     const float uOcnRel = uo - u, vOcnRel = v - vo;
     const float absocn = sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
-    const float Fo = static_cast<float>(p.F_ocean);
-    const float focn = Fo * absocn;
+    const float focn = p.F_oceanf * absocn;
     const float rden = 1.0f / (c1b + A * focn);
     const float Afocn = A * focn;
     // c1 (beta u + u0) + A (fau + focn uo) - rhfc u - gu + mx, with the
@@ -1512,6 +1726,16 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32TmaBatc
     const int x0 = (static_cast<int>(blockIdx.x) - M.tmaBlock0) * kTmaElems;
     stress32TmaBlock<false>(&M.maps.g, &M.maps.a, M.nx, M.N, M.ice, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, err, x0,
         smem);
+}
+
+template <int VM>
+__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32AffineBatched(
+    const EnsembleMember* __restrict__ members, const uint16_t* __restrict__ blockMember, MevpParams p)
+{
+    __shared__ float fs[4][9][kAffElems];
+    const EnsembleMember& M = members[blockMember[blockIdx.x]];
+    const size_t x0 = size_t(static_cast<int>(blockIdx.x) - M.tmaBlock0) * kAffElems;
+    affineBlock<VM>(M.nx, M.N, M.ice, M.affCoef, M.affLd, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, x0, fs);
 }
 
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
@@ -2029,8 +2253,9 @@ cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, con
 }
 
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
-    const double* v, const double* Pg, double* tdiv, const MevpParams& p)
+    const double* v, const double* Pg, double* tdiv, const MevpParams& pIn)
 {
+    const MevpParams p = withDerived(pIn);
     if (o.gm)
         kMevpStress<true><<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, tdiv, p);
     else
@@ -2105,8 +2330,9 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
 }
 
 cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
-    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err)
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& pIn, int* err)
 {
+    const MevpParams p = withDerived(pIn);
     cudaLaunchConfig_t cfg {};
     cfg.gridDim = dim3(blocksFor(m.N, kTmaElems));
     cfg.blockDim = dim3(kTmaElems * kStressParts);
@@ -2122,15 +2348,53 @@ cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const Stress
     return cudaLaunchKernelEx(&cfg, kMevpStress32Tma<false>, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
 }
 
-cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
-    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p)
+cudaError_t uploadAffineReference(const double ref[4][81])
 {
+    float h[4][81];
+    for (int b = 0; b < 4; ++b)
+        for (int r = 0; r < 81; ++r)
+            h[b][r] = static_cast<float>(ref[b][r]);
+    return cudaMemcpyToSymbol(cAff, h, sizeof(h));
+}
+
+cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& pIn, int viscosityMode)
+{
+    const MevpParams p = withDerived(pIn);
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocksFor(m.N, kAffElems));
+    cfg.blockDim = dim3(kAffElems * kStressParts);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    switch (viscosityMode) {
+    case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<0>, m, coef, ld, u, v, Pg, hP, tdiv, p);
+    case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<1>, m, coef, ld, u, v, Pg, hP, tdiv, p);
+    default: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<2>, m, coef, ld, u, v, Pg, hP, tdiv, p);
+    }
+}
+
+cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
+    float* out)
+{
+    kViscositySelfTest<<<blocksFor(n), kBlock, 0, s>>>(n, inv, Pa, dmin, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& pIn)
+{
+    const MevpParams p = withDerived(pIn);
     kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, hP, tdiv, p);
     return cudaGetLastError();
 }
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2* invmHL, const MevpNodeState32& st,
-    const float* tdiv, const MevpParams& p, int* err)
+    const float* tdiv, const MevpParams& pIn, int* err)
 {
+    const MevpParams p = withDerived(pIn);
     cudaLaunchConfig_t cfg {};
     cfg.gridDim = dim3(blocksFor(m.Ncg));
     cfg.blockDim = dim3(kBlock);
@@ -2143,14 +2407,16 @@ cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2*
     return cudaLaunchKernelEx(&cfg, kMevpMomentum32, m, invmHL, st, tdiv, p, err);
 }
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
-    int blocks, const MevpParams& p)
+    int blocks, const MevpParams& pIn)
 {
+    const MevpParams p = withDerived(pIn);
     kMevpStress32Batched<<<blocks, kStressElems * kStressParts, 0, s>>>(members, blockMember, p);
     return cudaGetLastError();
 }
 cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
-    int blocks, const MevpParams& p, int* err)
+    int blocks, const MevpParams& pIn, int* err)
 {
+    const MevpParams p = withDerived(pIn);
     cudaLaunchConfig_t cfg {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(kBlock);
@@ -2163,8 +2429,9 @@ cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* me
     return cudaLaunchKernelEx(&cfg, kMevpMomentum32Batched, members, blockMember, p, err);
 }
 cudaError_t launchMevpStress32TmaBatched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
-    int blocks, const MevpParams& p, int* err)
+    int blocks, const MevpParams& pIn, int* err)
 {
+    const MevpParams p = withDerived(pIn);
     cudaLaunchConfig_t cfg {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(kTmaElems * kStressParts);
@@ -2176,6 +2443,26 @@ cudaError_t launchMevpStress32TmaBatched(cudaStream_t s, const EnsembleMember* m
     cfg.attrs = at;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kMevpStress32TmaBatched, members, blockMember, p, err);
+}
+cudaError_t launchMevpStress32AffineBatched(cudaStream_t s, const EnsembleMember* members,
+    const uint16_t* blockMember, int blocks, const MevpParams& pIn, int viscosityMode)
+{
+    const MevpParams p = withDerived(pIn);
+    static_assert(kAffElems == kTmaElems, "the parallelogram and TMA kernels share the block map");
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kAffElems * kStressParts);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    switch (viscosityMode) {
+    case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<0>, members, blockMember, p);
+    case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<1>, members, blockMember, p);
+    default: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<2>, members, blockMember, p);
+    }
 }
 int stressElementsPerBlock() { return kStressElems; }
 int nodesPerBlock() { return kBlock; }

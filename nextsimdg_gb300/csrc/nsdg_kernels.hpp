@@ -137,7 +137,20 @@ struct MevpNodeState {
 };
 struct MevpParams {
     double rho_ice, F_atm, F_ocean, fc, gravity, Pstar, DeltaMin, alpha, beta, dt;
+    // derived on the host by withDerived() in every stress launcher, so that
+    // no thread spends FP64 instructions (about 1/60 of the FP32 rate on
+    // GB300) on a division or a square of the parameters
+    double keepd = 0;                          // 1 - 1/alpha
+    float keep = 0, dmin2f = 0, F_oceanf = 0;  // FP32 copies (dmin2f: DeltaMin^2)
 };
+inline MevpParams withDerived(MevpParams p)
+{
+    p.keepd = 1.0 - 1.0 / p.alpha;
+    p.keep = static_cast<float>(p.keepd);
+    p.dmin2f = static_cast<float>(p.DeltaMin * p.DeltaMin);
+    p.F_oceanf = static_cast<float>(p.F_ocean);
+    return p;
+}
 cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st,
     const MevpParams& p);
 // P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298):
@@ -206,6 +219,18 @@ struct MevpNodeState32 {
 // after launchMevpPrepNodes: FP32 copies of the per-step node constants
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
     const MevpNodeState32& st32, double beta);
+// kMevpStress32 for parallelogram meshes: the unit-square operators
+// (G_xi, G_eta [q][j], A_xi, A_eta [j][q]) in constant memory, uploaded once
+// per device (they depend only on the basis), and 5 coefficients per element
+// ([5][ld]).  viscosityMode selects the FP64 evaluation of P/(8 alpha Delta):
+// 0 CUDA's rsqrt(double), 1 a Newton step from an FP32 seed, 2 the same with
+// float/double conversions on the integer pipe.
+cudaError_t uploadAffineReference(const double ref[4][81]);
+cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
+    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int viscosityMode);
+// out[k n + i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode k = 0, 1, 2.
+cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
+    float* out);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
 // invmHL: the FP64 inverse lumped mass as float2 {hi, lo}, hi + lo = 1/m to 48 bits
@@ -226,8 +251,10 @@ struct EnsembleMember {
     float* tdiv;
     int tileW, tileH, tilesX;
     int stressBlock0, nodeBlock0;
-    int tmaBlock0;   // first block of this member in the TMA-staged batched launch (Cartesian members)
+    int tmaBlock0;   // first block of this member in the TMA-staged / parallelogram batched launch
     StressMaps maps; // the member's tensor maps (64-byte aligned inside the device table)
+    const float* affCoef; // [5][affLd] parallelogram coefficients (null: not a parallelogram mesh)
+    size_t affLd;
 };
 // One launch each for the element and the node phase of every member.
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
@@ -238,6 +265,10 @@ cudaError_t launchMevpMomentum32Batched(cudaStream_t s, const EnsembleMember* me
 // kTmaElems consecutive elements, tensor maps read from the member table.
 cudaError_t launchMevpStress32TmaBatched(cudaStream_t s, const EnsembleMember* members,
     const uint16_t* blockMember, int blocks, const MevpParams& p, int* err);
+// The element phase of every member with the parallelogram kernel (every
+// member must have coefficients); blocks as for the TMA-staged launch.
+cudaError_t launchMevpStress32AffineBatched(cudaStream_t s, const EnsembleMember* members,
+    const uint16_t* blockMember, int blocks, const MevpParams& p, int viscosityMode);
 int stressElementsPerBlock();
 int nodesPerBlock();
 

@@ -52,6 +52,38 @@ def _ptr(a: np.ndarray) -> c_void_p:
     return a.ctypes.data_as(c_void_p)
 
 
+def parallelogram_mismatch(coords, nx: int, ny: int, dg_comp: int = 6) -> float:
+    """Host only: the largest relative FP64 difference between a Cartesian
+    mesh's exact mEVP stress operators and those rebuilt from parallelogram
+    coefficients (mixed-precision handles take the parallelogram kernel when
+    it is at most 1e-9)."""
+    lib = _lib.load()
+    c = _f64(coords)
+    if c.size != 2 * (nx + 1) * (ny + 1):
+        raise ValueError("coords must hold (nx+1)(ny+1) vertices x 2")
+    out = c_double()
+    st = lib.nsdg_mesh_parallelogram_mismatch(nx, ny, _ptr(c), dg_comp, byref(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "parallelogram_mismatch failed")
+    return out.value
+
+
+def selftest_viscosity(inv, pa, delta_min: float) -> np.ndarray:
+    """P/(8 alpha Delta) of each (inv, Pa) by the three FP64 forms of the
+    mixed-precision stress kernels, shape (3, n) float32 (see
+    nsdg_selftest_viscosity)."""
+    lib = _lib.load()
+    inv = np.ascontiguousarray(inv, dtype=np.float32)
+    pa = np.ascontiguousarray(pa, dtype=np.float64)
+    if inv.shape != pa.shape or inv.ndim != 1:
+        raise ValueError("inv and pa must be 1-D arrays of the same length")
+    out = np.empty(3 * inv.size, dtype=np.float32)
+    st = lib.nsdg_selftest_viscosity(inv.size, _ptr(inv), _ptr(pa), float(delta_min), _ptr(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "selftest_viscosity failed")
+    return out.reshape(3, inv.size)
+
+
 class _KernelBase:
     rheology = _lib.RHEOLOGY_MEVP
 
@@ -181,6 +213,17 @@ class _KernelBase:
         n = c_int()
         self._check(self._l.nsdg_kernel_launches_per_update(self._h, byref(n)))
         return n.value
+
+    STRESS_KERNELS = ("global", "tma", "affine")
+
+    def stress_variant(self):
+        """(kind, mismatch): the mixed-precision mEVP stress kernel in use
+        ("global", "tma", "affine"; None for other handles) and the largest
+        relative FP64 mismatch of operators rebuilt from parallelogram
+        coefficients (-1 when not evaluated)."""
+        kind, mism = c_int(), c_double()
+        self._check(self._l.nsdg_kernel_stress_variant(self._h, byref(kind), byref(mism)))
+        return (self.STRESS_KERNELS[kind.value] if kind.value >= 0 else None), mism.value
 
     # -- learned warm start (mEVP, mixed precision) ------------------------------
     def warm_sample(self, tst, dt, k_iters: int, net, slot: int) -> float:

@@ -4,6 +4,7 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from nextsimdg_gb300 import _lib
@@ -72,3 +73,26 @@ def test_python_mirror_raises(nsdg_lib):
     with pytest.raises(NsdgError):
         k.update(0.0, 120.0)
     k.close()
+
+
+def test_parallelogram_mismatch_on_the_host(nsdg_lib):
+    """Host only: operators rebuilt from parallelogram coefficients match the
+    exact ones to FP64 rounding on box and sheared meshes, and not on a
+    distorted mesh (which keeps the operator-streaming kernels)."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    from nextsimdg_gb300.dynamics import NsdgError, parallelogram_mismatch
+    for n in (8, 33):
+        b = BoxTest(n, n + 3)
+        assert parallelogram_mismatch(b.coords(), n, n + 3) < 1e-12
+    n = 12
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1))
+    sheared = np.stack([(1000.0 * i + 300.0 * j).ravel(), (-200.0 * i + 900.0 * j).ravel()], axis=1)
+    for dg in (1, 3, 6):
+        assert parallelogram_mismatch(sheared, n, n, dg) < 1e-12
+    rng = np.random.default_rng(4)
+    distorted = sheared + rng.normal(0.0, 30.0, sheared.shape)
+    assert parallelogram_mismatch(distorted, n, n) > 1e-3
+    with pytest.raises(ValueError):
+        parallelogram_mismatch(sheared[:-1], n, n)
+    with pytest.raises(NsdgError):
+        parallelogram_mismatch(sheared, n, n, 2)

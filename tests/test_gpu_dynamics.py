@@ -247,10 +247,15 @@ def test_other_fields_are_stored_not_advected(gpu):
     np.testing.assert_array_equal(g.getDGData("tracer", ncomp=1), tracer)
 
 
-@pytest.mark.parametrize("n,steps,dg", [(32, 5, 6), (64, 3, 6), (32, 5, 3), (32, 5, 1)])
-def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps, dg):
+@pytest.mark.parametrize("n,steps,dg,kernel", [(32, 5, 6, None), (64, 3, 6, None), (32, 5, 3, None),
+                                               (32, 5, 1, None), (32, 5, 6, "tma"), (32, 5, 6, "global")])
+def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps, dg, kernel, monkeypatch):
     """FP32 bulk with FP64 Delta/viscosity, lumped-mass inverse and
-    conservation sums: RMS error against the FP64 oracle, stated bars."""
+    conservation sums: RMS error against the FP64 oracle, stated bars.  The
+    box mesh takes the parallelogram stress kernel; NSDG_STRESS_KERNEL forces
+    the operator-streaming ones."""
+    if kernel:
+        monkeypatch.setenv("NSDG_STRESS_KERNEL", kernel)
     box = BoxTest(n)
     prm = dict(alpha=300.0, beta=300.0, n_steps=100)
     g = _make(MEVPDynamicsKernel, box, dg, None, precision=1, **prm)
@@ -265,6 +270,81 @@ def test_mixed_precision_close_to_oracle(gpu, oracle, n, steps, dg):
     assert max(du, dv) <= 1e-5, (du, dv)       # m/s
     assert dh <= 1e-6 and da <= 1e-6, (dh, da)  # m, fraction
     assert np.abs(o.getDG0Data("u")).max() > 1e-3
+    assert g.stress_variant()[0] == (kernel or "affine")
+
+
+def test_mixed_precision_distorted_mesh_close_to_oracle(gpu, oracle):
+    """A mesh of general quadrilaterals (interior vertices moved by up to 8 %
+    of a cell) is not a parallelogram mesh: the mixed path streams the
+    element operators (TMA or global kernel, chosen by timing); stated bars
+    against the FP64 oracle."""
+    box = BoxTest(40, 36)
+    c = box.coords().copy()
+    rng = np.random.default_rng(11)
+    ix = np.tile(np.arange(41), 37)
+    iy = np.repeat(np.arange(37), 41)
+    inner = (ix > 0) & (ix < 40) & (iy > 0) & (iy < 36)
+    c[inner] += rng.uniform(-0.08, 0.08, (inner.sum(), 2)) * (box.L / 40)
+    box.coords = lambda c=c: c
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    kind, mismatch = g.stress_variant()
+    assert kind in ("tma", "global") and mismatch > 1e-3, (kind, mismatch)
+    _advance(g, box, 4)
+    _advance(o, box, 4)
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
+    err = {f: rms(g.getDG0Data(f), o.getDG0Data(f)) for f in ("u", "v", "hice", "cice")}
+    print(f"distorted 40x36 mixed ({kind}): RMS vs oracle {err}")
+    assert max(err["u"], err["v"]) <= 1e-5, err
+    assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
+
+
+def test_parallelogram_kernel_on_a_sheared_mesh(gpu, oracle):
+    """A sheared (non-rectangular) parallelogram mesh takes the coefficient
+    kernel and stays within the mixed-precision bars of the FP64 oracle."""
+    box = BoxTest(36, 30)
+    c = box.coords().copy()
+    c[:, 0] += 0.3 * c[:, 1]
+    c[:, 1] -= 0.1 * c[:, 0]
+    box.coords = lambda c=c: c
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    g = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    kind, mismatch = g.stress_variant()
+    assert kind == "affine" and 0 <= mismatch < 1e-12, (kind, mismatch)
+    _advance(g, box, 4)
+    _advance(o, box, 4)
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))  # noqa: E731
+    err = {f: rms(g.getDG0Data(f), o.getDG0Data(f)) for f in ("u", "v", "hice", "cice")}
+    print(f"sheared 36x30 mixed (affine): RMS vs oracle {err}")
+    assert max(err["u"], err["v"]) <= 1e-5, err
+    assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
+    assert np.abs(o.getDG0Data("u")).max() > 1e-3
+
+
+def test_fp64_viscosity_forms_agree(gpu):
+    """P/(8 alpha Delta) by CUDA's rsqrt(double) and by the Newton-Raphson
+    forms (FP32 seed, one FP64 step; conversions by the FP64 unit or on the
+    integer pipe): within one FP32 ulp, equal in almost every case, over
+    strain invariants from 0 (and denormals) to 1e-4 s^-2."""
+    from nextsimdg_gb300.dynamics import selftest_viscosity
+    rng = np.random.default_rng(2)
+    n = 1 << 18
+    inv = np.concatenate([[0.0, 1e-45, 1e-40, 1.1754942e-38, 1.1754944e-38],
+                          10.0 ** rng.uniform(-36, -4, n - 5)]).astype(np.float32)
+    pa = np.concatenate([[0.0, 1e-300, 5.0, 12.5, 1e3], 10.0 ** rng.uniform(-3, 4, n - 5)])
+    pa[rng.integers(5, n, 100)] = 0.0
+    out = selftest_viscosity(inv, pa, 2e-9)
+    ref = out[0].astype(np.float64)
+    for k in (1, 2):
+        d = np.abs(out[k].astype(np.float64) - ref)
+        ulp = np.spacing(np.abs(out[0])).astype(np.float64)
+        assert np.all(d <= ulp), (k, np.max(d / np.maximum(ulp, 1e-45)))
+        assert np.mean(d == 0) > 0.99, (k, np.mean(d == 0))
+    assert np.all(out[:, pa == 0.0] == 0.0)
+    assert np.all(np.isfinite(out))
 
 
 @pytest.mark.parametrize("n,steps", [(14, 3), (48, 3)])

@@ -53,12 +53,12 @@ def test_ensemble_members_match_single_runs(gpu):
     for i in range(len(boxes)):
         w, h = ens.tile(i)
         # an autotuned 2-D tile of 64 elements, or 32 consecutive elements
-        # for the TMA-staged element kernel
+        # for the TMA-staged and the parallelogram element kernels
         assert (w * h == 64 and w in (64, 32, 16, 8)) or (w, h) == (32, 1)
     assert ens.launches_per_update() < 2 * PRM["n_steps"] + 20 * len(boxes)
 
 
-@pytest.mark.parametrize("kernel", ["tma", "global"])
+@pytest.mark.parametrize("kernel", ["affine", "tma", "global"])
 def test_ensemble_both_element_kernels_match_single_runs(gpu, kernel, monkeypatch):
     """Each element kernel of the batched sub-cycle, forced through
     NSDG_STRESS_KERNEL, reproduces the members' single runs bitwise."""
@@ -83,10 +83,21 @@ def test_ensemble_both_element_kernels_match_single_runs(gpu, kernel, monkeypatc
         for name in ("u", "v", "hice", "cice"):
             np.testing.assert_array_equal(a.getDG0Data(name), b.getDG0Data(name))
     w, h = ens.tile(0)
-    if kernel == "tma":
+    if kernel in ("tma", "affine"):
         assert (w, h) == (32, 1)
     else:
         assert w * h == 64
+    assert ens_members[0].stress_variant()[0] == kernel
+
+
+def test_ensemble_of_box_members_takes_the_parallelogram_kernel(gpu):
+    """Without NSDG_STRESS_KERNEL, box members take the parallelogram
+    coefficient kernel in their single runs and in the ensemble."""
+    boxes = [BoxTest(24, seed=1), BoxTest(40, 33, seed=2)]
+    members = [_member(b) for b in boxes]
+    assert all(m.stress_variant()[0] == "affine" for m in members)
+    ens = Ensemble(members)
+    assert ens.tile(0) == (32, 1) and ens.tile(1) == (32, 1)
 
 
 def test_ensemble_rejects_fp64_members(gpu):
