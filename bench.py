@@ -307,6 +307,17 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
         roof["stress_kernel_ms"] = {names[i]: k.time_kernel(i, 50)[0] for i in ((3, 4, 5, 6, 7) if affine else (3, 4))}
         roof["stress_kernel"] = kind
         roof["parallelogram_mismatch"] = mismatch
+        if affine:
+            # with 5 coefficients per element the kernel's limiter is FP64
+            # issue: Delta and the viscosity take 3 DFMA + 2 DMUL per Gauss
+            # point, against the FMA-lane rate of the measured FP64 DGEMM
+            fp64_tf, fp64_kind = fp64_peak_tflops(local)
+            inst = N * 9 * 5
+            rate = inst / (kms * 1e-3) / 1e12
+            roof["limiter"] = "fp64 issue (Delta and viscosity in FP64), see fp64_issue"
+            roof["fp64_issue"] = {"fp64_instructions_per_launch": inst, "achieved_T_lane_inst_per_s": rate,
+                                  "peak_T_fma_lanes_per_s": fp64_tf / 2, "frac": rate / (fp64_tf / 2),
+                                  "peak_kind": fp64_kind}
     if prec == 0:
         fp64_tf, fp64_kind = fp64_peak_tflops(local)
         ach = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
@@ -573,7 +584,9 @@ def run_ours(args, world, rank, local):
                                   "the learned warm start is measured in variants.learned_fp32, not enabled here"
                                   if prec else "FP64 throughout (the reference's arithmetic)"),
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (per-step operator sweep well above 129 MB), no flush",
+                       "l2": "inputs larger than L2, no flush: each step sweeps the FP32 transport operators "
+                             "(113 MB), the FP64 inverse mass matrices (75 MB) and the FP64 stage buffers, "
+                             "besides the sub-cycle's ~110 MB working set",
                        "bytes_per_cell_update": bytes_per_cell_update(word=4 if prec else 8)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8},
             "gpu_launches": launches * args.steps,
