@@ -11,8 +11,9 @@ thickness with limiters, the preparation of the momentum solve and the 100
 mEVP iterations (strain, stress, divergence, momentum, boundaries).
 
   value  device-resident: K steps of the CUDA graph, CUDA events on the
-         library's stream; inputs (the per-iteration operator sweep, 405 MB
-         FP32 at 512^2, is larger than L2) are not re-flushed between steps.
+         library's stream; not re-flushed between steps: each step sweeps
+         more than L2 holds (the FP32 transport operators, the FP64 inverse
+         mass matrices and stage buffers, the sub-cycle's working set).
   e2e    the reference's module cycle through the C ABI with host buffers
          (MEVPDynamics::update: setData of h, A, winds, ocean, ssh, then
          update, then getDG0Data of h, A, u, v and the ice-ocean stress),
@@ -22,6 +23,9 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
   variants.learned_fp32   the learned warm start: data generation and
                           training on the GPU, then the warm update with and
                           without audit against the plain sub-cycle;
+  variants.ice_growth     the column thermodynamics before the dynamics
+                          (IceGrowth + ThermoIce0 + HiblerSpread +
+                          ConstantHealing) on the same cell count;
   velocity_error_vs_fp64  one simulated day: FP32 path vs FP64 path, next to
                           the FP64 path's own response to h x (1 + 1e-14).
 
@@ -451,6 +455,50 @@ def spherical_variant(args, N: int, local: int):
     return out
 
 
+def ice_growth_variant(args, N: int):
+    """The column thermodynamics step before the dynamics (IceGrowth with
+    ThermoIce0, HiblerSpread, ConstantHealing) on the same number of cells:
+    device time of repeated updates (the state evolves, forcing fixed), its
+    algorithmic bytes against HBM, and the CPU oracle on the same inputs."""
+    from nextsimdg_gb300.ice_growth import IceGrowth
+    rng = np.random.default_rng(5)
+    cice = rng.uniform(0.0, 1.0, N)
+    fields = {"hice": rng.uniform(0.0, 3.0, N) * cice, "cice": cice, "hsnow": rng.uniform(0.0, 0.3, N) * cice,
+              "tice": rng.uniform(-30.0, 0.0, N), "qia": rng.uniform(-100.0, 400.0, N),
+              "dqia_dt": rng.uniform(0.0, 30.0, N), "qow": rng.uniform(-200.0, 400.0, N),
+              "qio": rng.uniform(0.0, 200.0, N), "sublim": rng.uniform(-1e-5, 1e-5, N),
+              "snowfall": rng.uniform(0.0, 1e-4, N), "penSW": rng.uniform(0.0, 50.0, N),
+              "sst": rng.uniform(-1.8, 1.0, N), "tf": np.full(N, -1.751), "mlbhc": np.full(N, 4.29e7),
+              "damage": rng.uniform(0.0, 1.0, N)}
+    g = IceGrowth(N)
+    for name, arr in fields.items():
+        g.setData(name, arr)
+    reps = 50
+    g.time_updates(120.0, 5)
+    ms = g.time_updates(120.0, reps) / reps
+    g.close()
+    bpe = 23 * 8 + 19 * 8 + 1  # slots read, slots written, ocean flag
+    hbm, _ = measured_peaks()
+    out = {"cells": N, "value": N / (ms * 1e-3), "unit": "cell-updates/s", "ms_per_update": ms,
+           "algorithmic_bytes_per_cell": bpe, "achieved_GBps": N * bpe / (ms * 1e-3) / 1e9,
+           "hbm_frac": N * bpe / (ms * 1e-3) / 1e9 / hbm, "parity": "bit-identical to the CPU oracle (tests)"}
+    try:
+        from oracle import pyoracle
+        o = pyoracle.OracleIceGrowth(N)
+        for name, arr in fields.items():
+            o.setData(name, arr)
+        t0 = time.perf_counter()
+        n_cpu = 3
+        for _ in range(n_cpu):
+            o.update(120.0)
+        cpu_s = (time.perf_counter() - t0) / n_cpu
+        out["cpu_baseline"] = {"value": N / cpu_s, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                               "sample": f"{n_cpu} updates of {N} cells"}
+    except Exception as ex:  # the oracle is test infrastructure: report, do not fail the bench
+        out["cpu_baseline"] = {"unavailable": str(ex)[:200]}
+    return out
+
+
 def day_error(args, box, steps: int):
     """Velocity / thickness / concentration RMS after `steps` model steps: the
     headline precision path and the FP64 path with h scaled by (1 + 1e-14),
@@ -568,6 +616,7 @@ def run_ours(args, world, rank, local):
             variants["bbm"] = bbm_variant(args, box, N)
         if prec:
             variants["spherical"] = spherical_variant(args, N, local)
+            variants["ice_growth"] = ice_growth_variant(args, N)
     err = day_error(args, box, args.error_steps) if (prec and args.error_steps > 0 and world == 1) else None
 
     if rank == 0:

@@ -353,6 +353,102 @@ int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
 int nsdg_mean_value_noalloc(int dg, size_t n_elements, const double* phi, const double* jw,
     double* out, void* stream);
 
+/* ======================================================================== */
+/* Column thermodynamics: ice growth (the step before the dynamics)          */
+/* ======================================================================== */
+/* IceGrowth::update (physics/src/IceGrowth.cpp:148-171) on the GPU with the
+ * default modules it drives: ThermoIce0 (zero-layer vertical growth,
+ * physics/src/modules/IceThermodynamicsModule/ThermoIce0.cpp:85-172),
+ * HiblerSpread (lateral growth and melt, .../HiblerSpread.cpp:53-66),
+ * ConstantHealing (damage healing, .../ConstantHealing.cpp:53-73) and
+ * IceMinima, or their Dummy / NoHealing alternatives.  Per element, in the
+ * reference's order: true thicknesses from the cell averages, the minimum
+ * limits, vertical growth, new ice over open water, lateral spread, the
+ * limits again, healing.  All arithmetic is FP64, element-local, in the
+ * reference's operation order (bit-identical to the CPU oracle).  Fields are
+ * one double per element (H-type ModelArrays, index i + nx j); the update
+ * runs over the ocean elements of the mask (ModelComponent::overElements). */
+typedef struct nsdg_ice_growth nsdg_ice_growth;
+
+typedef struct nsdg_ice_growth_params {
+    double ks;           /* snow conductivity, W K^-1 m^-1 (nextsim_thermo.ks: 0.3096) */
+    double h_min;        /* minimum ice thickness, m (nextsim_thermo.min_thick: 0.01) */
+    double c_min;        /* minimum concentration (nextsim_thermo.min_conc: 1e-12) */
+    double h0;           /* thickness of newly frozen ice, m (Hibler.h0: 0.25) */
+    double phi_m;        /* melt exponent (Hibler.phiM: 0.5) */
+    double healing_time; /* healing time scale, s (ConstantHealing.td: 15 days) */
+    int use_thermo;      /* nextsim_thermo.use_thermo_forcing (1) */
+    int thermo_model;    /* 0 ThermoIce0, 1 DummyIceThermodynamics */
+    int lateral_model;   /* 0 HiblerSpread, 1 DummyIceSpread */
+    int healing_model;   /* 0 ConstantHealing, 1 NoHealing */
+    int flooding;        /* ThermoIce0 snow-to-ice conversion (1) */
+} nsdg_ice_growth_params;
+
+/* Field slots (the names nsdg_ice_growth_set_field / get_field take).
+ * Inputs: the prognostic cell averages and the forcing the other modules
+ * provide; outputs: IceGrowth's and ThermoIce0's arrays after an update.
+ * qow, qio and damage are read and written.  Outputs that an update leaves
+ * untouched keep their previous values (as the reference's member arrays
+ * do); every slot starts at zero. */
+enum {
+    NSDG_IG_HICE_CELL = 0, /* "hice": cell-averaged ice thickness, m (Protected::H_ICE) */
+    NSDG_IG_CICE0,         /* "cice": ice concentration (Protected::C_ICE) */
+    NSDG_IG_HSNOW_CELL,    /* "hsnow": cell-averaged snow thickness, m */
+    NSDG_IG_TICE0,         /* "tice": ice surface temperature, C (Protected::T_ICE) */
+    NSDG_IG_QIA,           /* "qia": ice-atmosphere heat flux, W m^-2 */
+    NSDG_IG_DQIA_DT,       /* "dqia_dt": its temperature derivative, W m^-2 K^-1 */
+    NSDG_IG_QOW,           /* "qow": open-water heat flux, W m^-2 (read, written) */
+    NSDG_IG_QIO,           /* "qio": ice-ocean heat flux, W m^-2 (read, written) */
+    NSDG_IG_SUBLIM,        /* "sublim": sublimation rate, kg m^-2 s^-1 */
+    NSDG_IG_SNOWFALL,      /* "snowfall": snowfall rate, kg m^-2 s^-1 */
+    NSDG_IG_PENSW,         /* "penSW": penetrating short wave, W m^-2 */
+    NSDG_IG_SST,           /* "sst": sea surface temperature, C */
+    NSDG_IG_TF,            /* "tf": sea water freezing point, C */
+    NSDG_IG_MLBHC,         /* "mlbhc": mixed layer bulk heat capacity, J K^-1 m^-2 */
+    NSDG_IG_DAMAGE,        /* "damage" (read, written) */
+    NSDG_IG_HICE,          /* "hice_updated": true ice thickness after the update, m */
+    NSDG_IG_CICE,          /* "cice_updated" */
+    NSDG_IG_HSNOW,         /* "hsnow_updated": true snow thickness, m */
+    NSDG_IG_HICE0,         /* "hice_initial": true ice thickness at the start, m */
+    NSDG_IG_HSNOW0,        /* "hsnow_initial" */
+    NSDG_IG_NEWICE,        /* "newice": new ice over open water, m */
+    NSDG_IG_DELTA_CICE,    /* "delta_cice" */
+    NSDG_IG_DELTA_HICE,    /* "delta_hice": vertical thickness change, m */
+    NSDG_IG_TICE,          /* "tice_updated": updated ice temperature, C */
+    NSDG_IG_QIC,           /* "qic": conductive heat flux in the ice, W m^-2 */
+    NSDG_IG_SNOW_TO_ICE,   /* "snow_to_ice": flooded snow converted to ice, m */
+    NSDG_IG_TOP_MELT,      /* "top_melt", m */
+    NSDG_IG_BOT_MELT,      /* "bottom_melt", m */
+    NSDG_IG_SNOW_MELT,     /* "snow_melt", m */
+    NSDG_IG_DELTA_CFREEZE, /* "delta_cfreeze" */
+    NSDG_IG_DELTA_CMELT,   /* "delta_cmelt" */
+    NSDG_IG_NFIELDS
+};
+
+void nsdg_ice_growth_default_params(nsdg_ice_growth_params* p);
+/* mask: n_elements doubles, > 0 for ocean (NULL: all ocean). */
+int nsdg_ice_growth_create(size_t n_elements, const double* mask, const nsdg_ice_growth_params* p,
+    nsdg_ice_growth** out);
+int nsdg_ice_growth_destroy(nsdg_ice_growth* g);
+const char* nsdg_ice_growth_last_error(nsdg_ice_growth* g);
+int nsdg_ice_growth_set_field(nsdg_ice_growth* g, const char* name, const double* data, size_t n);
+int nsdg_ice_growth_get_field(nsdg_ice_growth* g, const char* name, double* out, size_t n);
+/* One IceGrowth::update of dt seconds. */
+int nsdg_ice_growth_update(nsdg_ice_growth* g, double dt);
+/* Device time of `reps` updates (the fields evolve), for the benchmark. */
+int nsdg_ice_growth_time_updates(nsdg_ice_growth* g, double dt, int reps, float* ms);
+/* Device-side coupling with a dynamics handle on the same mesh, replacing
+ * the host round trip of PrognosticData::update / updatePrognosticFields
+ * (core/src/PrognosticData.cpp:83-118):
+ *   direction 0: the dynamics' DG0 thickness, concentration and damage
+ *                become the growth inputs "hice", "cice", "damage";
+ *   direction 1: hice_updated x cice_updated, cice_updated and damage
+ *                become the dynamics' "hice", "cice", "damage" as H-type
+ *                inputs (component 0 set, higher components zeroed, as
+ *                setData does with a one-component array).
+ * Ordered after both handles' queued work; no host copies. */
+int nsdg_ice_growth_exchange(nsdg_ice_growth* g, nsdg_kernel* k, int direction);
+
 #ifdef __cplusplus
 }
 #endif

@@ -130,6 +130,15 @@ SIGNATURES = [
     ("nsdg_selftest_viscosity", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("nsdg_ice_growth_default_params", None, [c_void_p]),
+    ("nsdg_ice_growth_create", c_int, [c_size_t, c_void_p, c_void_p, POINTER(c_void_p)]),
+    ("nsdg_ice_growth_destroy", c_int, [c_void_p]),
+    ("nsdg_ice_growth_last_error", c_char_p, [c_void_p]),
+    ("nsdg_ice_growth_set_field", c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
+    ("nsdg_ice_growth_get_field", c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
+    ("nsdg_ice_growth_update", c_int, [c_void_p, c_double]),
+    ("nsdg_ice_growth_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
+    ("nsdg_ice_growth_exchange", c_int, [c_void_p, c_void_p, c_int]),
 ]
 
 _lib = None
@@ -153,6 +162,24 @@ def load(path: Path | str | None = None) -> ctypes.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+class IceGrowthParams(ctypes.Structure):
+    """nsdg_ice_growth_params (include/nsdg.h)."""
+
+    _fields_ = [
+        ("ks", c_double), ("h_min", c_double), ("c_min", c_double), ("h0", c_double), ("phi_m", c_double),
+        ("healing_time", c_double), ("use_thermo", c_int), ("thermo_model", c_int),
+        ("lateral_model", c_int), ("healing_model", c_int), ("flooding", c_int),
+    ]
+
+
+# the field slots of the ice-growth handle (NSDG_IG_* in include/nsdg.h), in order
+ICE_GROWTH_FIELDS = (
+    "hice", "cice", "hsnow", "tice", "qia", "dqia_dt", "qow", "qio", "sublim", "snowfall", "penSW", "sst", "tf",
+    "mlbhc", "damage", "hice_updated", "cice_updated", "hsnow_updated", "hice_initial", "hsnow_initial", "newice",
+    "delta_cice", "delta_hice", "tice_updated", "qic", "snow_to_ice", "top_melt", "bottom_melt", "snow_melt",
+    "delta_cfreeze", "delta_cmelt")
 
 
 def default_params() -> Params:

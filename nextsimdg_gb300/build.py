@@ -23,8 +23,12 @@ LIB = PKG / "libnsdg_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
-CU_SOURCES = ["nsdg_kernels.cu", "nsdg_noalloc.cu", "nsdg_surrogate.cu"]
-CXX_SOURCES = ["nsdg_host.cpp", "nsdg_capi.cpp", "nsdg_transport_capi.cpp"]
+CU_SOURCES = ["nsdg_kernels.cu", "nsdg_noalloc.cu", "nsdg_surrogate.cu", "nsdg_ice_growth.cu"]
+CXX_SOURCES = ["nsdg_host.cpp", "nsdg_capi.cpp", "nsdg_transport_capi.cpp", "nsdg_ice_growth_capi.cpp"]
+# per-file nvcc flags: the column thermodynamics rounds every product and sum
+# separately (no fused multiply-add), as the reference's and the oracle's
+# arithmetic does
+CU_FLAGS = {"nsdg_ice_growth.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -55,7 +59,8 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         objs.append(obj)
         if force or _sources_newer(obj, [CSRC / src] + headers):
             cmd = [_nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(CSRC / src), "-o", str(obj)]
+                   "-Xcompiler", "-ffp-contract=off", *CU_FLAGS.get(src, []), *inc, "-c", str(CSRC / src),
+                   "-o", str(obj)]
             if ptxas:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

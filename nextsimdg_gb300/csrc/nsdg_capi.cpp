@@ -7,6 +7,7 @@
 #include "nsdg.h"
 
 #include "nsdg_host.hpp"
+#include "nsdg_ice_growth.hpp"
 #include "nsdg_kernels.hpp"
 #include "nsdg_surrogate.hpp"
 
@@ -2434,6 +2435,38 @@ int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out)
     if (e != cudaSuccess)
         return NSDG_ERR_CUDA;
     *timed_out = h;
+    return NSDG_OK;
+}
+
+int nsdg_ice_growth_exchange(nsdg_ice_growth* g, nsdg_kernel* k, int direction)
+{
+    if (!g || !k || (direction != 0 && direction != 1))
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return g->fail(NSDG_ERR_BAD_ARG, "exchange: the dynamics kernel is not initialised");
+    if (k->N != g->n)
+        return g->fail(NSDG_ERR_SIZE_MISMATCH, "exchange: the dynamics mesh has a different element count");
+    // the damage field is device state of the BBM kernel only (an mEVP
+    // handle keeps "damage" as a stored, unused field)
+    double* damage = k->rheology == NSDG_RHEOLOGY_BBM ? k->damage : nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    // the growth stream waits for the dynamics' queued work, runs the copy,
+    // and the dynamics stream waits for the copy before its next work
+    if (e == cudaSuccess) e = cudaEventRecord(ev, k->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g->stream, ev, 0);
+    if (e == cudaSuccess)
+        e = direction == 0 ? launchIceGrowthFromDynamics(g->stream, g->n, k->hice, k->cice, damage, g->fields)
+                           : launchIceGrowthToDynamics(g->stream, g->n, k->dg, g->fields, k->hice, k->cice, damage);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, g->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(k->stream, ev, 0);
+    if (ev)
+        cudaEventDestroy(ev);
+    if (e != cudaSuccess)
+        return g->fail(NSDG_ERR_CUDA, std::string("exchange: ") + cudaGetErrorString(e));
+    if (direction == 1)
+        k->readCache = 0; // the dynamics state changed
+    g->err.clear();
     return NSDG_OK;
 }
 

@@ -38,6 +38,7 @@ class Params(ctypes.Structure):
 
 
 def build(force: bool = False) -> Path:
+    build_ice_growth(force)
     src = HERE / "nsdg_oracle.cpp"
     hdr = HERE.parent / "include" / "nsdg.h"
     if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
@@ -46,6 +47,21 @@ def build(force: bool = False) -> Path:
         subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
                         "-I", str(HERE.parent / "include"), "-shared", "-o", str(LIB), str(src)], check=True)
     return LIB
+
+
+IG_SRC = HERE / "ice_growth_oracle.cpp"
+IG_LIB = HERE / "_build" / "libice_growth_oracle.so"
+
+
+def build_ice_growth(force: bool = False) -> Path:
+    """The column-thermodynamics oracle (oracle/ice_growth_oracle.cpp)."""
+    hdr = HERE.parent / "include" / "nsdg.h"
+    if force or not IG_LIB.exists() or IG_LIB.stat().st_mtime < max(IG_SRC.stat().st_mtime, hdr.stat().st_mtime):
+        IG_LIB.parent.mkdir(exist_ok=True)
+        cxx = os.environ.get("CXX", "g++")
+        subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+                        "-I", str(HERE.parent / "include"), "-shared", "-o", str(IG_LIB), str(IG_SRC)], check=True)
+    return IG_LIB
 
 
 _lib = None
@@ -94,6 +110,88 @@ def load() -> ctypes.CDLL:
             fn.argtypes = args
         _lib = lib
     return _lib
+
+
+class IceGrowthParams(ctypes.Structure):
+    """Same layout as nsdg_ice_growth_params in include/nsdg.h."""
+
+    _fields_ = [
+        ("ks", c_double), ("h_min", c_double), ("c_min", c_double), ("h0", c_double), ("phi_m", c_double),
+        ("healing_time", c_double), ("use_thermo", c_int), ("thermo_model", c_int),
+        ("lateral_model", c_int), ("healing_model", c_int), ("flooding", c_int),
+    ]
+
+
+# the field slots of include/nsdg.h (NSDG_IG_*), in order
+IG_FIELDS = ("hice", "cice", "hsnow", "tice", "qia", "dqia_dt", "qow", "qio", "sublim", "snowfall", "penSW",
+             "sst", "tf", "mlbhc", "damage", "hice_updated", "cice_updated", "hsnow_updated", "hice_initial",
+             "hsnow_initial", "newice", "delta_cice", "delta_hice", "tice_updated", "qic", "snow_to_ice",
+             "top_melt", "bottom_melt", "snow_melt", "delta_cfreeze", "delta_cmelt")
+
+_ig = None
+
+
+def _ig_lib() -> ctypes.CDLL:
+    global _ig
+    if _ig is None:
+        build_ice_growth()
+        lib = ctypes.CDLL(str(IG_LIB))
+        lib.oracle_ice_growth_default_params.restype = None
+        lib.oracle_ice_growth_default_params.argtypes = [POINTER(IceGrowthParams)]
+        lib.oracle_ice_growth_update.restype = None
+        lib.oracle_ice_growth_update.argtypes = [c_size_t, c_void_p, POINTER(IceGrowthParams), c_double, c_void_p]
+        lib.oracle_thermo_ice0.restype = None
+        lib.oracle_thermo_ice0.argtypes = [c_size_t, POINTER(IceGrowthParams), c_double, c_void_p]
+        lib.oracle_constant_healing.restype = c_double
+        lib.oracle_constant_healing.argtypes = [c_double, c_double, c_double, c_double, c_double]
+        lib.oracle_unesco_freezing.restype = c_double
+        lib.oracle_unesco_freezing.argtypes = [c_double]
+        _ig = lib
+    return _ig
+
+
+def ice_growth_params(**overrides) -> IceGrowthParams:
+    p = IceGrowthParams()
+    _ig_lib().oracle_ice_growth_default_params(byref(p))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def constant_healing(damage: float, cice: float, delta_ci: float, dt: float, td: float) -> float:
+    return _ig_lib().oracle_constant_healing(damage, cice, delta_ci, dt, td)
+
+
+def unesco_freezing(sss: float) -> float:
+    return _ig_lib().oracle_unesco_freezing(float(sss))
+
+
+class OracleIceGrowth:
+    """IceGrowth (ThermoIce0, HiblerSpread, ConstantHealing) restated on the
+    CPU, with the product's set/get-by-name interface."""
+
+    def __init__(self, n: int, mask=None, params: IceGrowthParams | None = None, **overrides):
+        self.n = n
+        self.params = params if params is not None else ice_growth_params(**overrides)
+        self.mask = None if mask is None else _f64(mask).ravel().copy()
+        self.fields = np.zeros((len(IG_FIELDS), n))
+
+    def setData(self, name: str, data):
+        self.fields[IG_FIELDS.index(name)] = np.broadcast_to(_f64(data).ravel(), (self.n,))
+
+    def getData(self, name: str) -> np.ndarray:
+        return self.fields[IG_FIELDS.index(name)].copy()
+
+    def update(self, dt: float):
+        m = None if self.mask is None else _p(self.mask)
+        _ig_lib().oracle_ice_growth_update(self.n, m, byref(self.params), float(dt), _p(self.fields))
+
+    def thermo_only(self, dt: float):
+        """ThermoIce0 alone on the true-thickness slots (the reference's
+        ThermoIce0 test drives the module that way)."""
+        _ig_lib().oracle_thermo_ice0(self.n, byref(self.params), float(dt), _p(self.fields))
 
 
 def default_params(**overrides) -> Params:

@@ -96,3 +96,21 @@ def test_parallelogram_mismatch_on_the_host(nsdg_lib):
         parallelogram_mismatch(sheared[:-1], n, n)
     with pytest.raises(NsdgError):
         parallelogram_mismatch(sheared, n, n, 2)
+
+
+def test_ice_growth_create_validates_arguments(nsdg_lib):
+    """Host-side checks of the column-thermodynamics handle (no GPU call is
+    made before they pass); the defaults equal the oracle's."""
+    from oracle import pyoracle
+    from nextsimdg_gb300.ice_growth import default_params
+    p = default_params()
+    o = pyoracle.ice_growth_params()
+    for name, _ in p._fields_:
+        assert getattr(p, name) == getattr(o, name), name
+    assert _lib.ICE_GROWTH_FIELDS == pyoracle.IG_FIELDS
+    h = ctypes.c_void_p()
+    for bad in (dict(h0=0.0), dict(healing_time=-1.0), dict(thermo_model=2), dict(ks=float("nan"))):
+        q = default_params(**bad)
+        assert nsdg_lib.nsdg_ice_growth_create(4, None, ctypes.byref(q), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
+    assert nsdg_lib.nsdg_ice_growth_create(0, None, ctypes.byref(p), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
+    assert nsdg_lib.nsdg_ice_growth_exchange(None, None, 0) == _lib.NSDG_ERR_BAD_ARG
