@@ -477,7 +477,7 @@ def ice_growth_variant(args, N: int):
     g.time_updates(120.0, 5)
     ms = g.time_updates(120.0, reps) / reps
     g.close()
-    bpe = 23 * 8 + 19 * 8 + 1  # slots read, slots written, ocean flag
+    bpe = 25 * 8 + 21 * 8 + 1  # slots read, slots written, ocean flag
     hbm, _ = measured_peaks()
     out = {"cells": N, "value": N / (ms * 1e-3), "unit": "cell-updates/s", "ms_per_update": ms,
            "algorithmic_bytes_per_cell": bpe, "achieved_GBps": N * bpe / (ms * 1e-3) / 1e9,

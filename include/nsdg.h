@@ -357,8 +357,9 @@ int nsdg_mean_value_noalloc(int dg, size_t n_elements, const double* phi, const 
 /* Column thermodynamics: ice growth (the step before the dynamics)          */
 /* ======================================================================== */
 /* IceGrowth::update (physics/src/IceGrowth.cpp:148-171) on the GPU with the
- * default modules it drives: ThermoIce0 (zero-layer vertical growth,
- * physics/src/modules/IceThermodynamicsModule/ThermoIce0.cpp:85-172),
+ * modules it drives: ThermoIce0 (zero-layer vertical growth, the default,
+ * physics/src/modules/IceThermodynamicsModule/ThermoIce0.cpp:85-172) or
+ * ThermoWinton (three-layer, .../ThermoWinton.cpp:102-342),
  * HiblerSpread (lateral growth and melt, .../HiblerSpread.cpp:53-66),
  * ConstantHealing (damage healing, .../ConstantHealing.cpp:53-73) and
  * IceMinima, or their Dummy / NoHealing alternatives.  Per element, in the
@@ -378,7 +379,8 @@ typedef struct nsdg_ice_growth_params {
     double phi_m;        /* melt exponent (Hibler.phiM: 0.5) */
     double healing_time; /* healing time scale, s (ConstantHealing.td: 15 days) */
     int use_thermo;      /* nextsim_thermo.use_thermo_forcing (1) */
-    int thermo_model;    /* 0 ThermoIce0, 1 DummyIceThermodynamics */
+    int thermo_model;    /* 0 ThermoIce0, 1 DummyIceThermodynamics, 2 ThermoWinton (three
+                            temperature levels: "tice", "tice_1", "tice_2") */
     int lateral_model;   /* 0 HiblerSpread, 1 DummyIceSpread */
     int healing_model;   /* 0 ConstantHealing, 1 NoHealing */
     int flooding;        /* ThermoIce0 snow-to-ice conversion (1) */
@@ -422,6 +424,10 @@ enum {
     NSDG_IG_SNOW_MELT,     /* "snow_melt", m */
     NSDG_IG_DELTA_CFREEZE, /* "delta_cfreeze" */
     NSDG_IG_DELTA_CMELT,   /* "delta_cmelt" */
+    NSDG_IG_TICE0_1,       /* "tice_1": ice temperature, upper layer, C (ThermoWinton) */
+    NSDG_IG_TICE0_2,       /* "tice_2": ice temperature, lower layer, C (ThermoWinton) */
+    NSDG_IG_TICE_1,        /* "tice_updated_1" */
+    NSDG_IG_TICE_2,        /* "tice_updated_2" */
     NSDG_IG_NFIELDS
 };
 

@@ -18,7 +18,8 @@ namespace {
 const char* const kSlotNames[NSDG_IG_NFIELDS] = { "hice", "cice", "hsnow", "tice", "qia", "dqia_dt", "qow", "qio",
     "sublim", "snowfall", "penSW", "sst", "tf", "mlbhc", "damage", "hice_updated", "cice_updated", "hsnow_updated",
     "hice_initial", "hsnow_initial", "newice", "delta_cice", "delta_hice", "tice_updated", "qic", "snow_to_ice",
-    "top_melt", "bottom_melt", "snow_melt", "delta_cfreeze", "delta_cmelt" };
+    "top_melt", "bottom_melt", "snow_melt", "delta_cfreeze", "delta_cmelt", "tice_1", "tice_2", "tice_updated_1",
+    "tice_updated_2" };
 
 int slotOf(const char* name)
 {
@@ -32,7 +33,7 @@ bool validParams(const nsdg_ice_growth_params& p)
 {
     return std::isfinite(p.ks) && p.ks > 0 && std::isfinite(p.h_min) && p.h_min >= 0 && std::isfinite(p.c_min)
         && p.c_min >= 0 && std::isfinite(p.h0) && p.h0 > 0 && std::isfinite(p.phi_m)
-        && std::isfinite(p.healing_time) && p.healing_time > 0 && (p.thermo_model == 0 || p.thermo_model == 1)
+        && std::isfinite(p.healing_time) && p.healing_time > 0 && (p.thermo_model >= 0 && p.thermo_model <= 2)
         && (p.lateral_model == 0 || p.lateral_model == 1) && (p.healing_model == 0 || p.healing_model == 1);
 }
 

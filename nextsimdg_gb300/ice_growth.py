@@ -1,6 +1,7 @@
 """Column thermodynamics on the GPU: the reference's IceGrowth
 (physics/src/IceGrowth.cpp) with its default modules ThermoIce0, HiblerSpread
-and ConstantHealing (or DummyIceThermodynamics, DummyIceSpread, NoHealing),
+and ConstantHealing (or ThermoWinton, DummyIceThermodynamics, DummyIceSpread,
+NoHealing),
 through the C ABI (nsdg_ice_growth_* in include/nsdg.h).
 
 The interface mirrors the module's data flow: the prognostic cell averages
@@ -21,7 +22,7 @@ import numpy as np
 from . import _lib
 from ._lib import ICE_GROWTH_FIELDS, IceGrowthParams, NsdgError
 
-THERMO_MODELS = {"ThermoIce0": 0, "DummyIceThermodynamics": 1}
+THERMO_MODELS = {"ThermoIce0": 0, "DummyIceThermodynamics": 1, "ThermoWinton": 2}
 LATERAL_MODELS = {"HiblerSpread": 0, "DummyIceSpread": 1}
 HEALING_MODELS = {"ConstantHealing": 0, "NoHealing": 1}
 

@@ -1,13 +1,13 @@
-// CPU oracle of the column thermodynamics step (IceGrowth with ThermoIce0,
-// HiblerSpread, ConstantHealing, IceMinima, and the Dummy / NoHealing
+// CPU oracle of the column thermodynamics step (IceGrowth with ThermoIce0 or
+// ThermoWinton, HiblerSpread, ConstantHealing, IceMinima, and the Dummy / NoHealing
 // alternatives).  TEST INFRASTRUCTURE ONLY: the checker of the GPU ice-growth
 // path, never linked into the product.  A plain C++17 restatement of the
 // reference's per-element arithmetic in its operation order, each function
 // citing the reference lines it follows; built with -ffp-contract=off.
 //
 // Pinned against the reference's own known-answer tests that its build runs
-// (physics/test/IceGrowth_test.cpp, ThermoIce0_test.cpp, DamageHealing_test.cpp,
-// physics/test/CMakeLists.txt:51-117) in tests/test_oracle_ice_growth.py.
+// (physics/test/IceGrowth_test.cpp, ThermoIce0_test.cpp, ThermoWintonTemperature_test.cpp,
+// DamageHealing_test.cpp; physics/test/CMakeLists.txt:51-117) in tests/test_oracle_ice_growth.py.
 // physics/test/ThermoIce0Temperature_test.cpp is not built there (it uses a
 // retired array-store API) and its expected conductive flux predates the
 // Semtner factor gamma = 1.065 (its 44.4839 W m^-2 is 47.375 / 1.065).
@@ -21,6 +21,7 @@ namespace {
 
 // core/src/include/constants.hpp:46-69 (Ice), 105-120 (Water)
 constexpr double kIceKappa = 2.0334;
+constexpr double kIceCp = 2100.;
 constexpr double kLf = 333.55e3;
 constexpr double kRhoIce = 917;
 constexpr double kRhoSnow = 330.;
@@ -135,6 +136,175 @@ void thermoIce0(const Elem& x, const nsdg_ice_growth_params& p, double dt)
     }
 }
 
+// ThermoWinton::calculateTemps (physics/src/modules/IceThermodynamicsModule/ThermoWinton.cpp:298-342):
+// Winton (2000) eqs. (5)-(22) for the surface and the two layer temperatures
+void wintonTemps(const Elem& x, const nsdg_ice_growth_params& p, double& tSurf, double& tUppr, double& tLowr,
+    double& mSurf, double dt)
+{
+    const double cVol = kIceCp * kRhoIce;
+    const double seaIceTf = -kMu * kIceS;
+    const double hi = x[NSDG_IG_HICE];
+    const double hsnow = x[NSDG_IG_HSNOW];
+    const double tBase = x[NSDG_IG_TF];
+    const double tMelt = (hsnow > 0) ? 0 : seaIceTf;
+    const double k12 = 4 * kIceKappa * p.ks / (p.ks * hi + 4 * kIceKappa * hsnow); // (5)
+    const double a = x[NSDG_IG_QIA] - tSurf * x[NSDG_IG_DQIA_DT];                    // (7)
+    const double b = x[NSDG_IG_DQIA_DT];                                             // (8)
+    const double k32 = 2 * kIceKappa / hi;                                           // (10)
+    double a1 = hi * cVol / (2 * dt) + k32 * (4 * dt * k32 + hi * cVol) / (6 * dt * k32 + hi * cVol)
+        + b * k12 / (k12 + b); // (16)
+    double b1 = -hi * (cVol * tUppr + kLf * kRhoIce * seaIceTf / tUppr) / (2 * dt) - x[NSDG_IG_PENSW]
+        - k32 * (4 * dt * k32 * tBase + hi * cVol * tLowr) / (6 * dt * k32 + hi * cVol)
+        + a * k12 / (k12 + b); // (17)
+    const double c1 = hi * kLf * kRhoIce * seaIceTf / (2 * dt); // (18)
+    tUppr = -(b1 + std::sqrt(b1 * b1 - 4 * a1 * c1)) / (2 * a1); // (21)
+    tSurf = (k12 * tUppr - a) / (k12 + b);                         // (6)
+    if (tSurf > tMelt) {
+        tSurf = tMelt;
+        a1 += k12 - k12 * b / (k12 + b);                           // (19)
+        b1 -= k12 * tSurf + a * k12 / (k12 + b);                   // (20)
+        tUppr = -(b1 + std::sqrt(b1 * b1 - 4 * a1 * c1)) / (2 * a1); // (21)
+        mSurf = k12 * (tUppr - tSurf) - (a + b * tSurf);           // (22)
+    }
+    tLowr = (2 * dt * k32 * (tUppr + 2 * x[NSDG_IG_TF]) + hi * cVol * tLowr) / (6 * dt * k32 + hi * cVol); // (15)
+}
+
+// ThermoWinton::calculateElement (ThermoWinton.cpp:102-296).  As in the
+// reference, bottom_melt and snow_to_ice accumulate onto their previous values.
+void thermoWinton(const Elem& x, const nsdg_ice_growth_params& p, double dt)
+{
+    const double cVol = kIceCp * kRhoIce;
+    const double seaIceTf = -kMu * kIceS;
+    double& hice = x[NSDG_IG_HICE];
+    if (x[NSDG_IG_CICE] <= 0 || hice <= 0) {
+        x[NSDG_IG_SNOW_TO_ICE] = 0;
+        x[NSDG_IG_DELTA_HICE] = 0;
+        hice = 0;
+        x[NSDG_IG_HSNOW] = 0;
+        x[NSDG_IG_TICE] = seaIceTf;
+        x[NSDG_IG_TICE_1] = seaIceTf;
+        x[NSDG_IG_TICE_2] = seaIceTf;
+        return;
+    }
+    const double bulkLHFusionSnow = kLf * kRhoSnow;
+    const double bulkLHFusionIce = kLf * kRhoIce;
+    double tSurf = x[NSDG_IG_TICE0];
+    double tUppr = x[NSDG_IG_TICE0_1];
+    double tLowr = x[NSDG_IG_TICE0_2];
+    const double tBott = x[NSDG_IG_TF];
+    double surfMelt = 0;
+    wintonTemps(x, p, tSurf, tUppr, tLowr, surfMelt, dt);
+    const double dHfTf_cp = kLf * seaIceTf / kIceCp;
+    double h1 = hice / 2;
+    double h2 = hice / 2;
+    const double e1 = cVol * (tUppr - seaIceTf) - bulkLHFusionIce * (1 - seaIceTf / tUppr);
+    const double e2 = cVol * (tLowr - seaIceTf) - bulkLHFusionIce;
+    double& hs = x[NSDG_IG_HSNOW];
+    hs += x[NSDG_IG_SNOWFALL] / kRhoSnow * dt;
+    // sublimation, four cases
+    const double deltaSnow = x[NSDG_IG_SUBLIM] * dt / kRhoSnow;
+    double deltaIce1 = (deltaSnow - hs) * kRhoSnow / kRhoIce;
+    double deltaIce2 = deltaIce1 - h1;
+    if (deltaSnow <= hs) {
+        hs -= deltaSnow;
+    } else if (deltaIce1 <= h1) {
+        h1 -= deltaIce1;
+        hs = 0;
+    } else if (deltaIce2 <= h2) {
+        h2 -= deltaIce2;
+        h1 = 0;
+        hs = 0;
+    } else {
+        h2 = 0;
+        h1 = 0;
+        hs = 0;
+    }
+    double& topMelt = x[NSDG_IG_TOP_MELT];
+    double& botMelt = x[NSDG_IG_BOT_MELT];
+    double& snowMelt = x[NSDG_IG_SNOW_MELT];
+    double& qio = x[NSDG_IG_QIO];
+    topMelt = stdMax(0., h1 + h2 - hice); // (23)
+    // bottom melt / freezing
+    const double meltBottom = (qio - 4 * kIceKappa * (tBott - tLowr) / hice) * dt;
+    snowMelt = 0;
+    if (meltBottom <= 0.) {
+        const double eBot = cVol * (tBott - seaIceTf) - bulkLHFusionIce;
+        deltaIce2 = meltBottom / eBot;                                 // (24)
+        tLowr = (deltaIce2 * tBott + h2 * tLowr) / (deltaIce2 + h2);   // (26)
+        h2 += deltaIce2;
+    } else {
+        deltaIce2 = -stdMin(-meltBottom / e2, h2);
+        deltaIce1 = -stdMin(stdMax(-(meltBottom + e2 * h2) / e1, 0.), h1);
+        snowMelt = -stdMin(stdMax((meltBottom + e2 * h2 + e1 * h1) / bulkLHFusionSnow, 0.), hs);
+        if (h2 + h1 + hs - deltaIce2 - deltaIce1 - snowMelt <= 0.)
+            qio -= stdMax(meltBottom - bulkLHFusionSnow * hs + e1 * h1 + e2 * h2, 0.) / dt; // (34)
+        hs += snowMelt;
+        h1 += deltaIce1;
+        h2 += deltaIce2;
+        botMelt += deltaIce1 + deltaIce2;
+    }
+    // surface melt (27)-(29)
+    snowMelt -= stdMin(surfMelt * dt / bulkLHFusionSnow, hs);
+    deltaIce1 = -stdMin(stdMax(-(surfMelt * dt - bulkLHFusionSnow * hs) / e1, 0.), h1);
+    deltaIce2 = -stdMin(stdMax(-(surfMelt * dt - bulkLHFusionSnow * hs + e1 * h1) / e2, 0.), h2);
+    if (h2 + h1 + hs - deltaIce2 - deltaIce1 - snowMelt <= 0.)
+        qio -= stdMax(surfMelt * dt - bulkLHFusionSnow * hs + e1 * h1 + e2 * h2, 0.) / dt; // (30)
+    hs += snowMelt;
+    h1 += deltaIce1;
+    h2 += deltaIce2;
+    topMelt += deltaIce1 + deltaIce2;
+    // snow to ice (35)-(39)
+    const double freeboard = (hice * (kRhoOcean - kRhoIce) - hs * kRhoSnow) / kRhoOcean;
+    if (p.flooding && freeboard < 0.) {
+        hs += stdMin(freeboard * kRhoIce / kRhoSnow, 0.);
+        deltaIce1 = stdMax(-freeboard, 0.);
+        const double f1 = 1 - deltaIce1 / (deltaIce1 + h1);
+        const double tBar = f1 * (tUppr + dHfTf_cp / tUppr) + (1 - f1) * seaIceTf;
+        tUppr = (tBar - std::sqrt(tBar * tBar - 4 * dHfTf_cp)) / 2;
+        h1 += deltaIce1;
+        x[NSDG_IG_SNOW_TO_ICE] += deltaIce1;
+    }
+    double& hi = hice;
+    hi = h1 + h2;
+    // even layers (38)-(40)
+    if (h2 > h1) {
+        const double f1 = h1 / hi * 2;
+        const double tBar = f1 * (tUppr + dHfTf_cp / tUppr) + (1 - f1) * tLowr;
+        tUppr = (tBar - std::sqrt(tBar * tBar - 4 * dHfTf_cp)) / 2;
+    } else {
+        const double f1 = (2 * h1 - hi) / hi;
+        tLowr = f1 * (tUppr + dHfTf_cp / tUppr) + (1 - f1) * tLowr;
+        if (tLowr > seaIceTf) {
+            const double deltaMelt = hi / 4 * kIceCp * (tLowr - seaIceTf) * tUppr
+                / (kLf * tUppr + (kIceCp * tUppr - kLf) * (seaIceTf - tUppr));
+            topMelt -= deltaMelt;
+            botMelt -= deltaMelt;
+            hi -= 2 * deltaMelt;
+            tLowr = seaIceTf;
+        }
+    }
+    double& deltaHi = x[NSDG_IG_DELTA_HICE];
+    const double oldHi = x[NSDG_IG_HICE0];
+    deltaHi = hi - oldHi;
+    if (hi < p.h_min) {
+        qio -= (-bulkLHFusionSnow * hs + (e1 + e2) * hi / 2) / dt;
+        if (deltaHi < 0) {
+            topMelt *= oldHi / deltaHi;
+            botMelt *= oldHi / deltaHi;
+        }
+        x[NSDG_IG_SNOW_TO_ICE] = 0;
+        deltaHi = -oldHi;
+        hi = 0;
+        hs = 0;
+        tSurf = seaIceTf;
+        tUppr = seaIceTf;
+        tLowr = seaIceTf;
+    }
+    x[NSDG_IG_TICE] = tSurf;
+    x[NSDG_IG_TICE_1] = tUppr;
+    x[NSDG_IG_TICE_2] = tLowr;
+}
+
 // IceGrowth::newIceFormation (physics/src/IceGrowth.cpp:201-227)
 void newIceFormation(const Elem& x, double dt)
 {
@@ -243,14 +413,20 @@ void oracle_ice_growth_update(size_t n, const double* mask, const nsdg_ice_growt
         fields[size_t(NSDG_IG_CICE) * n + i] = fields[size_t(NSDG_IG_CICE0) * n + i];
     for (size_t i : ocean)
         initializeThicknessesElement(Elem { fields, n, i });
-    for (size_t i = 0; i < n; ++i)
+    for (size_t i = 0; i < n; ++i) { // IIceThermodynamics::initialiseTice: all levels
         fields[size_t(NSDG_IG_TICE) * n + i] = fields[size_t(NSDG_IG_TICE0) * n + i];
+        fields[size_t(NSDG_IG_TICE_1) * n + i] = fields[size_t(NSDG_IG_TICE0_1) * n + i];
+        fields[size_t(NSDG_IG_TICE_2) * n + i] = fields[size_t(NSDG_IG_TICE0_2) * n + i];
+    }
     for (size_t i : ocean)
         applyLimits(Elem { fields, n, i }, *p, dt);
     if (p->use_thermo) {
         if (p->thermo_model == 0)
             for (size_t i : ocean)
                 thermoIce0(Elem { fields, n, i }, *p, dt);
+        else if (p->thermo_model == 2)
+            for (size_t i : ocean)
+                thermoWinton(Elem { fields, n, i }, *p, dt);
         for (size_t i : ocean) { // updateWrapper (IceGrowth.hpp)
             const Elem x { fields, n, i };
             newIceFormation(x, dt);
@@ -263,14 +439,20 @@ void oracle_ice_growth_update(size_t n, const double* mask, const nsdg_ice_growt
             constantHealing(Elem { fields, n, i }, *p, dt);
 }
 
-// ThermoIce0::update alone on the true thickness slots (hice_updated,
+// The vertical thermodynamics alone (ThermoIce0, or ThermoWinton when
+// thermo_model is 2) on the true thickness slots (hice_updated,
 // cice_updated, hsnow_updated, hice_initial) with tice = tice0 first, as the
 // known-answer test physics/test/ThermoIce0_test.cpp:30-160 drives it.
 void oracle_thermo_ice0(size_t n, const nsdg_ice_growth_params* p, double dt, double* fields)
 {
     for (size_t i = 0; i < n; ++i) {
         fields[size_t(NSDG_IG_TICE) * n + i] = fields[size_t(NSDG_IG_TICE0) * n + i];
-        thermoIce0(Elem { fields, n, i }, *p, dt);
+        fields[size_t(NSDG_IG_TICE_1) * n + i] = fields[size_t(NSDG_IG_TICE0_1) * n + i];
+        fields[size_t(NSDG_IG_TICE_2) * n + i] = fields[size_t(NSDG_IG_TICE0_2) * n + i];
+        if (p->thermo_model == 2)
+            thermoWinton(Elem { fields, n, i }, *p, dt);
+        else
+            thermoIce0(Elem { fields, n, i }, *p, dt);
     }
 }
 

@@ -126,7 +126,8 @@ class IceGrowthParams(ctypes.Structure):
 IG_FIELDS = ("hice", "cice", "hsnow", "tice", "qia", "dqia_dt", "qow", "qio", "sublim", "snowfall", "penSW",
              "sst", "tf", "mlbhc", "damage", "hice_updated", "cice_updated", "hsnow_updated", "hice_initial",
              "hsnow_initial", "newice", "delta_cice", "delta_hice", "tice_updated", "qic", "snow_to_ice",
-             "top_melt", "bottom_melt", "snow_melt", "delta_cfreeze", "delta_cmelt")
+             "top_melt", "bottom_melt", "snow_melt", "delta_cfreeze", "delta_cmelt", "tice_1", "tice_2",
+             "tice_updated_1", "tice_updated_2")
 
 _ig = None
 

@@ -109,7 +109,7 @@ def test_ice_growth_create_validates_arguments(nsdg_lib):
         assert getattr(p, name) == getattr(o, name), name
     assert _lib.ICE_GROWTH_FIELDS == pyoracle.IG_FIELDS
     h = ctypes.c_void_p()
-    for bad in (dict(h0=0.0), dict(healing_time=-1.0), dict(thermo_model=2), dict(ks=float("nan"))):
+    for bad in (dict(h0=0.0), dict(healing_time=-1.0), dict(thermo_model=3), dict(ks=float("nan"))):
         q = default_params(**bad)
         assert nsdg_lib.nsdg_ice_growth_create(4, None, ctypes.byref(q), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG
     assert nsdg_lib.nsdg_ice_growth_create(0, None, ctypes.byref(p), ctypes.byref(h)) == _lib.NSDG_ERR_BAD_ARG

@@ -1,5 +1,5 @@
-"""GPU column thermodynamics (IceGrowth + ThermoIce0 + HiblerSpread +
-ConstantHealing) against the CPU oracle, through the C ABI.
+"""GPU column thermodynamics (IceGrowth + ThermoIce0 or ThermoWinton +
+HiblerSpread + ConstantHealing) against the CPU oracle, through the C ABI.
 
 The bar is bit-identity: the kernel is element-local FP64 arithmetic in the
 reference's operation order, compiled without fused multiply-adds, so every
@@ -16,7 +16,7 @@ from nextsimdg_gb300._lib import NSDG_ERR_UNKNOWN_FIELD
 pytestmark = pytest.mark.gpu
 
 INPUTS = ("hice", "cice", "hsnow", "tice", "qia", "dqia_dt", "qow", "qio", "sublim", "snowfall", "penSW", "sst",
-          "tf", "mlbhc", "damage")
+          "tf", "mlbhc", "damage", "tice_1", "tice_2")
 
 
 def _inputs(n, rng, po):
@@ -39,7 +39,8 @@ def _inputs(n, rng, po):
                 dqia_dt=rng.uniform(0.0, 30.0, n), qow=rng.uniform(-200.0, 400.0, n), qio=qio,
                 sublim=rng.uniform(-1e-5, 1e-5, n), snowfall=rng.uniform(0.0, 1e-4, n) * (rng.random(n) < 0.5),
                 penSW=rng.uniform(0.0, 50.0, n), sst=tf + rng.uniform(-0.2, 2.0, n), tf=tf,
-                mlbhc=4186.84e3 * rng.uniform(5.0, 50.0, n), damage=rng.uniform(0.0, 1.0, n))
+                mlbhc=4186.84e3 * rng.uniform(5.0, 50.0, n), damage=rng.uniform(0.0, 1.0, n),
+                tice_1=rng.uniform(-25.0, -0.5, n), tice_2=rng.uniform(-15.0, -0.3, n))
 
 
 def _pair(n, mask, oracle_mod, **params):
@@ -56,7 +57,7 @@ def _compare_all(g, o):
 
 @pytest.mark.parametrize("params", [
     {}, dict(thermo_model=1), dict(lateral_model=1), dict(healing_model=1), dict(use_thermo=0),
-    dict(flooding=0), dict(thermo_model=1, lateral_model=1)])
+    dict(flooding=0), dict(thermo_model=1, lateral_model=1), dict(thermo_model=2), dict(thermo_model=2, flooding=0)])
 def test_ice_growth_bitwise_equals_oracle(gpu, oracle, params):
     from oracle import pyoracle as po
     rng = np.random.default_rng(4)
@@ -76,11 +77,15 @@ def test_ice_growth_bitwise_equals_oracle(gpu, oracle, params):
                 k.setData("hsnow", k.getData("hsnow_updated") * c)
                 k.setData("cice", c)
                 k.setData("tice", k.getData("tice_updated"))
+                k.setData("tice_1", k.getData("tice_updated_1"))
+                k.setData("tice_2", k.getData("tice_updated_2"))
         g.update(dt)
         o.update(dt)
         _compare_all(g, o)
     if params.get("use_thermo", 1):
         assert np.count_nonzero(g.getData("newice")) > 100
+    if params.get("thermo_model") == 2:
+        assert np.all(np.isfinite(g.getData("tice_updated_1")))
     if not params:
         assert np.count_nonzero(g.getData("snow_to_ice")) > 10
         assert np.count_nonzero(g.getData("delta_cmelt")) > 100

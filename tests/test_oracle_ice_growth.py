@@ -1,7 +1,8 @@
 """The column-thermodynamics oracle (oracle/ice_growth_oracle.cpp) against the
-reference's own known-answer tests of IceGrowth, ThermoIce0 and
+reference's own known-answer tests of IceGrowth, ThermoIce0, ThermoWinton and
 ConstantHealing (physics/test/IceGrowth_test.cpp, ThermoIce0_test.cpp,
-DamageHealing_test.cpp), with doctest's Approx semantics:
+ThermoWintonTemperature_test.cpp, DamageHealing_test.cpp), with doctest's
+Approx semantics:
 |a - b| < eps (1 + max(|a|, |b|)).
 
 The inputs are those the tests set through their boundary modules:
@@ -134,3 +135,32 @@ def test_constant_healing_time_scale():
     """DamageHealing_test.cpp:17-64: 0.5 -> 0.55, 0.99 -> 1 (capped)."""
     assert approx(po.constant_healing(0.5, 0.5, 0.0, 86400.0, 20 * 86400.0), 0.55, 1e-8)
     assert po.constant_healing(0.99, 0.5, 0.0, 86400.0, 20 * 86400.0) == 1.0
+
+
+@pytest.mark.parametrize("case,expect", [
+    ("melting", (0.0, -0.999261, -0.275)), ("freezing", (-10.5129, -9.00726, -8.20454))])
+def test_thermo_winton_temperatures(case, expect):
+    """ThermoWintonTemperature_test.cpp:32-233: ThermoWinton alone for 600 s on
+    true thicknesses 0.2 m ice, 0.02 m snow; UniformOcean(sst, 32 PSU,
+    4.29151e7 / (rho_w cp_w)); the three temperature levels."""
+    t0, qio, qia, dqia, subl, pensw = {
+        "melting": (-1.0, 53717.8, -85.6364, 19.7016, -7.3858e-06, 1.04125),
+        "freezing": (-9.0, 73.9465, 42.2955, 16.7615, 2.15132e-6, 0.0)}[case]
+    g = po.OracleIceGrowth(1, thermo_model=2)
+    for k, v in dict(cice_updated=0.5, hice_updated=0.2, hice_initial=0.2, hsnow_updated=0.02, tice=t0, tice_1=t0,
+                     tice_2=t0, tf=po.unesco_freezing(32.0), qio=qio, qia=qia, dqia_dt=dqia, sublim=subl,
+                     penSW=pensw).items():
+        g.setData(k, v)
+    g.thermo_only(600.0)
+    got = [g.getData(n)[0] for n in ("tice_updated", "tice_updated_1", "tice_updated_2")]
+    assert all(approx(a, b) for a, b in zip(got, expect)), got
+
+
+def test_thermo_winton_no_ice():
+    """ThermoWintonTemperature_test.cpp:235-346: no ice stays no ice."""
+    g = po.OracleIceGrowth(1, thermo_model=2)
+    for k, v in dict(cice=0.0, hice=0.0, hsnow=0.0, tice=0.0, sst=1.75, tf=po.unesco_freezing(32.0),
+                     mlbhc=4.29151e7, qow=143.266, qia=42.2955, dqia_dt=16.7615, sublim=2.15132e-6).items():
+        g.setData(k, v)
+    g.update(600.0)
+    assert g.getData("hice_updated")[0] == 0.0 and g.getData("cice_updated")[0] == 0.0
