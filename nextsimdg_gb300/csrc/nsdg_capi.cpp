@@ -119,6 +119,7 @@ struct nsdg_kernel {
     StressMaps maps32 {};
     float* hP32 = nullptr; // P/(2 alpha) at the Gauss points (mixed precision)
     float *cellX32 = nullptr, *cellY32 = nullptr; // FP32 transport cell operators (mixed precision)
+    float* jwA32 = nullptr; // FP32 J w at the advection Gauss points (mixed-precision CG2DG)
     float2* invmHL = nullptr; // inverse lumped CG2 mass as {hi, lo} floats (mixed precision)
     BbmOps32 bbm32 {};        // FP32 BBM operators (mixed precision BBM)
     float *cellX8_32 = nullptr, *cellY8_32 = nullptr; // FP32 DG8 stress-transport operators
@@ -367,13 +368,16 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
     if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
         add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
+        add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
         add(18 * N, 4);
-        for (int i = 0; i < 12; ++i) add(Ncg, 4);
+        for (int i = 0; i < 9; ++i) add(Ncg, 4);  // FP32 node state
+        add(2 * Ncg, 4);                          // (1 / lumped mass) / c1 as {hi, lo}
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
     }
     if (P.precision == NSDG_PRECISION_MIXED) {
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
+        add(ops.jwA.size(), 4);                             // FP32 J w of the CG2DG quadrature
         add(Ncg, 8);                                        // inverse lumped mass {hi, lo}
     }
     if (P.precision == NSDG_PRECISION_MIXED && bbm) {
@@ -512,6 +516,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (mixed()) {
         cellX32 = upf(ops.cellX);
         cellY32 = upf(ops.cellY);
+        jwA32 = upf(ops.jwA);
         std::vector<float2> hl(Ncg);
         for (size_t i = 0; i < Ncg; ++i) {
             const float hi = static_cast<float>(invm[i]);
@@ -593,10 +598,10 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             return p;
         };
         tdiv32 = zf(18 * N);
-        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.A, &st32.uo, &st32.vo, &st32.c1b,
-            &st32.rhfc, &st32.c1beta, &st32.ku, &st32.kv };
+        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.uo, &st32.vo, &st32.a, &st32.ku, &st32.kv };
         for (float** q : f32)
             *q = zf(Ncg);
+        st32.im = reinterpret_cast<float2*>(zf(2 * Ncg));
         tdivLast = zf(18 * N);
         uLast = zf(Ncg);
         vLast = zf(Ncg);
@@ -695,7 +700,10 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
     {
         const double* cgv[2] = { bbm ? avgU : u, bbm ? avgV : v };
         double* dgv[2] = { velx, vely };
-        LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minvP ? dops.minvP : dops.minv, 2, cgv, dgv));
+        if (mixed() && jwA32)
+            LCH(launchCG2DG32(s, dm, dg, jwA32, dops.minvP ? dops.minvP : dops.minv, cgv, dgv));
+        else
+            LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minvP ? dops.minvP : dops.minv, 2, cgv, dgv));
         LCH(launchNormalVelocity(s, dm, dg, velx, vely, nvX, nvY));
         StageFields a, b;
         const int nf = bbm ? 3 : 2;
@@ -763,10 +771,12 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         const MevpParams mp = mevpParams(dt);
         MevpNodeState st { u, v, u0, v0, cgH, cgA, uo, vo, ua, va, uGrad, vGrad, c1, c1b, fau, fav, rhfc, gu, gv };
         if (prep) {
-            LCH(launchMevpPrepNodes(s, dm, st, mp));
+            // the mixed path forms its FP32 node constants in one kernel
+            if (!mixed())
+                LCH(launchMevpPrepNodes(s, dm, st, mp));
             LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp, mixed() ? hP32 : nullptr));
             if (mixed())
-                LCH(launchMevpPrepNodes32(s, dm, st, st32, P.beta));
+                LCH(launchMevpPrepNodes32(s, dm, st, st32, dops.invm2, mp));
         }
         if (loop && mixed()) {
             const int sv = saveLast(s, nullptr, nullptr, nullptr);
@@ -781,7 +791,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
                     LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
                 } else {
                     LCH(launchStress32(s, mp, derr));
-                    LCH(launchMevpMomentum32(s, dm, invmHL, st32, tdiv32, mp, derr));
+                    LCH(launchMevpMomentum32(s, dm, st32, tdiv32, mp, derr));
                 }
             }
         }
@@ -812,7 +822,7 @@ int nsdg_kernel::mixedIterations(cudaStream_t s, double dt, int count, int* errW
     for (int it = 0; it < count; ++it) {
         cudaError_t e = launchStress32(s, mp, errWord);
         if (e == cudaSuccess)
-            e = launchMevpMomentum32(s, dm, invmHL, st32, tdiv32, mp, errWord);
+            e = launchMevpMomentum32(s, dm, st32, tdiv32, mp, errWord);
         if (e != cudaSuccess)
             return fail(NSDG_ERR_CUDA, std::string("mEVP iteration: ") + cudaGetErrorString(e));
         launches += 2;
@@ -1636,7 +1646,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                        : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
             if (!bbm && k->mixed())
-                return launchMevpMomentum32(k->stream, k->dm, k->invmHL, k->st32, k->tdiv32, mp, k->derr);
+                return launchMevpMomentum32(k->stream, k->dm, k->st32, k->tdiv32, mp, k->derr);
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr,
                              k->mixed() ? k->invmHL : nullptr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
@@ -1926,7 +1936,6 @@ struct nsdg_ensemble {
         d.ice = k->dm.ice;
         d.cg2Dir = k->dm.cg2Dir;
         d.invm2 = k->dops.invm2;
-        d.invmHL = k->invmHL;
         d.o = k->dops32;
         d.st = k->st32;
         d.Pg = k->Pg;

@@ -62,6 +62,7 @@ struct ConstTables32 {
     float psi[4][8][16];
     float psie[4][3][3];
     float psiew[4][4][3][8];
+    float phi2[4][9][16];
 };
 
 // The structured quad mesh with arbitrary vertex positions (ParametricMesh).

@@ -37,6 +37,10 @@ cudaError_t uploadConstTables()
                 for (int c = 0; c < 3; ++c)
                     for (int d = 0; d < 8; ++d)
                         host32.psiew[a][b][c][d] = static_cast<float>(host.psiew[a][b][c][d]);
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 9; ++b)
+                for (int c = 0; c < 16; ++c)
+                    host32.phi2[a][b][c] = static_cast<float>(host.phi2[a][b][c]);
         filled = true;
     }
     const cudaError_t e = cudaMemcpyToSymbol(cT, &host, sizeof(ConstTables));
@@ -90,6 +94,63 @@ __global__ void __launch_bounds__(kBlock) kCG2DG(int nx, size_t N, const double*
             for (int q = 0; q < QQ; ++q)
                 a += cT.psi[Q][i][q] * t[q];
             r[i] = a;
+        }
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            double a = 0.0;
+#pragma unroll
+            for (int k = 0; k < DG; ++k)
+                a += minv[(i * DG + k) * N + e] * r[k];
+            out[f][i * N + e] = a;
+        }
+    }
+}
+
+// The same projection for the mixed-precision transport velocity: the CG2
+// values at the Gauss points and the weighted moments against the DG basis in
+// FP32 (jw32: FP32 copy of J w), the inverse mass matrix applied in FP64.
+template <int DG, int NF>
+__global__ void __launch_bounds__(kBlock) kCG2DG32(int nx, size_t N, const float* __restrict__ jw32,
+    const double* __restrict__ minv, const double* __restrict__ cg0, const double* __restrict__ cg1,
+    double* __restrict__ out0, double* __restrict__ out1)
+{
+    constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q;
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    const size_t s2 = 2 * size_t(nx) + 1;
+    const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx);
+    const size_t iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
+    const size_t base = 2 * s2 * iy + 2 * ix;
+    const double* cg[2] = { cg0, cg1 };
+    double* out[2] = { out0, out1 };
+    float w[QQ];
+#pragma unroll
+    for (int q = 0; q < QQ; ++q)
+        w[q] = jw32[q * N + e];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        float loc[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+            loc[j] = static_cast<float>(cg[f][base + (j % 3) + (j / 3) * s2]);
+        float t[QQ];
+#pragma unroll
+        for (int q = 0; q < QQ; ++q) {
+            float v = 0.f;
+#pragma unroll
+            for (int j = 0; j < 9; ++j)
+                v = fmaf(cT32.phi2[Q][j][q], loc[j], v);
+            t[q] = w[q] * v;
+        }
+        double r[DG];
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            float a = 0.f;
+#pragma unroll
+            for (int q = 0; q < QQ; ++q)
+                a = fmaf(cT32.psi[Q][i][q], t[q], a);
+            r[i] = static_cast<double>(a);
         }
 #pragma unroll
         for (int i = 0; i < DG; ++i) {
@@ -1061,25 +1122,39 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
 // ===========================================================================
 // mEVP, mixed precision
 // ===========================================================================
-__global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f, double beta)
+__global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f,
+    const double* __restrict__ invm2, MevpParams p)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
         return;
-    const float u = static_cast<float>(st.u[i]), v = static_cast<float>(st.v[i]);
-    f.u[i] = u;
-    f.v[i] = v;
-    f.u0[i] = u;
-    f.v0[i] = v;
-    f.A[i] = static_cast<float>(st.cgA[i]);
+    // clamps of prepareIteration (CGDynamicsKernel.cpp:273-275)
+    const double A = fmax(fmin(st.cgA[i], 1.0), 1.e-4);
+    const double H = fmax(st.cgH[i], 1.e-4);
+    st.cgA[i] = A;
+    st.cgH[i] = H;
+    const double u = st.u[i], v = st.v[i];
+    st.u0[i] = u;
+    st.v0[i] = v;
+    // c1 = rho H / dt and its reciprocal: one FP64 division per node
+    const double rhoH = p.rho_ice * H;
+    const double rc1 = p.dt / rhoH;
+    const double ua = st.ua[i], va = st.va[i];
+    const double fatm = p.F_atm * sqrt(ua * ua + va * va);
+    const float uf = static_cast<float>(u), vf = static_cast<float>(v);
+    f.u[i] = uf;
+    f.v[i] = vf;
+    f.u0[i] = uf;
+    f.v0[i] = vf;
     f.uo[i] = static_cast<float>(st.uo[i]);
     f.vo[i] = static_cast<float>(st.vo[i]);
-    f.c1b[i] = static_cast<float>(st.c1b[i]);
-    f.rhfc[i] = static_cast<float>(st.rhfc[i]);
-    // the iteration-independent parts of the momentum update, formed in FP64
-    f.c1beta[i] = static_cast<float>(st.c1[i] * beta);
-    f.ku[i] = static_cast<float>(st.c1[i] * st.u[i] + st.cgA[i] * st.fau[i] - st.gu[i]);
-    f.kv[i] = static_cast<float>(st.c1[i] * st.v[i] + st.cgA[i] * st.fav[i] - st.gv[i]);
+    f.a[i] = static_cast<float>(A * rc1);
+    // u0 + (A F_atm |wind| uwind - rho H g dxSSH) / c1, in FP64
+    f.ku[i] = static_cast<float>(u + (A * (fatm * ua) - rhoH * p.gravity * st.uGrad[i]) * rc1);
+    f.kv[i] = static_cast<float>(v + (A * (fatm * va) - rhoH * p.gravity * st.vGrad[i]) * rc1);
+    const double im = invm2[i] * rc1;
+    const float hi = static_cast<float>(im);
+    f.im[i] = make_float2(hi, static_cast<float>(im - static_cast<double>(hi)));
 }
 
 // The FP64 kernel kMevpStress with FP32 operators and state.  The strain
@@ -1615,8 +1690,7 @@ __global__ void kViscositySelfTest(size_t n, const float* __restrict__ inv, cons
 
 // Body of the mixed-precision node kernel for CG2 node i.
 __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, size_t i, const uint8_t* __restrict__ cg2Dir,
-    const float2* __restrict__ invmHL, const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p,
-    int* __restrict__ err)
+    const MevpNodeState32& st, const float* __restrict__ tdiv, const MevpParams& p, int* __restrict__ err)
 {
     // 32-bit index arithmetic (node counts stay far below 2^31)
     const unsigned s2 = 2u * static_cast<unsigned>(nx) + 1u;
@@ -1624,9 +1698,8 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     const bool dir = cg2Dir[i] != 0;
     // per-step constants first (a programmatic dependent launch overlaps
     // them with the stress kernel's tail), then the wait for its results
-    const float2 im = invmHL[i];
-    const float uo = st.uo[i], vo = st.vo[i], A = st.A[i];
-    const float c1b = st.c1b[i], c1beta = st.c1beta[i], rhfc = st.rhfc[i], ku = st.ku[i], kv = st.kv[i];
+    const float2 im = st.im[i];
+    const float uo = st.uo[i], vo = st.vo[i], a = st.a[i], ku = st.ku[i], kv = st.kv[i];
     asm volatile("griddepcontrol.wait;" ::: "memory");
     float dSx = 0.f, dSy = 0.f;
     if (!dir) {
@@ -1648,20 +1721,17 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
             }
         }
     }
-    // divided by the lumped mass: its FP64 inverse held as the unevaluated sum
-    // hi + lo of two floats (48 significant bits), applied with FP32 FMAs
+    // the divergence over the lumped mass and c1: that factor is FP64, held
+    // as the unevaluated sum hi + lo of two floats and applied with FP32 FMAs
     const float mx = fmaf(dSx, im.y, dSx * im.x);
     const float my = fmaf(dSy, im.y, dSy * im.x);
     const float u = st.u[i], v = st.v[i];
     const float uOcnRel = uo - u, vOcnRel = v - vo;
-    const float absocn = sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel);
-    const float focn = p.F_oceanf * absocn;
-    const float rden = 1.0f / (c1b + A * focn);
-    const float Afocn = A * focn;
-    // c1 (beta u + u0) + A (fau + focn uo) - rhfc u - gu + mx, with the
-    // iteration-independent part ku = c1 u0 + A fau - gu formed once per step
-    float un = rden * (c1beta * u + ku + Afocn * uo - rhfc * u + mx);
-    float vn = rden * (c1beta * v + kv + Afocn * vo + rhfc * v + my);
+    const float afocn = a * (p.F_oceanf * sqrtf(uOcnRel * uOcnRel + vOcnRel * vOcnRel));
+    const float rden = 1.0f / (p.onePlusBetaf + afocn);
+    // (beta u + ku + a focn uo - fc dt u + mx) / (1 + beta + a focn), VPCGDynamicsKernel.hpp:132-172 over c1
+    float un = rden * (p.betaf * u + ku + afocn * uo - p.fcdtf * u + mx);
+    float vn = rden * (p.betaf * v + kv + afocn * vo + p.fcdtf * v + my);
     if (!isfinite(un) || !isfinite(vn))
         atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
     if (dir) {
@@ -1672,13 +1742,13 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     st.v[i] = vn;
 }
 
-__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, const float2* __restrict__ invmHL,
-    MevpNodeState32 st, const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
+__global__ void __launch_bounds__(kBlock) kMevpMomentum32(DevMesh m, MevpNodeState32 st,
+    const float* __restrict__ tdiv, MevpParams p, int* __restrict__ err)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= m.Ncg)
         return;
-    mevpMomentum32Node(m.nx, m.ny, m.N, i, m.cg2Dir, invmHL, st, tdiv, p, err);
+    mevpMomentum32Node(m.nx, m.ny, m.N, i, m.cg2Dir, st, tdiv, p, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1745,7 +1815,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleM
     const size_t i = (static_cast<size_t>(blockIdx.x) - M.nodeBlock0) * kBlock + threadIdx.x;
     if (i >= M.Ncg)
         return;
-    mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.invmHL, M.st, M.tdiv, p, err);
+    mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.st, M.tdiv, p, err);
 }
 
 __global__ void kWidenVelocity(size_t n, const float* __restrict__ u32, const float* __restrict__ v32,
@@ -2176,6 +2246,14 @@ cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* 
     return cudaGetLastError();
 }
 
+cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float* jw32, const double* minv,
+    const double* const* cg, double* const* out)
+{
+    const unsigned g = blocksFor(m.N);
+    NSDG_DG_SWITCH(dg, (kCG2DG32<D, 2><<<g, kBlock, 0, s>>>(m.nx, m.N, jw32, minv, cg[0], cg[1], out[0], out[1])));
+    return cudaGetLastError();
+}
+
 cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
     const double* vely, double* nvX, double* nvY)
 {
@@ -2271,9 +2349,9 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 }
 
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32, double beta)
+    const MevpNodeState32& st32, const double* invm2, const MevpParams& p)
 {
-    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, beta);
+    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, invm2, p);
     return cudaGetLastError();
 }
 namespace {
@@ -2391,7 +2469,7 @@ cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32&
     kMevpStress32<<<blocksFor(m.N, kStressElems), kStressElems * kStressParts, 0, s>>>(m, o, u, v, Pg, hP, tdiv, p);
     return cudaGetLastError();
 }
-cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2* invmHL, const MevpNodeState32& st,
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const MevpNodeState32& st,
     const float* tdiv, const MevpParams& pIn, int* err)
 {
     const MevpParams p = withDerived(pIn);
@@ -2404,7 +2482,7 @@ cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2*
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kMevpMomentum32, m, invmHL, st, tdiv, p, err);
+    return cudaLaunchKernelEx(&cfg, kMevpMomentum32, m, st, tdiv, p, err);
 }
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& pIn)

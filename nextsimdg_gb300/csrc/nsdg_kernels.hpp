@@ -91,6 +91,11 @@ struct StageFields {
 // Uses jw/minv for `dg` components (jwA/minv, or jw3/minv8 for dg == 8).
 cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* jw,
     const double* minv, int nf, const double* const* cg, double* const* out);
+// CG2DG of two fields with FP32 quadrature (jw32: J w at the advection Gauss
+// points in FP32) and the FP64 inverse mass matrix (the mixed-precision
+// transport velocity).
+cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float* jw32, const double* minv,
+    const double* const* cg, double* const* out);
 // Edge normal velocities (DGTransport.cpp:158-252).
 cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
     const double* vely, double* nvX, double* nvY);
@@ -142,6 +147,7 @@ struct MevpParams {
     // GB300) on a division or a square of the parameters
     double keepd = 0;                          // 1 - 1/alpha
     float keep = 0, dmin2f = 0, F_oceanf = 0;  // FP32 copies (dmin2f: DeltaMin^2)
+    float betaf = 0, onePlusBetaf = 0, fcdtf = 0; // beta, 1 + beta, fc dt
 };
 inline MevpParams withDerived(MevpParams p)
 {
@@ -149,6 +155,9 @@ inline MevpParams withDerived(MevpParams p)
     p.keep = static_cast<float>(p.keepd);
     p.dmin2f = static_cast<float>(p.DeltaMin * p.DeltaMin);
     p.F_oceanf = static_cast<float>(p.F_ocean);
+    p.betaf = static_cast<float>(p.beta);
+    p.onePlusBetaf = static_cast<float>(1.0 + p.beta);
+    p.fcdtf = static_cast<float>(p.fc * p.dt);
     return p;
 }
 cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st,
@@ -202,23 +211,33 @@ cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* 
 // kMevpStress32 with the operator tiles staged in shared memory by TMA.
 cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const StressMaps& maps, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int* err);
+// The mixed-precision node state.  The momentum update is divided through by
+// c1 = rho H / dt, so that per node it needs only
+//   u_new = (beta u + ku + a F_ocean |u_o - u| u_o - fc dt u + im dSx)
+//           / (1 + beta + a F_ocean |u_o - u|)
+// (and likewise v with +fc dt v), with the per-step constants
+//   a = A / c1,  ku = u0 + (A F_atm |wind| uwind - rho H g dxSSH) / c1,
+//   im = (1 / lumped mass) / c1
+// formed in FP64 (im kept as the unevaluated sum hi + lo of two floats).
 struct MevpNodeState32 {
     float* u;
     float* v;
     float* u0;
     float* v0;
-    float* A;
     float* uo;
     float* vo;
-    float* c1b;     // rho H / dt (1 + beta)
-    float* rhfc;    // rho H fc
-    float* c1beta;  // rho H / dt * beta
-    float* ku;      // rho H / dt u0 + A F_atm |wind| uwind - rho H g dxSSH (formed in FP64)
+    float* a;
+    float* ku;
     float* kv;
+    float2* im;
 };
-// after launchMevpPrepNodes: FP32 copies of the per-step node constants
+// The per-step node preparation of the mixed path (prepareIteration's clamps,
+// CGDynamicsKernel.cpp:260-276, and the constants of updateMomentum,
+// VPCGDynamicsKernel.hpp:132-172): FP64 inputs, the FP32 state above; the
+// clamped cgA, cgH and u0, v0 are written back in FP64.  invm2: the FP64
+// inverse lumped CG2 mass.
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32, double beta);
+    const MevpNodeState32& st32, const double* invm2, const MevpParams& p);
 // kMevpStress32 for parallelogram meshes: the unit-square operators
 // (G_xi, G_eta [q][j], A_xi, A_eta [j][q]) in constant memory, uploaded once
 // per device (they depend only on the basis), and 5 coefficients per element
@@ -233,8 +252,7 @@ cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, 
     float* out);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
-// invmHL: the FP64 inverse lumped mass as float2 {hi, lo}, hi + lo = 1/m to 48 bits
-cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m, const float2* invmHL,
+cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m,
     const MevpNodeState32& st, const float* tdiv, const MevpParams& p, int* err);
 // One member of a batched ensemble (device-resident table entry).
 struct EnsembleMember {
@@ -243,7 +261,6 @@ struct EnsembleMember {
     const uint8_t* ice;
     const uint8_t* cg2Dir;
     const double* invm2;
-    const float2* invmHL;
     DevOps32 o;
     MevpNodeState32 st;
     const double* Pg;
