@@ -291,6 +291,41 @@ __global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const doubl
 }
 
 // ===========================================================================
+// float <-> double on the integer pipe (GB300 issues FP64 instructions, the
+// conversions among them, at about 1/60 of its FP32 rate).  Round to nearest
+// (ties away from zero); magnitudes below the smallest normal float become a
+// signed zero; infinities and NaNs are kept.
+// ===========================================================================
+__device__ __forceinline__ float narrowAny(double d)
+{
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+    const unsigned long long mag = b & 0x7fffffffffffffffull;
+    const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
+    if (mag < (897ull << 52))
+        return __uint_as_float(sign);
+    if (mag >= 0x47effffff0000000ull) // beyond the largest float (or inf / NaN)
+        return __uint_as_float(sign | (mag > 0x7ff0000000000000ull ? 0x7fc00000u : 0x7f800000u));
+    return __uint_as_float(sign | static_cast<unsigned>((mag - (896ull << 52) + (1ull << 28)) >> 29));
+}
+__device__ __forceinline__ double widenAny(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned mag = u & 0x7fffffffu;
+    const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+    if (mag < 0x00800000u)
+        return __longlong_as_double(static_cast<long long>(sign));
+    if (mag >= 0x7f800000u)
+        return __longlong_as_double(static_cast<long long>(
+            sign | 0x7ff0000000000000ull | (mag > 0x7f800000u ? 0x8000000000000ull : 0ull)));
+    return __longlong_as_double(static_cast<long long>(sign | ((static_cast<unsigned long long>(mag) << 29)
+        + (896ull << 52))));
+}
+template <class T> __device__ __forceinline__ T toT(double x) { return x; }
+template <> __device__ __forceinline__ float toT<float>(double x) { return narrowAny(x); }
+template <class T> __device__ __forceinline__ double fromT(T x) { return x; }
+template <> __device__ __forceinline__ double fromT<float>(float x) { return widenAny(x); }
+
+// ===========================================================================
 // DG transport operator + Runge-Kutta stage  (DGTransport.cpp:278-566)
 // ===========================================================================
 template <int DG> struct Cell {
@@ -334,7 +369,10 @@ __device__ __forceinline__ void loadCell(const double* __restrict__ p, size_t N,
         out[j] = p[j * N + c];
 }
 
-template <int DG> __device__ __forceinline__ void limitMax(double* r, double mx)
+// The DG6 limiters evaluate the Gauss-point values in T (FP32 for the mixed
+// transport: the coefficients narrowed on the integer pipe); the limited
+// coefficients and the scaling stay FP64.
+template <int DG, class T = double> __device__ __forceinline__ void limitMax(double* r, double mx)
 {
     if constexpr (DG == 1) {
         r[0] = fmin(r[0], mx);
@@ -347,24 +385,28 @@ template <int DG> __device__ __forceinline__ void limitMax(double* r, double mx)
         }
     } else if constexpr (DG == 6) {
         r[0] = fmin(mx, r[0]);
-        double mv = -INFINITY;
+        T rt[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+            rt[j] = toT<T>(r[j]);
+        T mv = T(-INFINITY);
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            double s = 0.0;
+            T s = T(0);
 #pragma unroll
             for (int j = 0; j < 6; ++j)
-                s += r[j] * cT.psi[3][j][q];
+                s += rt[j] * tab<T>::psi(3, j, q);
             mv = fmax(mv, s);
         }
-        if (mv > mx) {
-            const double f = (mx - r[0]) / (mv - r[0]);
+        if (fromT<T>(mv) > mx) {
+            const double f = (mx - r[0]) / (fromT<T>(mv) - r[0]);
 #pragma unroll
             for (int j = 1; j < 6; ++j)
                 r[j] *= f;
         }
     }
 }
-template <int DG> __device__ __forceinline__ void limitMin(double* r, double mn)
+template <int DG, class T = double> __device__ __forceinline__ void limitMin(double* r, double mn)
 {
     if constexpr (DG == 1) {
         r[0] = fmax(r[0], mn);
@@ -377,17 +419,21 @@ template <int DG> __device__ __forceinline__ void limitMin(double* r, double mn)
         }
     } else if constexpr (DG == 6) {
         r[0] = fmax(mn, r[0]);
-        double mv = INFINITY;
+        T rt[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+            rt[j] = toT<T>(r[j]);
+        T mv = T(INFINITY);
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            double s = 0.0;
+            T s = T(0);
 #pragma unroll
             for (int j = 0; j < 6; ++j)
-                s += r[j] * cT.psi[3][j][q];
+                s += rt[j] * tab<T>::psi(3, j, q);
             mv = fmin(mv, s);
         }
-        if (mv < mn) {
-            const double f = (r[0] - mn) / (mv - r[0]);
+        if (fromT<T>(mv) < mn) {
+            const double f = (r[0] - mn) / (fromT<T>(mv) - r[0]);
 #pragma unroll
             for (int j = 1; j < 6; ++j)
                 r[j] *= f;
@@ -445,7 +491,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         loadCell<DG>(f.src[k], N, c, own[k]);
 #pragma unroll
         for (int j = 0; j < DG; ++j) {
-            ownT[k][j] = static_cast<T>(own[k][j]);
+            ownT[k][j] = toT<T>(own[k][j]);
             acc[k][j] = T(0);
         }
     }
@@ -457,8 +503,8 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
             T vx[DG], vy[DG];
 #pragma unroll
             for (int j = 0; j < DG; ++j) {
-                vx[j] = static_cast<T>(a.velx[j * N + c]);
-                vy[j] = static_cast<T>(a.vely[j * N + c]);
+                vx[j] = toT<T>(a.velx[j * N + c]);
+                vy[j] = toT<T>(a.vely[j * N + c]);
             }
 #pragma unroll
             for (int q = 0; q < QQ; ++q) {
@@ -503,12 +549,12 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
     auto loadNb = [&](const double* src, size_t cc) {
 #pragma unroll
         for (int j = 0; j < DG; ++j)
-            nb[j] = static_cast<T>(src[j * N + cc]);
+            nb[j] = toT<T>(src[j * N + cc]);
     };
     auto loadNv = [&](const double* nvp, size_t ne, size_t e) {
 #pragma unroll
         for (int k = 0; k < ED; ++k)
-            nv[k] = static_cast<T>(nvp[k * ne + e]);
+            nv[k] = toT<T>(nvp[k * ne + e]);
     };
     // left Y-edge (this cell is "cell 2"), interior edges only
     if (ix >= 1) {
@@ -582,8 +628,8 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
             T b1[DG], b2[DG];
 #pragma unroll
             for (int j = 0; j < DG; ++j) {
-                b1[j] = static_cast<T>(f.src[k][j * N + p1]);
-                b2[j] = static_cast<T>(f.src[k][j * N + p2]);
+                b1[j] = toT<T>(f.src[k][j * N + p1]);
+                b2[j] = toT<T>(f.src[k][j * N + p2]);
             }
             if (type == 0) {
                 traceTop<DG, T>(b1, t1);
@@ -640,7 +686,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
             double s = 0.0;
 #pragma unroll
             for (int j = 0; j < DG; ++j)
-                s += Mi[i * DG + j] * static_cast<double>(acc[k][j]);
+                s += Mi[i * DG + j] * fromT<T>(acc[k][j]);
             r[i] = s;
         }
         switch (a.mode) {
@@ -678,9 +724,9 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
             break;
         }
         if (f.lmax[k])
-            limitMax<DG>(out, f.vmax[k]);
+            limitMax<DG, T>(out, f.vmax[k]);
         if (f.lmin[k])
-            limitMin<DG>(out, f.vmin[k]);
+            limitMin<DG, T>(out, f.vmin[k]);
 #pragma unroll
         for (int i = 0; i < DG; ++i)
             f.dst[k][i * N + c] = out[i];
