@@ -69,11 +69,13 @@ def bytes_per_element_iteration_stress(word: int = 8, spherical: bool = False, p
     element: the strain operators G_x, G_y and the divergence operators A_1,
     A_2 (4 x 81 words; on a parallelogram mesh the FP32 kernel reads 5 FP32
     coefficients instead), the pressure terms at the 9 Gauss points (FP64
-    P/alpha; in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha)), the
+    P/alpha; in the FP32 kernels FP64 P/(8 alpha) and FP32 P/(2 alpha), the
+    latter formed in-kernel by the parallelogram kernel), the
     18 divergence coefficients read and written, and the CG2 velocity counted
     once per node (about 4 nodes per element, u and v)."""
     operators = 5 * 4 if parallelogram else (6 if spherical else 4) * 81 * word  # + G_m, A_3 on a sphere
-    pressure = 9 * 8 + (9 * 4 if word == 4 else 0)
+    # the parallelogram kernel forms P/(2 alpha) from P/(8 alpha) (an exact x4)
+    pressure = 9 * 8 + (9 * 4 if word == 4 and not parallelogram else 0)
     tdiv = 2 * 18 * word
     velocity = 4 * 2 * word
     return operators + pressure + tdiv + velocity

@@ -136,7 +136,7 @@ struct nsdg_kernel {
     {
         const int kind = variant < 0 ? stressKind : variant;
         if (kind == 2 && affCoef)
-            return launchMevpStress32Affine(s, dm, affCoef, affLd, st32.u, st32.v, Pg, hP32, tdiv32, mp,
+            return launchMevpStress32Affine(s, dm, affCoef, affLd, st32.u, st32.v, Pg, tdiv32, mp,
                 vm < 0 ? viscMode : vm);
         return kind == 1 ? launchMevpStress32Tma(s, dm, maps32, st32.u, st32.v, Pg, hP32, tdiv32, mp, errWord)
                          : launchMevpStress32(s, dm, dops32, st32.u, st32.v, Pg, hP32, tdiv32, mp);

@@ -1659,8 +1659,8 @@ __device__ __forceinline__ void affineDivergence(float (*fs)[9][kAffElems], int 
 template <int VM>
 __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __restrict__ ice,
     const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
-    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, const MevpParams& p,
-    size_t x0, float (*fs)[9][kAffElems])
+    const double* __restrict__ Pg, float* __restrict__ tdiv, const MevpParams& p, size_t x0,
+    float (*fs)[9][kAffElems])
 {
     const int le = threadIdx.x % kAffElems;
     const int part = threadIdx.x / kAffElems; // one warp per third of the Gauss points / nodes
@@ -1677,7 +1677,10 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
 #pragma unroll
         for (int qq = 0; qq < 3; ++qq) {
             Pa[qq] = Pg[(3 * part + qq) * N + e];
-            hP[qq] = hPg[(3 * part + qq) * N + e];
+            // P/(2 alpha) = 4 P/(8 alpha): an exact power-of-two scaling,
+            // rounded to float on the integer pipe (the value the prep kernel
+            // stores for the other element kernels)
+            hP[qq] = narrowPos(__longlong_as_double(__double_as_longlong(Pa[qq]) + (2ll << 52)));
         }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -1712,12 +1715,12 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
 }
 
 template <int VM>
-__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32Affine(DevMesh m,
+__global__ void __launch_bounds__(kAffElems * kStressParts, 12) kMevpStress32Affine(DevMesh m,
     const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
-    const double* __restrict__ Pg, const float* __restrict__ hPg, float* __restrict__ tdiv, MevpParams p)
+    const double* __restrict__ Pg, float* __restrict__ tdiv, MevpParams p)
 {
     __shared__ float fs[4][9][kAffElems];
-    affineBlock<VM>(m.nx, m.N, m.ice, coef, ld, u, v, Pg, hPg, tdiv, p, blockIdx.x * size_t(kAffElems), fs);
+    affineBlock<VM>(m.nx, m.N, m.ice, coef, ld, u, v, Pg, tdiv, p, blockIdx.x * size_t(kAffElems), fs);
 }
 
 // Self-test of the FP64 viscosity forms: out[3 n] = P/(8 alpha Delta) for
@@ -1851,7 +1854,7 @@ __global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32AffineB
     __shared__ float fs[4][9][kAffElems];
     const EnsembleMember& M = members[blockMember[blockIdx.x]];
     const size_t x0 = size_t(static_cast<int>(blockIdx.x) - M.tmaBlock0) * kAffElems;
-    affineBlock<VM>(M.nx, M.N, M.ice, M.affCoef, M.affLd, M.st.u, M.st.v, M.Pg, M.hP, M.tdiv, p, x0, fs);
+    affineBlock<VM>(M.nx, M.N, M.ice, M.affCoef, M.affLd, M.st.u, M.st.v, M.Pg, M.tdiv, p, x0, fs);
 }
 
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
@@ -2482,7 +2485,7 @@ cudaError_t uploadAffineReference(const double ref[4][81])
 }
 
 cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
-    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& pIn, int viscosityMode)
+    const float* v, const double* Pg, float* tdiv, const MevpParams& pIn, int viscosityMode)
 {
     const MevpParams p = withDerived(pIn);
     cudaLaunchConfig_t cfg {};
@@ -2495,9 +2498,9 @@ cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const flo
     cfg.attrs = at;
     cfg.numAttrs = 1;
     switch (viscosityMode) {
-    case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<0>, m, coef, ld, u, v, Pg, hP, tdiv, p);
-    case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<1>, m, coef, ld, u, v, Pg, hP, tdiv, p);
-    default: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<2>, m, coef, ld, u, v, Pg, hP, tdiv, p);
+    case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<0>, m, coef, ld, u, v, Pg, tdiv, p);
+    case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<1>, m, coef, ld, u, v, Pg, tdiv, p);
+    default: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<2>, m, coef, ld, u, v, Pg, tdiv, p);
     }
 }
 

@@ -246,7 +246,7 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
 // float/double conversions on the integer pipe.
 cudaError_t uploadAffineReference(const double ref[4][81]);
 cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
-    const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p, int viscosityMode);
+    const float* v, const double* Pg, float* tdiv, const MevpParams& p, int viscosityMode);
 // out[k n + i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode k = 0, 1, 2.
 cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
     float* out);
