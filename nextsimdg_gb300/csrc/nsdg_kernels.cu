@@ -1715,7 +1715,7 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
 }
 
 template <int VM>
-__global__ void __launch_bounds__(kAffElems * kStressParts, 12) kMevpStress32Affine(DevMesh m,
+__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32Affine(DevMesh m,
     const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
     const double* __restrict__ Pg, float* __restrict__ tdiv, MevpParams p)
 {
