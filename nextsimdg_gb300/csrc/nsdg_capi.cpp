@@ -370,8 +370,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
         add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
         add(18 * N, 4);
-        for (int i = 0; i < 9; ++i) add(Ncg, 4);  // FP32 node state
-        add(2 * Ncg, 4);                          // (1 / lumped mass) / c1 as {hi, lo}
+        for (int i = 0; i < 4; ++i) add(Ncg, 4);  // FP32 u, v, u0, v0
+        add(8 * Ncg, 4);                          // the packed per-step node constants
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
     }
@@ -598,10 +598,11 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
             return p;
         };
         tdiv32 = zf(18 * N);
-        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0, &st32.uo, &st32.vo, &st32.a, &st32.ku, &st32.kv };
+        float** f32[] = { &st32.u, &st32.v, &st32.u0, &st32.v0 };
         for (float** q : f32)
             *q = zf(Ncg);
-        st32.im = reinterpret_cast<float2*>(zf(2 * Ncg));
+        st32.k0 = reinterpret_cast<float4*>(zf(4 * Ncg));
+        st32.k1 = reinterpret_cast<float4*>(zf(4 * Ncg));
         tdivLast = zf(18 * N);
         uLast = zf(Ncg);
         vLast = zf(Ncg);

@@ -1169,7 +1169,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
 // mEVP, mixed precision
 // ===========================================================================
 __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f,
-    const double* __restrict__ invm2, MevpParams p)
+    const double* __restrict__ invm2, const uint8_t* __restrict__ dir, MevpParams p)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
@@ -1192,15 +1192,15 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeSta
     f.v[i] = vf;
     f.u0[i] = uf;
     f.v0[i] = vf;
-    f.uo[i] = static_cast<float>(st.uo[i]);
-    f.vo[i] = static_cast<float>(st.vo[i]);
-    f.a[i] = static_cast<float>(A * rc1);
     // u0 + (A F_atm |wind| uwind - rho H g dxSSH) / c1, in FP64
-    f.ku[i] = static_cast<float>(u + (A * (fatm * ua) - rhoH * p.gravity * st.uGrad[i]) * rc1);
-    f.kv[i] = static_cast<float>(v + (A * (fatm * va) - rhoH * p.gravity * st.vGrad[i]) * rc1);
+    const double ku = u + (A * (fatm * ua) - rhoH * p.gravity * st.uGrad[i]) * rc1;
+    const double kv = v + (A * (fatm * va) - rhoH * p.gravity * st.vGrad[i]) * rc1;
     const double im = invm2[i] * rc1;
     const float hi = static_cast<float>(im);
-    f.im[i] = make_float2(hi, static_cast<float>(im - static_cast<double>(hi)));
+    f.k0[i] = make_float4(static_cast<float>(A * rc1), static_cast<float>(ku), static_cast<float>(kv),
+        static_cast<float>(st.uo[i]));
+    f.k1[i] = make_float4(static_cast<float>(st.vo[i]), hi, static_cast<float>(im - static_cast<double>(hi)),
+        dir[i] ? 1.f : 0.f);
 }
 
 // The FP64 kernel kMevpStress with FP32 operators and state.  The strain
@@ -1744,11 +1744,13 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     // 32-bit index arithmetic (node counts stay far below 2^31)
     const unsigned s2 = 2u * static_cast<unsigned>(nx) + 1u;
     const int i2 = static_cast<int>(static_cast<unsigned>(i) % s2), j2 = static_cast<int>(static_cast<unsigned>(i) / s2);
-    const bool dir = cg2Dir[i] != 0;
-    // per-step constants first (a programmatic dependent launch overlaps
-    // them with the stress kernel's tail), then the wait for its results
-    const float2 im = st.im[i];
-    const float uo = st.uo[i], vo = st.vo[i], a = st.a[i], ku = st.ku[i], kv = st.kv[i];
+    // per-step constants first, two 16-byte loads (a programmatic dependent
+    // launch overlaps them with the stress kernel's tail), then the wait for
+    // its results
+    const float4 c0 = st.k0[i], c1 = st.k1[i];
+    const float a = c0.x, ku = c0.y, kv = c0.z, uo = c0.w, vo = c1.x;
+    const float2 im = make_float2(c1.y, c1.z);
+    const bool dir = c1.w != 0.f;
     asm volatile("griddepcontrol.wait;" ::: "memory");
     float dSx = 0.f, dSy = 0.f;
     if (!dir) {
@@ -2400,7 +2402,7 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
     const MevpNodeState32& st32, const double* invm2, const MevpParams& p)
 {
-    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, invm2, p);
+    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, invm2, m.cg2Dir, p);
     return cudaGetLastError();
 }
 namespace {

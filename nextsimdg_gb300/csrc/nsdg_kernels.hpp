@@ -224,12 +224,8 @@ struct MevpNodeState32 {
     float* v;
     float* u0;
     float* v0;
-    float* uo;
-    float* vo;
-    float* a;
-    float* ku;
-    float* kv;
-    float2* im;
+    float4* k0; // (a, ku, kv, u_ocean)
+    float4* k1; // (v_ocean, im hi, im lo, 1 on a Dirichlet node else 0)
 };
 // The per-step node preparation of the mixed path (prepareIteration's clamps,
 // CGDynamicsKernel.cpp:260-276, and the constants of updateMomentum,
@@ -238,6 +234,7 @@ struct MevpNodeState32 {
 // inverse lumped CG2 mass.
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
     const MevpNodeState32& st32, const double* invm2, const MevpParams& p);
+// (the Dirichlet flags of the nodes come from m.cg2Dir)
 // kMevpStress32 for parallelogram meshes: the unit-square operators
 // (G_xi, G_eta [q][j], A_xi, A_eta [j][q]) in constant memory, uploaded once
 // per device (they depend only on the basis), and 5 coefficients per element
