@@ -759,6 +759,32 @@ __device__ __forceinline__ int nodeCandidates(int i2, int n, int* cell, int* loc
     return k;
 }
 
+// The same candidates in registers (no local arrays): n of them, ascending
+struct NodeCand {
+    int n, c0, l0, c1, l1;
+};
+__device__ __forceinline__ NodeCand nodeCand(int i2, int n)
+{
+    NodeCand r { 1, 0, 0, 0, 0 };
+    if (i2 & 1) {
+        r.c0 = (i2 - 1) / 2;
+        r.l0 = 1;
+    } else if (i2 >= 2 && i2 / 2 < n) {
+        r.n = 2;
+        r.c0 = i2 / 2 - 1;
+        r.l0 = 2;
+        r.c1 = i2 / 2;
+        r.l1 = 0;
+    } else if (i2 >= 2) {
+        r.c0 = i2 / 2 - 1;
+        r.l0 = 2;
+    } else {
+        r.c0 = i2 / 2;
+        r.l0 = 0;
+    }
+    return r;
+}
+
 template <int DG, int NF>
 __global__ void __launch_bounds__(kBlock) kDG2CG(DevMesh m, const double* __restrict__ in0,
     const double* __restrict__ in1, double* __restrict__ out0, double* __restrict__ out1)
@@ -1754,21 +1780,28 @@ __device__ __forceinline__ void mevpMomentum32Node(int nx, int ny, size_t N, siz
     asm volatile("griddepcontrol.wait;" ::: "memory");
     float dSx = 0.f, dSy = 0.f;
     if (!dir) {
-        int cxs[2], lxs[2], cys[2], lys[2];
-        const int nxc = nodeCandidates(i2, nx, cxs, lxs);
-        const int nyc = nodeCandidates(j2, ny, cys, lys);
-        int order[2] = { 0, 1 };
-        if (nyc == 2 && (cys[0] % 2) == 1) {
-            order[0] = 1;
-            order[1] = 0;
+        const NodeCand X = nodeCand(i2, nx);
+        NodeCand Y = nodeCand(j2, ny);
+        if (Y.n == 2 && (Y.c0 & 1)) { // even cell rows first (the reference's accumulation order)
+            const int c = Y.c0, l = Y.l0;
+            Y.c0 = Y.c1;
+            Y.l0 = Y.l1;
+            Y.c1 = c;
+            Y.l1 = l;
         }
-        for (int r = 0; r < nyc; ++r) {
-            const int cy = cys[order[r]], ly = lys[order[r]];
-            for (int k = 0; k < nxc; ++k) {
-                const size_t c = size_t(cy) * nx + cxs[k];
-                const int j = lxs[k] + 3 * ly;
-                dSx -= tdiv[j * N + c];
-                dSy -= tdiv[(9 + j) * N + c];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (r < Y.n) {
+                const int cy = r ? Y.c1 : Y.c0, ly = r ? Y.l1 : Y.l0;
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    if (k < X.n) {
+                        const size_t c = size_t(cy) * nx + (k ? X.c1 : X.c0);
+                        const int j = (k ? X.l1 : X.l0) + 3 * ly;
+                        dSx -= tdiv[j * N + c];
+                        dSy -= tdiv[(9 + j) * N + c];
+                    }
+                }
             }
         }
     }
