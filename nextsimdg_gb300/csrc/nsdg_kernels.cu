@@ -739,27 +739,9 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
 // reference's reversed-parity stripes), cells in ascending x; then the
 // boundary rows and columns are doubled.
 // ===========================================================================
-__device__ __forceinline__ int nodeCandidates(int i2, int n, int* cell, int* loc)
-{
-    // cells along one direction touching CG2 index i2 (0..2n), ascending
-    int k = 0;
-    if (i2 & 1) {
-        cell[k] = (i2 - 1) / 2;
-        loc[k++] = 1;
-    } else {
-        if (i2 >= 2) {
-            cell[k] = i2 / 2 - 1;
-            loc[k++] = 2;
-        }
-        if (i2 / 2 < n) {
-            cell[k] = i2 / 2;
-            loc[k++] = 0;
-        }
-    }
-    return k;
-}
-
-// The same candidates in registers (no local arrays): n of them, ascending
+// The cells along one direction touching CG2 index i2 (0..2n) and the node's
+// local index in each (0, 1, 2), ascending; kept in registers (no local
+// arrays): n of them
 struct NodeCand {
     int n, c0, l0, c1, l1;
 };
@@ -794,24 +776,30 @@ __global__ void __launch_bounds__(kBlock) kDG2CG(DevMesh m, const double* __rest
         return;
     const int s2 = 2 * m.nx + 1;
     const int i2 = static_cast<int>(t % s2), j2 = static_cast<int>(t / s2);
-    int cxs[2], lxs[2], cys[2], lys[2];
-    const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
-    const int nyc = nodeCandidates(j2, m.ny, cys, lys);
-    // odd rows first
-    int order[2] = { 0, 1 };
-    if (nyc == 2 && (cys[0] % 2) == 0) {
-        order[0] = 1;
-        order[1] = 0;
+    const NodeCand X = nodeCand(i2, m.nx);
+    NodeCand Y = nodeCand(j2, m.ny);
+    if (Y.n == 2 && !(Y.c0 & 1)) { // odd cell rows first
+        const int c = Y.c0, l = Y.l0;
+        Y.c0 = Y.c1;
+        Y.l0 = Y.l1;
+        Y.c1 = c;
+        Y.l1 = l;
     }
     const double* in[2] = { in0, in1 };
     double acc[NF];
 #pragma unroll
     for (int f = 0; f < NF; ++f)
         acc[f] = 0.0;
-    for (int r = 0; r < nyc; ++r) {
-        const int cy = cys[order[r]], ly = lys[order[r]];
-        for (int k = 0; k < nxc; ++k) {
-            const int cx = cxs[k], lx = lxs[k];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        if (r >= Y.n)
+            continue;
+        const int cy = r ? Y.c1 : Y.c0, ly = r ? Y.l1 : Y.l0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (k >= X.n)
+                continue;
+            const int cx = k ? X.c1 : X.c0, lx = k ? X.l1 : X.l0;
             const size_t c = size_t(cy) * m.nx + cx;
             const int q = lx + 3 * ly;
 #pragma unroll
@@ -1133,23 +1121,30 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMe
 __device__ __forceinline__ void gatherDivergence(const DevMesh& m, int i2, int j2,
     const double* __restrict__ contrib, double& dx, double& dy)
 {
-    int cxs[2], lxs[2], cys[2], lys[2];
-    const int nxc = nodeCandidates(i2, m.nx, cxs, lxs);
-    const int nyc = nodeCandidates(j2, m.ny, cys, lys);
-    int order[2] = { 0, 1 };
-    if (nyc == 2 && (cys[0] % 2) == 1) {
-        order[0] = 1;
-        order[1] = 0;
+    const NodeCand X = nodeCand(i2, m.nx);
+    NodeCand Y = nodeCand(j2, m.ny);
+    if (Y.n == 2 && (Y.c0 & 1)) { // even cell rows first
+        const int c = Y.c0, l = Y.l0;
+        Y.c0 = Y.c1;
+        Y.l0 = Y.l1;
+        Y.c1 = c;
+        Y.l1 = l;
     }
     const size_t N = m.N;
     double ax = 0.0, ay = 0.0;
-    for (int r = 0; r < nyc; ++r) {
-        const int cy = cys[order[r]], ly = lys[order[r]];
-        for (int k = 0; k < nxc; ++k) {
-            const size_t c = size_t(cy) * m.nx + cxs[k];
-            const int j = lxs[k] + 3 * ly;
-            ax -= contrib[j * N + c];
-            ay -= contrib[(9 + j) * N + c];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        if (r < Y.n) {
+            const int cy = r ? Y.c1 : Y.c0, ly = r ? Y.l1 : Y.l0;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k < X.n) {
+                    const size_t c = size_t(cy) * m.nx + (k ? X.c1 : X.c0);
+                    const int j = (k ? X.l1 : X.l0) + 3 * ly;
+                    ax -= contrib[j * N + c];
+                    ay -= contrib[(9 + j) * N + c];
+                }
+            }
         }
     }
     dx = ax;
