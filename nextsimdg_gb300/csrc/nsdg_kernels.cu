@@ -836,23 +836,28 @@ __global__ void __launch_bounds__(kBlock) kSSHToCG1(DevMesh m, const double* __r
     const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (t >= m.Ncg1)
         return;
-    const int s1 = m.nx + 1;
-    const int i1 = static_cast<int>(t % s1), j1 = static_cast<int>(t / s1);
-    int rows[2], nr = 0;
-    if (j1 >= 1) rows[nr++] = j1 - 1;
-    if (j1 < m.ny) rows[nr++] = j1;
-    if (nr == 2 && (rows[0] % 2) == 0) {
-        const int tmp = rows[0];
-        rows[0] = rows[1];
-        rows[1] = tmp;
+    const unsigned s1 = static_cast<unsigned>(m.nx) + 1u;
+    const int i1 = static_cast<int>(static_cast<unsigned>(t) % s1), j1 = static_cast<int>(static_cast<unsigned>(t) / s1);
+    // the cell rows touching the node, odd rows first (registers, no local arrays)
+    const bool below = j1 >= 1, above = j1 < m.ny;
+    const int nr = int(below) + int(above);
+    int row0 = below ? j1 - 1 : j1, row1 = j1;
+    if (nr == 2 && (row0 % 2) == 0) {
+        row0 = j1;
+        row1 = j1 - 1;
     }
     double acc = 0.0;
-    for (int r = 0; r < nr; ++r)
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        if (r >= nr)
+            continue;
+        const int row = r ? row1 : row0;
         for (int cx = i1 - 1; cx <= i1; ++cx) {
             if (cx < 0 || cx >= m.nx)
                 continue;
-            acc += 0.25 * ssh[size_t(rows[r]) * m.nx + cx];
+            acc += 0.25 * ssh[size_t(row) * m.nx + cx];
         }
+    }
     double scale = 1.0;
     if (j1 == 0 || j1 == m.ny)
         scale *= 2.0;
@@ -867,23 +872,30 @@ __global__ void __launch_bounds__(kBlock) kSSHGrad1(DevMesh m, DevOps o, const d
     const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (t >= m.Ncg1)
         return;
-    const int s1 = m.nx + 1;
-    const int i1 = static_cast<int>(t % s1), j1 = static_cast<int>(t / s1);
-    int rows[2], lys[2], nr = 0;
-    if (j1 >= 1) { rows[nr] = j1 - 1; lys[nr++] = 1; }
-    if (j1 < m.ny) { rows[nr] = j1; lys[nr++] = 0; }
-    if (nr == 2 && (rows[0] % 2) == 1) {
-        int a = rows[0]; rows[0] = rows[1]; rows[1] = a;
-        a = lys[0]; lys[0] = lys[1]; lys[1] = a;
+    const unsigned s1 = static_cast<unsigned>(m.nx) + 1u;
+    const int i1 = static_cast<int>(static_cast<unsigned>(t) % s1), j1 = static_cast<int>(static_cast<unsigned>(t) / s1);
+    // the cell rows touching the node with the node's local row in each, even
+    // rows first (registers, no local arrays)
+    const bool below = j1 >= 1, above = j1 < m.ny;
+    const int nr = int(below) + int(above);
+    int row0 = below ? j1 - 1 : j1, ly0 = below ? 1 : 0, row1 = j1, ly1 = 0;
+    if (nr == 2 && (row0 % 2) == 1) {
+        row0 = j1;
+        ly0 = 0;
+        row1 = j1 - 1;
+        ly1 = 1;
     }
     double au = 0.0, av = 0.0;
     const size_t N = m.N;
-    for (int r = 0; r < nr; ++r)
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        if (r >= nr)
+            continue;
         for (int lx = 1; lx >= 0; --lx) {
             const int cx = i1 - lx;
             if (cx < 0 || cx >= m.nx)
                 continue;
-            const int cy = rows[r], ly = lys[r];
+            const int cy = r ? row1 : row0, ly = r ? ly1 : ly0;
             const size_t e = size_t(cy) * m.nx + cx;
             const size_t n0 = size_t(cy) * s1 + cx;
             const double loc[4] = { cg1[n0], cg1[n0 + 1], cg1[n0 + s1], cg1[n0 + s1 + 1] };
@@ -897,6 +909,7 @@ __global__ void __launch_bounds__(kBlock) kSSHGrad1(DevMesh m, DevOps o, const d
             au -= tx;
             av -= ty;
         }
+    }
     ug[t] = au / o.lumped1[t];
     vg[t] = av / o.lumped1[t];
 }
