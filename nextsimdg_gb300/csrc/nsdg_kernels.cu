@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kBlock) kCG2DG(int nx, size_t N, const double*
     if (e >= N)
         return;
     const size_t s2 = 2 * size_t(nx) + 1;
-    const size_t ix = e % nx, iy = e / nx;
+    const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx), iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
     const size_t base = 2 * s2 * iy + 2 * ix;
     const double* cg[2] = { cg0, cg1 };
     double* out[2] = { out0, out1 };
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(kBlock) kNormalVelocity(DevMesh m, const doubl
     const int nx = m.nx, ny = m.ny;
     const size_t sv = size_t(nx) + 1;
     if (t < m.nXe) {
-        const size_t ix = t % nx, iy = t / nx;
+        const size_t ix = static_cast<unsigned>(t) % static_cast<unsigned>(nx), iy = static_cast<unsigned>(t) / static_cast<unsigned>(nx);
         const size_t n0 = iy * sv + ix;
         const double t0 = wrapLon(m, m.vx[n0 + 1] - m.vx[n0]), t1 = m.vy[n0 + 1] - m.vy[n0];
         double acc[ED];
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
     if (c >= N)
         return;
     const int nx = m.nx, ny = m.ny;
-    const int ix = static_cast<int>(c % nx), iy = static_cast<int>(c / nx);
+    const int ix = static_cast<int>(static_cast<unsigned>(c) % static_cast<unsigned>(nx)), iy = static_cast<int>(static_cast<unsigned>(c) / static_cast<unsigned>(nx));
     const T dt = static_cast<T>(a.dt);
     const bool ice = m.ice[c] != 0;
     const T* cellX;
@@ -775,7 +775,7 @@ __global__ void __launch_bounds__(kBlock) kDG2CG(DevMesh m, const double* __rest
     if (t >= m.Ncg)
         return;
     const int s2 = 2 * m.nx + 1;
-    const int i2 = static_cast<int>(t % s2), j2 = static_cast<int>(t / s2);
+    const int i2 = static_cast<int>(static_cast<unsigned>(t) % static_cast<unsigned>(s2)), j2 = static_cast<int>(static_cast<unsigned>(t) / static_cast<unsigned>(s2));
     const NodeCand X = nodeCand(i2, m.nx);
     NodeCand Y = nodeCand(j2, m.ny);
     if (Y.n == 2 && !(Y.c0 & 1)) { // odd cell rows first
@@ -931,7 +931,7 @@ __global__ void __launch_bounds__(kBlock) kSSHToCG2(DevMesh m, const double* __r
     if (t >= m.Ncg)
         return;
     const int s2 = 2 * m.nx + 1;
-    const int i2 = static_cast<int>(t % s2), j2 = static_cast<int>(t / s2);
+    const int i2 = static_cast<int>(static_cast<unsigned>(t) % static_cast<unsigned>(s2)), j2 = static_cast<int>(static_cast<unsigned>(t) / static_cast<unsigned>(s2));
     const int nx = m.nx, ny = m.ny;
     const int ix = i2 / 2, iy = j2 / 2;
     double u, v;
@@ -1057,7 +1057,7 @@ __global__ void __launch_bounds__(kStressElems * kStressParts) kMevpStress(DevMe
     const bool active = e < N && m.ice[e];
     if (active) {
         const size_t s2 = 2 * size_t(m.nx) + 1;
-        const size_t ix = e % m.nx, iy = e / m.nx;
+        const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(m.nx), iy = static_cast<unsigned>(e) / static_cast<unsigned>(m.nx);
         const size_t base = 2 * s2 * iy + 2 * ix;
         double ul[9], vl[9];
 #pragma unroll
@@ -1171,7 +1171,7 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
     if (i >= m.Ncg)
         return;
     const int s2 = 2 * m.nx + 1;
-    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    const int i2 = static_cast<int>(static_cast<unsigned>(i) % static_cast<unsigned>(s2)), j2 = static_cast<int>(static_cast<unsigned>(i) / static_cast<unsigned>(s2));
     const bool dir = m.cg2Dir[i] != 0;
     double dSx = 0.0, dSy = 0.0;
     if (!dir)
@@ -1976,7 +1976,7 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         return;
     const bool ice = m.ice[e] != 0;
     const size_t s2 = 2 * size_t(m.nx) + 1;
-    const size_t ix = e % m.nx, iy = e / m.nx;
+    const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(m.nx), iy = static_cast<unsigned>(e) / static_cast<unsigned>(m.nx);
     const size_t base = 2 * s2 * iy + 2 * ix;
     T ul[9], vl[9];
 #pragma unroll
@@ -2155,7 +2155,7 @@ __global__ void __launch_bounds__(kBlock) kBbmMomentum(DevMesh m, DevOps o, BbmN
     if (i >= m.Ncg)
         return;
     const int s2 = 2 * m.nx + 1;
-    const int i2 = static_cast<int>(i % s2), j2 = static_cast<int>(i / s2);
+    const int i2 = static_cast<int>(static_cast<unsigned>(i) % static_cast<unsigned>(s2)), j2 = static_cast<int>(static_cast<unsigned>(i) / static_cast<unsigned>(s2));
     const bool dir = m.cg2Dir[i] != 0;
     double dSx = 0.0, dSy = 0.0;
     if (!dir)
