@@ -252,9 +252,8 @@ def run_reference(args, world, rank):
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
         k.setData(name, arr)
-    # each step is a bounded sample: the full mEVP step at a reduced iteration
-    # count is not the workload, so the sample is the full step on a sub-box
-    # when the full box would not finish within minutes
+    # each step is a full model step of the workload (1.3 s on 16 Arm cores
+    # at 512^2): the default 3 + 20 steps finish within a minute
     for s in range(args.warmup):
         k.update(s * DT, DT)
     t0 = time.perf_counter()
