@@ -1,6 +1,6 @@
 """bench.py's host-side contract, without a GPU: the reference arm (the CPU
-oracle on the host cores) prints one JSON line with the keys the driver
-reads, and the algorithmic byte counts used by the roofline are the
+oracle on the host cores) prints one JSON line with every key of the
+benchmark line, and the algorithmic byte counts used by the roofline are the
 documented per-element figures."""
 import json
 import subprocess
