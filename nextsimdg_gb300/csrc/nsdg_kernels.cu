@@ -1891,7 +1891,7 @@ __global__ void __launch_bounds__(kTmaElems * kStressParts) kMevpStress32TmaBatc
 }
 
 template <int VM>
-__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32AffineBatched(
+__global__ void __launch_bounds__(kAffElems * kStressParts, 12) kMevpStress32AffineBatched(
     const EnsembleMember* __restrict__ members, const uint16_t* __restrict__ blockMember, MevpParams p)
 {
     __shared__ float fs[4][9][kAffElems];
