@@ -1367,7 +1367,10 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
         if (!(k->readCache & 1)) {
             const double* in[2] = { k->u, k->v };
             double* outd[2] = { k->velx, k->vely };
-            e = launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+            // the mixed path's velocity is its FP32 iterate: its projection
+            // takes the FP32-quadrature CG2DG (FP64 inverse mass)
+            e = (k->mixed() && k->jwA32) ? launchCG2DG32(st, k->dm, dg, k->jwA32, minvP, in, outd)
+                                         : launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
             if (e == cudaSuccess)
                 k->readCache |= 1;
         }
@@ -1383,7 +1386,8 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
             const double* in[2] = { tx, ty };
             double* outd[2] = { k->phiA, k->phiA + size_t(dg) * N };
             if (e == cudaSuccess)
-                e = launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+                e = (k->mixed() && k->jwA32) ? launchCG2DG32(st, k->dm, dg, k->jwA32, minvP, in, outd)
+                                             : launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
             if (e == cudaSuccess)
                 k->readCache |= 2;
         }
