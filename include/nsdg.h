@@ -120,7 +120,10 @@ int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny,
 /* setData semantics of the reference: hice/cice/ssh/damage and unknown names
  * follow DGModelArray::ma2dg (zero, then all components if n_comp equals the
  * DG count, else component 0 only); u, v, uwind, vwind, uocean, vocean are
- * DG->CG2 interpolated.  data: n_elements*n_comp doubles from host memory. */
+ * DG->CG2 interpolated.  data: n_elements*n_comp doubles from host memory,
+ * which the caller may reuse when the call returns (the copy has landed; the
+ * conversion on the device runs on behind the return, ahead of any later
+ * work on the handle).  Pinned host memory makes the copy faster. */
 int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data,
     size_t n_elements, size_t n_comp);
 

@@ -150,6 +150,17 @@ struct nsdg_kernel {
     bool mixed() const { return P.precision == NSDG_PRECISION_MIXED; }
     double *partials = nullptr, *dsum = nullptr;
     int* derr = nullptr;
+    // pinned host copy of derr (a pageable target would make the read a
+    // staged, synchronous copy) and the event set_data waits on
+    int* hErr = nullptr;
+    cudaEvent_t copied = nullptr;
+    // set_data's host copies run on copyStream into two staging buffers in
+    // turn, so that a copy overlaps the conversion of the one before it;
+    // converted[i]: the last conversion that read staging buffer i
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t converted[2] = { nullptr, nullptr };
+    double* stage2 = nullptr;
+    int stageSlot = 0;
     // graph of one update
     cudaGraphExec_t graph = nullptr;
     double graphDt = -1.0;
@@ -219,7 +230,24 @@ struct nsdg_kernel {
             cudaGraphExecDestroy(graph);
         graph = nullptr;
         graphDt = -1.0;
+        if (copyStream)
+            cudaStreamSynchronize(copyStream);
         arena.release();
+        if (copied)
+            cudaEventDestroy(copied);
+        copied = nullptr;
+        for (auto& c : converted) {
+            if (c)
+                cudaEventDestroy(c);
+            c = nullptr;
+        }
+        if (copyStream)
+            cudaStreamDestroy(copyStream);
+        copyStream = nullptr;
+        stageSlot = 0;
+        if (hErr)
+            cudaFreeHost(hErr);
+        hErr = nullptr;
         if (stream)
             cudaStreamDestroy(stream);
         stream = nullptr;
@@ -251,9 +279,9 @@ struct nsdg_kernel {
 
 int nsdg_kernel::checkDeviceError()
 {
-    int h = 0;
-    CUDA_TRY(cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(hErr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
+    const int h = *hErr;
     if (h) {
         CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), stream));
         std::string m = "non-finite values detected on the device:";
@@ -365,7 +393,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     if (bbm) {
         add(8 * N); add(8 * N); add(3 * nXe); add(3 * nYe); add(24 * N); add(24 * N);
     }
-    add(3 * Ncg1); add(8 * N); add(8 * N); add(Ncg);
+    add(3 * Ncg1); add(8 * N); add(8 * N); add(8 * N); add(Ncg);
     if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
         add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
         add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
@@ -391,6 +419,12 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     bytes += 4096;
 
     CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
+    for (auto& c : converted)
+        CUDA_TRY(cudaEventCreateWithFlags(&c, cudaEventDisableTiming));
+    CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&hErr), sizeof(int), cudaHostAllocDefault));
+    *hErr = 0;
     CUDA_TRY(uploadConstTables());
     CUDA_TRY(arena.reserve(bytes));
 
@@ -502,6 +536,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     }
     sshScratch = z(3 * Ncg1);
     staging = z(8 * N);
+    stage2 = z(8 * N);
     dgTmp = z(8 * N);
     cgTmp = z(Ncg);
     partials = z((N + 255) / 256 + 1);
@@ -1296,29 +1331,46 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
     auto cu = [&](cudaError_t e, const char* what) {
         return e == cudaSuccess ? NSDG_OK : k->fail(NSDG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     };
-    int r = cu(cudaMemcpyAsync(k->staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, st), "set_data copy");
+    // the copy waits only for the conversion that last read its staging
+    // buffer; the conversion waits for the copy (and, in stream order, for
+    // everything already enqueued on the kernel's stream)
+    const int slot = k->stageSlot;
+    k->stageSlot ^= 1;
+    double* const staging = slot ? k->stage2 : k->staging;
+    int r = cu(cudaStreamWaitEvent(k->copyStream, k->converted[slot], 0), "set_data wait");
+    if (r) return r;
+    r = cu(cudaMemcpyAsync(staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, k->copyStream),
+        "set_data copy");
+    if (r) return r;
+    r = cu(cudaEventRecord(k->copied, k->copyStream), "set_data event");
+    if (r) return r;
+    r = cu(cudaStreamWaitEvent(st, k->copied, 0), "set_data wait");
     if (r) return r;
     if (cgTarget && n_comp != size_t(dg)) {
         // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so DG2CG
         // of the one-component field gives the same node values (the higher
         // components' contributions are exact zeros)
-        const double* in[1] = { k->staging };
+        const double* in[1] = { staging };
         double* out[1] = { cgTarget };
         r = cu(launchDG2CG(st, k->dm, 1, 1, in, out), "set_data DG2CG");
         if (r) return r;
     } else if (cgTarget) {
         // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
-        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, k->staging, k->dgTmp), "set_data convert");
+        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, staging, k->dgTmp), "set_data convert");
         if (r) return r;
         const double* in[1] = { k->dgTmp };
         double* out[1] = { cgTarget };
         r = cu(launchDG2CG(st, k->dm, dg, 1, in, out), "set_data DG2CG");
         if (r) return r;
     } else {
-        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, k->staging, dgTarget), "set_data convert");
+        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, staging, dgTarget), "set_data convert");
         if (r) return r;
     }
-    r = cu(cudaStreamSynchronize(st), "set_data sync");
+    r = cu(cudaEventRecord(k->converted[slot], st), "set_data event");
+    if (r) return r;
+    // the caller may reuse `data` once the copy has landed; the conversion
+    // runs on behind the return
+    r = cu(cudaEventSynchronize(k->copied), "set_data sync");
     if (r) return r;
     return k->ok();
 }
@@ -1367,10 +1419,9 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
         if (!(k->readCache & 1)) {
             const double* in[2] = { k->u, k->v };
             double* outd[2] = { k->velx, k->vely };
-            // the mixed path's velocity is its FP32 iterate: its projection
-            // takes the FP32-quadrature CG2DG (FP64 inverse mass)
-            e = (k->mixed() && k->jwA32) ? launchCG2DG32(st, k->dm, dg, k->jwA32, minvP, in, outd)
-                                         : launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+            // only the cell averages are read: component 0 of the projection
+            // (the mixed path's velocity is its FP32 iterate: FP32 quadrature)
+            e = launchCG2DG0(st, k->dm, dg, k->dops.jwA, k->mixed() ? k->jwA32 : nullptr, minvP, in, outd);
             if (e == cudaSuccess)
                 k->readCache |= 1;
         }
@@ -1382,12 +1433,11 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
             double* tx = k->cgTmp;
             double* ty = k->u0; // reused as scratch outside update
             e = launchIceOceanStress(st, k->Ncg, bbm ? 1 : 0, bbm ? k->avgU : k->u, bbm ? k->avgV : k->v,
-                k->uo, k->vo, k->P.F_ocean, std::cos(rad * ang), std::sin(rad * ang), tx, ty);
+                k->uo, k->vo, k->P.F_ocean, std::cos(rad * ang), std::sin(rad * ang), tx, ty, k->mixed());
             const double* in[2] = { tx, ty };
             double* outd[2] = { k->phiA, k->phiA + size_t(dg) * N };
             if (e == cudaSuccess)
-                e = (k->mixed() && k->jwA32) ? launchCG2DG32(st, k->dm, dg, k->jwA32, minvP, in, outd)
-                                             : launchCG2DG(st, k->dm, dg, k->dops.jwA, minvP, 2, in, outd);
+                e = launchCG2DG0(st, k->dm, dg, k->dops.jwA, k->mixed() ? k->jwA32 : nullptr, minvP, in, outd);
             if (e == cudaSuccess)
                 k->readCache |= 2;
         }

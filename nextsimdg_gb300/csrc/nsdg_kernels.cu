@@ -320,6 +320,106 @@ __device__ __forceinline__ double widenAny(float f)
     return __longlong_as_double(static_cast<long long>(sign | ((static_cast<unsigned long long>(mag) << 29)
         + (896ull << 52))));
 }
+// ===========================================================================
+// Cell averages of the CG2 -> DG projection of two fields (what getDG0Data
+// returns): the quadrature of kCG2DG (FP64) or kCG2DG32 (F32: FP32
+// quadrature, conversions on the integer pipe) and only row 0 of M^{-1}.  In
+// FP64 the arithmetic is kCG2DG's for component 0, operation for operation.
+// ===========================================================================
+template <int DG, bool F32>
+__global__ void __launch_bounds__(kBlock) kCG2DG0(int nx, size_t N, const double* __restrict__ jw,
+    const float* __restrict__ jw32, const double* __restrict__ minv, const double* __restrict__ cg0,
+    const double* __restrict__ cg1, double* __restrict__ out0, double* __restrict__ out1)
+{
+    constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q;
+    const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (e >= N)
+        return;
+    const size_t s2 = 2 * size_t(nx) + 1;
+    const size_t ix = static_cast<unsigned>(e) % static_cast<unsigned>(nx);
+    const size_t iy = static_cast<unsigned>(e) / static_cast<unsigned>(nx);
+    const size_t base = 2 * s2 * iy + 2 * ix;
+    const double* cg[2] = { cg0, cg1 };
+    double* out[2] = { out0, out1 };
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+        double r[DG];
+        if constexpr (F32) {
+            float loc[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j)
+                loc[j] = narrowAny(cg[f][base + (j % 3) + (j / 3) * s2]);
+            float t[QQ];
+#pragma unroll
+            for (int q = 0; q < QQ; ++q) {
+                float v = 0.f;
+#pragma unroll
+                for (int j = 0; j < 9; ++j)
+                    v = fmaf(cT32.phi2[Q][j][q], loc[j], v);
+                t[q] = jw32[q * N + e] * v;
+            }
+#pragma unroll
+            for (int i = 0; i < DG; ++i) {
+                float a = 0.f;
+#pragma unroll
+                for (int q = 0; q < QQ; ++q)
+                    a = fmaf(cT32.psi[Q][i][q], t[q], a);
+                r[i] = widenAny(a);
+            }
+        } else {
+            double loc[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j)
+                loc[j] = cg[f][base + (j % 3) + (j / 3) * s2];
+            double t[QQ];
+#pragma unroll
+            for (int q = 0; q < QQ; ++q) {
+                double v = 0.0;
+#pragma unroll
+                for (int j = 0; j < 9; ++j)
+                    v += cT.phi2[Q][j][q] * loc[j];
+                t[q] = jw[q * N + e] * v;
+            }
+#pragma unroll
+            for (int i = 0; i < DG; ++i) {
+                double a = 0.0;
+#pragma unroll
+                for (int q = 0; q < QQ; ++q)
+                    a += cT.psi[Q][i][q] * t[q];
+                r[i] = a;
+            }
+        }
+        double a = 0.0;
+#pragma unroll
+        for (int k = 0; k < DG; ++k)
+            a += minv[k * N + e] * r[k];
+        out[f][e] = a;
+    }
+}
+
+// The ice-ocean stress at the CG2 nodes in FP32 for the mixed path's
+// read-out (its velocities are FP32 iterates), kIceOceanStress's formulas
+__global__ void __launch_bounds__(kBlock) kIceOceanStress32(size_t n, int brittle, const double* __restrict__ u,
+    const double* __restrict__ v, const double* __restrict__ uo, const double* __restrict__ vo,
+    float Fo, float ca, float sa, double* __restrict__ tx, double* __restrict__ ty)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const float ui = narrowAny(u[i]), vi = narrowAny(v[i]), uoi = narrowAny(uo[i]), voi = narrowAny(vo[i]);
+    if (!brittle) {
+        const float ur = ui - uoi, vr = vi - voi;
+        const float a = sqrtf(ur * ur + vr * vr);
+        tx[i] = widenAny(Fo * a * ur);
+        ty[i] = widenAny(Fo * a * vr);
+    } else {
+        const float ur = uoi - ui, vr = voi - vi;
+        const float cp = Fo * hypotf(ur, vr);
+        tx[i] = widenAny(cp * (ur * ca - vr * sa));
+        ty[i] = widenAny(cp * (vr * ca + ur * sa));
+    }
+}
+
 template <class T> __device__ __forceinline__ T toT(double x) { return x; }
 template <> __device__ __forceinline__ float toT<float>(double x) { return narrowAny(x); }
 template <class T> __device__ __forceinline__ double fromT(T x) { return x; }
@@ -2346,6 +2446,20 @@ cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float*
     return cudaGetLastError();
 }
 
+cudaError_t launchCG2DG0(cudaStream_t s, const DevMesh& m, int dg, const double* jw, const float* jw32,
+    const double* minv, const double* const* cg, double* const* out)
+{
+    const unsigned g = blocksFor(m.N);
+    if (jw32) {
+        NSDG_DG_SWITCH(dg, (kCG2DG0<D, true><<<g, kBlock, 0, s>>>(m.nx, m.N, nullptr, jw32, minv, cg[0], cg[1],
+                                                                  out[0], out[1])));
+    } else {
+        NSDG_DG_SWITCH(dg, (kCG2DG0<D, false><<<g, kBlock, 0, s>>>(m.nx, m.N, jw, nullptr, minv, cg[0], cg[1],
+                                                                   out[0], out[1])));
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
     const double* vely, double* nvX, double* nvY)
 {
@@ -2644,9 +2758,14 @@ cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, cons
 }
 
 cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const double* u, const double* v,
-    const double* uo, const double* vo, double F_ocean, double cosA, double sinA, double* tx, double* ty)
+    const double* uo, const double* vo, double F_ocean, double cosA, double sinA, double* tx, double* ty,
+    bool fp32)
 {
-    kIceOceanStress<<<blocksFor(n), kBlock, 0, s>>>(n, brittle, u, v, uo, vo, F_ocean, cosA, sinA, tx, ty);
+    if (fp32)
+        kIceOceanStress32<<<blocksFor(n), kBlock, 0, s>>>(n, brittle, u, v, uo, vo, static_cast<float>(F_ocean),
+            static_cast<float>(cosA), static_cast<float>(sinA), tx, ty);
+    else
+        kIceOceanStress<<<blocksFor(n), kBlock, 0, s>>>(n, brittle, u, v, uo, vo, F_ocean, cosA, sinA, tx, ty);
     return cudaGetLastError();
 }
 

@@ -96,6 +96,11 @@ cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* 
 // transport velocity).
 cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float* jw32, const double* minv,
     const double* const* cg, double* const* out);
+// Cell averages (component 0) of the CG2DG projection of two fields, written
+// to out[0][0..N) and out[1][0..N): FP32 quadrature when jw32 is given (the
+// mixed path), else kCG2DG's FP64 arithmetic.  Row 0 of minv only.
+cudaError_t launchCG2DG0(cudaStream_t s, const DevMesh& m, int dg, const double* jw, const float* jw32,
+    const double* minv, const double* const* cg, double* const* out);
 // Edge normal velocities (DGTransport.cpp:158-252).
 cudaError_t launchNormalVelocity(cudaStream_t s, const DevMesh& m, int dg, const double* velx,
     const double* vely, double* nvX, double* nvY);
@@ -290,10 +295,11 @@ int nodesPerBlock();
 cudaError_t launchWidenVelocity(cudaStream_t s, size_t n, const float* u32, const float* v32, double* u,
     double* v);
 
-// Ice-ocean stress on CG2 nodes (VPCGDynamicsKernel.hpp:96-120 / BrittleCGDynamicsKernel.hpp:168-192).
+// Ice-ocean stress on CG2 nodes (VPCGDynamicsKernel.hpp:96-120 / BrittleCGDynamicsKernel.hpp:168-192);
+// fp32: the same formulas in FP32 (the mixed path's read-out).
 cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const double* u,
     const double* v, const double* uo, const double* vo, double F_ocean, double cosA, double sinA,
-    double* tx, double* ty);
+    double* tx, double* ty, bool fp32 = false);
 
 // --- BBM -----------------------------------------------------------------
 struct BbmParams {
