@@ -1343,36 +1343,43 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
         "set_data copy");
     if (r) return r;
     r = cu(cudaEventRecord(k->copied, k->copyStream), "set_data event");
-    if (r) return r;
-    r = cu(cudaStreamWaitEvent(st, k->copied, 0), "set_data wait");
-    if (r) return r;
-    if (cgTarget && n_comp != size_t(dg)) {
-        // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so DG2CG
-        // of the one-component field gives the same node values (the higher
-        // components' contributions are exact zeros)
-        const double* in[1] = { staging };
-        double* out[1] = { cgTarget };
-        r = cu(launchDG2CG(st, k->dm, 1, 1, in, out), "set_data DG2CG");
-        if (r) return r;
-    } else if (cgTarget) {
-        // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
-        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, staging, k->dgTmp), "set_data convert");
-        if (r) return r;
-        const double* in[1] = { k->dgTmp };
-        double* out[1] = { cgTarget };
-        r = cu(launchDG2CG(st, k->dm, dg, 1, in, out), "set_data DG2CG");
-        if (r) return r;
-    } else {
-        r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, staging, dgTarget), "set_data convert");
-        if (r) return r;
+    if (r) {
+        cudaStreamSynchronize(k->copyStream); // the caller's buffer is read until the copy ends
+        return r;
     }
-    r = cu(cudaEventRecord(k->converted[slot], st), "set_data event");
-    if (r) return r;
-    // the caller may reuse `data` once the copy has landed; the conversion
-    // runs on behind the return
-    r = cu(cudaEventSynchronize(k->copied), "set_data sync");
-    if (r) return r;
-    return k->ok();
+    r = cu(cudaStreamWaitEvent(st, k->copied, 0), "set_data wait");
+    if (r == NSDG_OK) {
+        if (cgTarget && n_comp != size_t(dg)) {
+            // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so
+            // DG2CG of the one-component field gives the same node values
+            // (the higher components' contributions are exact zeros)
+            const double* in[1] = { staging };
+            double* out[1] = { cgTarget };
+            r = cu(launchDG2CG(st, k->dm, 1, 1, in, out), "set_data DG2CG");
+        } else if (cgTarget) {
+            // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
+            r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, staging, k->dgTmp), "set_data convert");
+            if (r == NSDG_OK) {
+                const double* in[1] = { k->dgTmp };
+                double* out[1] = { cgTarget };
+                r = cu(launchDG2CG(st, k->dm, dg, 1, in, out), "set_data DG2CG");
+            }
+        } else {
+            r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, staging, dgTarget),
+                "set_data convert");
+        }
+    }
+    // recorded after whatever reads this staging buffer, also on a failure
+    const cudaError_t er = cudaEventRecord(k->converted[slot], st);
+    if (r == NSDG_OK)
+        r = cu(er, "set_data event");
+    // the caller may reuse `data` once the copy has landed (on every return
+    // from here); the conversion runs on behind the return
+    const cudaError_t es = cudaEventSynchronize(k->copied);
+    if (r)
+        return r;
+    r = cu(es, "set_data sync");
+    return r ? r : k->ok();
 }
 
 int nsdg_kernel_update(nsdg_kernel* k, double t_start, double dt)
