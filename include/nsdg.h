@@ -328,6 +328,16 @@ int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
  * Mixed-precision handles use the parallelogram stress kernel when it is at
  * most 1e-9. */
 int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords, int dg_comp, double* mismatch);
+
+/* The closed (Dirichlet) element sides a handle derives from its mask at
+ * initialise (ParametricMesh::landmaskFromModelArray, dirichletFromMask,
+ * dirichletFromEdge and sortDirichlet, ParametricMesh.cpp:217-272): counts[s]
+ * ascending element ids i + nx*j for side s (0 bottom, 1 right, 2 top,
+ * 3 left), written to ids side after side.  mask: nx*ny doubles, 1.0 = ice.
+ * NSDG_ERR_SIZE_MISMATCH (counts still set) when capacity < their sum.
+ * Host only. */
+int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts, size_t* ids,
+    size_t capacity);
 /* P / (8 alpha Delta), Delta = sqrt(inv + delta_min^2), for n host values by
  * the three FP64 forms of the mixed-precision stress kernels: out[k n + i]
  * for form k = 0 (CUDA's rsqrt(double)), 1 (one Newton-Raphson step in FP64

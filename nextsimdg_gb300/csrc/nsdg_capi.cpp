@@ -2454,6 +2454,30 @@ int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords,
     return NSDG_OK;
 }
 
+int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts, size_t* ids, size_t capacity)
+{
+    if (!mask || !counts || nx < 1 || ny < 1 || (capacity > 0 && !ids))
+        return NSDG_ERR_BAD_ARG;
+    HostMesh m;
+    m.nx = nx;
+    m.ny = ny;
+    m.ice.resize(nx * ny);
+    for (size_t i = 0; i < nx * ny; ++i)
+        m.ice[i] = (mask[i] == 1.0) ? 1 : 0; // the kernel's initialise rule
+    m.dirichletFromMaskAndEdges();
+    size_t total = 0;
+    for (int s = 0; s < 4; ++s) {
+        counts[s] = m.dirichlet[s].size();
+        total += counts[s];
+    }
+    if (total > capacity)
+        return NSDG_ERR_SIZE_MISMATCH;
+    for (const auto& d : m.dirichlet)
+        for (size_t e : d)
+            *ids++ = e;
+    return NSDG_OK;
+}
+
 int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
 {
     if (!inv || !Pa || !out || n == 0 || n > (size_t(1) << 26) || !(delta_min > 0.0))

@@ -68,6 +68,26 @@ def parallelogram_mismatch(coords, nx: int, ny: int, dg_comp: int = 6) -> float:
     return out.value
 
 
+def mesh_dirichlet(mask, nx: int, ny: int) -> list:
+    """Host only: the closed (Dirichlet) element sides a handle derives from
+    its mask at initialise, as four ascending arrays of element ids (bottom,
+    right, top, left), ParametricMesh.cpp:217-272."""
+    lib = _lib.load()
+    m = _f64(mask)
+    if m.size != nx * ny:
+        raise ValueError("mask must hold nx*ny values")
+    counts = (c_size_t * 4)()
+    ids = np.empty(4 * nx * ny, dtype=np.uint64)
+    st = lib.nsdg_mesh_dirichlet(nx, ny, _ptr(m), counts, _ptr(ids), ids.size)
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "mesh_dirichlet failed")
+    out, o = [], 0
+    for c in counts:
+        out.append(ids[o:o + c].astype(np.int64))
+        o += c
+    return out
+
+
 def selftest_viscosity(inv, pa, delta_min: float) -> np.ndarray:
     """P/(8 alpha Delta) of each (inv, Pa) by the three FP64 forms of the
     mixed-precision stress kernels, shape (3, n) float32 (see

@@ -23,6 +23,9 @@
  *     the divM / iMM metric terms) have no reference test either; the
  *     geometry is checked against the exact area of a lon/lat rectangle on
  *     the unit sphere (tests/test_oracle_spherical.py).
+ *   - The closed (Dirichlet) element sides derived from a land mask are
+ *     PINNED against the lists stored in the reference's 25 km Arctic mesh
+ *     fixture (dynamics/test/ParametricMesh_test.cpp:87-138, exact).
  *
  * Arithmetic: FP64 throughout, compiled with -ffp-contract=off so x86-64 and
  * aarch64 give identical results.  Sums run in the order the reference's
@@ -2043,6 +2046,34 @@ double oracle_kernel_mean_value(void* kp, const char* name)
     if (s == "damage") return MeanValue(k->mesh, k->damage);
     return NAN;
 }
+/* ParametricMesh::landmaskFromModelArray + dirichletFromMask + dirichletFromEdge
+ * (ParametricMesh.cpp:217-272), as the kernel's initialise runs them: counts[s]
+ * ascending element ids for side s, written to ids side after side; -1 when
+ * capacity is short (counts still set). */
+int oracle_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts, size_t* ids, size_t capacity)
+{
+    Mesh m;
+    m.nx = nx;
+    m.ny = ny;
+    m.nelements = nx * ny;
+    m.nnodes = (nx + 1) * (ny + 1);
+    m.landmask.resize(m.nelements);
+    for (size_t i = 0; i < m.nelements; ++i) m.landmask[i] = (mask[i] == 1.) ? 1 : 0;
+    m.dirichletFromMask();
+    for (int e = 0; e < 4; ++e) m.dirichletFromEdge(e);
+    size_t total = 0;
+    for (int s = 0; s < 4; ++s) {
+        counts[s] = m.dirichlet[s].size();
+        total += counts[s];
+    }
+    if (total > capacity)
+        return -1;
+    for (int s = 0; s < 4; ++s)
+        for (size_t e : m.dirichlet[s])
+            *ids++ = e;
+    return 0;
+}
+
 int oracle_num_threads(void)
 {
 #ifdef _OPENMP

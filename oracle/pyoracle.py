@@ -103,6 +103,8 @@ def load() -> ctypes.CDLL:
             "oracle_transport_l2error": (c_double, [c_void_p, c_int, c_double, c_void_p]),
             "oracle_advection_golden": (c_double, [c_int, c_double, c_int, POINTER(c_double)]),
             "oracle_periodic_golden": (c_double, [c_int, c_int, POINTER(c_double)]),
+            "oracle_mesh_dirichlet": (c_int, [c_size_t, c_size_t, c_void_p, POINTER(c_size_t), c_void_p,
+                                              c_size_t]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -359,6 +361,23 @@ class OracleTransport:
 
 # Reference test functions (ids of oracle_transport_function2dg)
 SMOOTH_BUMP, ROT_VX, ROT_VY, PACKMAN, RING_VX, RING_VY = range(6)
+
+
+def mesh_dirichlet(nx: int, ny: int, mask) -> list:
+    """The four closed-side element lists (bottom, right, top, left) the
+    oracle derives from a mask (1.0 = ice), ParametricMesh.cpp:217-272."""
+    m = _f64(mask)
+    if m.size != nx * ny:
+        raise ValueError("mask must hold nx*ny values")
+    counts = (c_size_t * 4)()
+    ids = np.empty(4 * nx * ny, dtype=np.uint64)
+    if load().oracle_mesh_dirichlet(nx, ny, _p(m), counts, _p(ids), ids.size) != 0:
+        raise RuntimeError("oracle_mesh_dirichlet failed")
+    out, o = [], 0
+    for c in counts:
+        out.append(ids[o:o + c].astype(np.int64))
+        o += c
+    return out
 
 
 def rectangle_mesh(Lx, Ly, Nx, Ny, distort=0.0):
