@@ -162,8 +162,8 @@ int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms);
  * 1 = node momentum kernel, 2 = transport operator; for mixed-precision mEVP
  * also 3 = stress kernel with operators by global loads, 4 = with operator
  * tiles by TMA, and on parallelogram meshes 5, 6, 7 = the coefficient kernel
- * with FP64 viscosity form 0, 1, 2 (see nsdg_selftest_viscosity).  *name gets
- * its name. */
+ * with FP64 viscosity form 0, 1, 2 (see nsdg_selftest_viscosity), 8 = with
+ * the float-pair form 3 (nsdg_selftest_viscosity_ff).  *name gets its name. */
 int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms,
     const char** name);
 /* Which mixed-precision mEVP stress kernel the updates use: *kind 0 =
@@ -344,6 +344,11 @@ int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts
  * from an FP32 rsqrtf seed), 2 (the same with float/double conversions on
  * the integer pipe).  Inputs: inv >= 0, Pa >= 0. */
 int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
+/* The same quantity by form 3: the Newton step of form 2 from the same seed
+ * with float pairs on the FP32 pipe (one FP64 subtraction per value).  out[n].
+ * The stress kernel with this form runs only through
+ * nsdg_kernel_time_kernel(kernel_id = 8). */
+int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
 
 /* ======================================================================== */

@@ -128,6 +128,7 @@ SIGNATURES = [
     ("nsdg_kernel_warm_stats", c_int, [c_void_p, c_void_p]),
     ("nsdg_selftest_bounded_wait", c_int, [c_double, POINTER(c_int)]),
     ("nsdg_selftest_viscosity", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
+    ("nsdg_selftest_viscosity_ff", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
     ("nsdg_mesh_dirichlet", c_int, [c_size_t, c_size_t, c_void_p, POINTER(c_size_t), c_void_p, c_size_t]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),

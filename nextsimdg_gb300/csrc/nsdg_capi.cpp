@@ -1718,6 +1718,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 5:
         case 6:
         case 7:
+        case 8:
             return k->launchStress32(k->stream, mp, k->derr, 2, kernel_id - 5);
         default:
             return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
@@ -1725,10 +1726,10 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                 k->mixed() ? k->cellY32 : nullptr);
         }
     };
-    if (kernel_id < 0 || kernel_id > 7 || (kernel_id >= 3 && (bbm || !k->mixed()))
+    if (kernel_id < 0 || kernel_id > 8 || (kernel_id >= 3 && (bbm || !k->mixed()))
         || (kernel_id >= 5 && !k->affCoef))
         return k->fail(NSDG_ERR_BAD_ARG,
-            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-7: on parallelogram meshes)");
+            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8: on parallelogram meshes)");
     static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
         *name = kernel_id == 0 ? (bbm ? "kBbmStress" : (k->mixed() ? kStress32Names[k->stressKind] : "kMevpStress"))
@@ -2478,7 +2479,9 @@ int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts
     return NSDG_OK;
 }
 
-int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
+// the viscosity self-tests: forms = 3 (modes 0, 1, 2) or 1 (mode 3)
+static int viscositySelfTest(size_t n, const float* inv, const double* Pa, double delta_min, float* out,
+    int forms)
 {
     if (!inv || !Pa || !out || n == 0 || n > (size_t(1) << 26) || !(delta_min > 0.0))
         return NSDG_ERR_BAD_ARG;
@@ -2489,14 +2492,17 @@ int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double
     float *dInv = nullptr, *dOut = nullptr;
     double* dPa = nullptr;
     cudaStream_t s = nullptr;
+    const size_t nOut = size_t(forms) * n;
     cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&dInv, n * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&dPa, n * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&dOut, 3 * n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dOut, nOut * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpyAsync(dInv, inv, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dPa, Pa, n * sizeof(double), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = launchViscositySelfTest(s, n, dInv, dPa, delta_min, dOut);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dOut, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = forms == 1 ? launchViscositySelfTestFF(s, n, dInv, dPa, delta_min, dOut)
+                       : launchViscositySelfTest(s, n, dInv, dPa, delta_min, dOut);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dOut, nOut * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     for (void* p : { static_cast<void*>(dInv), static_cast<void*>(dPa), static_cast<void*>(dOut) })
         if (p)
@@ -2504,6 +2510,16 @@ int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double
     if (s)
         cudaStreamDestroy(s);
     return e == cudaSuccess ? NSDG_OK : NSDG_ERR_CUDA;
+}
+
+int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
+{
+    return viscositySelfTest(n, inv, Pa, delta_min, out, 3);
+}
+
+int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
+{
+    return viscositySelfTest(n, inv, Pa, delta_min, out, 1);
 }
 
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out)

@@ -14,6 +14,7 @@ __constant__ ConstTables32 cT32;
 
 #include "nsdg_common.cuh"
 #include "nsdg_kernels.hpp"
+#include "nsdg_visc_ff.hpp"
 
 namespace nsdg {
 
@@ -1707,22 +1708,31 @@ __device__ __forceinline__ float narrowPos(double d)
 // rounding, e0 <= 2^-21 for the seed and its FP32 argument, i.e. below
 // 1e-12); VM 2 converts between float and double on the integer pipe (y0/2
 // by the exponent bias).  Five FP64 instructions per Gauss point in VM 2.
+// VM 3: the same Newton step from the same seed with float pairs on the FP32
+// pipe (nsdg_visc_ff.hpp: one FP64 subtraction per Gauss point, and one FMA
+// per thread for the low part of DeltaMin^2, which the unrolled Gauss-point
+// loop shares).
 template <int VM>
 __device__ __forceinline__ float viscosity8(float inv, double Pa, double dmin, float dmin2f)
 {
-    const double td = VM == 2 ? widenNonneg(inv) : static_cast<double>(inv);
-    const double t = fma(dmin, dmin, td);
-    if constexpr (VM == 0) {
-        return static_cast<float>(Pa * rsqrt(t));
+    if constexpr (VM == 3) {
+        const float d2l = nsdg_ff::narrowAny(fma(dmin, dmin, -nsdg_ff::widenPos(dmin2f)));
+        return nsdg_ff::viscFloatFloat(inv, Pa, dmin2f, d2l, rsqrtf(inv + dmin2f));
     } else {
-        const float y0 = rsqrtf(inv + dmin2f);
-        const double yd = VM == 1 ? static_cast<double>(y0) : widenPos(y0);
-        const double yh = VM == 1 ? 0.5 * yd : widenHalfPos(y0);
-        const double h = t * yd;
-        const double e2 = fma(-h, yh, 0.5); // (1 - t y0^2) / 2
-        const double z = Pa * yd;
-        const double z8 = fma(z, e2, z);
-        return VM == 1 ? static_cast<float>(z8) : narrowPos(z8);
+        const double td = VM == 2 ? widenNonneg(inv) : static_cast<double>(inv);
+        const double t = fma(dmin, dmin, td);
+        if constexpr (VM == 0) {
+            return static_cast<float>(Pa * rsqrt(t));
+        } else {
+            const float y0 = rsqrtf(inv + dmin2f);
+            const double yd = VM == 1 ? static_cast<double>(y0) : widenPos(y0);
+            const double yh = VM == 1 ? 0.5 * yd : widenHalfPos(y0);
+            const double h = t * yd;
+            const double e2 = fma(-h, yh, 0.5); // (1 - t y0^2) / 2
+            const double z = Pa * yd;
+            const double z8 = fma(z, e2, z);
+            return VM == 1 ? static_cast<float>(z8) : narrowPos(z8);
+        }
     }
 }
 
@@ -1869,6 +1879,16 @@ __global__ void kViscositySelfTest(size_t n, const float* __restrict__ inv, cons
     out[i] = viscosity8<0>(inv[i], Pa[i], dmin, dmin2f);
     out[n + i] = viscosity8<1>(inv[i], Pa[i], dmin, dmin2f);
     out[2 * n + i] = viscosity8<2>(inv[i], Pa[i], dmin, dmin2f);
+}
+
+// The float-float form (VM 3) at each (inv, Pa): out[n].
+__global__ void kViscositySelfTestFF(size_t n, const float* __restrict__ inv, const double* __restrict__ Pa,
+    double dmin, float* __restrict__ out)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    out[i] = viscosity8<3>(inv[i], Pa[i], dmin, static_cast<float>(dmin * dmin));
 }
 
 // Body of the mixed-precision node kernel for CG2 node i.
@@ -2657,6 +2677,7 @@ cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const flo
     switch (viscosityMode) {
     case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<0>, m, coef, ld, u, v, Pg, tdiv, p);
     case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<1>, m, coef, ld, u, v, Pg, tdiv, p);
+    case 3: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<3>, m, coef, ld, u, v, Pg, tdiv, p);
     default: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<2>, m, coef, ld, u, v, Pg, tdiv, p);
     }
 }
@@ -2665,6 +2686,13 @@ cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, 
     float* out)
 {
     kViscositySelfTest<<<blocksFor(n), kBlock, 0, s>>>(n, inv, Pa, dmin, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchViscositySelfTestFF(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
+    float* out)
+{
+    kViscositySelfTestFF<<<blocksFor(n), kBlock, 0, s>>>(n, inv, Pa, dmin, out);
     return cudaGetLastError();
 }
 

@@ -245,12 +245,17 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
 // per device (they depend only on the basis), and 5 coefficients per element
 // ([5][ld]).  viscosityMode selects the FP64 evaluation of P/(8 alpha Delta):
 // 0 CUDA's rsqrt(double), 1 a Newton step from an FP32 seed, 2 the same with
-// float/double conversions on the integer pipe.
+// float/double conversions on the integer pipe (the default); 3 the same
+// Newton step with float pairs on the FP32 pipe (nsdg_visc_ff.hpp; reached
+// only through nsdg_kernel_time_kernel).
 cudaError_t uploadAffineReference(const double ref[4][81]);
 cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
     const float* v, const double* Pg, float* tdiv, const MevpParams& p, int viscosityMode);
 // out[k n + i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode k = 0, 1, 2.
 cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
+    float* out);
+// out[i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode 3.
+cudaError_t launchViscositySelfTestFF(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
     float* out);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);

@@ -104,6 +104,21 @@ def selftest_viscosity(inv, pa, delta_min: float) -> np.ndarray:
     return out.reshape(3, inv.size)
 
 
+def selftest_viscosity_ff(inv, pa, delta_min: float) -> np.ndarray:
+    """The same quantity by the float-pair form 3 (FP32 pipe), shape (n,)
+    float32 (see nsdg_selftest_viscosity_ff)."""
+    lib = _lib.load()
+    inv = np.ascontiguousarray(inv, dtype=np.float32)
+    pa = np.ascontiguousarray(pa, dtype=np.float64)
+    if inv.shape != pa.shape or inv.ndim != 1:
+        raise ValueError("inv and pa must be 1-D arrays of the same length")
+    out = np.empty(inv.size, dtype=np.float32)
+    st = lib.nsdg_selftest_viscosity_ff(inv.size, _ptr(inv), _ptr(pa), float(delta_min), _ptr(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "selftest_viscosity_ff failed")
+    return out
+
+
 class _KernelBase:
     rheology = _lib.RHEOLOGY_MEVP
 
