@@ -584,17 +584,18 @@ def run_ours(args, world, rank, local):
     h, a = pin(k.getDG0Data("hice")), pin(k.getDG0Data("cice"))
     outs = {n: pin(np.empty(N)) for n in ("hice", "cice", "u", "v", "uiostress", "viostress")}
 
-    def cycle(s):
-        k.setData("hice", outs["hice"] if s else h)
-        k.setData("cice", outs["cice"] if s else a)
-        k.setData("uwind", winds[s][0])
-        k.setData("vwind", winds[s][1])
-        k.setData("uocean", uo)
-        k.setData("vocean", vo)
-        k.setData("ssh", ssh)
-        k.update(s * DT, DT)
+    def cycle(s, kk=None):
+        kk = k if kk is None else kk
+        kk.setData("hice", outs["hice"] if s else h)
+        kk.setData("cice", outs["cice"] if s else a)
+        kk.setData("uwind", winds[s][0])
+        kk.setData("vwind", winds[s][1])
+        kk.setData("uocean", uo)
+        kk.setData("vocean", vo)
+        kk.setData("ssh", ssh)
+        kk.update(s * DT, DT)
         for n, buf in outs.items():
-            k.getDG0Data(n, out=buf)
+            kk.getDG0Data(n, out=buf)
 
     for s in range(args.warmup):
         cycle(s)
@@ -612,6 +613,7 @@ def run_ours(args, world, rank, local):
     t_e2e = statistics.median(trials)
     e2e = world * N * args.steps / t_e2e
     e2e_trials = [world * N * args.steps / t for t in trials]
+    e2e_calls = e2e_call_breakdown(k, cycle, args.warmup, args.steps) if args.e2e_calls else None
 
     roof, node = stress_roofline(k, N, prec, ms_max / args.steps, local, args.nx)
     k.close()
@@ -661,7 +663,8 @@ def run_ours(args, world, rank, local):
                              "besides the sub-cycle's ~110 MB working set",
                        "bytes_per_cell_update": bytes_per_cell_update(word=4 if prec else 8)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8,
-                    "trials": e2e_trials, "timing": "median of 3 repetitions of the timed steps, wall clock"},
+                    "trials": e2e_trials, "timing": "median of 3 repetitions of the timed steps, wall clock",
+                    **({"calls_us": e2e_calls} if e2e_calls else {})},
             "gpu_launches": launches * args.steps,
             "roofline": roof,
             "node_kernel": node,
@@ -674,6 +677,39 @@ def run_ours(args, world, rank, local):
         if variants:
             line["variants"] = variants
         print(json.dumps(line), flush=True)
+
+
+def e2e_call_breakdown(k, cycle, start: int, steps: int) -> dict:
+    """Median wall-clock microseconds of each call of the module cycle
+    (--e2e-calls): the calls of `cycle` are timed one by one, with an explicit
+    wait for the step after `update` so that the first read times only its own
+    work.  Runs after the timed region; not part of any reported rate."""
+    samples: dict[str, list[float]] = {}
+
+    class Timed:
+        def __init__(self, inner):
+            self._k = inner
+
+        def __getattr__(self, name):
+            fn = getattr(self._k, name)
+
+            def timed(*a, **kw):
+                label = f"{name}({a[0]})" if name in ("setData", "getDG0Data") else name
+                t0 = time.perf_counter()
+                r = fn(*a, **kw)
+                if name == "update":
+                    samples.setdefault("update (enqueue)", []).append((time.perf_counter() - t0) * 1e6)
+                    t0 = time.perf_counter()
+                    self._k.synchronize()
+                    label = "wait for the step"
+                samples.setdefault(label, []).append((time.perf_counter() - t0) * 1e6)
+                return r
+            return timed
+
+    proxy = Timed(k)
+    for s in range(start, start + steps):
+        cycle(s, proxy)
+    return {name: statistics.median(v) for name, v in samples.items()}
 
 
 def ensemble_boxes(n_members: int, seed: int = 2024):
@@ -761,6 +797,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--e2e-calls", action="store_true",
+                    help="add e2e.calls_us: median microseconds of each call of the module cycle")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time a batched ensemble of this many box tests (mixed precision) instead")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
