@@ -372,6 +372,59 @@ int nsdg_mean_value_noalloc(int dg, size_t n_elements, const double* phi, const 
     double* out, void* stream);
 
 /* ======================================================================== */
+/* Restart and forcing files: ParaGridIO's NetCDF-4 layout (reading)         */
+/* ======================================================================== */
+/* Replaces the netCDF-C reads of ParaGridIO::getModelState
+ * (core/src/ParaGridIO.cpp:87-208) and ParaGridIO::readForcingTimeStatic
+ * (core/src/ParaGridIO.cpp:210-270) with a self-contained host reader of the
+ * HDF5 subset netCDF-4 files use (no netCDF or HDF5 library needed).  A file
+ * holds the groups "structure" (attribute "type"), "metadata" and "data";
+ * the model fields are the variables of "data".  Host code only: no GPU is
+ * touched; the values go to a kernel handle through nsdg_kernel_set_data. */
+typedef struct nsdg_restart nsdg_restart;
+
+/* ModelArray::Type (core/src/discontinuousgalerkin/include/ModelArrayDetails.hpp:19-28) */
+#define NSDG_MA_H 0
+#define NSDG_MA_VERTEX 1
+#define NSDG_MA_U 2
+#define NSDG_MA_V 3
+#define NSDG_MA_Z 4
+#define NSDG_MA_DG 5
+#define NSDG_MA_DGSTRESS 6
+#define NSDG_MA_CG 7
+#define NSDG_MA_NONE (-1) /* no ModelArray type for the variable's dimensions */
+
+/* Opens and maps a file; NSDG_ERR_BAD_ARG when it cannot be opened,
+ * NSDG_ERR_UNSUPPORTED for HDF5 features outside the subset (compression,
+ * old-style groups), NSDG_ERR_LOGIC for a damaged file (message in
+ * nsdg_restart_last_error of the returned handle, or of NULL). */
+int nsdg_restart_open(const char* path, nsdg_restart** out);
+int nsdg_restart_close(nsdg_restart* r);
+const char* nsdg_restart_last_error(const nsdg_restart* r);
+/* Number of netCDF variables in a group ("data", "metadata/time"; "" is the
+ * root group), in creation order; NSDG_ERR_UNKNOWN_FIELD for no such group. */
+int nsdg_restart_num_vars(nsdg_restart* r, const char* group, size_t* n);
+/* Variable `index` of `group`: its name (NUL-terminated, at most name_cap
+ * bytes), the ModelArray type its dimension names give (the dimension keys
+ * of ParaGridIO.cpp:34-47, accepting the time record dimension of forcing
+ * files in front), the component count (DG, DGSTRESS, VERTEX: the last
+ * dimension; otherwise 1), the number of time records (1 for variables
+ * without the unlimited "time" dimension) and the values per record.  Any
+ * output pointer may be NULL. */
+int nsdg_restart_var_info(nsdg_restart* r, const char* group, size_t index, char* name, size_t name_cap,
+    int* model_type, size_t* n_components, size_t* n_records, size_t* n_values);
+/* The variable's dimension names, comma-separated in netCDF order ("time,y,x"). */
+int nsdg_restart_dim_names(nsdg_restart* r, const char* path, char* out, size_t cap);
+/* Record `record` of the variable at `path` ("data/hice") as double, in
+ * ModelArray order (index = component + n_components (i + nx j), the order
+ * the file stores); n must equal the values per record. */
+int nsdg_restart_read(nsdg_restart* r, const char* path, size_t record, double* out, size_t n);
+/* A text attribute of the object at `path` (attribute non-NULL: "structure"
+ * and "type"), or the first string of a string variable (attribute NULL:
+ * "metadata/time/formatted").  NSDG_ERR_SIZE_MISMATCH when cap is too small. */
+int nsdg_restart_text(nsdg_restart* r, const char* path, const char* attribute, char* out, size_t cap);
+
+/* ======================================================================== */
 /* Column thermodynamics: ice growth (the step before the dynamics)          */
 /* ======================================================================== */
 /* IceGrowth::update (physics/src/IceGrowth.cpp:148-171) on the GPU with the

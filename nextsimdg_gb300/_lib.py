@@ -141,6 +141,15 @@ SIGNATURES = [
     ("nsdg_ice_growth_update", c_int, [c_void_p, c_double]),
     ("nsdg_ice_growth_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
     ("nsdg_ice_growth_exchange", c_int, [c_void_p, c_void_p, c_int]),
+    ("nsdg_restart_open", c_int, [c_char_p, POINTER(c_void_p)]),
+    ("nsdg_restart_close", c_int, [c_void_p]),
+    ("nsdg_restart_last_error", c_char_p, [c_void_p]),
+    ("nsdg_restart_num_vars", c_int, [c_void_p, c_char_p, POINTER(c_size_t)]),
+    ("nsdg_restart_var_info", c_int, [c_void_p, c_char_p, c_size_t, c_char_p, c_size_t, POINTER(c_int),
+                                       POINTER(c_size_t), POINTER(c_size_t), POINTER(c_size_t)]),
+    ("nsdg_restart_dim_names", c_int, [c_void_p, c_char_p, c_char_p, c_size_t]),
+    ("nsdg_restart_read", c_int, [c_void_p, c_char_p, c_size_t, c_void_p, c_size_t]),
+    ("nsdg_restart_text", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_size_t]),
 ]
 
 _lib = None

@@ -1,0 +1,211 @@
+// nsdg_restart_capi.cpp — the C ABI of the restart and forcing file reader
+// (nsdg_restart_* in include/nsdg.h): ParaGridIO::getModelState and
+// ParaGridIO::readForcingTimeStatic (core/src/ParaGridIO.cpp:87-270) over
+// the host reader in nsdg_restart.cpp.
+#include "nsdg.h"
+#include "nsdg_restart.hpp"
+
+#include <cstring>
+#include <map>
+#include <string>
+
+struct nsdg_restart {
+    std::unique_ptr<nsdg_nc::File> file;
+    std::string error;
+};
+
+namespace {
+
+thread_local std::string gOpenError;
+
+// ParaGridIO's dimension keys (core/src/ParaGridIO.cpp:34-47): the netCDF
+// dimension names of a variable, concatenated in file order
+int modelType(const std::string& key)
+{
+    static const std::map<std::string, int> keys = {
+        { "yx", NSDG_MA_H },
+        { "ydimxdim", NSDG_MA_H },
+        { "zyx", NSDG_MA_Z },
+        { "zdimydimxdim", NSDG_MA_Z },
+        { "yxdg_comp", NSDG_MA_DG },
+        { "ydimxdimdg_comp", NSDG_MA_DG },
+        { "yxdgstress_comp", NSDG_MA_DGSTRESS },
+        { "ydimxdimdgstress_comp", NSDG_MA_DGSTRESS },
+        { "ycgxcg", NSDG_MA_CG },
+        { "yvertexxvertexncoords", NSDG_MA_VERTEX },
+    };
+    const auto it = keys.find(key);
+    return it == keys.end() ? NSDG_MA_NONE : it->second;
+}
+
+// the leading record dimension of forcing files
+bool isRecordDim(const nsdg_nc::Variable& v)
+{
+    return !v.dims.empty() && v.dimNames[0] == "time" && v.dims.size() > 1;
+}
+
+template <class F>
+int guarded(nsdg_restart* r, F&& f)
+{
+    if (!r)
+        return NSDG_ERR_BAD_ARG;
+    try {
+        r->error.clear();
+        return f();
+    } catch (const nsdg_nc::Unsupported& e) {
+        r->error = e.what();
+        return NSDG_ERR_UNSUPPORTED;
+    } catch (const nsdg_nc::FormatError& e) {
+        r->error = e.what();
+        return NSDG_ERR_LOGIC;
+    } catch (const std::out_of_range& e) {
+        r->error = e.what();
+        return NSDG_ERR_UNKNOWN_FIELD;
+    } catch (const std::exception& e) {
+        r->error = e.what();
+        return NSDG_ERR_BAD_ARG;
+    }
+}
+
+int copyText(const std::string& s, char* out, size_t cap)
+{
+    if (!out || cap == 0)
+        return NSDG_ERR_BAD_ARG;
+    if (s.size() + 1 > cap)
+        return NSDG_ERR_SIZE_MISMATCH;
+    std::memcpy(out, s.c_str(), s.size() + 1);
+    return NSDG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int nsdg_restart_open(const char* path, nsdg_restart** out)
+{
+    if (!path || !out)
+        return NSDG_ERR_BAD_ARG;
+    *out = nullptr;
+    try {
+        auto r = std::make_unique<nsdg_restart>();
+        r->file = std::make_unique<nsdg_nc::File>(path);
+        r->file->at(""); // parses the root group
+        *out = r.release();
+        gOpenError.clear();
+        return NSDG_OK;
+    } catch (const nsdg_nc::Unsupported& e) {
+        gOpenError = e.what();
+        return NSDG_ERR_UNSUPPORTED;
+    } catch (const nsdg_nc::FormatError& e) {
+        gOpenError = e.what();
+        return NSDG_ERR_LOGIC;
+    } catch (const std::exception& e) {
+        gOpenError = e.what();
+        return NSDG_ERR_BAD_ARG;
+    }
+}
+
+int nsdg_restart_close(nsdg_restart* r)
+{
+    delete r;
+    return NSDG_OK;
+}
+
+const char* nsdg_restart_last_error(const nsdg_restart* r)
+{
+    return r ? r->error.c_str() : gOpenError.c_str();
+}
+
+int nsdg_restart_num_vars(nsdg_restart* r, const char* group, size_t* n)
+{
+    return guarded(r, [&] {
+        if (!n)
+            return NSDG_ERR_BAD_ARG;
+        *n = r->file->variables(group ? group : "").size();
+        return NSDG_OK;
+    });
+}
+
+int nsdg_restart_var_info(nsdg_restart* r, const char* group, size_t index, char* name, size_t name_cap,
+    int* model_type, size_t* n_components, size_t* n_records, size_t* n_values)
+{
+    return guarded(r, [&] {
+        const auto vars = r->file->variables(group ? group : "");
+        if (index >= vars.size())
+            return NSDG_ERR_BAD_ARG;
+        const auto& v = vars[index];
+        const size_t skip = isRecordDim(v) ? 1 : 0;
+        std::string key;
+        for (size_t i = skip; i < v.dimNames.size(); ++i)
+            key += v.dimNames[i];
+        const int type = modelType(key);
+        size_t values = 1;
+        for (size_t i = skip; i < v.dims.size(); ++i)
+            values *= v.dims[i];
+        if (name) {
+            const int st = copyText(v.name, name, name_cap);
+            if (st != NSDG_OK)
+                return st;
+        }
+        if (model_type)
+            *model_type = type;
+        if (n_components)
+            *n_components = (type == NSDG_MA_DG || type == NSDG_MA_DGSTRESS || type == NSDG_MA_VERTEX)
+                ? v.dims.back() : 1;
+        if (n_records)
+            *n_records = skip ? v.dims[0] : 1;
+        if (n_values)
+            *n_values = values;
+        return NSDG_OK;
+    });
+}
+
+int nsdg_restart_dim_names(nsdg_restart* r, const char* path, char* out, size_t cap)
+{
+    return guarded(r, [&] {
+        if (!path)
+            return NSDG_ERR_BAD_ARG;
+        const auto v = r->file->variable(path);
+        std::string s;
+        for (size_t i = 0; i < v.dimNames.size(); ++i)
+            s += (i ? "," : "") + v.dimNames[i];
+        return copyText(s, out, cap);
+    });
+}
+
+int nsdg_restart_read(nsdg_restart* r, const char* path, size_t record, double* out, size_t n)
+{
+    return guarded(r, [&] {
+        if (!path || (!out && n))
+            return NSDG_ERR_BAD_ARG;
+        const auto v = r->file->variable(path);
+        const bool rec = isRecordDim(v);
+        const uint64_t records = rec ? v.dims[0] : 1;
+        uint64_t per = 1;
+        for (size_t i = rec ? 1 : 0; i < v.dims.size(); ++i)
+            per *= v.dims[i];
+        if (record >= records)
+            return NSDG_ERR_BAD_ARG;
+        if (n != per)
+            return NSDG_ERR_SIZE_MISMATCH;
+        r->file->readDoubles(*v.obj, record * per, per, out);
+        return NSDG_OK;
+    });
+}
+
+int nsdg_restart_text(nsdg_restart* r, const char* path, const char* attribute, char* out, size_t cap)
+{
+    return guarded(r, [&] {
+        if (!path)
+            return NSDG_ERR_BAD_ARG;
+        const auto& o = r->file->at(path);
+        if (!attribute)
+            return copyText(r->file->readText(o), out, cap);
+        const auto* a = o.attr(attribute);
+        if (!a)
+            throw std::out_of_range(std::string("no attribute ") + attribute + " on " + path);
+        return copyText(r->file->attrText(*a), out, cap);
+    });
+}
+
+} // extern "C"

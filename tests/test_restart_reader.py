@@ -1,0 +1,159 @@
+"""Restart and forcing file reader (nsdg_restart_* in include/nsdg.h,
+nextsimdg_gb300/restart.py): ParaGridIO's read side without netCDF or HDF5.
+
+Pinned on the reference's own input file core/test/ParaGridIO_input_test.nc
+(written by netCDF4-python through core/test/ParaGridIO_input_test.py; read
+by the reference test "Test array ordering", core/test/ParaGrid_test.cpp:
+478-519, which asserts index2d(3, 5) == 35).  The file's contents follow from
+the generating script: on a 9 x 11 grid, index2d = 10 x + y, longitude = x,
+latitude = y, one time record at 0 s, the "structure" type
+"parametric_rectangular" and the metadata time "1970-01-01T00:00:00Z".  Its
+HDF5 checksums (superblock, object headers, continuation chunks) are all
+verified on the way, which also pins the lookup3 checksum; lookup3 itself is
+checked against the published test values of Jenkins' lookup3.c driver.
+Damaged files (truncated, flipped bytes, bad checksums) must give an error
+status, never a crash: checked by mutating the fixture in child processes."""
+import os
+import shutil
+import subprocess
+import sys
+import textwrap
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+FIXTURE = Path(os.environ.get("NSDG_REFERENCE", "/root/reference")) / "core" / "test" / "ParaGridIO_input_test.nc"
+needs_fixture = pytest.mark.skipif(not FIXTURE.exists(), reason="the reference's test input is not on this machine")
+
+
+@pytest.fixture(scope="module")
+def lib_built():
+    from nextsimdg_gb300 import build
+    build.build()
+
+
+def test_lookup3_known_answers(tmp_path):
+    src = tmp_path / "l3.cpp"
+    src.write_text(textwrap.dedent("""
+        #include "nsdg_restart.hpp"
+        #include <cstdio>
+        int main() {
+            const char* s = "Four score and seven years ago";
+            const uint8_t* e = reinterpret_cast<const uint8_t*>("");
+            const uint8_t* f = reinterpret_cast<const uint8_t*>(s);
+            std::printf("%08x %08x %08x %08x\\n", nsdg_nc::lookup3(e, 0, 0), nsdg_nc::lookup3(e, 0, 0xdeadbeef),
+                nsdg_nc::lookup3(f, 30, 0), nsdg_nc::lookup3(f, 30, 1));
+        }"""))
+    exe = tmp_path / "l3"
+    csrc = ROOT / "nextsimdg_gb300" / "csrc"
+    subprocess.run([shutil.which("g++") or "g++", "-std=c++17", "-O2", "-I", str(csrc), str(src),
+                    str(csrc / "nsdg_restart.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["deadbeef", "bd5b7dde", "17770551", "cd628161"]
+
+
+@needs_fixture
+def test_reference_input_file(lib_built):
+    from nextsimdg_gb300.restart import ParaGridFile
+    with ParaGridFile(FIXTURE) as f:
+        assert f.structure_type() == "parametric_rectangular"
+        assert f.text("metadata", "type") == "parametric_rectangular"
+        assert f.metadata_time() == (0.0, "1970-01-01T00:00:00Z")
+        assert f.text("metadata/time/formatted") == "1970-01-01T00:00:00Z"
+        assert f.text("metadata/time/formatted", "format") == "%Y-%m-%dT%H:%M:%SZ"
+        assert f.text("metadata/time/time", "units") == "seconds since 1970-01-01T00:00:00Z"
+        vs = {v.name: v for v in f.variables("data")}
+        assert list(vs) == ["longitude", "latitude", "time", "index2d"]
+        assert vs["index2d"].dim_names == ("time", "y", "x")
+        assert (vs["index2d"].model_type, vs["index2d"].n_records, vs["index2d"].n_values) == ("H", 1, 99)
+        assert vs["longitude"].dim_names == ("y", "x") and vs["longitude"].model_type == "H"
+        assert vs["time"].dim_names == ("time",) and vs["time"].model_type is None
+        x, y = np.meshgrid(np.arange(9), np.arange(11))
+        idx = f.read("data/index2d")
+        np.testing.assert_array_equal(idx, (10 * x + y).ravel())
+        # ModelArray index i + nx j: the reference's index2d(3, 5) == 35
+        assert idx[3 + 9 * 5] == 35
+        np.testing.assert_array_equal(f.read("data/longitude"), x.ravel())
+        np.testing.assert_array_equal(f.read("data/latitude"), y.ravel())
+        np.testing.assert_array_equal(f.read("data/time"), [0.0])
+
+
+@needs_fixture
+def test_read_forcing_time_static_and_get_model_state(lib_built):
+    from nextsimdg_gb300.restart import ParaGridFile
+    with ParaGridFile(FIXTURE) as f:
+        for t in (-3600.0, 0.0, 86400.0):  # before, at and after the only record
+            st = f.read_forcing_time_static({"index2d", "not_in_file"}, t)
+            assert set(st) == {"index2d"}
+            assert st["index2d"][3 + 9 * 5] == 35
+        # the data group's "time" variable has no ModelArray type: the
+        # reference's getModelState throws std::out_of_range for it
+        with pytest.raises(KeyError, match="dimensional key time"):
+            f.get_model_state()
+
+
+@needs_fixture
+def test_errors_are_statuses(lib_built, tmp_path):
+    from nextsimdg_gb300._lib import NsdgError
+    from nextsimdg_gb300.restart import ParaGridFile
+    with pytest.raises(FileNotFoundError):
+        ParaGridFile(tmp_path / "a44f5cc1f7934a8ae8dd03a95308745d.nc")
+    (tmp_path / "text.nc").write_text("netcdf not really\n" * 8)
+    with pytest.raises(NsdgError):
+        ParaGridFile(tmp_path / "text.nc")
+    b = bytearray(FIXTURE.read_bytes())
+    b[0x40] ^= 0x01  # inside the root object header: its checksum no longer holds
+    (tmp_path / "flip.nc").write_bytes(bytes(b))
+    with pytest.raises(NsdgError, match="checksum"):
+        ParaGridFile(tmp_path / "flip.nc")
+    (tmp_path / "cut.nc").write_bytes(FIXTURE.read_bytes()[:0x800])
+    with pytest.raises(NsdgError):
+        with ParaGridFile(tmp_path / "cut.nc") as f:
+            f.read("data/index2d")
+    with ParaGridFile(FIXTURE) as f:
+        with pytest.raises(KeyError):
+            f.read("data/hice")
+        with pytest.raises(KeyError):
+            f.variables("nodata")
+
+
+_PROBE = """
+import sys
+from nextsimdg_gb300.restart import ParaGridFile
+from nextsimdg_gb300._lib import NsdgError
+for p in sys.argv[1:]:
+    try:
+        with ParaGridFile(p) as f:
+            for g in ("data", "metadata/time"):
+                for v in f.variables(g):
+                    try:
+                        f.read(g + "/" + v.name) if v.n_values < 10**7 else None
+                    except (NsdgError, KeyError):
+                        pass
+            f.structure_type()
+    except (NsdgError, KeyError, FileNotFoundError, UnicodeDecodeError):
+        pass
+print("survived")
+"""
+
+
+@needs_fixture
+def test_damaged_files_never_crash(lib_built, tmp_path):
+    rng = np.random.default_rng(11)
+    src = FIXTURE.read_bytes()
+    paths = []
+    for i in range(120):
+        b = bytearray(src)
+        for pos in rng.integers(0, len(b), rng.integers(1, 9)):
+            b[pos] = int(rng.integers(0, 256))
+        if i % 5 == 0:
+            b = b[: int(rng.integers(48, len(b)))]
+        p = tmp_path / f"m{i}.nc"
+        p.write_bytes(bytes(b))
+        paths.append(str(p))
+    env = dict(os.environ, PYTHONPATH=str(ROOT))
+    r = subprocess.run([sys.executable, "-c", _PROBE, *paths], capture_output=True, text=True, env=env,
+                       timeout=300)
+    assert r.returncode == 0 and "survived" in r.stdout, r.stderr[-2000:]
