@@ -424,6 +424,23 @@ int nsdg_restart_read(nsdg_restart* r, const char* path, size_t record, double* 
  * "metadata/time/formatted").  NSDG_ERR_SIZE_MISMATCH when cap is too small. */
 int nsdg_restart_text(nsdg_restart* r, const char* path, const char* attribute, char* out, size_t cap);
 
+/* Writing: ParaGridIO::dumpModelState (core/src/ParaGridIO.cpp:272-348)
+ * with CommonRestartMetadata's "structure" and "metadata" groups
+ * (core/src/CommonRestartMetadata.cpp:18-72).  create() lays out the groups,
+ * the metadata time (seconds since 1970 and its formatted string) and every
+ * dimension of the data group (xdim, ydim, zdim, xvertex, yvertex, x_cg,
+ * y_cg, dg_comp, dgstress_comp, ncoords); add() copies one field in
+ * ModelArray order with the dimensions of its type and a missing_value
+ * attribute; save() writes the file (NetCDF-4 layout, contiguous doubles).
+ * The writer is host memory only. */
+typedef struct nsdg_restart_writer nsdg_restart_writer;
+int nsdg_restart_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
+    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out);
+int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_type, const double* data, size_t n);
+int nsdg_restart_writer_save(nsdg_restart_writer* w, const char* path);
+int nsdg_restart_writer_destroy(nsdg_restart_writer* w);
+const char* nsdg_restart_writer_last_error(const nsdg_restart_writer* w);
+
 /* ======================================================================== */
 /* Column thermodynamics: ice growth (the step before the dynamics)          */
 /* ======================================================================== */

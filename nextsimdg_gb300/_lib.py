@@ -150,6 +150,12 @@ SIGNATURES = [
     ("nsdg_restart_dim_names", c_int, [c_void_p, c_char_p, c_char_p, c_size_t]),
     ("nsdg_restart_read", c_int, [c_void_p, c_char_p, c_size_t, c_void_p, c_size_t]),
     ("nsdg_restart_text", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_size_t]),
+    ("nsdg_restart_writer_create", c_int, [c_size_t, c_size_t, c_size_t, c_int, c_int, c_int, c_char_p,
+                                            ctypes.c_longlong, c_char_p, POINTER(c_void_p)]),
+    ("nsdg_restart_writer_add", c_int, [c_void_p, c_char_p, c_int, c_void_p, c_size_t]),
+    ("nsdg_restart_writer_save", c_int, [c_void_p, c_char_p]),
+    ("nsdg_restart_writer_destroy", c_int, [c_void_p]),
+    ("nsdg_restart_writer_last_error", c_char_p, [c_void_p]),
 ]
 
 _lib = None

@@ -145,4 +145,30 @@ private:
     std::vector<std::string> dimNames(const Object& o, const std::string& group);
 };
 
+// Builder of a file in the same subset (nsdg_restart_write.cpp).  Node 0 is
+// the root group; nodes are groups, dimension scales or variables.
+class Writer {
+public:
+    Writer();
+    ~Writer();
+    int addGroup(int parent, const std::string& name);
+    void attrText(int node, const std::string& name, const std::string& value);
+    void attrDouble(int node, const std::string& name, double value);
+    void attrInt(int node, const std::string& name, int32_t value);
+    // a netCDF dimension without a coordinate variable
+    int addDimension(int group, const std::string& name, uint64_t length, int dimid);
+    // a double variable over dimension nodes (slowest first), data row-major
+    int addDouble(int group, const std::string& name, const std::vector<int>& dims, const double* data);
+    // a scalar int64 variable
+    int addInt64(int group, const std::string& name, int64_t value);
+    std::vector<uint8_t> serialize();
+    void save(const std::string& path);
+
+private:
+    struct Attr;
+    struct Node;
+    std::vector<Node> nodes_;
+    std::vector<uint8_t> header(const Node& n, uint64_t heapAddr) const;
+};
+
 } // namespace nsdg_nc

@@ -209,3 +209,128 @@ int nsdg_restart_text(nsdg_restart* r, const char* path, const char* attribute, 
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------- writer
+struct nsdg_restart_writer {
+    nsdg_nc::Writer w;
+    std::string error;
+    size_t nx = 0, ny = 0, nz = 1;
+    int dg = 0, dgs = 0, cg = 2;
+    int data = 0;
+    int dim[10] = {}; // xdim ydim zdim xvertex yvertex x_cg y_cg dg_comp dgstress_comp ncoords
+};
+
+extern "C" {
+
+int nsdg_restart_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
+    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out)
+{
+    if (!out || !structure_type || !time_formatted || nx == 0 || ny == 0 || nz == 0 || dg_comp <= 0
+        || dgstress_comp <= 0 || (cg_degree != 1 && cg_degree != 2))
+        return NSDG_ERR_BAD_ARG;
+    auto r = std::make_unique<nsdg_restart_writer>();
+    r->nx = nx;
+    r->ny = ny;
+    r->nz = nz;
+    r->dg = dg_comp;
+    r->dgs = dgstress_comp;
+    r->cg = cg_degree;
+    auto& w = r->w;
+    // CommonRestartMetadata::writeStructureType and writeRestartMetadata
+    w.attrText(w.addGroup(0, "structure"), "type", structure_type);
+    const int meta = w.addGroup(0, "metadata");
+    w.attrText(meta, "type", structure_type);
+    const int timeGroup = w.addGroup(meta, "time");
+    const int t = w.addInt64(timeGroup, "time", time_seconds);
+    w.attrText(t, "units", "seconds since 1970-01-01T00:00:00Z");
+    w.attrText(t, "format", "%Y-%m-%dT%H:%M:%SZ");
+    w.attrText(t, "formatted", time_formatted);
+    w.addGroup(meta, "configuration");
+    // ParaGridIO::dumpModelState: every defined dimension, in
+    // ModelArray::Dimension order (ModelArrayDetails.cpp:30-43)
+    r->data = w.addGroup(0, "data");
+    const char* names[10] = { "xdim", "ydim", "zdim", "xvertex", "yvertex", "x_cg", "y_cg", "dg_comp",
+        "dgstress_comp", "ncoords" };
+    const uint64_t sizes[10] = { nx, ny, nz, nx + 1, ny + 1, cg_degree * nx + 1, cg_degree * ny + 1,
+        static_cast<uint64_t>(dg_comp), static_cast<uint64_t>(dgstress_comp), 2 };
+    for (int i = 0; i < 10; ++i)
+        r->dim[i] = w.addDimension(r->data, names[i], sizes[i], i);
+    *out = r.release();
+    return NSDG_OK;
+}
+
+int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_type, const double* data, size_t n)
+{
+    if (!w || !name || !*name || (!data && n))
+        return NSDG_ERR_BAD_ARG;
+    const int* d = w->dim;
+    std::vector<int> dims; // netCDF order, as dumpModelState builds dimMap
+    switch (model_type) {
+    case NSDG_MA_H:
+    case NSDG_MA_U:
+    case NSDG_MA_V:
+        dims = { d[1], d[0] };
+        break;
+    case NSDG_MA_Z:
+        dims = { d[2], d[1], d[0] };
+        break;
+    case NSDG_MA_DG:
+        dims = { d[1], d[0], d[7] };
+        break;
+    case NSDG_MA_DGSTRESS:
+        dims = { d[1], d[0], d[8] };
+        break;
+    case NSDG_MA_CG:
+        dims = { d[6], d[5] };
+        break;
+    case NSDG_MA_VERTEX:
+        dims = { d[4], d[3], d[9] };
+        break;
+    default:
+        return NSDG_ERR_BAD_ARG;
+    }
+    size_t expect = 1;
+    const size_t sizes[10] = { w->nx, w->ny, w->nz, w->nx + 1, w->ny + 1, w->cg * w->nx + 1, w->cg * w->ny + 1,
+        static_cast<size_t>(w->dg), static_cast<size_t>(w->dgs), 2 };
+    for (int id : dims)
+        for (int k = 0; k < 10; ++k)
+            if (w->dim[k] == id)
+                expect *= sizes[k];
+    if (n != expect)
+        return NSDG_ERR_SIZE_MISMATCH;
+    try {
+        const int v = w->w.addDouble(w->data, name, dims, data);
+        w->w.attrDouble(v, "missing_value", 1.7e38); // MissingData::defaultValue
+        return NSDG_OK;
+    } catch (const std::exception& e) {
+        w->error = e.what();
+        return NSDG_ERR_BAD_ARG;
+    }
+}
+
+int nsdg_restart_writer_save(nsdg_restart_writer* w, const char* path)
+{
+    if (!w || !path)
+        return NSDG_ERR_BAD_ARG;
+    try {
+        w->error.clear();
+        w->w.save(path);
+        return NSDG_OK;
+    } catch (const std::exception& e) {
+        w->error = e.what();
+        return NSDG_ERR_BAD_ARG;
+    }
+}
+
+int nsdg_restart_writer_destroy(nsdg_restart_writer* w)
+{
+    delete w;
+    return NSDG_OK;
+}
+
+const char* nsdg_restart_writer_last_error(const nsdg_restart_writer* w)
+{
+    return w ? w->error.c_str() : "";
+}
+
+} // extern "C"

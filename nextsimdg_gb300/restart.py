@@ -13,6 +13,9 @@ Mirrors the read side of the reference's ParaGridIO (core/src/ParaGridIO.cpp):
   (:210-270): the record of the "time" axis with the largest time not after
   t (the first record when t precedes the axis), for each requested field
   present in the file (absent ones are skipped, as there).
+* ``dump_model_state(path, state, ...)`` is ParaGridIO::dumpModelState
+  (:272-348): the restart fields of the state (the reference's
+  restartFields set) written with CommonRestartMetadata's groups.
 * ``structure_type()`` is the "structure" group's "type" attribute
   (ParametricGrid checks it is "parametric_rectangular"), ``metadata_time()``
   the "metadata/time" variables ModelMetadata reads.
@@ -120,8 +123,14 @@ class ParaGridFile:
         return self.text("structure", "type")
 
     def metadata_time(self) -> tuple[float, str]:
-        """(seconds since the epoch, formatted) of "metadata/time"."""
-        return float(self.read("metadata/time/time")[0]), self.text("metadata/time/formatted")
+        """(seconds since the epoch, formatted) of "metadata/time": the
+        formatted time is an attribute of the time variable in the files
+        CommonRestartMetadata writes, a string variable in older inputs."""
+        t = float(self.read("metadata/time/time")[0])
+        try:
+            return t, self.text("metadata/time/time", "formatted")
+        except KeyError:
+            return t, self.text("metadata/time/formatted")
 
     def get_model_state(self) -> dict[str, tuple[str, np.ndarray]]:
         state = {}
@@ -138,3 +147,42 @@ class ParaGridFile:
         idx = max(idx - 1, 0)
         present = {v.name for v in self.variables("data")}
         return {f: self.read(f"data/{f}", idx) for f in fields if f in present}
+
+
+# ParaGridIO::dumpModelState's restartFields (core/src/ParaGridIO.cpp:309-311)
+RESTART_FIELDS = {"hice", "cice", "hsnow", "tice", "sst", "sss", "mask", "coords", "x", "y", "longitude",
+                  "latitude", "grid_azimuth", "u", "v", "damage"}
+_TYPE_CODES = {v: k for k, v in MODEL_TYPES.items() if v}
+
+
+def dump_model_state(path, state: dict, nx: int, ny: int, *, nz: int = 1, dg_comp: int = 6,
+                     dgstress_comp: int = 8, cg_degree: int = 2, time_seconds: int = 0,
+                     time_formatted: str = "1970-01-01T00:00:00Z",
+                     structure_type: str = "parametric_rectangular") -> list[str]:
+    """Writes the restart fields of `state` ({name: (type name, flat array in
+    ModelArray order)}) in name order, as the reference iterates its
+    std::map, and returns the names written; other names are skipped."""
+    lib = _lib.load()
+    w = c_void_p()
+    st = lib.nsdg_restart_writer_create(nx, ny, nz, dg_comp, dgstress_comp, cg_degree, structure_type.encode(),
+                                        int(time_seconds), time_formatted.encode(), byref(w))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "nsdg_restart_writer_create")
+    written = []
+    try:
+        for name in sorted(state):
+            if name not in RESTART_FIELDS:
+                continue
+            mtype, arr = state[name]
+            a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+            st = lib.nsdg_restart_writer_add(w, name.encode(), _TYPE_CODES[mtype], a.ctypes.data_as(c_void_p),
+                                             a.size)
+            if st != _lib.NSDG_OK:
+                raise NsdgError(st, f"{name}: {lib.nsdg_restart_writer_last_error(w).decode()}")
+            written.append(name)
+        st = lib.nsdg_restart_writer_save(w, str(path).encode())
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, lib.nsdg_restart_writer_last_error(w).decode())
+    finally:
+        lib.nsdg_restart_writer_destroy(w)
+    return written

@@ -1,5 +1,6 @@
-"""Restart and forcing file reader (nsdg_restart_* in include/nsdg.h,
-nextsimdg_gb300/restart.py): ParaGridIO's read side without netCDF or HDF5.
+"""Restart and forcing files (nsdg_restart_* in include/nsdg.h,
+nextsimdg_gb300/restart.py): ParaGridIO's read and write sides without
+netCDF or HDF5.
 
 Pinned on the reference's own input file core/test/ParaGridIO_input_test.nc
 (written by netCDF4-python through core/test/ParaGridIO_input_test.py; read
@@ -12,7 +13,10 @@ HDF5 checksums (superblock, object headers, continuation chunks) are all
 verified on the way, which also pins the lookup3 checksum; lookup3 itself is
 checked against the published test values of Jenkins' lookup3.c driver.
 Damaged files (truncated, flipped bytes, bad checksums) must give an error
-status, never a crash: checked by mutating the fixture in child processes."""
+status, never a crash: checked by mutating the fixture in child processes.
+The writer (dumpModelState) is checked by reading its files back: no
+netCDF-C or HDF5 library exists on either machine to read them
+independently."""
 import os
 import shutil
 import subprocess
@@ -157,3 +161,66 @@ def test_damaged_files_never_crash(lib_built, tmp_path):
     r = subprocess.run([sys.executable, "-c", _PROBE, *paths], capture_output=True, text=True, env=env,
                        timeout=300)
     assert r.returncode == 0 and "survived" in r.stdout, r.stderr[-2000:]
+
+
+def test_dump_model_state_round_trip(lib_built, tmp_path):
+    """The writer (ParaGridIO::dumpModelState) and the reader agree bit for
+    bit on every ModelArray type; only the reference's restart fields are
+    written; dimension names and sizes follow the reference's
+    definedDimensions; CG fields come back untyped because the reference's
+    read key for them ("ycgxcg") does not match the names it writes
+    ("y_cg", "x_cg"), kept as in the reference."""
+    from nextsimdg_gb300.restart import ParaGridFile, dump_model_state
+    nx, ny, nz = 13, 9, 3
+    rng = np.random.default_rng(3)
+    state = {
+        "hice": ("DG", rng.random(nx * ny * 6)),
+        "cice": ("DG", rng.random(nx * ny * 6)),
+        "damage": ("DG", rng.random(nx * ny * 6)),
+        "mask": ("H", (rng.random(nx * ny) > 0.2).astype(float)),
+        "u": ("H", rng.standard_normal(nx * ny)),
+        "coords": ("VERTEX", rng.random((nx + 1) * (ny + 1) * 2) * 1e6),
+        "tice": ("Z", -rng.random(nx * ny * nz) * 10),
+        "grid_azimuth": ("CG", rng.random((2 * nx + 1) * (2 * ny + 1))),
+        "uwind": ("H", rng.random(nx * ny)),      # not a restart field
+        "stress": ("DGSTRESS", rng.random(nx * ny * 8)),  # not a restart field
+    }
+    path = tmp_path / "restart.nc"
+    written = dump_model_state(path, state, nx, ny, nz=nz, time_seconds=86400 * 3,
+                               time_formatted="1970-01-04T00:00:00Z")
+    assert written == ["cice", "coords", "damage", "grid_azimuth", "hice", "mask", "tice", "u"]
+    with ParaGridFile(path) as f:
+        assert f.structure_type() == "parametric_rectangular"
+        assert f.metadata_time() == (259200.0, "1970-01-04T00:00:00Z")
+        assert f.text("metadata/time/time", "units") == "seconds since 1970-01-01T00:00:00Z"
+        assert f.variables("metadata/configuration") == []
+        vs = {v.name: v for v in f.variables("data")}
+        assert list(vs) == written  # dimension-only scales are not variables
+        assert vs["hice"].dim_names == ("ydim", "xdim", "dg_comp") and vs["hice"].model_type == "DG"
+        assert vs["hice"].n_components == 6
+        assert vs["coords"].dim_names == ("yvertex", "xvertex", "ncoords") and vs["coords"].model_type == "VERTEX"
+        assert vs["tice"].dim_names == ("zdim", "ydim", "xdim") and vs["tice"].model_type == "Z"
+        assert vs["grid_azimuth"].dim_names == ("y_cg", "x_cg") and vs["grid_azimuth"].model_type is None
+        for name in written:
+            np.testing.assert_array_equal(f.read(f"data/{name}"), state[name][1])
+        with pytest.raises(KeyError, match="y_cgx_cg"):
+            f.get_model_state()
+    # without the CG field, getModelState returns the state as written
+    del state["grid_azimuth"]
+    dump_model_state(path, state, nx, ny, nz=nz)
+    with ParaGridFile(path) as f:
+        got = f.get_model_state()
+    assert set(got) == {"cice", "coords", "damage", "hice", "mask", "tice", "u"}
+    for name, (mtype, arr) in got.items():
+        expect = "H" if name in ("mask", "u") else state[name][0]
+        assert mtype == expect
+        np.testing.assert_array_equal(arr, state[name][1])
+
+
+def test_writer_rejects_bad_sizes(lib_built, tmp_path):
+    from nextsimdg_gb300._lib import NsdgError
+    from nextsimdg_gb300.restart import dump_model_state
+    with pytest.raises(NsdgError):
+        dump_model_state(tmp_path / "bad.nc", {"hice": ("DG", np.zeros(10))}, 4, 4)
+    with pytest.raises(NsdgError):
+        dump_model_state(tmp_path / "no_such_dir" / "x.nc", {"hice": ("H", np.zeros(16))}, 4, 4)
