@@ -440,6 +440,22 @@ int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_
 int nsdg_restart_writer_save(nsdg_restart_writer* w, const char* path);
 int nsdg_restart_writer_destroy(nsdg_restart_writer* w);
 const char* nsdg_restart_writer_last_error(const nsdg_restart_writer* w);
+/* Diagnostic files: ParaGridIO::writeDiagnosticTime
+ * (core/src/ParaGridIO.cpp:350-500).  The same groups, with an unlimited
+ * "time" axis in the data group; each record() call is one
+ * writeDiagnosticTime call: it appends the time (seconds since 1970) and one
+ * record of every field (n_fields names, NSDG_MA_* types, data in ModelArray
+ * order, value counts).  The first call defines the variables; "mask" and
+ * VERTEX fields are written once, without the time axis, the mask with the
+ * dimensions (xdim, ydim) in the order the reference lists them; a later
+ * record naming a field the first did not gives NSDG_ERR_UNKNOWN_FIELD, and
+ * a field it leaves out holds the fill value there.  Records stay in host
+ * memory until nsdg_restart_writer_save writes the file (the reference
+ * writes them when its open file is closed). */
+int nsdg_diagnostic_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
+    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out);
+int nsdg_diagnostic_writer_record(nsdg_restart_writer* w, double time_seconds, size_t n_fields,
+    const char* const* names, const int* model_types, const double* const* data, const size_t* n);
 
 /* ======================================================================== */
 /* Column thermodynamics: ice growth (the step before the dynamics)          */

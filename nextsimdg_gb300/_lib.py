@@ -156,6 +156,10 @@ SIGNATURES = [
     ("nsdg_restart_writer_save", c_int, [c_void_p, c_char_p]),
     ("nsdg_restart_writer_destroy", c_int, [c_void_p]),
     ("nsdg_restart_writer_last_error", c_char_p, [c_void_p]),
+    ("nsdg_diagnostic_writer_create", c_int, [c_size_t, c_size_t, c_size_t, c_int, c_int, c_int, c_char_p,
+                                               ctypes.c_longlong, c_char_p, POINTER(c_void_p)]),
+    ("nsdg_diagnostic_writer_record", c_int, [c_void_p, c_double, c_size_t, POINTER(c_char_p), POINTER(c_int),
+                                               POINTER(c_void_p), POINTER(c_size_t)]),
 ]
 
 _lib = None

@@ -161,6 +161,11 @@ public:
     int addDouble(int group, const std::string& name, const std::vector<int>& dims, const double* data);
     // a scalar int64 variable
     int addInt64(int group, const std::string& name, int64_t value);
+    // the unlimited "time" axis: a coordinate variable that is its own dimension
+    int addTimeAxis(int group, const std::string& name, int dimid);
+    // a double variable over (time axis, dimension nodes...); records appended in order
+    int addRecordDouble(int group, const std::string& name, const std::vector<int>& dims);
+    void appendRecord(int var, const double* data);
     std::vector<uint8_t> serialize();
     void save(const std::string& path);
 

@@ -218,53 +218,60 @@ struct nsdg_restart_writer {
     int dg = 0, dgs = 0, cg = 2;
     int data = 0;
     int dim[10] = {}; // xdim ydim zdim xvertex yvertex x_cg y_cg dg_comp dgstress_comp ncoords
+    // diagnostic files: the time axis and the record variables by name
+    int time = -1;
+    size_t records = 0;
+    std::map<std::string, std::pair<int, int>> vars; // name -> (node, model type)
 };
 
-extern "C" {
+namespace {
 
-int nsdg_restart_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
-    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out)
+bool validShape(size_t nx, size_t ny, size_t nz, int dg, int dgs, int cg)
 {
-    if (!out || !structure_type || !time_formatted || nx == 0 || ny == 0 || nz == 0 || dg_comp <= 0
-        || dgstress_comp <= 0 || (cg_degree != 1 && cg_degree != 2))
-        return NSDG_ERR_BAD_ARG;
-    auto r = std::make_unique<nsdg_restart_writer>();
-    r->nx = nx;
-    r->ny = ny;
-    r->nz = nz;
-    r->dg = dg_comp;
-    r->dgs = dgstress_comp;
-    r->cg = cg_degree;
-    auto& w = r->w;
-    // CommonRestartMetadata::writeStructureType and writeRestartMetadata
-    w.attrText(w.addGroup(0, "structure"), "type", structure_type);
-    const int meta = w.addGroup(0, "metadata");
-    w.attrText(meta, "type", structure_type);
-    const int timeGroup = w.addGroup(meta, "time");
-    const int t = w.addInt64(timeGroup, "time", time_seconds);
-    w.attrText(t, "units", "seconds since 1970-01-01T00:00:00Z");
-    w.attrText(t, "format", "%Y-%m-%dT%H:%M:%SZ");
-    w.attrText(t, "formatted", time_formatted);
-    w.addGroup(meta, "configuration");
-    // ParaGridIO::dumpModelState: every defined dimension, in
-    // ModelArray::Dimension order (ModelArrayDetails.cpp:30-43)
-    r->data = w.addGroup(0, "data");
-    const char* names[10] = { "xdim", "ydim", "zdim", "xvertex", "yvertex", "x_cg", "y_cg", "dg_comp",
-        "dgstress_comp", "ncoords" };
-    const uint64_t sizes[10] = { nx, ny, nz, nx + 1, ny + 1, cg_degree * nx + 1, cg_degree * ny + 1,
-        static_cast<uint64_t>(dg_comp), static_cast<uint64_t>(dgstress_comp), 2 };
-    for (int i = 0; i < 10; ++i)
-        r->dim[i] = w.addDimension(r->data, names[i], sizes[i], i);
-    *out = r.release();
-    return NSDG_OK;
+    return nx && ny && nz && dg > 0 && dgs > 0 && (cg == 1 || cg == 2);
 }
 
-int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_type, const double* data, size_t n)
+// CommonRestartMetadata's groups and the data group's dimensions, in the
+// order dumpModelState (diagnostic = false) or writeDiagnosticTime
+// (diagnostic = true: metadata and data first, the time axis before the
+// other dimensions) creates them
+void layOut(nsdg_restart_writer& r, const char* structure, long long t, const char* formatted, bool diagnostic)
 {
-    if (!w || !name || !*name || (!data && n))
-        return NSDG_ERR_BAD_ARG;
-    const int* d = w->dim;
-    std::vector<int> dims; // netCDF order, as dumpModelState builds dimMap
+    auto& w = r.w;
+    int meta = 0;
+    if (!diagnostic)
+        w.attrText(w.addGroup(0, "structure"), "type", structure);
+    meta = w.addGroup(0, "metadata");
+    if (diagnostic)
+        r.data = w.addGroup(0, "data");
+    if (diagnostic)
+        w.attrText(w.addGroup(0, "structure"), "type", structure);
+    w.attrText(meta, "type", structure);
+    const int timeGroup = w.addGroup(meta, "time");
+    const int tv = w.addInt64(timeGroup, "time", t);
+    w.attrText(tv, "units", "seconds since 1970-01-01T00:00:00Z");
+    w.attrText(tv, "format", "%Y-%m-%dT%H:%M:%SZ");
+    w.attrText(tv, "formatted", formatted);
+    w.addGroup(meta, "configuration");
+    if (!diagnostic)
+        r.data = w.addGroup(0, "data");
+    int dimid = 0;
+    if (diagnostic)
+        r.time = w.addTimeAxis(r.data, "time", dimid++);
+    const char* names[10] = { "xdim", "ydim", "zdim", "xvertex", "yvertex", "x_cg", "y_cg", "dg_comp",
+        "dgstress_comp", "ncoords" };
+    const uint64_t sizes[10] = { r.nx, r.ny, r.nz, r.nx + 1, r.ny + 1, r.cg * r.nx + 1, r.cg * r.ny + 1,
+        static_cast<uint64_t>(r.dg), static_cast<uint64_t>(r.dgs), 2 };
+    for (int i = 0; i < 10; ++i)
+        r.dim[i] = w.addDimension(r.data, names[i], sizes[i], dimid++);
+}
+
+// the netCDF dimensions of a ModelArray type (dumpModelState's dimMap) and
+// the values they hold; empty for an unknown type
+std::vector<int> typeDims(const nsdg_restart_writer& w, int model_type, size_t& values)
+{
+    const int* d = w.dim;
+    std::vector<int> dims;
     switch (model_type) {
     case NSDG_MA_H:
     case NSDG_MA_U:
@@ -287,20 +294,141 @@ int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_
         dims = { d[4], d[3], d[9] };
         break;
     default:
-        return NSDG_ERR_BAD_ARG;
+        break;
     }
-    size_t expect = 1;
-    const size_t sizes[10] = { w->nx, w->ny, w->nz, w->nx + 1, w->ny + 1, w->cg * w->nx + 1, w->cg * w->ny + 1,
-        static_cast<size_t>(w->dg), static_cast<size_t>(w->dgs), 2 };
+    const size_t sizes[10] = { w.nx, w.ny, w.nz, w.nx + 1, w.ny + 1, w.cg * w.nx + 1, w.cg * w.ny + 1,
+        static_cast<size_t>(w.dg), static_cast<size_t>(w.dgs), 2 };
+    values = 1;
     for (int id : dims)
         for (int k = 0; k < 10; ++k)
-            if (w->dim[k] == id)
-                expect *= sizes[k];
+            if (d[k] == id)
+                values *= sizes[k];
+    return dims;
+}
+
+} // namespace
+
+extern "C" {
+
+int nsdg_restart_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
+    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out)
+{
+    if (!out || !structure_type || !time_formatted || !validShape(nx, ny, nz, dg_comp, dgstress_comp, cg_degree))
+        return NSDG_ERR_BAD_ARG;
+    auto r = std::make_unique<nsdg_restart_writer>();
+    r->nx = nx;
+    r->ny = ny;
+    r->nz = nz;
+    r->dg = dg_comp;
+    r->dgs = dgstress_comp;
+    r->cg = cg_degree;
+    layOut(*r, structure_type, time_seconds, time_formatted, false);
+    *out = r.release();
+    return NSDG_OK;
+}
+
+int nsdg_restart_writer_add(nsdg_restart_writer* w, const char* name, int model_type, const double* data, size_t n)
+{
+    if (!w || !name || !*name || (!data && n))
+        return NSDG_ERR_BAD_ARG;
+    if (w->time >= 0)
+        return NSDG_ERR_LOGIC; // a diagnostic file takes records
+    size_t expect = 0;
+    const std::vector<int> dims = typeDims(*w, model_type, expect);
+    if (dims.empty())
+        return NSDG_ERR_BAD_ARG;
     if (n != expect)
         return NSDG_ERR_SIZE_MISMATCH;
     try {
         const int v = w->w.addDouble(w->data, name, dims, data);
         w->w.attrDouble(v, "missing_value", 1.7e38); // MissingData::defaultValue
+        return NSDG_OK;
+    } catch (const std::exception& e) {
+        w->error = e.what();
+        return NSDG_ERR_BAD_ARG;
+    }
+}
+
+int nsdg_diagnostic_writer_create(size_t nx, size_t ny, size_t nz, int dg_comp, int dgstress_comp, int cg_degree,
+    const char* structure_type, long long time_seconds, const char* time_formatted, nsdg_restart_writer** out)
+{
+    if (!out || !structure_type || !time_formatted || !validShape(nx, ny, nz, dg_comp, dgstress_comp, cg_degree))
+        return NSDG_ERR_BAD_ARG;
+    auto r = std::make_unique<nsdg_restart_writer>();
+    r->nx = nx;
+    r->ny = ny;
+    r->nz = nz;
+    r->dg = dg_comp;
+    r->dgs = dgstress_comp;
+    r->cg = cg_degree;
+    layOut(*r, structure_type, time_seconds, time_formatted, true);
+    *out = r.release();
+    return NSDG_OK;
+}
+
+int nsdg_diagnostic_writer_record(nsdg_restart_writer* w, double time_seconds, size_t n_fields,
+    const char* const* names, const int* model_types, const double* const* data, const size_t* n)
+{
+    if (!w || w->time < 0 || (n_fields && (!names || !model_types || !data || !n)))
+        return NSDG_ERR_BAD_ARG;
+    const bool first = w->records == 0;
+    // check the whole record before anything is appended
+    std::vector<std::vector<int>> dims(n_fields);
+    for (size_t f = 0; f < n_fields; ++f) {
+        if (!names[f] || !*names[f] || (!data[f] && n[f]))
+            return NSDG_ERR_BAD_ARG;
+        size_t expect = 0;
+        dims[f] = typeDims(*w, model_types[f], expect);
+        if (dims[f].empty())
+            return NSDG_ERR_BAD_ARG;
+        if (n[f] != expect)
+            return NSDG_ERR_SIZE_MISMATCH;
+        const std::string nm = names[f];
+        const bool once = nm == "mask" || model_types[f] == NSDG_MA_VERTEX;
+        if (!first && !once) {
+            const auto it = w->vars.find(nm);
+            if (it == w->vars.end() || it->second.second != model_types[f]) {
+                w->error = "field " + nm + " is not a variable of this diagnostic file";
+                return NSDG_ERR_UNKNOWN_FIELD;
+            }
+        }
+    }
+    try {
+        w->w.appendRecord(w->time, &time_seconds);
+        std::map<std::string, bool> given;
+        for (size_t f = 0; f < n_fields; ++f) {
+            const std::string nm = names[f];
+            if (nm == "mask" || model_types[f] == NSDG_MA_VERTEX) {
+                if (!first)
+                    continue;
+                // written once, without the time axis; the mask with the
+                // dimensions (xdim, ydim) in the order writeDiagnosticTime
+                // lists them (ParaGridIO.cpp:439-451)
+                const std::vector<int> d = nm == "mask" ? std::vector<int> { w->dim[0], w->dim[1] } : dims[f];
+                const int v = w->w.addDouble(w->data, nm, d, data[f]);
+                if (nm != "mask")
+                    w->w.attrDouble(v, "missing_value", 1.7e38);
+                continue;
+            }
+            if (first) {
+                std::vector<int> d { w->time };
+                d.insert(d.end(), dims[f].begin(), dims[f].end());
+                const int v = w->w.addRecordDouble(w->data, nm, d);
+                w->w.attrDouble(v, "missing_value", 1.7e38);
+                w->vars[nm] = { v, model_types[f] };
+            }
+            w->w.appendRecord(w->vars.at(nm).first, data[f]);
+            given[nm] = true;
+        }
+        // variables this record leaves out keep netCDF's fill value there
+        for (const auto& kv : w->vars)
+            if (!given.count(kv.first)) {
+                size_t values = 0;
+                typeDims(*w, kv.second.second, values);
+                const std::vector<double> fill(values, 9.9692099683868690e+36);
+                w->w.appendRecord(kv.second.first, fill.data());
+            }
+        ++w->records;
         return NSDG_OK;
     } catch (const std::exception& e) {
         w->error = e.what();

@@ -8,9 +8,12 @@
 // messages), contiguous datasets, version 3 attribute messages, and netCDF-4
 // dimensions as dimension scales (CLASS, NAME, _Netcdf4Dimid on the scale;
 // DIMENSION_LIST on each variable, through one global heap collection).
-// Dimension scales carry no REFERENCE_LIST back-references, and link and
-// attribute creation order is not tracked: netCDF-C then lists them by
-// name.  The file is built in memory and written in one pass.
+// Record variables (the diagnostic files of writeDiagnosticTime) are chunked
+// along the unlimited time axis, one chunk per record, with a version 1
+// B-tree chunk index.  Dimension scales carry no REFERENCE_LIST
+// back-references, and link and attribute creation order is not tracked:
+// netCDF-C then lists them by name.  The file is built in memory (records
+// included) and written in one pass when it is saved.
 #include "nsdg_restart.hpp"
 
 #include <cstdio>
@@ -102,7 +105,18 @@ struct Writer::Node {
     std::vector<uint8_t> fill;
     uint64_t addr = 0, dataAddr = kUndef;
     uint32_t heapFirst = 0;      // first global heap index of its DIMENSION_LIST
+    // record variables: chunked along an unlimited first dimension, one
+    // chunk per record, indexed by a version 1 B-tree
+    bool chunked = false;
+    std::vector<std::vector<uint8_t>> records;
+    std::vector<uint64_t> recordAddrs;
+    uint64_t btreeAddr = kUndef;
 };
+
+namespace {
+constexpr uint64_t kUnlimited = UINT64_MAX;
+constexpr unsigned kBtreeK = 32; // HDF5's default for chunk B-trees: at most 2K entries a node
+} // namespace
 
 Writer::Writer() { nodes_.emplace_back(); }
 Writer::~Writer() = default;
@@ -191,6 +205,55 @@ int Writer::addInt64(int group, const std::string& name, int64_t value)
     return id;
 }
 
+int Writer::addTimeAxis(int group, const std::string& name, int dimid)
+{
+    const int id = addGroup(group, name);
+    Node& n = nodes_[id];
+    n.group = false;
+    n.chunked = true;
+    n.type = typeF64();
+    n.dims = { 0 };
+    attrText(id, "CLASS", "DIMENSION_SCALE");
+    attrText(id, "NAME", name);
+    attrInt(id, "_Netcdf4Dimid", dimid);
+    return id;
+}
+
+int Writer::addRecordDouble(int group, const std::string& name, const std::vector<int>& dims)
+{
+    if (dims.empty() || !nodes_.at(dims[0]).chunked)
+        throw std::invalid_argument("a record variable's first dimension is the time axis");
+    const int id = addGroup(group, name);
+    Node& n = nodes_[id];
+    n.group = false;
+    n.chunked = true;
+    n.type = typeF64();
+    n.dims.push_back(0);
+    for (size_t i = 1; i < dims.size(); ++i)
+        n.dims.push_back(nodes_.at(dims[i]).dims.at(0));
+    n.dimRefs = dims;
+    const double fill = 9.9692099683868690e+36;
+    uint64_t u;
+    std::memcpy(&u, &fill, 8);
+    put(n.fill, u, 8);
+    return id;
+}
+
+void Writer::appendRecord(int var, const double* data)
+{
+    Node& n = nodes_.at(var);
+    if (!n.chunked)
+        throw std::invalid_argument("not a record variable");
+    uint64_t count = 1;
+    for (size_t i = 1; i < n.dims.size(); ++i)
+        count *= n.dims[i];
+    std::vector<uint8_t> r(8 * count);
+    if (count)
+        std::memcpy(r.data(), data, r.size());
+    n.records.push_back(std::move(r));
+    n.dims[0] = n.records.size();
+}
+
 // ------------------------------------------------------------ encoding
 std::vector<uint8_t> Writer::header(const Node& n, uint64_t heapAddr) const
 {
@@ -219,7 +282,16 @@ std::vector<uint8_t> Writer::header(const Node& n, uint64_t heapAddr) const
             msg(0x06, l, 0);
         }
     } else {
-        msg(0x01, space(n.dims), 0);
+        if (n.chunked) {
+            std::vector<uint8_t> sp { 2, static_cast<uint8_t>(n.dims.size()), 1, 1 };
+            for (uint64_t d : n.dims)
+                put(sp, d, 8);
+            for (size_t i = 0; i < n.dims.size(); ++i)
+                put(sp, i == 0 ? kUnlimited : n.dims[i], 8);
+            msg(0x01, sp, 0);
+        } else {
+            msg(0x01, space(n.dims), 0);
+        }
         msg(0x03, n.type, 0x01);
         // fill value: allocation early (written data) or late (scales),
         // written if set, the value when defined
@@ -229,10 +301,19 @@ std::vector<uint8_t> Writer::header(const Node& n, uint64_t heapAddr) const
             fv.insert(fv.end(), n.fill.begin(), n.fill.end());
         }
         msg(0x05, fv, 0);
-        std::vector<uint8_t> lay { 3, 1 }; // contiguous
-        put(lay, n.dataAddr, 8);
-        put(lay, n.storageSize, 8);
-        msg(0x08, lay, 0);
+        if (n.chunked) { // chunk = one record; the last chunk dimension is the element size
+            std::vector<uint8_t> lay { 3, 2, static_cast<uint8_t>(n.dims.size() + 1) };
+            put(lay, n.btreeAddr, 8);
+            for (size_t i = 0; i < n.dims.size(); ++i)
+                put(lay, i == 0 ? 1 : n.dims[i], 4);
+            put(lay, 8, 4);
+            msg(0x08, lay, 0);
+        } else {
+            std::vector<uint8_t> lay { 3, 1 }; // contiguous
+            put(lay, n.dataAddr, 8);
+            put(lay, n.storageSize, 8);
+            msg(0x08, lay, 0);
+        }
     }
     auto attrMsg = [&](const Attr& a) {
         std::vector<uint8_t> d { 3, 0 };
@@ -289,12 +370,39 @@ std::vector<uint8_t> Writer::serialize()
         nodes_[i].addr = pos;
         pos += sizes[i];
     }
+    // chunk B-trees of the record variables: leaves of at most 2K chunks,
+    // then parent levels of at most 2K children, root last
+    std::vector<std::vector<std::vector<uint64_t>>> levels(nodes_.size()); // [node][level][i] address
+    auto nodeSize = [](size_t rank) { return 24 + 2 * kBtreeK * 8 + (2 * kBtreeK + 1) * (8 + 8 * (rank + 1)); };
+    for (size_t i = 0; i < nodes_.size(); ++i) {
+        Node& n = nodes_[i];
+        if (!n.chunked || n.records.empty())
+            continue;
+        size_t count = n.records.size();
+        do {
+            count = (count + 2 * kBtreeK - 1) / (2 * kBtreeK);
+            levels[i].emplace_back();
+            for (size_t k = 0; k < count; ++k) {
+                levels[i].back().push_back(pos);
+                pos += nodeSize(n.dims.size());
+            }
+        } while (count > 1);
+        n.btreeAddr = levels[i].back().at(0);
+    }
     for (auto& n : nodes_) {
         if (n.group || n.data.empty())
             continue;
         pos = (pos + 7) & ~uint64_t(7);
         n.dataAddr = pos;
         pos += n.data.size();
+    }
+    for (auto& n : nodes_) {
+        n.recordAddrs.clear();
+        for (const auto& r : n.records) {
+            pos = (pos + 7) & ~uint64_t(7);
+            n.recordAddrs.push_back(pos);
+            pos += r.size();
+        }
     }
     std::vector<uint8_t> f;
     f.reserve(pos);
@@ -329,12 +437,58 @@ std::vector<uint8_t> Writer::serialize()
             throw std::logic_error("object header size changed between passes");
         f.insert(f.end(), h.begin(), h.end());
     }
+    // B-tree nodes: a key is (chunk bytes, filter mask, chunk offset in
+    // every dimension and 0 for the element); a node's last key bounds its
+    // last chunk (offset plus the chunk extent)
+    for (size_t i = 0; i < nodes_.size(); ++i) {
+        const Node& n = nodes_[i];
+        const size_t rank = n.dims.size();
+        const uint64_t csize = n.records.empty() ? 0 : n.records[0].size();
+        auto key = [&](std::vector<uint8_t>& b, uint64_t rec, bool upper) {
+            put(b, upper ? 0 : csize, 4);
+            put(b, 0, 4);
+            put(b, upper ? rec + 1 : rec, 8);
+            for (size_t d = 1; d < rank; ++d)
+                put(b, upper ? n.dims[d] : 0, 8);
+            put(b, 0, 8);
+        };
+        uint64_t span = 1; // records under one entry at this level
+        for (size_t lv = 0; lv < levels[i].size(); ++lv) {
+            const auto& addrs = levels[i][lv];
+            const uint64_t per = span * 2 * kBtreeK;
+            for (size_t k = 0; k < addrs.size(); ++k) {
+                const uint64_t first = k * per;
+                const uint64_t last = std::min<uint64_t>(first + per, n.records.size());
+                const uint64_t entries = (last - first + span - 1) / span;
+                std::vector<uint8_t> b { 'T', 'R', 'E', 'E', 1, static_cast<uint8_t>(lv) };
+                put(b, entries, 2);
+                put(b, k ? addrs[k - 1] : kUndef, 8);
+                put(b, k + 1 < addrs.size() ? addrs[k + 1] : kUndef, 8);
+                for (uint64_t e = 0; e < entries; ++e) {
+                    const uint64_t rec = first + e * span;
+                    key(b, rec, false);
+                    put(b, lv == 0 ? n.recordAddrs[rec] : levels[i][lv - 1][rec / span], 8);
+                }
+                key(b, last - 1, true);
+                b.resize(nodeSize(rank), 0);
+                if (f.size() != addrs[k])
+                    throw std::logic_error("B-tree node placed out of order");
+                f.insert(f.end(), b.begin(), b.end());
+            }
+            span = per;
+        }
+    }
     for (const auto& n : nodes_) {
         if (n.group || n.data.empty())
             continue;
         f.resize(n.dataAddr, 0);
         f.insert(f.end(), n.data.begin(), n.data.end());
     }
+    for (const auto& n : nodes_)
+        for (size_t r = 0; r < n.records.size(); ++r) {
+            f.resize(n.recordAddrs[r], 0);
+            f.insert(f.end(), n.records[r].begin(), n.records[r].end());
+        }
     return f;
 }
 

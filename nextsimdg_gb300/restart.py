@@ -186,3 +186,54 @@ def dump_model_state(path, state: dict, nx: int, ny: int, *, nz: int = 1, dg_com
     finally:
         lib.nsdg_restart_writer_destroy(w)
     return written
+
+
+class DiagnosticFile:
+    """ParaGridIO::writeDiagnosticTime (core/src/ParaGridIO.cpp:350-500):
+    ``write(state, t)`` appends one record of every field of the state at time
+    t (seconds since 1970); "mask" and VERTEX fields are written with the
+    first record only.  Records stay in host memory until ``close()`` writes
+    the file, as the reference's file is finished when ParaGridIO closes it."""
+
+    def __init__(self, path, nx: int, ny: int, *, nz: int = 1, dg_comp: int = 6, dgstress_comp: int = 8,
+                 cg_degree: int = 2, time_seconds: int = 0, time_formatted: str = "1970-01-01T00:00:00Z",
+                 structure_type: str = "parametric_rectangular"):
+        self._lib = _lib.load()
+        self.path = str(path)
+        w = c_void_p()
+        st = self._lib.nsdg_diagnostic_writer_create(nx, ny, nz, dg_comp, dgstress_comp, cg_degree,
+                                                     structure_type.encode(), int(time_seconds),
+                                                     time_formatted.encode(), byref(w))
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, "nsdg_diagnostic_writer_create")
+        self._w = w
+
+    def write(self, state: dict, time_seconds: float):
+        names = sorted(state)  # the reference iterates its std::map in name order
+        arrays = [np.ascontiguousarray(state[n][1], dtype=np.float64).ravel() for n in names]
+        c_names = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+        c_types = (c_int * len(names))(*[_TYPE_CODES[state[n][0]] for n in names])
+        c_data = (c_void_p * len(names))(*[a.ctypes.data_as(c_void_p) for a in arrays])
+        c_n = (c_size_t * len(names))(*[a.size for a in arrays])
+        st = self._lib.nsdg_diagnostic_writer_record(self._w, float(time_seconds), len(names), c_names, c_types,
+                                                     c_data, c_n)
+        if st == _lib.NSDG_ERR_UNKNOWN_FIELD:
+            raise KeyError(self._lib.nsdg_restart_writer_last_error(self._w).decode())
+        if st != _lib.NSDG_OK:
+            raise NsdgError(st, self._lib.nsdg_restart_writer_last_error(self._w).decode())
+
+    def close(self):
+        if getattr(self, "_w", None):
+            try:
+                st = self._lib.nsdg_restart_writer_save(self._w, self.path.encode())
+                if st != _lib.NSDG_OK:
+                    raise NsdgError(st, self._lib.nsdg_restart_writer_last_error(self._w).decode())
+            finally:
+                self._lib.nsdg_restart_writer_destroy(self._w)
+                self._w = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

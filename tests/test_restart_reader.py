@@ -224,3 +224,47 @@ def test_writer_rejects_bad_sizes(lib_built, tmp_path):
         dump_model_state(tmp_path / "bad.nc", {"hice": ("DG", np.zeros(10))}, 4, 4)
     with pytest.raises(NsdgError):
         dump_model_state(tmp_path / "no_such_dir" / "x.nc", {"hice": ("H", np.zeros(16))}, 4, 4)
+
+
+def test_diagnostic_file_records(lib_built, tmp_path):
+    """writeDiagnosticTime: one record per call along an unlimited time axis
+    (chunked, one chunk per record; 70 records need a two-level chunk
+    B-tree), mask and VERTEX written once (the mask with the (xdim, ydim)
+    dimension order of the reference, which no dimension key maps to a
+    type), a field left out of a record holds the fill value, a field new
+    after the first record is refused, and readForcingTimeStatic picks the
+    record at or before the requested time."""
+    from nextsimdg_gb300.restart import DiagnosticFile, ParaGridFile
+    nx, ny = 6, 4
+    rng = np.random.default_rng(8)
+    recs = []
+    path = tmp_path / "diagnostic.nc"
+    with DiagnosticFile(path, nx, ny) as d:
+        for r in range(70):
+            st = {"hice": ("DG", rng.random(nx * ny * 6)), "cice": ("H", rng.random(nx * ny)),
+                  "mask": ("H", (rng.random(nx * ny) > 0.5).astype(float)),
+                  "coords": ("VERTEX", rng.random((nx + 1) * (ny + 1) * 2))}
+            if r == 5:
+                del st["cice"]
+            recs.append(st)
+            d.write(st, 1800.0 * r)
+        with pytest.raises(KeyError):
+            d.write({"damage": ("DG", np.zeros(nx * ny * 6))}, 1e9)
+    with ParaGridFile(path) as f:
+        vs = {v.name: v for v in f.variables("data")}
+        assert list(vs) == ["time", "cice", "coords", "hice", "mask"]
+        assert vs["hice"].dim_names == ("time", "ydim", "xdim", "dg_comp")
+        assert (vs["hice"].model_type, vs["hice"].n_records, vs["hice"].n_values) == ("DG", 70, nx * ny * 6)
+        assert vs["mask"].dim_names == ("xdim", "ydim") and vs["mask"].model_type is None
+        assert vs["coords"].dim_names == ("yvertex", "xvertex", "ncoords") and vs["coords"].n_records == 1
+        np.testing.assert_array_equal(f.read("data/time"), 1800.0 * np.arange(70))
+        for r in range(70):
+            np.testing.assert_array_equal(f.read("data/hice", r), recs[r]["hice"][1])
+            expect = np.full(nx * ny, 9.9692099683868690e+36) if r == 5 else recs[r]["cice"][1]
+            np.testing.assert_array_equal(f.read("data/cice", r), expect)
+        np.testing.assert_array_equal(f.read("data/mask"), recs[0]["mask"][1])
+        np.testing.assert_array_equal(f.read("data/coords"), recs[0]["coords"][1])
+        got = f.read_forcing_time_static({"hice", "cice"}, 1800.0 * 64 + 900.0)
+        np.testing.assert_array_equal(got["hice"], recs[64]["hice"][1])
+        got = f.read_forcing_time_static({"hice"}, 1e12)
+        np.testing.assert_array_equal(got["hice"], recs[69]["hice"][1])
