@@ -652,28 +652,36 @@ std::vector<uint8_t> File::heapObject(uint64_t collection, uint32_t index)
     throw FormatError("global heap object not found");
 }
 
-// the dataset's bytes in row-major order (unwritten parts hold the fill value)
-void File::readRaw(const Object& o, std::vector<uint8_t>& out)
+// elements [first, first + count) of the dataset's row-major order, as
+// stored bytes (unwritten parts hold the fill value); a chunked dataset
+// copies only the chunk rows that overlap the window
+void File::readRaw(const Object& o, uint8_t* out, uint64_t first, uint64_t count)
 {
     if (!o.isDataset)
         throw std::invalid_argument("not a dataset");
     if (o.hasFilters)
         throw Unsupported("filtered (compressed) variables");
     const uint64_t es = o.type.size;
-    const uint64_t total = product(o.dims) * es;
-    if (total > size_ * 64 + (uint64_t(1) << 30))
+    const uint64_t n = product(o.dims);
+    if (first > n || count > n - first)
+        throw std::out_of_range("read beyond the variable");
+    if (count > (size_ + (uint64_t(1) << 30)) / std::max<uint64_t>(es, 1))
         throw FormatError("dataset larger than its file allows");
-    out.assign(total, 0);
-    if (o.fill.size() == es && es > 0)
+    const uint64_t total = count * es;
+    std::memset(out, 0, total);
+    if (o.fill.size() == es && es > 0 && o.layoutClass == 2)
         for (uint64_t i = 0; i < total; i += es)
-            std::memcpy(out.data() + i, o.fill.data(), es);
+            std::memcpy(out + i, o.fill.data(), es);
     if (o.layoutClass == 0) {
-        if (o.compact.size() < total)
+        if (o.compact.size() < (first + count) * es)
             throw FormatError("compact dataset shorter than its dataspace");
-        std::memcpy(out.data(), o.compact.data(), total);
+        std::memcpy(out, o.compact.data() + first * es, total);
     } else if (o.layoutClass == 1) {
         if (o.dataAddr != kUndef)
-            std::memcpy(out.data(), span(o.dataAddr, total), total);
+            std::memcpy(out, span(o.dataAddr, n * es) + first * es, total);
+        else if (o.fill.size() == es && es > 0)
+            for (uint64_t i = 0; i < total; i += es)
+                std::memcpy(out + i, o.fill.data(), es);
     } else {
         if (o.chunk.size() != o.dims.size() + 1 || o.chunk.back() != es)
             throw FormatError("chunk dimensions do not match the dataspace");
@@ -682,15 +690,15 @@ void File::readRaw(const Object& o, std::vector<uint8_t>& out)
                 throw FormatError("zero chunk dimension");
         if (o.dataAddr != kUndef) {
             std::set<uint64_t> seen;
-            chunkWalk(o, o.dataAddr, 0, out, seen);
+            chunkWalk(o, o.dataAddr, 0, out, first, count, seen);
         }
     }
 }
 
 // version 1 B-tree of raw-data chunks: "TREE", type 1, level, entries,
 // siblings, then keys (chunk size, filter mask, offsets) and child addresses
-void File::chunkWalk(const Object& o, uint64_t node, int depth, std::vector<uint8_t>& out,
-    std::set<uint64_t>& seen)
+void File::chunkWalk(const Object& o, uint64_t node, int depth, uint8_t* out, uint64_t first,
+    uint64_t count, std::set<uint64_t>& seen)
 {
     if (depth > 32)
         throw FormatError("chunk B-tree too deep");
@@ -718,21 +726,39 @@ void File::chunkWalk(const Object& o, uint64_t node, int depth, std::vector<uint
         c.skip(8);
         const uint64_t child = c.u64();
         if (level > 0) {
-            chunkWalk(o, child, depth + 1, out, seen);
+            chunkWalk(o, child, depth + 1, out, first, count, seen);
             continue;
         }
         if (csize != chunkBytes)
             throw FormatError("chunk of unexpected size");
-        const uint8_t* src = span(child, chunkBytes);
-        // copy the part of the chunk inside the dataspace, row by row
-        bool inside = true;
+        bool inside = rank > 0;
         for (size_t d = 0; d < rank; ++d)
             inside = inside && off[d] < o.dims[d];
-        if (!inside || rank == 0)
+        if (!inside)
             continue;
+        // the chunk's flat index range; skip chunks outside the window
+        uint64_t lo0 = 0, hi0 = 0;
+        for (size_t d = 0; d < rank; ++d) {
+            lo0 = lo0 * o.dims[d] + off[d];
+            hi0 = hi0 * o.dims[d] + std::min<uint64_t>(off[d] + chunkDims[d], o.dims[d]) - 1;
+        }
+        if (hi0 + 1 <= first || lo0 >= first + count)
+            continue;
+        const uint8_t* src = span(child, chunkBytes);
+        // a chunk spanning every dimension but the first (one record of a
+        // forcing or diagnostic file) is one contiguous run
+        bool whole = true;
+        for (size_t d = 1; d < rank; ++d)
+            whole = whole && off[d] == 0 && chunkDims[d] == o.dims[d];
+        if (whole) {
+            const uint64_t lo = std::max(lo0, first), hi = std::min(hi0 + 1, first + count);
+            std::memcpy(out + (lo - first) * es, src + (lo - lo0) * es, (hi - lo) * es);
+            continue;
+        }
+        // otherwise copy the chunk's rows (fastest dimension) in the window
         const uint64_t rowLen = std::min<uint64_t>(chunkDims[rank - 1], o.dims[rank - 1] - off[rank - 1]);
-        std::vector<uint64_t> k(rank, 0); // index within the chunk, last dimension fixed at 0
-        for (;;) {
+        std::vector<uint64_t> k(rank, 0);
+        for (bool more = true; more;) {
             bool ok = true;
             uint64_t dst = 0, srcIdx = 0;
             for (size_t d = 0; d < rank; ++d) {
@@ -740,21 +766,20 @@ void File::chunkWalk(const Object& o, uint64_t node, int depth, std::vector<uint
                 dst = dst * o.dims[d] + off[d] + k[d];
                 srcIdx = srcIdx * chunkDims[d] + k[d];
             }
-            if (ok)
-                std::memcpy(out.data() + dst * es, src + srcIdx * es, rowLen * es);
-            size_t d = rank - 1;
-            while (d > 0) {
-                --d;
-                if (++k[d] < chunkDims[d])
-                    break;
-                k[d] = 0;
-                if (d == 0) {
-                    d = SIZE_MAX;
+            if (ok) {
+                const uint64_t lo = std::max(dst, first), hi = std::min(dst + rowLen, first + count);
+                if (lo < hi)
+                    std::memcpy(out + (lo - first) * es, src + (srcIdx + lo - dst) * es, (hi - lo) * es);
+            }
+            // next row: increment the chunk index over all but the last dimension
+            more = false;
+            for (size_t d = rank - 1; d-- > 0;) {
+                if (++k[d] < chunkDims[d]) {
+                    more = true;
                     break;
                 }
+                k[d] = 0;
             }
-            if (d == SIZE_MAX || rank == 1)
-                break;
         }
     }
 }
@@ -767,16 +792,17 @@ void File::readDoubles(const Object& o, uint64_t first, uint64_t count, double* 
     if (o.type.cls != TypeClass::Float && o.type.cls != TypeClass::Fixed)
         throw Unsupported("variable is not numeric");
     const uint64_t es = o.type.size;
-    // contiguous little-endian FP64: straight from the mapped file
-    if (o.layoutClass == 1 && o.dataAddr != kUndef && o.type.cls == TypeClass::Float && es == 8
-        && !o.type.bigEndian && !o.hasFilters) {
-        std::memcpy(out, span(o.dataAddr, n * es) + first * es, count * es);
+    // little-endian FP64 is stored as the caller wants it: no conversion
+    if (o.type.cls == TypeClass::Float && es == 8 && !o.type.bigEndian) {
+        readRaw(o, reinterpret_cast<uint8_t*>(out), first, count);
         return;
     }
-    std::vector<uint8_t> raw;
-    readRaw(o, raw);
+    if (count > (size_ + (uint64_t(1) << 30)) / std::max<uint64_t>(es, 1))
+        throw FormatError("dataset larger than its file allows");
+    std::vector<uint8_t> raw(count * es);
+    readRaw(o, raw.data(), first, count);
     for (uint64_t i = 0; i < count; ++i)
-        out[i] = toDouble(o.type, raw.data() + (first + i) * es);
+        out[i] = toDouble(o.type, raw.data() + i * es);
 }
 
 std::vector<double> File::readDoubles(const Object& o)
@@ -822,7 +848,11 @@ std::string File::readText(const Object& o)
     std::vector<uint8_t> raw;
     if (o.type.cls != TypeClass::String && !(o.type.cls == TypeClass::VarLen && o.type.vlenString))
         throw Unsupported("variable is not text");
-    readRaw(o, raw);
+    const uint64_t n = product(o.dims);
+    if (n > (size_ + (uint64_t(1) << 30)) / std::max<uint64_t>(o.type.size, 1))
+        throw FormatError("dataset larger than its file allows");
+    raw.resize(n * o.type.size);
+    readRaw(o, raw.data(), 0, n);
     Attribute a;
     a.type = o.type;
     a.raw = raw;

@@ -140,8 +140,9 @@ private:
         std::vector<std::pair<uint64_t, uint64_t>>& conts);
     void readDenseLinks(Object& o, uint64_t heapAddr, uint64_t btreeAddr);
     std::vector<uint8_t> heapObject(uint64_t collection, uint32_t index);
-    void readRaw(const Object& o, std::vector<uint8_t>& out);
-    void chunkWalk(const Object& o, uint64_t node, int depth, std::vector<uint8_t>& out, std::set<uint64_t>& seen);
+    void readRaw(const Object& o, uint8_t* out, uint64_t first, uint64_t count);
+    void chunkWalk(const Object& o, uint64_t node, int depth, uint8_t* out, uint64_t first,
+        uint64_t count, std::set<uint64_t>& seen);
     std::vector<std::string> dimNames(const Object& o, const std::string& group);
 };
 
