@@ -268,3 +268,51 @@ def test_diagnostic_file_records(lib_built, tmp_path):
         np.testing.assert_array_equal(got["hice"], recs[64]["hice"][1])
         got = f.read_forcing_time_static({"hice"}, 1e12)
         np.testing.assert_array_equal(got["hice"], recs[69]["hice"][1])
+
+
+_PROBE_RECORDS = """
+import sys
+from nextsimdg_gb300.restart import ParaGridFile
+from nextsimdg_gb300._lib import NsdgError
+for p in sys.argv[1:]:
+    try:
+        with ParaGridFile(p) as f:
+            for v in f.variables("data"):
+                for rec in {0, v.n_records // 2, v.n_records - 1}:
+                    try:
+                        f.read("data/" + v.name, rec) if v.n_values < 10**7 else None
+                    except (NsdgError, KeyError):
+                        pass
+            f.metadata_time()
+    except (NsdgError, KeyError, FileNotFoundError, UnicodeDecodeError):
+        pass
+print("survived")
+"""
+
+
+def test_damaged_written_files_never_crash(lib_built, tmp_path):
+    """The same robustness on the writer's own files, which hold the
+    structures the reference's fixture lacks (a two-level chunk B-tree, many
+    global heap references): damaged copies give statuses, never a crash."""
+    from nextsimdg_gb300.restart import DiagnosticFile
+    nx, ny = 5, 3
+    rng = np.random.default_rng(21)
+    src = tmp_path / "d.nc"
+    with DiagnosticFile(src, nx, ny) as d:
+        for r in range(70):
+            d.write({"hice": ("DG", rng.random(nx * ny * 6)), "cice": ("H", rng.random(nx * ny))}, 60.0 * r)
+    data = src.read_bytes()
+    paths = []
+    for i in range(100):
+        b = bytearray(data)
+        for pos in rng.integers(0, len(b), rng.integers(1, 9)):
+            b[pos] = int(rng.integers(0, 256))
+        if i % 5 == 0:
+            b = b[: int(rng.integers(48, len(b)))]
+        p = tmp_path / f"w{i}.nc"
+        p.write_bytes(bytes(b))
+        paths.append(str(p))
+    env = dict(os.environ, PYTHONPATH=str(ROOT))
+    r = subprocess.run([sys.executable, "-c", _PROBE_RECORDS, *paths], capture_output=True, text=True, env=env,
+                       timeout=300)
+    assert r.returncode == 0 and "survived" in r.stdout, r.stderr[-2000:]
