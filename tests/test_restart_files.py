@@ -316,3 +316,17 @@ def test_damaged_written_files_never_crash(lib_built, tmp_path):
     r = subprocess.run([sys.executable, "-c", _PROBE_RECORDS, *paths], capture_output=True, text=True, env=env,
                        timeout=300)
     assert r.returncode == 0 and "survived" in r.stdout, r.stderr[-2000:]
+
+
+def test_restart_entry_points_from_c(lib_built, tmp_path):
+    """tests/cpp/restart_capi_test.c: the nsdg_restart_* and
+    nsdg_diagnostic_writer_* entry points compiled as C99 against
+    include/nsdg.h and linked to the library, run without a GPU."""
+    exe = tmp_path / "restart_capi_test"
+    lib_dir = ROOT / "nextsimdg_gb300"
+    subprocess.run([shutil.which("gcc") or "gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I",
+                    str(ROOT / "include"), str(ROOT / "tests" / "cpp" / "restart_capi_test.c"), "-L", str(lib_dir),
+                    "-lnsdg_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe), str(tmp_path / "r.nc"), str(tmp_path / "d.nc")], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
