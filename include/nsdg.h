@@ -26,6 +26,9 @@
  *                           BrittleCGDynamicsKernel::update (BrittleCGDynamicsKernel.hpp:91-136)
  *   nsdg_transport_*        DGTransport<DG> (dynamics/src/include/DGTransport.hpp:27-152),
  *                           dgLimit.hpp:16-85 and Tools::MeanValue (Tools.hpp:24-50)
+ *   nsdg_restart_*          ParaGridIO::getModelState / readForcingTimeStatic /
+ *                           dumpModelState (core/src/ParaGridIO.cpp:87-348)
+ *   nsdg_diagnostic_writer_* ParaGridIO::writeDiagnosticTime (ParaGridIO.cpp:350-500)
  */
 #ifndef NSDG_H
 #define NSDG_H
