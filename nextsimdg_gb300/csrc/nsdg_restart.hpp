@@ -175,6 +175,7 @@ private:
     struct Node;
     std::vector<Node> nodes_;
     std::vector<uint8_t> header(const Node& n, uint64_t heapAddr) const;
+    std::vector<uint8_t> encode(bool withData);
 };
 
 } // namespace nsdg_nc

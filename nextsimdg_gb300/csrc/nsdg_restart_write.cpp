@@ -348,6 +348,14 @@ std::vector<uint8_t> Writer::header(const Node& n, uint64_t heapAddr) const
 
 std::vector<uint8_t> Writer::serialize()
 {
+    return encode(true);
+}
+
+// The metadata (superblock, global heap, object headers, chunk B-trees)
+// followed, when withData, by the contiguous data and the records at the
+// addresses the headers give them (all data lies after the metadata).
+std::vector<uint8_t> Writer::encode(bool withData)
+{
     // global heap objects: one object reference per variable dimension
     uint32_t nHeap = 0;
     for (auto& n : nodes_)
@@ -478,6 +486,8 @@ std::vector<uint8_t> Writer::serialize()
             span = per;
         }
     }
+    if (!withData)
+        return f;
     for (const auto& n : nodes_) {
         if (n.group || n.data.empty())
             continue;
@@ -494,11 +504,27 @@ std::vector<uint8_t> Writer::serialize()
 
 void Writer::save(const std::string& path)
 {
-    const auto bytes = serialize();
+    const auto meta = encode(false);
     std::ofstream out(path, std::ios::binary | std::ios::trunc);
     if (!out)
         throw std::runtime_error("cannot create " + path);
-    out.write(reinterpret_cast<const char*>(bytes.data()), static_cast<std::streamsize>(bytes.size()));
+    uint64_t pos = 0;
+    auto block = [&](uint64_t addr, const std::vector<uint8_t>& b) {
+        static const char zeros[8] = {};
+        if (addr < pos || addr - pos > 8)
+            throw std::logic_error("data block out of order");
+        out.write(zeros, static_cast<std::streamsize>(addr - pos));
+        out.write(reinterpret_cast<const char*>(b.data()), static_cast<std::streamsize>(b.size()));
+        pos = addr + b.size();
+    };
+    out.write(reinterpret_cast<const char*>(meta.data()), static_cast<std::streamsize>(meta.size()));
+    pos = meta.size();
+    for (const auto& n : nodes_)
+        if (!n.group && !n.data.empty())
+            block(n.dataAddr, n.data);
+    for (const auto& n : nodes_)
+        for (size_t r = 0; r < n.records.size(); ++r)
+            block(n.recordAddrs[r], n.records[r]);
     if (!out)
         throw std::runtime_error("cannot write " + path);
 }
