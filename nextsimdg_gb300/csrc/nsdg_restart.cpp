@@ -36,7 +36,7 @@ struct Cur {
     const uint8_t* end;
     void need(size_t n) const
     {
-        if (static_cast<size_t>(end - p) < n)
+        if (p > end || static_cast<size_t>(end - p) < n)
             throw FormatError("truncated HDF5 structure");
     }
     uint64_t u(size_t n)
@@ -55,7 +55,7 @@ struct Cur {
         need(n);
         p += n;
     }
-    size_t left() const { return static_cast<size_t>(end - p); }
+    size_t left() const { return p > end ? 0 : static_cast<size_t>(end - p); }
 };
 
 int log2u(uint64_t v)
@@ -544,7 +544,7 @@ void File::readDenseLinks(Object& o, uint64_t heapAddr, uint64_t btreeAddr)
                 }
             }
         }
-        if (blockAddr == kUndef || off - blockOff + len > blockSize)
+        if (blockAddr == kUndef || off - blockOff + len > blockSize || blockSize < 5 + 8 + offBytes + 4)
             throw FormatError("fractal heap object outside its block");
         const uint8_t* b = span(blockAddr, blockSize);
         if (std::memcmp(b, "FHDB", 4) != 0 || le(b + 5 + 8, offBytes) != blockOff)
@@ -567,7 +567,7 @@ void File::readDenseLinks(Object& o, uint64_t heapAddr, uint64_t btreeAddr)
     bt.skip(2);
     const uint64_t root = bt.u64();
     const unsigned rootRecs = bt.u16();
-    if (recSize != 4 + idLen || nodeSize < 16 || depth > 16)
+    if (recSize != 4 + idLen || nodeSize < 10 + recSize || depth > 16)
         throw FormatError("bad version 2 B-tree header");
     struct Level {
         uint64_t maxNrec, cumMax;
@@ -578,6 +578,8 @@ void File::readDenseLinks(Object& o, uint64_t heapAddr, uint64_t btreeAddr)
     const int maxNrecSize = log2u(lv[0].maxNrec) / 8 + 1;
     for (unsigned u = 1; u <= depth; ++u) {
         const uint64_t ptr = 8 + maxNrecSize + (u > 1 ? lv[u - 1].cumSize : 0);
+        if (nodeSize < 10 + 2 * ptr + recSize)
+            throw FormatError("version 2 B-tree nodes too small for their depth");
         lv[u].maxNrec = (nodeSize - (10 + ptr)) / (recSize + ptr);
         lv[u].cumMax = (lv[u].maxNrec + 1) * lv[u - 1].cumMax + lv[u].maxNrec;
         lv[u].cumSize = log2u(lv[u].cumMax) / 8 + 1;
@@ -637,6 +639,8 @@ std::vector<uint8_t> File::heapObject(uint64_t collection, uint32_t index)
     if (std::memcmp(g, "GCOL", 4) != 0)
         throw FormatError("bad global heap collection");
     const uint64_t csize = le(g + 8, 8);
+    if (csize < 16)
+        throw FormatError("bad global heap collection size");
     Cur c { span(collection, csize) + 16, span(collection, csize) + csize };
     while (c.left() >= 16) {
         const unsigned idx = c.u16();
