@@ -330,3 +330,15 @@ def test_restart_entry_points_from_c(lib_built, tmp_path):
     r = subprocess.run([str(exe), str(tmp_path / "r.nc"), str(tmp_path / "d.nc")], capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
+
+
+def test_paragrid_io_cpp_wrapper(lib_built, tmp_path):
+    """tests/cpp/paragrid_io_test.cpp: include/nsdg_paragrid_io.hpp
+    (Nextsim::GB300::ParaGridIO) compiled as C++17 and run without a GPU."""
+    exe = tmp_path / "paragrid_io_test"
+    lib_dir = ROOT / "nextsimdg_gb300"
+    subprocess.run([shutil.which("g++") or "g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I",
+                    str(ROOT / "include"), str(ROOT / "tests" / "cpp" / "paragrid_io_test.cpp"), "-L", str(lib_dir),
+                    "-lnsdg_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
