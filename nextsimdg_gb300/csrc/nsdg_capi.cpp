@@ -673,6 +673,14 @@ int nsdg_kernel::chooseStress32()
 {
     // NSDG_STRESS_KERNEL=global|tma|affine fixes the choice (for profilers,
     // whose serialised launches make the timing below meaningless)
+    // NSDG_VISC_FORM=0..3 fixes the FP64 viscosity form of the
+    // parallelogram kernel (0 rsqrt, 1 Newton, 2 Newton with integer
+    // conversions, 3 float pairs)
+    if (const char* env = std::getenv("NSDG_VISC_FORM")) {
+        const int f = std::atoi(env);
+        if (f >= 0 && f <= 3)
+            viscMode = f;
+    }
     if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
         const char* names[3] = { "global", "tma", "affine" };
         for (int i = 0; i < 3; ++i)
