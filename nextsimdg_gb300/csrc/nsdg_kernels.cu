@@ -1119,7 +1119,7 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const doub
 // One mEVP iteration, element part, carried in divergence space.
 //
 // The reference updates the stress coefficients s (8 per component,
-// MEVPStressUpdateStep.hpp:301-337) and then forms the element's share of the
+// MEVPStressUpdateStep.hpp:80-116) and then forms the element's share of the
 // stress divergence at its 9 CG2 nodes, divS1 s11 + divS2 s12 and
 // divS1 s12 + divS2 s22 (CGDynamicsKernel.cpp:340-363).  In the mEVP solver s
 // is observed only through that divergence, and the update is linear in s:

@@ -167,7 +167,7 @@ inline MevpParams withDerived(MevpParams p)
 }
 cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNodeState& st,
     const MevpParams& p);
-// P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:275-298):
+// P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:54-57,75-77):
 // Pg = P/alpha, or, for the mixed-precision kernels (hP32 given),
 // Pg = P/(8 alpha) (FP64, the viscosity numerator) and hP32 = P/(2 alpha).
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
@@ -176,7 +176,7 @@ cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, con
 // the Gauss points, Delta, and the relaxed update of the element's stress
 // divergence contributions tdiv[18][N] = (divS1 s11 + divS2 s12, divS1 s12 +
 // divS2 s22) at its 9 CG2 nodes (CGDynamicsKernel.cpp:300-398,
-// MEVPStressUpdateStep.hpp:251-339).  Pg holds P/alpha at the Gauss points.
+// MEVPStressUpdateStep.hpp:30-118).  Pg holds P/alpha at the Gauss points.
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
     const double* v, const double* Pg, double* tdiv, const MevpParams& p);
 // Node gather of the divergence, Dirichlet zero, implicit velocity update and

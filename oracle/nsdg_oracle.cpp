@@ -1539,7 +1539,7 @@ struct Kernel {
         }
     }
 
-    // MEVPStressUpdateStep.hpp:251-339
+    // MEVPStressUpdateStep.hpp:30-118
     void mevpStress()
     {
         const double alpha = P.alpha;

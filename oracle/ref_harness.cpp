@@ -21,9 +21,20 @@
  * and sets the ModelArray dimensions (ModelArray::setDimension,
  * setNComponents; core/src/ModelArray.cpp:187-213) for the handle's grid
  * before every call, since ModelArray keeps them in static storage.
+ *
+ * It also replays the procedure of the reference's transport tests
+ * (dynamics/test/Advection_test.cpp:136-301,
+ * dynamics/test/AdvectionPeriodicBC_test.cpp:117-297) on the reference's
+ * DGTransport, Interpolations, Tools and dgLimit code, so that its results
+ * can be checked against the golden values those tests hold.
  */
 #include "include/BBMDynamicsKernel.hpp"
 #include "MEVPDynamicsKernel.hpp" // the copy in oracle/_ref/gen (alpha, beta from ref_params.h)
+
+#include "include/DGTransport.hpp"
+#include "include/Interpolations.hpp"
+#include "include/Tools.hpp"
+#include "include/dgLimit.hpp"
 
 #include "include/ModelArray.hpp"
 #include "include/Time.hpp"
@@ -303,6 +314,200 @@ int ref_kernel_get_stress(void* p, const char* name, double* out, size_t n)
         for (int c = 0; c < DGstressComp; ++c)
             out[e * DGstressComp + c] = v(e, c);
     return 0;
+}
+
+
+} // extern "C"
+
+// ---- the transport tests -------------------------------------------------
+// The analytic fields and meshes below are the test cases' definitions
+// (Advection_test.cpp:56-100,198-241; AdvectionPeriodicBC_test.cpp:68-116,
+// 207-255), written here as Interpolations::Function objects.
+
+namespace {
+struct Bump : Nextsim::Interpolations::Function {
+    double L;
+    explicit Bump(double l)
+        : L(l)
+    {
+    }
+    double operator()(double x, double y) const override
+    {
+        const double X = x / L, Y = y / L;
+        const double r = ((X - 0.25) * (X - 0.25) + (Y - 0.5) * (Y - 0.5)) / 0.025;
+        return r < 1 ? std::exp(-1.0 / (1.0 - r)) : 0.0;
+    }
+};
+struct RotX : Nextsim::Interpolations::Function {
+    double L;
+    explicit RotX(double l)
+        : L(l)
+    {
+    }
+    double operator()(double, double y) const override { return (y - 0.5 * L) * 2.0 * M_PI / L; }
+};
+struct RotY : Nextsim::Interpolations::Function {
+    double L;
+    explicit RotY(double l)
+        : L(l)
+    {
+    }
+    double operator()(double x, double) const override { return (0.5 * L - x) * 2.0 * M_PI / L; }
+};
+struct RingX : Nextsim::Interpolations::Function {
+    double R1;
+    explicit RingX(double r)
+        : R1(r)
+    {
+    }
+    double operator()(double, double y) const override { return y * 2.0 * M_PI / R1; }
+};
+struct RingY : Nextsim::Interpolations::Function {
+    double R1;
+    explicit RingY(double r)
+        : R1(r)
+    {
+    }
+    double operator()(double x, double) const override { return -x * 2.0 * M_PI / R1; }
+};
+// four shapes on the ring: a smooth bump, a slotted disc, a cone, a disc
+struct Shapes : Nextsim::Interpolations::Function {
+    double operator()(double x, double y) const override
+    {
+        const double a = 50000.0, c = 175000.0;
+        double r = ((x + c) / a) * ((x + c) / a) + (y / a) * (y / a);
+        if (r < 1.0)
+            return std::exp(1.0) * std::exp(-1.0 / (1.0 - r));
+        r = (x / a) * (x / a) + ((y - c) / a) * ((y - c) / a);
+        if (r < 1.0)
+            return (y > c || std::fabs(x) > 15000.0) ? 1.0 : 0.0;
+        r = std::sqrt(((x - c) / a) * ((x - c) / a) + (y / a) * (y / a));
+        if (r < 1.0)
+            return 1.0 - r;
+        r = std::sqrt((x / a) * (x / a) + ((y + c) / a) * ((y + c) / a));
+        return r < 1.0 ? 1.0 : 0.0;
+    }
+};
+
+void boxMesh(ParametricMesh& m, double Lx, double Ly, size_t Nx, size_t Ny, double distort)
+{
+    m.reset();
+    m.nx = Nx;
+    m.ny = Ny;
+    m.nnodes = (Nx + 1) * (Ny + 1);
+    m.nelements = Nx * Ny;
+    m.vertices.resize(m.nnodes, 2);
+    for (size_t iy = 0, k = 0; iy <= Ny; ++iy)
+        for (size_t ix = 0; ix <= Nx; ++ix, ++k) {
+            m.vertices(k, 0) = Lx * ix / Nx + Lx * distort * std::sin(M_PI * ix / Nx * 3.0) * std::sin(M_PI * iy / Ny);
+            m.vertices(k, 1)
+                = Ly * iy / Ny + Ly * distort * std::sin(M_PI * iy / Ny * 2.0) * std::sin(M_PI * ix / Nx * 2.0);
+        }
+    m.landmask.resize(m.nelements, 1);
+    for (size_t i = 0; i < Nx; ++i) {
+        m.dirichlet[0].push_back(i);
+        m.dirichlet[2].push_back(Nx * (Ny - 1) + i);
+    }
+    for (size_t j = 0; j < Ny; ++j) {
+        m.dirichlet[1].push_back(j * Nx + Nx - 1);
+        m.dirichlet[3].push_back(j * Nx);
+    }
+}
+
+void ringMesh(ParametricMesh& m, double R0, double R1, size_t Nx, size_t Ny)
+{
+    m.reset();
+    m.nx = Nx;
+    m.ny = Ny;
+    m.nnodes = (Nx + 1) * (Ny + 1);
+    m.nelements = Nx * Ny;
+    m.vertices.resize(m.nnodes, 2);
+    for (size_t iy = 0, k = 0; iy <= Ny; ++iy)
+        for (size_t ix = 0; ix <= Nx; ++ix, ++k) {
+            const double r = R0 + (R1 - R0) * iy / Ny, p = -2.0 * M_PI * ix / Nx;
+            m.vertices(k, 0) = r * std::cos(p);
+            m.vertices(k, 1) = r * std::sin(p);
+        }
+    m.landmask.resize(m.nelements, 1);
+    for (size_t i = 0; i < Nx; ++i) {
+        m.dirichlet[0].push_back(i);
+        m.dirichlet[2].push_back(Nx * (Ny - 1) + i);
+    }
+    m.periodic.resize(1);
+    m.periodic[0].resize(Ny);
+    for (size_t j = 0; j < Ny; ++j)
+        m.periodic[0][j] = { 1, (j + 1) * Nx - 1, j * Nx, j * (Nx + 1) + j };
+}
+
+template <int DG> double advection(double distort, int it, double* massloss)
+{
+    const double Lx = 409600.0, Ly = 512000.0;
+    const size_t Nx = size_t(12) << it, Ny = size_t(13) << it;
+    const int deg = DG == 1 ? 0 : (DG == 3 ? 1 : 2);
+    const size_t NT = size_t(100 * (deg + 1) * (deg + 1)) << it;
+    ParametricMesh m(CARTESIAN);
+    boxMesh(m, Lx, Ly, Nx, Ny, distort);
+    DGTransport<DG> tr(m);
+    tr.settimesteppingscheme(DG < 3 ? "rk2" : "rk3");
+    const double dt = Lx / NT;
+    DGVector<DG> phi;
+    phi.resize_by_mesh(m);
+    Interpolations::Function2DG(m, phi, Bump(Lx));
+    const double initial = Tools::MeanValue(m, phi);
+    Interpolations::Function2DG(m, tr.GetVx(), RotX(Lx));
+    Interpolations::Function2DG(m, tr.GetVy(), RotY(Lx));
+    for (size_t i = 1; i <= NT; ++i) {
+        tr.reinitnormalvelocity();
+        tr.step(dt, phi);
+    }
+    if (massloss)
+        *massloss = (initial - Tools::MeanValue(m, phi)) / initial;
+    return std::sqrt(Interpolations::L2ErrorFunctionDG(m, phi, Bump(Lx))) / Lx;
+}
+
+template <int DG> double periodic(int it, double* massloss)
+{
+    const double R0 = 100000.0, R1 = 250000.0;
+    const size_t Nx = size_t(32) << it, Ny = size_t(4) << it;
+    const int deg = DG == 1 ? 0 : (DG == 3 ? 1 : 2);
+    const size_t NT = size_t(50 * (deg + 1) * (deg + 1)) << it;
+    ParametricMesh m(CARTESIAN);
+    ringMesh(m, R0, R1, Nx, Ny);
+    DGTransport<DG> tr(m);
+    tr.settimesteppingscheme(DG < 3 ? "rk2" : "rk3");
+    const double dt = R1 / NT;
+    DGVector<DG> phi;
+    phi.resize_by_mesh(m);
+    Interpolations::Function2DG(m, phi, Shapes());
+    LimitMax(phi, 1.0);
+    const double initial = Tools::MeanValue(m, phi);
+    Interpolations::Function2DG(m, tr.GetVx(), RingX(R1));
+    Interpolations::Function2DG(m, tr.GetVy(), RingY(R1));
+    for (size_t i = 1; i <= NT; ++i) {
+        tr.reinitnormalvelocity();
+        tr.step(dt, phi);
+        LimitMax(phi, 1.0);
+        LimitMin(phi, 0.0);
+    }
+    if (massloss)
+        *massloss = (initial - Tools::MeanValue(m, phi)) / initial;
+    return std::sqrt(Interpolations::L2ErrorFunctionDG(m, phi, Shapes())) / R0;
+}
+} // namespace
+
+extern "C" {
+
+// L2 error of the rotating-bump test (Advection_test.cpp:136-196,244-268)
+double ref_advection_golden(int dg, double distort, int it, double* massloss)
+{
+    return dg == 1 ? advection<1>(distort, it, massloss)
+                   : (dg == 3 ? advection<3>(distort, it, massloss) : advection<6>(distort, it, massloss));
+}
+
+// L2 error of the periodic ring test (AdvectionPeriodicBC_test.cpp:117-276)
+double ref_periodic_golden(int dg, int it, double* massloss)
+{
+    return dg == 1 ? periodic<1>(it, massloss) : (dg == 3 ? periodic<3>(it, massloss) : periodic<6>(it, massloss));
 }
 
 } // extern "C"

@@ -54,3 +54,21 @@ def gpu(nsdg_lib):
     if not gpu_available():
         pytest.fail("GPU test selected but no CUDA device is visible")
     return nsdg_lib
+
+
+@pytest.fixture(scope="session")
+def ref_goldens():
+    """(case definitions module, read-outs) of tests/golden/ref_dynamics.npz:
+    the reference's own dynamics code run on the cases of ref_cases.py."""
+    import numpy as np
+    gdir = ROOT / "tests" / "golden"
+    if str(gdir) not in sys.path:
+        sys.path.insert(0, str(gdir))
+    import ref_cases
+    z = np.load(gdir / "ref_dynamics.npz")
+    data = {}
+    for key in z.files:
+        if "/" in key:
+            case, name = key.split("/", 1)
+            data.setdefault(case, {})[name] = z[key]
+    return ref_cases, data

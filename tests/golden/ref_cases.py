@@ -1,0 +1,101 @@
+"""Dynamics cases run on the reference build and stored as golden fixtures.
+
+Each case is a box test (nextsimdg_gb300.boxtest) stepped through the
+dynamics-kernel interface (initialise, the module's setData calls, update
+with the moving cyclone's wind).  make_ref_goldens.py runs them on the
+reference's own code (oracle/_ref, see oracle/pyref.py) and stores the
+read-outs in ref_dynamics.npz; the tests run the same cases on the
+restated CPU oracle and on the GPU and compare with those read-outs.
+
+Read-outs: the cell averages (getDG0Data) of h, A, u, v and the ice-ocean
+stress (and damage for BBM), plus all DG components (getDGData) of h and A
+(and damage) on the small grids.  On the 256 x 256 grid the cell averages are
+kept at every 13th cell, with the full-field maxima.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from nextsimdg_gb300.boxtest import BoxTest
+
+# name: rheology (0 mEVP, 1 BBM), DG components, alpha = beta, grid, model
+# steps, sub-cycle count, land holes, read-out mode
+CASES = {
+    "mevp_dg6_a300_12x12": dict(rheology=0, dg=6, alpha=300.0, nx=12, ny=12, steps=3, sub=100),
+    "mevp_dg3_a300_17x18": dict(rheology=0, dg=3, alpha=300.0, nx=17, ny=18, steps=3, sub=100),
+    "mevp_dg1_a300_16x16": dict(rheology=0, dg=1, alpha=300.0, nx=16, ny=16, steps=2, sub=100),
+    "mevp_dg6_a1500_32x32": dict(rheology=0, dg=6, alpha=1500.0, nx=32, ny=32, steps=4, sub=100),
+    "mevp_dg6_a1500_20x15_holes": dict(rheology=0, dg=6, alpha=1500.0, nx=20, ny=15, steps=3, sub=60,
+                                       holes=True),
+    "mevp_dg6_a300_64x64": dict(rheology=0, dg=6, alpha=300.0, nx=64, ny=64, steps=3, sub=100, dg0_only=True),
+    "mevp_dg3_a1500_64x64": dict(rheology=0, dg=3, alpha=1500.0, nx=64, ny=64, steps=3, sub=100,
+                                 dg0_only=True),
+    "bbm_dg6_14x14": dict(rheology=1, dg=6, alpha=1500.0, nx=14, ny=14, steps=3, sub=50),
+    "bbm_dg3_16x12": dict(rheology=1, dg=3, alpha=1500.0, nx=16, ny=12, steps=2, sub=50),
+    "mevp_dg6_a1500_256x256": dict(rheology=0, dg=6, alpha=1500.0, nx=256, ny=256, steps=7, sub=100,
+                                   sampled=13),
+}
+
+DG0_NAMES = ("hice", "cice", "u", "v", "uiostress", "viostress")
+
+
+def box(case: dict) -> BoxTest:
+    b = BoxTest(case["nx"], case["ny"])
+    if case.get("holes"):
+        m = b.mask()
+        rng = np.random.default_rng(5)
+        for _ in range(12):
+            m[rng.integers(1, case["ny"] - 1), rng.integers(1, case["nx"] - 1)] = 0.0
+        b.mask = lambda m=m: m
+    return b
+
+
+def run(kernel, case: dict, b: BoxTest | None = None):
+    """initialise, the initial setData calls, then `steps` model steps."""
+    b = box(case) if b is None else b
+    kernel.initialise(b.coords(), False, b.mask())
+    for name, arr in b.initial_fields().items():
+        kernel.setData(name, arr)
+    if case["rheology"] == 1:
+        kernel.setData("damage", b.damage())
+    for s in range(case["steps"]):
+        uw, vw = b.wind(s * b.dt)
+        kernel.setData("uwind", uw)
+        kernel.setData("vwind", vw)
+        kernel.update(s * b.dt, b.dt)
+    return kernel
+
+
+def readouts(kernel, case: dict) -> dict:
+    names = DG0_NAMES + (("damage",) if case["rheology"] == 1 else ())
+    out = {}
+    n = case["nx"] * case["ny"]
+    idx = np.arange(0, n, case["sampled"]) if case.get("sampled") else None
+    for f in names:
+        a = kernel.getDG0Data(f)
+        if idx is not None:
+            out[f"dg0_{f}_absmax"] = np.array([np.abs(a).max()])
+            a = a[idx]
+        out[f"dg0_{f}"] = a
+    if not case.get("dg0_only") and not case.get("sampled") and case["dg"] > 1:
+        for f in ("hice", "cice") + (("damage",) if case["rheology"] == 1 else ()):
+            out[f"dg_{f}"] = kernel.getDGData(f)
+    return out
+
+
+def max_rel(a: np.ndarray, b: np.ndarray, scale: float | None = None) -> float:
+    """max |a - b| / max |b| (or / scale)."""
+    s = float(np.abs(b).max()) if scale is None else scale
+    return float(np.abs(a - b).max()) / max(s, 1e-300)
+
+
+def compare(got: dict, want: dict) -> dict:
+    """Worst relative difference per read-out, against the fixture's
+    magnitude (the full-field maximum for sampled read-outs)."""
+    worst = {}
+    for k, w in want.items():
+        if k.endswith("_absmax"):
+            continue
+        scale = float(want[k + "_absmax"][0]) if (k + "_absmax") in want else None
+        worst[k] = max_rel(got[k], w, scale)
+    return worst

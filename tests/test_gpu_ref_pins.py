@@ -1,0 +1,61 @@
+"""The GPU path against the reference's own results, through the C ABI.
+
+The fixture tests/golden/ref_dynamics.npz holds the read-outs of the
+reference's dynamics code (its unmodified sources built with the project's
+Eigen subset, oracle/_ref) on the box-test cases of
+tests/golden/ref_cases.py.  The FP64 path must match every read-out within
+1e-10 of the reference's magnitude; the mixed-precision path within its
+stated tolerance (velocity RMS <= 1e-5 m/s, h and A RMS <= 1e-6).
+"""
+import numpy as np
+import pytest
+
+from nextsimdg_gb300.dynamics import BBMDynamicsKernel, MEVPDynamicsKernel
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+ALL = ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16", "mevp_dg6_a1500_32x32",
+       "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64", "mevp_dg3_a1500_64x64", "bbm_dg6_14x14",
+       "bbm_dg3_16x12", "mevp_dg6_a1500_256x256"]
+
+
+def _kernel(case, precision):
+    if case["rheology"] == 1:
+        return BBMDynamicsKernel(dg_comp=case["dg"], n_steps=case["sub"], precision=precision)
+    return MEVPDynamicsKernel(dg_comp=case["dg"], alpha=case["alpha"], beta=case["alpha"], n_steps=case["sub"],
+                              precision=precision)
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_fp64_matches_reference(gpu, ref_goldens, name):
+    """FP64 GPU path vs the reference build: h, A (and damage) in every DG
+    component, u, v and the ice-ocean stress, 1e-10 relative.  The 256 x 256
+    case (alpha = beta = 1500) runs the 7 steps over which the reference's
+    own sensitivity to h x (1 + 1e-14) stays below 1e-11."""
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    k = _kernel(case, 0)
+    got = cases.readouts(cases.run(k, case), case)
+    k.close()
+    worst = cases.compare(got, data[name])
+    assert max(worst.values()) <= TOL, worst
+
+
+@pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg6_a1500_32x32", "mevp_dg6_a300_64x64",
+                                  "mevp_dg3_a1500_64x64"])
+def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, name):
+    """Mixed precision (FP32 bulk; FP64 conservation sums, inverse mass
+    matrices, Delta and viscosity) against the reference's FP64 results."""
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    k = _kernel(case, 1)
+    cases.run(k, case)
+    ref = data[name]
+    rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+    du = rms(np.hypot(k.getDG0Data("u") - ref["dg0_u"], k.getDG0Data("v") - ref["dg0_v"]))
+    dh = rms(k.getDG0Data("hice") - ref["dg0_hice"])
+    da = rms(k.getDG0Data("cice") - ref["dg0_cice"])
+    k.close()
+    assert du <= 1e-5 and dh <= 1e-6 and da <= 1e-6, (du, dh, da)

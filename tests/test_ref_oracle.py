@@ -1,0 +1,77 @@
+"""The CPU oracle pinned on the reference's own code.
+
+oracle/_ref is the reference's dynamics sources, unmodified, compiled against
+the project's Eigen 3.4 API subset (oracle/eigen_min, recipe oracle/Makefile
+target `ref`, harness oracle/ref_harness.cpp).  Where it is built (only where
+the reference sources are) it must reproduce the golden values of the
+reference's transport tests and the stored fixture; everywhere, the C++
+restatement (oracle/nsdg_oracle.cpp) must reproduce the fixture
+(tests/golden/ref_dynamics.npz, made by tests/golden/make_ref_goldens.py):
+full mEVP and BBM model steps on box tests, 12 x 12 to 256 x 256, DG 1/3/6,
+alpha = beta = 300 and 1500, land holes, at 1e-10 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyref
+
+TOL = 1e-10
+
+needs_ref = pytest.mark.skipif(not pyref.available(), reason="the reference build (oracle/_ref) is not built here")
+
+
+@needs_ref
+def test_reference_build_reproduces_transport_goldens(goldens):
+    """Advection_test.cpp:274-301 and AdvectionPeriodicBC_test.cpp:281-290
+    replayed on the reference's DGTransport built with the Eigen subset: the
+    18 golden L2 errors within the tests' own tolerance 1e-7."""
+    worst = 0.0
+    for key, distort in (("advection_regular", 0.0), ("advection_distorted", 0.05)):
+        for dg in (1, 3, 6):
+            for it in (0, 1):
+                e, _ = pyref.advection_golden(dg, distort, it)
+                ex = goldens[key][str(dg)][it]
+                worst = max(worst, abs(e - ex) / ex)
+    for dg in (1, 3, 6):
+        for it in (0, 1):
+            e, _ = pyref.periodic_golden(dg, it)
+            ex = goldens["periodic"][str(dg)][it]
+            worst = max(worst, abs(e - ex) / ex)
+    assert worst <= goldens["tolerance"], worst
+    assert worst <= 1e-12  # in practice the same to rounding
+
+
+SMALL = ["mevp_dg6_a300_12x12", "mevp_dg1_a300_16x16", "bbm_dg3_16x12"]
+
+
+@needs_ref
+@pytest.mark.parametrize("name", SMALL)
+def test_fixture_is_the_reference_output(ref_goldens, name):
+    """The stored fixture is what the reference build computes now."""
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], case["alpha"], case["sub"])
+    got = cases.readouts(cases.run(k, case), case)
+    for key, want in data[name].items():
+        np.testing.assert_array_equal(got[key], want, err_msg=key)
+
+
+@pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16",
+                                  "mevp_dg6_a1500_32x32", "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64",
+                                  "mevp_dg3_a1500_64x64", "bbm_dg6_14x14", "bbm_dg3_16x12",
+                                  "mevp_dg6_a1500_256x256"])
+def test_restatement_matches_reference(oracle, ref_goldens, name):
+    """oracle/nsdg_oracle.cpp against the reference's own results: every
+    read-out (h, A, damage in all DG components; u, v and the ice-ocean
+    stress cell averages) within 1e-10 of the reference's magnitude.  The
+    256 x 256 case runs 7 steps: the reference's own response to
+    h x (1 + 1e-14) stays below 1e-11 up to step 7 and reaches 1.6e-11 at
+    step 8 (alpha = beta = 1500)."""
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    k = oracle.OracleKernel(case["rheology"], case["dg"], alpha=case["alpha"], beta=case["alpha"],
+                            n_steps=case["sub"])
+    got = cases.readouts(cases.run(k, case), case)
+    worst = cases.compare(got, data[name])
+    assert max(worst.values()) <= TOL, worst
+    assert np.abs(data[name]["dg0_u"]).max() > 1e-3  # the case moves the ice
