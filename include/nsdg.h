@@ -130,6 +130,37 @@ int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny,
 int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data,
     size_t n_elements, size_t n_comp);
 
+/* The benchmark forcing computed on the device.  In the reference the
+ * atmosphere and ocean boundary modules update their fields right before the
+ * dynamics (core/src/PrognosticData.cpp:87-95) and the dynamics module passes
+ * them to its kernel with setData.  For the benchmark case they are closed-
+ * form fields on the cell centres x = i dx, y = j dy, dx = length_x / nx
+ * (physics/src/BenchmarkCoordinates.cpp:21-40):
+ *   ocean  u = ocean_vmax (2 y / length_y - 1), v = ocean_vmax (1 - 2 x / length_x)
+ *          (physics/src/modules/OceanBoundaryModule/BenchmarkOcean.cpp:15-39);
+ *   wind   a cyclone centred at (centre_x + centre_vx t, centre_y + centre_vy t),
+ *          t the seconds since the first update: x' = x - x0, y' = y - y0,
+ *          scale = wind_A exp(-wind_k hypot(x', y')),
+ *          u = -scale wind_vmax (cos a x' + sin a y'),
+ *          v = -scale wind_vmax (-sin a x' + cos a y'), a = wind_angle_deg
+ *          (physics/src/modules/AtmosphereBoundaryModule/BenchmarkAtmosphere.cpp:29-77).
+ * nsdg_kernel_benchmark_ocean / _atmosphere compute these on the device and
+ * feed them to the handle exactly as set_data of the H fields uocean/vocean
+ * or uwind/vwind would (DG0 -> CG2 interpolation), with no host copy.
+ * nsdg_benchmark_forcing_defaults fills the reference's constants for a box
+ * of length_x x length_y: wind_A 1e-5, wind_vmax 30 m/s, wind_k 1e-5 1/m,
+ * 72 degrees, the centre starting mid-box and reaching the far corner
+ * after 5 days, ocean_vmax 0.01 m/s. */
+typedef struct nsdg_benchmark_forcing {
+    double length_x, length_y;
+    double wind_A, wind_vmax, wind_k, wind_angle_deg;
+    double centre_x, centre_y, centre_vx, centre_vy;
+    double ocean_vmax;
+} nsdg_benchmark_forcing;
+void nsdg_benchmark_forcing_defaults(nsdg_benchmark_forcing* f, double length_x, double length_y);
+int nsdg_kernel_benchmark_ocean(nsdg_kernel* k, const nsdg_benchmark_forcing* f);
+int nsdg_kernel_benchmark_atmosphere(nsdg_kernel* k, const nsdg_benchmark_forcing* f, double seconds);
+
 /* getDG0Data: component 0 (cell average) of hice, cice, damage, u, v,
  * uiostress, viostress or a stored field.  out: n_elements doubles. */
 int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_elements);
@@ -352,6 +383,16 @@ int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double
  * The stress kernel with this form runs only through
  * nsdg_kernel_time_kernel(kernel_id = 8). */
 int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
+/* The float-pair arithmetic of the FP64 path's stress kernel
+ * (kMevpStressPairs) on n value pairs (a[i], x[i]), returned in FP64:
+ * out[4 i + 0] = split(a) - a (the representation error of the pair),
+ * out[4 i + 1] = RN_float(x) widened back to double by its bit pattern,
+ * out[4 i + 2] = a x in float pairs,
+ * out[4 i + 3] = sum_k a[j_k] x[j_k] over j_k = (i + 7 k) mod n, k < 9, in
+ *                float pairs (the kernel's dot-product accumulation).
+ * Inputs must be finite and, where non-zero, between 2^-74 and 2^127 in
+ * magnitude.  No reference counterpart: a check of this library's arithmetic. */
+int nsdg_selftest_pairs(size_t n, const double* a, const double* x, double* out);
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
 
 /* ======================================================================== */
@@ -362,13 +403,19 @@ int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out);
  * whose pool allocator owns the GPU memory, or a time-critical loop that may
  * not pay cudaMalloc's implicit synchronisation.  phi: device array
  * double[dg][n_elements] (component-major); jw: device array
- * double[9][n_elements], Jacobian times Gauss weight at the 3x3 Gauss points;
+ * double[9][n_elements], Jacobian times Gauss weight at the 3x3 Gauss points,
+ * point q = ix + 3 iy at local coordinates (g[ix], g[iy]) of the unit square,
+ * g = (1/2 - sqrt(3/20), 1/2, 1/2 + sqrt(3/20)), x fastest (for a field that
+ * is not symmetric the other order gives a wrong integral);
  * out: one device double; stream: a cudaStream_t (NULL = legacy default).
  * The reduction's scratch is a fixed array inside the library, held on every
  * GPU that loads it until the process exits; n_elements above
  * NSDG_NOALLOC_MAX_ELEMENTS returns NSDG_ERR_SIZE_MISMATCH.  The first call on
  * a device looks up that array's address with the device current (make it
- * before any stream capture that would record a later call).  Calls share the
+ * before any stream capture that would record a later call), and keeps it
+ * for the life of the process: after cudaDeviceReset (or anything else that
+ * re-creates the device's primary context) that address is stale, so do not
+ * call this entry point on a device after resetting it.  Calls share the
  * array: calls that overlap on the GPU race.  Nothing is allocated. */
 #define NSDG_NOALLOC_MAX_ELEMENTS (1u << 24)
 int nsdg_mean_value_noalloc(int dg, size_t n_elements, const double* phi, const double* jw,

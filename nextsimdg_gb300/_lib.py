@@ -53,6 +53,17 @@ class Params(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BenchmarkForcing(ctypes.Structure):
+    """nsdg_benchmark_forcing (include/nsdg.h)."""
+
+    _fields_ = [
+        ("length_x", c_double), ("length_y", c_double),
+        ("wind_A", c_double), ("wind_vmax", c_double), ("wind_k", c_double), ("wind_angle_deg", c_double),
+        ("centre_x", c_double), ("centre_y", c_double), ("centre_vx", c_double), ("centre_vy", c_double),
+        ("ocean_vmax", c_double),
+    ]
+
+
 class WarmStats(ctypes.Structure):
     """nsdg_warm_stats (include/nsdg.h)."""
 
@@ -77,6 +88,9 @@ SIGNATURES = [
     ("nsdg_kernel_last_error", c_char_p, [c_void_p]),
     ("nsdg_kernel_initialise", c_int, [c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]),
     ("nsdg_kernel_set_data", c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
+    ("nsdg_benchmark_forcing_defaults", None, [ctypes.POINTER(BenchmarkForcing), c_double, c_double]),
+    ("nsdg_kernel_benchmark_ocean", c_int, [c_void_p, ctypes.POINTER(BenchmarkForcing)]),
+    ("nsdg_kernel_benchmark_atmosphere", c_int, [c_void_p, ctypes.POINTER(BenchmarkForcing), c_double]),
     ("nsdg_kernel_get_dg0", c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
     ("nsdg_kernel_get_dg", c_int, [c_void_p, c_char_p, c_void_p, c_size_t, c_size_t]),
     ("nsdg_kernel_update", c_int, [c_void_p, c_double, c_double]),
@@ -127,6 +141,7 @@ SIGNATURES = [
     ("nsdg_kernel_set_warm_start", c_int, [c_void_p, c_void_p, c_int, c_double, c_int, c_double]),
     ("nsdg_kernel_warm_stats", c_int, [c_void_p, c_void_p]),
     ("nsdg_selftest_bounded_wait", c_int, [c_double, POINTER(c_int)]),
+    ("nsdg_selftest_pairs", c_int, [c_size_t, c_void_p, c_void_p, c_void_p]),
     ("nsdg_selftest_viscosity", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_selftest_viscosity_ff", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
@@ -201,6 +216,18 @@ ICE_GROWTH_FIELDS = (
     "mlbhc", "damage", "hice_updated", "cice_updated", "hsnow_updated", "hice_initial", "hsnow_initial", "newice",
     "delta_cice", "delta_hice", "tice_updated", "qic", "snow_to_ice", "top_melt", "bottom_melt", "snow_melt",
     "delta_cfreeze", "delta_cmelt", "tice_1", "tice_2", "tice_updated_1", "tice_updated_2")
+
+
+def benchmark_forcing(length_x: float = 512e3, length_y: float = 512e3, **overrides) -> BenchmarkForcing:
+    """The reference's benchmark forcing constants for a box of the given size
+    (nsdg_benchmark_forcing_defaults), with overrides."""
+    f = BenchmarkForcing()
+    load().nsdg_benchmark_forcing_defaults(ctypes.byref(f), float(length_x), float(length_y))
+    for k, v in overrides.items():
+        if not hasattr(f, k):
+            raise AttributeError(f"unknown forcing parameter {k}")
+        setattr(f, k, float(v))
+    return f
 
 
 def default_params() -> Params:

@@ -112,6 +112,19 @@ class BoxTest:
         v = -f * (-sa * xp + ca * yp)
         return u, v
 
+    def device_forcing(self):
+        """The same wind and ocean current as nsdg_benchmark_forcing, for the
+        kernels that compute them on the device: scale = wind_A exp(-k r) with
+        wind_A = wind_max e k and wind_vmax = 1 gives |wind| = wind_max at
+        r = 1/k; the centre moves along the diagonal at wind_speed."""
+        from . import _lib
+        k = 1.0 / self.decay
+        v = self.wind_speed / math.sqrt(2.0)
+        return _lib.benchmark_forcing(self.L, self.L, wind_A=self.wind_max * math.e * k,
+                                      wind_vmax=1.0, wind_k=k, wind_angle_deg=self.convergence_deg,
+                                      centre_x=self.start[0], centre_y=self.start[1], centre_vx=v, centre_vy=v,
+                                      ocean_vmax=self.ocean_max)
+
     def ssh(self) -> np.ndarray:
         return np.zeros(self.nelements)
 

@@ -23,13 +23,13 @@ LIB = PKG / "libnsdg_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
-CU_SOURCES = ["nsdg_kernels.cu", "nsdg_noalloc.cu", "nsdg_surrogate.cu", "nsdg_ice_growth.cu"]
+CU_SOURCES = ["nsdg_kernels.cu", "nsdg_stress_pairs.cu", "nsdg_forcing.cu", "nsdg_noalloc.cu", "nsdg_surrogate.cu", "nsdg_ice_growth.cu"]
 CXX_SOURCES = ["nsdg_host.cpp", "nsdg_capi.cpp", "nsdg_transport_capi.cpp", "nsdg_ice_growth_capi.cpp",
                "nsdg_restart.cpp", "nsdg_restart_write.cpp", "nsdg_restart_capi.cpp"]
-# per-file nvcc flags: the column thermodynamics rounds every product and sum
-# separately (no fused multiply-add), as the reference's and the oracle's
-# arithmetic does
-CU_FLAGS = {"nsdg_ice_growth.cu": ["--fmad=false"]}
+# per-file nvcc flags: the column thermodynamics and the benchmark forcing
+# round every product and sum separately (no fused multiply-add), as the
+# reference's and the oracle's arithmetic does
+CU_FLAGS = {"nsdg_ice_growth.cu": ["--fmad=false"], "nsdg_forcing.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:

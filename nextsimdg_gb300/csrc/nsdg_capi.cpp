@@ -128,6 +128,11 @@ struct nsdg_kernel {
     // 2 parallelogram coefficients (when the mesh allows it)
     int stressKind = 1;
     int viscMode = 2;                // FP64 viscosity form of the parallelogram kernel
+    // FP64 path: the element stress kernel, 0 = FP64 FMA (kMevpStress, the
+    // default), 1 = float-pair products (kMevpStressPairs, Cartesian mEVP),
+    // with its operators [4][81][N] as float pairs
+    int fp64Stress = 0;
+    float2* opsPairs = nullptr;
     float* affCoef = nullptr;        // [5][ld] parallelogram coefficients (null: not a parallelogram mesh)
     size_t affLd = 0;
     double affWorst = -1;            // largest relative mismatch of the rebuilt operators (FP64)
@@ -394,6 +399,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(8 * N); add(8 * N); add(3 * nXe); add(3 * nYe); add(24 * N); add(24 * N);
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(8 * N); add(Ncg);
+    if (P.precision == NSDG_PRECISION_FP64 && !bbm && !mesh.spherical)
+        add(324 * N, 8);                          // float-pair stress operators
     if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
         add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
         add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
@@ -541,6 +548,17 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     cgTmp = z(Ncg);
     partials = z((N + 255) / 256 + 1);
     dsum = z(1);
+    if (P.precision == NSDG_PRECISION_FP64 && !bbm && !mesh.spherical) {
+        // NSDG_FP64_STRESS=pairs selects the float-pair stress kernel
+        const char* env = std::getenv("NSDG_FP64_STRESS");
+        fp64Stress = (env && std::strcmp(env, "pairs") == 0) ? 1 : 0;
+        opsPairs = arena.take<float2>(324 * N);
+        if (!opsPairs && e == cudaSuccess)
+            e = cudaErrorMemoryAllocation;
+        const double* src[4] = { dops.gx, dops.gy, dops.a1, dops.a2 };
+        for (int b = 0; b < 4 && e == cudaSuccess; ++b)
+            e = launchSplitPairs(stream, 81 * N, src[b], opsPairs + b * 81 * N);
+    }
     auto upf = [&](const std::vector<double>& src) {
         std::vector<float> tmp(src.begin(), src.end());
         float* p = arena.take<float>(tmp.size());
@@ -818,11 +836,17 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
             // the mixed path forms its FP32 node constants in one kernel
             if (!mixed())
                 LCH(launchMevpPrepNodes(s, dm, st, mp));
-            LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp, mixed() ? hP32 : nullptr));
+            // a full mixed-precision update also records the sub-cycle's
+            // start (the warm-start features of the next update) inside
+            // the two preparation kernels
+            const bool save = loop && mixed();
+            LCH(launchMevpPrepElements(s, dm, dg, hice, cice, Pg, mp, mixed() ? hP32 : nullptr,
+                save ? tdiv32 : nullptr, save ? tdivLast : nullptr));
             if (mixed())
-                LCH(launchMevpPrepNodes32(s, dm, st, st32, dops.invm2, mp));
+                LCH(launchMevpPrepNodes32(s, dm, st, st32, dops.invm2, mp, save ? uLast : nullptr,
+                    save ? vLast : nullptr));
         }
-        if (loop && mixed()) {
+        if (loop && mixed() && !prep) {
             const int sv = saveLast(s, nullptr, nullptr, nullptr);
             if (sv != NSDG_OK)
                 return sv;
@@ -831,7 +855,10 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         if (loop) {
             for (int it = 0; it < nS; ++it) {
                 if (!mixed()) {
-                    LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
+                    if (opsPairs && fp64Stress == 1)
+                        LCH(launchMevpStressPairs(s, dm, opsPairs, u, v, Pg, contrib, mp));
+                    else
+                        LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
                     LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
                 } else {
                     LCH(launchStress32(s, mp, derr));
@@ -1295,6 +1322,81 @@ int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny, const double* c
     }
 }
 
+void nsdg_benchmark_forcing_defaults(nsdg_benchmark_forcing* f, double length_x, double length_y)
+{
+    if (!f)
+        return;
+    const double fiveDays = 5.0 * 86400.0; // BenchmarkAtmosphere.cpp:41-51
+    f->length_x = length_x;
+    f->length_y = length_y;
+    f->wind_A = 1e-5;
+    f->wind_vmax = 30.0;
+    f->wind_k = 1e-5;
+    f->wind_angle_deg = 72.0;
+    f->centre_x = 0.5 * length_x;
+    f->centre_y = 0.5 * length_y;
+    f->centre_vx = 0.5 * length_x / fiveDays;
+    f->centre_vy = 0.5 * length_y / fiveDays;
+    f->ocean_vmax = 0.01; // BenchmarkOcean.cpp:31
+}
+
+namespace {
+// the one-component cell fields f0, f1 (device, [N] each) into the CG2
+// targets t0, t1, as set_data of an H field does (CGDynamicsKernel.cpp:54-90)
+int cellsToNodes(nsdg_kernel* k, const double* f0, const double* f1, double* t0, double* t1)
+{
+    const double* in[2] = { f0, f1 };
+    double* out[2] = { t0, t1 };
+    const cudaError_t e = launchDG2CG(k->stream, k->dm, 1, 2, in, out);
+    return e == cudaSuccess ? NSDG_OK : k->fail(NSDG_ERR_CUDA, std::string("benchmark forcing: ") + cudaGetErrorString(e));
+}
+int forcingArgs(nsdg_kernel* k, const nsdg_benchmark_forcing* f)
+{
+    if (!k)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "benchmark forcing: kernel not initialised");
+    if (!f || !(f->length_x > 0) || !(f->length_y > 0) || !std::isfinite(f->length_x) || !std::isfinite(f->length_y))
+        return k->fail(NSDG_ERR_BAD_ARG, "benchmark forcing: positive finite box lengths needed");
+    return NSDG_OK;
+}
+} // namespace
+
+int nsdg_kernel_benchmark_ocean(nsdg_kernel* k, const nsdg_benchmark_forcing* f)
+{
+    int r = forcingArgs(k, f);
+    if (r)
+        return r;
+    k->readCache = 0;
+    const size_t nx = size_t(k->dm.nx), ny = size_t(k->dm.ny), N = k->N;
+    // BenchmarkCoordinates.cpp:28-29: dx = length / n
+    cudaError_t e = launchBenchmarkOcean(k->stream, nx, ny, f->length_x / double(nx), f->length_y / double(ny),
+        f->ocean_vmax, k->dgTmp, k->dgTmp + N);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("benchmark ocean: ") + cudaGetErrorString(e));
+    r = cellsToNodes(k, k->dgTmp, k->dgTmp + N, k->uo, k->vo);
+    return r ? r : k->ok();
+}
+
+int nsdg_kernel_benchmark_atmosphere(nsdg_kernel* k, const nsdg_benchmark_forcing* f, double seconds)
+{
+    int r = forcingArgs(k, f);
+    if (r)
+        return r;
+    if (!std::isfinite(seconds))
+        return k->fail(NSDG_ERR_BAD_ARG, "benchmark atmosphere: finite time needed");
+    k->readCache = 0;
+    const size_t nx = size_t(k->dm.nx), ny = size_t(k->dm.ny), N = k->N;
+    const double a = f->wind_angle_deg / 180.0 * M_PI; // BenchmarkAtmosphere.cpp:50-52
+    BenchmarkWindArgs w { f->length_x / double(nx), f->length_y / double(ny), f->centre_x + f->centre_vx * seconds,
+        f->centre_y + f->centre_vy * seconds, f->wind_A, f->wind_k, f->wind_vmax, std::cos(a), std::sin(a) };
+    cudaError_t e = launchBenchmarkWind(k->stream, nx, ny, w, k->dgTmp, k->dgTmp + N);
+    if (e != cudaSuccess)
+        return k->fail(NSDG_ERR_CUDA, std::string("benchmark atmosphere: ") + cudaGetErrorString(e));
+    r = cellsToNodes(k, k->dgTmp, k->dgTmp + N, k->ua, k->va);
+    return r ? r : k->ok();
+}
+
 int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, size_t n_elements, size_t n_comp)
 {
     if (!k || !name)
@@ -1711,9 +1813,16 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 0:
             if (!bbm && k->mixed())
                 return k->launchStress32(k->stream, mp, k->derr);
-            return bbm ? launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
-                             k->s11, k->s12, k->s22, k->contrib, bp, k->derr, k->mixed() ? &k->bbm32 : nullptr)
-                       : launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
+            if (bbm)
+                return launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
+                    k->s11, k->s12, k->s22, k->contrib, bp, k->derr, k->mixed() ? &k->bbm32 : nullptr);
+            if (k->opsPairs && k->fp64Stress == 1)
+                return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->u, k->v, k->Pg, k->contrib, mp);
+            return launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
+        case 9:
+            return launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
+        case 10:
+            return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->u, k->v, k->Pg, k->contrib, mp);
         case 1:
             if (!bbm && k->mixed())
                 return launchMevpMomentum32(k->stream, k->dm, k->st32, k->tdiv32, mp, k->derr);
@@ -1734,13 +1843,20 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                 k->mixed() ? k->cellY32 : nullptr);
         }
     };
-    if (kernel_id < 0 || kernel_id > 8 || (kernel_id >= 3 && (bbm || !k->mixed()))
-        || (kernel_id >= 5 && !k->affCoef))
+    const bool fp64Ids = kernel_id == 9 || kernel_id == 10;
+    if (kernel_id < 0 || kernel_id > 10 || (kernel_id >= 3 && kernel_id <= 8 && (bbm || !k->mixed()))
+        || (kernel_id >= 5 && kernel_id <= 8 && !k->affCoef) || (fp64Ids && (bbm || k->mixed()))
+        || (kernel_id == 10 && !k->opsPairs))
         return k->fail(NSDG_ERR_BAD_ARG,
-            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8: on parallelogram meshes)");
+            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8: on parallelogram meshes; "
+            "9, 10: the FP64 mEVP stress kernels, FMA and float pairs)");
     static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
-        *name = kernel_id == 0 ? (bbm ? "kBbmStress" : (k->mixed() ? kStress32Names[k->stressKind] : "kMevpStress"))
+        *name = kernel_id == 9 ? "kMevpStress" : kernel_id == 10 ? "kMevpStressPairs"
+            : kernel_id == 0 ? (bbm ? "kBbmStress"
+                                    : (k->mixed() ? kStress32Names[k->stressKind]
+                                                  : (k->opsPairs && k->fp64Stress == 1 ? "kMevpStressPairs"
+                                                                                       : "kMevpStress")))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
             : kernel_id == 2 ? "kTransportStage"
             : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3];
@@ -2528,6 +2644,33 @@ int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double
 int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
 {
     return viscositySelfTest(n, inv, Pa, delta_min, out, 1);
+}
+
+int nsdg_selftest_pairs(size_t n, const double* a, const double* x, double* out)
+{
+    if (!a || !x || !out || n == 0)
+        return NSDG_ERR_BAD_ARG;
+    std::string m;
+    const int st = deviceCheck(m);
+    if (st != NSDG_OK)
+        return st;
+    double *da = nullptr, *dx = nullptr, *dout = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&da, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dx, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dout, 4 * n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(da, a, n * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launchPairsSelfTest(s, n, da, dx, dout);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(da);
+    cudaFree(dx);
+    cudaFree(dout);
+    if (s)
+        cudaStreamDestroy(s);
+    return e == cudaSuccess ? NSDG_OK : NSDG_ERR_CUDA;
 }
 
 int nsdg_selftest_bounded_wait(double limit_seconds, int* timed_out)

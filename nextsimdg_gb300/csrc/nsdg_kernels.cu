@@ -1088,11 +1088,16 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes(size_t n, MevpNodeState
 
 template <int DG>
 __global__ void __launch_bounds__(kBlock) kMevpPrepElements(size_t N, const double* __restrict__ h,
-    const double* __restrict__ a, double* __restrict__ Pg, double Pstar, double invAlpha, float* __restrict__ hP32)
+    const double* __restrict__ a, double* __restrict__ Pg, double Pstar, double invAlpha, float* __restrict__ hP32,
+    const float* __restrict__ tdiv32, float* __restrict__ tdivLast)
 {
     const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (e >= N)
         return;
+    if (tdivLast) // the divergence at the start of this sub-cycle (warm-start features)
+#pragma unroll
+        for (int k = 0; k < 18; ++k)
+            tdivLast[k * N + e] = tdiv32[k * N + e];
     double hc[DG], ac[DG];
     loadCell<DG>(h, N, e, hc);
     loadCell<DG>(a, N, e, ac);
@@ -1304,7 +1309,8 @@ __global__ void __launch_bounds__(kBlock) kMevpMomentum(DevMesh m, DevOps o, Mev
 // mEVP, mixed precision
 // ===========================================================================
 __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeState st, MevpNodeState32 f,
-    const double* __restrict__ invm2, const uint8_t* __restrict__ dir, MevpParams p)
+    const double* __restrict__ invm2, const uint8_t* __restrict__ dir, MevpParams p, float* __restrict__ uLast,
+    float* __restrict__ vLast)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
@@ -1327,6 +1333,10 @@ __global__ void __launch_bounds__(kBlock) kMevpPrepNodes32(size_t n, MevpNodeSta
     f.v[i] = vf;
     f.u0[i] = uf;
     f.v0[i] = vf;
+    if (uLast) { // the velocity at the start of this sub-cycle (warm-start features)
+        uLast[i] = uf;
+        vLast[i] = vf;
+    }
     // u0 + (A F_atm |wind| uwind - rho H g dxSSH) / c1, in FP64
     const double ku = u + (A * (fatm * ua) - rhoH * p.gravity * st.uGrad[i]) * rc1;
     const double kv = v + (A * (fatm * va) - rhoH * p.gravity * st.vGrad[i]) * rc1;
@@ -2544,13 +2554,14 @@ cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNode
 }
 
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
-    const double* a, double* Pg, const MevpParams& p, float* hP32)
+    const double* a, double* Pg, const MevpParams& p, float* hP32, const float* tdiv32, float* tdivLast)
 {
     const unsigned g = blocksFor(m.N);
+    const double ia = 1.0 / p.alpha;
     switch (dg) {
-    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
-    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
-    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, 1.0 / p.alpha, hP32); break;
+    case 1: kMevpPrepElements<1><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, ia, hP32, tdiv32, tdivLast); break;
+    case 3: kMevpPrepElements<3><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, ia, hP32, tdiv32, tdivLast); break;
+    case 6: kMevpPrepElements<6><<<g, kBlock, 0, s>>>(m.N, h, a, Pg, p.Pstar, ia, hP32, tdiv32, tdivLast); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -2575,9 +2586,9 @@ cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o
 }
 
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32, const double* invm2, const MevpParams& p)
+    const MevpNodeState32& st32, const double* invm2, const MevpParams& p, float* uLast, float* vLast)
 {
-    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, invm2, m.cg2Dir, p);
+    kMevpPrepNodes32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st64, st32, invm2, m.cg2Dir, p, uLast, vLast);
     return cudaGetLastError();
 }
 namespace {

@@ -152,6 +152,7 @@ struct MevpParams {
     // GB300) on a division or a square of the parameters
     double keepd = 0;                          // 1 - 1/alpha
     float keep = 0, dmin2f = 0, F_oceanf = 0;  // FP32 copies (dmin2f: DeltaMin^2)
+    float dmin2lo = 0;                         // DeltaMin^2 - dmin2f (its float-pair low part)
     float betaf = 0, onePlusBetaf = 0, fcdtf = 0; // beta, 1 + beta, fc dt
 };
 inline MevpParams withDerived(MevpParams p)
@@ -159,6 +160,7 @@ inline MevpParams withDerived(MevpParams p)
     p.keepd = 1.0 - 1.0 / p.alpha;
     p.keep = static_cast<float>(p.keepd);
     p.dmin2f = static_cast<float>(p.DeltaMin * p.DeltaMin);
+    p.dmin2lo = static_cast<float>(p.DeltaMin * p.DeltaMin - static_cast<double>(p.dmin2f));
     p.F_oceanf = static_cast<float>(p.F_ocean);
     p.betaf = static_cast<float>(p.beta);
     p.onePlusBetaf = static_cast<float>(1.0 + p.beta);
@@ -170,8 +172,11 @@ cudaError_t launchMevpPrepNodes(cudaStream_t s, const DevMesh& m, const MevpNode
 // P at the 3x3 Gauss points from h and A (MEVPStressUpdateStep.hpp:54-57,75-77):
 // Pg = P/alpha, or, for the mixed-precision kernels (hP32 given),
 // Pg = P/(8 alpha) (FP64, the viscosity numerator) and hP32 = P/(2 alpha).
+// tdivLast (mixed precision, optional): also copies tdiv32 there (the
+// sub-cycle's starting divergence, a warm-start feature).
 cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, const double* h,
-    const double* a, double* Pg, const MevpParams& p, float* hP32 = nullptr);
+    const double* a, double* Pg, const MevpParams& p, float* hP32 = nullptr, const float* tdiv32 = nullptr,
+    float* tdivLast = nullptr);
 // One mEVP iteration, element part, carried in divergence space: the strain at
 // the Gauss points, Delta, and the relaxed update of the element's stress
 // divergence contributions tdiv[18][N] = (divS1 s11 + divS2 s12, divS1 s12 +
@@ -179,6 +184,26 @@ cudaError_t launchMevpPrepElements(cudaStream_t s, const DevMesh& m, int dg, con
 // MEVPStressUpdateStep.hpp:30-118).  Pg holds P/alpha at the Gauss points.
 cudaError_t launchMevpStress(cudaStream_t s, const DevMesh& m, const DevOps& o, const double* u,
     const double* v, const double* Pg, double* tdiv, const MevpParams& p);
+// The benchmark forcing on the cell centres (nsdg_forcing.cu):
+// BenchmarkAtmosphere.cpp:29-77 and BenchmarkOcean.cpp:15-39.
+struct BenchmarkWindArgs {
+    double dx, dy, x0, y0, A, k, vmax, cosa, sina;
+};
+cudaError_t launchBenchmarkWind(cudaStream_t s, size_t nx, size_t ny, const BenchmarkWindArgs& a, double* uw,
+    double* vw);
+cudaError_t launchBenchmarkOcean(cudaStream_t s, size_t nx, size_t ny, double dx, double dy, double vmax,
+    double* uo, double* vo);
+// FP64 operator entries as float pairs {RN(x), RN(x - RN(x))} (n entries).
+cudaError_t launchSplitPairs(cudaStream_t s, size_t n, const double* src, float2* dst);
+// launchMevpStress with the operator products, Delta^2 and the stress
+// increments in float-pair arithmetic (nsdg_stress_pairs.cu); 1/Delta,
+// P / (8 alpha Delta) and the divergence update in FP64.  ops: [4][81][N]
+// float pairs of G_x, G_y, A_1, A_2 (Cartesian meshes).
+cudaError_t launchMevpStressPairs(cudaStream_t s, const DevMesh& m, const float2* ops, const double* u,
+    const double* v, const double* Pg, double* tdiv, const MevpParams& p);
+// out[4 i + 0..3]: split(a) - a, widen(RN(x)), a x and a 9-term dot product,
+// each formed in float pairs and returned in FP64 (checks of nsdg_pairs.cuh).
+cudaError_t launchPairsSelfTest(cudaStream_t s, size_t n, const double* a, const double* x, double* out);
 // Node gather of the divergence, Dirichlet zero, implicit velocity update and
 // boundary zero (CGDynamicsKernel.cpp:365-444, VPCGDynamicsKernel.hpp:132-172).
 cudaError_t launchMevpMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
@@ -238,7 +263,8 @@ struct MevpNodeState32 {
 // clamped cgA, cgH and u0, v0 are written back in FP64.  invm2: the FP64
 // inverse lumped CG2 mass.
 cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNodeState& st64,
-    const MevpNodeState32& st32, const double* invm2, const MevpParams& p);
+    const MevpNodeState32& st32, const double* invm2, const MevpParams& p,
+    float* uLast = nullptr, float* vLast = nullptr);
 // (the Dirichlet flags of the nodes come from m.cg2Dir)
 // kMevpStress32 for parallelogram meshes: the unit-square operators
 // (G_xi, G_eta [q][j], A_xi, A_eta [j][q]) in constant memory, uploaded once

@@ -139,6 +139,14 @@ void parseSpace(Cur& c, std::vector<uint64_t>& dims, std::vector<uint64_t>* maxD
     }
 }
 
+// n elements of es bytes: a damaged dataspace or type must not wrap the size
+uint64_t bytesOf(uint64_t n, uint64_t es)
+{
+    if (es != 0 && n > UINT64_MAX / es)
+        throw FormatError("data size overflows");
+    return n * es;
+}
+
 uint64_t product(const std::vector<uint64_t>& d)
 {
     uint64_t n = 1;
@@ -467,7 +475,7 @@ void File::parseMessage(Object& o, int type, const uint8_t* p, size_t len, std::
         Cur sc { c.p, c.p + ss };
         parseSpace(sc, a.dims, nullptr);
         c.skip(pad(ss));
-        const uint64_t n = product(a.dims) * a.type.size;
+        const uint64_t n = bytesOf(product(a.dims), a.type.size);
         c.need(n);
         a.raw.assign(c.p, c.p + n);
         o.attrs.push_back(std::move(a));
@@ -677,12 +685,12 @@ void File::readRaw(const Object& o, uint8_t* out, uint64_t first, uint64_t count
         for (uint64_t i = 0; i < total; i += es)
             std::memcpy(out + i, o.fill.data(), es);
     if (o.layoutClass == 0) {
-        if (o.compact.size() < (first + count) * es)
+        if (o.compact.size() < bytesOf(first + count, es))
             throw FormatError("compact dataset shorter than its dataspace");
         std::memcpy(out, o.compact.data() + first * es, total);
     } else if (o.layoutClass == 1) {
         if (o.dataAddr != kUndef)
-            std::memcpy(out, span(o.dataAddr, n * es) + first * es, total);
+            std::memcpy(out, span(o.dataAddr, bytesOf(n, es)) + first * es, total);
         else if (o.fill.size() == es && es > 0)
             for (uint64_t i = 0; i < total; i += es)
                 std::memcpy(out + i, o.fill.data(), es);
@@ -720,7 +728,7 @@ void File::chunkWalk(const Object& o, uint64_t node, int depth, uint8_t* out, ui
     c.need(entries * (keySize + 8) + keySize);
     const uint64_t es = o.type.size;
     std::vector<uint64_t> chunkDims(o.chunk.begin(), o.chunk.end() - 1);
-    const uint64_t chunkBytes = product(chunkDims) * es;
+    const uint64_t chunkBytes = bytesOf(product(chunkDims), es);
     for (unsigned e = 0; e < entries; ++e) {
         const uint32_t csize = c.u32();
         c.skip(4);

@@ -502,12 +502,16 @@ std::vector<uint8_t> Writer::encode(bool withData)
     return f;
 }
 
+// Writes to path + ".tmp" and renames it over path once every byte has been
+// written and the stream closed without error, so that a failed dump (disk
+// full, quota) leaves the previous file at path intact.
 void Writer::save(const std::string& path)
 {
     const auto meta = encode(false);
-    std::ofstream out(path, std::ios::binary | std::ios::trunc);
+    const std::string tmp = path + ".tmp";
+    std::ofstream out(tmp, std::ios::binary | std::ios::trunc);
     if (!out)
-        throw std::runtime_error("cannot create " + path);
+        throw std::runtime_error("cannot create " + tmp);
     uint64_t pos = 0;
     auto block = [&](uint64_t addr, const std::vector<uint8_t>& b) {
         static const char zeros[8] = {};
@@ -525,8 +529,15 @@ void Writer::save(const std::string& path)
     for (const auto& n : nodes_)
         for (size_t r = 0; r < n.records.size(); ++r)
             block(n.recordAddrs[r], n.records[r]);
-    if (!out)
+    out.close(); // the final flush can fail too
+    if (!out) {
+        std::remove(tmp.c_str());
         throw std::runtime_error("cannot write " + path);
+    }
+    if (std::rename(tmp.c_str(), path.c_str()) != 0) {
+        std::remove(tmp.c_str());
+        throw std::runtime_error("cannot rename " + tmp + " to " + path);
+    }
 }
 
 } // namespace nsdg_nc

@@ -104,6 +104,21 @@ def selftest_viscosity(inv, pa, delta_min: float) -> np.ndarray:
     return out.reshape(3, inv.size)
 
 
+def selftest_pairs(a, x) -> np.ndarray:
+    """The float-pair arithmetic of the FP64 stress kernel on (a, x) pairs,
+    shape (4, n) float64 (see nsdg_selftest_pairs)."""
+    lib = _lib.load()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if a.shape != x.shape or a.ndim != 1:
+        raise ValueError("a and x must be 1-D arrays of the same length")
+    out = np.empty(4 * a.size)
+    st = lib.nsdg_selftest_pairs(a.size, _ptr(a), _ptr(x), _ptr(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "selftest_pairs failed")
+    return out.reshape(a.size, 4).T.copy()
+
+
 def selftest_viscosity_ff(inv, pa, delta_min: float) -> np.ndarray:
     """The same quantity by the float-pair form 3 (FP32 pipe), shape (n,)
     float32 (see nsdg_selftest_viscosity_ff)."""
@@ -183,6 +198,17 @@ class _KernelBase:
         m = _f64(mask).reshape(-1)
         self._check(self._l.nsdg_kernel_initialise(self._h, nx, ny, _ptr(coords), int(bool(isSpherical)), _ptr(m)))
         self.nx, self.ny = nx, ny
+
+    def benchmark_ocean(self, forcing):
+        """uocean, vocean of the benchmark ocean computed on the device
+        (nsdg_kernel_benchmark_ocean; BenchmarkOcean.cpp:15-39)."""
+        self._check(self._l.nsdg_kernel_benchmark_ocean(self._h, byref(forcing)))
+
+    def benchmark_atmosphere(self, forcing, seconds: float):
+        """uwind, vwind of the benchmark cyclone `seconds` after the first
+        update, computed on the device (nsdg_kernel_benchmark_atmosphere;
+        BenchmarkAtmosphere.cpp:29-77)."""
+        self._check(self._l.nsdg_kernel_benchmark_atmosphere(self._h, byref(forcing), float(seconds)))
 
     def setData(self, name: str, data):
         a = _f64(data)

@@ -380,6 +380,33 @@ def mesh_dirichlet(nx: int, ny: int, mask) -> list:
     return out
 
 
+def benchmark_forcing_fields(nx: int, ny: int, f, seconds: float):
+    """(uwind, vwind, uocean, vocean) of the benchmark case on the cell
+    centres, restated from the reference in numpy (element index i + nx j):
+    BenchmarkCoordinates.cpp:21-40 (x = i dx, dx = length_x / nx),
+    BenchmarkAtmosphere.cpp:29-77 (the cyclone; its centre moves from
+    (centre_x, centre_y) at centre_v), BenchmarkOcean.cpp:15-39.  `f` holds
+    the fields of nsdg_benchmark_forcing."""
+    dx, dy = f.length_x / nx, f.length_y / ny
+    i = np.arange(nx, dtype=np.float64)
+    j = np.arange(ny, dtype=np.float64)
+    x = np.tile(i * dx, ny)
+    y = np.repeat(j * dy, nx)
+    x0 = f.centre_x + f.centre_vx * seconds
+    y0 = f.centre_y + f.centre_vy * seconds
+    xp, yp = x - x0, y - y0
+    a = f.wind_angle_deg / 180.0 * np.pi
+    ca, sa = np.cos(a), np.sin(a)
+    scale = f.wind_A * np.exp(-f.wind_k * np.hypot(xp, yp))
+    uw = -scale * f.wind_vmax * (ca * xp + sa * yp)
+    vw = -scale * f.wind_vmax * (-sa * xp + ca * yp)
+    fx = x / (nx * dx)
+    fy = y / (ny * dy)
+    uo = f.ocean_vmax * (2.0 * fy - 1.0)
+    vo = f.ocean_vmax * (1.0 - 2.0 * fx)
+    return uw, vw, uo, vo
+
+
 def rectangle_mesh(Lx, Ly, Nx, Ny, distort=0.0):
     """dynamics/test/Advection_test.cpp:198-241."""
     ix = np.arange(Nx + 1)

@@ -9,7 +9,8 @@ Only the first two resolutions of each table are exercised by the reference
 tests (the loop runs it = 0, 1); the json keeps all six values and marks the
 checked ones.
 
-Usage: python tests/golden/make_goldens.py [/path/to/nextsimdg]
+Usage: python tests/golden/make_goldens.py [reference source tree]
+(default: $NSDG_REFERENCE, else the location the oracle build recipe uses)
 """
 import json
 import re
@@ -54,5 +55,14 @@ def main(root):
     print("wrote", dst)
 
 
+def _reference() -> str:
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent.parent))
+    from oracle import pyref
+    root = pyref.reference_root()
+    if root is None:
+        sys.exit("give the reference source tree as the argument or in NSDG_REFERENCE")
+    return str(root)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else _reference())

@@ -24,7 +24,7 @@ from pathlib import Path
 
 import numpy as np
 
-SRC = "/root/reference/dynamics/test/25km_NH.smesh"
+MESH = "dynamics/test/25km_NH.smesh"  # within the reference source tree
 OUT = Path(__file__).resolve().parent / "mesh_25km_NH.json"
 
 
@@ -58,7 +58,18 @@ def parse_smesh(path: str) -> dict:
     return dict(nx=nx, ny=ny, vertices=v, mask=mask, dirichlet=dirichlet, periodic=int(tok[i + 1]))
 
 
-def main(path: str = SRC) -> None:
+def _default_path() -> str:
+    """$NSDG_REFERENCE, else the location the oracle build recipe uses."""
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent.parent))
+    from oracle import pyref
+    root = pyref.reference_root()
+    if root is None:
+        sys.exit("give the .smesh path as the argument or the reference source tree in NSDG_REFERENCE")
+    return str(root / MESH)
+
+
+def main(path: str | None = None) -> None:
+    path = path or _default_path()
     m = parse_smesh(path)
     nx, ny, v = m["nx"], m["ny"], m["vertices"]
     dx, dy = float(v[1, 0] - v[0, 0]), float(v[nx + 1, 1] - v[0, 1])

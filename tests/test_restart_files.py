@@ -28,7 +28,16 @@ import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-FIXTURE = Path(os.environ.get("NSDG_REFERENCE", "/root/reference")) / "core" / "test" / "ParaGridIO_input_test.nc"
+def _fixture() -> Path:
+    """The reference's ParaGridIO test input, core/test/ParaGridIO_input_test.nc,
+    in the reference source tree ($NSDG_REFERENCE, else the location the
+    oracle build recipe uses); read where that tree is present."""
+    from oracle import pyref
+    root = pyref.reference_root()
+    return (root if root else Path("/nonexistent")) / "core" / "test" / "ParaGridIO_input_test.nc"
+
+
+FIXTURE = _fixture()
 needs_fixture = pytest.mark.skipif(not FIXTURE.exists(), reason="the reference's test input is not on this machine")
 
 
@@ -342,3 +351,101 @@ def test_paragrid_io_cpp_wrapper(lib_built, tmp_path):
                     "-lnsdg_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
+
+
+_PROBE_OVERSIZED = """
+import sys
+from ctypes import c_void_p
+import numpy as np
+from nextsimdg_gb300.restart import ParaGridFile
+n = int(sys.argv[2])
+errors = 0
+with ParaGridFile(sys.argv[1]) as f:
+    buf = np.zeros(n)
+    for name in ("u", "mask"):
+        for rec in range(3):
+            # a caller's buffer of the undamaged size, straight through the C ABI
+            st = f._lib.nsdg_restart_read(f._h, ("data/" + name).encode(), rec, buf.ctypes.data_as(c_void_p), n)
+            errors += st != 0
+print("errors", errors)
+"""
+
+
+def _lookup3(data: bytes, initval: int = 0) -> int:
+    """Bob Jenkins' lookup3 hashlittle (public domain), the HDF5 checksum."""
+    M = 0xFFFFFFFF
+
+    def rot(x, k):
+        return ((x << k) | (x >> (32 - k))) & M
+
+    n = len(data)
+    a = b = c = (0xDEADBEEF + n + initval) & M
+    i = 0
+    while n - i > 12:
+        a = (a + int.from_bytes(data[i:i + 4], "little")) & M
+        b = (b + int.from_bytes(data[i + 4:i + 8], "little")) & M
+        c = (c + int.from_bytes(data[i + 8:i + 12], "little")) & M
+        a = ((a - c) & M) ^ rot(c, 4); c = (c + b) & M
+        b = ((b - a) & M) ^ rot(a, 6); a = (a + c) & M
+        c = ((c - b) & M) ^ rot(b, 8); b = (b + a) & M
+        a = ((a - c) & M) ^ rot(c, 16); c = (c + b) & M
+        b = ((b - a) & M) ^ rot(a, 19); a = (a + c) & M
+        c = ((c - b) & M) ^ rot(b, 4); b = (b + a) & M
+        i += 12
+    if n - i == 0:
+        return c
+    tail = data[i:] + bytes(12 - (n - i))
+    a = (a + int.from_bytes(tail[0:4], "little")) & M
+    b = (b + int.from_bytes(tail[4:8], "little")) & M
+    c = (c + int.from_bytes(tail[8:12], "little")) & M
+    c ^= b; c = (c - rot(b, 14)) & M
+    a ^= c; a = (a - rot(c, 11)) & M
+    b ^= a; b = (b - rot(a, 25)) & M
+    c ^= b; c = (c - rot(b, 16)) & M
+    a ^= c; a = (a - rot(c, 4)) & M
+    b ^= a; b = (b - rot(a, 14)) & M
+    c ^= b; c = (c - rot(b, 24)) & M
+    return c
+
+
+def _reseal(b: bytearray, pos: int) -> None:
+    """Recomputes the checksum of the version 2 object header ("OHDR", chunk
+    0) that contains byte `pos`."""
+    start = b.rfind(b"OHDR", 0, pos)
+    assert start >= 0
+    flags = b[start + 5]
+    o = start + 6 + (16 if flags & 0x20 else 0) + (4 if flags & 0x10 else 0)
+    w = 1 << (flags & 3)
+    end = o + w + int.from_bytes(b[o:o + w], "little")
+    assert start < pos < end
+    b[end:end + 4] = _lookup3(bytes(b[start:end])).to_bytes(4, "little")
+
+
+def test_oversized_dataspace_is_an_error(lib_built, tmp_path):
+    """A damaged dataspace whose element count times the element size
+    overflows 64 bits (dims [2^61 + 3, 13] of 8-byte values, the object
+    header's checksum recomputed so that the damage is not caught there)
+    must give an error status, never a read past the mapped file."""
+    assert [_lookup3(b""), _lookup3(b"", 0xDEADBEEF), _lookup3(b"Four score and seven years ago"),
+            _lookup3(b"Four score and seven years ago", 1)] == [0xDEADBEEF, 0xBD5B7DDE, 0x17770551, 0xCD628161]
+    import struct
+    from nextsimdg_gb300.restart import dump_model_state
+    nx, ny = 13, 9
+    rng = np.random.default_rng(4)
+    path = tmp_path / "r.nc"
+    dump_model_state(path, {"u": ("H", rng.standard_normal(nx * ny)), "mask": ("H", np.ones(nx * ny))}, nx, ny)
+    data = path.read_bytes()
+    pattern = struct.pack("<QQ", ny, nx)
+    hits = [i for i in range(len(data) - 15) if data[i:i + 16] == pattern]
+    assert hits, "no dataspace with the grid's dimensions found"
+    env = dict(os.environ, PYTHONPATH=str(ROOT))
+    for k, pos in enumerate(hits):
+        b = bytearray(data)
+        b[pos:pos + 8] = struct.pack("<Q", (1 << 61) + 3)
+        _reseal(b, pos)
+        p = tmp_path / f"o{k}.nc"
+        p.write_bytes(bytes(b))
+        r = subprocess.run([sys.executable, "-c", _PROBE_OVERSIZED, str(p), str(nx * ny)], capture_output=True,
+                           text=True, env=env, timeout=120)
+        assert r.returncode == 0 and "errors" in r.stdout, r.stderr[-2000:]
+        assert int(r.stdout.split()[-1]) >= 1  # the damaged variable is refused

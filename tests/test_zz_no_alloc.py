@@ -7,8 +7,9 @@ pass device pointers to the field and the quadrature weights and get the
 integral written to a device pointer; the reduction's scratch is a fixed
 file-scope device array inside the library.  The test checks it against the
 allocating entry point (nsdg_transport_mean_value) on two calls in a row,
-with different fields, so a stale scratch would show.  This file is collected
-last on purpose.
+with different fields, so a stale scratch would show, and directly against
+the CPU oracle's MeanValue of the same field on the same mesh.  This file is
+collected last on purpose.
 """
 import ctypes
 
@@ -56,9 +57,13 @@ def test_noalloc_mean_value_matches_allocating_entry_point(gpu, oracle):
         assert st == 0
     torch.cuda.synchronize()
     got = out.cpu().numpy()
+    o = oracle.OracleTransport(dg, nx, ny, verts, dirichlet)
     for i, f in enumerate(fields):
         want = t.meanValue(f)
         assert got[i] == pytest.approx(want, rel=1e-12, abs=1e-12 * abs(want) + 1e-300)
+        # the oracle's Tools::MeanValue (Tools.hpp:24-50) of the same field
+        want_oracle = o.meanValue(f)
+        assert got[i] == pytest.approx(want_oracle, rel=1e-12, abs=1e-12 * abs(want_oracle) + 1e-300)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
