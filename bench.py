@@ -97,6 +97,37 @@ def bytes_per_cell_update(n_iter: int = NSTEPS, word: int = 8) -> float:
     return n_iter * (bytes_per_element_iteration_stress(word) + node_per_element) + transport + prepare
 
 
+def launched_bytes_per_cell_update(box, prec: int, stress_kind: str) -> dict:
+    """Algorithmic DRAM bytes per cell-update of the kernels one step
+    actually launches (each array counted once per launch), by part:
+    100 x (element stress kernel + node momentum kernel) + transport,
+    preparation and read-outs.  stress_kind names the element kernel:
+    "fp64" (FP64 operators), "pairs" (the same bytes as float pairs),
+    "affine" (5 FP32 coefficients per element), "tma"/"global" (FP32
+    operators)."""
+    N = box.nelements
+    ncg = (2 * box.nx + 1) * (2 * box.ny + 1)
+    word = 8 if prec == 0 else 4
+    stress = bytes_per_element_iteration_stress(word, parallelogram=stress_kind == "affine")
+    if prec == 0:
+        # 15 FP64 node streams read, u and v written, the Dirichlet flag
+        node = ncg * (15 * 8 + 2 * 8 + 1) / N
+    else:
+        # two float4 of per-step constants, u and v read and written (FP32)
+        node = ncg * (32 + 4 * 4) / N
+    # transport of 2 fields in 2 RK stages: cell operators (FP32 on the mixed
+    # path), FP64 inverse mass matrices, phi / k1 / stage I/O, edge velocities
+    dg = 6
+    cell = 2 * dg * 9 * word
+    transport = 2 * (cell + dg * dg * 8 + 2 * (4 * dg * 8)) + 4 * 3 * 8
+    # preparation: CG2DG of u, v, DG2CG of h, A, node and element constants
+    prepare = 2 * 9 * 8 + 2 * dg * 8 + 9 * 8 + ncg * (12 * 8) / N
+    per_iter = stress + node
+    total = NSTEPS * per_iter + transport + prepare
+    return {"total": total, "per_iteration_stress": stress, "per_iteration_node_share": node,
+            "transport": transport, "prepare": prepare, "stress_kernel": stress_kind}
+
+
 # --------------------------------------------------------------------------
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -216,9 +247,28 @@ def fp64_peak_tflops(local: int):
 
 
 # --------------------------------------------------------------------------
-def cpu_baseline(nx: int = NX, sample_steps: int = 2, warm: int = 1):
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_baseline(nx: int = NX, sample_steps: int = 10, warm: int = 1, single_steps: int = 1):
     """The oracle (CPU restatement of the reference) on the host cores, all
-    OpenMP threads, on a bounded sample of the same workload."""
+    OpenMP threads, on a bounded sample of the same workload, and the same
+    restatement on one thread for `single_steps` steps."""
     from oracle import pyoracle
     from nextsimdg_gb300.boxtest import BoxTest
 
@@ -235,9 +285,22 @@ def cpu_baseline(nx: int = NX, sample_steps: int = 2, warm: int = 1):
         k.update((warm + s) * DT, DT)
     t = time.perf_counter() - t0
     v = box.nelements * sample_steps / t
-    return {"value": v, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
-            "sample": f"{sample_steps} model steps of the {nx}x{nx} DG2 box test after {warm} warm-up step(s), "
-                      f"{t:.1f} s"}
+    cores = pyoracle.num_threads()
+    out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{sample_steps} model steps of the {nx}x{nx} DG2 box test after {warm} warm-up step(s), "
+                     f"{t:.1f} s", "cpu_model": cpu_model()}
+    if single_steps > 0:
+        pyoracle.set_threads(1)
+        try:
+            t0 = time.perf_counter()
+            for s in range(single_steps):
+                k.update((warm + sample_steps + s) * DT, DT)
+            t1 = time.perf_counter() - t0
+        finally:
+            pyoracle.set_threads(cores)
+        out["single_thread"] = {"value": box.nelements * single_steps / t1, "unit": UNIT, "cores": 1,
+                                "sample": f"{single_steps} model step(s) of the same run, {t1:.1f} s"}
+    return out
 
 
 def run_reference(args, world, rank):
@@ -294,7 +357,7 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
     achieved = N * bpe / (kms * 1e-3) / 1e9
     hbm, hbm_kind = measured_peaks()
     traffic = None
-    prof = ROOT / "profiles" / (f"{kname}_box{nx}_fp32.md" if prec else f"kMevpStress_box{nx}_fp64.md")
+    prof = ROOT / "profiles" / (f"{kname}_box{nx}_fp32.md" if prec else f"{kname}_box{nx}_fp64.md")
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.startswith(f"traffic_bytes_per_launch_{nx}:"):
@@ -329,6 +392,59 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
         roof["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_tf, "frac": ach / fp64_tf,
                         "peak_kind": fp64_kind}
     return roof, {"name": nname, "ms": nms}
+
+
+def fp64_pairs_variant(args, box, N: int, local: int) -> dict:
+    """The FP64 path with the float-pair stress kernel staged by TMA
+    (NSDG_FP64_STRESS=pairs_tma): the 9 x 9 operator products, Delta^2 and
+    the stress increments in float pairs (about 48 significant bits), 1/Delta
+    and the divergence update in FP64; the same operator bytes as FP64."""
+    os.environ["NSDG_FP64_STRESS"] = "pairs_tma"
+    try:
+        k = make_kernel(box, 0)
+    finally:
+        os.environ.pop("NSDG_FP64_STRESS", None)
+    k.time_updates(DT, 3)
+    ms = k.time_updates(DT, args.steps) / args.steps
+    k.synchronize()
+    roof, node = stress_roofline(k, N, 0, ms, local, args.nx)
+    times = {name: k.time_kernel(i, 50)[0] for name, i in (("fma", 9), ("pairs_global_loads", 10),
+                                                           ("pairs_tma", 11))}
+    k.close()
+    return {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "roofline": roof, "node_kernel": node,
+            "stress_kernel_ms": times, "stress_kernel": "kMevpStressPairsTma",
+            "arithmetic": "operator products, Delta^2 and stress increments in float pairs (about 48 bits); "
+                          "1/Delta, P/(8 alpha Delta) and the divergence update in FP64",
+            "launched_bytes_per_cell_update": launched_bytes_per_cell_update(box, 0, "pairs")}
+
+
+def distorted_variant(args, local: int) -> dict:
+    """Mixed precision on a 512 x 512 box whose vertices are displaced
+    (sinusoidally, 3 % of the box: the elements are general quadrilaterals,
+    not parallelograms), so the element kernel streams the per-element FP32
+    operators (TMA tiles or global loads, whichever the library times as
+    faster on this mesh) instead of the parallelogram coefficients."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    box = BoxTest(args.nx, distort=0.03)
+    N = box.nelements
+    k = make_kernel(box, 1)
+    k.time_updates(DT, 3)
+    ms = k.time_updates(DT, args.steps) / args.steps
+    k.synchronize()
+    roof, node = stress_roofline(k, N, 1, ms, local, args.nx)
+    kind = k.stress_variant()[0]
+    k.close()
+    return {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "stress_kernel": kind, "roofline": roof,
+            "node_kernel": node, "mesh": "box test vertices displaced by 3 % of the box (sin x sin)",
+            "launched_bytes_per_cell_update": launched_bytes_per_cell_update(box, 1, kind)}
+
+
+def ensemble_variant(args) -> dict:
+    """The 32-member uneven ensemble (sides from {64..384}, perturbed
+    cyclones and h), batched against the members stepped one by one."""
+    r = ensemble_measure(args, 32)
+    return {kk: r[kk] for kk in ("value", "unit", "ms_per_step", "cells", "sequential_members", "autotuned_tiles",
+                                 "gpu_launches_per_step", "sides")}
 
 
 def learned_variant(args, box_eval, N: int, plain_ms: float):
@@ -551,6 +667,73 @@ def day_error(args, box, steps: int, alpha: float = ALPHA, every: int = 120):
     return out
 
 
+def e2e_cycle(k, box, args, world, pinned: bool = True, device_forcing: bool = False) -> dict:
+    """The reference's module cycle through the C ABI with host buffers
+    (MEVPDynamics::update, MEVPDynamics.cpp:59-87): setData of h, A, the
+    winds, the ocean current and ssh, update, then getDG0Data of h, A, u, v
+    and the ice-ocean stress; wall clock, host <-> device copies inside,
+    median of three repetitions of the K steps.  pinned: page-locked host
+    buffers (through torch) or the pageable numpy arrays a ModelArray-like
+    caller holds.  device_forcing: the winds and the ocean current computed on
+    the device (nsdg_kernel_benchmark_*), so each step copies only h, A and
+    ssh in."""
+    N = box.nelements
+    if pinned:
+        try:
+            import torch
+            pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        except Exception:
+            pin = np.ascontiguousarray
+    else:
+        pin = lambda a: np.array(a, dtype=np.float64, copy=True)  # noqa: E731
+    uo, vo = box.ocean()
+    uo, vo, ssh = pin(uo), pin(vo), pin(box.ssh())
+    start = args.warmup + args.steps
+    winds = [tuple(pin(w) for w in box.wind(s * DT)) for s in range(start)] if not device_forcing else None
+    h, a = pin(k.getDG0Data("hice")), pin(k.getDG0Data("cice"))
+    outs = {n: pin(np.empty(N)) for n in ("hice", "cice", "u", "v", "uiostress", "viostress")}
+    forcing = box.device_forcing() if device_forcing else None
+
+    def cycle(s, kk=None):
+        kk = k if kk is None else kk
+        kk.setData("hice", outs["hice"] if s else h)
+        kk.setData("cice", outs["cice"] if s else a)
+        if device_forcing:
+            kk.benchmark_atmosphere(forcing, s * DT)
+            if s == 0:
+                kk.benchmark_ocean(forcing)
+        else:
+            kk.setData("uwind", winds[s][0])
+            kk.setData("vwind", winds[s][1])
+            kk.setData("uocean", uo)
+            kk.setData("vocean", vo)
+        kk.setData("ssh", ssh)
+        kk.update(s * DT, DT)
+        for n, buf in outs.items():
+            kk.getDG0Data(n, out=buf)
+
+    for s in range(args.warmup):
+        cycle(s)
+    # three timed repetitions of the K steps (the host shares its cores with
+    # the rest of the box): the median is reported, every trial is kept
+    trials = []
+    for _ in range(3):
+        dist_barrier(world)
+        t0 = time.perf_counter()
+        for s in range(args.warmup, args.warmup + args.steps):
+            cycle(s)
+        t_e2e = time.perf_counter() - t0
+        dist_barrier(world)
+        trials.append(dist_max(t_e2e, world))
+    t = statistics.median(trials)
+    copies_in = 3 if device_forcing else 7
+    return {"value": world * N * args.steps / t, "unit": UNIT, "h2d_bytes_per_step": copies_in * N * 8,
+            "d2h_bytes_per_step": 6 * N * 8, "trials": [world * N * args.steps / x for x in trials],
+            "host_buffers": "pinned" if pinned else "pageable",
+            "forcing": "device (nsdg_kernel_benchmark_*)" if device_forcing else "host, setData",
+            "timing": "median of 3 repetitions of the timed steps, wall clock", "cycle": cycle}
+
+
 def run_ours(args, world, rank, local):
     from nextsimdg_gb300.boxtest import BoxTest
 
@@ -573,49 +756,13 @@ def run_ours(args, world, rank, local):
     launches = k.launches_per_update()
 
     # ---- e2e: the module cycle through the C ABI, host buffers ----
-    try:
-        import torch
-        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
-    except Exception:
-        pin = np.ascontiguousarray
-    uo, vo = box.ocean()
-    uo, vo, ssh = pin(uo), pin(vo), pin(box.ssh())
-    winds = [tuple(pin(w) for w in box.wind(s * DT)) for s in range(args.warmup + args.steps)]
-    h, a = pin(k.getDG0Data("hice")), pin(k.getDG0Data("cice"))
-    outs = {n: pin(np.empty(N)) for n in ("hice", "cice", "u", "v", "uiostress", "viostress")}
-
-    def cycle(s, kk=None):
-        kk = k if kk is None else kk
-        kk.setData("hice", outs["hice"] if s else h)
-        kk.setData("cice", outs["cice"] if s else a)
-        kk.setData("uwind", winds[s][0])
-        kk.setData("vwind", winds[s][1])
-        kk.setData("uocean", uo)
-        kk.setData("vocean", vo)
-        kk.setData("ssh", ssh)
-        kk.update(s * DT, DT)
-        for n, buf in outs.items():
-            kk.getDG0Data(n, out=buf)
-
-    for s in range(args.warmup):
-        cycle(s)
-    # three timed repetitions of the K steps (the host shares its cores with
-    # the rest of the box): the median is reported, every trial is kept
-    trials = []
-    for _ in range(3):
-        dist_barrier(world)
-        t0 = time.perf_counter()
-        for s in range(args.warmup, args.warmup + args.steps):
-            cycle(s)
-        t_e2e = time.perf_counter() - t0
-        dist_barrier(world)
-        trials.append(dist_max(t_e2e, world))
-    t_e2e = statistics.median(trials)
-    e2e = world * N * args.steps / t_e2e
-    e2e_trials = [world * N * args.steps / t for t in trials]
-    e2e_calls = e2e_call_breakdown(k, cycle, args.warmup, args.steps) if args.e2e_calls else None
+    e2e_res = e2e_cycle(k, box, args, world, pinned=True)
+    e2e_pageable = e2e_cycle(k, box, args, world, pinned=False)
+    e2e_device_forcing = e2e_cycle(k, box, args, world, pinned=True, device_forcing=True)
+    e2e_calls = e2e_call_breakdown(k, e2e_res["cycle"], args.warmup, args.steps) if args.e2e_calls else None
 
     roof, node = stress_roofline(k, N, prec, ms_max / args.steps, local, args.nx)
+    launched = launched_bytes_per_cell_update(box, prec, (k.stress_variant()[0] or "fp64") if prec else "fp64")
     k.close()
 
     variants = {}
@@ -626,10 +773,19 @@ def run_ours(args, world, rank, local):
         oms = ko.time_updates(DT, args.steps) / args.steps
         ko.synchronize()
         oroof, _ = stress_roofline(ko, N, other, oms, local, args.nx)
+        oe2e = e2e_cycle(ko, box, args, world, pinned=True) if other == 0 else None
+        oe2e_pageable = e2e_cycle(ko, box, args, world, pinned=False) if other == 0 else None
         ko.close()
         variants["plain_fp64" if prec else "mixed_fp32"] = {
             "value": N / (oms * 1e-3), "unit": UNIT, "ms_per_step": oms,
-            "headline_speedup_over_this": oms / (ms_max / args.steps), "roofline": oroof}
+            "headline_speedup_over_this": oms / (ms_max / args.steps), "roofline": oroof,
+            "launched_bytes_per_cell_update": launched_bytes_per_cell_update(box, other, "fp64"),
+            **({"e2e": {kk: vv for kk, vv in oe2e.items() if kk != "cycle"},
+                "e2e_pageable": {kk: vv for kk, vv in oe2e_pageable.items() if kk != "cycle"}} if oe2e else {})}
+        if prec:
+            variants["plain_fp64_pairs"] = fp64_pairs_variant(args, box, N, local)
+            variants["distorted_mixed"] = distorted_variant(args, local)
+            variants["ensemble32"] = ensemble_variant(args)
         if prec and args.warm_train_iters > 0:
             variants["learned_fp32"] = learned_variant(args, box, N, ms_max / args.steps)
         if prec and not args.no_bbm:
@@ -661,10 +817,16 @@ def run_ours(args, world, rank, local):
                        "l2": "inputs larger than L2, no flush: each step sweeps the FP32 transport operators "
                              "(113 MB), the FP64 inverse mass matrices (75 MB) and the FP64 stage buffers, "
                              "besides the sub-cycle's ~110 MB working set",
-                       "bytes_per_cell_update": bytes_per_cell_update(word=4 if prec else 8)},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 7 * N * 8, "d2h_bytes_per_step": 6 * N * 8,
-                    "trials": e2e_trials, "timing": "median of 3 repetitions of the timed steps, wall clock",
+                       "bytes_per_cell_update_reference_layout": bytes_per_cell_update(word=4 if prec else 8),
+                       "bytes_per_cell_update": launched["total"],
+                       "bytes_per_cell_update_parts": launched,
+                       "bytes_note": "bytes_per_cell_update counts the arrays the launched kernels move; "
+                                     "the reference-layout figure (every per-element operator streamed, "
+                                     "the unfused reference data flow) is the survey's nominal"},
+            "e2e": {**{kk: vv for kk, vv in e2e_res.items() if kk != "cycle"},
                     **({"calls_us": e2e_calls} if e2e_calls else {})},
+            "e2e_pageable": {kk: vv for kk, vv in e2e_pageable.items() if kk != "cycle"},
+            "e2e_device_forcing": {kk: vv for kk, vv in e2e_device_forcing.items() if kk != "cycle"},
             "gpu_launches": launches * args.steps,
             "roofline": roof,
             "node_kernel": node,
@@ -728,12 +890,12 @@ def ensemble_boxes(n_members: int, seed: int = 2024):
     return boxes
 
 
-def run_ensemble(args):
+def ensemble_measure(args, n_members: int) -> dict:
     """Batched ensemble (one graph per step for all members) against the same
     members stepped one after another, each with its own graph."""
     from nextsimdg_gb300.dynamics import Ensemble, MEVPDynamicsKernel
 
-    boxes = ensemble_boxes(args.ensemble)
+    boxes = ensemble_boxes(n_members)
     members = []
     for b in boxes:
         k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=1)
@@ -754,20 +916,28 @@ def run_ensemble(args):
     tiles = {}
     for i, b in enumerate(boxes):
         tiles[f"{b.nx}"] = "x".join(map(str, ens.tile(i)))
-    line = {"metric": METRIC, "value": cells * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic box-test ensemble",
-            "config": {"workload": f"ensemble of {len(boxes)} box tests, sides "
-                                   f"{sorted(set(int(b.nx) for b in boxes))}, {cells} cells, DG2, mEVP {NSTEPS} "
-                                   f"iterations, mixed precision", "members": len(boxes)},
-            "sequential_members": {"value": cells * args.steps / (t_seq * 1e-3), "ms_per_step": t_seq / args.steps},
-            "autotuned_tiles": tiles, "gpu_launches": ens.launches_per_update() * args.steps,
-            "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+    out = {"value": cells * args.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.steps, "cells": cells,
+           "members": len(boxes), "sides": sorted(int(b.nx) for b in boxes),
+           "sequential_members": {"value": cells * args.steps / (t_seq * 1e-3), "ms_per_step": t_seq / args.steps},
+           "autotuned_tiles": tiles, "gpu_launches_per_step": ens.launches_per_update(), "clocks": clk.summary()}
     ens.close()
     for k in members:
         k.close()
+    return out
+
+
+def run_ensemble(args):
+    r = ensemble_measure(args, args.ensemble)
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic box-test ensemble",
+            "config": {"workload": f"ensemble of {r['members']} box tests, sides "
+                                   f"{sorted(set(r['sides']))}, {r['cells']} cells, DG2, mEVP {NSTEPS} "
+                                   f"iterations, mixed precision", "members": r["members"]},
+            "sequential_members": r["sequential_members"], "autotuned_tiles": r["autotuned_tiles"],
+            "gpu_launches": r["gpu_launches_per_step"] * args.steps, "clocks": r["clocks"]}
+    print(json.dumps(line), flush=True)
 
 
 def run_profile(args):

@@ -35,6 +35,7 @@ class BoxTest:
     start: tuple = field(default=None)  # cyclone centre at t = 0 (default: domain centre)
     h_noise: float = 0.0        # std of seeded Gaussian noise added to h [m]
     land_ring: bool = True      # outer ring of cells is land (make_init_benchmark.py:20-24)
+    distort: float = 0.0        # vertex displacement, fraction of the box (0: the regular box)
 
     def __post_init__(self):
         if self.ny is None:
@@ -58,10 +59,20 @@ class BoxTest:
         return self.L / self.ny
 
     def coords(self) -> np.ndarray:
-        """Vertices ((nx+1)*(ny+1), 2): x_i = i*L/nx, y_j = j*L/ny."""
-        x = self.L * np.arange(self.nx + 1) / self.nx
-        y = self.L * np.arange(self.ny + 1) / self.ny
-        X, Y = np.meshgrid(x, y)
+        """Vertices ((nx+1)*(ny+1), 2): x_i = i*L/nx, y_j = j*L/ny; with
+        distort > 0 displaced as the reference's distorted test mesh
+        (Advection_test.cpp:213-217): x += L d sin(3 pi i/nx) sin(pi j/ny),
+        y += L d sin(2 pi j/ny) sin(2 pi i/nx), which makes the elements
+        general quadrilaterals (the boundary stays straight)."""
+        i = np.arange(self.nx + 1)
+        j = np.arange(self.ny + 1)
+        I, J = np.meshgrid(i, j)
+        X = self.L * I / self.nx
+        Y = self.L * J / self.ny
+        if self.distort:
+            d = self.distort
+            X = X + self.L * d * np.sin(np.pi * I / self.nx * 3.0) * np.sin(np.pi * J / self.ny)
+            Y = Y + self.L * d * np.sin(np.pi * J / self.ny * 2.0) * np.sin(np.pi * I / self.nx * 2.0)
         return np.stack([X.ravel(), Y.ravel()], axis=1)
 
     def mask(self) -> np.ndarray:

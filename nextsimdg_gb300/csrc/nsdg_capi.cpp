@@ -129,10 +129,17 @@ struct nsdg_kernel {
     int stressKind = 1;
     int viscMode = 2;                // FP64 viscosity form of the parallelogram kernel
     // FP64 path: the element stress kernel, 0 = FP64 FMA (kMevpStress, the
-    // default), 1 = float-pair products (kMevpStressPairs, Cartesian mEVP),
-    // with its operators [4][81][N] as float pairs
+    // default), 1 = float-pair products (kMevpStressPairs), 2 = the same with
+    // TMA-staged operators (kMevpStressPairsTma); Cartesian mEVP.  The
+    // operators as float pairs [324][pairsLd(N)] and their TMA descriptors.
     int fp64Stress = 0;
     float2* opsPairs = nullptr;
+    size_t pairsLdN = 0;
+    PairsMaps pairsMaps {};
+    // mixed path: transport velocity (CG2DG) and fluxes in FP32 (the
+    // default); NSDG_MIXED_TRANSPORT=fp64 keeps them in FP64 (to measure what
+    // the FP32 transport contributes to the mixed path's error)
+    bool transport32 = true;
     float* affCoef = nullptr;        // [5][ld] parallelogram coefficients (null: not a parallelogram mesh)
     size_t affLd = 0;
     double affWorst = -1;            // largest relative mismatch of the rebuilt operators (FP64)
@@ -400,7 +407,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     }
     add(3 * Ncg1); add(8 * N); add(8 * N); add(8 * N); add(Ncg);
     if (P.precision == NSDG_PRECISION_FP64 && !bbm && !mesh.spherical)
-        add(324 * N, 8);                          // float-pair stress operators
+        add(324 * pairsLd(N), 8);                 // float-pair stress operators
     if (P.precision == NSDG_PRECISION_MIXED && !bbm) {
         add((mesh.spherical ? 486 : 324) * ops32Ld(N), 4);
         add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
@@ -549,15 +556,18 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     partials = z((N + 255) / 256 + 1);
     dsum = z(1);
     if (P.precision == NSDG_PRECISION_FP64 && !bbm && !mesh.spherical) {
-        // NSDG_FP64_STRESS=pairs selects the float-pair stress kernel
+        // NSDG_FP64_STRESS=pairs or pairs_tma selects a float-pair stress kernel
         const char* env = std::getenv("NSDG_FP64_STRESS");
-        fp64Stress = (env && std::strcmp(env, "pairs") == 0) ? 1 : 0;
-        opsPairs = arena.take<float2>(324 * N);
+        fp64Stress = !env ? 0 : std::strcmp(env, "pairs") == 0 ? 1 : std::strcmp(env, "pairs_tma") == 0 ? 2 : 0;
+        pairsLdN = pairsLd(N);
+        opsPairs = arena.take<float2>(324 * pairsLdN);
         if (!opsPairs && e == cudaSuccess)
             e = cudaErrorMemoryAllocation;
         const double* src[4] = { dops.gx, dops.gy, dops.a1, dops.a2 };
         for (int b = 0; b < 4 && e == cudaSuccess; ++b)
-            e = launchSplitPairs(stream, 81 * N, src[b], opsPairs + b * 81 * N);
+            e = launchSplitPairs(stream, 81, N, pairsLdN, src[b], opsPairs + b * 81 * pairsLdN);
+        if (e == cudaSuccess)
+            e = makePairsMaps(opsPairs, pairsLdN, &pairsMaps);
     }
     auto upf = [&](const std::vector<double>& src) {
         std::vector<float> tmp(src.begin(), src.end());
@@ -567,6 +577,8 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         return p;
     };
     if (mixed()) {
+        const char* tenv = std::getenv("NSDG_MIXED_TRANSPORT");
+        transport32 = !(tenv && std::strcmp(tenv, "fp64") == 0);
         cellX32 = upf(ops.cellX);
         cellY32 = upf(ops.cellY);
         jwA32 = upf(ops.jwA);
@@ -762,7 +774,7 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
     {
         const double* cgv[2] = { bbm ? avgU : u, bbm ? avgV : v };
         double* dgv[2] = { velx, vely };
-        if (mixed() && jwA32)
+        if (mixed() && jwA32 && transport32)
             LCH(launchCG2DG32(s, dm, dg, jwA32, dops.minvP ? dops.minvP : dops.minv, cgv, dgv));
         else
             LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minvP ? dops.minvP : dops.minv, 2, cgv, dgv));
@@ -784,8 +796,8 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         b.lmax[0] = 1; b.vmax[0] = 1.0; b.lmin[0] = 1; b.vmin[0] = 0.0;  // cice
         b.lmin[1] = 1; b.vmin[1] = 0.0;                                   // hice
         if (bbm) { b.lmax[2] = 1; b.vmax[2] = 1.0; b.lmin[2] = 1; b.vmin[2] = 1e-12; } // damage
-        const float* cx32 = mixed() ? cellX32 : nullptr;
-        const float* cy32 = mixed() ? cellY32 : nullptr;
+        const float* cx32 = mixed() && transport32 ? cellX32 : nullptr;
+        const float* cy32 = mixed() && transport32 ? cellY32 : nullptr;
         LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
             STAGE_RK2_A, dt, a, cx32, cy32));
         LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
@@ -855,8 +867,10 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         if (loop) {
             for (int it = 0; it < nS; ++it) {
                 if (!mixed()) {
-                    if (opsPairs && fp64Stress == 1)
-                        LCH(launchMevpStressPairs(s, dm, opsPairs, u, v, Pg, contrib, mp));
+                    if (opsPairs && fp64Stress == 2)
+                        LCH(launchMevpStressPairsTma(s, dm, pairsMaps, u, v, Pg, contrib, mp, derr));
+                    else if (opsPairs && fp64Stress == 1)
+                        LCH(launchMevpStressPairs(s, dm, opsPairs, pairsLdN, u, v, Pg, contrib, mp));
                     else
                         LCH(launchMevpStress(s, dm, dops, u, v, Pg, contrib, mp));
                     LCH(launchMevpMomentum(s, dm, dops, st, contrib, mp, derr));
@@ -1816,13 +1830,21 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
             if (bbm)
                 return launchBbmStress(k->stream, k->dm, k->dops, k->dg, k->u, k->v, k->hice, k->cice, k->damage,
                     k->s11, k->s12, k->s22, k->contrib, bp, k->derr, k->mixed() ? &k->bbm32 : nullptr);
+            if (k->opsPairs && k->fp64Stress == 2)
+                return launchMevpStressPairsTma(k->stream, k->dm, k->pairsMaps, k->u, k->v, k->Pg, k->contrib, mp,
+                    k->derr);
             if (k->opsPairs && k->fp64Stress == 1)
-                return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->u, k->v, k->Pg, k->contrib, mp);
+                return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->pairsLdN, k->u, k->v, k->Pg,
+                    k->contrib, mp);
             return launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 9:
             return launchMevpStress(k->stream, k->dm, k->dops, k->u, k->v, k->Pg, k->contrib, mp);
         case 10:
-            return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->u, k->v, k->Pg, k->contrib, mp);
+            return launchMevpStressPairs(k->stream, k->dm, k->opsPairs, k->pairsLdN, k->u, k->v, k->Pg, k->contrib,
+                mp);
+        case 11:
+            return launchMevpStressPairsTma(k->stream, k->dm, k->pairsMaps, k->u, k->v, k->Pg, k->contrib, mp,
+                k->derr);
         case 1:
             if (!bbm && k->mixed())
                 return launchMevpMomentum32(k->stream, k->dm, k->st32, k->tdiv32, mp, k->derr);
@@ -1843,20 +1865,22 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                 k->mixed() ? k->cellY32 : nullptr);
         }
     };
-    const bool fp64Ids = kernel_id == 9 || kernel_id == 10;
-    if (kernel_id < 0 || kernel_id > 10 || (kernel_id >= 3 && kernel_id <= 8 && (bbm || !k->mixed()))
+    const bool fp64Ids = kernel_id >= 9 && kernel_id <= 11;
+    if (kernel_id < 0 || kernel_id > 11 || (kernel_id >= 3 && kernel_id <= 8 && (bbm || !k->mixed()))
         || (kernel_id >= 5 && kernel_id <= 8 && !k->affCoef) || (fp64Ids && (bbm || k->mixed()))
-        || (kernel_id == 10 && !k->opsPairs))
+        || (kernel_id >= 10 && !k->opsPairs))
         return k->fail(NSDG_ERR_BAD_ARG,
             "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8: on parallelogram meshes; "
-            "9, 10: the FP64 mEVP stress kernels, FMA and float pairs)");
+            "9-11: the FP64 mEVP stress kernels, FMA, float pairs and float pairs through TMA)");
     static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
         *name = kernel_id == 9 ? "kMevpStress" : kernel_id == 10 ? "kMevpStressPairs"
+            : kernel_id == 11 ? "kMevpStressPairsTma"
             : kernel_id == 0 ? (bbm ? "kBbmStress"
                                     : (k->mixed() ? kStress32Names[k->stressKind]
-                                                  : (k->opsPairs && k->fp64Stress == 1 ? "kMevpStressPairs"
-                                                                                       : "kMevpStress")))
+                                                  : (k->opsPairs && k->fp64Stress == 2 ? "kMevpStressPairsTma"
+                                                     : k->opsPairs && k->fp64Stress == 1 ? "kMevpStressPairs"
+                                                                                         : "kMevpStress")))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
             : kernel_id == 2 ? "kTransportStage"
             : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3];

@@ -15,6 +15,7 @@ __constant__ ConstTables32 cT32;
 #include "nsdg_common.cuh"
 #include "nsdg_kernels.hpp"
 #include "nsdg_visc_ff.hpp"
+#include "nsdg_tma.cuh"
 
 namespace nsdg {
 
@@ -1469,58 +1470,6 @@ constexpr int kTmaRows = 162;                           // G_x | G_y  (A_1 | A_2
 constexpr int kTmaRowsSph = 243;                        // G_x | G_y | G_m  (A_1 | A_2 | A_3)
 template <bool SPH> __host__ __device__ constexpr int tmaRows() { return SPH ? kTmaRowsSph : kTmaRows; }
 template <bool SPH> __host__ __device__ constexpr unsigned tmaTileBytes() { return tmaRows<SPH>() * kTmaElems * 4; }
-constexpr long kTmaSpin = 1L << 26;
-constexpr unsigned long long kWaitNs = 1000000000ull; // 1 s
-
-__device__ __forceinline__ unsigned smemAddr(const void* p)
-{
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbarInit(uint64_t* bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbarExpectTx(uint64_t* bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, unsigned parity)
-{
-    unsigned done;
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(done)
-                 : "r"(smemAddr(bar)), "r"(parity)
-                 : "memory");
-    return done != 0;
-}
-__device__ __forceinline__ unsigned long long globalTimerNs()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ bool mbarWaitBounded(uint64_t* bar, unsigned parity,
-    unsigned long long limitNs = kWaitNs)
-{
-    const unsigned long long t0 = globalTimerNs();
-    for (long i = 0; i < kTmaSpin; ++i) {
-        if (mbarTryWait(bar, parity))
-            return true;
-        if ((i & 63) == 63 && globalTimerNs() - t0 > limitNs)
-            break;
-    }
-    return false;
-}
-__device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
-{
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(smemAddr(dst)),
-                 "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smemAddr(bar))
-                 : "memory");
-}
 } // namespace
 
 // One block of the TMA-staged stress kernel: elements x0 .. x0+31 of a grid
@@ -1785,7 +1734,7 @@ __device__ __forceinline__ void affineStrain(const float (&ul)[9], const float (
 
 template <int PART>
 __device__ __forceinline__ void affineDivergence(float (*fs)[9][kAffElems], int le, size_t e, size_t N,
-    float* __restrict__ tdiv, float keep)
+    float* __restrict__ tdiv, float keep, const float (&told)[6])
 {
     float w[4][9];
 #pragma unroll
@@ -1803,8 +1752,8 @@ __device__ __forceinline__ void affineDivergence(float (*fs)[9][kAffElems], int 
             ax = fmaf(axi, w[0][q], fmaf(aet, w[1][q], ax));
             ay = fmaf(axi, w[2][q], fmaf(aet, w[3][q], ay));
         }
-        tdiv[j * N + e] = fmaf(tdiv[j * N + e], keep, ax);
-        tdiv[(9 + j) * N + e] = fmaf(tdiv[(9 + j) * N + e], keep, ay);
+        tdiv[j * N + e] = fmaf(told[jj], keep, ax);
+        tdiv[(9 + j) * N + e] = fmaf(told[3 + jj], keep, ay);
     }
 }
 
@@ -1821,10 +1770,19 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
     const size_t e = x0 + le;
     const bool active = e < N && ice[e];
     // step constants first: a programmatic dependent launch overlaps them
-    // with the previous kernel's tail
-    float c[5], ul[9], vl[9], hP[3];
+    // with the previous kernel's tail.  So does this element's divergence
+    // from the previous iteration: no launch triggers its dependents early,
+    // so this kernel starts only after the node kernel before it has exited,
+    // and that kernel read the divergence only after the stress kernel that
+    // wrote it had completed; the node kernel only reads it.
+    float c[5], ul[9], vl[9], hP[3], told[6];
     double Pa[3];
     if (active) {
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+            told[jj] = tdiv[(3 * part + jj) * N + e];
+            told[3 + jj] = tdiv[(9 + 3 * part + jj) * N + e];
+        }
 #pragma unroll
         for (int k = 0; k < 5; ++k)
             c[k] = coef[k * ld + e];
@@ -1862,9 +1820,9 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
         return;
     const float keep = p.keep;
     switch (part) {
-    case 0: affineDivergence<0>(fs, le, e, N, tdiv, keep); break;
-    case 1: affineDivergence<1>(fs, le, e, N, tdiv, keep); break;
-    default: affineDivergence<2>(fs, le, e, N, tdiv, keep); break;
+    case 0: affineDivergence<0>(fs, le, e, N, tdiv, keep, told); break;
+    case 1: affineDivergence<1>(fs, le, e, N, tdiv, keep, told); break;
+    default: affineDivergence<2>(fs, le, e, N, tdiv, keep, told); break;
     }
 }
 
@@ -2606,17 +2564,47 @@ cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* 
     return cudaGetLastError();
 }
 
-cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
+namespace {
+EncodeTiledFn encodeTiledFn(cudaError_t& e)
 {
     static EncodeTiledFn encode = nullptr;
+    e = cudaSuccess;
     if (!encode) {
         void* fn = nullptr;
         cudaDriverEntryPointQueryResult q;
-        const cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q);
-        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-            return e != cudaSuccess ? e : cudaErrorNotSupported;
-        encode = reinterpret_cast<EncodeTiledFn>(fn);
+        e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q);
+        if (e == cudaSuccess && (q != cudaDriverEntryPointSuccess || !fn))
+            e = cudaErrorNotSupported;
+        if (e == cudaSuccess)
+            encode = reinterpret_cast<EncodeTiledFn>(fn);
     }
+    return encode;
+}
+} // namespace
+
+cudaError_t encodeTiled2d(CUtensorMap* map, CUtensorMapDataType type, const void* base, uint64_t inner,
+    uint64_t outer, uint64_t rowBytes, uint32_t boxInner, uint32_t boxOuter)
+{
+    cudaError_t e;
+    const EncodeTiledFn encode = encodeTiledFn(e);
+    if (!encode)
+        return e;
+    const cuuint64_t dims[2] = { inner, outer };
+    const cuuint64_t strides[1] = { rowBytes };
+    const cuuint32_t box[2] = { boxInner, boxOuter };
+    const cuuint32_t estr[2] = { 1, 1 };
+    const CUresult r = encode(map, type, 2, const_cast<void*>(base), dims, strides, box, estr,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
+{
+    cudaError_t ee;
+    const EncodeTiledFn encode = encodeTiledFn(ee);
+    if (!encode)
+        return ee;
     // the four operator blocks are rows of one [324][ld] array; ld * 4 bytes
     // is a multiple of 128 and the base is 256-byte aligned
     const cuuint64_t dims[2] = { o.ld, static_cast<cuuint64_t>(o.rowsG) };

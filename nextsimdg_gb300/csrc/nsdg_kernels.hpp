@@ -193,14 +193,26 @@ cudaError_t launchBenchmarkWind(cudaStream_t s, size_t nx, size_t ny, const Benc
     double* vw);
 cudaError_t launchBenchmarkOcean(cudaStream_t s, size_t nx, size_t ny, double dx, double dy, double vmax,
     double* uo, double* vo);
-// FP64 operator entries as float pairs {RN(x), RN(x - RN(x))} (n entries).
-cudaError_t launchSplitPairs(cudaStream_t s, size_t n, const double* src, float2* dst);
+// FP64 operator entries as float pairs {RN(x), RN(x - RN(x))}: rows x n
+// entries, rows n apart in src and ld apart in dst.
+cudaError_t launchSplitPairs(cudaStream_t s, size_t rows, size_t n, size_t ld, const double* src, float2* dst);
 // launchMevpStress with the operator products, Delta^2 and the stress
 // increments in float-pair arithmetic (nsdg_stress_pairs.cu); 1/Delta,
 // P / (8 alpha Delta) and the divergence update in FP64.  ops: [4][81][N]
 // float pairs of G_x, G_y, A_1, A_2 (Cartesian meshes).
-cudaError_t launchMevpStressPairs(cudaStream_t s, const DevMesh& m, const float2* ops, const double* u,
+// ops: [324][ld] float pairs, rows G_x | G_y | A_1 | A_2, ld = pairsLd(N).
+size_t pairsLd(size_t N);
+cudaError_t launchMevpStressPairs(cudaStream_t s, const DevMesh& m, const float2* ops, size_t ld, const double* u,
     const double* v, const double* Pg, double* tdiv, const MevpParams& p);
+// The same kernel with each phase's operator rows staged in shared memory by
+// one TMA copy per 32 elements (descriptors from makePairsMaps).
+struct alignas(64) PairsMaps {
+    CUtensorMap g;
+    CUtensorMap a;
+};
+cudaError_t makePairsMaps(const float2* ops, size_t ld, PairsMaps* out);
+cudaError_t launchMevpStressPairsTma(cudaStream_t s, const DevMesh& m, const PairsMaps& maps, const double* u,
+    const double* v, const double* Pg, double* tdiv, const MevpParams& p, int* err);
 // out[4 i + 0..3]: split(a) - a, widen(RN(x)), a x and a 9-term dot product,
 // each formed in float pairs and returned in FP64 (checks of nsdg_pairs.cuh).
 cudaError_t launchPairsSelfTest(cudaStream_t s, size_t n, const double* a, const double* x, double* out);
@@ -235,6 +247,11 @@ struct alignas(64) StressMaps {
     CUtensorMap a;
 };
 cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out);
+// A 2-D tiled TMA descriptor (cuTensorMapEncodeTiled through the runtime's
+// driver entry point): inner x outer elements of `type`, rows rowBytes apart
+// (a multiple of 16), boxes of boxInner x boxOuter, no swizzle, zero fill.
+cudaError_t encodeTiled2d(CUtensorMap* map, CUtensorMapDataType type, const void* base, uint64_t inner,
+    uint64_t outer, uint64_t rowBytes, uint32_t boxInner, uint32_t boxOuter);
 // One block waits (bounded) on an mbarrier nothing completes; *timedOut = 1
 // when the wait ran out as it must.
 cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* timedOut);

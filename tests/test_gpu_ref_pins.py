@@ -28,7 +28,7 @@ def _kernel(case, precision):
                               precision=precision)
 
 
-@pytest.mark.parametrize("stress", ["pairs", "fma"])
+@pytest.mark.parametrize("stress", ["fma", "pairs", "pairs_tma"])
 @pytest.mark.parametrize("name", ALL)
 def test_fp64_matches_reference(gpu, ref_goldens, name, stress, monkeypatch):
     """FP64 GPU path vs the reference build: h, A (and damage) in every DG
@@ -36,7 +36,8 @@ def test_fp64_matches_reference(gpu, ref_goldens, name, stress, monkeypatch):
     case (alpha = beta = 1500) runs the 7 steps over which the reference's
     own sensitivity to h x (1 + 1e-14) stays below 1e-11.  Both mEVP stress
     kernels of the FP64 path: FP64 FMA (the default) and float-pair products
-    (NSDG_FP64_STRESS=pairs)."""
+    with operators from global memory or staged by TMA
+    (NSDG_FP64_STRESS=pairs, pairs_tma)."""
     monkeypatch.setenv("NSDG_FP64_STRESS", stress)
     cases, data = ref_goldens
     case = cases.CASES[name]
