@@ -20,9 +20,12 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
          wall clock, host<->device copies inside.
   variants.plain_fp64     the FP64 path (the reference's arithmetic) on the
                           same grid, with its own roofline;
-  variants.learned_fp32   the learned warm start: data generation and
-                          training on the GPU, then the warm update with and
-                          without audit against the plain sub-cycle;
+  variants.learned_fp32   the learned warm start as configured for it:
+                          data from 2000 plain steps on 256^2 boxes with
+                          randomised cyclone tracks, training on the GPU,
+                          then the warm update on 1024^2 with and without
+                          audit against the plain sub-cycle, and a plain
+                          statement of the speed-up at equal error (or none);
   variants.ice_growth     the column thermodynamics before the dynamics
                           (IceGrowth + ThermoIce0 + HiblerSpread +
                           ConstantHealing) on the same cell count;
@@ -30,10 +33,18 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
                           the FP64 path's own response to h x (1 + 1e-14).
 
 --precision fp64 --nx 256 gives the FP64 drop-in path on the 256^2 grid.
+--ensemble 32 times the 32-member uneven ensemble alone.
+--table prints one line per benchmark configuration (64^2 DG1, 256^2, 512^2
+with BBM, the ensemble, 1024^2): the oracle on all host threads and on one
+thread beside the GPU paths.
+--day-error bbm|parts prints error checkpoints over a simulated day (the BBM
+at 512^2; the parts of the mixed path at 256^2) against the FP64 path.
 
 --impl reference times the CPU restatement of the reference algorithm (the
-oracle; the reference itself cannot be built: it needs Eigen, absent here)
-on the host cores with all threads, on the same workload.
+oracle, pinned against the reference's own code by the golden fixtures) on
+the host cores with all threads, on the same workload.  The reference's own
+build (oracle/_ref) needs the reference sources, which the timing host does
+not have.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -444,7 +455,7 @@ def ensemble_variant(args) -> dict:
     cyclones and h), batched against the members stepped one by one."""
     r = ensemble_measure(args, 32)
     return {kk: r[kk] for kk in ("value", "unit", "ms_per_step", "cells", "sequential_members", "autotuned_tiles",
-                                 "gpu_launches_per_step", "sides")}
+                                 "gpu_launches_per_step", "sides", "persistent_subcycle")}
 
 
 def learned_config5_variant(args) -> dict:
@@ -538,43 +549,23 @@ def learned_config5_variant(args) -> dict:
     for k in ks.values():
         k.close()
     big.close()
-    return out
-
-
-def learned_variant(args, box_eval, N: int, plain_ms: float):
-    """The learned warm start: samples from a perturbed trajectory (other h
-    phases, cyclone start and speed), training on the GPU, then (a) the warm
-    update without audit and (b) audited every 10th update against the
-    plain sub-cycle with a relative tolerance of 0.1, on the evaluation box."""
-    from nextsimdg_gb300 import surrogate
-    from nextsimdg_gb300.boxtest import BoxTest, step_forcing
-
-    K = args.warm_iters
-    tb = BoxTest(args.nx, seed=1, start=(0.45 * 512e3, 0.47 * 512e3), wind_speed=9.0, h_noise=0.02)
-    kt = make_kernel(tb, 1)
-    t0 = time.perf_counter()
-    net, kappa, loss = surrogate.train_warm_start(
-        kt, lambda k, s: step_forcing(k, tb, s), args.warm_samples, K, DT, stride=3,
-        iterations=args.warm_train_iters, batch=1, nx=args.nx, ny=args.nx, seed=1)
-    t_train = time.perf_counter() - t0
-    kt.close()
-    out = {"k_iters": K, "samples": args.warm_samples, "train_iterations": args.warm_train_iters,
-           "train_loss": loss, "data_and_training_s": t_train, "kappa": kappa * 1.5}
-    res = {}
-    for name, je, jt in (("unaudited", 0, 0.0), ("audited_every_10_tol_0.1", 10, 0.1)):
-        k = make_kernel(box_eval, 1)
-        k.set_warm_start(net, K, kappa * 1.5, je, jt)
-        for s in range(args.warmup):
-            step_forcing(k, box_eval, s)
-            k.update(s * DT, DT)
-        ms = k.time_updates(DT, args.steps) / args.steps
-        st = k.warm_stats()
-        res[name] = {"value": N / (ms * 1e-3), "ms_per_step": ms, "speedup_vs_plain_fp32": plain_ms / ms,
-                     "accepted": st["accepted"], "fallbacks": st["fallbacks"], "audited": st["audited"],
-                     "audit_rejected": st["audit_rejected"], "last_audit_rel_error": st["last_audit_error"]}
-        k.close()
-    out.update(res)
-    net.close()
+    un = out["unaudited"]
+    equal = out["error_after_steps"]["learned_vs_plain_fp32_m_per_s"] <= \
+        out["error_after_steps"]["plain_fp32_vs_fp64_m_per_s"]
+    if un["accepted"] == 0:
+        out["speedup_at_equal_error"] = None
+        out["statement"] = ("none: the network trained on 256x256 never passes the residual acceptance on "
+                            "1024x1024, so every step runs the plain sub-cycle after the network and K "
+                            f"iterations ({un['speedup_vs_plain_fp32']:.2f}x the plain FP32 step, same result)")
+    elif equal:
+        out["speedup_at_equal_error"] = un["speedup_vs_plain_fp32"]
+        out["statement"] = (f"{un['speedup_vs_plain_fp32']:.2f}x the plain FP32 step, with the 30-step velocity "
+                            "difference to plain FP32 within plain FP32's own difference to FP64")
+    else:
+        out["speedup_at_equal_error"] = None
+        out["statement"] = (f"none at equal error: unaudited {un['speedup_vs_plain_fp32']:.2f}x the plain FP32 "
+                            "step, but its 30-step velocity difference to plain FP32 exceeds plain FP32's "
+                            "difference to FP64")
     return out
 
 
@@ -881,7 +872,7 @@ def run_ours(args, world, rank, local):
             variants["distorted_mixed"] = distorted_variant(args, local)
             variants["ensemble32"] = ensemble_variant(args)
         if prec and args.warm_train_iters > 0:
-            variants["learned_fp32_config5"] = learned_config5_variant(args)
+            variants["learned_fp32"] = learned_config5_variant(args)
         if prec and not args.no_bbm:
             variants["bbm"] = bbm_variant(args, box, N)
         if prec:
@@ -905,7 +896,7 @@ def run_ours(args, world, rank, local):
                                    f"iterations, alpha=beta={ALPHA:g}, dt={DT:g} s",
                        "precision": args.precision,
                        "method": ("FP32 bulk (FP64: conservation sums, inverse mass matrices, Delta, viscosity); "
-                                  "the learned warm start is measured in variants.learned_fp32, not enabled here"
+                                  "the learned warm start is measured in variants.learned_fp32 (1024 x 1024), not enabled here"
                                   if prec else "FP64 throughout (the reference's arithmetic)"),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2, no flush: each step sweeps the FP32 transport operators "
@@ -1002,6 +993,18 @@ def ensemble_measure(args, n_members: int) -> dict:
     ens.time_updates(DT, max(args.warmup, 3))
     with ClockSampler(0) as clk:
         ms = ens.time_updates(DT, args.steps)
+    launches = ens.launches_per_update()
+    # the sub-cycle as one persistent cooperative launch per step (every box
+    # test is a parallelogram mesh)
+    try:
+        ens.set_persistent(True)
+        ens.time_updates(DT, max(args.warmup, 3))
+        pms = ens.time_updates(DT, args.steps)
+        persistent = {"value": sum(b.nelements for b in boxes) * args.steps / (pms * 1e-3),
+                      "ms_per_step": pms / args.steps, "gpu_launches_per_step": ens.launches_per_update()}
+        ens.set_persistent(False)
+    except Exception as exc:  # reported, not fatal for the other variants
+        persistent = {"error": str(exc)}
     # the same members one by one (each its own graph, same stream order)
     t_seq = 0.0
     for k in members:
@@ -1013,7 +1016,8 @@ def ensemble_measure(args, n_members: int) -> dict:
     out = {"value": cells * args.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.steps, "cells": cells,
            "members": len(boxes), "sides": sorted(int(b.nx) for b in boxes),
            "sequential_members": {"value": cells * args.steps / (t_seq * 1e-3), "ms_per_step": t_seq / args.steps},
-           "autotuned_tiles": tiles, "gpu_launches_per_step": ens.launches_per_update(), "clocks": clk.summary()}
+           "autotuned_tiles": tiles, "gpu_launches_per_step": launches, "persistent_subcycle": persistent,
+           "clocks": clk.summary()}
     ens.close()
     for k in members:
         k.close()
@@ -1053,6 +1057,202 @@ def run_profile(args):
     k.close()
 
 
+def _oracle_rate(box, dg: int, rheology: int, n_steps: int, steps: int, threads: int | None = None,
+                 warm: int = 1) -> dict:
+    """The oracle stepping `box` (all OpenMP threads, or `threads`): cell-updates/s
+    over `steps` model steps after `warm` untimed ones."""
+    from oracle import pyoracle
+    from nextsimdg_gb300.boxtest import step_forcing
+    pyoracle.load()
+    cores = pyoracle.num_threads()
+    k = pyoracle.OracleKernel(rheology, dg, alpha=ALPHA, beta=BETA, n_steps=n_steps)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    if rheology == 1:
+        k.setData("damage", box.damage())
+    if threads:
+        pyoracle.set_threads(threads)
+    try:
+        for s in range(warm):
+            step_forcing(k, box, s)
+            k.update(s * DT, DT)
+        t = 0.0
+        for s in range(warm, warm + steps):
+            step_forcing(k, box, s)
+            t0 = time.perf_counter()
+            k.update(s * DT, DT)
+            t += time.perf_counter() - t0
+    finally:
+        pyoracle.set_threads(cores)
+    return {"value": box.nelements * steps / t, "steps": steps, "seconds": round(t, 2),
+            "threads": threads or cores}
+
+
+def _gpu_rate(box, dg: int, rheology: int, precision: int, n_steps: int, steps: int) -> dict:
+    """The library's kernel stepping `box` as one CUDA graph per step (CUDA
+    events, device-resident inputs)."""
+    from nextsimdg_gb300.boxtest import step_forcing
+    from nextsimdg_gb300.dynamics import BBMDynamicsKernel, MEVPDynamicsKernel
+    if rheology == 1:
+        k = BBMDynamicsKernel(dg_comp=dg, n_steps=n_steps, precision=precision)
+    else:
+        k = MEVPDynamicsKernel(dg_comp=dg, alpha=ALPHA, beta=BETA, n_steps=n_steps, precision=precision)
+    k.initialise(box.coords(), False, box.mask())
+    for name, arr in box.initial_fields().items():
+        k.setData(name, arr)
+    if rheology == 1:
+        k.setData("damage", box.damage())
+    for s in range(3):
+        step_forcing(k, box, s)
+        k.update(s * DT, DT)
+    ms = k.time_updates(DT, steps) / steps
+    k.close()
+    return {"value": box.nelements / (ms * 1e-3), "ms_per_step": ms, "steps": steps}
+
+
+def run_table(args):
+    """One JSON line per benchmark configuration: the oracle on the host cores
+    (all threads and one thread) next to the GPU paths, same grid, same
+    forcing.  The one-thread and large-grid CPU samples are bounded (a few
+    steps); each entry states its sample."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    from oracle import pyoracle
+    pyoracle.load()
+    host = {"cpu_model": cpu_model(), "cores": pyoracle.num_threads()}
+    bbm_sub = lambda b: int(math.ceil(max(NSTEPS, math.ceil(  # noqa: E731
+        DT / (0.5 * (b.L / b.nx) / math.sqrt(5.9467e8 / 900.0)))) / 50.0)) * 50
+    rows = []
+    b = BoxTest(64)
+    rows.append({"config": "64x64 DG1/CG2 FP64, one day (720 steps)",
+                 "cpu_all_cores": _oracle_rate(b, 1, 0, NSTEPS, 720),
+                 "cpu_one_thread": _oracle_rate(b, 1, 0, NSTEPS, 20, threads=1),
+                 "gpu_fp64": _gpu_rate(b, 1, 0, 0, NSTEPS, 720),
+                 "gpu_mixed": _gpu_rate(b, 1, 0, 1, NSTEPS, 720)})
+    b = BoxTest(256)
+    rows.append({"config": "256x256 DG2/CG2 FP64",
+                 "cpu_all_cores": _oracle_rate(b, DG, 0, NSTEPS, 10),
+                 "cpu_one_thread": _oracle_rate(b, DG, 0, NSTEPS, 1, threads=1),
+                 "gpu_fp64": _gpu_rate(b, DG, 0, 0, NSTEPS, 20),
+                 "gpu_mixed": _gpu_rate(b, DG, 0, 1, NSTEPS, 20)})
+    b = BoxTest(512)
+    sub = bbm_sub(b)
+    rows.append({"config": f"512x512 DG2/CG2: mEVP, and BBM with {sub} elastic sub-steps",
+                 "cpu_all_cores": _oracle_rate(b, DG, 0, NSTEPS, 5),
+                 "cpu_one_thread": _oracle_rate(b, DG, 0, NSTEPS, 1, threads=1, warm=0),
+                 "cpu_all_cores_bbm": _oracle_rate(b, DG, 1, sub, 1),
+                 "gpu_fp64": _gpu_rate(b, DG, 0, 0, NSTEPS, 10),
+                 "gpu_mixed": _gpu_rate(b, DG, 0, 1, NSTEPS, 20),
+                 "gpu_fp64_bbm": _gpu_rate(b, DG, 1, 0, sub, 3),
+                 "gpu_mixed_bbm": _gpu_rate(b, DG, 1, 1, sub, 3)})
+    boxes = ensemble_boxes(32)
+    cells = sum(x.nelements for x in boxes)
+    t_cpu = sum(x.nelements / _oracle_rate(x, DG, 0, NSTEPS, 1)["value"] for x in boxes)
+    t_fp64 = sum(x.nelements / _gpu_rate(x, DG, 0, 0, NSTEPS, 3)["value"] for x in boxes)
+    ens = ensemble_measure(args, 32)
+    rows.append({"config": f"32-member uneven ensemble, {cells} cells",
+                 "cpu_all_cores": {"value": cells / t_cpu, "steps": 1, "seconds": round(t_cpu, 2),
+                                   "sample": "one step of every member after one warm-up step"},
+                 "cpu_one_thread": None,
+                 "gpu_fp64": {"value": cells / t_fp64, "sample": "members stepped one by one, FP64"},
+                 "gpu_mixed": {kk: ens[kk] for kk in ("value", "ms_per_step", "persistent_subcycle")}})
+    b = BoxTest(1024)
+    rows.append({"config": "1024x1024 DG2/CG2 (the learned warm start's grid)",
+                 "cpu_all_cores": _oracle_rate(b, DG, 0, NSTEPS, 1, warm=0),
+                 "cpu_one_thread": None,
+                 "gpu_fp64": _gpu_rate(b, DG, 0, 0, NSTEPS, 3),
+                 "gpu_mixed": _gpu_rate(b, DG, 0, 1, NSTEPS, 10),
+                 "gpu_learned": "variants.learned_fp32_config5 of the default bench line"})
+    for r in rows:
+        print(json.dumps({"table": True, "unit": UNIT, **host, **r}), flush=True)
+
+
+def _day_kernel(box, prec: int, env: dict | None = None, scale: float = 1.0, alpha: float = ALPHA):
+    """make_kernel with the library's selection variables set while the
+    kernel is created (they are read at creation)."""
+    old = {k: os.environ.get(k) for k in (env or {})}
+    os.environ.update(env or {})
+    try:
+        return make_kernel(box, prec, scale_h=scale, alpha=alpha)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def run_day_error(args):
+    """Error checkpoints over a simulated day, one JSON line per checkpoint
+    and a final RESULT line: RMS of u/v (as |(du, dv)|) and of the other
+    fields against the plain FP64 path, for the FP64 path with h x (1 + 1e-14)
+    (its own sensitivity, the floor) and the other paths.
+
+    bbm:   512 x 512 BBM (damage 1, elastic sub-steps resolving the elastic
+           wave), FP64 and mixed precision, 720 steps, every 120.
+    parts: 256 x 256 mEVP alpha = beta = 1500: the mixed path, the mixed path
+           with FP64 transport, the FP64 path with the float-pair stress
+           kernel, 360 steps, every 60 (which part of the mixed path carries
+           its excess over the floor)."""
+    from nextsimdg_gb300._lib import NsdgError
+    from nextsimdg_gb300.boxtest import BoxTest, step_forcing
+    from nextsimdg_gb300.dynamics import BBMDynamicsKernel
+    rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+    if args.day_error == "parts":
+        box = BoxTest(256)
+        ks = {"fp64": _day_kernel(box, 0, alpha=1500.0), "fp64p": _day_kernel(box, 0, scale=1 + 1e-14, alpha=1500.0),
+              "mixed": _day_kernel(box, 1, alpha=1500.0),
+              "mixed_fp64_transport": _day_kernel(box, 1, {"NSDG_MIXED_TRANSPORT": "fp64"}, alpha=1500.0),
+              "fp64_pairs": _day_kernel(box, 0, {"NSDG_FP64_STRESS": "pairs_tma"}, alpha=1500.0)}
+        steps, every, fields = 360, 60, ("u", "v", "hice", "cice")
+        extra = {"grid": "256x256", "alpha": 1500.0}
+    else:
+        box = BoxTest(512)
+        dx = box.L / box.nx
+        sub = max(NSTEPS, int(math.ceil(DT / (0.5 * dx / math.sqrt(5.9467e8 / 900.0)))))
+        sub = int(math.ceil(sub / 50.0)) * 50
+        ks = {}
+        for name, prec, scale in (("fp64", 0, 1.0), ("fp64p", 0, 1.0 + 1e-14), ("mixed", 1, 1.0)):
+            k = BBMDynamicsKernel(dg_comp=DG, n_steps=sub, precision=prec)
+            k.initialise(box.coords(), False, box.mask())
+            for f, arr in box.initial_fields().items():
+                k.setData(f, arr * scale if f == "hice" else arr)
+            k.setData("damage", box.damage())
+            ks[name] = k
+        steps, every, fields = 720, 120, ("u", "v", "hice", "cice", "damage")
+        extra = {"grid": "512x512", "rheology": "BBM", "sub_steps": sub}
+    failed, cps = {}, []
+    t0 = time.time()
+    for s in range(steps):
+        for n, k in ks.items():
+            if n not in failed:
+                step_forcing(k, box, s)
+                k.update(s * DT, DT)
+        if (s + 1) % every == 0 or s == steps - 1:
+            r = {}
+            for n, k in ks.items():
+                if n in failed:
+                    continue
+                try:
+                    r[n] = {f: k.getDG0Data(f) for f in fields}
+                except NsdgError:
+                    failed[n] = s + 1
+            cp = {"step": s + 1, "t": round(time.time() - t0, 1)}
+            for n in ks:
+                if n != "fp64" and n in r and "fp64" in r:
+                    x, ref = r[n], r["fp64"]
+                    cp[n] = {"uv": rms(np.hypot(x["u"] - ref["u"], x["v"] - ref["v"]))}
+                    for f in fields:
+                        if f not in ("u", "v"):
+                            cp[n][f] = rms(x[f] - ref[f])
+            cps.append(cp)
+            print(json.dumps(cp), flush=True)
+    for k in ks.values():
+        k.close()
+    print("RESULT", json.dumps({"day_error": args.day_error, **extra, "checkpoints": cps, "failed": failed}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1074,12 +1274,21 @@ def main():
     ap.add_argument("--warm-samples", type=int, default=120, help="training samples (every 3rd step)")
     ap.add_argument("--warm-train-iters", type=int, default=2000, help="Adam steps (0: skip the learned variant)")
     ap.add_argument("--no-bbm", action="store_true", help="skip the BBM variant")
+    ap.add_argument("--day-error", choices=["bbm", "parts"],
+                    help="error checkpoints over a simulated day against the FP64 path (BBM at 512^2, or the "
+                         "mixed path's parts at 256^2)")
+    ap.add_argument("--table", action="store_true",
+                    help="one line per benchmark configuration: the oracle (all threads, one thread) beside the GPU")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident steps (for ncu captures): no e2e, no baselines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
-    if args.ensemble:
+    if args.day_error:
+        run_day_error(args)
+    elif args.table:
+        run_table(args)
+    elif args.ensemble:
         run_ensemble(args)
     elif args.profile:
         run_profile(args)

@@ -234,6 +234,14 @@ int nsdg_ensemble_synchronize(nsdg_ensemble* ens);
 int nsdg_ensemble_time_updates(nsdg_ensemble* ens, double dt, int steps, float* ms);
 int nsdg_ensemble_tile(nsdg_ensemble* ens, int member, int* tile_w, int* tile_h);
 int nsdg_ensemble_launches_per_update(nsdg_ensemble* ens, int* launches);
+/* on != 0: run the mEVP sub-cycle of all members as one persistent
+ * cooperative launch per update (the iterations' element and node phases as
+ * grid-stride loops separated by grid barriers whose waits are bounded: a wait
+ * that runs out reports NSDG_ERR_CUDA through the next read) instead of one
+ * element and one node launch per iteration.  Bitwise the same results.
+ * Every member must be a parallelogram mesh (NSDG_ERR_UNSUPPORTED otherwise).
+ * No reference counterpart. */
+int nsdg_ensemble_set_persistent(nsdg_ensemble* ens, int on);
 
 /* ======================================================================== */
 /* Stand-alone DG transport (the DGTransport<DG> class of the reference)    */

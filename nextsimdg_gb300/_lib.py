@@ -120,6 +120,7 @@ SIGNATURES = [
     ("nsdg_ensemble_time_updates", c_int, [c_void_p, c_double, c_int, POINTER(c_float)]),
     ("nsdg_ensemble_tile", c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int)]),
     ("nsdg_ensemble_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
+    ("nsdg_ensemble_set_persistent", c_int, [c_void_p, c_int]),
     ("nsdg_net_create", c_int, [c_int, POINTER(c_int), c_int, c_int, c_int, c_int, ctypes.c_ulonglong,
                                 POINTER(c_void_p)]),
     ("nsdg_net_destroy", c_int, [c_void_p]),

@@ -2100,8 +2100,13 @@ struct nsdg_ensemble {
     uint16_t* dStressMap = nullptr;
     uint16_t* dNodeMap = nullptr;
     uint16_t* dTmaMap = nullptr;
+    uint16_t* dNodeMapP = nullptr; // node blocks of the persistent sub-cycle
+    unsigned* dBar = nullptr;      // its grid barrier (arrivals, generation)
     int* derr = nullptr;
-    int stressBlocks = 0, nodeBlocks = 0, tmaBlocks = 0;
+    int stressBlocks = 0, nodeBlocks = 0, tmaBlocks = 0, nodeBlocksP = 0;
+    // the sub-cycle as one persistent cooperative launch (parallelogram
+    // members only) instead of two launches per iteration
+    bool persistent = false;
     // element phase: 0 tiled global-load kernel, 1 TMA-staged, 2 parallelogram
     // coefficients (every member a parallelogram mesh)
     int elementKind = 0;
@@ -2255,22 +2260,26 @@ int nsdg_ensemble::autotune()
 int nsdg_ensemble::build()
 {
     std::vector<EnsembleMember> table;
-    std::vector<uint16_t> smap, nmap, tmap;
+    std::vector<uint16_t> smap, nmap, tmap, pmap;
+    const size_t perP = static_cast<size_t>(persistentNodesPerBlock());
     for (size_t mi = 0; mi < members.size(); ++mi) {
         EnsembleMember d = describe(members[mi], tileW[mi]);
         d.stressBlock0 = static_cast<int>(smap.size());
         d.nodeBlock0 = static_cast<int>(nmap.size());
         d.tmaBlock0 = static_cast<int>(tmap.size());
+        d.nodeBlockP = static_cast<int>(pmap.size());
         smap.insert(smap.end(), stressBlocksOf(d), static_cast<uint16_t>(mi));
         nmap.insert(nmap.end(), nodeBlocksOf(d), static_cast<uint16_t>(mi));
         tmap.insert(tmap.end(), tmaBlocksOf(d), static_cast<uint16_t>(mi));
+        pmap.insert(pmap.end(), (d.Ncg + perP - 1) / perP, static_cast<uint16_t>(mi));
         table.push_back(d);
     }
     stressBlocks = static_cast<int>(smap.size());
     nodeBlocks = static_cast<int>(nmap.size());
     tmaBlocks = static_cast<int>(tmap.size());
+    nodeBlocksP = static_cast<int>(pmap.size());
     const size_t bytes = al(table.size() * sizeof(EnsembleMember)) + al(smap.size() * 2) + al(nmap.size() * 2)
-        + al(tmap.size() * 2) + al(4);
+        + al(tmap.size() * 2) + al(pmap.size() * 2) + al(2 * sizeof(unsigned)) + al(4);
     if (cudaMalloc(&dmem, bytes) != cudaSuccess)
         return fail(NSDG_ERR_CUDA, "ensemble: allocation failed");
     char* p = static_cast<char*>(dmem);
@@ -2282,11 +2291,17 @@ int nsdg_ensemble::build()
     p += al(nmap.size() * 2);
     dTmaMap = reinterpret_cast<uint16_t*>(p);
     p += al(tmap.size() * 2);
+    dNodeMapP = reinterpret_cast<uint16_t*>(p);
+    p += al(pmap.size() * 2);
+    dBar = reinterpret_cast<unsigned*>(p);
+    p += al(2 * sizeof(unsigned));
     derr = reinterpret_cast<int*>(p);
     cudaError_t e = cudaMemcpy(dMembers, table.data(), table.size() * sizeof(EnsembleMember), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dStressMap, smap.data(), smap.size() * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dNodeMap, nmap.data(), nmap.size() * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dTmaMap, tmap.data(), tmap.size() * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dNodeMapP, pmap.data(), pmap.size() * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(dBar, 0, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
     if (e != cudaSuccess)
         return fail(NSDG_ERR_CUDA, std::string("ensemble: upload failed: ") + cudaGetErrorString(e));
@@ -2388,7 +2403,14 @@ int nsdg_ensemble::ensureGraph(double dt)
             break;
         }
     }
-    for (int it = 0; it < P.n_steps && st == NSDG_OK; ++it) {
+    if (persistent && elementKind == 2 && st == NSDG_OK) {
+        e = launchEnsembleSubcyclePersistent(stream, dMembers, dTmaMap, tmaBlocks, dNodeMapP, nodeBlocksP, mp,
+            viscMode, P.n_steps, dBar, derr);
+        if (e != cudaSuccess)
+            st = fail(NSDG_ERR_CUDA, std::string("ensemble persistent sub-cycle: ") + cudaGetErrorString(e));
+        total += 1;
+    }
+    for (int it = 0; it < P.n_steps && st == NSDG_OK && !(persistent && elementKind == 2); ++it) {
         e = launchElements(stream, dMembers, mp);
         if (e == cudaSuccess)
             e = launchMevpMomentum32Batched(stream, dMembers, dNodeMap, nodeBlocks, mp, derr);
@@ -2505,6 +2527,23 @@ int nsdg_ensemble_update(nsdg_ensemble* ens, double t_start, double dt)
     return NSDG_OK;
 }
 
+int nsdg_ensemble_set_persistent(nsdg_ensemble* ens, int on)
+{
+    if (!ens)
+        return NSDG_ERR_BAD_ARG;
+    if (on && ens->elementKind != 2)
+        return ens->fail(NSDG_ERR_UNSUPPORTED, "set_persistent: every member must be a parallelogram mesh");
+    if (ens->stream)
+        cudaStreamSynchronize(ens->stream);
+    if (ens->graph) {
+        cudaGraphExecDestroy(ens->graph);
+        ens->graph = nullptr;
+    }
+    ens->persistent = on != 0;
+    ens->err.clear();
+    return NSDG_OK;
+}
+
 int nsdg_ensemble_synchronize(nsdg_ensemble* ens)
 {
     if (!ens)
@@ -2516,6 +2555,8 @@ int nsdg_ensemble_synchronize(nsdg_ensemble* ens)
         return ens->fail(NSDG_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
     if (h) {
         cudaMemsetAsync(ens->derr, 0, sizeof(int), ens->stream);
+        if (h & DEV_ERR_TIMEOUT)
+            return ens->fail(NSDG_ERR_CUDA, "a bounded wait of the ensemble's sub-cycle ran out");
         return ens->fail(NSDG_ERR_NUMERIC, "non-finite velocity in an ensemble member");
     }
     return NSDG_OK;

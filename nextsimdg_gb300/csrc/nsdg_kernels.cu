@@ -3,6 +3,7 @@
 // One thread per element (element kernels) or per CG2 node (node kernels);
 // every accumulation into a node or an element is a gather in a fixed order,
 // so results are bitwise reproducible from run to run (no atomics on data).
+#include <algorithm>
 #include <cmath>
 
 #include "nsdg_host.hpp"
@@ -1988,6 +1989,81 @@ __global__ void __launch_bounds__(kAffElems * kStressParts, 12) kMevpStress32Aff
     affineBlock<VM>(M.nx, M.N, M.ice, M.affCoef, M.affLd, M.st.u, M.st.v, M.Pg, M.tdiv, p, x0, fs);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent sub-cycle of a parallelogram ensemble: one cooperative launch
+// runs all mEVP iterations of every member, the element phase and the node
+// phase as grid-stride loops over the same block maps as the per-phase
+// launches, separated by grid barriers.  Each element and node is computed
+// by the same arithmetic in the same order as in kMevpStress32AffineBatched
+// and kMevpMomentum32Batched, so the results are bitwise the same.
+//
+// The grid barrier is the project's own, with a bounded wait: bar[0] counts
+// arrivals, bar[1] is the generation (both zero before the launch).  A block
+// whose wait runs out (1 s of the GPU's global timer, or 2^26 polls) sets
+// DEV_ERR_TIMEOUT and leaves the loop; every other block then runs out at
+// its next barrier, so the kernel always ends.
+namespace {
+__device__ bool gridBarrierBounded(unsigned* bar, int* err, int* okShared)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        bool ok = true;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const unsigned long long t0 = globalTimerNs();
+            for (long i = 0;; ++i) {
+                if (*gen != g)
+                    break;
+                if (i >= kTmaSpin || ((i & 63) == 63 && globalTimerNs() - t0 > kWaitNs)) {
+                    ok = false;
+                    atomicOr(err, DEV_ERR_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        *okShared = ok ? 1 : 0;
+    }
+    __syncthreads();
+    return *okShared != 0;
+}
+} // namespace
+
+template <int VM>
+__global__ void __launch_bounds__(kAffElems * kStressParts) kEnsembleSubcyclePersistent(
+    const EnsembleMember* __restrict__ members, const uint16_t* __restrict__ elemMap, int elemBlocks,
+    const uint16_t* __restrict__ nodeMap, int nodeBlocks, MevpParams p, int iterations, unsigned* __restrict__ bar,
+    int* __restrict__ err)
+{
+    __shared__ float fs[4][9][kAffElems];
+    __shared__ int okShared;
+    constexpr int kThreads = kAffElems * kStressParts;
+    for (int it = 0; it < iterations; ++it) {
+        for (int b = blockIdx.x; b < elemBlocks; b += gridDim.x) {
+            const EnsembleMember& M = members[elemMap[b]];
+            const size_t x0 = size_t(b - M.tmaBlock0) * kAffElems;
+            affineBlock<VM>(M.nx, M.N, M.ice, M.affCoef, M.affLd, M.st.u, M.st.v, M.Pg, M.tdiv, p, x0, fs);
+            __syncthreads(); // the next work block reuses fs
+        }
+        if (!gridBarrierBounded(bar, err, &okShared))
+            break;
+        for (int b = blockIdx.x; b < nodeBlocks; b += gridDim.x) {
+            const EnsembleMember& M = members[nodeMap[b]];
+            const size_t i = size_t(b - M.nodeBlockP) * kThreads + threadIdx.x;
+            if (i < M.Ncg)
+                mevpMomentum32Node(M.nx, M.ny, M.N, i, M.cg2Dir, M.st, M.tdiv, p, err);
+        }
+        if (!gridBarrierBounded(bar, err, &okShared))
+            break;
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) kMevpMomentum32Batched(const EnsembleMember* __restrict__ members,
     const uint16_t* __restrict__ blockMember, MevpParams p, int* __restrict__ err)
 {
@@ -2775,6 +2851,41 @@ cudaError_t launchMevpStress32AffineBatched(cudaStream_t s, const EnsembleMember
     default: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<2>, members, blockMember, p);
     }
 }
+int persistentNodesPerBlock() { return kAffElems * kStressParts; }
+
+cudaError_t launchEnsembleSubcyclePersistent(cudaStream_t s, const EnsembleMember* members, const uint16_t* elemMap,
+    int elemBlocks, const uint16_t* nodeMap, int nodeBlocks, const MevpParams& pIn, int viscosityMode,
+    int iterations, unsigned* bar, int* err)
+{
+    const MevpParams p = withDerived(pIn);
+    int dev = 0, sms = 0, perSm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto kern = viscosityMode == 0 ? kEnsembleSubcyclePersistent<0>
+        : viscosityMode == 1 ? kEnsembleSubcyclePersistent<1> : kEnsembleSubcyclePersistent<2>;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kAffElems * kStressParts, 0);
+    if (e != cudaSuccess)
+        return e;
+    if (perSm < 1)
+        return cudaErrorInvalidConfiguration;
+    // every block resident at once (the cooperative launch enforces it), and
+    // no more blocks than the larger phase has work blocks
+    const int grid = std::max(1, std::min(perSm * sms, std::max(elemBlocks, nodeBlocks)));
+    e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess)
+        return e;
+    cudaLaunchConfig_t cfg {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kAffElems * kStressParts);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, members, elemMap, elemBlocks, nodeMap, nodeBlocks, p, iterations, bar, err);
+}
+
 int stressElementsPerBlock() { return kStressElems; }
 int nodesPerBlock() { return kBlock; }
 

@@ -319,10 +319,21 @@ struct EnsembleMember {
     int tileW, tileH, tilesX;
     int stressBlock0, nodeBlock0;
     int tmaBlock0;   // first block of this member in the TMA-staged / parallelogram batched launch
+    int nodeBlockP;  // first block of this member in the persistent sub-cycle's node phase
     StressMaps maps; // the member's tensor maps (64-byte aligned inside the device table)
     const float* affCoef; // [5][affLd] parallelogram coefficients (null: not a parallelogram mesh)
     size_t affLd;
 };
+// The whole mEVP sub-cycle of a parallelogram ensemble (every member has
+// coefficients) as one cooperative, persistent launch: `iterations` times the
+// element phase (the parallelogram kernel, blocks of elemMap as in the batched
+// launch) and the node phase (nodeMap: blocks of persistentNodesPerBlock()
+// nodes), separated by bounded grid barriers on bar[2] (set to zero here
+// first).  Bitwise the same results as the per-phase launches.
+int persistentNodesPerBlock();
+cudaError_t launchEnsembleSubcyclePersistent(cudaStream_t s, const EnsembleMember* members, const uint16_t* elemMap,
+    int elemBlocks, const uint16_t* nodeMap, int nodeBlocks, const MevpParams& p, int viscosityMode,
+    int iterations, unsigned* bar, int* err);
 // One launch each for the element and the node phase of every member.
 cudaError_t launchMevpStress32Batched(cudaStream_t s, const EnsembleMember* members, const uint16_t* blockMember,
     int blocks, const MevpParams& p);

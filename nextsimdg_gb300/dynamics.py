@@ -379,6 +379,11 @@ class Ensemble:
         self._check(self._l.nsdg_ensemble_launches_per_update(self._h, byref(n)))
         return n.value
 
+    def set_persistent(self, on: bool = True):
+        """Run the sub-cycle as one persistent cooperative launch per update
+        (nsdg_ensemble_set_persistent; parallelogram members only)."""
+        self._check(self._l.nsdg_ensemble_set_persistent(self._h, int(bool(on))))
+
 
 class DGTransport:
     """Stand-alone DG transport (DGTransport<DG>) on an explicitly described mesh.

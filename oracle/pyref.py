@@ -186,3 +186,93 @@ class RefKernel:
         out = np.empty((self.nelements, 8))
         self._check(self._l.ref_kernel_get_stress(self._h, name.encode(), _p(out), out.size))
         return out
+
+
+# -- the module build (oracle/_ref/libnsdg_module.so) ----------------------
+MODLIB = HERE / "_ref" / "libnsdg_module.so"
+_mlib = None
+
+
+def build_module() -> Path | None:
+    """`make -C oracle module` where the reference sources are (needs the
+    product library nextsimdg_gb300/libnsdg_gb300.so).  None when it cannot
+    be built here."""
+    root = reference_root()
+    if root is None:
+        return MODLIB if MODLIB.exists() else None
+    subprocess.run(["make", "-C", str(HERE), "module", f"REF={root}", f"-j{os.cpu_count() or 4}"], check=True,
+                   stdout=subprocess.DEVNULL)
+    return MODLIB
+
+
+def load_module() -> ctypes.CDLL:
+    global _mlib
+    if _mlib is None:
+        if not MODLIB.exists():
+            raise FileNotFoundError(f"{MODLIB} is not built (make -C oracle module REF=<reference sources>)")
+        lib = ctypes.CDLL(str(MODLIB))
+        sig = {
+            "mod_last_error": (c_char_p, [c_void_p]),
+            "mod_create": (c_void_p, [c_char_p, c_size_t, c_size_t, c_int]),
+            "mod_destroy": (None, [c_void_p]),
+            "mod_configure": (c_int, [c_void_p, c_char_p]),
+            "mod_precision": (c_int, [c_void_p]),
+            "mod_set_state": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p]),
+            "mod_step": (c_int, [c_void_p, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+            "mod_get": (c_int, [c_void_p, c_char_p, c_void_p, c_size_t]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _mlib = lib
+    return _mlib
+
+
+class DynamicsModule:
+    """A dynamics module of the model: "MEVPDynamics" or "BBMDynamics" (the
+    reference's own), "GPUMEVPDynamics" or "GPUBBMDynamics" (the product's
+    adapters), driven as the model drives it: setData with the initial
+    state, then per step the forcing put into the shared store and update."""
+
+    def __init__(self, kind: str, nx: int, ny: int, precision: int = 0):
+        self._l = load_module()
+        self._h = self._l.mod_create(kind.encode(), nx, ny, precision)
+        if not self._h:
+            raise RuntimeError(self._l.mod_last_error(None).decode())
+        self.kind, self.nx, self.ny = kind, nx, ny
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.mod_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st):
+        if st != 0:
+            raise RuntimeError(self._l.mod_last_error(self._h).decode())
+
+    def configure(self, text: str = ""):
+        self._check(self._l.mod_configure(self._h, text.encode()))
+
+    @property
+    def precision(self) -> int:
+        return self._l.mod_precision(self._h)
+
+    def set_state(self, coords, mask, hice, cice, u, v, damage=None, spherical=False):
+        arrs = [_f64(a) for a in (coords, mask, hice, cice, u, v)]
+        d = None if damage is None else _f64(damage)
+        self._check(self._l.mod_set_state(self._h, _p(arrs[0]), int(spherical), *[_p(a) for a in arrs[1:]],
+                                          None if d is None else _p(d)))
+
+    def step(self, t: float, dt: float, uwind=None, vwind=None, uocean=None, vocean=None, ssh=None):
+        arrs = [None if a is None else _f64(a) for a in (uwind, vwind, uocean, vocean, ssh)]
+        self._check(self._l.mod_step(self._h, float(t), float(dt), *[None if a is None else _p(a) for a in arrs]))
+
+    def get(self, name: str) -> np.ndarray:
+        out = np.empty(self.nx * self.ny)
+        self._check(self._l.mod_get(self._h, name.encode(), _p(out), out.size))
+        return out

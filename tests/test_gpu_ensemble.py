@@ -105,3 +105,42 @@ def test_ensemble_rejects_fp64_members(gpu):
     k.initialise(BoxTest(8).coords(), False, BoxTest(8).mask())
     with pytest.raises(NsdgError):
         Ensemble([k])
+
+
+def test_persistent_subcycle_matches_the_per_phase_launches(gpu):
+    """The sub-cycle as one persistent cooperative launch per step
+    (nsdg_ensemble_set_persistent): bitwise the same as the per-phase
+    launches and as the members stepped alone."""
+    boxes = _boxes()
+    persistent = [_member(b) for b in boxes]
+    solo = [_member(b) for b in boxes]
+    ens = Ensemble(persistent)
+    ens.set_persistent(True)
+    for s in range(3):
+        for b, k in zip(boxes, persistent):
+            uw, vw = b.wind(s * b.dt)
+            k.setData("uwind", uw)
+            k.setData("vwind", vw)
+        ens.update(s * 120.0, 120.0)
+        for b, k in zip(boxes, solo):
+            uw, vw = b.wind(s * b.dt)
+            k.setData("uwind", uw)
+            k.setData("vwind", vw)
+            k.update(s * 120.0, 120.0)
+    ens.synchronize()
+    for a, b in zip(persistent, solo):
+        for name in ("u", "v", "hice", "cice", "uiostress"):
+            np.testing.assert_array_equal(a.getDG0Data(name), b.getDG0Data(name))
+    # one launch for the whole sub-cycle (plus its barrier reset)
+    assert ens.launches_per_update() < 2 + 20 * len(boxes)
+    ens.close()
+
+
+def test_persistent_needs_parallelogram_members(gpu):
+    box = BoxTest(16, distort=0.05)
+    k = _member(box)
+    ens = Ensemble([k])
+    with pytest.raises(NsdgError) as e:
+        ens.set_persistent(True)
+    assert e.value.status == 6  # NSDG_ERR_UNSUPPORTED
+    ens.close()
