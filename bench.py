@@ -382,21 +382,33 @@ def stress_roofline(k, N: int, prec: int, ms_step: float, local: int, nx: int):
         # every FP32 stress kernel on this mesh: the operator-streaming ones
         # (global loads, TMA tiles) and, on a parallelogram mesh, the
         # coefficient kernel with each FP64 viscosity form
-        names = {3: "global", 4: "tma", 5: "affine_rsqrt_f64", 6: "affine_newton_f64", 7: "affine_newton_f64_intcvt"}
-        roof["stress_kernel_ms"] = {names[i]: k.time_kernel(i, 50)[0] for i in ((3, 4, 5, 6, 7) if affine else (3, 4))}
+        names = {3: "global", 4: "tma", 5: "affine_rsqrt_f64", 6: "affine_newton_f64", 7: "affine_newton_f64_intcvt",
+                 8: "affine_float_pairs", 12: "affine_float_pairs_checked"}
+        ids = (3, 4, 5, 6, 7, 8, 12) if affine else (3, 4)
+        roof["stress_kernel_ms"] = {names[i]: k.time_kernel(i, 50)[0] for i in ids}
         roof["stress_kernel"] = kind
         roof["parallelogram_mismatch"] = mismatch
         if affine:
-            # with 5 coefficients per element the kernel's limiter is FP64
-            # issue: Delta and the viscosity take 3 DFMA + 2 DMUL per Gauss
-            # point, against the FMA-lane rate of the measured FP64 DGEMM
+            # form 2 (the default: the FP64 Newton step, 3 DFMA + 2 DMUL per
+            # Gauss point) is bound by FP64 issue, against the FMA-lane rate
+            # of the measured FP64 DGEMM; form 4 computes the same step in
+            # float pairs, bitwise equal, and runs the FP64 step only where
+            # its rounding check fails (about 1e-4 of the Gauss points)
+            form = k.viscosity_form()
+            roof["viscosity_form"] = form
             fp64_tf, fp64_kind = fp64_peak_tflops(local)
             inst = N * 9 * 5
-            rate = inst / (kms * 1e-3) / 1e12
-            roof["limiter"] = "fp64 issue (Delta and viscosity in FP64), see fp64_issue"
-            roof["fp64_issue"] = {"fp64_instructions_per_launch": inst, "achieved_T_lane_inst_per_s": rate,
-                                  "peak_T_fma_lanes_per_s": fp64_tf / 2, "frac": rate / (fp64_tf / 2),
-                                  "peak_kind": fp64_kind}
+            t2 = roof["stress_kernel_ms"]["affine_newton_f64_intcvt"]
+            rate = inst / (t2 * 1e-3) / 1e12
+            issue = {"kernel_ms": t2, "fp64_instructions_per_launch": inst, "achieved_T_lane_inst_per_s": rate,
+                     "peak_T_fma_lanes_per_s": fp64_tf / 2, "frac": rate / (fp64_tf / 2), "peak_kind": fp64_kind}
+            if form == 2:
+                roof["limiter"] = "fp64 issue (Delta and viscosity in FP64), see fp64_issue"
+                roof["fp64_issue"] = issue
+            else:
+                roof["limiter"] = ("memory and FP32 issue: Delta and the viscosity by float pairs checked against "
+                                   "the FP64 form's rounding (bitwise equal); fp64_issue_form2 is the FP64 form")
+                roof["fp64_issue_form2"] = issue
     if prec == 0:
         fp64_tf, fp64_kind = fp64_peak_tflops(local)
         ach = N * flops_per_element_iteration_stress() / (kms * 1e-3) / 1e12
@@ -1162,9 +1174,33 @@ def run_table(args):
                  "cpu_one_thread": None,
                  "gpu_fp64": _gpu_rate(b, DG, 0, 0, NSTEPS, 3),
                  "gpu_mixed": _gpu_rate(b, DG, 0, 1, NSTEPS, 10),
-                 "gpu_learned": "variants.learned_fp32_config5 of the default bench line"})
+                 "gpu_learned": "variants.learned_fp32 of the default bench line"})
     for r in rows:
         print(json.dumps({"table": True, "unit": UNIT, **host, **r}), flush=True)
+
+
+def run_net_forward(args):
+    """The learned warm start's network (6 layers of 3x3 convolutions,
+    64-48-48-48-48-48-32 channels, BF16 on the tensor cores, FP32
+    accumulation) on one nx x nx grid: CUDA-event time per forward pass,
+    its FLOPs (2 x 9 x c_in x c_out per cell and layer) and the fraction of
+    the measured bf16 GEMM rate (burst: the pass is timed alone)."""
+    from nextsimdg_gb300 import surrogate
+    n = args.nx
+    net = surrogate.warm_net(n, n, seed=1)
+    x = np.random.default_rng(0).standard_normal((1, n, n, net.channels[0])).astype(np.float32)
+    net.set_batch(x)
+    net.time_forward(max(args.warmup, 3))
+    ms = net.time_forward(args.steps)
+    ch = net.channels
+    flops = 2.0 * n * n * sum(9 * ch[i] * ch[i + 1] for i in range(len(ch) - 1))
+    p = ROOT / "MEASURED_PEAKS.json"
+    peak, kind = (json.loads(p.read_text()).get("bf16_tflops"), "measured") if p.exists() else (1900.0, "fallback")
+    tf = flops / (ms * 1e-3) / 1e12
+    print(json.dumps({"net_forward": True, "grid": f"{n}x{n}", "channels": list(ch), "ms_per_forward": ms,
+                      "gflop_per_forward": flops / 1e9, "tflops": tf, "bf16_peak_tflops": peak,
+                      "peak_kind": kind, "frac": tf / peak, "steps": args.steps}), flush=True)
+    net.close()
 
 
 def _day_kernel(box, prec: int, env: dict | None = None, scale: float = 1.0, alpha: float = ALPHA):
@@ -1277,6 +1313,8 @@ def main():
     ap.add_argument("--day-error", choices=["bbm", "parts"],
                     help="error checkpoints over a simulated day against the FP64 path (BBM at 512^2, or the "
                          "mixed path's parts at 256^2)")
+    ap.add_argument("--net-forward", action="store_true",
+                    help="time the learned warm start's network forward pass on the --nx grid instead")
     ap.add_argument("--table", action="store_true",
                     help="one line per benchmark configuration: the oracle (all threads, one thread) beside the GPU")
     ap.add_argument("--profile", action="store_true",
@@ -1284,7 +1322,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
-    if args.day_error:
+    if args.net_forward:
+        run_net_forward(args)
+    elif args.day_error:
         run_day_error(args)
     elif args.table:
         run_table(args)

@@ -197,7 +197,10 @@ int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms);
  * also 3 = stress kernel with operators by global loads, 4 = with operator
  * tiles by TMA, and on parallelogram meshes 5, 6, 7 = the coefficient kernel
  * with FP64 viscosity form 0, 1, 2 (see nsdg_selftest_viscosity), 8 = with
- * the float-pair form 3 (nsdg_selftest_viscosity_ff).  *name gets its name. */
+ * the float-pair form 3 (nsdg_selftest_viscosity_ff), 12 = with the checked
+ * form 4 (nsdg_selftest_viscosity_checked); for FP64 mEVP 9, 10, 11 = the
+ * stress kernel with FP64 FMAs, with float pairs, with float pairs staged by
+ * TMA.  *name gets its name. */
 int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean_ms,
     const char** name);
 /* Which mixed-precision mEVP stress kernel the updates use: *kind 0 =
@@ -207,6 +210,13 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
  * in FP64, between the exact operators and those rebuilt from parallelogram
  * coefficients (-1 when not evaluated, e.g. spherical or FP64 handles). */
 int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch);
+/* The evaluation of P/(8 alpha Delta) in the parallelogram stress kernel:
+ * 0 CUDA's rsqrt(double), 1 and 2 one FP64 Newton step from an FP32 seed
+ * (2, the default: conversions on the integer pipe), 3 the same step in
+ * float pairs, 4 form 3 checked against form 2's rounding, with form 2 where
+ * the check fails: bitwise form 2.  NSDG_VISC_FORM=0..4 in the environment
+ * before initialise selects one.  No reference counterpart. */
+int nsdg_kernel_viscosity_form(nsdg_kernel* k, int* form);
 /* Kernel launches issued by one update (for gpu_launches accounting). */
 int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches);
 
@@ -294,6 +304,9 @@ int nsdg_net_get_grads(nsdg_net* net, float* host, size_t n);
 int nsdg_net_set_batch(nsdg_net* net, int batch, const float* input, const float* target,
     const float* mask);
 int nsdg_net_forward(nsdg_net* net, int batch, float* out_host);
+/* The forward pass `reps` times on the network's stream, without copies:
+ * *ms = milliseconds per pass by CUDA events.  No reference counterpart. */
+int nsdg_net_time_forward(nsdg_net* net, int batch, int reps, float* ms);
 /* loss and gradients of the last forward pass (gradients stay on the device) */
 int nsdg_net_loss_backward(nsdg_net* net, int batch, float* loss);
 int nsdg_net_adam_step(nsdg_net* net, float lr, float beta1, float beta2, float eps);
@@ -391,6 +404,10 @@ int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double
  * The stress kernel with this form runs only through
  * nsdg_kernel_time_kernel(kernel_id = 8). */
 int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
+/* The kernels' form 4 (the float-pair form checked against form 2's rounding,
+ * form 2 where the check fails) at each (inv, Pa): out[n], bitwise equal to
+ * form 2 (out[2 n + i] of nsdg_selftest_viscosity).  No reference counterpart. */
+int nsdg_selftest_viscosity_checked(size_t n, const float* inv, const double* Pa, double delta_min, float* out);
 /* The float-pair arithmetic of the FP64 path's stress kernel
  * (kMevpStressPairs) on n value pairs (a[i], x[i]), returned in FP64:
  * out[4 i + 0] = split(a) - a (the representation error of the pair),

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("nsdg_kernel_time_kernel", c_int, [c_void_p, c_int, c_int, POINTER(c_float), POINTER(c_char_p)]),
     ("nsdg_kernel_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_kernel_stress_variant", c_int, [c_void_p, POINTER(c_int), POINTER(c_double)]),
+    ("nsdg_kernel_viscosity_form", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_transport_create", c_int, [c_int, c_size_t, c_size_t, c_void_p, c_void_p,
                                       POINTER(c_void_p), POINTER(c_size_t), c_void_p, c_size_t, c_int,
                                       POINTER(c_void_p)]),
@@ -131,6 +132,7 @@ SIGNATURES = [
     ("nsdg_net_get_grads", c_int, [c_void_p, c_void_p, c_size_t]),
     ("nsdg_net_set_batch", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     ("nsdg_net_forward", c_int, [c_void_p, c_int, c_void_p]),
+    ("nsdg_net_time_forward", c_int, [c_void_p, c_int, c_int, POINTER(c_float)]),
     ("nsdg_net_loss_backward", c_int, [c_void_p, c_int, POINTER(c_float)]),
     ("nsdg_net_adam_step", c_int, [c_void_p, c_float, c_float, c_float, c_float]),
     ("nsdg_net_dataset_reserve", c_int, [c_void_p, c_int]),
@@ -145,6 +147,7 @@ SIGNATURES = [
     ("nsdg_selftest_pairs", c_int, [c_size_t, c_void_p, c_void_p, c_void_p]),
     ("nsdg_selftest_viscosity", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_selftest_viscosity_ff", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
+    ("nsdg_selftest_viscosity_checked", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
     ("nsdg_mesh_dirichlet", c_int, [c_size_t, c_size_t, c_void_p, POINTER(c_size_t), c_void_p, c_size_t]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -703,12 +703,13 @@ int nsdg_kernel::chooseStress32()
 {
     // NSDG_STRESS_KERNEL=global|tma|affine fixes the choice (for profilers,
     // whose serialised launches make the timing below meaningless)
-    // NSDG_VISC_FORM=0..3 fixes the FP64 viscosity form of the
+    // NSDG_VISC_FORM=0..4 fixes the FP64 viscosity form of the
     // parallelogram kernel (0 rsqrt, 1 Newton, 2 Newton with integer
-    // conversions, 3 float pairs)
+    // conversions, 3 float pairs, 4 float pairs checked against form 2 with
+    // form 2 where the check fails: bitwise form 2)
     if (const char* env = std::getenv("NSDG_VISC_FORM")) {
         const int f = std::atoi(env);
-        if (f >= 0 && f <= 3)
+        if (f >= 0 && f <= 4)
             viscMode = f;
     }
     if (const char* env = std::getenv("NSDG_STRESS_KERNEL")) {
@@ -1859,6 +1860,8 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         case 7:
         case 8:
             return k->launchStress32(k->stream, mp, k->derr, 2, kernel_id - 5);
+        case 12:
+            return k->launchStress32(k->stream, mp, k->derr, 2, 4);
         default:
             return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
                 k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a, k->mixed() ? k->cellX32 : nullptr,
@@ -1866,11 +1869,13 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
         }
     };
     const bool fp64Ids = kernel_id >= 9 && kernel_id <= 11;
-    if (kernel_id < 0 || kernel_id > 11 || (kernel_id >= 3 && kernel_id <= 8 && (bbm || !k->mixed()))
-        || (kernel_id >= 5 && kernel_id <= 8 && !k->affCoef) || (fp64Ids && (bbm || k->mixed()))
-        || (kernel_id >= 10 && !k->opsPairs))
+    const bool affIds = (kernel_id >= 5 && kernel_id <= 8) || kernel_id == 12;
+    if (kernel_id < 0 || kernel_id > 12 || (((kernel_id >= 3 && kernel_id <= 8) || kernel_id == 12)
+            && (bbm || !k->mixed()))
+        || (affIds && !k->affCoef) || (fp64Ids && (bbm || k->mixed()))
+        || ((kernel_id == 10 || kernel_id == 11) && !k->opsPairs))
         return k->fail(NSDG_ERR_BAD_ARG,
-            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8: on parallelogram meshes; "
+            "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8, 12: on parallelogram meshes; "
             "9-11: the FP64 mEVP stress kernels, FMA, float pairs and float pairs through TMA)");
     static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
@@ -1883,7 +1888,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                                                                                          : "kMevpStress")))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
             : kernel_id == 2 ? "kTransportStage"
-            : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3];
+            : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3]; // 5-8, 12: the coefficient kernel
     cudaEvent_t ea, eb;
     if (cudaEventCreate(&ea) != cudaSuccess || cudaEventCreate(&eb) != cudaSuccess)
         return k->fail(NSDG_ERR_CUDA, "time_kernel: event create failed");
@@ -1913,6 +1918,14 @@ int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch)
     *kind = k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP ? k->stressKind : -1;
     *mismatch = k->affWorst;
     return k->ok();
+}
+
+int nsdg_kernel_viscosity_form(nsdg_kernel* k, int* form)
+{
+    if (!k || !form)
+        return NSDG_ERR_BAD_ARG;
+    *form = k->viscMode;
+    return NSDG_OK;
 }
 
 int nsdg_kernel_launches_per_update(nsdg_kernel* k, int* launches)
@@ -2669,9 +2682,11 @@ int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts
 }
 
 // the viscosity self-tests: forms = 3 (modes 0, 1, 2) or 1 (mode 3)
+// kind 0: forms 0, 1, 2 (out[3 n]); 1: form 3; 2: form 4 (out[n])
 static int viscositySelfTest(size_t n, const float* inv, const double* Pa, double delta_min, float* out,
-    int forms)
+    int kind)
 {
+    const int forms = kind == 0 ? 3 : 1;
     if (!inv || !Pa || !out || n == 0 || n > (size_t(1) << 26) || !(delta_min > 0.0))
         return NSDG_ERR_BAD_ARG;
     std::string m;
@@ -2689,8 +2704,9 @@ static int viscositySelfTest(size_t n, const float* inv, const double* Pa, doubl
     if (e == cudaSuccess) e = cudaMemcpyAsync(dInv, inv, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dPa, Pa, n * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = forms == 1 ? launchViscositySelfTestFF(s, n, dInv, dPa, delta_min, dOut)
-                       : launchViscositySelfTest(s, n, dInv, dPa, delta_min, dOut);
+        e = kind == 1 ? launchViscositySelfTestFF(s, n, dInv, dPa, delta_min, dOut)
+            : kind == 2   ? launchViscositySelfTestChecked(s, n, dInv, dPa, delta_min, dOut)
+                          : launchViscositySelfTest(s, n, dInv, dPa, delta_min, dOut);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dOut, nOut * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     for (void* p : { static_cast<void*>(dInv), static_cast<void*>(dPa), static_cast<void*>(dOut) })
@@ -2703,12 +2719,17 @@ static int viscositySelfTest(size_t n, const float* inv, const double* Pa, doubl
 
 int nsdg_selftest_viscosity(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
 {
-    return viscositySelfTest(n, inv, Pa, delta_min, out, 3);
+    return viscositySelfTest(n, inv, Pa, delta_min, out, 0);
 }
 
 int nsdg_selftest_viscosity_ff(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
 {
     return viscositySelfTest(n, inv, Pa, delta_min, out, 1);
+}
+
+int nsdg_selftest_viscosity_checked(size_t n, const float* inv, const double* Pa, double delta_min, float* out)
+{
+    return viscositySelfTest(n, inv, Pa, delta_min, out, 2);
 }
 
 int nsdg_selftest_pairs(size_t n, const double* a, const double* x, double* out)

@@ -1669,15 +1669,34 @@ __device__ __forceinline__ float narrowPos(double d)
 // 1e-12); VM 2 converts between float and double on the integer pipe (y0/2
 // by the exponent bias).  Five FP64 instructions per Gauss point in VM 2.
 // VM 3: the same Newton step from the same seed with float pairs on the FP32
-// pipe (nsdg_visc_ff.hpp: one FP64 subtraction per Gauss point, and one FMA
-// per thread for the low part of DeltaMin^2, which the unrolled Gauss-point
-// loop shares).
+// pipe (nsdg_visc_ff.hpp: one FP64 subtraction per Gauss point; dmin2lo is
+// the low part of DeltaMin^2).  VM 4: VM 3's float pairs with the check of
+// nsdg_ff::viscFloatFloatChecked, and VM 2's FP64 operations from the same
+// seed wherever the check cannot prove the pair's rounding equal to theirs
+// (near a float rounding boundary: about 1e-4 of the Gauss points): bitwise
+// VM 2's result with one FP64 subtraction per Gauss point instead of five
+// FP64 instructions (measured slower than VM 2 on GB300: the float-pair
+// arithmetic and the check cost more issue than the FP64 pipe they free).
+__device__ __forceinline__ float viscNewton64(float inv, double Pa, double dmin, float y0)
+{
+    const double t = fma(dmin, dmin, widenNonneg(inv));
+    const double yd = widenPos(y0);
+    const double h = t * yd;
+    const double e2 = fma(-h, widenHalfPos(y0), 0.5); // (1 - t y0^2) / 2
+    const double z = Pa * yd;
+    return narrowPos(fma(z, e2, z));
+}
+
 template <int VM>
-__device__ __forceinline__ float viscosity8(float inv, double Pa, double dmin, float dmin2f)
+__device__ __forceinline__ float viscosity8(float inv, double Pa, double dmin, float dmin2f, float dmin2lo)
 {
     if constexpr (VM == 3) {
-        const float d2l = nsdg_ff::narrowAny(fma(dmin, dmin, -nsdg_ff::widenPos(dmin2f)));
-        return nsdg_ff::viscFloatFloat(inv, Pa, dmin2f, d2l, rsqrtf(inv + dmin2f));
+        return nsdg_ff::viscFloatFloat(inv, Pa, dmin2f, dmin2lo, rsqrtf(inv + dmin2f));
+    } else if constexpr (VM == 4) {
+        const float y0 = rsqrtf(inv + dmin2f);
+        bool exact;
+        const float z = nsdg_ff::viscFloatFloatChecked(inv, Pa, dmin2f, dmin2lo, y0, exact);
+        return exact ? z : viscNewton64(inv, Pa, dmin, y0);
     } else {
         const double td = VM == 2 ? widenNonneg(inv) : static_cast<double>(inv);
         const double t = fma(dmin, dmin, td);
@@ -1698,7 +1717,7 @@ __device__ __forceinline__ float viscosity8(float inv, double Pa, double dmin, f
 
 template <int PART, int VM>
 __device__ __forceinline__ void affineStrain(const float (&ul)[9], const float (&vl)[9], const float (&c)[5],
-    const double (&Pa)[3], const float (&hP)[3], double dmin, float dmin2f,
+    const double (&Pa)[3], const float (&hP)[3], double dmin, float dmin2f, float dmin2lo,
     float (*fs)[9][kAffElems], int le)
 {
 #pragma unroll
@@ -1720,7 +1739,7 @@ __device__ __forceinline__ void affineStrain(const float (&ul)[9], const float (
         const float eyu = c[4] * fmaf(c[2], ux, c[3] * ue); // G_y u
         const float sxy = exv + eyu;
         const float inv = 1.25f * (ex * ex + ey * ey) + 1.50f * ex * ey + 0.25f * sxy * sxy;
-        const float z8 = viscosity8<VM>(inv, Pa[qq], dmin, dmin2f);
+        const float z8 = viscosity8<VM>(inv, Pa[qq], dmin, dmin2f, dmin2lo);
         const float f11 = fmaf(z8, fmaf(5.f, ex, 3.f * ey), -hP[qq]);
         const float f12 = z8 * sxy;
         const float f22 = fmaf(z8, fmaf(5.f, ey, 3.f * ex), -hP[qq]);
@@ -1809,11 +1828,11 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
             vl[j] = v[nd];
         }
         const double dmin = p.DeltaMin;
-        const float dmin2f = p.dmin2f;
+        const float dmin2f = p.dmin2f, dmin2lo = p.dmin2lo;
         switch (part) {
-        case 0: affineStrain<0, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
-        case 1: affineStrain<1, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
-        default: affineStrain<2, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, fs, le); break;
+        case 0: affineStrain<0, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, dmin2lo, fs, le); break;
+        case 1: affineStrain<1, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, dmin2lo, fs, le); break;
+        default: affineStrain<2, VM>(ul, vl, c, Pa, hP, dmin, dmin2f, dmin2lo, fs, le); break;
         }
     }
     __syncthreads();
@@ -1828,7 +1847,7 @@ __device__ __forceinline__ void affineBlock(int nx, size_t N, const uint8_t* __r
 }
 
 template <int VM>
-__global__ void __launch_bounds__(kAffElems * kStressParts) kMevpStress32Affine(DevMesh m,
+__global__ void __launch_bounds__(kAffElems * kStressParts, 12) kMevpStress32Affine(DevMesh m,
     const float* __restrict__ coef, size_t ld, const float* __restrict__ u, const float* __restrict__ v,
     const double* __restrict__ Pg, float* __restrict__ tdiv, MevpParams p)
 {
@@ -1845,9 +1864,9 @@ __global__ void kViscositySelfTest(size_t n, const float* __restrict__ inv, cons
     if (i >= n)
         return;
     const float dmin2f = static_cast<float>(dmin * dmin);
-    out[i] = viscosity8<0>(inv[i], Pa[i], dmin, dmin2f);
-    out[n + i] = viscosity8<1>(inv[i], Pa[i], dmin, dmin2f);
-    out[2 * n + i] = viscosity8<2>(inv[i], Pa[i], dmin, dmin2f);
+    out[i] = viscosity8<0>(inv[i], Pa[i], dmin, dmin2f, 0.f);
+    out[n + i] = viscosity8<1>(inv[i], Pa[i], dmin, dmin2f, 0.f);
+    out[2 * n + i] = viscosity8<2>(inv[i], Pa[i], dmin, dmin2f, 0.f);
 }
 
 // The float-float form (VM 3) at each (inv, Pa): out[n].
@@ -1857,7 +1876,19 @@ __global__ void kViscositySelfTestFF(size_t n, const float* __restrict__ inv, co
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
         return;
-    out[i] = viscosity8<3>(inv[i], Pa[i], dmin, static_cast<float>(dmin * dmin));
+    const float d2h = static_cast<float>(dmin * dmin);
+    out[i] = viscosity8<3>(inv[i], Pa[i], dmin, d2h, nsdg_ff::narrowAny(fma(dmin, dmin, -nsdg_ff::widenPos(d2h))));
+}
+
+// The checked float-pair form (VM 4) at each (inv, Pa): out[n]; bitwise VM 2.
+__global__ void kViscositySelfTestChecked(size_t n, const float* __restrict__ inv, const double* __restrict__ Pa,
+    double dmin, float* __restrict__ out)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const float d2h = static_cast<float>(dmin * dmin);
+    out[i] = viscosity8<4>(inv[i], Pa[i], dmin, d2h, nsdg_ff::narrowAny(fma(dmin, dmin, -nsdg_ff::widenPos(d2h))));
 }
 
 // Body of the mixed-precision node kernel for CG2 node i.
@@ -2753,6 +2784,7 @@ cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const flo
     case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<0>, m, coef, ld, u, v, Pg, tdiv, p);
     case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<1>, m, coef, ld, u, v, Pg, tdiv, p);
     case 3: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<3>, m, coef, ld, u, v, Pg, tdiv, p);
+    case 4: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<4>, m, coef, ld, u, v, Pg, tdiv, p);
     default: return cudaLaunchKernelEx(&cfg, kMevpStress32Affine<2>, m, coef, ld, u, v, Pg, tdiv, p);
     }
 }
@@ -2768,6 +2800,13 @@ cudaError_t launchViscositySelfTestFF(cudaStream_t s, size_t n, const float* inv
     float* out)
 {
     kViscositySelfTestFF<<<blocksFor(n), kBlock, 0, s>>>(n, inv, Pa, dmin, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchViscositySelfTestChecked(cudaStream_t s, size_t n, const float* inv, const double* Pa,
+    double dmin, float* out)
+{
+    kViscositySelfTestChecked<<<blocksFor(n), kBlock, 0, s>>>(n, inv, Pa, dmin, out);
     return cudaGetLastError();
 }
 
@@ -2848,6 +2887,7 @@ cudaError_t launchMevpStress32AffineBatched(cudaStream_t s, const EnsembleMember
     switch (viscosityMode) {
     case 0: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<0>, members, blockMember, p);
     case 1: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<1>, members, blockMember, p);
+    case 4: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<4>, members, blockMember, p);
     default: return cudaLaunchKernelEx(&cfg, kMevpStress32AffineBatched<2>, members, blockMember, p);
     }
 }
@@ -2862,7 +2902,8 @@ cudaError_t launchEnsembleSubcyclePersistent(cudaStream_t s, const EnsembleMembe
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto kern = viscosityMode == 0 ? kEnsembleSubcyclePersistent<0>
-        : viscosityMode == 1 ? kEnsembleSubcyclePersistent<1> : kEnsembleSubcyclePersistent<2>;
+        : viscosityMode == 1 ? kEnsembleSubcyclePersistent<1>
+        : viscosityMode == 4 ? kEnsembleSubcyclePersistent<4> : kEnsembleSubcyclePersistent<2>;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kAffElems * kStressParts, 0);
     if (e != cudaSuccess)
         return e;

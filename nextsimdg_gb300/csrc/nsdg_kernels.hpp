@@ -5,6 +5,7 @@
 // cudaError_t of the launch.
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cuda.h>
@@ -160,7 +161,7 @@ inline MevpParams withDerived(MevpParams p)
     p.keepd = 1.0 - 1.0 / p.alpha;
     p.keep = static_cast<float>(p.keepd);
     p.dmin2f = static_cast<float>(p.DeltaMin * p.DeltaMin);
-    p.dmin2lo = static_cast<float>(p.DeltaMin * p.DeltaMin - static_cast<double>(p.dmin2f));
+    p.dmin2lo = static_cast<float>(std::fma(p.DeltaMin, p.DeltaMin, -static_cast<double>(p.dmin2f)));
     p.F_oceanf = static_cast<float>(p.F_ocean);
     p.betaf = static_cast<float>(p.beta);
     p.onePlusBetaf = static_cast<float>(1.0 + p.beta);
@@ -288,9 +289,9 @@ cudaError_t launchMevpPrepNodes32(cudaStream_t s, const DevMesh& m, const MevpNo
 // per device (they depend only on the basis), and 5 coefficients per element
 // ([5][ld]).  viscosityMode selects the FP64 evaluation of P/(8 alpha Delta):
 // 0 CUDA's rsqrt(double), 1 a Newton step from an FP32 seed, 2 the same with
-// float/double conversions on the integer pipe (the default); 3 the same
-// Newton step with float pairs on the FP32 pipe (nsdg_visc_ff.hpp; reached
-// only through nsdg_kernel_time_kernel).
+// float/double conversions on the integer pipe; 3 the same Newton step with
+// float pairs on the FP32 pipe (nsdg_visc_ff.hpp); 4 form 3 checked against
+// form 2's rounding, with form 2 where the check fails (bitwise form 2).
 cudaError_t uploadAffineReference(const double ref[4][81]);
 cudaError_t launchMevpStress32Affine(cudaStream_t s, const DevMesh& m, const float* coef, size_t ld, const float* u,
     const float* v, const double* Pg, float* tdiv, const MevpParams& p, int viscosityMode);
@@ -300,6 +301,9 @@ cudaError_t launchViscositySelfTest(cudaStream_t s, size_t n, const float* inv, 
 // out[i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode 3.
 cudaError_t launchViscositySelfTestFF(cudaStream_t s, size_t n, const float* inv, const double* Pa, double dmin,
     float* out);
+// out[i] = P/(8 alpha Delta) of (inv[i], Pa[i]) by viscosity mode 4.
+cudaError_t launchViscositySelfTestChecked(cudaStream_t s, size_t n, const float* inv, const double* Pa,
+    double dmin, float* out);
 cudaError_t launchMevpStress32(cudaStream_t s, const DevMesh& m, const DevOps32& o, const float* u,
     const float* v, const double* Pg, const float* hP, float* tdiv, const MevpParams& p);
 cudaError_t launchMevpMomentum32(cudaStream_t s, const DevMesh& m,

@@ -1269,6 +1269,38 @@ int nsdg_net_forward(nsdg_net* h, int batch, float* out_host)
     return NSDG_OK;
 }
 
+int nsdg_net_time_forward(nsdg_net* h, int batch, int reps, float* ms)
+{
+    if (!h || batch < 1 || batch > h->impl->maxB || reps < 1 || !ms)
+        return NSDG_ERR_BAD_ARG;
+    NetImpl* n = h->impl;
+    cudaStream_t s = netStream(n);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r)
+        e = netForward(n, s, batch);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess)
+        e = cudaEventElapsedTime(ms, e0, e1);
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        h->err = cudaGetErrorString(e);
+        return NSDG_ERR_CUDA;
+    }
+    *ms /= float(reps);
+    return NSDG_OK;
+}
+
 int nsdg_net_loss_backward(nsdg_net* h, int batch, float* loss)
 {
     if (!h || batch < 1 || batch > h->impl->maxB)

@@ -13,6 +13,12 @@
 //                 double-float arithmetic) on the FP32 pipe and one FP64
 //                 subtraction for the low part of Pa.
 //
+//   viscFloatFloatChecked (host and device) the float-float form with the
+//                 last sum kept as an exact pair, and a flag telling whether
+//                 the result is provably the FP64 form's: the device kernels'
+//                 form 4 uses it and evaluates the FP64 form only where the
+//                 flag is false, so their results are bitwise form 2's.
+//
 // Both approximate the same y1 from the same seed, so they round to the same
 // float unless Pa y1 lies within about 2^-44 of a rounding midpoint.  Every
 // FP32 operation is an explicit IEEE round-to-nearest operation (no
@@ -196,6 +202,69 @@ NSDG_FF_HD float viscFloatFloat(float inv, double Pa, float d2h, float d2l, floa
     // results below the smallest normal float are 0, as the FP64 form's
     // conversion to float makes them
     return z >= 0x1p-126f ? z : 0.f;
+}
+
+// The float-float form with a check that its result is bitwise the FP64
+// form's (viscNewton64 with the same seed).  Error bounds, relative to z, for
+// a seed with |r| = |1 - t y0^2| <= 2^-19 (rsqrtf's seed: about 2^-21):
+//   the pair m + s (before its last rounding) is within 2^-41 of the exact
+//   Newton value Pa y0 (1 + r / 2): r carries three roundings of at most
+//   2^-43 (its terms are below 2^-19) and the dropped tl pe (2^-48), which
+//   reach y1 halved (2^-42.4); y0 r / 2 one rounding of 2^-44; s one of
+//   2^-43.8; the dropped pl yl at most 2^-44; the pair splits of Pa and
+//   DeltaMin^2 at most 2^-48 each (for Pa >= 2^-76: below, pl could be
+//   flushed to 0);
+//   the FP64 form's z8 is within 2^-51 of the same value (four FP64
+//   roundings; the seed's widening is exact).
+// Hence if m + s = z + err (exact, Fast2Sum) lies farther than 2^-39 |z|
+// inside the interval of reals that round to z, z8 rounds to z as well:
+// `exact` is true and z is the FP64 form's result.  Otherwise `exact` is
+// false and the caller evaluates the FP64 form: z within 2^-39 of a
+// rounding boundary (about 2^-15 of random cases), z a power of two, z below
+// 2^-80 or not finite, Pa below 2^-76 and not zero, or a seed outside the
+// bound.  Pa = 0 gives +0, as the FP64 form does.
+NSDG_FF_HD float viscFloatFloatChecked(float inv, double Pa, float d2h, float d2l, float y0, bool& exact)
+{
+    exact = false;
+    const uint64_t pb = bitsOf(Pa);
+    if (pb == 0) {
+        exact = true;
+        return 0.f;
+    }
+    // Pa >= 2^-76: then the low part pl, flushed to 0 below 2^-126, loses at
+    // most 2^-50 of Pa
+    if (pb < (947ull << 52) || pb >= (1ull << 63))
+        return 0.f;
+    const float th = add(inv, d2h);
+    const float bv = sub(th, inv);
+    const float av = sub(th, bv);
+    const float tl = add(add(sub(inv, av), sub(d2h, bv)), d2l);
+    const float p = mul(y0, y0);
+    const float pe = fma(y0, y0, -p);
+    const float q = mul(th, p);
+    const float qe = fma(th, p, -q);
+    const float r = fma(-tl, p, fma(-th, pe, sub(sub(1.f, q), qe)));
+    if (!(r <= 0x1p-19f && r >= -0x1p-19f))
+        return 0.f;
+    const float yl = mul(mul(y0, r), 0.5f);
+    const float ph = narrowPos(Pa);
+    const float pl = narrowAny(Pa - widenNonneg(ph));
+    const float m = mul(ph, y0);
+    const float me = fma(ph, y0, -m);
+    const float s = fma(ph, yl, fma(pl, y0, me));
+    const float z = add(m, s);
+    const float err = sub(s, sub(z, m)); // m + s = z + err exactly: |s| < 2^-18 |m|
+    const uint32_t zb = bitsOf(z);
+    const uint32_t ex = zb & 0x7f800000u;
+    if (ex < (47u << 23) || ex == 0x7f800000u || (zb & 0x007fffffu) == 0u)
+        return z;
+    // z in (2^e, 2^(e+1)): the reals that round to z lie within 2^(e-24) of
+    // it; the margin 2^(e-38) is at least 2^-39 |z|
+    const float half = floatOf(ex - (24u << 23));
+    const float margin = floatOf(ex - (38u << 23));
+    const float aerr = err < 0.f ? -err : err;
+    exact = aerr < sub(half, margin);
+    return z;
 }
 
 // DeltaMin^2 as the pair (d2h, d2l) viscFloatFloat takes: d2h the float the

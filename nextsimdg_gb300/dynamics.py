@@ -134,6 +134,22 @@ def selftest_viscosity_ff(inv, pa, delta_min: float) -> np.ndarray:
     return out
 
 
+def selftest_viscosity_checked(inv, pa, delta_min: float) -> np.ndarray:
+    """The same quantity by the kernels' form 4 (float pairs checked against
+    form 2's rounding, form 2 where the check fails), shape (n,) float32;
+    bitwise form 2 (see nsdg_selftest_viscosity_checked)."""
+    lib = _lib.load()
+    inv = np.ascontiguousarray(inv, dtype=np.float32)
+    pa = np.ascontiguousarray(pa, dtype=np.float64)
+    if inv.shape != pa.shape or inv.ndim != 1:
+        raise ValueError("inv and pa must be 1-D arrays of the same length")
+    out = np.empty(inv.size, dtype=np.float32)
+    st = lib.nsdg_selftest_viscosity_checked(inv.size, _ptr(inv), _ptr(pa), float(delta_min), _ptr(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "selftest_viscosity_checked failed")
+    return out
+
+
 class _KernelBase:
     rheology = _lib.RHEOLOGY_MEVP
 
@@ -285,6 +301,14 @@ class _KernelBase:
         kind, mism = c_int(), c_double()
         self._check(self._l.nsdg_kernel_stress_variant(self._h, byref(kind), byref(mism)))
         return (self.STRESS_KERNELS[kind.value] if kind.value >= 0 else None), mism.value
+
+    def viscosity_form(self) -> int:
+        """The parallelogram stress kernel's evaluation of P/(8 alpha Delta)
+        (nsdg_kernel_viscosity_form: 2, the default, the FP64 Newton step;
+        4 float pairs checked against it, bitwise equal)."""
+        f = c_int()
+        self._check(self._l.nsdg_kernel_viscosity_form(self._h, byref(f)))
+        return f.value
 
     # -- learned warm start (mEVP, mixed precision) ------------------------------
     def warm_sample(self, tst, dt, k_iters: int, net, slot: int) -> float:

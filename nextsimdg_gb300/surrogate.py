@@ -86,6 +86,13 @@ class Net:
         self._check(self._l.nsdg_net_forward(self._h, self._B, out.ctypes.data_as(c_void_p)))
         return out
 
+    def time_forward(self, reps: int = 10) -> float:
+        """Milliseconds per forward pass of the batch set last (CUDA events,
+        no copies)."""
+        ms = c_float()
+        self._check(self._l.nsdg_net_time_forward(self._h, self._B, int(reps), byref(ms)))
+        return ms.value
+
     def loss_backward(self) -> float:
         loss = c_float()
         self._check(self._l.nsdg_net_loss_backward(self._h, self._B, byref(loss)))

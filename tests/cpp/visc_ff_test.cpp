@@ -3,7 +3,9 @@
 // against P / sqrt(inv + DeltaMin^2) correctly rounded to float (evaluated in
 // long double), over seeded samples of the strain invariant, the pressure
 // term and DeltaMin, and seeds up to 3 ulps away from the nearest float of
-// 1/sqrt(t) (the device seed, rsqrtf, is within 2 ulps).
+// 1/sqrt(t) (the device seed, rsqrtf, is within 2 ulps); and the checked
+// float-float form: wherever it reports its result exact, bitwise the FP64
+// form's.
 // Build with -ffp-contract=off.  Prints "key value" lines.
 #include "nsdg_visc_ff.hpp"
 
@@ -39,6 +41,7 @@ int main()
     const double dmins[] = { 2e-9, 1e-10, 5e-9, 3.3e-8 };
     const int perSet = 250000;
     uint64_t samples = 0, mismatchAB = 0, nonfinite = 0, seedsNormal = 0;
+    uint64_t checkedWrong = 0, checkedFallback = 0;
     uint32_t maxAB = 0, maxARef = 0, maxBRef = 0;
     for (double dmin : dmins) {
         float d2h, d2l;
@@ -80,6 +83,13 @@ int main()
                 const float a = nsdg_ff::viscNewton64(inv, Pa, dmin, y0);
                 const float b = nsdg_ff::viscFloatFloat(inv, Pa, d2h, d2l, y0);
                 ++samples;
+                // the checked form: where it says exact, bitwise the FP64 form
+                bool exact = false;
+                const float c = nsdg_ff::viscFloatFloatChecked(inv, Pa, d2h, d2l, y0, exact);
+                if (!exact)
+                    ++checkedFallback;
+                else if (nsdg_ff::bitsOf(c) != nsdg_ff::bitsOf(a))
+                    ++checkedWrong;
                 if (!std::isfinite(a) || !std::isfinite(b)) {
                     ++nonfinite;
                     continue;
@@ -101,6 +111,45 @@ int main()
             }
         }
     }
+    // Adversarial cases for the checked form: Pa chosen so that the exact
+    // Newton value lies at a float rounding midpoint, or 2^-60 to 2^-36 of it
+    // away on either side (the check's margin is 2^-39).
+    uint64_t advSamples = 0, advWrong = 0, advFallback = 0, physSamples = 0, physFallback = 0;
+    for (int i = 0; i < 200000; ++i) {
+        const double dmin = dmins[i % 4];
+        float d2h, d2l;
+        nsdg_ff::splitSquare(dmin, d2h, d2l);
+        const long double d2 = static_cast<long double>(dmin) * static_cast<long double>(dmin);
+        const float inv = uniform() < 0.2 ? 0.f : static_cast<float>(logUniform(1e-22, 1e-4));
+        const float th = inv + d2h;
+        const float y0 = static_cast<float>(1.0 / std::sqrt(static_cast<double>(th)));
+        const long double t = static_cast<long double>(inv) + d2;
+        const long double y1 = static_cast<long double>(y0) * (1.5L - 0.5L * t * y0 * y0);
+        // a float z0 in [1e-3, 1e3] and the midpoint above it
+        const float z0 = static_cast<float>(logUniform(1e-3, 1e3));
+        const long double mid = (static_cast<long double>(z0)
+            + static_cast<long double>(std::nextafter(z0, 2.f * z0))) / 2.0L;
+        for (int j = -7; j <= 7; ++j) {
+            const long double off = j == 0 ? 0.0L : (j > 0 ? 1.0L : -1.0L) * std::ldexp(1.0L, -60 + 4 * (j < 0 ? -j : j));
+            const double Pa = static_cast<double>(mid * (1.0L + off) / y1);
+            bool exact = false;
+            const float c = nsdg_ff::viscFloatFloatChecked(inv, Pa, d2h, d2l, y0, exact);
+            const float a = nsdg_ff::viscNewton64(inv, Pa, dmin, y0);
+            ++advSamples;
+            if (!exact)
+                ++advFallback;
+            else if (nsdg_ff::bitsOf(c) != nsdg_ff::bitsOf(a))
+                ++advWrong;
+        }
+        // the physical range: pressure terms 1e-3 to 1e4, random strain
+        const double Pp = logUniform(1e-3, 1e4);
+        bool ex2 = false;
+        nsdg_ff::viscFloatFloatChecked(inv, Pp, d2h, d2l, y0, ex2);
+        ++physSamples;
+        if (!ex2)
+            ++physFallback;
+    }
+
     std::printf("samples %" PRIu64 "\n", samples);
     std::printf("seeds %" PRIu64 "\n", seedsNormal);
     std::printf("mismatch_ab %" PRIu64 "\n", mismatchAB);
@@ -108,5 +157,12 @@ int main()
     std::printf("max_ulp_fp64_ref %u\n", maxARef);
     std::printf("max_ulp_ff_ref %u\n", maxBRef);
     std::printf("nonfinite %" PRIu64 "\n", nonfinite);
+    std::printf("checked_wrong %" PRIu64 "\n", checkedWrong);
+    std::printf("checked_fallback %" PRIu64 "\n", checkedFallback);
+    std::printf("adv_samples %" PRIu64 "\n", advSamples);
+    std::printf("adv_wrong %" PRIu64 "\n", advWrong);
+    std::printf("adv_fallback %" PRIu64 "\n", advFallback);
+    std::printf("phys_samples %" PRIu64 "\n", physSamples);
+    std::printf("phys_fallback %" PRIu64 "\n", physFallback);
     return 0;
 }

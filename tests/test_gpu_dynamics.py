@@ -352,6 +352,53 @@ def test_fp64_viscosity_forms_agree(gpu):
     assert np.all(np.isfinite(out))
 
 
+def test_checked_float_pair_viscosity_is_form_2(gpu):
+    """Form 4 (float pairs checked against form 2's rounding, form 2 where
+    the check fails) is bitwise form 2 on the device: random strain
+    invariants and pressure terms, and pressure terms aimed at float
+    rounding midpoints of the result (where form 3 alone may differ)."""
+    from nextsimdg_gb300.dynamics import selftest_viscosity, selftest_viscosity_checked
+    rng = np.random.default_rng(11)
+    n = 1 << 18
+    inv = np.concatenate([[0.0, 1e-45, 1e-40, 1.1754942e-38, 4e-18],
+                          10.0 ** rng.uniform(-36, -4, n - 5)]).astype(np.float32)
+    pa = np.concatenate([[0.0, 1e-300, 1e-31, 12.5, 1e3], 10.0 ** rng.uniform(-3, 4, n - 5)])
+    # aimed: Pa = midpoint / (1 / sqrt(inv + DeltaMin^2)) in extended
+    # precision, so that the result lies within about 2^-43 of a midpoint
+    m = n // 2
+    dmin = 2e-9
+    t = inv[:m].astype(np.longdouble) + np.longdouble(dmin) * np.longdouble(dmin)
+    z0 = (10.0 ** rng.uniform(-2, 3, m)).astype(np.float32)
+    mid = (z0.astype(np.longdouble) + np.nextafter(z0, np.float32(np.inf)).astype(np.longdouble)) / 2
+    pa[:m] = (mid * np.sqrt(t)).astype(np.float64)
+    f2 = selftest_viscosity(inv, pa, dmin)[2]
+    f4 = selftest_viscosity_checked(inv, pa, dmin)
+    assert np.array_equal(f4.view(np.uint32), f2.view(np.uint32)), int(np.sum(f4 != f2))
+
+
+def test_checked_float_pair_viscosity_steps_like_form_2(gpu, monkeypatch):
+    """The parallelogram stress kernel with form 4 (NSDG_VISC_FORM=4) and
+    with form 2: the same model steps, bitwise."""
+    from nextsimdg_gb300.boxtest import step_forcing
+    box = BoxTest(96)
+    out = {}
+    for form in ("2", "4"):
+        monkeypatch.setenv("NSDG_VISC_FORM", form)
+        k = MEVPDynamicsKernel(dg_comp=6, alpha=300.0, beta=300.0, n_steps=100, precision=1)
+        k.initialise(box.coords(), False, box.mask())
+        for name, arr in box.initial_fields().items():
+            k.setData(name, arr)
+        for s in range(4):
+            step_forcing(k, box, s)
+            k.update(s * box.dt, box.dt)
+        out[form] = {f: k.getDG0Data(f) for f in ("u", "v", "hice", "cice", "uiostress")}
+        assert k.stress_variant()[0] == "affine"
+        k.close()
+    for f in out["2"]:
+        assert np.array_equal(out["2"][f], out["4"][f]), f
+    assert np.abs(out["4"]["u"]).max() > 1e-3
+
+
 @pytest.mark.parametrize("n,steps", [(14, 3), (48, 3)])
 def test_bbm_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
     """BBM in the mixed mode (FP32 stress/damage arithmetic and transport

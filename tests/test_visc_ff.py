@@ -8,7 +8,10 @@ cases (strain invariants 0 to 1e-4 s^-2, subnormal ones, pressure terms from
 FP64 subnormals to 1e6, four DeltaMin, seeds up to 3 ulps off) the two agree
 except near rounding midpoints (bar: 1e-5 of the cases, measured 2e-6) and
 never by more than one FP32 ulp, and both are within one ulp of
-P / sqrt(inv + DeltaMin^2) correctly rounded.  On the GPU: the device build
+P / sqrt(inv + DeltaMin^2) correctly rounded.  The checked float-float form
+(the kernels' form 4) reports where its result is provably the FP64 form's:
+there it is bitwise equal, over the random cases and over 3 M cases aimed at
+float rounding midpoints.  On the GPU: the device build
 against form 2, and the stress kernel with form 3 (time_kernel id 8)."""
 import shutil
 import subprocess
@@ -32,6 +35,14 @@ def test_float_float_viscosity_matches_the_fp64_form(tmp_path):
     assert r["max_ulp_ab"] <= 1
     assert r["mismatch_ab"] <= 1e-5 * r["samples"], r
     assert r["max_ulp_fp64_ref"] <= 1 and r["max_ulp_ff_ref"] <= 1, r
+    # the checked form (the kernels' form 4): where it reports exact, bitwise
+    # the FP64 form, including on values aimed at rounding midpoints; every
+    # value within 2^-40 of a midpoint (11 of the 15 offsets) goes to the
+    # FP64 form; on physical pressure terms it falls back rarely
+    assert r["checked_wrong"] == 0, r
+    assert r["adv_wrong"] == 0, r
+    assert r["adv_fallback"] >= 11 * r["adv_samples"] // 15, r
+    assert r["phys_fallback"] <= 5e-4 * r["phys_samples"], r
 
 
 @pytest.mark.gpu
