@@ -2706,6 +2706,30 @@ cudaError_t encodeTiled2d(CUtensorMap* map, CUtensorMapDataType type, const void
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+cudaError_t encodeTiledNd(CUtensorMap* map, CUtensorMapDataType type, const void* base, int rank,
+    const uint64_t* dims, const uint64_t* strideBytes, const uint32_t* box)
+{
+    cudaError_t e;
+    const EncodeTiledFn encode = encodeTiledFn(e);
+    if (!encode)
+        return e;
+    if (rank < 1 || rank > 5)
+        return cudaErrorInvalidValue;
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], es[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (i + 1 < rank)
+            st[i] = strideBytes[i];
+    }
+    const CUresult r = encode(map, type, static_cast<cuuint32_t>(rank), const_cast<void*>(base), d, st, b, es,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out)
 {
     cudaError_t ee;

@@ -253,6 +253,12 @@ cudaError_t makeStressMaps(const DevOps32& o, StressMaps* out);
 // (a multiple of 16), boxes of boxInner x boxOuter, no swizzle, zero fill.
 cudaError_t encodeTiled2d(CUtensorMap* map, CUtensorMapDataType type, const void* base, uint64_t inner,
     uint64_t outer, uint64_t rowBytes, uint32_t boxInner, uint32_t boxOuter);
+// A tensor map of rank 1..5 without swizzle, out-of-bounds elements read as
+// zero: dims[0] innermost, strideBytes[i] the byte stride of dimension i + 1
+// (multiples of 16), box the tile copied per load (box[0] * element size a
+// multiple of 16 bytes).
+cudaError_t encodeTiledNd(CUtensorMap* map, CUtensorMapDataType type, const void* base, int rank,
+    const uint64_t* dims, const uint64_t* strideBytes, const uint32_t* box);
 // One block waits (bounded) on an mbarrier nothing completes; *timedOut = 1
 // when the wait ran out as it must.
 cudaError_t launchBoundedWaitSelfTest(cudaStream_t s, double limitSeconds, int* timedOut);

@@ -17,11 +17,15 @@
 // chunk and tap) and the chunks are added in a fixed order, so training is
 // deterministic.
 #include "nsdg.h"
+#include "nsdg_kernels.hpp"
 #include "nsdg_surrogate.hpp"
+#include "nsdg_tma.cuh"
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 #include <string>
@@ -134,6 +138,277 @@ __global__ void __launch_bounds__(kThreads) kConv3x3(int B, int H, int W, const 
                 }
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same convolutions on the fifth-generation tensor cores (tcgen05).
+//
+// One tile is 128 consecutive pixels of one image row (the MMA's M = 128, one
+// pixel per TMEM lane); N = output channels; K = 9 taps x CS channels, in
+// steps of 16 (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 in TMEM).
+// Operands are K-major in shared memory without swizzle, in 8 x 16-byte core
+// matrices: pixels (A rows) and output channels (B rows) 16 bytes apart, so
+// 8-row groups are 128 bytes apart (SBO) and one 8-channel group of all rows
+// is one contiguous block (LBO = the block's size).
+//   A: per tile, TMA loads the three input rows y-1, y, y+1 at pixels
+//      x0-1 ... x0+134 (136 pixels, 2176 bytes per 8-channel group; pixels
+//      outside the image read as zero), for every 8-channel group.  Tap
+//      (dy, dx) is then the same block with its descriptor's start address
+//      moved by dx pixels (16 bytes): no im2col copy.  The data gradient uses
+//      the mirrored taps (2-dy, 2-dx).
+//   B: all 9 taps of the weights, staged once per block.
+// Two A stages and two TMEM accumulators (64 columns each): the loads of the
+// next tile run during the MMAs and the epilogue of the current one.  Thread 0
+// issues the loads and the MMAs; all four warps read the accumulator (warp w:
+// TMEM lanes 32w..32w+31) and write the tile.  Every mbarrier wait is bounded
+// (nsdg_tma.cuh); a wait that runs out sets err, waits (bounded) for the
+// block's own copies and MMAs, frees the TMEM and leaves.
+constexpr int kTcM = 128;
+constexpr int kTcSpan = 136;
+constexpr int kTcThreads = 128;
+constexpr unsigned kTcRowBytes = kTcSpan * 16; // 17 x 128: every TMA destination 128-byte aligned
+constexpr unsigned kTcCols = 128;              // TMEM columns: two accumulators of up to 64
+
+template <int CS, int N>
+struct TcLayout {
+    static constexpr unsigned kGroups = CS / 8;
+    static constexpr unsigned kBBytes = 9u * CS * N * 2u;
+    static constexpr unsigned kStageBytes = 3u * kGroups * kTcRowBytes;
+    static constexpr unsigned kAOff = (kBBytes + 1023u) & ~1023u;
+    static constexpr unsigned kBarOff = kAOff + 2u * kStageBytes;
+    static constexpr unsigned kSmem = kBarOff + 64u + 1024u; // barriers, TMEM address, base alignment
+};
+
+__device__ __forceinline__ uint64_t ummaDesc(unsigned addr, unsigned lbo, unsigned sbo)
+{
+    // start, leading (K) and stride (M/N) byte offsets in 16-byte units;
+    // bits 46-48 = 0b001; base offset 0; no swizzle (bits 61-63 = 0)
+    return uint64_t((addr & 0x3FFFFu) >> 4) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16)
+        | (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+template <int N>
+__host__ __device__ constexpr uint32_t ummaIdescBf16()
+{
+    // D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both
+    // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmaLoad4d(void* dst, const CUtensorMap* map, int c, int x, int y, int b,
+    uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smemAddr(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(b), "r"(smemAddr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, int accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                 "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void ummaCommit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                 "[%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+template <int CS, int N, int MODE>
+__global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constant__ CUtensorMap srcMap, int B,
+    int H, int W, const __nv_bfloat16* __restrict__ wmat, const float* __restrict__ bias,
+    const __nv_bfloat16* __restrict__ reluMask, __nv_bfloat16* __restrict__ outBf, float* __restrict__ outF,
+    int* __restrict__ err)
+{
+    static_assert(CS % 16 == 0 && N % 16 == 0 && N <= 64, "channel counts");
+    using Lay = TcLayout<CS, N>;
+    extern __shared__ __align__(16) unsigned char tcSmemRaw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tcSmemRaw) + 1023) & ~uintptr_t(1023));
+    unsigned char* sB = sm;
+    unsigned char* sA = sm + Lay::kAOff;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [2]: an A stage has landed
+    uint64_t* done = full + 2;                                       // [2]: the MMAs of a tile completed
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(full + 4);
+    __shared__ int okFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // the weights in the core-matrix layout: 8-channel group g (tap * CS / 8
+    // + channel group) of output channel n at g * N * 16 + n * 16
+    for (int i = tid; i < 9 * (CS / 8) * N; i += kTcThreads) {
+        const int n = i % N, g = i / N;
+        const int tap = g / (CS / 8), cg = g % (CS / 8);
+        *reinterpret_cast<uint4*>(sB + size_t(g) * N * 16 + n * 16)
+            = *reinterpret_cast<const uint4*>(wmat + size_t(n) * 9 * CS + tap * CS + cg * 8);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) {
+        for (int i = 0; i < 4; ++i)
+            mbarInit(full + i, 1);
+        okFlag = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tmemSlot)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tcFenceBefore();
+    __syncthreads();
+    tcFenceAfter();
+    const uint32_t tmem = *tmemSlot;
+
+    const int tilesX = (W + kTcM - 1) / kTcM;
+    const long tiles = long(B) * H * tilesX;
+    const uint32_t idesc = ummaIdescBf16<N>();
+    const unsigned aBase = smemAddr(sA), bBase = smemAddr(sB);
+    // thread 0's view of what is in flight: the phase parity each stage's
+    // loads and MMAs will complete, -1 when nothing is outstanding
+    int loadsParity[2] = { -1, -1 }, mmaParity[2] = { -1, -1 };
+
+    auto issueLoads = [&](long t, int stage, int parity) {
+        const int x0 = static_cast<int>(t % tilesX) * kTcM;
+        const long r = t / tilesX;
+        const int y = static_cast<int>(r % H), b = static_cast<int>(r / H);
+        uint64_t* bar = full + stage;
+        mbarExpectTx(bar, Lay::kStageBytes);
+        unsigned char* dst = sA + stage * Lay::kStageBytes;
+#pragma unroll 1
+        for (int rr = 0; rr < 3; ++rr)
+#pragma unroll 1
+            for (int g = 0; g < CS / 8; ++g)
+                tmaLoad4d(dst + (rr * (CS / 8) + g) * kTcRowBytes, &srcMap, 8 * g, x0 - 1, y + rr - 1, b, bar);
+        loadsParity[stage] = parity;
+    };
+
+    int it = 0;
+    long t = blockIdx.x;
+    if (tid == 0 && t < tiles)
+        issueLoads(t, 0, 0);
+    for (; t < tiles; t += gridDim.x, ++it) {
+        const int stage = it & 1;
+        const unsigned parity = (it >> 1) & 1;
+        if (tid == 0) {
+            const long tn = t + gridDim.x;
+            if (tn < tiles) // the stage's MMAs (tile it - 1) completed last iteration
+                issueLoads(tn, stage ^ 1, static_cast<int>(((it + 1) >> 1) & 1));
+            if (mbarWaitBounded(full + stage, parity)) {
+                loadsParity[stage] = -1;
+                tcFenceAfter();
+                const uint32_t d = tmem + stage * 64;
+                int k = 0;
+#pragma unroll 1
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int dy = tap / 3, dx = tap % 3;
+                    const int rb = MODE == CONV_BWD_DATA ? 2 - dy : dy;
+                    const int sh = MODE == CONV_BWD_DATA ? 2 - dx : dx;
+#pragma unroll
+                    for (int ks = 0; ks < CS / 16; ++ks, ++k) {
+                        const uint64_t ad = ummaDesc(aBase + stage * Lay::kStageBytes
+                                + (rb * (CS / 8) + 2 * ks) * kTcRowBytes + sh * 16,
+                            kTcRowBytes, 128);
+                        const uint64_t bd = ummaDesc(bBase + (tap * (CS / 8) + 2 * ks) * N * 16, N * 16, 128);
+                        umma(d, ad, bd, idesc, k > 0);
+                    }
+                }
+                ummaCommit(done + stage);
+                mmaParity[stage] = static_cast<int>(parity);
+            } else {
+                atomicOr(err, 1);
+                okFlag = 0;
+            }
+        }
+        __syncthreads();
+        if (!okFlag)
+            break;
+        const bool mmaDone = mbarWaitBounded(done + stage, parity);
+        if (!mmaDone) {
+            atomicOr(err, 1);
+            okFlag = 0;
+        }
+        if (tid == 0 && mmaDone)
+            mmaParity[stage] = -1;
+        tcFenceAfter();
+        // epilogue: pixel x0 + 32 warp + lane of the tile, all N channels
+        float acc[N];
+        const uint32_t taddr = tmem + stage * 64 + (uint32_t(32 * warp) << 16);
+#pragma unroll
+        for (int c = 0; c < N; c += 16)
+            tmemLoad16(taddr + c, acc + c);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int x0 = static_cast<int>(t % tilesX) * kTcM;
+        const long r = t / tilesX;
+        const int y = static_cast<int>(r % H), b = static_cast<int>(r / H);
+        const int x = x0 + 32 * warp + lane;
+        if (x < W && okFlag) {
+            const long m = (long(b) * H + y) * W + x;
+            if (MODE == CONV_FWD_LINEAR) {
+#pragma unroll
+                for (int n = 0; n < N; n += 4)
+                    *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(acc[n] + bias[n],
+                        acc[n + 1] + bias[n + 1], acc[n + 2] + bias[n + 2], acc[n + 3] + bias[n + 3]);
+            } else {
+#pragma unroll
+                for (int n = 0; n < N; n += 8) {
+                    uint4 mk4 = make_uint4(0, 0, 0, 0);
+                    if (MODE == CONV_BWD_DATA)
+                        mk4 = *reinterpret_cast<const uint4*>(reluMask + m * N + n);
+                    const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(&mk4);
+                    __nv_bfloat16 o[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float v = acc[n + j];
+                        if (MODE == CONV_FWD_RELU)
+                            v = fmaxf(v + bias[n + j], 0.f);
+                        else
+                            v = __bfloat162float(mk[j]) > 0.f ? v : 0.f;
+                        o[j] = __float2bfloat16_rn(v);
+                    }
+                    *reinterpret_cast<uint4*>(outBf + m * N + n) = *reinterpret_cast<const uint4*>(o);
+                }
+            }
+        }
+        tcFenceBefore();
+        __syncthreads(); // the accumulator may be overwritten two tiles on
+        if (!okFlag)
+            break;
+    }
+    // after a wait ran out: the block's own copies and MMAs still in flight
+    // are waited for (bounded) before the shared memory and the TMEM go
+    if (tid == 0) {
+        for (int sIdx = 0; sIdx < 2; ++sIdx) {
+            if (loadsParity[sIdx] >= 0)
+                mbarWaitBounded(full + sIdx, static_cast<unsigned>(loadsParity[sIdx]));
+            if (mmaParity[sIdx] >= 0)
+                mbarWaitBounded(done + sIdx, static_cast<unsigned>(mmaParity[sIdx]));
+        }
+    }
+    tcFenceBefore();
+    __syncthreads();
+    if (warp == 0) {
+        tcFenceAfter();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
     }
 }
 
@@ -360,6 +635,36 @@ cudaError_t conv(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src, 
     return cudaGetLastError();
 }
 
+// The tensor-core form: a tensor map over the source [B][H][W][CS] (boxes of
+// 8 channels x 136 pixels), one block per SM looping over the tiles.
+template <int CS, int N, int MODE>
+cudaError_t convTcPrepare()
+{
+    return cudaFuncSetAttribute(kConv3x3Tc<CS, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        static_cast<int>(TcLayout<CS, N>::kSmem));
+}
+
+template <int CS, int N, int MODE>
+cudaError_t convTc(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src, const __nv_bfloat16* w,
+    const float* bias, const __nv_bfloat16* mask, __nv_bfloat16* outBf, float* outF, int* err)
+{
+    CUtensorMap map;
+    const uint64_t dims[4] = { uint64_t(CS), uint64_t(W), uint64_t(H), uint64_t(B) };
+    const uint64_t strides[3] = { uint64_t(CS) * 2, uint64_t(W) * CS * 2, uint64_t(H) * W * CS * 2 };
+    const uint32_t box[4] = { 8, kTcSpan, 1, 1 };
+    cudaError_t e = encodeTiledNd(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, src, 4, dims, strides, box);
+    int dev = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return e;
+    const long tiles = long(B) * H * ((W + kTcM - 1) / kTcM);
+    const unsigned grid = static_cast<unsigned>(std::min<long>(tiles, sms));
+    kConv3x3Tc<CS, N, MODE><<<grid, kTcThreads, TcLayout<CS, N>::kSmem, s>>>(map, B, H, W, w, bias, mask, outBf,
+        outF, err);
+    return cudaGetLastError();
+}
+
 // channel counts supported by the instantiations: 16, 32, 48, 64
 #define NSDG_CH_SWITCH(c, D, CALL)                                                                 \
     switch (c) {                                                                                   \
@@ -402,6 +707,10 @@ struct NetImpl {
     float* stats = nullptr; // device: featShift[kWarmFeat], featInv[kWarmFeat], tgtShift[kWarmTgt], tgtScale[kWarmTgt]
     int* dIdx = nullptr;    // batch sample indices
     double* dPart = nullptr;
+    // convolutions on tcgen05 (the default) or by mma.sync (NSDG_CONV=mma);
+    // the tensor-core kernels' error word (a bounded wait ran out)
+    bool tc = true;
+    int* derr = nullptr;
 };
 
 namespace {
@@ -453,7 +762,7 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     for (int l = 0; l < L; ++l)
         bytes += a256(size_t(M) * n->ch[l] * 2);
     bytes += 2 * a256(size_t(M) * n->ch[L] * 4) + a256(size_t(M) * 4) + 2 * a256(size_t(M) * cmax * 2)
-        + a256(n->partFloats * 4) + a256(size_t((M + 255) / 256 + 2) * 4);
+        + a256(n->partFloats * 4) + a256(size_t((M + 255) / 256 + 2) * 4) + a256(4);
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess
         || cudaMalloc(&n->mem, bytes) != cudaSuccess) {
         err = "network: device allocation failed";
@@ -485,6 +794,9 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     n->lossPart = static_cast<float*>(take(size_t((M + 255) / 256 + 2) * 4));
     n->stats = static_cast<float*>(take(kWarmNorm * 4));
     n->dIdx = static_cast<int*>(take(size_t(maxB) * 4));
+    n->derr = static_cast<int*>(take(4));
+    if (const char* env = std::getenv("NSDG_CONV"))
+        n->tc = std::strcmp(env, "mma") != 0;
     // He-normal initial weights, zero biases (host RNG: reproducible)
     std::vector<float> w(n->nParams, 0.f);
     std::mt19937_64 rng(seed);
@@ -499,6 +811,22 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     if (e == cudaSuccess) e = cudaMemset(n->m2, 0, n->nParams * 4);
     if (e == cudaSuccess) e = cudaMemset(n->mask, 0, size_t(M) * 4);
     if (e == cudaSuccess) e = cudaMemset(n->target, 0, size_t(M) * n->ch[L] * 4);
+    if (e == cudaSuccess) e = cudaMemset(n->derr, 0, 4);
+    // the tensor-core kernels' shared memory, once per instantiation used
+    for (int l = 0; l < L && e == cudaSuccess && n->tc; ++l) {
+        const int CI = n->ch[l], CO = n->ch[l + 1];
+        const auto prep = [&]() -> cudaError_t {
+            if (l + 1 < L) {
+                NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convTcPrepare<A, Bc, CONV_FWD_RELU>())));
+            } else {
+                NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convTcPrepare<A, Bc, CONV_FWD_LINEAR>())));
+            }
+            if (e == cudaSuccess && l > 0)
+                NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (e = convTcPrepare<A, Bc, CONV_BWD_DATA>())));
+            return e;
+        };
+        e = prep();
+    }
     if (e == cudaSuccess) {
         // identity normalisation until a dataset sets it
         std::vector<float> st(kWarmNorm, 0.f);
@@ -565,7 +893,13 @@ cudaError_t netForward(NetImpl* n, cudaStream_t s, int B)
         const int CI = n->ch[l], CO = n->ch[l + 1];
         const __nv_bfloat16* w = n->w16 + n->wOff[l];
         const float* b = n->w32 + n->bOff[l];
-        if (l + 1 < n->L) {
+        if (n->tc && l + 1 < n->L) {
+            NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convTc<A, Bc, CONV_FWD_RELU>(s, B, n->H, n->W, n->act[l],
+                                                         w, b, nullptr, n->act[l + 1], nullptr, n->derr))));
+        } else if (n->tc) {
+            NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convTc<A, Bc, CONV_FWD_LINEAR>(s, B, n->H, n->W,
+                                                         n->act[l], w, b, nullptr, nullptr, n->out, n->derr))));
+        } else if (l + 1 < n->L) {
             NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = conv<A, Bc, CONV_FWD_RELU>(s, B, n->H, n->W, n->act[l], w, b,
                                                          nullptr, n->act[l + 1], nullptr))));
         } else {
@@ -604,8 +938,15 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
         kSumChunks<<<1, CO, 0, s>>>(nChunks, CO, n->part, n->g32 + n->bOff[l]);
         // data gradient times relu' of the layer input (not needed for the network input)
         if (l > 0) {
-            NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (e = conv<A, Bc, CONV_BWD_DATA>(s, B, n->H, n->W, gz,
-                                                              n->wt16 + n->wOff[l], nullptr, n->act[l], gnext, nullptr))));
+            if (n->tc) {
+                NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (e = convTc<A, Bc, CONV_BWD_DATA>(s, B, n->H, n->W, gz,
+                                                                  n->wt16 + n->wOff[l], nullptr, n->act[l], gnext,
+                                                                  nullptr, n->derr))));
+            } else {
+                NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (e = conv<A, Bc, CONV_BWD_DATA>(s, B, n->H, n->W, gz,
+                                                                  n->wt16 + n->wOff[l], nullptr, n->act[l], gnext,
+                                                                  nullptr))));
+            }
             std::swap(gz, gnext);
         }
         if (e == cudaSuccess)
@@ -1192,6 +1533,24 @@ int nsdg_net_param_count(nsdg_net* h, size_t* n)
     return NSDG_OK;
 }
 
+// After the stream has been synchronised: the tensor-core convolutions'
+// error word (a bounded wait ran out), reported once and cleared.
+static int netDeviceStatus(nsdg_net* h)
+{
+    int word = 0;
+    cudaError_t e = cudaMemcpy(&word, h->impl->derr, sizeof word, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && word != 0) {
+        cudaMemset(h->impl->derr, 0, sizeof word);
+        h->err = "a bounded wait of a tensor-core convolution ran out";
+        return NSDG_ERR_CUDA;
+    }
+    if (e != cudaSuccess) {
+        h->err = cudaGetErrorString(e);
+        return NSDG_ERR_CUDA;
+    }
+    return NSDG_OK;
+}
+
 static int netCopy(nsdg_net* h, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind)
 {
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, netStream(h->impl));
@@ -1200,7 +1559,7 @@ static int netCopy(nsdg_net* h, void* dst, const void* src, size_t bytes, cudaMe
         h->err = cudaGetErrorString(e);
         return NSDG_ERR_CUDA;
     }
-    return NSDG_OK;
+    return netDeviceStatus(h);
 }
 
 int nsdg_net_get_params(nsdg_net* h, float* host, size_t n)
@@ -1298,7 +1657,7 @@ int nsdg_net_time_forward(nsdg_net* h, int batch, int reps, float* ms)
         return NSDG_ERR_CUDA;
     }
     *ms /= float(reps);
-    return NSDG_OK;
+    return netDeviceStatus(h);
 }
 
 int nsdg_net_loss_backward(nsdg_net* h, int batch, float* loss)

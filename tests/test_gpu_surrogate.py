@@ -1,5 +1,8 @@
-"""GPU network kernels (BF16 mma.sync, FP32 accumulate) against the numpy oracle:
-forward output, loss, weight and bias gradients; and a short training run."""
+"""GPU network kernels (BF16 products, FP32 accumulation) against the numpy
+oracle: forward output, loss, weight and bias gradients, with the
+convolutions on tcgen05 (the default) and by mma.sync (NSDG_CONV=mma); the
+two against each other on the warm start's network shape; and a short
+training run."""
 import numpy as np
 import pytest
 
@@ -12,9 +15,15 @@ def _rel(a, b):
     return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
 
 
-@pytest.mark.parametrize("chans,H,W,B,used", [([16, 32, 32, 16], 10, 13, 2, 12), ([48, 48, 32], 9, 70, 1, 26)])
-def test_net_gradients_match_oracle(gpu, chans, H, W, B, used):
+@pytest.mark.parametrize("conv", ["tcgen05", "mma"])
+@pytest.mark.parametrize("chans,H,W,B,used", [([16, 32, 32, 16], 10, 13, 2, 12), ([48, 48, 32], 9, 70, 1, 26),
+                                              ([64, 48, 64, 32], 5, 131, 2, 20)])
+def test_net_gradients_match_oracle(gpu, monkeypatch, conv, chans, H, W, B, used):
     from nextsimdg_gb300.surrogate import Net
+    if conv == "mma":
+        monkeypatch.setenv("NSDG_CONV", "mma")
+    else:
+        monkeypatch.delenv("NSDG_CONV", raising=False)
     rng = np.random.default_rng(11)
     net = Net(chans, H, W, max_batch=B, used_outputs=used, seed=5)
     p = net.get_params()
@@ -57,3 +66,34 @@ def test_net_training_reduces_loss(gpu):
         losses.append(net.loss_backward())
         net.adam_step(lr=3e-3)
     assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
+
+
+def test_tensor_core_convolutions_match_mma_sync(gpu, monkeypatch):
+    """The warm start's network (64-48-48-48-48-48-32) on a 3 x 40 x 200 batch
+    (two 128-pixel tiles per row, the second partial): forward output and
+    gradients with tcgen05 against mma.sync, and the tcgen05 forward run to
+    run bitwise reproducible."""
+    from nextsimdg_gb300 import surrogate
+    rng = np.random.default_rng(4)
+    H, W, B = 40, 200, 3
+    out, grads = {}, {}
+    for conv in ("mma", "tcgen05"):
+        if conv == "mma":
+            monkeypatch.setenv("NSDG_CONV", "mma")
+        else:
+            monkeypatch.delenv("NSDG_CONV", raising=False)
+        net = surrogate.Net(list(surrogate.WARM_CHANNELS), H, W, max_batch=B, used_outputs=26, seed=3)
+        x = rng.standard_normal((B, H, W, net.channels[0])).astype(np.float32) if conv == "mma" else x
+        t = np.zeros((B, H, W, net.channels[-1]), dtype=np.float32)
+        t[..., :26] = 0.3
+        m = np.ones((B, H, W), dtype=np.float32)
+        net.set_batch(x, t, m)
+        out[conv] = net.forward()
+        if conv == "tcgen05":
+            assert np.array_equal(net.forward(), out[conv])
+        net.loss_backward()
+        grads[conv] = net.get_grads()
+        net.close()
+    assert np.all(np.isfinite(out["tcgen05"]))
+    assert _rel(out["tcgen05"], out["mma"]) < 2e-3
+    assert _rel(grads["tcgen05"], grads["mma"]) < 2e-2
