@@ -50,6 +50,19 @@ __device__ __forceinline__ void mma16816(float* c, const uint32_t* a, const uint
 
 enum ConvMode { CONV_FWD_RELU = 0, CONV_FWD_LINEAR = 1, CONV_BWD_DATA = 2 };
 
+// Offset of the 8 channels [8 c8, 8 c8 + 8) of pixel m (m = (b H + y) W + x)
+// in a C-channel BF16 activation map: channels-last, m C + 8 c8 (wg = 0,
+// the mma.sync convolutions), or channel-group-major [b H + y][c8][x][8]
+// (wg = W, the tensor-core convolutions: one 8-channel group of a row of
+// pixels is contiguous, so one TMA box of it is one contiguous run).
+__host__ __device__ __forceinline__ long actChunk(long m, int c8, int C, int wg)
+{
+    if (wg == 0)
+        return m * C + c8 * 8;
+    const long r = m / wg;
+    return ((r * (C >> 3) + c8) * wg + (m - r * wg)) * 8;
+}
+
 // out[m][n] for m in a block of 64 pixels and all N channels.
 //   forward:   A[m][(tap,c)] = src[pixel m + (dy-1, dx-1)][c],   B = W  [n][tap*CS + c]
 //   bwd data:  A[m][(tap,c)] = src[pixel m - (dy-1, dx-1)][c],   B = W^T[n][tap*CS + c]
@@ -153,22 +166,30 @@ __global__ void __launch_bounds__(kThreads) kConv3x3(int B, int H, int W, const 
 // is one contiguous block (LBO = the block's size).
 //   A: per tile, TMA loads the three input rows y-1, y, y+1 at pixels
 //      x0-1 ... x0+134 (136 pixels, 2176 bytes per 8-channel group; pixels
-//      outside the image read as zero), for every 8-channel group.  Tap
+//      outside the image read as zero), for every 8-channel group, in one
+//      TMA copy per tile: the activations are stored channel-group-major
+//      (actChunk), which a 5-D box lays out in shared memory exactly as the
+//      MMAs read it, [row][group][pixel][8].  Tap
 //      (dy, dx) is then the same block with its descriptor's start address
 //      moved by dx pixels (16 bytes): no im2col copy.  The data gradient uses
 //      the mirrored taps (2-dy, 2-dx).
 //   B: all 9 taps of the weights, staged once per block.
-// Two A stages and two TMEM accumulators (64 columns each): the loads of the
-// next tile run during the MMAs and the epilogue of the current one.  Thread 0
-// issues the loads and the MMAs; all four warps read the accumulator (warp w:
-// TMEM lanes 32w..32w+31) and write the tile.  Every mbarrier wait is bounded
-// (nsdg_tma.cuh); a wait that runs out sets err, waits (bounded) for the
-// block's own copies and MMAs, frees the TMEM and leaves.
+// Warp roles: lane 0 of warp 4 loads A stages (a ring of 2-4, as many as
+// fit next to the weights) and issues the MMAs; warps 0-3 read the two TMEM
+// accumulators (warp w: lanes 32w..32w+31, the tile's pixels) and write the
+// tile.  full/empty barriers hand the A stages between the TMA and the
+// MMAs, accFull/accEmpty the accumulators between the MMAs and the
+// epilogue, so loads run ahead while the epilogue of the previous tile
+// overlaps the MMAs of the next.  Every wait is bounded (nsdg_tma.cuh); a
+// wait that runs out sets err and stops the block, whose copies and MMAs
+// still in flight are waited for (bounded) before the TMEM is freed.
 constexpr int kTcM = 128;
 constexpr int kTcSpan = 136;
-constexpr int kTcThreads = 128;
+constexpr int kTcEpiWarps = 4;
+constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);
 constexpr unsigned kTcRowBytes = kTcSpan * 16; // 17 x 128: every TMA destination 128-byte aligned
 constexpr unsigned kTcCols = 128;              // TMEM columns: two accumulators of up to 64
+constexpr unsigned kTcSmemMax = 232448;        // dynamic shared memory per block (227 KB)
 
 template <int CS, int N>
 struct TcLayout {
@@ -176,8 +197,11 @@ struct TcLayout {
     static constexpr unsigned kBBytes = 9u * CS * N * 2u;
     static constexpr unsigned kStageBytes = 3u * kGroups * kTcRowBytes;
     static constexpr unsigned kAOff = (kBBytes + 1023u) & ~1023u;
-    static constexpr unsigned kBarOff = kAOff + 2u * kStageBytes;
-    static constexpr unsigned kSmem = kBarOff + 64u + 1024u; // barriers, TMEM address, base alignment
+    static constexpr unsigned kFit = (kTcSmemMax - 1024u - 256u - kAOff) / kStageBytes;
+    static constexpr unsigned kStages = kFit > 4u ? 4u : kFit;
+    static constexpr unsigned kBarOff = kAOff + kStages * kStageBytes;
+    static constexpr unsigned kSmem = kBarOff + 128u + 1024u; // barriers, TMEM address, base alignment
+    static_assert(kStages >= 2, "two A stages must fit");
 };
 
 __device__ __forceinline__ uint64_t ummaDesc(unsigned addr, unsigned lbo, unsigned sbo)
@@ -196,13 +220,21 @@ __host__ __device__ constexpr uint32_t ummaIdescBf16()
     return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
 }
 
-__device__ __forceinline__ void tmaLoad4d(void* dst, const CUtensorMap* map, int c, int x, int y, int b,
-    uint64_t* bar)
+// the A stage of one tile in one copy: pixels x .. x + 135, all 8-channel
+// groups, rows y .. y + 2 of image b of the channel-group-major map
+// [b][y][g][x][8]; in shared memory [row][g][pixel][8], 2176 bytes per
+// (row, group)
+__device__ __forceinline__ void tmaLoadStage(void* dst, const CUtensorMap* map, int x, int y, int b, uint64_t* bar)
 {
-    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smemAddr(dst)),
-                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(b), "r"(smemAddr(bar))
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smemAddr(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(x), "r"(0), "r"(y), "r"(b), "r"(smemAddr(bar))
                  : "memory");
+}
+
+__device__ __forceinline__ void mbarArrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
 }
 
 __device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, int accumulate)
@@ -243,14 +275,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
 {
     static_assert(CS % 16 == 0 && N % 16 == 0 && N <= 64, "channel counts");
     using Lay = TcLayout<CS, N>;
+    constexpr int S = static_cast<int>(Lay::kStages);
     extern __shared__ __align__(16) unsigned char tcSmemRaw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tcSmemRaw) + 1023) & ~uintptr_t(1023));
     unsigned char* sB = sm;
     unsigned char* sA = sm + Lay::kAOff;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [2]: an A stage has landed
-    uint64_t* done = full + 2;                                       // [2]: the MMAs of a tile completed
-    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(full + 4);
-    __shared__ int okFlag;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [4] an A stage has landed
+    uint64_t* empty = full + 4;                                      // [4] its MMAs completed
+    uint64_t* accFull = full + 8;                                    // [2] an accumulator is ready
+    uint64_t* accEmpty = full + 10;                                  // [2] ... has been read
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(full + 12);
+    __shared__ volatile int abortFlag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // the weights in the core-matrix layout: 8-channel group g (tap * CS / 8
@@ -263,9 +298,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0) {
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 10; ++i)
             mbarInit(full + i, 1);
-        okFlag = 1;
+        mbarInit(accEmpty, kTcEpiWarps * 32);
+        mbarInit(accEmpty + 1, kTcEpiWarps * 32);
+        abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -281,127 +318,144 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
 
     const int tilesX = (W + kTcM - 1) / kTcM;
     const long tiles = long(B) * H * tilesX;
-    const uint32_t idesc = ummaIdescBf16<N>();
-    const unsigned aBase = smemAddr(sA), bBase = smemAddr(sB);
-    // thread 0's view of what is in flight: the phase parity each stage's
-    // loads and MMAs will complete, -1 when nothing is outstanding
-    int loadsParity[2] = { -1, -1 }, mmaParity[2] = { -1, -1 };
-
-    auto issueLoads = [&](long t, int stage, int parity) {
-        const int x0 = static_cast<int>(t % tilesX) * kTcM;
+    const long T = blockIdx.x < tiles ? (tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    auto tileOf = [&](long k, int& b, int& y, int& x0) {
+        const long t = blockIdx.x + k * long(gridDim.x);
+        x0 = static_cast<int>(t % tilesX) * kTcM;
         const long r = t / tilesX;
-        const int y = static_cast<int>(r % H), b = static_cast<int>(r / H);
-        uint64_t* bar = full + stage;
-        mbarExpectTx(bar, Lay::kStageBytes);
-        unsigned char* dst = sA + stage * Lay::kStageBytes;
-#pragma unroll 1
-        for (int rr = 0; rr < 3; ++rr)
-#pragma unroll 1
-            for (int g = 0; g < CS / 8; ++g)
-                tmaLoad4d(dst + (rr * (CS / 8) + g) * kTcRowBytes, &srcMap, 8 * g, x0 - 1, y + rr - 1, b, bar);
-        loadsParity[stage] = parity;
+        y = static_cast<int>(r % H);
+        b = static_cast<int>(r / H);
     };
 
-    int it = 0;
-    long t = blockIdx.x;
-    if (tid == 0 && t < tiles)
-        issueLoads(t, 0, 0);
-    for (; t < tiles; t += gridDim.x, ++it) {
-        const int stage = it & 1;
-        const unsigned parity = (it >> 1) & 1;
-        if (tid == 0) {
-            const long tn = t + gridDim.x;
-            if (tn < tiles) // the stage's MMAs (tile it - 1) completed last iteration
-                issueLoads(tn, stage ^ 1, static_cast<int>(((it + 1) >> 1) & 1));
-            if (mbarWaitBounded(full + stage, parity)) {
-                loadsParity[stage] = -1;
+    if (warp == kTcEpiWarps) {
+        if (lane == 0) {
+            // ---- loads and MMAs ----------------------------------------
+            const uint32_t idesc = ummaIdescBf16<N>();
+            const unsigned aBase = smemAddr(sA), bBase = smemAddr(sB);
+            int loadPar[4] = { -1, -1, -1, -1 }; // phase parity of a stage's outstanding loads
+            int lastAcc = -1, lastAccPar = 0;     // the last accumulator committed
+            auto issueLoads = [&](long k, int st) {
+                int b, y, x0;
+                tileOf(k, b, y, x0);
+                uint64_t* bar = full + st;
+                mbarExpectTx(bar, Lay::kStageBytes);
+                tmaLoadStage(sA + st * Lay::kStageBytes, &srcMap, x0 - 1, y - 1, b, bar);
+                loadPar[st] = static_cast<int>((k / S) & 1);
+            };
+            bool ok = true;
+            for (long k = 0; k < T && k < S; ++k)
+                issueLoads(k, static_cast<int>(k));
+            for (long k = 0; k < T && ok; ++k) {
+                if (abortFlag) {
+                    ok = false;
+                    break;
+                }
+                const int st = static_cast<int>(k % S);
+                const int acc = static_cast<int>(k & 1);
+                ok = mbarWaitBounded(full + st, static_cast<unsigned>((k / S) & 1));
+                if (ok)
+                    loadPar[st] = -1;
+                // the accumulator's previous tile has been read (its first
+                // use passes: the barrier's preceding phase counts as done)
+                ok = ok && mbarWaitBounded(accEmpty + acc, static_cast<unsigned>(((k >> 1) & 1) ^ 1));
+                if (!ok)
+                    break;
                 tcFenceAfter();
-                const uint32_t d = tmem + stage * 64;
-                int k = 0;
+                const uint32_t d = tmem + acc * 64;
+                int kk = 0;
 #pragma unroll 1
                 for (int tap = 0; tap < 9; ++tap) {
                     const int dy = tap / 3, dx = tap % 3;
                     const int rb = MODE == CONV_BWD_DATA ? 2 - dy : dy;
                     const int sh = MODE == CONV_BWD_DATA ? 2 - dx : dx;
 #pragma unroll
-                    for (int ks = 0; ks < CS / 16; ++ks, ++k) {
-                        const uint64_t ad = ummaDesc(aBase + stage * Lay::kStageBytes
+                    for (int ks = 0; ks < CS / 16; ++ks, ++kk) {
+                        const uint64_t ad = ummaDesc(aBase + st * Lay::kStageBytes
                                 + (rb * (CS / 8) + 2 * ks) * kTcRowBytes + sh * 16,
                             kTcRowBytes, 128);
                         const uint64_t bd = ummaDesc(bBase + (tap * (CS / 8) + 2 * ks) * N * 16, N * 16, 128);
-                        umma(d, ad, bd, idesc, k > 0);
+                        umma(d, ad, bd, idesc, kk > 0);
                     }
                 }
-                ummaCommit(done + stage);
-                mmaParity[stage] = static_cast<int>(parity);
-            } else {
+                ummaCommit(empty + st);
+                ummaCommit(accFull + acc);
+                lastAcc = acc;
+                lastAccPar = static_cast<int>((k >> 1) & 1);
+                // refill the stage of the previous tile (its MMAs went out
+                // one iteration ago) with the tile S - 1 ahead
+                if (k >= 1 && k - 1 + S < T) {
+                    const int sp = static_cast<int>((k - 1) % S);
+                    ok = mbarWaitBounded(empty + sp, static_cast<unsigned>(((k - 1) / S) & 1));
+                    if (ok)
+                        issueLoads(k - 1 + S, sp);
+                }
+            }
+            if (!ok) {
                 atomicOr(err, 1);
-                okFlag = 0;
+                abortFlag = 1;
             }
+            // nothing of this block may still be in flight when it leaves
+            for (int st = 0; st < S; ++st)
+                if (loadPar[st] >= 0)
+                    mbarWaitBounded(full + st, static_cast<unsigned>(loadPar[st]));
+            if (lastAcc >= 0)
+                mbarWaitBounded(accFull + lastAcc, static_cast<unsigned>(lastAccPar));
         }
-        __syncthreads();
-        if (!okFlag)
-            break;
-        const bool mmaDone = mbarWaitBounded(done + stage, parity);
-        if (!mmaDone) {
-            atomicOr(err, 1);
-            okFlag = 0;
-        }
-        if (tid == 0 && mmaDone)
-            mmaParity[stage] = -1;
-        tcFenceAfter();
-        // epilogue: pixel x0 + 32 warp + lane of the tile, all N channels
-        float acc[N];
-        const uint32_t taddr = tmem + stage * 64 + (uint32_t(32 * warp) << 16);
+    } else {
+        // ---- epilogue: warp w holds pixels x0 + 32 w + lane ---------------
+        for (long k = 0; k < T; ++k) {
+            if (__any_sync(0xffffffffu, abortFlag != 0))
+                break;
+            const int acc = static_cast<int>(k & 1);
+            const bool ready = __all_sync(0xffffffffu, mbarWaitBounded(accFull + acc, static_cast<unsigned>((k >> 1) & 1)));
+            if (!ready) {
+                if (lane == 0) {
+                    atomicOr(err, 1);
+                    abortFlag = 1;
+                }
+                break;
+            }
+            tcFenceAfter();
+            float v[N];
+            const uint32_t taddr = tmem + acc * 64 + (uint32_t(32 * warp) << 16);
 #pragma unroll
-        for (int c = 0; c < N; c += 16)
-            tmemLoad16(taddr + c, acc + c);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int x0 = static_cast<int>(t % tilesX) * kTcM;
-        const long r = t / tilesX;
-        const int y = static_cast<int>(r % H), b = static_cast<int>(r / H);
-        const int x = x0 + 32 * warp + lane;
-        if (x < W && okFlag) {
-            const long m = (long(b) * H + y) * W + x;
-            if (MODE == CONV_FWD_LINEAR) {
+            for (int c = 0; c < N; c += 16)
+                tmemLoad16(taddr + c, v + c);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            tcFenceBefore();
+            mbarArrive(accEmpty + acc);
+            int b, y, x0;
+            tileOf(k, b, y, x0);
+            const int x = x0 + 32 * warp + lane;
+            if (x < W) {
+                const long m = (long(b) * H + y) * W + x;
+                if (MODE == CONV_FWD_LINEAR) {
 #pragma unroll
-                for (int n = 0; n < N; n += 4)
-                    *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(acc[n] + bias[n],
-                        acc[n + 1] + bias[n + 1], acc[n + 2] + bias[n + 2], acc[n + 3] + bias[n + 3]);
-            } else {
+                    for (int n = 0; n < N; n += 4)
+                        *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(v[n] + bias[n],
+                            v[n + 1] + bias[n + 1], v[n + 2] + bias[n + 2], v[n + 3] + bias[n + 3]);
+                } else {
 #pragma unroll
-                for (int n = 0; n < N; n += 8) {
-                    uint4 mk4 = make_uint4(0, 0, 0, 0);
-                    if (MODE == CONV_BWD_DATA)
-                        mk4 = *reinterpret_cast<const uint4*>(reluMask + m * N + n);
-                    const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(&mk4);
-                    __nv_bfloat16 o[8];
+                    for (int n = 0; n < N; n += 8) {
+                        const long off = actChunk(m, n >> 3, N, W);
+                        uint4 mk4 = make_uint4(0, 0, 0, 0);
+                        if (MODE == CONV_BWD_DATA)
+                            mk4 = *reinterpret_cast<const uint4*>(reluMask + off);
+                        const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(&mk4);
+                        __nv_bfloat16 o[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        float v = acc[n + j];
-                        if (MODE == CONV_FWD_RELU)
-                            v = fmaxf(v + bias[n + j], 0.f);
-                        else
-                            v = __bfloat162float(mk[j]) > 0.f ? v : 0.f;
-                        o[j] = __float2bfloat16_rn(v);
+                        for (int j = 0; j < 8; ++j) {
+                            float val = v[n + j];
+                            if (MODE == CONV_FWD_RELU)
+                                val = fmaxf(val + bias[n + j], 0.f);
+                            else
+                                val = __bfloat162float(mk[j]) > 0.f ? val : 0.f;
+                            o[j] = __float2bfloat16_rn(val);
+                        }
+                        *reinterpret_cast<uint4*>(outBf + off) = *reinterpret_cast<const uint4*>(o);
                     }
-                    *reinterpret_cast<uint4*>(outBf + m * N + n) = *reinterpret_cast<const uint4*>(o);
                 }
             }
-        }
-        tcFenceBefore();
-        __syncthreads(); // the accumulator may be overwritten two tiles on
-        if (!okFlag)
-            break;
-    }
-    // after a wait ran out: the block's own copies and MMAs still in flight
-    // are waited for (bounded) before the shared memory and the TMEM go
-    if (tid == 0) {
-        for (int sIdx = 0; sIdx < 2; ++sIdx) {
-            if (loadsParity[sIdx] >= 0)
-                mbarWaitBounded(full + sIdx, static_cast<unsigned>(loadsParity[sIdx]));
-            if (mmaParity[sIdx] >= 0)
-                mbarWaitBounded(done + sIdx, static_cast<unsigned>(mmaParity[sIdx]));
         }
     }
     tcFenceBefore();
@@ -416,7 +470,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
 //   part[chunk][co][tap*CI + ci] = sum_{m in chunk} gz[m][co] * x[m + (dy-1, dx-1)][ci]
 template <int CO, int CI>
 __global__ void __launch_bounds__(kThreads) kConvWeightGrad(int B, int H, int W, const __nv_bfloat16* __restrict__ gz,
-    const __nv_bfloat16* __restrict__ x, float* __restrict__ part)
+    const __nv_bfloat16* __restrict__ x, float* __restrict__ part, int wg)
 {
     static_assert(CO % 16 == 0 && CI % 8 == 0 && CI <= 64 && CO <= 64, "channel counts");
     __shared__ __align__(16) __nv_bfloat16 As[CO][kStride]; // [co][pixel]
@@ -442,7 +496,7 @@ __global__ void __launch_bounds__(kThreads) kConvWeightGrad(int B, int H, int W,
             const long m = p0 + k0 + pk;
             uint4 v = make_uint4(0, 0, 0, 0);
             if (m < M)
-                v = *reinterpret_cast<const uint4*>(gz + m * CO + c8 * 8);
+                v = *reinterpret_cast<const uint4*>(gz + actChunk(m, c8, CO, wg));
             const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
 #pragma unroll
             for (int i = 0; i < 8; ++i)
@@ -458,7 +512,7 @@ __global__ void __launch_bounds__(kThreads) kConvWeightGrad(int B, int H, int W,
                 const int rem = static_cast<int>(m - long(b) * H * W);
                 const int sy = rem / W + dy, sx = rem % W + dx;
                 if (sy >= 0 && sy < H && sx >= 0 && sx < W)
-                    v = *reinterpret_cast<const uint4*>(x + ((long(b) * H + sy) * W + sx) * CI + c8 * 8);
+                    v = *reinterpret_cast<const uint4*>(x + actChunk((long(b) * H + sy) * W + sx, c8, CI, wg));
             }
             const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
 #pragma unroll
@@ -518,7 +572,7 @@ __global__ void kSumChunks(int nChunks, size_t n, const float* __restrict__ part
     out[i] = s;
 }
 template <int CO>
-__global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, float* __restrict__ part)
+__global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, float* __restrict__ part, int wg)
 {
     // one block per chunk, one thread per channel (blockDim.x = CO)
     const int co = threadIdx.x;
@@ -528,7 +582,7 @@ __global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, f
         const long m = p0 + k;
         if (m >= M)
             break;
-        s += __bfloat162float(gz[m * CO + co]);
+        s += __bfloat162float(gz[actChunk(m, co >> 3, CO, wg) + (co & 7)]);
     }
     part[long(blockIdx.x) * CO + co] = s;
 }
@@ -537,7 +591,7 @@ __global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, f
 // (BF16, zero in the padding), per-block partial losses.
 __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const float* __restrict__ out,
     const float* __restrict__ target, const float* __restrict__ mask, const float* __restrict__ invDenomPtr,
-    __nv_bfloat16* __restrict__ gz, float* __restrict__ partial)
+    __nv_bfloat16* __restrict__ gz, float* __restrict__ partial, int wg)
 {
     __shared__ float ws[8];
     const float invDenom = *invDenomPtr;
@@ -552,7 +606,7 @@ __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const floa
                 s += mk * d * d;
                 gval = 2.f * mk * d * invDenom;
             }
-            gz[m * C + c] = __float2bfloat16_rn(gval);
+            gz[actChunk(m, c >> 3, C, wg) + (c & 7)] = __float2bfloat16_rn(gval);
         }
     }
     for (int off = 16; off > 0; off >>= 1)
@@ -618,11 +672,15 @@ __global__ void kRefreshWeights(int CO, int CI, const float* __restrict__ w32, _
     wt16[long(ci) * 9 * CO + tap * CO + co] = v;
 }
 
-__global__ void kToBf16(long n, const float* __restrict__ a, __nv_bfloat16* __restrict__ b)
+// channels-last FP32 input [M][C] -> the network's BF16 input map
+__global__ void kToBf16(long n, int C, int wg, const float* __restrict__ a, __nv_bfloat16* __restrict__ b)
 {
     const long i = blockIdx.x * long(blockDim.x) + threadIdx.x;
-    if (i < n)
-        b[i] = __float2bfloat16_rn(a[i]);
+    if (i < n) {
+        const long m = i / C;
+        const int c = static_cast<int>(i - m * C);
+        b[actChunk(m, c >> 3, C, wg) + (c & 7)] = __float2bfloat16_rn(a[i]);
+    }
 }
 
 template <int CS, int N, int MODE>
@@ -648,11 +706,13 @@ template <int CS, int N, int MODE>
 cudaError_t convTc(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src, const __nv_bfloat16* w,
     const float* bias, const __nv_bfloat16* mask, __nv_bfloat16* outBf, float* outF, int* err)
 {
+    // the source [B][H][CS/8][W][8] (channel-group-major), boxes of 136
+    // pixels x all channel groups x 3 rows: one tile's A stage
     CUtensorMap map;
-    const uint64_t dims[4] = { uint64_t(CS), uint64_t(W), uint64_t(H), uint64_t(B) };
-    const uint64_t strides[3] = { uint64_t(CS) * 2, uint64_t(W) * CS * 2, uint64_t(H) * W * CS * 2 };
-    const uint32_t box[4] = { 8, kTcSpan, 1, 1 };
-    cudaError_t e = encodeTiledNd(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, src, 4, dims, strides, box);
+    const uint64_t dims[5] = { 8, uint64_t(W), uint64_t(CS / 8), uint64_t(H), uint64_t(B) };
+    const uint64_t strides[4] = { 16, uint64_t(W) * 16, uint64_t(W) * CS * 2, uint64_t(H) * W * CS * 2 };
+    const uint32_t box[5] = { 8, kTcSpan, uint32_t(CS / 8), 3, 1 };
+    cudaError_t e = encodeTiledNd(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, src, 5, dims, strides, box);
     int dev = 0, sms = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -710,6 +770,7 @@ struct NetImpl {
     // convolutions on tcgen05 (the default) or by mma.sync (NSDG_CONV=mma);
     // the tensor-core kernels' error word (a bounded wait ran out)
     bool tc = true;
+    int wg = 0; // activation layout: 0 channels-last, W channel-group-major (tc)
     int* derr = nullptr;
 };
 
@@ -797,6 +858,7 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
     n->derr = static_cast<int*>(take(4));
     if (const char* env = std::getenv("NSDG_CONV"))
         n->tc = std::strcmp(env, "mma") != 0;
+    n->wg = n->tc ? W : 0;
     // He-normal initial weights, zero biases (host RNG: reproducible)
     std::vector<float> w(n->nParams, 0.f);
     std::mt19937_64 rng(seed);
@@ -920,7 +982,7 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
     float* invDenom = n->lossPart + (long(n->maxB) * n->H * n->W + 255) / 256 + 1;
     kInvDenom<<<1, 1024, 0, s>>>(M, n->used, n->mask, invDenom);
     const unsigned lb = static_cast<unsigned>((M + 255) / 256);
-    kLoss<<<lb, 256, 0, s>>>(M, CL, n->used, n->out, n->target, n->mask, invDenom, n->gA, n->lossPart);
+    kLoss<<<lb, 256, 0, s>>>(M, CL, n->used, n->out, n->target, n->mask, invDenom, n->gA, n->lossPart, n->wg);
     kSumChunks<<<1, 1, 0, s>>>(static_cast<int>(lb), 1, n->lossPart, lossDev);
     const int nChunks = static_cast<int>((M + kChunk - 1) / kChunk);
     __nv_bfloat16* gz = n->gA;
@@ -931,10 +993,10 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
         // weight gradient
         dim3 grid(nChunks, 9);
         NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (kConvWeightGrad<A, Bc><<<grid, kThreads, 0, s>>>(B, n->H, n->W, gz,
-                                                          n->act[l], n->part))));
+                                                          n->act[l], n->part, n->wg))));
         kSumChunks<<<static_cast<unsigned>((nw + 255) / 256), 256, 0, s>>>(nChunks, nw, n->part, n->g32 + n->wOff[l]);
         // bias gradient
-        NSDG_CH_SWITCH(CO, A, (kBiasGradPartial<A><<<nChunks, A, 0, s>>>(M, gz, n->part)));
+        NSDG_CH_SWITCH(CO, A, (kBiasGradPartial<A><<<nChunks, A, 0, s>>>(M, gz, n->part, n->wg)));
         kSumChunks<<<1, CO, 0, s>>>(nChunks, CO, n->part, n->g32 + n->bOff[l]);
         // data gradient times relu' of the layer input (not needed for the network input)
         if (l > 0) {
@@ -967,7 +1029,8 @@ cudaError_t netAdam(NetImpl* n, float lr, float b1, float b2, float eps)
 
 cudaError_t netInputFromFloat(NetImpl* n, long count, const float* dev)
 {
-    kToBf16<<<static_cast<unsigned>((count + 255) / 256), 256, 0, n->stream>>>(count, dev, n->act[0]);
+    kToBf16<<<static_cast<unsigned>((count + 255) / 256), 256, 0, n->stream>>>(count, n->ch[0], n->wg, dev,
+        n->act[0]);
     return cudaGetLastError();
 }
 
@@ -1025,7 +1088,7 @@ __global__ void kWarmFeaturesRaw(WarmState w, float* __restrict__ out)
         out[e * kWarmFeat + k] = f[k];
 }
 
-__global__ void kWarmFeaturesNet(WarmState w, const float* __restrict__ stats, __nv_bfloat16* __restrict__ in)
+__global__ void kWarmFeaturesNet(WarmState w, const float* __restrict__ stats, __nv_bfloat16* __restrict__ in, int wg)
 {
     const size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (e >= w.N)
@@ -1034,7 +1097,8 @@ __global__ void kWarmFeaturesNet(WarmState w, const float* __restrict__ stats, _
     warmFeature(w, e, f);
 #pragma unroll
     for (int k = 0; k < kWarmFeat; ++k)
-        in[e * kWarmFeat + k] = __float2bfloat16_rn((f[k] - stats[k]) * stats[kWarmFeat + k]);
+        in[actChunk(static_cast<long>(e), k >> 3, kWarmFeat, wg) + (k & 7)]
+            = __float2bfloat16_rn((f[k] - stats[k]) * stats[kWarmFeat + k]);
 }
 
 __device__ __forceinline__ void warmCurrent(const WarmState& w, size_t e, float* t)
@@ -1146,7 +1210,7 @@ __global__ void kWarmResidualFinal(size_t nb, const double* __restrict__ partial
 // dataset -> network batch (normalised)
 __global__ void kGatherBatch(long N, int B, const int* __restrict__ idx, const float* __restrict__ X,
     const float* __restrict__ Y, const float* __restrict__ M, const float* __restrict__ stats,
-    __nv_bfloat16* __restrict__ in, float* __restrict__ tgt, float* __restrict__ mask)
+    __nv_bfloat16* __restrict__ in, float* __restrict__ tgt, float* __restrict__ mask, int wg)
 {
     const long t = blockIdx.x * long(blockDim.x) + threadIdx.x;
     if (t >= long(B) * N)
@@ -1156,7 +1220,8 @@ __global__ void kGatherBatch(long N, int B, const int* __restrict__ idx, const f
     const long src = long(idx[b]) * N + p;
 #pragma unroll 4
     for (int k = 0; k < kWarmFeat; ++k)
-        in[t * kWarmFeat + k] = __float2bfloat16_rn((X[src * kWarmFeat + k] - stats[k]) * stats[kWarmFeat + k]);
+        in[actChunk(t, k >> 3, kWarmFeat, wg) + (k & 7)]
+            = __float2bfloat16_rn((X[src * kWarmFeat + k] - stats[k]) * stats[kWarmFeat + k]);
     const float* tShift = stats + 2 * kWarmFeat;
     const float* tScale = tShift + kWarmTgt;
 #pragma unroll 4
@@ -1289,7 +1354,7 @@ cudaError_t launchWarmFeaturesRaw(cudaStream_t s, const WarmState& w, float* out
 }
 cudaError_t launchWarmFeaturesNet(cudaStream_t s, const WarmState& w, NetImpl* net)
 {
-    kWarmFeaturesNet<<<gridOf(w.N), 256, 0, s>>>(w, net->stats, net->act[0]);
+    kWarmFeaturesNet<<<gridOf(w.N), 256, 0, s>>>(w, net->stats, net->act[0], net->wg);
     return cudaGetLastError();
 }
 cudaError_t launchWarmBase(cudaStream_t s, const WarmState& w, float* base, float* mask)
@@ -1438,7 +1503,7 @@ int netTrain(NetImpl* n, int count, int iterations, int batch, float lr, unsigne
         if (e == cudaSuccess) {
             const long T = long(batch) * N;
             kGatherBatch<<<static_cast<unsigned>((T + 255) / 256), 256, 0, n->stream>>>(N, batch, n->dIdx, n->dsX,
-                n->dsY, n->dsM, n->stats, n->act[0], n->target, n->mask);
+                n->dsY, n->dsM, n->stats, n->act[0], n->target, n->mask, n->wg);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = netForward(n, n->stream, batch);
