@@ -1,8 +1,8 @@
 """Dynamics cases run on the reference build and stored as golden fixtures.
 
-Each case is a box test (nextsimdg_gb300.boxtest) stepped through the
-dynamics-kernel interface (initialise, the module's setData calls, update
-with the moving cyclone's wind).  make_ref_goldens.py runs them on the
+Each case is a box test (nextsimdg_gb300.boxtest), or a lon/lat patch on the
+sphere (SphereCase), stepped through the dynamics-kernel interface
+(initialise, the module's setData calls, update with the time-varying wind).  make_ref_goldens.py runs them on the
 reference's own code (oracle/_ref, see oracle/pyref.py) and stores the
 read-outs in ref_dynamics.npz; the tests run the same cases on the
 restated CPU oracle and on the GPU and compare with those read-outs.
@@ -34,12 +34,55 @@ CASES = {
     "bbm_dg3_16x12": dict(rheology=1, dg=3, alpha=1500.0, nx=16, ny=12, steps=2, sub=50),
     "mevp_dg6_a1500_256x256": dict(rheology=0, dg=6, alpha=1500.0, nx=256, ny=256, steps=7, sub=100,
                                    sampled=13),
+    # spherical meshes (coordinates in radians, DynamicsKernel.hpp:44-75)
+    "mevp_sph_dg3_a1500_20x16": dict(rheology=0, dg=3, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
+    "mevp_sph_dg6_a1500_20x16": dict(rheology=0, dg=6, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
 }
+
+
+class SphereCase:
+    """A lon/lat patch (longitudes -0.3..0.3 rad, latitudes 1.0..1.3 rad) with
+    a land border, smooth thickness with seeded noise, a zonal ocean current
+    and a time-varying wind; the same calls as BoxTest."""
+
+    spherical = True
+    dt = 120.0
+
+    def __init__(self, nx: int, ny: int, seed: int = 3):
+        self.nx, self.ny = nx, ny
+        self.lon = np.linspace(-0.3, 0.3, nx + 1)
+        self.lat = np.linspace(1.0, 1.3, ny + 1)
+        cx = 0.5 * (self.lon[:-1] + self.lon[1:])
+        cy = 0.5 * (self.lat[:-1] + self.lat[1:])
+        self.CX, self.CY = np.meshgrid(cx, cy)
+        self.noise = np.random.default_rng(seed).standard_normal(nx * ny)
+
+    def coords(self) -> np.ndarray:
+        X, Y = np.meshgrid(self.lon, self.lat)
+        return np.stack([X.ravel(), Y.ravel()], 1)
+
+    def mask(self) -> np.ndarray:
+        m = np.ones((self.ny, self.nx))
+        m[0, :] = m[-1, :] = 0
+        m[:, 0] = m[:, -1] = 0
+        return m
+
+    def initial_fields(self) -> dict:
+        n = self.nx * self.ny
+        return {"hice": (0.3 + 0.05 * np.sin(9 * self.CX) * np.cos(7 * self.CY)).ravel() + 0.01 * self.noise,
+                "cice": np.full(n, 0.95), "u": np.zeros(n), "v": np.zeros(n),
+                "uocean": 0.05 * np.cos(5 * self.CY).ravel(), "vocean": np.zeros(n), "ssh": np.zeros(n)}
+
+    def wind(self, t: float):
+        s = t / self.dt
+        return (12.0 * np.cos(4 * self.CY + 0.01 * s).ravel(), 6.0 * np.sin(3 * self.CX - 0.02 * s).ravel())
 
 DG0_NAMES = ("hice", "cice", "u", "v", "uiostress", "viostress")
 
 
-def box(case: dict) -> BoxTest:
+def box(case: dict):
+    if case.get("sphere"):
+        return SphereCase(case["nx"], case["ny"])
     b = BoxTest(case["nx"], case["ny"])
     if case.get("holes"):
         m = b.mask()
@@ -53,7 +96,7 @@ def box(case: dict) -> BoxTest:
 def run(kernel, case: dict, b: BoxTest | None = None):
     """initialise, the initial setData calls, then `steps` model steps."""
     b = box(case) if b is None else b
-    kernel.initialise(b.coords(), False, b.mask())
+    kernel.initialise(b.coords(), getattr(b, "spherical", False), b.mask())
     for name, arr in b.initial_fields().items():
         kernel.setData(name, arr)
     if case["rheology"] == 1:

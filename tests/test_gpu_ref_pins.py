@@ -2,7 +2,7 @@
 
 The fixture tests/golden/ref_dynamics.npz holds the read-outs of the
 reference's dynamics code (its unmodified sources built with the project's
-Eigen subset, oracle/_ref) on the box-test cases of
+Eigen subset, oracle/_ref) on the box-test and spherical cases of
 tests/golden/ref_cases.py.  The FP64 path must match every read-out within
 1e-10 of the reference's magnitude; the mixed-precision path within its
 stated tolerance (velocity RMS <= 1e-5 m/s, h and A RMS <= 1e-6).
@@ -18,7 +18,7 @@ TOL = 1e-10
 
 ALL = ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16", "mevp_dg6_a1500_32x32",
        "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64", "mevp_dg3_a1500_64x64", "bbm_dg6_14x14",
-       "bbm_dg3_16x12", "mevp_dg6_a1500_256x256"]
+       "bbm_dg3_16x12", "mevp_dg6_a1500_256x256", "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16"]
 
 
 def _kernel(case, precision):

@@ -10,6 +10,9 @@ restatement (oracle/nsdg_oracle.cpp) must reproduce the fixture
 full mEVP and BBM model steps on box tests, 12 x 12 to 256 x 256, DG 1/3/6,
 alpha = beta = 300 and 1500, land holes, at 1e-10 relative.
 """
+import sys
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -41,7 +44,7 @@ def test_reference_build_reproduces_transport_goldens(goldens):
     assert worst <= 1e-12  # in practice the same to rounding
 
 
-SMALL = ["mevp_dg6_a300_12x12", "mevp_dg1_a300_16x16", "bbm_dg3_16x12"]
+SMALL = ["mevp_dg6_a300_12x12", "mevp_dg1_a300_16x16", "bbm_dg3_16x12", "mevp_sph_dg3_a1500_20x16"]
 
 
 @needs_ref
@@ -59,7 +62,8 @@ def test_fixture_is_the_reference_output(ref_goldens, name):
 @pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16",
                                   "mevp_dg6_a1500_32x32", "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64",
                                   "mevp_dg3_a1500_64x64", "bbm_dg6_14x14", "bbm_dg3_16x12",
-                                  "mevp_dg6_a1500_256x256"])
+                                  "mevp_dg6_a1500_256x256", "mevp_sph_dg3_a1500_20x16",
+                                  "mevp_sph_dg6_a1500_20x16"])
 def test_restatement_matches_reference(oracle, ref_goldens, name):
     """oracle/nsdg_oracle.cpp against the reference's own results: every
     read-out (h, A, damage in all DG components; u, v and the ice-ocean
@@ -75,3 +79,31 @@ def test_restatement_matches_reference(oracle, ref_goldens, name):
     worst = cases.compare(got, data[name])
     assert max(worst.values()) <= TOL, worst
     assert np.abs(data[name]["dg0_u"]).max() > 1e-3  # the case moves the ice
+
+
+@needs_ref
+def test_reference_bbm_diverges_on_a_sphere():
+    """The reference's own BBM kernel on a lon/lat patch: its element size is
+    taken from the raw vertex coordinates, in radians on a sphere
+    (BrittleCGDynamicsKernel.hpp:222 notes the missing latitude), and the
+    first step already blows up (velocities beyond 1e100, negative damage),
+    the second is not finite.  This is why the library refuses BBM on a
+    spherical mesh (NSDG_ERR_UNSUPPORTED) rather than reproduce it."""
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import ref_cases as cases
+    b = cases.SphereCase(14, 12)
+    k = pyref.RefKernel(1, 6, 1500.0, 1500.0, 50)
+    k.initialise(b.coords(), True, b.mask())
+    for name, arr in b.initial_fields().items():
+        k.setData(name, arr)
+    k.setData("damage", np.ones(b.nx * b.ny))
+    worst = []
+    for s in range(2):
+        uw, vw = b.wind(s * b.dt)
+        k.setData("uwind", uw)
+        k.setData("vwind", vw)
+        k.update(s * b.dt, b.dt)
+        u = k.getDG0Data("u")
+        worst.append(float(np.max(np.abs(u))) if np.all(np.isfinite(u)) else float("inf"))
+    k.close()
+    assert worst[0] > 1e50 and worst[1] == float("inf"), worst
