@@ -7,18 +7,27 @@ The reference build (oracle/_ref/libnsdg_ref.so) is made by
 unmodified sources and the project's Eigen subset; this script builds it
 first when the reference sources are found ($NSDG_REFERENCE or the recipe's
 default), then runs every case and stores its read-outs, with the case
-definitions, in one compressed file.
+definitions, in one compressed file.  It runs the reference single-threaded
+(see OMP_NUM_THREADS below).
 
     NSDG_REFERENCE=<reference source tree> python tests/golden/make_ref_goldens.py
 """
 from __future__ import annotations
 
 import json
+import os
 import sys
 import time
 from pathlib import Path
 
 import numpy as np
+
+# One OpenMP thread: the reference's SSH gradient (CGDynamicsKernel.cpp:211-219)
+# advances a counter shared by the threads of a parallel loop, so with more
+# than one thread its CG2 node values (and every result of a case with a
+# non-zero sea-surface height) vary from run to run; single-threaded they are
+# deterministic.  The other cases are the same with any thread count.
+os.environ["OMP_NUM_THREADS"] = "1"
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent

@@ -34,6 +34,10 @@ CASES = {
     "bbm_dg3_16x12": dict(rheology=1, dg=3, alpha=1500.0, nx=16, ny=12, steps=2, sub=50),
     "mevp_dg6_a1500_256x256": dict(rheology=0, dg=6, alpha=1500.0, nx=256, ny=256, steps=7, sub=100,
                                    sampled=13),
+    # a sea-surface height with a gradient (the SSH term of the momentum
+    # equation, CGDynamicsKernel.cpp:126-258)
+    "mevp_dg6_a1500_24x20_ssh": dict(rheology=0, dg=6, alpha=1500.0, nx=24, ny=20, steps=3, sub=100, ssh=0.5),
+    "bbm_dg6_16x14_ssh": dict(rheology=1, dg=6, alpha=1500.0, nx=16, ny=14, steps=2, sub=50, ssh=0.5),
     # spherical meshes (coordinates in radians, DynamicsKernel.hpp:44-75)
     "mevp_sph_dg3_a1500_20x16": dict(rheology=0, dg=3, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
     "mevp_sph_dg6_a1500_20x16": dict(rheology=0, dg=6, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
@@ -84,6 +88,11 @@ def box(case: dict):
     if case.get("sphere"):
         return SphereCase(case["nx"], case["ny"])
     b = BoxTest(case["nx"], case["ny"])
+    if case.get("ssh"):
+        # a tilted, wavy sea surface of the given amplitude (m)
+        X, Y = np.meshgrid((np.arange(b.nx) + 0.5) / b.nx, (np.arange(b.ny) + 0.5) / b.ny)
+        eta = case["ssh"] * (X - 0.5 + 0.3 * np.sin(2 * np.pi * Y) * np.cos(3 * np.pi * X))
+        b.ssh = lambda eta=eta: eta.ravel().copy()
     if case.get("holes"):
         m = b.mask()
         rng = np.random.default_rng(5)

@@ -62,8 +62,8 @@ def test_fixture_is_the_reference_output(ref_goldens, name):
 @pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16",
                                   "mevp_dg6_a1500_32x32", "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64",
                                   "mevp_dg3_a1500_64x64", "bbm_dg6_14x14", "bbm_dg3_16x12",
-                                  "mevp_dg6_a1500_256x256", "mevp_sph_dg3_a1500_20x16",
-                                  "mevp_sph_dg6_a1500_20x16"])
+                                  "mevp_dg6_a1500_256x256", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_16x14_ssh",
+                                  "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16"])
 def test_restatement_matches_reference(oracle, ref_goldens, name):
     """oracle/nsdg_oracle.cpp against the reference's own results: every
     read-out (h, A, damage in all DG components; u, v and the ice-ocean
@@ -107,3 +107,31 @@ def test_reference_bbm_diverges_on_a_sphere():
         worst.append(float(np.max(np.abs(u))) if np.all(np.isfinite(u)) else float("inf"))
     k.close()
     assert worst[0] > 1e50 and worst[1] == float("inf"), worst
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["mevp_dg6_a1500_24x20_ssh", "bbm_dg6_16x14_ssh"])
+def test_reference_ssh_cases_single_threaded(ref_goldens, name):
+    """With a sea-surface height gradient the reference's results depend on
+    its OpenMP thread count: CGDynamicsKernel.cpp:211-219 advances a counter
+    shared by the threads of a parallel loop.  Run on one thread (as the
+    fixtures are made) the reference build is deterministic and reproduces
+    the fixture exactly; the restatement, the GPU path and the fixture follow
+    these serial semantics."""
+    from oracle import pyoracle
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    pyoracle.load()
+    threads = pyoracle.num_threads()
+    pyoracle.set_threads(1)  # the process's OpenMP runtime, shared by both libraries
+    try:
+        runs = []
+        for _ in range(2):
+            k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], case["alpha"], case["sub"])
+            runs.append(cases.readouts(cases.run(k, case), case))
+            k.close()
+    finally:
+        pyoracle.set_threads(threads)
+    for key, want in data[name].items():
+        np.testing.assert_array_equal(runs[0][key], runs[1][key], err_msg=key)
+        np.testing.assert_array_equal(runs[0][key], want, err_msg=key)
