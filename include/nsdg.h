@@ -169,6 +169,28 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
 int nsdg_kernel_get_dg(nsdg_kernel* k, const char* name, double* out,
     size_t n_elements, size_t n_comp);
 
+/* One module step in one call, as MEVPDynamics::update / BBMDynamics::update
+ * (MEVPDynamics.cpp:59-87, BBMDynamics.cpp:63-104) make it with separate
+ * calls: the inputs as nsdg_kernel_set_data takes them, in order, then
+ * nsdg_kernel_update(t_start, dt), then the cell averages of the outputs as
+ * nsdg_kernel_get_dg0 returns them.  Every host buffer has n_elements
+ * (x n_comp) doubles.  The host copies of all inputs are issued at once and
+ * the call waits once, at the end; the results are those of the separate
+ * calls.  Errors as those calls report them; an unknown output name is
+ * NSDG_ERR_UNKNOWN_FIELD before anything is copied.  No reference
+ * counterpart (the reference makes the separate calls). */
+typedef struct nsdg_field_in {
+    const char* name;
+    const double* data;
+    size_t n_comp;
+} nsdg_field_in;
+typedef struct nsdg_field_out {
+    const char* name;
+    double* data;
+} nsdg_field_out;
+int nsdg_kernel_module_step(nsdg_kernel* k, const nsdg_field_in* in, size_t n_in, double t_start, double dt,
+    const nsdg_field_out* out, size_t n_out);
+
 /* One model step of length dt seconds (TimestepTime::step).  The step is
  * enqueued on the handle's CUDA stream (as one CUDA graph) and the call
  * returns without waiting; every get / snapshot / mean-value call waits for

@@ -29,6 +29,7 @@
 #include <cstddef>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace Nextsim {
@@ -109,6 +110,27 @@ namespace GB300 {
         }
 
         void update(const TimestepTime& tst) { check(nsdg_kernel_update(handle, tst.start, tst.step), "update"); }
+
+        //! One module step in one call (nsdg_kernel_module_step): setData of
+        //! every input in order, update, then the cell averages of every
+        //! output into its buffer (nelements() doubles each).
+        void moduleStep(const std::vector<std::pair<std::string, FieldView>>& inputs, const TimestepTime& tst,
+            const std::vector<std::pair<std::string, double*>>& outputs)
+        {
+            std::vector<nsdg_field_in> in;
+            in.reserve(inputs.size());
+            for (const auto& f : inputs) {
+                if (f.second.nElements != nElements)
+                    throw std::invalid_argument("moduleStep: size mismatch for " + f.first);
+                in.push_back({ f.first.c_str(), f.second.data, f.second.nComponents });
+            }
+            std::vector<nsdg_field_out> out;
+            out.reserve(outputs.size());
+            for (const auto& f : outputs)
+                out.push_back({ f.first.c_str(), f.second });
+            check(nsdg_kernel_module_step(handle, in.data(), in.size(), tst.start, tst.step, out.data(), out.size()),
+                "moduleStep");
+        }
 
         //! Waits for the device and reports numeric faults of the last steps.
         void synchronize() { check(nsdg_kernel_synchronize(handle), "synchronize"); }

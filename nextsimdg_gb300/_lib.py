@@ -64,6 +64,18 @@ class BenchmarkForcing(ctypes.Structure):
     ]
 
 
+class FieldIn(ctypes.Structure):
+    """nsdg_field_in (include/nsdg.h)."""
+
+    _fields_ = [("name", c_char_p), ("data", c_void_p), ("n_comp", c_size_t)]
+
+
+class FieldOut(ctypes.Structure):
+    """nsdg_field_out (include/nsdg.h)."""
+
+    _fields_ = [("name", c_char_p), ("data", c_void_p)]
+
+
 class WarmStats(ctypes.Structure):
     """nsdg_warm_stats (include/nsdg.h)."""
 
@@ -103,6 +115,8 @@ SIGNATURES = [
     ("nsdg_kernel_time_kernel", c_int, [c_void_p, c_int, c_int, POINTER(c_float), POINTER(c_char_p)]),
     ("nsdg_kernel_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_kernel_stress_variant", c_int, [c_void_p, POINTER(c_int), POINTER(c_double)]),
+    ("nsdg_kernel_module_step", c_int, [c_void_p, POINTER(FieldIn), c_size_t, c_double, c_double,
+                                        POINTER(FieldOut), c_size_t]),
     ("nsdg_kernel_viscosity_form", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_transport_create", c_int, [c_int, c_size_t, c_size_t, c_void_p, c_void_p,
                                       POINTER(c_void_p), POINTER(c_size_t), c_void_p, c_size_t, c_int,

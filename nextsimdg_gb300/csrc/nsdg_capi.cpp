@@ -173,6 +173,9 @@ struct nsdg_kernel {
     cudaEvent_t converted[2] = { nullptr, nullptr };
     double* stage2 = nullptr;
     int stageSlot = 0;
+    // nsdg_kernel_module_step's staging for all of a step's inputs at once
+    double* moduleStage = nullptr;
+    size_t moduleStageDoubles = 0;
     // graph of one update
     cudaGraphExec_t graph = nullptr;
     double graphDt = -1.0;
@@ -257,6 +260,10 @@ struct nsdg_kernel {
             cudaStreamDestroy(copyStream);
         copyStream = nullptr;
         stageSlot = 0;
+        if (moduleStage)
+            cudaFree(moduleStage);
+        moduleStage = nullptr;
+        moduleStageDoubles = 0;
         if (hErr)
             cudaFreeHost(hErr);
         hErr = nullptr;
@@ -287,6 +294,21 @@ struct nsdg_kernel {
     int captureAuditGraph(double dt, cudaGraph_t& g, int& launches);
     int launchStep(double dt);
     int checkDeviceError();
+    // setData's device target for a field name: CG2 node values (cg, by the
+    // DG -> CG2 interpolation) or DG components (dg, comps of them); neither
+    // for a field that is only stored (DynamicsKernel.hpp:104-109)
+    struct SetTarget {
+        double* cg = nullptr;
+        double* dg = nullptr;
+        int comps = 0;
+    };
+    SetTarget setTarget(const std::string& s);
+    void storeField(const std::string& s, const double* data, size_t nComp);
+    // the conversion of a field copied to `staging` into its target, on `stream`
+    int enqueueConversion(const SetTarget& t, const double* staging, size_t nComp);
+    // the cell averages of a field into host memory `out`: projections and
+    // the copy enqueued on `stream` (a stored field is copied at once)
+    int enqueueReadout(const std::string& s, double* out);
 };
 
 int nsdg_kernel::checkDeviceError()
@@ -1412,6 +1434,60 @@ int nsdg_kernel_benchmark_atmosphere(nsdg_kernel* k, const nsdg_benchmark_forcin
     return r ? r : k->ok();
 }
 
+nsdg_kernel::SetTarget nsdg_kernel::setTarget(const std::string& s)
+{
+    SetTarget t;
+    t.comps = dg;
+    if (s == "u") t.cg = u;
+    else if (s == "v") t.cg = v;
+    else if (s == "uwind") t.cg = ua;
+    else if (s == "vwind") t.cg = va;
+    else if (s == "uocean") t.cg = uo;
+    else if (s == "vocean") t.cg = vo;
+    else if (s == "hice") t.dg = hice;
+    else if (s == "cice") t.dg = cice;
+    else if (s == "ssh") { t.dg = ssh; t.comps = 1; }
+    else if (s == "damage" && rheology == NSDG_RHEOLOGY_BBM) t.dg = damage;
+    return t;
+}
+
+void nsdg_kernel::storeField(const std::string& s, const double* data, size_t nComp)
+{
+    // DynamicsKernel.hpp:104-109: any other name is stored (ma2dg semantics)
+    std::vector<double>& b = bucket[s];
+    b.assign(N * dg, 0.0);
+    if (nComp == size_t(dg))
+        std::memcpy(b.data(), data, N * dg * sizeof(double));
+    else
+        for (size_t i = 0; i < N; ++i)
+            b[i * dg] = data[i * nComp];
+    bucketComps[s] = static_cast<int>(nComp);
+}
+
+int nsdg_kernel::enqueueConversion(const SetTarget& t, const double* staging, size_t nComp)
+{
+    cudaError_t e;
+    if (t.cg && nComp != size_t(dg)) {
+        // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so DG2CG
+        // of the one-component field gives the same node values (the higher
+        // components' contributions are exact zeros)
+        const double* in[1] = { staging };
+        double* out[1] = { t.cg };
+        e = launchDG2CG(stream, dm, 1, 1, in, out);
+    } else if (t.cg) {
+        // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
+        e = launchAosToSoa(stream, N, static_cast<int>(nComp), dg, staging, dgTmp);
+        if (e == cudaSuccess) {
+            const double* in[1] = { dgTmp };
+            double* out[1] = { t.cg };
+            e = launchDG2CG(stream, dm, dg, 1, in, out);
+        }
+    } else {
+        e = launchAosToSoa(stream, N, static_cast<int>(nComp), t.comps, staging, t.dg);
+    }
+    return e == cudaSuccess ? NSDG_OK : fail(NSDG_ERR_CUDA, std::string("set_data convert: ") + cudaGetErrorString(e));
+}
+
 int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, size_t n_elements, size_t n_comp)
 {
     if (!k || !name)
@@ -1424,33 +1500,11 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
         return k->fail(NSDG_ERR_SIZE_MISMATCH, std::string("set_data: size mismatch for ") + name);
     k->readCache = 0;
     const std::string s(name);
-    const int dg = k->dg;
     const size_t N = k->N;
     cudaStream_t st = k->stream;
-    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
-    double* cgTarget = nullptr;
-    if (s == "u") cgTarget = k->u;
-    else if (s == "v") cgTarget = k->v;
-    else if (s == "uwind") cgTarget = k->ua;
-    else if (s == "vwind") cgTarget = k->va;
-    else if (s == "uocean") cgTarget = k->uo;
-    else if (s == "vocean") cgTarget = k->vo;
-    double* dgTarget = nullptr;
-    int targetComps = dg;
-    if (s == "hice") dgTarget = k->hice;
-    else if (s == "cice") dgTarget = k->cice;
-    else if (s == "ssh") { dgTarget = k->ssh; targetComps = 1; }
-    else if (s == "damage" && bbm) dgTarget = k->damage;
-    if (!cgTarget && !dgTarget) {
-        // DynamicsKernel.hpp:104-109: any other name is stored (ma2dg semantics)
-        std::vector<double>& b = k->bucket[s];
-        b.assign(N * dg, 0.0);
-        if (n_comp == size_t(dg))
-            std::memcpy(b.data(), data, N * dg * sizeof(double));
-        else
-            for (size_t i = 0; i < N; ++i)
-                b[i * dg] = data[i * n_comp];
-        k->bucketComps[s] = static_cast<int>(n_comp);
+    const nsdg_kernel::SetTarget target = k->setTarget(s);
+    if (!target.cg && !target.dg) {
+        k->storeField(s, data, n_comp);
         return k->ok();
     }
     auto cu = [&](cudaError_t e, const char* what) {
@@ -1473,27 +1527,8 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
         return r;
     }
     r = cu(cudaStreamWaitEvent(st, k->copied, 0), "set_data wait");
-    if (r == NSDG_OK) {
-        if (cgTarget && n_comp != size_t(dg)) {
-            // CGDynamicsKernel.cpp:54-90: ma2dg keeps component 0 only, so
-            // DG2CG of the one-component field gives the same node values
-            // (the higher components' contributions are exact zeros)
-            const double* in[1] = { staging };
-            double* out[1] = { cgTarget };
-            r = cu(launchDG2CG(st, k->dm, 1, 1, in, out), "set_data DG2CG");
-        } else if (cgTarget) {
-            // CGDynamicsKernel.cpp:54-90: ma2dg into a DG vector, then DG2CG
-            r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), dg, staging, k->dgTmp), "set_data convert");
-            if (r == NSDG_OK) {
-                const double* in[1] = { k->dgTmp };
-                double* out[1] = { cgTarget };
-                r = cu(launchDG2CG(st, k->dm, dg, 1, in, out), "set_data DG2CG");
-            }
-        } else {
-            r = cu(launchAosToSoa(st, N, static_cast<int>(n_comp), targetComps, staging, dgTarget),
-                "set_data convert");
-        }
-    }
+    if (r == NSDG_OK)
+        r = k->enqueueConversion(target, staging, n_comp);
     // recorded after whatever reads this staging buffer, also on a failure
     const cudaError_t er = cudaEventRecord(k->converted[slot], st);
     if (r == NSDG_OK)
@@ -1530,6 +1565,56 @@ int nsdg_kernel_synchronize(nsdg_kernel* k)
     return r ? r : k->ok();
 }
 
+int nsdg_kernel::enqueueReadout(const std::string& s, double* out)
+{
+    const bool bbm = rheology == NSDG_RHEOLOGY_BBM;
+    const double* src = nullptr;
+    cudaError_t e = cudaSuccess;
+    const double* minvP = dops.minvP ? dops.minvP : dops.minv;
+    if (s == "u" || s == "v") {
+        // both components are projected on the first read after a state change
+        if (!(readCache & 1)) {
+            const double* in[2] = { u, v };
+            double* outd[2] = { velx, vely };
+            // only the cell averages are read: component 0 of the projection
+            // (the mixed path's velocity is its FP32 iterate: FP32 quadrature)
+            e = launchCG2DG0(stream, dm, dg, dops.jwA, mixed() ? jwA32 : nullptr, minvP, in, outd);
+            if (e == cudaSuccess)
+                readCache |= 1;
+        }
+        src = (s == "u") ? velx : vely;
+    } else if (s == "uiostress" || s == "viostress") {
+        if (!(readCache & 2)) {
+            const double rad = 0x1.1df46a2529d39p-6;
+            const double ang = bbm ? P.ocean_turning_angle : 0.0;
+            double* tx = cgTmp;
+            double* ty = u0; // reused as scratch outside update
+            e = launchIceOceanStress(stream, Ncg, bbm ? 1 : 0, bbm ? avgU : u, bbm ? avgV : v, uo, vo, P.F_ocean,
+                std::cos(rad * ang), std::sin(rad * ang), tx, ty, mixed());
+            const double* in[2] = { tx, ty };
+            double* outd[2] = { phiA, phiA + size_t(dg) * N };
+            if (e == cudaSuccess)
+                e = launchCG2DG0(stream, dm, dg, dops.jwA, mixed() ? jwA32 : nullptr, minvP, in, outd);
+            if (e == cudaSuccess)
+                readCache |= 2;
+        }
+        src = (s == "uiostress") ? phiA : phiA + size_t(dg) * N;
+    } else if (s == "hice") src = hice;
+    else if (s == "cice") src = cice;
+    else if (s == "damage" && bbm) src = damage;
+    else {
+        auto it = bucket.find(s);
+        if (it == bucket.end())
+            return fail(NSDG_ERR_UNKNOWN_FIELD, "get_dg0: unknown field " + s);
+        for (size_t i = 0; i < N; ++i)
+            out[i] = it->second[i * dg];
+        return NSDG_OK;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, src, N * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    return e == cudaSuccess ? NSDG_OK : fail(NSDG_ERR_CUDA, std::string("get_dg0: ") + cudaGetErrorString(e));
+}
+
 int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_elements)
 {
     if (!k || !name || !out)
@@ -1538,59 +1623,103 @@ int nsdg_kernel_get_dg0(nsdg_kernel* k, const char* name, double* out, size_t n_
         return k->fail(NSDG_ERR_BAD_ARG, "get_dg0: kernel not initialised");
     if (n_elements != k->N)
         return k->fail(NSDG_ERR_SIZE_MISMATCH, "get_dg0: size mismatch");
-    const std::string s(name);
-    const size_t N = k->N;
-    const int dg = k->dg;
-    cudaStream_t st = k->stream;
-    const bool bbm = k->rheology == NSDG_RHEOLOGY_BBM;
-    const double* src = nullptr;
-    cudaError_t e = cudaSuccess;
-    const double* minvP = k->dops.minvP ? k->dops.minvP : k->dops.minv;
-    if (s == "u" || s == "v") {
-        // both components are projected on the first read after a state change
-        if (!(k->readCache & 1)) {
-            const double* in[2] = { k->u, k->v };
-            double* outd[2] = { k->velx, k->vely };
-            // only the cell averages are read: component 0 of the projection
-            // (the mixed path's velocity is its FP32 iterate: FP32 quadrature)
-            e = launchCG2DG0(st, k->dm, dg, k->dops.jwA, k->mixed() ? k->jwA32 : nullptr, minvP, in, outd);
-            if (e == cudaSuccess)
-                k->readCache |= 1;
-        }
-        src = (s == "u") ? k->velx : k->vely;
-    } else if (s == "uiostress" || s == "viostress") {
-        if (!(k->readCache & 2)) {
-            const double rad = 0x1.1df46a2529d39p-6;
-            const double ang = bbm ? k->P.ocean_turning_angle : 0.0;
-            double* tx = k->cgTmp;
-            double* ty = k->u0; // reused as scratch outside update
-            e = launchIceOceanStress(st, k->Ncg, bbm ? 1 : 0, bbm ? k->avgU : k->u, bbm ? k->avgV : k->v,
-                k->uo, k->vo, k->P.F_ocean, std::cos(rad * ang), std::sin(rad * ang), tx, ty, k->mixed());
-            const double* in[2] = { tx, ty };
-            double* outd[2] = { k->phiA, k->phiA + size_t(dg) * N };
-            if (e == cudaSuccess)
-                e = launchCG2DG0(st, k->dm, dg, k->dops.jwA, k->mixed() ? k->jwA32 : nullptr, minvP, in, outd);
-            if (e == cudaSuccess)
-                k->readCache |= 2;
-        }
-        src = (s == "uiostress") ? k->phiA : k->phiA + size_t(dg) * N;
-    } else if (s == "hice") src = k->hice;
-    else if (s == "cice") src = k->cice;
-    else if (s == "damage" && bbm) src = k->damage;
-    else {
-        auto it = k->bucket.find(s);
-        if (it == k->bucket.end())
-            return k->fail(NSDG_ERR_UNKNOWN_FIELD, "get_dg0: unknown field " + s);
-        for (size_t i = 0; i < N; ++i)
-            out[i] = it->second[i * dg];
-        return k->ok();
-    }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(out, src, N * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess)
-        return k->fail(NSDG_ERR_CUDA, std::string("get_dg0: ") + cudaGetErrorString(e));
-    const int r = k->checkDeviceError();
+    int r = k->enqueueReadout(std::string(name), out);
+    if (r)
+        return r;
+    r = k->checkDeviceError();
     return r ? r : k->ok();
+}
+
+// One module step in one call (MEVPDynamics::update / BBMDynamics::update):
+// every input's host copy goes out on the copy stream into one staging pool,
+// the conversions follow on the kernel's stream once all have landed, then
+// the update and every read-out; one wait at the end.  The same kernels as
+// the separate calls, so the same results.
+int nsdg_kernel_module_step(nsdg_kernel* k, const nsdg_field_in* in, size_t n_in, double t_start, double dt,
+    const nsdg_field_out* out, size_t n_out)
+{
+    (void)t_start;
+    if (!k || (n_in && !in) || (n_out && !out))
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "module_step: kernel not initialised");
+    if (!(dt > 0) || !std::isfinite(dt))
+        return k->fail(NSDG_ERR_BAD_ARG, "module_step: dt must be positive");
+    const size_t N = k->N;
+    size_t need = 0;
+    std::vector<nsdg_kernel::SetTarget> targets(n_in);
+    for (size_t i = 0; i < n_in; ++i) {
+        if (!in[i].name || !in[i].data)
+            return k->fail(NSDG_ERR_BAD_ARG, "module_step: null input name or data");
+        if (in[i].n_comp == 0 || in[i].n_comp > 8)
+            return k->fail(NSDG_ERR_SIZE_MISMATCH, std::string("module_step: size mismatch for ") + in[i].name);
+        targets[i] = k->setTarget(in[i].name);
+        if (targets[i].cg || targets[i].dg)
+            need += N * in[i].n_comp;
+    }
+    for (size_t j = 0; j < n_out; ++j) {
+        if (!out[j].name || !out[j].data)
+            return k->fail(NSDG_ERR_BAD_ARG, "module_step: null output name or data");
+        const std::string s(out[j].name);
+        const bool known = s == "u" || s == "v" || s == "uiostress" || s == "viostress" || s == "hice"
+            || s == "cice" || (s == "damage" && k->rheology == NSDG_RHEOLOGY_BBM);
+        bool stored = k->bucket.count(s) > 0;
+        for (size_t i = 0; i < n_in && !stored; ++i)
+            stored = s == in[i].name && !targets[i].cg && !targets[i].dg;
+        if (!known && !stored)
+            return k->fail(NSDG_ERR_UNKNOWN_FIELD, "module_step: unknown field " + s);
+    }
+    auto cu = [&](cudaError_t e, const char* what) {
+        return e == cudaSuccess ? NSDG_OK : k->fail(NSDG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    k->readCache = 0;
+    if (need > k->moduleStageDoubles) {
+        // the pool is read only by this call's conversions, all finished
+        // when the previous call returned
+        if (k->moduleStage)
+            cudaFree(k->moduleStage);
+        k->moduleStage = nullptr;
+        k->moduleStageDoubles = 0;
+        int r = cu(cudaMalloc(&k->moduleStage, need * sizeof(double)), "module_step staging");
+        if (r)
+            return r;
+        k->moduleStageDoubles = need;
+    }
+    int r = NSDG_OK;
+    size_t off = 0;
+    for (size_t i = 0; i < n_in && r == NSDG_OK; ++i) {
+        if (!targets[i].cg && !targets[i].dg) {
+            k->storeField(in[i].name, in[i].data, in[i].n_comp);
+            continue;
+        }
+        r = cu(cudaMemcpyAsync(k->moduleStage + off, in[i].data, N * in[i].n_comp * sizeof(double),
+                   cudaMemcpyHostToDevice, k->copyStream),
+            "module_step copy");
+        off += N * in[i].n_comp;
+    }
+    if (r == NSDG_OK)
+        r = cu(cudaEventRecord(k->copied, k->copyStream), "module_step event");
+    if (r == NSDG_OK)
+        r = cu(cudaStreamWaitEvent(k->stream, k->copied, 0), "module_step wait");
+    if (r) {
+        cudaStreamSynchronize(k->copyStream); // the callers' buffers are read until the copies end
+        return r;
+    }
+    off = 0;
+    for (size_t i = 0; i < n_in && r == NSDG_OK; ++i) {
+        if (!targets[i].cg && !targets[i].dg)
+            continue;
+        r = k->enqueueConversion(targets[i], k->moduleStage + off, in[i].n_comp);
+        off += N * in[i].n_comp;
+    }
+    if (r == NSDG_OK)
+        r = k->launchStep(dt);
+    for (size_t j = 0; j < n_out && r == NSDG_OK; ++j)
+        r = k->enqueueReadout(out[j].name, out[j].data);
+    const int rs = k->checkDeviceError(); // waits for the copies out as well
+    if (r)
+        return r;
+    return rs ? rs : k->ok();
 }
 
 int nsdg_kernel_get_dg(nsdg_kernel* k, const char* name, double* out, size_t n_elements, size_t n_comp)

@@ -242,6 +242,32 @@ class _KernelBase:
         self._check(self._l.nsdg_kernel_get_dg0(self._h, name.encode(), _ptr(out), self.nelements))
         return out
 
+    def module_step(self, t: float, dt: float, inputs: dict, outputs) -> dict:
+        """One module step in one call (nsdg_kernel_module_step): the inputs
+        (name -> array of one value or n_comp values per element, as setData
+        takes them), update(t, dt), then the cell averages of the outputs
+        (names, or name -> preallocated contiguous float64 arrays, as
+        getDG0Data fills them).  Returns name -> array."""
+        keep = []
+        fin = (_lib.FieldIn * max(len(inputs), 1))()
+        for i, (name, arr) in enumerate(inputs.items()):
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            keep.append(a)
+            fin[i].name = name.encode()
+            fin[i].data = a.ctypes.data
+            fin[i].n_comp = 1 if a.ndim == 1 else a.shape[-1]
+        if not isinstance(outputs, dict):
+            outputs = {n: np.empty(self.nelements) for n in outputs}
+        fout = (_lib.FieldOut * max(len(outputs), 1))()
+        for j, (name, buf) in enumerate(outputs.items()):
+            if buf.dtype != np.float64 or not buf.flags.c_contiguous or buf.size != self.nelements:
+                raise ValueError("outputs must be contiguous float64 arrays with one value per element")
+            fout[j].name = name.encode()
+            fout[j].data = buf.ctypes.data
+        self._check(self._l.nsdg_kernel_module_step(self._h, fin, len(inputs), float(t), float(dt), fout,
+                                                    len(outputs)))
+        return outputs
+
     def getDGData(self, name: str, ncomp: int | None = None) -> np.ndarray:
         nc = self.dg if ncomp is None else ncomp
         out = np.empty((self.nelements, nc))

@@ -91,29 +91,40 @@ void GPUDynamicsBase::setData(const ModelState::DataMap& ms)
 void GPUDynamicsBase::update(const TimestepTime& tst)
 {
     GB300::GPUDynamicsKernel<DGCOMP>& k = kernel();
-    if (m_rheology == GB300::Rheology::BBM)
+    const bool bbm = m_rheology == GB300::Rheology::BBM;
+    if (bbm)
         damage = damage0.data();
 
-    k.setData(hiceName, view(hice.data()));
-    k.setData(ciceName, view(cice.data()));
-    if (m_rheology == GB300::Rheology::BBM)
-        k.setData(damageName, view(damage));
-    k.setData(uWindName, view(uwind.data()));
-    k.setData(vWindName, view(vwind.data()));
-    k.setData(uOceanName, view(uocean.data()));
-    k.setData(vOceanName, view(vocean.data()));
-    k.setData(sshName, view(ssh.data()));
+    // the module step of MEVPDynamics.cpp:59-87 / BBMDynamics.cpp:63-104 as
+    // one library call: the same inputs and read-outs, one wait
+    std::vector<std::pair<std::string, GB300::FieldView>> inputs = {
+        { hiceName, view(hice.data()) },
+        { ciceName, view(cice.data()) },
+    };
+    if (bbm)
+        inputs.push_back({ damageName, view(damage) });
+    inputs.insert(inputs.end(),
+        { { uWindName, view(uwind.data()) }, { vWindName, view(vwind.data()) },
+            { uOceanName, view(uocean.data()) }, { vOceanName, view(vocean.data()) }, { sshName, view(ssh.data()) } });
+    const size_t n = k.nelements();
+    std::vector<double> hOut(n), cOut(n), dOut(n), uOut(n), vOut(n), txOut(n), tyOut(n);
+    std::vector<std::pair<std::string, double*>> outputs = { { hiceName, hOut.data() }, { ciceName, cOut.data() } };
+    if (bbm)
+        outputs.push_back({ damageName, dOut.data() });
+    outputs.insert(outputs.end(),
+        { { uName, uOut.data() }, { vName, vOut.data() }, { uIOStressName, txOut.data() },
+            { vIOStressName, tyOut.data() } });
 
-    k.update({ (tst.start - TimePoint()).seconds(), tst.step.seconds() });
+    k.moduleStep(inputs, { (tst.start - TimePoint()).seconds(), tst.step.seconds() }, outputs);
 
-    assign(hice.data(), k.getDG0Data(hiceName));
-    assign(cice.data(), k.getDG0Data(ciceName));
-    if (m_rheology == GB300::Rheology::BBM)
-        assign(damage, k.getDG0Data(damageName));
-    assign(uice, k.getDG0Data(uName));
-    assign(vice, k.getDG0Data(vName));
-    assign(taux, k.getDG0Data(uIOStressName));
-    assign(tauy, k.getDG0Data(vIOStressName));
+    assign(hice.data(), hOut);
+    assign(cice.data(), cOut);
+    if (bbm)
+        assign(damage, dOut);
+    assign(uice, uOut);
+    assign(vice, vOut);
+    assign(taux, txOut);
+    assign(tauy, tyOut);
 }
 
 ModelState GPUDynamicsBase::getStateRecursive(const OutputSpec& os) const

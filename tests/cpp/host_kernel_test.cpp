@@ -1,7 +1,9 @@
 // Drives the C++17 host class (include/nsdg_dynamics_kernel.hpp) the way the
 // reference's MEVPDynamics module drives MEVPDynamicsKernel: initialise, the
-// setData calls, update, getDG0Data.  Inputs are raw FP64 files written by
-// the pytest that runs this program; outputs are written next to them.
+// setData calls, update, getDG0Data; then the same steps through moduleStep
+// (one call per step), which must give the same results.  Inputs are raw FP64
+// files written by the pytest that runs this program; outputs are written
+// next to them.
 #include "nsdg_dynamics_kernel.hpp"
 
 #include <cstdio>
@@ -57,6 +59,37 @@ int main(int argc, char** argv)
     try {
         kernel.getDG0Data("not_a_field");
         std::cerr << "missing std::out_of_range\n";
+        return 1;
+    } catch (const std::out_of_range&) {
+    }
+    // the same steps as one moduleStep call each (the winds as inputs, the
+    // read-outs of the last step as outputs): the same results
+    GPUDynamicsKernel<6> batched(Rheology::MEVP, p);
+    batched.initialise(n, n, { coords.data(), nn, 2 }, false, { mask.data(), N, 1 });
+    for (const char* name : { "hice", "cice", "u", "v", "uocean", "vocean", "ssh" }) {
+        const auto f = readRaw(dir + "/" + name + ".bin", N);
+        batched.setData(name, { f.data(), N, 1 });
+    }
+    const char* outNames[] = { "hice", "cice", "u", "v", "uiostress", "viostress" };
+    std::vector<std::vector<double>> outs(6, std::vector<double>(N));
+    for (int s = 0; s < steps; ++s) {
+        const auto uw = readRaw(dir + "/uwind_" + std::to_string(s) + ".bin", N);
+        const auto vw = readRaw(dir + "/vwind_" + std::to_string(s) + ".bin", N);
+        std::vector<std::pair<std::string, double*>> o;
+        for (int i = 0; i < 6; ++i)
+            o.push_back({ outNames[i], outs[i].data() });
+        batched.moduleStep({ { "uwind", { uw.data(), N, 1 } }, { "vwind", { vw.data(), N, 1 } } },
+            { s * 120.0, 120.0 }, o);
+    }
+    for (int i = 0; i < 6; ++i)
+        if (outs[i] != kernel.getDG0Data(outNames[i])) {
+            std::cerr << "moduleStep differs from the separate calls for " << outNames[i] << "\n";
+            return 1;
+        }
+    try {
+        double dummy = 0.0;
+        batched.moduleStep({}, { 0.0, 120.0 }, { { "not_a_field", &dummy } });
+        std::cerr << "missing std::out_of_range from moduleStep\n";
         return 1;
     } catch (const std::out_of_range&) {
     }

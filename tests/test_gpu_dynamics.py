@@ -614,3 +614,44 @@ def test_full_size_512_within_oracle_sensitivity(gpu, oracle, precision, alpha):
         bar = TOL if sens[n] < 1e-11 else 10.0 * sens[n]
         assert worst[n] <= max(bar, floor), (n, worst, sens)
     assert np.abs(o.getDG0Data("u")).max() > 1e-3
+
+
+@pytest.mark.parametrize("rheology,precision", [("mevp", 0), ("mevp", 1), ("bbm", 0)])
+def test_module_step_matches_separate_calls(gpu, rheology, precision):
+    """nsdg_kernel_module_step (the module step in one call: the inputs,
+    update, the read-outs, one wait) gives bitwise what the separate setData,
+    update and getDG0Data calls give, including a stored (not advected)
+    field passed through; an unknown output is refused before anything is
+    copied."""
+    box = BoxTest(40, 36)
+    bbm = rheology == "bbm"
+    cls = BBMDynamicsKernel if bbm else MEVPDynamicsKernel
+    prm = dict(n_steps=50) if bbm else dict(alpha=300.0, beta=300.0, n_steps=100)
+    ks = []
+    for _ in range(2):
+        k = cls(dg_comp=6, precision=precision, **prm)
+        k.initialise(box.coords(), False, box.mask())
+        for name, arr in box.initial_fields().items():
+            k.setData(name, arr)
+        if bbm:
+            k.setData("damage", box.damage())
+        ks.append(k)
+    sep, bat = ks
+    outs = ["hice", "cice", "u", "v", "uiostress", "viostress"] + (["damage"] if bbm else [])
+    tracer = np.linspace(0.0, 1.0, box.nelements)
+    for s in range(3):
+        uw, vw = box.wind(s * box.dt)
+        h, a = sep.getDG0Data("hice"), sep.getDG0Data("cice")
+        inputs = {"hice": h, "cice": a, "uwind": uw, "vwind": vw, "tracer": tracer + s}
+        for name, arr in inputs.items():
+            sep.setData(name, arr)
+        sep.update(s * box.dt, box.dt)
+        want = {n: sep.getDG0Data(n) for n in outs + ["tracer"]}
+        got = bat.module_step(s * box.dt, box.dt, inputs, outs + ["tracer"])
+        for n in want:
+            np.testing.assert_array_equal(got[n], want[n], err_msg=f"step {s}: {n}")
+    with pytest.raises(NsdgError) as e:
+        bat.module_step(0.0, box.dt, {"uwind": uw}, ["not_a_field"])
+    assert e.value.status == 2  # NSDG_ERR_UNKNOWN_FIELD
+    for k in ks:
+        k.close()
