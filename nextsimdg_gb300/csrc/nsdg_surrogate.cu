@@ -164,29 +164,31 @@ __global__ void __launch_bounds__(kThreads) kConv3x3(int B, int H, int W, const 
 // matrices: pixels (A rows) and output channels (B rows) 16 bytes apart, so
 // 8-row groups are 128 bytes apart (SBO) and one 8-channel group of all rows
 // is one contiguous block (LBO = the block's size).
-//   A: per tile, TMA loads the three input rows y-1, y, y+1 at pixels
-//      x0-1 ... x0+134 (136 pixels, 2176 bytes per 8-channel group; pixels
-//      outside the image read as zero), for every 8-channel group, in one
-//      TMA copy per tile: the activations are stored channel-group-major
-//      (actChunk), which a 5-D box lays out in shared memory exactly as the
-//      MMAs read it, [row][group][pixel][8].  Tap
-//      (dy, dx) is then the same block with its descriptor's start address
-//      moved by dx pixels (16 bytes): no im2col copy.  The data gradient uses
-//      the mirrored taps (2-dy, 2-dx).
+//   A: the input rows, each in one slot of a ring in shared memory: pixels
+//      x0-1 ... x0+134 (136 pixels) of all channel groups, [group][pixel][8]
+//      (2176 bytes per group; pixels and rows outside the image read as zero),
+//      brought by one TMA copy per row: the activations are stored
+//      channel-group-major (actChunk), which a 5-D box lays out in shared
+//      memory exactly as the MMAs read it.  A block walks a vertical strip
+//      of tiles (one 128-pixel column, rows y0 .. y1-1) top to bottom, so
+//      each input row is copied once and serves the three tiles that need
+//      it.  Tap (dy, dx) of row y is the slot of input row y + dy - 1 with
+//      its descriptor's start moved by dx pixels (16 bytes): no im2col.  The
+//      data gradient uses the mirrored taps (2-dy, 2-dx).
 //   B: all 9 taps of the weights, staged once per block.
-// Warp roles: lane 0 of warp 4 loads A stages (a ring of 2-4, as many as
-// fit next to the weights) and issues the MMAs; warps 0-3 read the two TMEM
-// accumulators (warp w: lanes 32w..32w+31, the tile's pixels) and write the
-// tile.  full/empty barriers hand the A stages between the TMA and the
-// MMAs, accFull/accEmpty the accumulators between the MMAs and the
-// epilogue, so loads run ahead while the epilogue of the previous tile
-// overlaps the MMAs of the next.  Every wait is bounded (nsdg_tma.cuh); a
-// wait that runs out sets err and stops the block, whose copies and MMAs
-// still in flight are waited for (bounded) before the TMEM is freed.
+// Warp roles: lane 0 of warp 4 loads the rows and issues the MMAs; warps 0-3
+// read the two TMEM accumulators (warp w: lanes 32w..32w+31, the tile's
+// pixels) and write the tile.  rowFull/rowEmpty barriers hand the slots
+// between the TMA and the MMAs (a row is released by the commit after the
+// last tile that reads it), accFull/accEmpty the accumulators between the
+// MMAs and the epilogue.  Every wait is bounded (nsdg_tma.cuh); a wait that
+// runs out sets err and stops the block, whose copies and MMAs still in
+// flight are waited for (bounded) before the TMEM is freed.
 constexpr int kTcM = 128;
 constexpr int kTcSpan = 136;
 constexpr int kTcEpiWarps = 4;
 constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);
+constexpr int kTcMaxSlots = 8;
 constexpr unsigned kTcRowBytes = kTcSpan * 16; // 17 x 128: every TMA destination 128-byte aligned
 constexpr unsigned kTcCols = 128;              // TMEM columns: two accumulators of up to 64
 constexpr unsigned kTcSmemMax = 232448;        // dynamic shared memory per block (227 KB)
@@ -195,13 +197,13 @@ template <int CS, int N>
 struct TcLayout {
     static constexpr unsigned kGroups = CS / 8;
     static constexpr unsigned kBBytes = 9u * CS * N * 2u;
-    static constexpr unsigned kStageBytes = 3u * kGroups * kTcRowBytes;
+    static constexpr unsigned kSlotBytes = kGroups * kTcRowBytes; // one input row
     static constexpr unsigned kAOff = (kBBytes + 1023u) & ~1023u;
-    static constexpr unsigned kFit = (kTcSmemMax - 1024u - 256u - kAOff) / kStageBytes;
-    static constexpr unsigned kStages = kFit > 4u ? 4u : kFit;
-    static constexpr unsigned kBarOff = kAOff + kStages * kStageBytes;
-    static constexpr unsigned kSmem = kBarOff + 128u + 1024u; // barriers, TMEM address, base alignment
-    static_assert(kStages >= 2, "two A stages must fit");
+    static constexpr unsigned kFit = (kTcSmemMax - 1024u - 256u - kAOff) / kSlotBytes;
+    static constexpr unsigned kSlots = kFit > unsigned(kTcMaxSlots) ? unsigned(kTcMaxSlots) : kFit;
+    static constexpr unsigned kBarOff = kAOff + kSlots * kSlotBytes;
+    static constexpr unsigned kSmem = kBarOff + 256u + 1024u; // barriers, TMEM address, base alignment
+    static_assert(kSlots >= 4, "four row slots must fit");
 };
 
 __device__ __forceinline__ uint64_t ummaDesc(unsigned addr, unsigned lbo, unsigned sbo)
@@ -220,11 +222,9 @@ __host__ __device__ constexpr uint32_t ummaIdescBf16()
     return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
 }
 
-// the A stage of one tile in one copy: pixels x .. x + 135, all 8-channel
-// groups, rows y .. y + 2 of image b of the channel-group-major map
-// [b][y][g][x][8]; in shared memory [row][g][pixel][8], 2176 bytes per
-// (row, group)
-__device__ __forceinline__ void tmaLoadStage(void* dst, const CUtensorMap* map, int x, int y, int b, uint64_t* bar)
+// input row y of image b, pixels x .. x + 135, all channel groups of the
+// channel-group-major map [b][y][g][x][8]: in shared memory [g][pixel][8]
+__device__ __forceinline__ void tmaLoadRow(void* dst, const CUtensorMap* map, int x, int y, int b, uint64_t* bar)
 {
     asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
                  " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smemAddr(dst)),
@@ -267,24 +267,41 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
 __device__ __forceinline__ void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// The work of a block: strips (b, 128-pixel column xt, rows y0 .. y1-1),
+// strip i = blockIdx.x + k gridDim.x; a column holds `ns` strips of `hs` rows.
+struct TcStrip {
+    int b, x0, y0, y1;
+};
+__device__ __forceinline__ TcStrip tcStrip(long i, int H, int tilesX, int hs, int ns)
+{
+    const long col = i / ns;
+    const int st = static_cast<int>(i - col * ns);
+    TcStrip s;
+    s.b = static_cast<int>(col / tilesX);
+    s.x0 = static_cast<int>(col - long(s.b) * tilesX) * kTcM;
+    s.y0 = st * hs;
+    s.y1 = min(H, s.y0 + hs);
+    return s;
+}
+
 template <int CS, int N, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constant__ CUtensorMap srcMap, int B,
-    int H, int W, const __nv_bfloat16* __restrict__ wmat, const float* __restrict__ bias,
+    int H, int W, int hs, int ns, const __nv_bfloat16* __restrict__ wmat, const float* __restrict__ bias,
     const __nv_bfloat16* __restrict__ reluMask, __nv_bfloat16* __restrict__ outBf, float* __restrict__ outF,
     int* __restrict__ err)
 {
     static_assert(CS % 16 == 0 && N % 16 == 0 && N <= 64, "channel counts");
     using Lay = TcLayout<CS, N>;
-    constexpr int S = static_cast<int>(Lay::kStages);
+    constexpr int S = static_cast<int>(Lay::kSlots);
     extern __shared__ __align__(16) unsigned char tcSmemRaw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tcSmemRaw) + 1023) & ~uintptr_t(1023));
     unsigned char* sB = sm;
     unsigned char* sA = sm + Lay::kAOff;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [4] an A stage has landed
-    uint64_t* empty = full + 4;                                      // [4] its MMAs completed
-    uint64_t* accFull = full + 8;                                    // [2] an accumulator is ready
-    uint64_t* accEmpty = full + 10;                                  // [2] ... has been read
-    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(full + 12);
+    uint64_t* rowFull = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [8] a row has landed
+    uint64_t* rowEmpty = rowFull + kTcMaxSlots;                         // [8] its last tile's MMAs completed
+    uint64_t* accFull = rowEmpty + kTcMaxSlots;                         // [2] an accumulator is ready
+    uint64_t* accEmpty = accFull + 2;                                   // [2] ... has been read
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accEmpty + 2);
     __shared__ volatile int abortFlag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -298,8 +315,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0) {
-        for (int i = 0; i < 10; ++i)
-            mbarInit(full + i, 1);
+        for (int i = 0; i < 2 * kTcMaxSlots + 2; ++i)
+            mbarInit(rowFull + i, 1);
         mbarInit(accEmpty, kTcEpiWarps * 32);
         mbarInit(accEmpty + 1, kTcEpiWarps * 32);
         abortFlag = 0;
@@ -317,142 +334,158 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
     const uint32_t tmem = *tmemSlot;
 
     const int tilesX = (W + kTcM - 1) / kTcM;
-    const long tiles = long(B) * H * tilesX;
-    const long T = blockIdx.x < tiles ? (tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-    auto tileOf = [&](long k, int& b, int& y, int& x0) {
-        const long t = blockIdx.x + k * long(gridDim.x);
-        x0 = static_cast<int>(t % tilesX) * kTcM;
-        const long r = t / tilesX;
-        y = static_cast<int>(r % H);
-        b = static_cast<int>(r / H);
-    };
+    const long strips = long(B) * tilesX * ns;
 
     if (warp == kTcEpiWarps) {
         if (lane == 0) {
-            // ---- loads and MMAs ----------------------------------------
+            // ---- rows and MMAs --------------------------------------------
             const uint32_t idesc = ummaIdescBf16<N>();
             const unsigned aBase = smemAddr(sA), bBase = smemAddr(sB);
-            int loadPar[4] = { -1, -1, -1, -1 }; // phase parity of a stage's outstanding loads
-            int lastAcc = -1, lastAccPar = 0;     // the last accumulator committed
-            auto issueLoads = [&](long k, int st) {
-                int b, y, x0;
-                tileOf(k, b, y, x0);
-                uint64_t* bar = full + st;
-                mbarExpectTx(bar, Lay::kStageBytes);
-                tmaLoadStage(sA + st * Lay::kStageBytes, &srcMap, x0 - 1, y - 1, b, bar);
-                loadPar[st] = static_cast<int>((k / S) & 1);
-            };
+            int loadPar[kTcMaxSlots];
+            for (int i = 0; i < kTcMaxSlots; ++i)
+                loadPar[i] = -1; // phase parity of a slot's outstanding copy
+            int lastAcc = -1, lastAccPar = 0;
+            long rowSeq = 0, tileSeq = 0;
             bool ok = true;
-            for (long k = 0; k < T && k < S; ++k)
-                issueLoads(k, static_cast<int>(k));
-            for (long k = 0; k < T && ok; ++k) {
-                if (abortFlag) {
-                    ok = false;
-                    break;
-                }
-                const int st = static_cast<int>(k % S);
-                const int acc = static_cast<int>(k & 1);
-                ok = mbarWaitBounded(full + st, static_cast<unsigned>((k / S) & 1));
-                if (ok)
-                    loadPar[st] = -1;
-                // the accumulator's previous tile has been read (its first
-                // use passes: the barrier's preceding phase counts as done)
-                ok = ok && mbarWaitBounded(accEmpty + acc, static_cast<unsigned>(((k >> 1) & 1) ^ 1));
-                if (!ok)
-                    break;
-                tcFenceAfter();
-                const uint32_t d = tmem + acc * 64;
-                int kk = 0;
+            for (long si = blockIdx.x; si < strips && ok; si += gridDim.x) {
+                const TcStrip sp = tcStrip(si, H, tilesX, hs, ns);
+                const int nt = sp.y1 - sp.y0, nr = nt + 2;
+                const long base = rowSeq;
+                int next = 0; // rows of this strip issued (input rows y0 - 1 + r)
+                auto issueUpTo = [&](int limit) {
+                    for (; ok && next < nr && next < limit; ++next) {
+                        const long q = base + next;
+                        const int slot = static_cast<int>(q % S);
+                        // the slot's previous row has been read by its last tile
+                        ok = mbarWaitBounded(rowEmpty + slot, static_cast<unsigned>(((q / S) & 1) ^ 1));
+                        if (!ok)
+                            break;
+                        mbarExpectTx(rowFull + slot, Lay::kSlotBytes);
+                        tmaLoadRow(sA + slot * Lay::kSlotBytes, &srcMap, sp.x0 - 1, sp.y0 - 1 + next, sp.b,
+                            rowFull + slot);
+                        loadPar[slot] = static_cast<int>((q / S) & 1);
+                    }
+                };
+                for (int t = 0; t < nt && ok; ++t, ++tileSeq) {
+                    if (abortFlag) {
+                        ok = false;
+                        break;
+                    }
+                    issueUpTo(t + S - 1);
+                    // the tile's three rows t, t+1, t+2 of the strip
+                    int slot3[3];
+                    for (int r = 0; r < 3 && ok; ++r) {
+                        const long q = base + t + r;
+                        slot3[r] = static_cast<int>(q % S);
+                        ok = mbarWaitBounded(rowFull + slot3[r], static_cast<unsigned>((q / S) & 1));
+                        if (ok)
+                            loadPar[slot3[r]] = -1;
+                    }
+                    const int acc = static_cast<int>(tileSeq & 1);
+                    // the accumulator's previous tile has been read (its first
+                    // use passes: the barrier's preceding phase counts as done)
+                    ok = ok && mbarWaitBounded(accEmpty + acc, static_cast<unsigned>(((tileSeq >> 1) & 1) ^ 1));
+                    if (!ok)
+                        break;
+                    tcFenceAfter();
+                    const uint32_t d = tmem + acc * 64;
+                    int kk = 0;
 #pragma unroll 1
-                for (int tap = 0; tap < 9; ++tap) {
-                    const int dy = tap / 3, dx = tap % 3;
-                    const int rb = MODE == CONV_BWD_DATA ? 2 - dy : dy;
-                    const int sh = MODE == CONV_BWD_DATA ? 2 - dx : dx;
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int dy = tap / 3, dx = tap % 3;
+                        const int rb = MODE == CONV_BWD_DATA ? 2 - dy : dy;
+                        const int sh = MODE == CONV_BWD_DATA ? 2 - dx : dx;
+                        const unsigned rowAddr = aBase + slot3[rb] * Lay::kSlotBytes + sh * 16;
 #pragma unroll
-                    for (int ks = 0; ks < CS / 16; ++ks, ++kk) {
-                        const uint64_t ad = ummaDesc(aBase + st * Lay::kStageBytes
-                                + (rb * (CS / 8) + 2 * ks) * kTcRowBytes + sh * 16,
-                            kTcRowBytes, 128);
-                        const uint64_t bd = ummaDesc(bBase + (tap * (CS / 8) + 2 * ks) * N * 16, N * 16, 128);
-                        umma(d, ad, bd, idesc, kk > 0);
+                        for (int ks = 0; ks < CS / 16; ++ks, ++kk) {
+                            const uint64_t ad = ummaDesc(rowAddr + 2 * ks * kTcRowBytes, kTcRowBytes, 128);
+                            const uint64_t bd = ummaDesc(bBase + (tap * (CS / 8) + 2 * ks) * N * 16, N * 16, 128);
+                            umma(d, ad, bd, idesc, kk > 0);
+                        }
+                    }
+                    ummaCommit(accFull + acc);
+                    lastAcc = acc;
+                    lastAccPar = static_cast<int>((tileSeq >> 1) & 1);
+                    // row t is last read by tile t; the strip's last tile also
+                    // releases its two lower rows
+                    ummaCommit(rowEmpty + slot3[0]);
+                    if (t == nt - 1) {
+                        ummaCommit(rowEmpty + slot3[1]);
+                        ummaCommit(rowEmpty + slot3[2]);
                     }
                 }
-                ummaCommit(empty + st);
-                ummaCommit(accFull + acc);
-                lastAcc = acc;
-                lastAccPar = static_cast<int>((k >> 1) & 1);
-                // refill the stage of the previous tile (its MMAs went out
-                // one iteration ago) with the tile S - 1 ahead
-                if (k >= 1 && k - 1 + S < T) {
-                    const int sp = static_cast<int>((k - 1) % S);
-                    ok = mbarWaitBounded(empty + sp, static_cast<unsigned>(((k - 1) / S) & 1));
-                    if (ok)
-                        issueLoads(k - 1 + S, sp);
-                }
+                rowSeq += nr;
             }
             if (!ok) {
                 atomicOr(err, 1);
                 abortFlag = 1;
             }
             // nothing of this block may still be in flight when it leaves
-            for (int st = 0; st < S; ++st)
-                if (loadPar[st] >= 0)
-                    mbarWaitBounded(full + st, static_cast<unsigned>(loadPar[st]));
+            for (int slot = 0; slot < S; ++slot)
+                if (loadPar[slot] >= 0)
+                    mbarWaitBounded(rowFull + slot, static_cast<unsigned>(loadPar[slot]));
             if (lastAcc >= 0)
                 mbarWaitBounded(accFull + lastAcc, static_cast<unsigned>(lastAccPar));
         }
     } else {
         // ---- epilogue: warp w holds pixels x0 + 32 w + lane ---------------
-        for (long k = 0; k < T; ++k) {
-            if (__any_sync(0xffffffffu, abortFlag != 0))
-                break;
-            const int acc = static_cast<int>(k & 1);
-            const bool ready = __all_sync(0xffffffffu, mbarWaitBounded(accFull + acc, static_cast<unsigned>((k >> 1) & 1)));
-            if (!ready) {
-                if (lane == 0) {
-                    atomicOr(err, 1);
-                    abortFlag = 1;
+        long tileSeq = 0;
+        bool go = true;
+        for (long si = blockIdx.x; si < strips && go; si += gridDim.x) {
+            const TcStrip sp = tcStrip(si, H, tilesX, hs, ns);
+            for (int y = sp.y0; y < sp.y1; ++y, ++tileSeq) {
+                if (__any_sync(0xffffffffu, abortFlag != 0)) {
+                    go = false;
+                    break;
                 }
-                break;
-            }
-            tcFenceAfter();
-            float v[N];
-            const uint32_t taddr = tmem + acc * 64 + (uint32_t(32 * warp) << 16);
+                const int acc = static_cast<int>(tileSeq & 1);
+                const bool ready
+                    = __all_sync(0xffffffffu, mbarWaitBounded(accFull + acc, static_cast<unsigned>((tileSeq >> 1) & 1)));
+                if (!ready) {
+                    if (lane == 0) {
+                        atomicOr(err, 1);
+                        abortFlag = 1;
+                    }
+                    go = false;
+                    break;
+                }
+                tcFenceAfter();
+                float v[N];
+                const uint32_t taddr = tmem + acc * 64 + (uint32_t(32 * warp) << 16);
 #pragma unroll
-            for (int c = 0; c < N; c += 16)
-                tmemLoad16(taddr + c, v + c);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            tcFenceBefore();
-            mbarArrive(accEmpty + acc);
-            int b, y, x0;
-            tileOf(k, b, y, x0);
-            const int x = x0 + 32 * warp + lane;
-            if (x < W) {
-                const long m = (long(b) * H + y) * W + x;
-                if (MODE == CONV_FWD_LINEAR) {
+                for (int c = 0; c < N; c += 16)
+                    tmemLoad16(taddr + c, v + c);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                tcFenceBefore();
+                mbarArrive(accEmpty + acc);
+                const int x = sp.x0 + 32 * warp + lane;
+                if (x < W) {
+                    const long m = (long(sp.b) * H + y) * W + x;
+                    if (MODE == CONV_FWD_LINEAR) {
 #pragma unroll
-                    for (int n = 0; n < N; n += 4)
-                        *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(v[n] + bias[n],
-                            v[n + 1] + bias[n + 1], v[n + 2] + bias[n + 2], v[n + 3] + bias[n + 3]);
-                } else {
+                        for (int n = 0; n < N; n += 4)
+                            *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(v[n] + bias[n],
+                                v[n + 1] + bias[n + 1], v[n + 2] + bias[n + 2], v[n + 3] + bias[n + 3]);
+                    } else {
 #pragma unroll
-                    for (int n = 0; n < N; n += 8) {
-                        const long off = actChunk(m, n >> 3, N, W);
-                        uint4 mk4 = make_uint4(0, 0, 0, 0);
-                        if (MODE == CONV_BWD_DATA)
-                            mk4 = *reinterpret_cast<const uint4*>(reluMask + off);
-                        const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(&mk4);
-                        __nv_bfloat16 o[8];
+                        for (int n = 0; n < N; n += 8) {
+                            const long off = actChunk(m, n >> 3, N, W);
+                            uint4 mk4 = make_uint4(0, 0, 0, 0);
+                            if (MODE == CONV_BWD_DATA)
+                                mk4 = *reinterpret_cast<const uint4*>(reluMask + off);
+                            const __nv_bfloat16* mk = reinterpret_cast<const __nv_bfloat16*>(&mk4);
+                            __nv_bfloat16 o[8];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            float val = v[n + j];
-                            if (MODE == CONV_FWD_RELU)
-                                val = fmaxf(val + bias[n + j], 0.f);
-                            else
-                                val = __bfloat162float(mk[j]) > 0.f ? val : 0.f;
-                            o[j] = __float2bfloat16_rn(val);
+                            for (int j = 0; j < 8; ++j) {
+                                float val = v[n + j];
+                                if (MODE == CONV_FWD_RELU)
+                                    val = fmaxf(val + bias[n + j], 0.f);
+                                else
+                                    val = __bfloat162float(mk[j]) > 0.f ? val : 0.f;
+                                o[j] = __float2bfloat16_rn(val);
+                            }
+                            *reinterpret_cast<uint4*>(outBf + off) = *reinterpret_cast<const uint4*>(o);
                         }
-                        *reinterpret_cast<uint4*>(outBf + off) = *reinterpret_cast<const uint4*>(o);
                     }
                 }
             }
@@ -707,21 +740,26 @@ cudaError_t convTc(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src
     const float* bias, const __nv_bfloat16* mask, __nv_bfloat16* outBf, float* outF, int* err)
 {
     // the source [B][H][CS/8][W][8] (channel-group-major), boxes of 136
-    // pixels x all channel groups x 3 rows: one tile's A stage
+    // pixels x all channel groups of one row
     CUtensorMap map;
     const uint64_t dims[5] = { 8, uint64_t(W), uint64_t(CS / 8), uint64_t(H), uint64_t(B) };
     const uint64_t strides[4] = { 16, uint64_t(W) * 16, uint64_t(W) * CS * 2, uint64_t(H) * W * CS * 2 };
-    const uint32_t box[5] = { 8, kTcSpan, uint32_t(CS / 8), 3, 1 };
+    const uint32_t box[5] = { 8, kTcSpan, uint32_t(CS / 8), 1, 1 };
     cudaError_t e = encodeTiledNd(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, src, 5, dims, strides, box);
     int dev = 0, sms = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess)
         return e;
-    const long tiles = long(B) * H * ((W + kTcM - 1) / kTcM);
-    const unsigned grid = static_cast<unsigned>(std::min<long>(tiles, sms));
-    kConv3x3Tc<CS, N, MODE><<<grid, kTcThreads, TcLayout<CS, N>::kSmem, s>>>(map, B, H, W, w, bias, mask, outBf,
-        outF, err);
+    // vertical strips: about one per SM, each a 128-pixel column's rows
+    // y0 .. y0 + hs - 1
+    const long columns = long(B) * ((W + kTcM - 1) / kTcM);
+    const int want = static_cast<int>(std::max<long>(1, sms / columns));
+    const int hs = (H + want - 1) / want;
+    const int ns = (H + hs - 1) / hs;
+    const unsigned grid = static_cast<unsigned>(std::min<long>(columns * ns, sms));
+    kConv3x3Tc<CS, N, MODE><<<grid, kTcThreads, TcLayout<CS, N>::kSmem, s>>>(map, B, H, W, hs, ns, w, bias, mask,
+        outBf, outF, err);
     return cudaGetLastError();
 }
 
