@@ -340,7 +340,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
         if (lane == 0) {
             // ---- rows and MMAs --------------------------------------------
             const uint32_t idesc = ummaIdescBf16<N>();
-            const unsigned aBase = smemAddr(sA), bBase = smemAddr(sB);
+            const unsigned aBase = smemAddr(sA);
+            const uint64_t bDesc0 = ummaDesc(smemAddr(sB), N * 16, 128);
             int loadPar[kTcMaxSlots];
             for (int i = 0; i < kTcMaxSlots; ++i)
                 loadPar[i] = -1; // phase parity of a slot's outstanding copy
@@ -389,18 +390,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
                         break;
                     tcFenceAfter();
                     const uint32_t d = tmem + acc * 64;
-                    int kk = 0;
-#pragma unroll 1
+                    // a descriptor's start field is the address / 16, so the
+                    // operands of every tap and K step are the three rows'
+                    // and the weights' descriptors plus constants
+                    const uint64_t aRow[3] = { ummaDesc(aBase + slot3[0] * Lay::kSlotBytes, kTcRowBytes, 128),
+                        ummaDesc(aBase + slot3[1] * Lay::kSlotBytes, kTcRowBytes, 128),
+                        ummaDesc(aBase + slot3[2] * Lay::kSlotBytes, kTcRowBytes, 128) };
+#pragma unroll
                     for (int tap = 0; tap < 9; ++tap) {
                         const int dy = tap / 3, dx = tap % 3;
                         const int rb = MODE == CONV_BWD_DATA ? 2 - dy : dy;
                         const int sh = MODE == CONV_BWD_DATA ? 2 - dx : dx;
-                        const unsigned rowAddr = aBase + slot3[rb] * Lay::kSlotBytes + sh * 16;
 #pragma unroll
-                        for (int ks = 0; ks < CS / 16; ++ks, ++kk) {
-                            const uint64_t ad = ummaDesc(rowAddr + 2 * ks * kTcRowBytes, kTcRowBytes, 128);
-                            const uint64_t bd = ummaDesc(bBase + (tap * (CS / 8) + 2 * ks) * N * 16, N * 16, 128);
-                            umma(d, ad, bd, idesc, kk > 0);
+                        for (int ks = 0; ks < CS / 16; ++ks) {
+                            const uint64_t ad = aRow[rb] + uint64_t(sh + 2 * ks * (kTcRowBytes >> 4));
+                            const uint64_t bd = bDesc0 + uint64_t((tap * (CS / 8) + 2 * ks) * N);
+                            umma(d, ad, bd, idesc, (tap | ks) != 0);
                         }
                     }
                     ummaCommit(accFull + acc);
