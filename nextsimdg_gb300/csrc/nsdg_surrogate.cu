@@ -176,9 +176,10 @@ __global__ void __launch_bounds__(kThreads) kConv3x3(int B, int H, int W, const 
 //      its descriptor's start moved by dx pixels (16 bytes): no im2col.  The
 //      data gradient uses the mirrored taps (2-dy, 2-dx).
 //   B: all 9 taps of the weights, staged once per block.
-// Warp roles: lane 0 of warp 4 loads the rows and issues the MMAs; warps 0-3
-// read the two TMEM accumulators (warp w: lanes 32w..32w+31, the tile's
-// pixels) and write the tile.  rowFull/rowEmpty barriers hand the slots
+// Warp roles: lane 0 of warp 8 loads the rows and issues the MMAs; warps 0-7
+// read the two TMEM accumulators and write the tile: warp w reads TMEM lanes
+// 32 (w % 4) .. + 31 (the tile's pixels) and output channels of half w / 4,
+// two warps per scheduler.  rowFull/rowEmpty barriers hand the slots
 // between the TMA and the MMAs (a row is released by the commit after the
 // last tile that reads it), accFull/accEmpty the accumulators between the
 // MMAs and the epilogue.  Every wait is bounded (nsdg_tma.cuh); a wait that
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(kThreads) kConv3x3(int B, int H, int W, const 
 // flight are waited for (bounded) before the TMEM is freed.
 constexpr int kTcM = 128;
 constexpr int kTcSpan = 136;
-constexpr int kTcEpiWarps = 4;
+constexpr int kTcEpiWarps = 8;
 constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);
 constexpr int kTcMaxSlots = 8;
 constexpr unsigned kTcRowBytes = kTcSpan * 16; // 17 x 128: every TMA destination 128-byte aligned
@@ -264,6 +265,17 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
         v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmemLoad8(uint32_t taddr, float* v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -303,6 +315,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
     uint64_t* accEmpty = accFull + 2;                                   // [2] ... has been read
     uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accEmpty + 2);
     __shared__ volatile int abortFlag;
+    __shared__ float sBias[N];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // the weights in the core-matrix layout: 8-channel group g (tap * CS / 8
@@ -313,6 +326,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
         *reinterpret_cast<uint4*>(sB + size_t(g) * N * 16 + n * 16)
             = *reinterpret_cast<const uint4*>(wmat + size_t(n) * 9 * CS + tap * CS + cg * 8);
     }
+    if (MODE != CONV_BWD_DATA)
+        for (int n = tid; n < N; n += kTcThreads)
+            sBias[n] = bias[n];
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0) {
         for (int i = 0; i < 2 * kTcMaxSlots + 2; ++i)
@@ -433,7 +449,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
                 mbarWaitBounded(accFull + lastAcc, static_cast<unsigned>(lastAccPar));
         }
     } else {
-        // ---- epilogue: warp w holds pixels x0 + 32 w + lane ---------------
+        // ---- epilogue: warp w holds pixels x0 + 32 (w % 4) + lane, output
+        // channels [NH (w / 4), NH (w / 4 + 1)) ----------------------------
+        constexpr int NH = N / 2;
+        const int quarter = warp & 3, half = warp >> 2;
         long tileSeq = 0;
         bool go = true;
         for (long si = blockIdx.x; si < strips && go; si += gridDim.x) {
@@ -455,26 +474,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
                     break;
                 }
                 tcFenceAfter();
-                float v[N];
-                const uint32_t taddr = tmem + acc * 64 + (uint32_t(32 * warp) << 16);
+                float v[NH];
+                const uint32_t taddr = tmem + acc * 64 + half * NH + (uint32_t(32 * quarter) << 16);
 #pragma unroll
-                for (int c = 0; c < N; c += 16)
-                    tmemLoad16(taddr + c, v + c);
+                for (int c = 0; c < NH; c += 8)
+                    tmemLoad8(taddr + c, v + c);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 tcFenceBefore();
                 mbarArrive(accEmpty + acc);
-                const int x = sp.x0 + 32 * warp + lane;
+                const int x = sp.x0 + 32 * quarter + lane;
                 if (x < W) {
-                    const long m = (long(sp.b) * H + y) * W + x;
+                    const long row = long(sp.b) * H + y;
+                    const int n0 = half * NH;
                     if (MODE == CONV_FWD_LINEAR) {
+                        const long m = row * W + x;
 #pragma unroll
-                        for (int n = 0; n < N; n += 4)
-                            *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(v[n] + bias[n],
-                                v[n + 1] + bias[n + 1], v[n + 2] + bias[n + 2], v[n + 3] + bias[n + 3]);
+                        for (int c = 0; c < NH; c += 4) {
+                            const int n = n0 + c;
+                            *reinterpret_cast<float4*>(outF + m * N + n) = make_float4(v[c] + sBias[n],
+                                v[c + 1] + sBias[n + 1], v[c + 2] + sBias[n + 2], v[c + 3] + sBias[n + 3]);
+                        }
                     } else {
 #pragma unroll
-                        for (int n = 0; n < N; n += 8) {
-                            const long off = actChunk(m, n >> 3, N, W);
+                        for (int c = 0; c < NH; c += 8) {
+                            const int n = n0 + c;
+                            // actChunk of pixel (row, x): the row is known
+                            const long off = ((row * (N >> 3) + (n >> 3)) * W + x) * 8;
                             uint4 mk4 = make_uint4(0, 0, 0, 0);
                             if (MODE == CONV_BWD_DATA)
                                 mk4 = *reinterpret_cast<const uint4*>(reluMask + off);
@@ -482,9 +507,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
                             __nv_bfloat16 o[8];
 #pragma unroll
                             for (int j = 0; j < 8; ++j) {
-                                float val = v[n + j];
+                                float val = v[c + j];
                                 if (MODE == CONV_FWD_RELU)
-                                    val = fmaxf(val + bias[n + j], 0.f);
+                                    val = fmaxf(val + sBias[n + j], 0.f);
                                 else
                                     val = __bfloat162float(mk[j]) > 0.f ? val : 0.f;
                                 o[j] = __float2bfloat16_rn(val);
