@@ -110,7 +110,20 @@ def bytes_per_cell_update(n_iter: int = NSTEPS, word: int = 8) -> float:
     return n_iter * (bytes_per_element_iteration_stress(word) + node_per_element) + transport + prepare
 
 
-def launched_bytes_per_cell_update(box, prec: int, stress_kind: str) -> dict:
+def transport_bytes_per_element(tiled: bool, word: int = 4, dg: int = 6) -> int:
+    """Algorithmic DRAM bytes per element of one step's transport (two RK
+    stages of h and A).  Per-element kernel: the cell operators (2 x DG x 9
+    words), the FP64 M^{-1} (DG^2), and per field its coefficients, velocity
+    share, k1 and output (4 x DG FP64).  Tiled parallelogram kernel: per stage
+    the two fields' coefficients, the DG velocity, the diagonal of M^{-1}, the
+    four Jacobian coefficients, one X- and one Y-edge's 3 normal velocities,
+    and the stage output and k1 (written or read) of both fields."""
+    if not tiled:
+        return 2 * (2 * dg * 9 * word + dg * dg * 8 + 2 * (4 * dg * 8)) + 4 * 3 * 8
+    return 2 * (2 * dg * 8 + 2 * dg * 8 + dg * 8 + 4 * 4 + 2 * 3 * 8 + 2 * (2 * dg * 8))
+
+
+def launched_bytes_per_cell_update(box, prec: int, stress_kind: str, tiled_transport: bool = False) -> dict:
     """Algorithmic DRAM bytes per cell-update of the kernels one step
     actually launches (each array counted once per launch), by part:
     100 x (element stress kernel + node momentum kernel) + transport,
@@ -129,16 +142,33 @@ def launched_bytes_per_cell_update(box, prec: int, stress_kind: str) -> dict:
         # two float4 of per-step constants, u and v read and written (FP32)
         node = ncg * (32 + 4 * 4) / N
     # transport of 2 fields in 2 RK stages: cell operators (FP32 on the mixed
-    # path), FP64 inverse mass matrices, phi / k1 / stage I/O, edge velocities
+    # path) or the tiled kernel's coefficients, FP64 inverse mass matrices
+    # (or their diagonal), phi / k1 / stage I/O, edge velocities
     dg = 6
-    cell = 2 * dg * 9 * word
-    transport = 2 * (cell + dg * dg * 8 + 2 * (4 * dg * 8)) + 4 * 3 * 8
+    transport = transport_bytes_per_element(tiled_transport, word, dg)
     # preparation: CG2DG of u, v, DG2CG of h, A, node and element constants
     prepare = 2 * 9 * 8 + 2 * dg * 8 + 9 * 8 + ncg * (12 * 8) / N
     per_iter = stress + node
     total = NSTEPS * per_iter + transport + prepare
     return {"total": total, "per_iteration_stress": stress, "per_iteration_node_share": node,
-            "transport": transport, "prepare": prepare, "stress_kernel": stress_kind}
+            "transport": transport, "prepare": prepare, "stress_kernel": stress_kind,
+            "transport_kernel": "tiled" if tiled_transport else "element"}
+
+
+def transport_record(k, N: int, ms_step: float) -> dict:
+    """The transport stage the step uses, timed alone (CUDA events, 50
+    launches of one RK stage), beside the per-element kernel on the same
+    state, with its algorithmic bandwidth against the measured copy peak."""
+    kind, cell_mismatch, offdiag = k.transport_variant()
+    tms, tname = k.time_kernel(2, 50)
+    ems = k.time_kernel(13, 50)[0]
+    bpe = transport_bytes_per_element(kind == "tiled") // 2
+    hbm, hbm_kind = measured_peaks()
+    ach = N * bpe / (tms * 1e-3) / 1e9
+    return {"name": tname, "kernel": kind, "stage_ms": tms, "element_kernel_stage_ms": ems,
+            "share_of_step": 2 * tms / ms_step, "algorithmic_bytes_per_element_stage": bpe,
+            "achieved_gbs": ach, "peak_gbs": hbm, "frac": ach / hbm, "peak_kind": hbm_kind,
+            "cell_operator_mismatch": cell_mismatch, "minv_offdiag": offdiag}
 
 
 # --------------------------------------------------------------------------
@@ -458,9 +488,11 @@ def distorted_variant(args, local: int) -> dict:
     k.synchronize()
     roof, node = stress_roofline(k, N, 1, ms, local, args.nx)
     kind = k.stress_variant()[0]
+    transport = transport_record(k, N, ms)
     k.close()
     return {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "stress_kernel": kind, "roofline": roof,
-            "node_kernel": node, "mesh": "box test vertices displaced by 3 % of the box (sin x sin)",
+            "node_kernel": node, "transport_kernel": transport,
+            "mesh": "box test vertices displaced by 3 % of the box (sin x sin)",
             "launched_bytes_per_cell_update": launched_bytes_per_cell_update(box, 1, kind)}
 
 
@@ -872,7 +904,10 @@ def run_ours(args, world, rank, local):
     e2e_calls = e2e_call_breakdown(k, e2e_res["cycle"], args.warmup, args.steps) if args.e2e_calls else None
 
     roof, node = stress_roofline(k, N, prec, ms_max / args.steps, local, args.nx)
-    launched = launched_bytes_per_cell_update(box, prec, (k.stress_variant()[0] or "fp64") if prec else "fp64")
+    tiled = k.transport_variant()[0] == "tiled"
+    launched = launched_bytes_per_cell_update(box, prec, (k.stress_variant()[0] or "fp64") if prec else "fp64",
+                                              tiled_transport=tiled)
+    transport = transport_record(k, N, ms_max / args.steps)
     k.close()
 
     variants = {}
@@ -924,9 +959,12 @@ def run_ours(args, world, rank, local):
                                   "the learned warm start is measured in variants.learned_fp32 (1024 x 1024), not enabled here"
                                   if prec else "FP64 throughout (the reference's arithmetic)"),
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2, no flush: each step sweeps the FP32 transport operators "
-                             "(113 MB), the FP64 inverse mass matrices (75 MB) and the FP64 stage buffers, "
-                             "besides the sub-cycle's ~110 MB working set",
+                       "l2": ("inputs larger than L2, no flush: each step sweeps the FP64 DG state, RK stage "
+                              "buffers, transport velocities and M^-1 diagonals (~125 MB at 512^2), besides the "
+                              "sub-cycle's ~110 MB working set" if tiled else
+                              "inputs larger than L2, no flush: each step sweeps the transport cell operators "
+                              "(113 MB in FP32), the FP64 inverse mass matrices (75 MB) and the FP64 stage "
+                              "buffers, besides the sub-cycle's ~110 MB working set"),
                        "bytes_per_cell_update_reference_layout": bytes_per_cell_update(word=4 if prec else 8),
                        "bytes_per_cell_update": launched["total"],
                        "bytes_per_cell_update_parts": launched,
@@ -941,6 +979,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches * args.steps,
             "roofline": roof,
             "node_kernel": node,
+            "transport_kernel": transport,
             "clocks": clk.summary(),
         }
         if err:
@@ -1243,12 +1282,29 @@ def run_day_error(args):
     parts: 256 x 256 mEVP alpha = beta = 1500: the mixed path, the mixed path
            with FP64 transport, the FP64 path with the float-pair stress
            kernel, 360 steps, every 60 (which part of the mixed path carries
-           its excess over the floor)."""
+           its excess over the floor).
+    stability: 512 x 512 mEVP alpha = beta = 300 (the headline day), 720
+           steps, every 60: the FP64 path with h x (1 + k 1e-14), k = 1..4,
+           and the mixed path with each transport kernel and with h x
+           (1 + k 1e-14), k = 1, 2: which of these runs the library flags as
+           non-finite, and when (the configuration is near the mEVP's
+           stability limit on 1 km cells)."""
     from nextsimdg_gb300._lib import NsdgError
     from nextsimdg_gb300.boxtest import BoxTest, step_forcing
     from nextsimdg_gb300.dynamics import BBMDynamicsKernel
     rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
-    if args.day_error == "parts":
+    if args.day_error == "stability":
+        box = BoxTest(512)
+        ks = {"fp64": _day_kernel(box, 0)}
+        for j in range(1, 5):
+            ks[f"fp64_h_x_1p{j}e-14"] = _day_kernel(box, 0, scale=1 + j * 1e-14)
+        ks["mixed"] = _day_kernel(box, 1)
+        ks["mixed_element_transport"] = _day_kernel(box, 1, {"NSDG_TRANSPORT_KERNEL": "element"})
+        for j in (1, 2):
+            ks[f"mixed_h_x_1p{j}e-14"] = _day_kernel(box, 1, scale=1 + j * 1e-14)
+        steps, every, fields = 720, 60, ("u", "v", "hice", "cice")
+        extra = {"grid": "512x512", "alpha": ALPHA}
+    elif args.day_error == "parts":
         box = BoxTest(256)
         ks = {"fp64": _day_kernel(box, 0, alpha=1500.0), "fp64p": _day_kernel(box, 0, scale=1 + 1e-14, alpha=1500.0),
               "mixed": _day_kernel(box, 1, alpha=1500.0),
@@ -1324,9 +1380,9 @@ def main():
     ap.add_argument("--warm-samples", type=int, default=120, help="training samples (every 3rd step)")
     ap.add_argument("--warm-train-iters", type=int, default=2000, help="Adam steps (0: skip the learned variant)")
     ap.add_argument("--no-bbm", action="store_true", help="skip the BBM variant")
-    ap.add_argument("--day-error", choices=["bbm", "parts"],
-                    help="error checkpoints over a simulated day against the FP64 path (BBM at 512^2, or the "
-                         "mixed path's parts at 256^2)")
+    ap.add_argument("--day-error", choices=["bbm", "parts", "stability"],
+                    help="error checkpoints over a simulated day against the FP64 path (BBM at 512^2, the "
+                         "mixed path's parts at 256^2, or perturbed FP64 and mixed runs of the 512^2 day)")
     ap.add_argument("--net-forward", action="store_true",
                     help="time the learned warm start's network forward pass on the --nx grid instead")
     ap.add_argument("--table", action="store_true",

@@ -215,7 +215,8 @@ int nsdg_kernel_mean_value(nsdg_kernel* k, const char* name, double* out);
 int nsdg_kernel_time_updates(nsdg_kernel* k, double dt, int steps, float* ms);
 /* Times `reps` launches of one kernel of the step in isolation on the handle's
  * stream and returns the mean duration.  kernel_id: 0 = element stress kernel,
- * 1 = node momentum kernel, 2 = transport operator; for mixed-precision mEVP
+ * 1 = node momentum kernel, 2 = the transport stage the updates use, 13 = the
+ * per-element transport kernel (kTransportStage); for mixed-precision mEVP
  * also 3 = stress kernel with operators by global loads, 4 = with operator
  * tiles by TMA, and on parallelogram meshes 5, 6, 7 = the coefficient kernel
  * with FP64 viscosity form 0, 1, 2 (see nsdg_selftest_viscosity), 8 = with
@@ -232,6 +233,16 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
  * in FP64, between the exact operators and those rebuilt from parallelogram
  * coefficients (-1 when not evaluated, e.g. spherical or FP64 handles). */
 int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch);
+/* Which transport stage the updates use: *tiled 1 = the parallelogram-mesh
+ * kernel (mixed-precision mEVP on a Cartesian parallelogram mesh without
+ * periodic edges: tiles of 32 x 8 elements, each interior edge flux evaluated
+ * once into shared memory, the cell term from the Jacobian coefficients,
+ * diagonal M^{-1}), 0 = the per-element kernel (NSDG_TRANSPORT_KERNEL=element
+ * before initialise fixes it); *cell_mismatch = the largest relative
+ * difference, in FP64, between the exact cell operators and those rebuilt
+ * from the coefficients, *offdiag = the largest off-diagonal entry of an
+ * element's M^{-1} relative to its diagonal (-1 when not evaluated). */
+int nsdg_kernel_transport_variant(nsdg_kernel* k, int* tiled, double* cell_mismatch, double* offdiag);
 /* The evaluation of P/(8 alpha Delta) in the parallelogram stress kernel:
  * 0 CUDA's rsqrt(double), 1 and 2 one FP64 Newton step from an FP32 seed
  * (2, the default: conversions on the integer pipe), 3 the same step in

@@ -143,6 +143,21 @@ struct nsdg_kernel {
     float* affCoef = nullptr;        // [5][ld] parallelogram coefficients (null: not a parallelogram mesh)
     size_t affLd = 0;
     double affWorst = -1;            // largest relative mismatch of the rebuilt operators (FP64)
+    // mixed path on a parallelogram mesh without periodic edges: the tiled
+    // transport stage (edge fluxes staged in shared memory, cell term from
+    // affCoef, diagonal M^{-1}); NSDG_TRANSPORT_KERNEL=element keeps the
+    // per-element kernel
+    double* minvDiag = nullptr;      // [dg][N]
+    bool trAffine = false;
+    double trAffWorst[2] = { -1, -1 }; // cell-operator mismatch, relative off-diagonal of M^{-1}
+    cudaError_t launchTransport(cudaStream_t s, int mode, double dt, const StageFields& f, bool forceElement = false)
+    {
+        if (trAffine && !forceElement)
+            return launchTransportStageAffine(s, dm, dg, affCoef, affLd, minvDiag, velx, vely, nvX, nvY, mode, dt, f);
+        const bool t32 = mixed() && transport32;
+        return launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY, mode, dt, f,
+            t32 ? cellX32 : nullptr, t32 ? cellY32 : nullptr);
+    }
     cudaError_t launchStress32(cudaStream_t s, const MevpParams& mp, int* errWord, int variant = -1,
         int vm = -1)
     {
@@ -438,6 +453,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(8 * Ncg, 4);                          // the packed per-step node constants
         add(18 * N, 4); add(Ncg, 4); add(Ncg, 4); // start of the previous sub-cycle
         add(9 * N, 4);                            // P/(2 alpha)
+        add(size_t(dg) * N);                      // diagonal of M^{-1} (parallelogram transport)
     }
     if (P.precision == NSDG_PRECISION_MIXED) {
         add(ops.cellX.size(), 4); add(ops.cellY.size(), 4); // FP32 transport operators
@@ -677,6 +693,27 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
                 affLd = ld;
             }
             affWorst = aff.worst;
+            // the transport on the same coefficients: the rebuilt cell
+            // operators within 1e-9 of the exact ones (far below FP32
+            // rounding), M^{-1} diagonal to 1e-12 of its diagonal
+            const char* tk = std::getenv("NSDG_TRANSPORT_KERNEL");
+            if (affCoef && transport32 && flags.perEntry.empty()) {
+                AffineTransportOps atr;
+                const bool fits = buildAffineTransportOps(mesh, ops, 1e-9, 1e-12, atr);
+                trAffWorst[0] = atr.worstCell;
+                trAffWorst[1] = atr.worstOffDiag;
+                if (fits && !(tk && std::strcmp(tk, "element") == 0)) {
+                    minvDiag = arena.take<double>(atr.minvDiag.size());
+                    if (!minvDiag)
+                        e = cudaErrorMemoryAllocation;
+                    else if (e == cudaSuccess)
+                        e = cudaMemcpy(minvDiag, atr.minvDiag.data(), atr.minvDiag.size() * sizeof(double),
+                            cudaMemcpyHostToDevice);
+                    if (e == cudaSuccess)
+                        e = uploadAffineTransportReference(dg, atr.ref);
+                    trAffine = e == cudaSuccess;
+                }
+            }
         }
         auto zf = [&](size_t n) {
             float* p = arena.take<float>(n);
@@ -798,7 +835,8 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         const double* cgv[2] = { bbm ? avgU : u, bbm ? avgV : v };
         double* dgv[2] = { velx, vely };
         if (mixed() && jwA32 && transport32)
-            LCH(launchCG2DG32(s, dm, dg, jwA32, dops.minvP ? dops.minvP : dops.minv, cgv, dgv));
+            LCH(launchCG2DG32(s, dm, dg, jwA32, dops.minvP ? dops.minvP : dops.minv, cgv, dgv,
+                trAffine ? minvDiag : nullptr));
         else
             LCH(launchCG2DG(s, dm, dg, dops.jwA, dops.minvP ? dops.minvP : dops.minv, 2, cgv, dgv));
         LCH(launchNormalVelocity(s, dm, dg, velx, vely, nvX, nvY));
@@ -819,12 +857,8 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
         b.lmax[0] = 1; b.vmax[0] = 1.0; b.lmin[0] = 1; b.vmin[0] = 0.0;  // cice
         b.lmin[1] = 1; b.vmin[1] = 0.0;                                   // hice
         if (bbm) { b.lmax[2] = 1; b.vmax[2] = 1.0; b.lmin[2] = 1; b.vmin[2] = 1e-12; } // damage
-        const float* cx32 = mixed() && transport32 ? cellX32 : nullptr;
-        const float* cy32 = mixed() && transport32 ? cellY32 : nullptr;
-        LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
-            STAGE_RK2_A, dt, a, cx32, cy32));
-        LCH(launchTransportStage(s, dm, dg, dops.cellX, dops.cellY, dops.minv, velx, vely, nvX, nvY,
-            STAGE_RK2_B, dt, b, cx32, cy32));
+        LCH(launchTransport(s, STAGE_RK2_A, dt, a));
+        LCH(launchTransport(s, STAGE_RK2_B, dt, b));
     }
     if (bbm) {
         // stress transport with DGTransport<8> (BrittleCGDynamicsKernel.hpp:98-101)
@@ -1991,21 +2025,20 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
             return k->launchStress32(k->stream, mp, k->derr, 2, kernel_id - 5);
         case 12:
             return k->launchStress32(k->stream, mp, k->derr, 2, 4);
-        default:
-            return launchTransportStage(k->stream, k->dm, k->dg, k->dops.cellX, k->dops.cellY, k->dops.minv,
-                k->velx, k->vely, k->nvX, k->nvY, STAGE_RK2_A, dt, a, k->mixed() ? k->cellX32 : nullptr,
-                k->mixed() ? k->cellY32 : nullptr);
+        default: // 2: the step's transport stage; 13: the per-element transport kernel
+            return k->launchTransport(k->stream, STAGE_RK2_A, dt, a, kernel_id == 13);
         }
     };
     const bool fp64Ids = kernel_id >= 9 && kernel_id <= 11;
     const bool affIds = (kernel_id >= 5 && kernel_id <= 8) || kernel_id == 12;
-    if (kernel_id < 0 || kernel_id > 12 || (((kernel_id >= 3 && kernel_id <= 8) || kernel_id == 12)
+    if (kernel_id < 0 || kernel_id > 13 || (((kernel_id >= 3 && kernel_id <= 8) || kernel_id == 12)
             && (bbm || !k->mixed()))
         || (affIds && !k->affCoef) || (fp64Ids && (bbm || k->mixed()))
         || ((kernel_id == 10 || kernel_id == 11) && !k->opsPairs))
         return k->fail(NSDG_ERR_BAD_ARG,
             "time_kernel: kernel_id must be 0, 1, 2 (3, 4: mixed-precision mEVP; 5-8, 12: on parallelogram meshes; "
-            "9-11: the FP64 mEVP stress kernels, FMA, float pairs and float pairs through TMA)");
+            "9-11: the FP64 mEVP stress kernels, FMA, float pairs and float pairs through TMA; 13: the "
+            "per-element transport kernel)");
     static const char* kStress32Names[3] = { "kMevpStress32", "kMevpStress32Tma", "kMevpStress32Affine" };
     if (name)
         *name = kernel_id == 9 ? "kMevpStress" : kernel_id == 10 ? "kMevpStressPairs"
@@ -2016,7 +2049,8 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
                                                      : k->opsPairs && k->fp64Stress == 1 ? "kMevpStressPairs"
                                                                                          : "kMevpStress")))
             : kernel_id == 1 ? (bbm ? "kBbmMomentum" : (k->mixed() ? "kMevpMomentum32" : "kMevpMomentum"))
-            : kernel_id == 2 ? "kTransportStage"
+            : kernel_id == 2 ? (k->trAffine ? "kTransportStageAffine" : "kTransportStage")
+            : kernel_id == 13 ? "kTransportStage"
             : kStress32Names[kernel_id >= 5 ? 2 : kernel_id - 3]; // 5-8, 12: the coefficient kernel
     cudaEvent_t ea, eb;
     if (cudaEventCreate(&ea) != cudaSuccess || cudaEventCreate(&eb) != cudaSuccess)
@@ -2046,6 +2080,18 @@ int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch)
         return k->fail(NSDG_ERR_BAD_ARG, "stress_variant: kernel not initialised");
     *kind = k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP ? k->stressKind : -1;
     *mismatch = k->affWorst;
+    return k->ok();
+}
+
+int nsdg_kernel_transport_variant(nsdg_kernel* k, int* tiled, double* cell_mismatch, double* offdiag)
+{
+    if (!k || !tiled || !cell_mismatch || !offdiag)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "transport_variant: kernel not initialised");
+    *tiled = k->trAffine ? 1 : 0;
+    *cell_mismatch = k->trAffWorst[0];
+    *offdiag = k->trAffWorst[1];
     return k->ok();
 }
 

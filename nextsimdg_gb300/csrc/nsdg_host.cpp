@@ -491,6 +491,71 @@ bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, d
     return out.worst <= tol;
 }
 
+bool buildAffineTransportOps(const HostMesh& m, const ElementOps& ops, double tol, double offDiagTol,
+    AffineTransportOps& out, unsigned threads)
+{
+    const size_t N = m.nelements();
+    const int dg = ops.dg;
+    const int Q = gaussPoints1d(dg), QQ = Q * Q;
+    out.dg = dg;
+    if (m.spherical || N == 0 || (dg != 1 && dg != 3 && dg != 6) || ops.minv.size() != size_t(dg) * dg * N
+        || ops.cellX.size() != size_t(dg) * QQ * N)
+        return false;
+    // the unit square's cell operators: U_xi and U_eta
+    HostMesh u;
+    u.nx = u.ny = 1;
+    u.vx = { 0.0, 1.0, 0.0, 1.0 };
+    u.vy = { 0.0, 0.0, 1.0, 1.0 };
+    u.ice = { 1 };
+    ElementOps uo;
+    buildTransportOps(u, dg, uo, 1);
+    for (int r = 0; r < dg * QQ; ++r) {
+        out.ref[0][r] = uo.cellX[r];
+        out.ref[1][r] = uo.cellY[r];
+    }
+    out.minvDiag.assign(size_t(dg) * N, 0.0);
+    std::mutex mu;
+    out.worstCell = 0;
+    out.worstOffDiag = 0;
+    parallelFor(N, threads, [&](size_t lo, size_t hi) {
+        double wc = 0, wo = 0;
+        Geom g;
+        for (size_t e = lo; e < hi; ++e) {
+            geometry(m, e, 3, g);
+            const int qc = 4; // the element centre, as for the stress coefficients
+            const double c[4] = { g.deta[1][qc], -g.dxi[1][qc], -g.deta[0][qc], g.dxi[0][qc] };
+            for (int b = 0; b < 2; ++b) {
+                const std::vector<double>& exact = b == 0 ? ops.cellX : ops.cellY;
+                const double k0 = b == 0 ? c[0] : c[2], k1 = b == 0 ? c[1] : c[3];
+                double mx = 0, diff = 0;
+                for (int r = 0; r < dg * QQ; ++r) {
+                    const double x = exact[size_t(r) * N + e];
+                    mx = std::max(mx, std::fabs(x));
+                    diff = std::max(diff, std::fabs(x - (k0 * out.ref[0][r] + k1 * out.ref[1][r])));
+                }
+                if (mx > 0)
+                    wc = std::max(wc, diff / mx);
+            }
+            double dmax = 0, omax = 0;
+            for (int i = 0; i < dg; ++i)
+                for (int j = 0; j < dg; ++j) {
+                    const double x = std::fabs(ops.minv[size_t(i * dg + j) * N + e]);
+                    if (i == j)
+                        dmax = std::max(dmax, x);
+                    else
+                        omax = std::max(omax, x);
+                }
+            wo = std::max(wo, dmax > 0 ? omax / dmax : (omax > 0 ? INFINITY : 0.0));
+            for (int i = 0; i < dg; ++i)
+                out.minvDiag[size_t(i) * N + e] = ops.minv[size_t(i * dg + i) * N + e];
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        out.worstCell = std::max(out.worstCell, wc);
+        out.worstOffDiag = std::max(out.worstOffDiag, wo);
+    });
+    return out.worstCell <= tol && out.worstOffDiag <= offDiagTol;
+}
+
 void buildTransportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads)
 {
     ops.dg = dg;

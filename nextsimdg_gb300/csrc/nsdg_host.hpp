@@ -142,6 +142,26 @@ struct AffineStressOps {
 bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, double tol,
     AffineStressOps& out, unsigned threads = 0);
 
+// Parallelogram meshes, transport: the cell operators of DGTransport
+// (J dT^{-T} grad psi_i w_q, ParametricMap.cpp:13-66) are
+//   cellX = c0 U_xi + c1 U_eta,   cellY = c2 U_xi + c3 U_eta
+// with U_xi[i][q] = w_q dpsi_i/dxi(q), U_eta[i][q] = w_q dpsi_i/deta(q) on
+// the unit square and c the coefficients above, and the mass matrix is J
+// times the unit square's, which the Legendre basis makes diagonal.
+struct AffineTransportOps {
+    int dg = 0;
+    double ref[2][8 * 16] {};     // U_xi [i * Q^2 + q], U_eta
+    std::vector<double> minvDiag; // [dg][N]: the diagonal of each element's M^{-1}
+    double worstCell = 0;         // max relative mismatch of the rebuilt cell operators (FP64)
+    double worstOffDiag = 0;      // max |off-diagonal| / max |diagonal| of M^{-1} over the elements
+};
+// Fills `out` and returns true if the mesh is Cartesian, has the transport
+// operators of `ops.dg` in {1, 3, 6}, every element's cell operators rebuilt
+// from its coefficients match `ops` within `tol` and every M^{-1} is diagonal
+// within `offDiagTol` (relative to its largest diagonal entry).
+bool buildAffineTransportOps(const HostMesh& m, const ElementOps& ops, double tol, double offDiagTol,
+    AffineTransportOps& out, unsigned threads = 0);
+
 // Builds only the transport operators (cellX/Y, minv, jwA, jw3) for a DG
 // degree (used by the stand-alone transport handle).
 void buildTransportOps(const HostMesh& m, int dg, ElementOps& ops, unsigned threads = 0);

@@ -5,6 +5,7 @@
 // so results are bitwise reproducible from run to run (no atomics on data).
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 
 #include "nsdg_host.hpp"
 
@@ -111,8 +112,9 @@ __global__ void __launch_bounds__(kBlock) kCG2DG(int nx, size_t N, const double*
 
 // The same projection for the mixed-precision transport velocity: the CG2
 // values at the Gauss points and the weighted moments against the DG basis in
-// FP32 (jw32: FP32 copy of J w), the inverse mass matrix applied in FP64.
-template <int DG, int NF>
+// FP32 (jw32: FP32 copy of J w), the inverse mass matrix applied in FP64 (on a
+// parallelogram mesh, DIAG: its diagonal, minv = [DG][N]).
+template <int DG, int NF, bool DIAG>
 __global__ void __launch_bounds__(kBlock) kCG2DG32(int nx, size_t N, const float* __restrict__ jw32,
     const double* __restrict__ minv, const double* __restrict__ cg0, const double* __restrict__ cg1,
     double* __restrict__ out0, double* __restrict__ out1)
@@ -157,11 +159,15 @@ __global__ void __launch_bounds__(kBlock) kCG2DG32(int nx, size_t N, const float
         }
 #pragma unroll
         for (int i = 0; i < DG; ++i) {
-            double a = 0.0;
+            if constexpr (DIAG) {
+                out[f][i * N + e] = minv[i * N + e] * r[i];
+            } else {
+                double a = 0.0;
 #pragma unroll
-            for (int k = 0; k < DG; ++k)
-                a += minv[(i * DG + k) * N + e] * r[k];
-            out[f][i * N + e] = a;
+                for (int k = 0; k < DG; ++k)
+                    a += minv[(i * DG + k) * N + e] * r[k];
+                out[f][i * N + e] = a;
+            }
         }
     }
 }
@@ -559,6 +565,99 @@ struct TransportArgs {
     const float* cellY32;
 };
 
+// Dirichlet (closed) boundaries of cell c: outflow only (DGTransport.cpp:306-351)
+template <int DG, int NF, typename T>
+__device__ __forceinline__ void dirichletOutflow(const DevMesh& m, const double* __restrict__ nvX,
+    const double* __restrict__ nvY, size_t c, int ix, int iy, const T (*ownT)[DG], T (*acc)[DG], T dt)
+{
+    constexpr int ED = DGTraits<DG>::ED;
+    const int seg = m.cellSeg[c];
+    if (!seg)
+        return;
+    const int nx = m.nx;
+    T nv[ED], t1[ED], tmp[ED];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        if (!(seg & (1 << s)))
+            continue;
+        const double* nvp = (s == 0 || s == 2) ? nvX : nvY;
+        const size_t ne = (s == 0 || s == 2) ? m.nXe : m.nYe;
+        const size_t e = s == 0 ? size_t(iy) * nx + ix
+            : s == 1          ? size_t(iy) * (nx + 1) + ix + 1
+            : s == 2          ? size_t(iy + 1) * nx + ix
+                              : size_t(iy) * (nx + 1) + ix;
+#pragma unroll
+        for (int k = 0; k < ED; ++k)
+            nv[k] = toT<T>(nvp[k * ne + e]);
+        T vg[ED];
+        edgeGauss<ED, T>(nv, vg);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            if (s == 0) traceBottom<DG, T>(ownT[k], t1);
+            else if (s == 1) traceRight<DG, T>(ownT[k], t1);
+            else if (s == 2) traceTop<DG, T>(ownT[k], t1);
+            else traceLeft<DG, T>(ownT[k], t1);
+            T tg[ED];
+            edgeGauss<ED, T>(t1, tg);
+#pragma unroll
+            for (int g = 0; g < ED; ++g)
+                tmp[g] = tg[g] * ((s == 0 || s == 3) ? fmax(-vg[g], T(0)) : fmax(vg[g], T(0)));
+            addEdge<DG, T>(acc[k], -dt, tmp, s);
+        }
+    }
+}
+
+// The Runge-Kutta combination (FP64) of field k of cell c from its
+// M^{-1}-scaled right-hand side r, the limiters, the store
+// (DGTransport.cpp:498-566)
+template <int DG, typename T>
+__device__ __forceinline__ void finishStage(int mode, const StageFields& f, int k, size_t N, size_t c,
+    const double* own, const double* r)
+{
+    double out[DG];
+    switch (mode) {
+    case STAGE_RK1:
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            out[i] = own[i] + r[i];
+        break;
+    case STAGE_RK2_A:
+#pragma unroll
+        for (int i = 0; i < DG; ++i) {
+            f.k1[k][i * N + c] = r[i];
+            out[i] = f.phi[k][i * N + c] + r[i];
+        }
+        break;
+    case STAGE_RK2_B:
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            out[i] = own[i] + 0.5 * (r[i] - f.k1[k][i * N + c]);
+        break;
+    case STAGE_RK3_A:
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            out[i] = r[i] + f.phi[k][i * N + c];
+        break;
+    case STAGE_RK3_B:
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            out[i] = (r[i] + own[i]) * 0.25 + 0.75 * f.phi[k][i * N + c];
+        break;
+    default: // STAGE_RK3_C
+#pragma unroll
+        for (int i = 0; i < DG; ++i)
+            out[i] = f.phi[k][i * N + c] * (1.0 / 3.0) + 2.0 / 3.0 * (r[i] + own[i]);
+        break;
+    }
+    if (f.lmax[k])
+        limitMax<DG, T>(out, f.vmax[k]);
+    if (f.lmin[k])
+        limitMin<DG, T>(out, f.vmin[k]);
+#pragma unroll
+    for (int i = 0; i < DG; ++i)
+        f.dst[k][i * N + c] = out[i];
+}
+
 // One Runge-Kutta stage of DGTransport for NF fields.  T is the type of the
 // flux arithmetic (cell term, edge traces, upwind fluxes, the accumulated
 // right-hand side): double reproduces the reference's arithmetic; float is
@@ -748,34 +847,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
                 addEdge<DG, T>(acc[k], dt, tmp, type == 0 ? 0 : 3);
         }
     }
-    // Dirichlet (closed) boundaries: outflow only (DGTransport.cpp:306-351)
-    const int seg = m.cellSeg[c];
-    if (seg) {
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-            if (!(seg & (1 << s)))
-                continue;
-            if (s == 0) loadNv(a.nvX, m.nXe, size_t(iy) * nx + ix);
-            else if (s == 1) loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix + 1);
-            else if (s == 2) loadNv(a.nvX, m.nXe, size_t(iy + 1) * nx + ix);
-            else loadNv(a.nvY, m.nYe, size_t(iy) * (nx + 1) + ix);
-            T vg[ED];
-            edgeGauss<ED, T>(nv, vg);
-#pragma unroll
-            for (int k = 0; k < NF; ++k) {
-                if (s == 0) traceBottom<DG, T>(ownT[k], t1);
-                else if (s == 1) traceRight<DG, T>(ownT[k], t1);
-                else if (s == 2) traceTop<DG, T>(ownT[k], t1);
-                else traceLeft<DG, T>(ownT[k], t1);
-                T tg[ED];
-                edgeGauss<ED, T>(t1, tg);
-#pragma unroll
-                for (int g = 0; g < ED; ++g)
-                    tmp[g] = tg[g] * ((s == 0 || s == 3) ? fmax(-vg[g], T(0)) : fmax(vg[g], T(0)));
-                addEdge<DG, T>(acc[k], -dt, tmp, s);
-            }
-        }
-    }
+    dirichletOutflow<DG, NF, T>(m, a.nvX, a.nvY, c, ix, iy, ownT, acc, dt);
     // inverse mass (FP64) and the Runge-Kutta combination (FP64)
     double Mi[DG * DG];
 #pragma unroll
@@ -783,7 +855,7 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
         Mi[i] = a.minv[i * N + c];
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-        double r[DG], out[DG];
+        double r[DG];
 #pragma unroll
         for (int i = 0; i < DG; ++i) {
             double s = 0.0;
@@ -792,47 +864,281 @@ __global__ void __launch_bounds__(kBlock) kTransportStage(TransportArgs a, Stage
                 s += Mi[i * DG + j] * fromT<T>(acc[k][j]);
             r[i] = s;
         }
-        switch (a.mode) {
-        case STAGE_RK1:
+        finishStage<DG, T>(a.mode, f, k, N, c, own[k], r);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same stage on a mesh of parallelograms, FP32 fluxes (mixed precision),
+// by tiles of kTrX x kTrY elements.
+//
+// * The tile's coefficients and a one-cell halo (narrowed to FP32) and the
+//   ice flags are staged in shared memory; each interior edge's upwind flux
+//   at its Gauss points is evaluated once, by one thread, into shared memory,
+//   and read by the two cells it separates (the per-element kernel evaluates
+//   every interior edge twice, once from each side).  Edges on the tile's
+//   border are evaluated by both tiles.
+// * The cell term takes the element's four Jacobian coefficients c0..c3
+//   instead of its 2 x DG x Q^2 operator entries:
+//   sum_q (cellX_iq vx_q + cellY_iq vy_q) phi_q
+//     = sum_q (U_xi,iq (c0 vx_q + c2 vy_q) + U_eta,iq (c1 vx_q + c3 vy_q)) phi_q
+//   with the unit square's U in constant memory.
+// * M^{-1} is diagonal (J M_ref with the Legendre basis): DG FP64 products
+//   per field instead of DG^2.
+// Each cell adds its terms in the per-element kernel's order (cell term,
+// left, right, bottom, top edge, Dirichlet outflow).  Meshes with periodic
+// edges keep the per-element kernel.
+// ---------------------------------------------------------------------------
+constexpr int kTrX = 32, kTrY = 8;
+
+struct AffTransportTables {
+    float u6[2][6][9]; // U_xi, U_eta [i][q] for DG 6 (3 x 3 Gauss points)
+    float u3[2][3][4]; // for DG 3 (2 x 2 Gauss points)
+};
+__constant__ AffTransportTables cTrAff;
+
+template <int DG> __device__ __forceinline__ float trU(int b, int i, int q)
+{
+    if constexpr (DG == 6)
+        return cTrAff.u6[b][i][q];
+    else
+        return cTrAff.u3[b][i][q];
+}
+
+struct TransportAffArgs {
+    DevMesh m;
+    const float* coef; // [5][ld] c0 .. c4
+    size_t ld;
+    const double* minvDiag; // [DG][N]
+    const double* velx;
+    const double* vely;
+    const double* nvX;
+    const double* nvY;
+    double dt;
+    int mode;
+};
+
+template <int DG, int NF>
+__global__ void __launch_bounds__(kTrX * kTrY) kTransportStageAffine(TransportAffArgs a, StageFields f)
+{
+    constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q, ED = DGTraits<DG>::ED;
+    constexpr int SX = kTrX + 2, SY = kTrY + 2;
+    __shared__ float sc[NF][DG][SY][SX];        // coefficients, tile + halo
+    __shared__ uint8_t sIce[SY][SX];            // ice flags (0 outside the grid)
+    __shared__ float fy[NF][ED][kTrY][kTrX + 1]; // upwind Gauss values of the Y-edges (x = x0 .. x0 + kTrX)
+    __shared__ float fx[NF][ED][kTrY + 1][kTrX]; // of the X-edges (y = y0 .. y0 + kTrY)
+    const DevMesh& m = a.m;
+    const size_t N = m.N;
+    const int nx = m.nx, ny = m.ny;
+    const int lx = threadIdx.x, ly = threadIdx.y;
+    const int x0 = blockIdx.x * kTrX, y0 = blockIdx.y * kTrY;
+    const int ix = x0 + lx, iy = y0 + ly;
+    const bool in = ix < nx && iy < ny;
+    const size_t c = in ? size_t(iy) * nx + ix : 0;
+    const float dt = static_cast<float>(a.dt);
+
+    double own[NF][DG];
+    float ownT[NF][DG];
+    bool ice = false;
+    if (in) {
+        ice = m.ice[c] != 0;
 #pragma unroll
-            for (int i = 0; i < DG; ++i)
-                out[i] = own[k][i] + r[i];
-            break;
-        case STAGE_RK2_A:
+        for (int k = 0; k < NF; ++k) {
+            loadCell<DG>(f.src[k], N, c, own[k]);
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                ownT[k][j] = toT<float>(own[k][j]);
+                sc[k][j][ly + 1][lx + 1] = ownT[k][j];
+            }
+        }
+    }
+    sIce[ly + 1][lx + 1] = ice ? 1 : 0;
+    // the halo: bottom and top rows, left and right columns (no corners)
+    const int t = ly * kTrX + lx;
+    if (t < 2 * (kTrX + kTrY)) {
+        int hx, hy;
+        if (t < kTrX) { hx = t + 1; hy = 0; }
+        else if (t < 2 * kTrX) { hx = t - kTrX + 1; hy = SY - 1; }
+        else if (t < 2 * kTrX + kTrY) { hx = 0; hy = t - 2 * kTrX + 1; }
+        else { hx = SX - 1; hy = t - 2 * kTrX - kTrY + 1; }
+        const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+        uint8_t hi = 0;
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+            const size_t cc = size_t(gy) * nx + gx;
+            hi = m.ice[cc] != 0 ? 1 : 0;
+            if (hi) {
+#pragma unroll
+                for (int k = 0; k < NF; ++k)
+#pragma unroll
+                    for (int j = 0; j < DG; ++j)
+                        sc[k][j][hy][hx] = toT<float>(f.src[k][j * N + cc]);
+            }
+        }
+        sIce[hy][hx] = hi;
+    }
+    __syncthreads();
+
+    // upwind fluxes: Y-edge e of tile row r lies between smem cells (r+1, e)
+    // (cell 1, left) and (r+1, e+1) (cell 2, right); X-edge r of tile column
+    // e between (r, e+1) (cell 1, below) and (r+1, e+1) (cell 2, above).  An
+    // edge carries a flux only if both cells are ice, which also excludes the
+    // grid's outer boundary (cells outside the grid are flagged land).
+    auto yEdge = [&](int r, int e) {
+        if (!(sIce[r + 1][e] && sIce[r + 1][e + 1]))
+            return;
+        const size_t ei = size_t(y0 + r) * (nx + 1) + x0 + e;
+        float nv[ED], t1[ED], t2[ED], tmp[ED], cb[DG];
+#pragma unroll
+        for (int g = 0; g < ED; ++g)
+            nv[g] = toT<float>(a.nvY[g * m.nYe + ei]);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                cb[j] = sc[k][j][r + 1][e];
+            traceRight<DG, float>(cb, t1);
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                cb[j] = sc[k][j][r + 1][e + 1];
+            traceLeft<DG, float>(cb, t2);
+            upwind<DG, float>(nv, t1, t2, tmp);
+#pragma unroll
+            for (int g = 0; g < ED; ++g)
+                fy[k][g][r][e] = tmp[g];
+        }
+    };
+    auto xEdge = [&](int r, int e) {
+        if (!(sIce[r][e + 1] && sIce[r + 1][e + 1]))
+            return;
+        const size_t ei = size_t(y0 + r) * nx + x0 + e;
+        float nv[ED], t1[ED], t2[ED], tmp[ED], cb[DG];
+#pragma unroll
+        for (int g = 0; g < ED; ++g)
+            nv[g] = toT<float>(a.nvX[g * m.nXe + ei]);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                cb[j] = sc[k][j][r][e + 1];
+            traceTop<DG, float>(cb, t1);
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                cb[j] = sc[k][j][r + 1][e + 1];
+            traceBottom<DG, float>(cb, t2);
+            upwind<DG, float>(nv, t1, t2, tmp);
+#pragma unroll
+            for (int g = 0; g < ED; ++g)
+                fx[k][g][r][e] = tmp[g];
+        }
+    };
+    yEdge(ly, lx); // the edge left of this thread's cell
+    xEdge(ly, lx); // the edge below it
+    if (t < kTrY)
+        yEdge(t, kTrX); // the tile's right border
+    else if (t < kTrY + kTrX)
+        xEdge(kTrY, t - kTrY); // the tile's top border
+    __syncthreads();
+    if (!in)
+        return;
+
+    float acc[NF][DG];
+#pragma unroll
+    for (int k = 0; k < NF; ++k)
+#pragma unroll
+        for (int j = 0; j < DG; ++j)
+            acc[k][j] = 0.f;
+
+    if constexpr (DG > 1) {
+        if (ice) {
+            float vx[DG], vy[DG], ag[QQ], bg[QQ], pg[NF][QQ];
+#pragma unroll
+            for (int j = 0; j < DG; ++j) {
+                vx[j] = toT<float>(a.velx[j * N + c]);
+                vy[j] = toT<float>(a.vely[j * N + c]);
+            }
+            const float c0 = a.coef[c], c1 = a.coef[a.ld + c], c2 = a.coef[2 * a.ld + c],
+                        c3 = a.coef[3 * a.ld + c];
+#pragma unroll
+            for (int q = 0; q < QQ; ++q) {
+                float sx = 0.f, sy = 0.f;
+#pragma unroll
+                for (int j = 0; j < DG; ++j) {
+                    sx += vx[j] * tab<float>::psi(Q, j, q);
+                    sy += vy[j] * tab<float>::psi(Q, j, q);
+                }
+                ag[q] = c0 * sx + c2 * sy;
+                bg[q] = c1 * sx + c3 * sy;
+#pragma unroll
+                for (int k = 0; k < NF; ++k) {
+                    float sp = 0.f;
+#pragma unroll
+                    for (int j = 0; j < DG; ++j)
+                        sp += ownT[k][j] * tab<float>::psi(Q, j, q);
+                    pg[k][q] = sp;
+                }
+            }
 #pragma unroll
             for (int i = 0; i < DG; ++i) {
-                f.k1[k][i * N + c] = r[i];
-                out[i] = f.phi[k][i * N + c] + r[i];
+                float tt[NF];
+#pragma unroll
+                for (int k = 0; k < NF; ++k)
+                    tt[k] = 0.f;
+#pragma unroll
+                for (int q = 0; q < QQ; ++q) {
+                    const float mq = trU<DG>(0, i, q) * ag[q] + trU<DG>(1, i, q) * bg[q];
+#pragma unroll
+                    for (int k = 0; k < NF; ++k)
+                        tt[k] += mq * pg[k][q];
+                }
+#pragma unroll
+                for (int k = 0; k < NF; ++k)
+                    acc[k][i] += dt * tt[k];
             }
-            break;
-        case STAGE_RK2_B:
-#pragma unroll
-            for (int i = 0; i < DG; ++i)
-                out[i] = own[k][i] + 0.5 * (r[i] - f.k1[k][i * N + c]);
-            break;
-        case STAGE_RK3_A:
-#pragma unroll
-            for (int i = 0; i < DG; ++i)
-                out[i] = r[i] + f.phi[k][i * N + c];
-            break;
-        case STAGE_RK3_B:
-#pragma unroll
-            for (int i = 0; i < DG; ++i)
-                out[i] = (r[i] + own[k][i]) * 0.25 + 0.75 * f.phi[k][i * N + c];
-            break;
-        default: // STAGE_RK3_C
-#pragma unroll
-            for (int i = 0; i < DG; ++i)
-                out[i] = f.phi[k][i * N + c] * (1.0 / 3.0) + 2.0 / 3.0 * (r[i] + own[k][i]);
-            break;
         }
-        if (f.lmax[k])
-            limitMax<DG, T>(out, f.vmax[k]);
-        if (f.lmin[k])
-            limitMin<DG, T>(out, f.vmin[k]);
+    }
+
+    if (ice) {
+        float tmp[ED];
+        const bool left = sIce[ly + 1][lx], right = sIce[ly + 1][lx + 2];
+        const bool below = sIce[ly][lx + 1], above = sIce[ly + 2][lx + 1];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            if (left) {
+#pragma unroll
+                for (int g = 0; g < ED; ++g)
+                    tmp[g] = fy[k][g][ly][lx];
+                addEdge<DG, float>(acc[k], dt, tmp, 3);
+            }
+            if (right) {
+#pragma unroll
+                for (int g = 0; g < ED; ++g)
+                    tmp[g] = fy[k][g][ly][lx + 1];
+                addEdge<DG, float>(acc[k], -dt, tmp, 1);
+            }
+            if (below) {
+#pragma unroll
+                for (int g = 0; g < ED; ++g)
+                    tmp[g] = fx[k][g][ly][lx];
+                addEdge<DG, float>(acc[k], dt, tmp, 0);
+            }
+            if (above) {
+#pragma unroll
+                for (int g = 0; g < ED; ++g)
+                    tmp[g] = fx[k][g][ly + 1][lx];
+                addEdge<DG, float>(acc[k], -dt, tmp, 2);
+            }
+        }
+    }
+    dirichletOutflow<DG, NF, float>(m, a.nvX, a.nvY, c, ix, iy, ownT, acc, dt);
+
+    // diagonal inverse mass (FP64) and the Runge-Kutta combination (FP64)
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        double r[DG];
 #pragma unroll
         for (int i = 0; i < DG; ++i)
-            f.dst[k][i * N + c] = out[i];
+            r[i] = a.minvDiag[i * N + c] * fromT<float>(acc[k][i]);
+        finishStage<DG, float>(a.mode, f, k, N, c, own[k], r);
     }
 }
 
@@ -2534,10 +2840,16 @@ cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* 
 }
 
 cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float* jw32, const double* minv,
-    const double* const* cg, double* const* out)
+    const double* const* cg, double* const* out, const double* minvDiag)
 {
     const unsigned g = blocksFor(m.N);
-    NSDG_DG_SWITCH(dg, (kCG2DG32<D, 2><<<g, kBlock, 0, s>>>(m.nx, m.N, jw32, minv, cg[0], cg[1], out[0], out[1])));
+    if (minvDiag) {
+        NSDG_DG_SWITCH(dg, (kCG2DG32<D, 2, true><<<g, kBlock, 0, s>>>(m.nx, m.N, jw32, minvDiag, cg[0], cg[1],
+                                                                       out[0], out[1])));
+    } else {
+        NSDG_DG_SWITCH(dg, (kCG2DG32<D, 2, false><<<g, kBlock, 0, s>>>(m.nx, m.N, jw32, minv, cg[0], cg[1],
+                                                                        out[0], out[1])));
+    }
     return cudaGetLastError();
 }
 
@@ -2585,6 +2897,54 @@ cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const
     case 3: NSDG_DG_SWITCH(dg, (kTransportStage<D, 3, double><<<g, kBlock, 0, s>>>(a, f))); break;
     default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t uploadAffineTransportReference(int dg, const double ref[2][8 * 16])
+{
+    if (dg == 1)
+        return cudaSuccess;
+    if (dg != 3 && dg != 6)
+        return cudaErrorInvalidValue;
+    const int Q = dg == 6 ? 3 : 2, QQ = Q * Q;
+    if (dg == 6) {
+        float h[2][6][9];
+        for (int b = 0; b < 2; ++b)
+            for (int i = 0; i < 6; ++i)
+                for (int q = 0; q < QQ; ++q)
+                    h[b][i][q] = static_cast<float>(ref[b][i * QQ + q]);
+        return cudaMemcpyToSymbol(cTrAff, h, sizeof(h), offsetof(AffTransportTables, u6));
+    }
+    float h[2][3][4];
+    for (int b = 0; b < 2; ++b)
+        for (int i = 0; i < 3; ++i)
+            for (int q = 0; q < QQ; ++q)
+                h[b][i][q] = static_cast<float>(ref[b][i * QQ + q]);
+    return cudaMemcpyToSymbol(cTrAff, h, sizeof(h), offsetof(AffTransportTables, u3));
+}
+
+cudaError_t launchTransportStageAffine(cudaStream_t s, const DevMesh& m, int dg, const float* coef, size_t ld,
+    const double* minvDiag, const double* velx, const double* vely, const double* nvX, const double* nvY,
+    int mode, double dt, const StageFields& f)
+{
+    TransportAffArgs a { m, coef, ld, minvDiag, velx, vely, nvX, nvY, dt, mode };
+    const dim3 g((m.nx + kTrX - 1) / kTrX, (m.ny + kTrY - 1) / kTrY), b(kTrX, kTrY);
+    if (m.nx <= 0 || m.ny <= 0)
+        return cudaSuccess;
+#define NSDG_TR_AFF(D)                                                                     \
+    switch (f.nf) {                                                                        \
+    case 1: kTransportStageAffine<D, 1><<<g, b, 0, s>>>(a, f); break;                      \
+    case 2: kTransportStageAffine<D, 2><<<g, b, 0, s>>>(a, f); break;                      \
+    case 3: kTransportStageAffine<D, 3><<<g, b, 0, s>>>(a, f); break;                      \
+    default: return cudaErrorInvalidValue;                                                 \
+    }
+    switch (dg) {
+    case 1: NSDG_TR_AFF(1); break;
+    case 3: NSDG_TR_AFF(3); break;
+    case 6: NSDG_TR_AFF(6); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef NSDG_TR_AFF
     return cudaGetLastError();
 }
 

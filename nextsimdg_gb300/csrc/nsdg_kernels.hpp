@@ -94,9 +94,10 @@ cudaError_t launchCG2DG(cudaStream_t s, const DevMesh& m, int dg, const double* 
     const double* minv, int nf, const double* const* cg, double* const* out);
 // CG2DG of two fields with FP32 quadrature (jw32: J w at the advection Gauss
 // points in FP32) and the FP64 inverse mass matrix (the mixed-precision
-// transport velocity).
+// transport velocity); with minvDiag ([dg][N], parallelogram meshes) only
+// the diagonal of M^{-1} is applied.
 cudaError_t launchCG2DG32(cudaStream_t s, const DevMesh& m, int dg, const float* jw32, const double* minv,
-    const double* const* cg, double* const* out);
+    const double* const* cg, double* const* out, const double* minvDiag = nullptr);
 // Cell averages (component 0) of the CG2DG projection of two fields, written
 // to out[0][0..N) and out[1][0..N): FP32 quadrature when jw32 is given (the
 // mixed path), else kCG2DG's FP64 arithmetic.  Row 0 of minv only.
@@ -113,6 +114,15 @@ cudaError_t launchTransportStage(cudaStream_t s, const DevMesh& m, int dg, const
     const double* cellY, const double* minv, const double* velx, const double* vely,
     const double* nvX, const double* nvY, int mode, double dt, const StageFields& f,
     const float* cellX32 = nullptr, const float* cellY32 = nullptr);
+// The same stage on a mesh of parallelograms with FP32 fluxes: tiles of
+// 32 x 8 elements with the edge fluxes staged in shared memory, the cell term
+// from the Jacobian coefficients coef ([5][ld], c0 .. c3 used) and the
+// unit-square operators uploaded by uploadAffineTransportReference, and the
+// diagonal of M^{-1} (minvDiag, [dg][N]).  dg in {1, 3, 6}; no periodic edges.
+cudaError_t uploadAffineTransportReference(int dg, const double ref[2][8 * 16]);
+cudaError_t launchTransportStageAffine(cudaStream_t s, const DevMesh& m, int dg, const float* coef, size_t ld,
+    const double* minvDiag, const double* velx, const double* vely, const double* nvX, const double* nvY,
+    int mode, double dt, const StageFields& f);
 
 // --- interpolation / preparation ----------------------------------------
 // DG -> CG2 Lagrange averaging of nf (<=2) DG fields (Interpolations.cpp:144-204).

@@ -328,6 +328,16 @@ class _KernelBase:
         self._check(self._l.nsdg_kernel_stress_variant(self._h, byref(kind), byref(mism)))
         return (self.STRESS_KERNELS[kind.value] if kind.value >= 0 else None), mism.value
 
+    def transport_variant(self):
+        """(kernel, cell_mismatch, offdiag): the transport stage the updates
+        use ("tiled", the parallelogram-mesh kernel with edge fluxes staged
+        in shared memory, or "element") and the FP64 checks that admit the
+        tiled kernel (rebuilt cell operators' relative mismatch, M^{-1}'s
+        relative off-diagonal; -1 when not evaluated)."""
+        t, cm, od = c_int(), c_double(), c_double()
+        self._check(self._l.nsdg_kernel_transport_variant(self._h, byref(t), byref(cm), byref(od)))
+        return ("tiled" if t.value else "element"), cm.value, od.value
+
     def viscosity_form(self) -> int:
         """The parallelogram stress kernel's evaluation of P/(8 alpha Delta)
         (nsdg_kernel_viscosity_form: 2, the default, the FP64 Newton step;
