@@ -32,7 +32,10 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
                           (IceGrowth + ThermoIce0 + HiblerSpread +
                           ConstantHealing) on the same cell count;
   velocity_error_vs_fp64  one simulated day: FP32 path vs FP64 path, next to
-                          the FP64 path's own response to h x (1 + 1e-14).
+                          the FP64 path's own response to h x (1 + 1e-14),
+                          with the FP64 path at h x (1 + 2e-14) and the FP32
+                          path at h x (1 + 1e-14) beside them (which runs the
+                          library flags non-finite, and when).
 
 --precision fp64 --nx 256 gives the FP64 drop-in path on the 256^2 grid.
 --ensemble 32 times the 32-member uneven ensemble alone.
@@ -747,7 +750,7 @@ def ice_growth_variant(args, N: int):
     return out
 
 
-def day_error(args, box, steps: int, alpha: float = ALPHA, every: int = 120):
+def day_error(args, box, steps: int, alpha: float = ALPHA, every: int = 120, perturbed_runs: bool = False):
     """Velocity / thickness / concentration RMS against the FP64 path every
     `every` model steps up to `steps`: the headline precision path and the
     FP64 path with h scaled by (1 + 1e-14), the floor no implementation can
@@ -755,12 +758,19 @@ def day_error(args, box, steps: int, alpha: float = ALPHA, every: int = 120):
     1 km cells (its iteration needs alpha beta well above zeta dt (pi / dx)^2
     / (rho h)), so a trajectory can go unstable; the library flags the
     non-finite velocity and the run is reported with the checkpoint at which
-    it was flagged, not measured after it."""
+    it was flagged, not measured after it.  perturbed_runs adds the FP64 path
+    with h x (1 + 2e-14) and the FP32 path with h x (1 + 1e-14): whether a
+    run goes unstable within the day depends on the rounding that seeds the
+    growing mode, in either precision."""
     from nextsimdg_gb300._lib import NsdgError
     from nextsimdg_gb300.boxtest import step_forcing
     ks = {"fp64": make_kernel(box, 0, alpha=alpha), "fp64_h_times_1p1e-14": make_kernel(box, 0, scale_h=1 + 1e-14,
                                                                                         alpha=alpha),
           "fp32": make_kernel(box, 1, alpha=alpha)}
+    if perturbed_runs:
+        ks["fp64_h_times_1p2e-14"] = make_kernel(box, 0, scale_h=1 + 2e-14, alpha=alpha)
+        ks["fp32_h_times_1p1e-14"] = make_kernel(box, 1, scale_h=1 + 1e-14, alpha=alpha)
+    compared = [n for n in ks if n != "fp64"]
     failed = {}
     rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
     out = {"steps": steps, "simulated_hours": steps * DT / 3600.0, "alpha": alpha, "cells": box.nelements,
@@ -780,19 +790,20 @@ def day_error(args, box, steps: int, alpha: float = ALPHA, every: int = 120):
                 except NsdgError:
                     failed[n] = s + 1
             cp = {"step": s + 1}
-            for n in ("fp32", "fp64_h_times_1p1e-14"):
+            for n in compared:
                 if n in r and "fp64" in r:
                     x, ref = r[n], r["fp64"]
                     cp[n] = {"u_v_rms_m_per_s": rms(np.hypot(x["u"] - ref["u"], x["v"] - ref["v"])),
                              "h_rms_m": rms(x["hice"] - ref["hice"]), "A_rms": rms(x["cice"] - ref["cice"])}
             out["checkpoints"].append(cp)
     last = out["checkpoints"][-1]
-    for n in ("fp32", "fp64_h_times_1p1e-14"):
+    for n in compared:
         if n in last:
             out[n] = last[n]
         else:
             run = n if n in failed else "fp64"
             out[n] = {"non_finite_by_step": failed.get(run), "run": run}
+    out["non_finite_by_step"] = dict(failed)
     for k in ks.values():
         k.close()
     return out
@@ -938,7 +949,8 @@ def run_ours(args, world, rank, local):
         if prec:
             variants["spherical"] = spherical_variant(args, N, local)
             variants["ice_growth"] = ice_growth_variant(args, N)
-    err = day_error(args, box, args.error_steps) if (prec and args.error_steps > 0 and world == 1) else None
+    err = (day_error(args, box, args.error_steps, every=60, perturbed_runs=True)
+           if (prec and args.error_steps > 0 and world == 1) else None)
     if err is not None and args.nx != 256:
         # the same day on 2 km cells with the reference's default relaxation,
         # where the plain mEVP stays stable

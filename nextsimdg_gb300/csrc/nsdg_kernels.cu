@@ -919,7 +919,7 @@ struct TransportAffArgs {
 };
 
 template <int DG, int NF>
-__global__ void __launch_bounds__(kTrX * kTrY) kTransportStageAffine(TransportAffArgs a, StageFields f)
+__global__ void __launch_bounds__(kTrX * kTrY, 4) kTransportStageAffine(TransportAffArgs a, StageFields f)
 {
     constexpr int Q = DGTraits<DG>::Q, QQ = Q * Q, ED = DGTraits<DG>::ED;
     constexpr int SX = kTrX + 2, SY = kTrY + 2;
@@ -937,20 +937,17 @@ __global__ void __launch_bounds__(kTrX * kTrY) kTransportStageAffine(TransportAf
     const size_t c = in ? size_t(iy) * nx + ix : 0;
     const float dt = static_cast<float>(a.dt);
 
-    double own[NF][DG];
-    float ownT[NF][DG];
+    // the cell's own coefficients live in shared memory (FP32) and are
+    // reloaded in FP64 for the Runge-Kutta combination: fewer registers,
+    // more resident blocks
     bool ice = false;
     if (in) {
         ice = m.ice[c] != 0;
 #pragma unroll
-        for (int k = 0; k < NF; ++k) {
-            loadCell<DG>(f.src[k], N, c, own[k]);
+        for (int k = 0; k < NF; ++k)
 #pragma unroll
-            for (int j = 0; j < DG; ++j) {
-                ownT[k][j] = toT<float>(own[k][j]);
-                sc[k][j][ly + 1][lx + 1] = ownT[k][j];
-            }
-        }
+            for (int j = 0; j < DG; ++j)
+                sc[k][j][ly + 1][lx + 1] = toT<float>(f.src[k][j * N + c]);
     }
     sIce[ly + 1][lx + 1] = ice ? 1 : 0;
     // the halo: bottom and top rows, left and right columns (no corners)
@@ -1073,7 +1070,7 @@ __global__ void __launch_bounds__(kTrX * kTrY) kTransportStageAffine(TransportAf
                     float sp = 0.f;
 #pragma unroll
                     for (int j = 0; j < DG; ++j)
-                        sp += ownT[k][j] * tab<float>::psi(Q, j, q);
+                        sp += sc[k][j][ly + 1][lx + 1] * tab<float>::psi(Q, j, q);
                     pg[k][q] = sp;
                 }
             }
@@ -1129,16 +1126,25 @@ __global__ void __launch_bounds__(kTrX * kTrY) kTransportStageAffine(TransportAf
             }
         }
     }
-    dirichletOutflow<DG, NF, float>(m, a.nvX, a.nvY, c, ix, iy, ownT, acc, dt);
+    if (m.cellSeg[c]) {
+        float ownT[NF][DG];
+#pragma unroll
+        for (int k = 0; k < NF; ++k)
+#pragma unroll
+            for (int j = 0; j < DG; ++j)
+                ownT[k][j] = sc[k][j][ly + 1][lx + 1];
+        dirichletOutflow<DG, NF, float>(m, a.nvX, a.nvY, c, ix, iy, ownT, acc, dt);
+    }
 
     // diagonal inverse mass (FP64) and the Runge-Kutta combination (FP64)
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-        double r[DG];
+        double r[DG], own[DG];
+        loadCell<DG>(f.src[k], N, c, own);
 #pragma unroll
         for (int i = 0; i < DG; ++i)
             r[i] = a.minvDiag[i * N + c] * fromT<float>(acc[k][i]);
-        finishStage<DG, float>(a.mode, f, k, N, c, own[k], r);
+        finishStage<DG, float>(a.mode, f, k, N, c, own, r);
     }
 }
 
