@@ -1268,6 +1268,36 @@ def run_net_forward(args):
     net.close()
 
 
+def run_net_train(args):
+    """One training step of the same network on one nx x nx grid (forward,
+    loss, backward: the weight, bias and data gradients; the Adam update):
+    wall-clock milliseconds per step (each step ends with the loss read back,
+    so the steps do not overlap), after the warm-up steps."""
+    from nextsimdg_gb300 import surrogate
+    n = args.nx
+    net = surrogate.warm_net(n, n, seed=1)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1, n, n, net.channels[0])).astype(np.float32)
+    t = rng.standard_normal((1, n, n, net.channels[-1])).astype(np.float32)
+    net.set_batch(x, t, np.ones((1, n, n), dtype=np.float32))
+    for _ in range(max(args.warmup, 3)):
+        net.loss_backward()
+        net.adam_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.loss_backward()
+        net.adam_step()
+    net.loss_backward()  # the last Adam update has been applied when this returns
+    ms = (time.perf_counter() - t0) * 1e3 / (args.steps + 1)
+    ch = net.channels
+    flops = 3 * 2.0 * n * n * sum(9 * ch[i] * ch[i + 1] for i in range(len(ch) - 1))
+    print(json.dumps({"net_train_step": True, "grid": f"{n}x{n}", "channels": list(ch), "ms_per_step": ms,
+                      "gflop_per_step": flops / 1e9, "steps": args.steps,
+                      "note": "forward + weight and data gradients (3 x the forward's GEMM FLOPs) + Adam"}),
+          flush=True)
+    net.close()
+
+
 def _day_kernel(box, prec: int, env: dict | None = None, scale: float = 1.0, alpha: float = ALPHA):
     """make_kernel with the library's selection variables set while the
     kernel is created (they are read at creation)."""
@@ -1395,6 +1425,8 @@ def main():
     ap.add_argument("--day-error", choices=["bbm", "parts", "stability"],
                     help="error checkpoints over a simulated day against the FP64 path (BBM at 512^2, the "
                          "mixed path's parts at 256^2, or perturbed FP64 and mixed runs of the 512^2 day)")
+    ap.add_argument("--net-train", action="store_true",
+                    help="time one training step of the learned warm start's network on the --nx grid instead")
     ap.add_argument("--net-forward", action="store_true",
                     help="time the learned warm start's network forward pass on the --nx grid instead")
     ap.add_argument("--table", action="store_true",
@@ -1406,6 +1438,8 @@ def main():
     world, rank, local = dist_setup()
     if args.net_forward:
         run_net_forward(args)
+    elif args.net_train:
+        run_net_train(args)
     elif args.day_error:
         run_day_error(args)
     elif args.table:

@@ -529,6 +529,219 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
     }
 }
 
+// ---------------------------------------------------------------------------
+// The weight gradient on the tensor cores:
+//   part[blk][co][tap*CI + ci] = sum over the block's pixels p of
+//                                x[p + (dy-1, dx-1)][ci] gz[p][co]
+// One MMA: M = 128 rows of input channels (rows CI .. 127 read whatever lies
+// beyond the row in shared memory and are discarded), N = CO, K = 16 pixels.
+// Both operands are MN-major and come straight from the channel-group-major
+// rows ([g][pixel][8]: 8 channels of one pixel in 16 bytes), no transposes:
+//   A: the input row y + dy - 1 in a ring slot (pixels x0-1 .. x0+134, the
+//      forward kernel's rows), start moved by dx pixels; 8-channel groups
+//      2176 bytes apart (SBO), 8-pixel groups 128 bytes apart (LBO);
+//   B: gz row y, pixels x0 .. x0+127, one TMA copy into one of two buffers;
+//      groups 2048 bytes apart, 8-pixel groups 128 bytes apart.
+// Nine accumulators (one per tap) of CO columns stay in TMEM while the block
+// walks its strips (each a 128-pixel column's rows y0 .. y1-1; each input row
+// copied once and used by three rows of gz), and are read once at the end by
+// warps 0-3 (TMEM lanes = input channels).  Lane 0 of warp 4 issues the
+// copies and the MMAs.  Every wait is bounded; a wait that runs out sets err,
+// and the block still waits (bounded) for its copies and MMAs in flight
+// before it frees the TMEM.
+constexpr int kWgThreads = 32 * 5;
+constexpr unsigned kWgGzGroupBytes = kTcM * 16; // one 8-channel group of one gz row: 128 pixels
+
+template <int CI, int CO>
+struct WgLayout {
+    static constexpr unsigned kSlotBytes = (CI / 8) * kTcRowBytes;
+    static constexpr unsigned kGzBytes = (CO / 8) * kWgGzGroupBytes;
+    static constexpr unsigned kAOff = (2 * kGzBytes + 1023u) & ~1023u;
+    // the 128-row A operand of the last slot reads up to 16 groups and the
+    // largest shift and K step beyond the slot's start
+    static constexpr unsigned kPad = (16u - CI / 8) * kTcRowBytes + kTcRowBytes;
+    static constexpr unsigned kFit = (kTcSmemMax - 1024u - 256u - kAOff - kPad) / kSlotBytes;
+    static constexpr unsigned kSlots = kFit > unsigned(kTcMaxSlots) ? unsigned(kTcMaxSlots) : kFit;
+    static constexpr unsigned kBarOff = kAOff + kSlots * kSlotBytes + kPad;
+    static constexpr unsigned kSmem = kBarOff + 256u + 1024u;
+    static_assert(kSlots >= 4, "four row slots must fit");
+};
+
+__device__ __forceinline__ void tmaLoadGzRow(void* dst, const CUtensorMap* map, int x, int y, int b, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smemAddr(dst)),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(x), "r"(0), "r"(y), "r"(b), "r"(smemAddr(bar))
+                 : "memory");
+}
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(kWgThreads, 1) kConvWeightGradTc(const __grid_constant__ CUtensorMap xMap,
+    const __grid_constant__ CUtensorMap gzMap, int B, int H, int W, int hs, int ns, float* __restrict__ part,
+    int* __restrict__ err)
+{
+    static_assert(CI % 8 == 0 && CI <= 64 && CO % 16 == 0 && 9 * CO <= 512, "channel counts");
+    using Lay = WgLayout<CI, CO>;
+    constexpr int S = static_cast<int>(Lay::kSlots);
+    constexpr uint32_t kCols = 512;
+    extern __shared__ __align__(16) unsigned char wgSmemRaw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(wgSmemRaw) + 1023) & ~uintptr_t(1023));
+    unsigned char* sGz = sm;
+    unsigned char* sA = sm + Lay::kAOff;
+    uint64_t* rowFull = reinterpret_cast<uint64_t*>(sm + Lay::kBarOff); // [8]
+    uint64_t* rowEmpty = rowFull + kTcMaxSlots;                         // [8]
+    uint64_t* gzFull = rowEmpty + kTcMaxSlots;                          // [2]
+    uint64_t* gzEmpty = gzFull + 2;                                     // [2]
+    uint64_t* done = gzEmpty + 2;                                       // [1] every MMA of the block completed
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(done + 1);
+    __shared__ volatile int abortFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int i = 0; i < 2 * kTcMaxSlots + 5; ++i)
+            mbarInit(rowFull + i, 1);
+        abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tmemSlot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tcFenceBefore();
+    __syncthreads();
+    tcFenceAfter();
+    const uint32_t tmem = *tmemSlot;
+    const int tilesX = (W + kTcM - 1) / kTcM;
+    const long strips = long(B) * tilesX * ns;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            // D F32, A and B BF16, both MN-major (bits 15, 16), N = CO, M = 128
+            constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16)
+                | (uint32_t(CO >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
+            const unsigned aBase = smemAddr(sA);
+            const uint64_t gzDesc[2] = { ummaDesc(smemAddr(sGz), 128, kWgGzGroupBytes),
+                ummaDesc(smemAddr(sGz + Lay::kGzBytes), 128, kWgGzGroupBytes) };
+            int loadPar[kTcMaxSlots];
+            for (int i = 0; i < kTcMaxSlots; ++i)
+                loadPar[i] = -1;
+            int gzPar[2] = { -1, -1 };
+            long rowSeq = 0, chunkSeq = 0;
+            bool ok = true;
+            for (long si = blockIdx.x; si < strips && ok; si += gridDim.x) {
+                const TcStrip sp = tcStrip(si, H, tilesX, hs, ns);
+                const int nt = sp.y1 - sp.y0, nr = nt + 2;
+                const long base = rowSeq;
+                int next = 0;
+                auto issueUpTo = [&](int limit) {
+                    for (; ok && next < nr && next < limit; ++next) {
+                        const long q = base + next;
+                        const int slot = static_cast<int>(q % S);
+                        ok = mbarWaitBounded(rowEmpty + slot, static_cast<unsigned>(((q / S) & 1) ^ 1));
+                        if (!ok)
+                            break;
+                        mbarExpectTx(rowFull + slot, Lay::kSlotBytes);
+                        tmaLoadRow(sA + slot * Lay::kSlotBytes, &xMap, sp.x0 - 1, sp.y0 - 1 + next, sp.b,
+                            rowFull + slot);
+                        loadPar[slot] = static_cast<int>((q / S) & 1);
+                    }
+                };
+                auto issueGz = [&](long c, int y) {
+                    const int g = static_cast<int>(c & 1);
+                    ok = ok && mbarWaitBounded(gzEmpty + g, static_cast<unsigned>(((c >> 1) & 1) ^ 1));
+                    if (!ok)
+                        return;
+                    mbarExpectTx(gzFull + g, Lay::kGzBytes);
+                    tmaLoadGzRow(sGz + g * Lay::kGzBytes, &gzMap, sp.x0, y, sp.b, gzFull + g);
+                    gzPar[g] = static_cast<int>((c >> 1) & 1);
+                };
+                issueGz(chunkSeq, sp.y0);
+                for (int t = 0; t < nt && ok; ++t, ++chunkSeq) {
+                    if (t + 1 < nt)
+                        issueGz(chunkSeq + 1, sp.y0 + t + 1);
+                    issueUpTo(t + S - 1);
+                    int slot3[3];
+                    for (int r = 0; r < 3 && ok; ++r) {
+                        const long q = base + t + r;
+                        slot3[r] = static_cast<int>(q % S);
+                        ok = mbarWaitBounded(rowFull + slot3[r], static_cast<unsigned>((q / S) & 1));
+                        if (ok)
+                            loadPar[slot3[r]] = -1;
+                    }
+                    const int g = static_cast<int>(chunkSeq & 1);
+                    ok = ok && mbarWaitBounded(gzFull + g, static_cast<unsigned>((chunkSeq >> 1) & 1));
+                    if (!ok)
+                        break;
+                    gzPar[g] = -1;
+                    tcFenceAfter();
+                    const uint64_t aRow[3] = { ummaDesc(aBase + slot3[0] * Lay::kSlotBytes, 128, kTcRowBytes),
+                        ummaDesc(aBase + slot3[1] * Lay::kSlotBytes, 128, kTcRowBytes),
+                        ummaDesc(aBase + slot3[2] * Lay::kSlotBytes, 128, kTcRowBytes) };
+#pragma unroll
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+                        for (int ks = 0; ks < kTcM / 16; ++ks)
+                            umma(tmem + tap * CO, aRow[dy] + uint64_t(dx + 16 * ks), gzDesc[g] + uint64_t(16 * ks),
+                                idesc, (chunkSeq > 0 || ks > 0) ? 1 : 0);
+                    }
+                    ummaCommit(gzEmpty + g);
+                    ummaCommit(rowEmpty + slot3[0]);
+                    if (t == nt - 1) {
+                        ummaCommit(rowEmpty + slot3[1]);
+                        ummaCommit(rowEmpty + slot3[2]);
+                    }
+                }
+                rowSeq += nr;
+            }
+            if (!ok) {
+                atomicOr(err, 1);
+                abortFlag = 1;
+            }
+            ummaCommit(done); // arrives once every MMA issued above has completed
+            for (int slot = 0; slot < S; ++slot)
+                if (loadPar[slot] >= 0)
+                    mbarWaitBounded(rowFull + slot, static_cast<unsigned>(loadPar[slot]));
+            for (int g = 0; g < 2; ++g)
+                if (gzPar[g] >= 0)
+                    mbarWaitBounded(gzFull + g, static_cast<unsigned>(gzPar[g]));
+        }
+    } else {
+        // warp w reads TMEM lanes 32 w .. 32 w + 31: input channels ci
+        const bool ready = __all_sync(0xffffffffu, mbarWaitBounded(done, 0));
+        if (!ready && lane == 0) {
+            atomicOr(err, 1);
+            abortFlag = 1;
+        }
+        if (ready && !abortFlag) {
+            tcFenceAfter();
+            const int ci = 32 * warp + lane;
+            float* out = part + long(blockIdx.x) * CO * 9 * CI;
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+#pragma unroll
+                for (int c = 0; c < CO; c += 8) {
+                    float v[8];
+                    tmemLoad8(tmem + tap * CO + c + (uint32_t(32 * warp) << 16), v);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (ci < CI) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            out[long(c + j) * 9 * CI + tap * CI + ci] = v[j];
+                    }
+                }
+            }
+        }
+    }
+    tcFenceBefore();
+    __syncthreads();
+    if (warp == 0) {
+        tcFenceAfter();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
 // Partial weight gradient of one tap over one chunk of pixels:
 //   part[chunk][co][tap*CI + ci] = sum_{m in chunk} gz[m][co] * x[m + (dy-1, dx-1)][ci]
 template <int CO, int CI>
@@ -793,6 +1006,55 @@ cudaError_t convTc(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* src
     return cudaGetLastError();
 }
 
+template <int CI, int CO>
+cudaError_t convWeightGradTcPrepare()
+{
+    if constexpr (9 * CO > 512) {
+        return cudaSuccess; // kept on mma.sync (nine accumulators of CO columns exceed the TMEM)
+    } else {
+        return cudaFuncSetAttribute(kConvWeightGradTc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            static_cast<int>(WgLayout<CI, CO>::kSmem));
+    }
+}
+
+// The weight gradient's partial sums on the tensor cores into part[0 ..
+// *nParts); maxParts bounds the partial buffer (in CO x 9 x CI sets).
+template <int CI, int CO>
+cudaError_t convWeightGradTc(cudaStream_t s, int B, int H, int W, const __nv_bfloat16* gz, const __nv_bfloat16* x,
+    float* part, long maxParts, int* err, int* nParts)
+{
+    if constexpr (9 * CO > 512) {
+        return cudaErrorNotSupported;
+    } else {
+        CUtensorMap xm, gm;
+        const uint64_t xd[5] = { 8, uint64_t(W), uint64_t(CI / 8), uint64_t(H), uint64_t(B) };
+        const uint64_t xs[4] = { 16, uint64_t(W) * 16, uint64_t(W) * CI * 2, uint64_t(H) * W * CI * 2 };
+        const uint32_t xb[5] = { 8, kTcSpan, uint32_t(CI / 8), 1, 1 };
+        const uint64_t gd[5] = { 8, uint64_t(W), uint64_t(CO / 8), uint64_t(H), uint64_t(B) };
+        const uint64_t gs[4] = { 16, uint64_t(W) * 16, uint64_t(W) * CO * 2, uint64_t(H) * W * CO * 2 };
+        const uint32_t gb[5] = { 8, uint32_t(kTcM), uint32_t(CO / 8), 1, 1 };
+        cudaError_t e = encodeTiledNd(&xm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, x, 5, xd, xs, xb);
+        if (e == cudaSuccess) e = encodeTiledNd(&gm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, gz, 5, gd, gs, gb);
+        int dev = 0, sms = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return e;
+        // one block per SM at most, no more blocks than partial sets; each
+        // block's strips as tall as that allows
+        const long columns = long(B) * ((W + kTcM - 1) / kTcM);
+        const long cap = std::max<long>(1, std::min<long>(sms, maxParts));
+        const int want = static_cast<int>(std::max<long>(1, cap / columns));
+        const int hs = (H + want - 1) / want;
+        const int ns = (H + hs - 1) / hs;
+        const unsigned grid = static_cast<unsigned>(std::min<long>(columns * ns, cap));
+        kConvWeightGradTc<CI, CO><<<grid, kWgThreads, WgLayout<CI, CO>::kSmem, s>>>(xm, gm, B, H, W, hs, ns, part,
+            err);
+        *nParts = static_cast<int>(grid);
+        return cudaGetLastError();
+    }
+}
+
 // channel counts supported by the instantiations: 16, 32, 48, 64
 #define NSDG_CH_SWITCH(c, D, CALL)                                                                 \
     switch (c) {                                                                                   \
@@ -953,6 +1215,8 @@ int netCreate(int L, const int* channels, int H, int W, int maxB, int used, unsi
             }
             if (e == cudaSuccess && l > 0)
                 NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (e = convTcPrepare<A, Bc, CONV_BWD_DATA>())));
+            if (e == cudaSuccess)
+                NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convWeightGradTcPrepare<A, Bc>())));
             return e;
         };
         e = prep();
@@ -1058,11 +1322,19 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
     for (int l = n->L - 1; l >= 0 && e == cudaSuccess; --l) {
         const int CI = n->ch[l], CO = n->ch[l + 1];
         const size_t nw = size_t(CO) * 9 * CI;
-        // weight gradient
-        dim3 grid(nChunks, 9);
-        NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (kConvWeightGrad<A, Bc><<<grid, kThreads, 0, s>>>(B, n->H, n->W, gz,
-                                                          n->act[l], n->part, n->wg))));
-        kSumChunks<<<static_cast<unsigned>((nw + 255) / 256), 256, 0, s>>>(nChunks, nw, n->part, n->g32 + n->wOff[l]);
+        // weight gradient: tcgen05 (nine TMEM accumulators of CO columns) or mma.sync
+        int nParts = nChunks;
+        if (n->tc && 9 * CO <= 512) {
+            NSDG_CH_SWITCH(CI, A, NSDG_CH_SWITCH(CO, Bc, (e = convWeightGradTc<A, Bc>(s, B, n->H, n->W, gz, n->act[l],
+                                                             n->part, nChunks, n->derr, &nParts))));
+        } else {
+            dim3 grid(nChunks, 9);
+            NSDG_CH_SWITCH(CO, A, NSDG_CH_SWITCH(CI, Bc, (kConvWeightGrad<A, Bc><<<grid, kThreads, 0, s>>>(B, n->H,
+                                                              n->W, gz, n->act[l], n->part, n->wg))));
+        }
+        if (e != cudaSuccess)
+            break;
+        kSumChunks<<<static_cast<unsigned>((nw + 255) / 256), 256, 0, s>>>(nParts, nw, n->part, n->g32 + n->wOff[l]);
         // bias gradient
         NSDG_CH_SWITCH(CO, A, (kBiasGradPartial<A><<<nChunks, A, 0, s>>>(M, gz, n->part, n->wg)));
         kSumChunks<<<1, CO, 0, s>>>(nChunks, CO, n->part, n->g32 + n->bOff[l]);
