@@ -1281,12 +1281,15 @@ def run_net_train(args):
     t = rng.standard_normal((1, n, n, net.channels[-1])).astype(np.float32)
     net.set_batch(x, t, np.ones((1, n, n), dtype=np.float32))
     for _ in range(max(args.warmup, 3)):
+        net.forward(copy=False)
         net.loss_backward()
         net.adam_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        net.forward(copy=False)
         net.loss_backward()
         net.adam_step()
+    net.forward(copy=False)
     net.loss_backward()  # the last Adam update has been applied when this returns
     ms = (time.perf_counter() - t0) * 1e3 / (args.steps + 1)
     ch = net.channels

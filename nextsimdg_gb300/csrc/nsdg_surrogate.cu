@@ -847,20 +847,68 @@ __global__ void kSumChunks(int nChunks, size_t n, const float* __restrict__ part
         s += part[size_t(c) * n + i];
     out[i] = s;
 }
-template <int CO>
-__global__ void kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz, float* __restrict__ part, int wg)
+// out[i] = sum over c < nParts of part[c * n + i], one block of 256 threads
+// per output (for few outputs with many partials: the bias gradients, the loss)
+__global__ void __launch_bounds__(256) kSumPartsBlock(int nParts, size_t n, const float* __restrict__ part,
+    float* __restrict__ out)
 {
-    // one block per chunk, one thread per channel (blockDim.x = CO)
-    const int co = threadIdx.x;
-    const long p0 = long(blockIdx.x) * kChunk;
+    __shared__ float ws[8];
+    const size_t i = blockIdx.x;
     float s = 0.f;
-    for (int k = 0; k < kChunk; ++k) {
-        const long m = p0 + k;
-        if (m >= M)
-            break;
-        s += __bfloat162float(gz[actChunk(m, co >> 3, CO, wg) + (co & 7)]);
+    for (int c = threadIdx.x; c < nParts; c += 256)
+        s += part[size_t(c) * n + i];
+    for (int off = 16; off > 0; off >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; ++w)
+            t += ws[w];
+        out[i] = t;
     }
-    part[long(blockIdx.x) * CO + co] = s;
+}
+
+// Bias gradient partial of one chunk of kChunk pixels: part[chunk][co] =
+// sum of gz[m][co]; 256 threads read one 8-channel group of consecutive
+// pixels at a time (16 bytes each, coalesced), then reduce per channel.
+template <int CO>
+__global__ void __launch_bounds__(256) kBiasGradPartial(long M, const __nv_bfloat16* __restrict__ gz,
+    float* __restrict__ part, int wg)
+{
+    __shared__ float red[8][8];
+    const long p0 = long(blockIdx.x) * kChunk;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int g = 0; g < CO / 8; ++g) {
+        float acc[8] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
+        for (int k = tid; k < kChunk; k += 256) {
+            const long m = p0 + k;
+            if (m >= M)
+                break;
+            const uint4 v = *reinterpret_cast<const uint4*>(gz + actChunk(m, g, CO, wg));
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                acc[j] += __bfloat162float(e[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            for (int off = 16; off > 0; off >>= 1)
+                acc[j] += __shfl_down_sync(0xffffffffu, acc[j], off);
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                red[warp][j] = acc[j];
+        __syncthreads();
+        if (tid < 8) {
+            float t = 0.f;
+            for (int w = 0; w < 8; ++w)
+                t += red[w][tid];
+            part[long(blockIdx.x) * CO + g * 8 + tid] = t;
+        }
+        __syncthreads();
+    }
 }
 
 // Masked MSE: gz = 2 m (out - target) / denom for the first `used` channels
@@ -875,14 +923,26 @@ __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const floa
     float s = 0.f;
     if (m < M) {
         const float mk = mask[m];
-        for (int c = 0; c < C; ++c) {
-            float gval = 0.f;
-            if (c < used) {
-                const float d = out[m * C + c] - target[m * C + c];
-                s += mk * d * d;
-                gval = 2.f * mk * d * invDenom;
+        // 8 channels at a time: two float4 of the output and of the target,
+        // one 16-byte group of gz
+        for (int g = 0; g < C / 8; ++g) {
+            const float4* o4 = reinterpret_cast<const float4*>(out + m * C + g * 8);
+            const float4* t4 = reinterpret_cast<const float4*>(target + m * C + g * 8);
+            const float4 oa = o4[0], ob = o4[1], ta = t4[0], tb = t4[1];
+            const float ov[8] = { oa.x, oa.y, oa.z, oa.w, ob.x, ob.y, ob.z, ob.w };
+            const float tv[8] = { ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w };
+            __align__(16) __nv_bfloat16 gv[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float gval = 0.f;
+                if (g * 8 + j < used) {
+                    const float d = ov[j] - tv[j];
+                    s += mk * d * d;
+                    gval = 2.f * mk * d * invDenom;
+                }
+                gv[j] = __float2bfloat16_rn(gval);
             }
-            gz[actChunk(m, c >> 3, C, wg) + (c & 7)] = __float2bfloat16_rn(gval);
+            *reinterpret_cast<uint4*>(gz + actChunk(m, g, C, wg)) = *reinterpret_cast<const uint4*>(gv);
         }
     }
     for (int off = 16; off > 0; off >>= 1)
@@ -899,13 +959,34 @@ __global__ void __launch_bounds__(256) kLoss(long M, int C, int used, const floa
 }
 
 // 1 / (sum of the mask * used channels), one block, fixed summation order
-__global__ void __launch_bounds__(1024) kInvDenom(long M, int used, const float* __restrict__ mask,
+// The loss denominator (sum of the mask times the used channels) in two
+// passes: per-block sums of 256 mask values (exact in FP32 for a 0/1 mask),
+// then one block adds them in FP64 and stores 1 / denominator.
+__global__ void __launch_bounds__(256) kMaskPartial(long M, const float* __restrict__ mask,
+    float* __restrict__ partial)
+{
+    __shared__ float ws[8];
+    const long m = blockIdx.x * 256L + threadIdx.x;
+    float s = m < M ? mask[m] : 0.f;
+    for (int off = 16; off > 0; off >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; ++w)
+            t += ws[w];
+        partial[blockIdx.x] = t;
+    }
+}
+__global__ void __launch_bounds__(256) kInvDenom(int nPartial, int used, const float* __restrict__ partial,
     float* __restrict__ invDenom)
 {
-    __shared__ double ws[32];
+    __shared__ double ws[8];
     double s = 0.0;
-    for (long m = threadIdx.x; m < M; m += blockDim.x)
-        s += mask[m];
+    for (int i = threadIdx.x; i < nPartial; i += 256)
+        s += partial[i];
     for (int off = 16; off > 0; off >>= 1)
         s += __shfl_down_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0)
@@ -913,7 +994,7 @@ __global__ void __launch_bounds__(1024) kInvDenom(long M, int used, const float*
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        for (int w = 0; w < 32; ++w)
+        for (int w = 0; w < 8; ++w)
             t += ws[w];
         *invDenom = t > 0.0 ? static_cast<float>(1.0 / (t * used)) : 0.f;
     }
@@ -1312,10 +1393,13 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
     // denominator: sum of the mask times the used channels
     cudaError_t e = cudaSuccess;
     float* invDenom = n->lossPart + (long(n->maxB) * n->H * n->W + 255) / 256 + 1;
-    kInvDenom<<<1, 1024, 0, s>>>(M, n->used, n->mask, invDenom);
     const unsigned lb = static_cast<unsigned>((M + 255) / 256);
+    // the weight-gradient partial buffer is free until the first layer's
+    // weight gradient: it holds the mask partial sums
+    kMaskPartial<<<lb, 256, 0, s>>>(M, n->mask, n->part);
+    kInvDenom<<<1, 256, 0, s>>>(static_cast<int>(lb), n->used, n->part, invDenom);
     kLoss<<<lb, 256, 0, s>>>(M, CL, n->used, n->out, n->target, n->mask, invDenom, n->gA, n->lossPart, n->wg);
-    kSumChunks<<<1, 1, 0, s>>>(static_cast<int>(lb), 1, n->lossPart, lossDev);
+    kSumPartsBlock<<<1, 256, 0, s>>>(static_cast<int>(lb), 1, n->lossPart, lossDev);
     const int nChunks = static_cast<int>((M + kChunk - 1) / kChunk);
     __nv_bfloat16* gz = n->gA;
     __nv_bfloat16* gnext = n->gB;
@@ -1336,8 +1420,8 @@ cudaError_t netLossBackward(NetImpl* n, int B, float* lossDev)
             break;
         kSumChunks<<<static_cast<unsigned>((nw + 255) / 256), 256, 0, s>>>(nParts, nw, n->part, n->g32 + n->wOff[l]);
         // bias gradient
-        NSDG_CH_SWITCH(CO, A, (kBiasGradPartial<A><<<nChunks, A, 0, s>>>(M, gz, n->part, n->wg)));
-        kSumChunks<<<1, CO, 0, s>>>(nChunks, CO, n->part, n->g32 + n->bOff[l]);
+        NSDG_CH_SWITCH(CO, A, (kBiasGradPartial<A><<<nChunks, 256, 0, s>>>(M, gz, n->part, n->wg)));
+        kSumPartsBlock<<<CO, 256, 0, s>>>(nChunks, CO, n->part, n->g32 + n->bOff[l]);
         // data gradient times relu' of the layer input (not needed for the network input)
         if (l > 0) {
             if (n->tc) {

@@ -81,7 +81,12 @@ class Net:
             None if m is None else m.ctypes.data_as(c_void_p)))
         self._B = B
 
-    def forward(self):
+    def forward(self, copy: bool = True):
+        """The forward pass of the batch set last; its output copied to the
+        host (copy=False: left on the device, for a following loss_backward)."""
+        if not copy:
+            self._check(self._l.nsdg_net_forward(self._h, self._B, None))
+            return None
         out = np.empty((self._B, self.H, self.W, self.channels[-1]), dtype=np.float32)
         self._check(self._l.nsdg_net_forward(self._h, self._B, out.ctypes.data_as(c_void_p)))
         return out
