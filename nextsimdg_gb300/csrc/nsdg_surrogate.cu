@@ -552,14 +552,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) kConv3x3Tc(const __grid_constan
 constexpr int kWgThreads = 32 * 5;
 constexpr unsigned kWgGzGroupBytes = kTcM * 16; // one 8-channel group of one gz row: 128 pixels
 
-template <int CI, int CO>
+template <int CI, int CO, int MR>
 struct WgLayout {
     static constexpr unsigned kSlotBytes = (CI / 8) * kTcRowBytes;
     static constexpr unsigned kGzBytes = (CO / 8) * kWgGzGroupBytes;
     static constexpr unsigned kAOff = (2 * kGzBytes + 1023u) & ~1023u;
-    // the 128-row A operand of the last slot reads up to 16 groups and the
-    // largest shift and K step beyond the slot's start
-    static constexpr unsigned kPad = (16u - CI / 8) * kTcRowBytes + kTcRowBytes;
+    // the MR-row A operand of the last slot reads up to MR / 8 groups and
+    // the largest shift and K step beyond the slot's start
+    static constexpr unsigned kPad = (unsigned(MR / 8) - CI / 8) * kTcRowBytes + kTcRowBytes;
     static constexpr unsigned kFit = (kTcSmemMax - 1024u - 256u - kAOff - kPad) / kSlotBytes;
     static constexpr unsigned kSlots = kFit > unsigned(kTcMaxSlots) ? unsigned(kTcMaxSlots) : kFit;
     static constexpr unsigned kBarOff = kAOff + kSlots * kSlotBytes + kPad;
@@ -575,13 +575,14 @@ __device__ __forceinline__ void tmaLoadGzRow(void* dst, const CUtensorMap* map, 
                  : "memory");
 }
 
-template <int CI, int CO>
+template <int CI, int CO, int MR>
 __global__ void __launch_bounds__(kWgThreads, 1) kConvWeightGradTc(const __grid_constant__ CUtensorMap xMap,
     const __grid_constant__ CUtensorMap gzMap, int B, int H, int W, int hs, int ns, float* __restrict__ part,
     int* __restrict__ err)
 {
-    static_assert(CI % 8 == 0 && CI <= 64 && CO % 16 == 0 && 9 * CO <= 512, "channel counts");
-    using Lay = WgLayout<CI, CO>;
+    static_assert(CI % 8 == 0 && CI <= MR && (MR == 64 || MR == 128) && CO % 16 == 0 && 9 * CO <= 512,
+        "channel counts");
+    using Lay = WgLayout<CI, CO, MR>;
     constexpr int S = static_cast<int>(Lay::kSlots);
     constexpr uint32_t kCols = 512;
     extern __shared__ __align__(16) unsigned char wgSmemRaw[];
@@ -617,9 +618,9 @@ __global__ void __launch_bounds__(kWgThreads, 1) kConvWeightGradTc(const __grid_
 
     if (warp == 4) {
         if (lane == 0) {
-            // D F32, A and B BF16, both MN-major (bits 15, 16), N = CO, M = 128
+            // D F32, A and B BF16, both MN-major (bits 15, 16), N = CO, M = MR
             constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16)
-                | (uint32_t(CO >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
+                | (uint32_t(CO >> 3) << 17) | (uint32_t(MR >> 4) << 24);
             const unsigned aBase = smemAddr(sA);
             const uint64_t gzDesc[2] = { ummaDesc(smemAddr(sGz), 128, kWgGzGroupBytes),
                 ummaDesc(smemAddr(sGz + Lay::kGzBytes), 128, kWgGzGroupBytes) };
@@ -708,7 +709,9 @@ __global__ void __launch_bounds__(kWgThreads, 1) kConvWeightGradTc(const __grid_
                     mbarWaitBounded(gzFull + g, static_cast<unsigned>(gzPar[g]));
         }
     } else {
-        // warp w reads TMEM lanes 32 w .. 32 w + 31: input channels ci
+        // warp w reads TMEM lanes 32 w .. 32 w + 31: input channel ci = 32 w +
+        // lane for M = 128; for M = 64 the accumulator rows sit in the first
+        // 16 lanes of each 32-lane quarter, ci = 16 w + lane (lane < 16)
         const bool ready = __all_sync(0xffffffffu, mbarWaitBounded(done, 0));
         if (!ready && lane == 0) {
             atomicOr(err, 1);
@@ -716,7 +719,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) kConvWeightGradTc(const __grid_
         }
         if (ready && !abortFlag) {
             tcFenceAfter();
-            const int ci = 32 * warp + lane;
+            const int ci = MR == 128 ? 32 * warp + lane : (lane < 16 ? 16 * warp + lane : CI);
             float* out = part + long(blockIdx.x) * CO * 9 * CI;
 #pragma unroll 1
             for (int tap = 0; tap < 9; ++tap) {
@@ -1093,9 +1096,21 @@ cudaError_t convWeightGradTcPrepare()
     if constexpr (9 * CO > 512) {
         return cudaSuccess; // kept on mma.sync (nine accumulators of CO columns exceed the TMEM)
     } else {
-        return cudaFuncSetAttribute(kConvWeightGradTc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-            static_cast<int>(WgLayout<CI, CO>::kSmem));
+        cudaError_t e = cudaFuncSetAttribute(kConvWeightGradTc<CI, CO, 128>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(WgLayout<CI, CO, 128>::kSmem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kConvWeightGradTc<CI, CO, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                static_cast<int>(WgLayout<CI, CO, 64>::kSmem));
+        return e;
     }
+}
+
+// MMA rows of the weight gradient: 64 (input channels padded to 64, the
+// default) or 128 (NSDG_WGRAD_M=128)
+inline int wgradRows()
+{
+    const char* e = std::getenv("NSDG_WGRAD_M");
+    return e && std::strcmp(e, "128") == 0 ? 128 : 64;
 }
 
 // The weight gradient's partial sums on the tensor cores into part[0 ..
@@ -1129,8 +1144,12 @@ cudaError_t convWeightGradTc(cudaStream_t s, int B, int H, int W, const __nv_bfl
         const int hs = (H + want - 1) / want;
         const int ns = (H + hs - 1) / hs;
         const unsigned grid = static_cast<unsigned>(std::min<long>(columns * ns, cap));
-        kConvWeightGradTc<CI, CO><<<grid, kWgThreads, WgLayout<CI, CO>::kSmem, s>>>(xm, gm, B, H, W, hs, ns, part,
-            err);
+        if (wgradRows() == 128)
+            kConvWeightGradTc<CI, CO, 128><<<grid, kWgThreads, WgLayout<CI, CO, 128>::kSmem, s>>>(xm, gm, B, H, W, hs,
+                ns, part, err);
+        else
+            kConvWeightGradTc<CI, CO, 64><<<grid, kWgThreads, WgLayout<CI, CO, 64>::kSmem, s>>>(xm, gm, B, H, W, hs,
+                ns, part, err);
         *nParts = static_cast<int>(grid);
         return cudaGetLastError();
     }

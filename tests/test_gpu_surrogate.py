@@ -15,15 +15,22 @@ def _rel(a, b):
     return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
 
 
-@pytest.mark.parametrize("conv", ["tcgen05", "mma"])
+@pytest.mark.parametrize("conv", ["tcgen05", "tcgen05_m128", "mma"])
 @pytest.mark.parametrize("chans,H,W,B,used", [([16, 32, 32, 16], 10, 13, 2, 12), ([48, 48, 32], 9, 70, 1, 26),
                                               ([64, 48, 64, 32], 5, 131, 2, 20)])
 def test_net_gradients_match_oracle(gpu, monkeypatch, conv, chans, H, W, B, used):
+    """tcgen05: the weight gradient's MMAs with the input channels as 64 rows
+    (the default); tcgen05_m128: as 128 rows (NSDG_WGRAD_M=128); mma: every
+    convolution on mma.sync."""
     from nextsimdg_gb300.surrogate import Net
     if conv == "mma":
         monkeypatch.setenv("NSDG_CONV", "mma")
     else:
         monkeypatch.delenv("NSDG_CONV", raising=False)
+    if conv == "tcgen05_m128":
+        monkeypatch.setenv("NSDG_WGRAD_M", "128")
+    else:
+        monkeypatch.delenv("NSDG_WGRAD_M", raising=False)
     rng = np.random.default_rng(11)
     net = Net(chans, H, W, max_batch=B, used_outputs=used, seed=5)
     p = net.get_params()
