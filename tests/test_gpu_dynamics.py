@@ -64,6 +64,43 @@ def test_mevp_matches_oracle(gpu, oracle, n, dg, steps):
     assert np.abs(o.getDG0Data("u")).max() > 1e-3  # the test moves the ice
 
 
+@pytest.mark.parametrize("nx,ny,mask_kind", [(2, 7, "ice"), (9, 2, "ice"), (2, 2, "ice"), (6, 5, "land"),
+                                              (7, 6, "one cell"), (33, 3, "checker")])
+def test_degenerate_grids_match_oracle(gpu, oracle, nx, ny, mask_kind):
+    """Two-column and two-row grids, a 2 x 2 grid, an all-land mask, one ice
+    cell in land and a checkerboard of ice and land (every ice cell's edges
+    closed): FP64 within 1e-10 of the oracle after two steps, the mixed path
+    (parallelogram kernels, tiled transport) finite and within 1e-5 m/s of
+    it.  A single row or column is refused at initialise."""
+    if nx == 2 and ny == 7:
+        k = MEVPDynamicsKernel(dg_comp=6)
+        with pytest.raises(NsdgError, match="nx >= 2"):
+            k.initialise(BoxTest(1, 7).coords(), False, np.ones((7, 1)))
+        k.close()
+    box = BoxTest(nx, ny)
+    if mask_kind != "ice":
+        m = np.zeros((ny, nx))
+        if mask_kind == "one cell":
+            m[ny // 2, nx // 2] = 1.0
+        elif mask_kind == "checker":
+            m[(np.add.outer(np.arange(ny), np.arange(nx)) % 2) == 0] = 1.0
+        box.mask = lambda m=m: m
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    o = _make(oracle.OracleKernel, box, 6, 0, **prm)
+    g = _make(MEVPDynamicsKernel, box, 6, None, **prm)
+    x = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    for k in (o, g, x):
+        _advance(k, box, 2)
+    names = ["hice", "cice", "u", "v", "uiostress", "viostress"]
+    worst = _compare(g, o, names, 6)
+    assert all(v <= TOL for v in worst.values()), worst
+    for n in ("u", "v"):
+        a, b = x.getDG0Data(n), o.getDG0Data(n)
+        assert np.all(np.isfinite(a)) and float(np.sqrt(np.mean((a - b) ** 2))) <= 1e-5, n
+    g.close()
+    x.close()
+
+
 def test_mevp_land_holes_matches_oracle(gpu, oracle):
     box = BoxTest(20, 15)
     m = box.mask()
