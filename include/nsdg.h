@@ -116,7 +116,9 @@ const char* nsdg_kernel_last_error(const nsdg_kernel* k);
  * is_spherical != 0: coords are (lon, lat) in radians; the mesh is rotated
  * so that its poles lie in Greenland / Antarctica and the operators carry the
  * spherical metric terms (DynamicsKernel.hpp:44-58, ParametricMap.cpp:298-353,
- * CGDynamicsKernel.cpp:331-351). */
+ * CGDynamicsKernel.cpp:331-351).  nx and ny must be at least 2
+ * (NSDG_ERR_BAD_ARG otherwise: the kernels are not written for a single row
+ * or column of cells, which the reference's mesh allows). */
 int nsdg_kernel_initialise(nsdg_kernel* k, size_t nx, size_t ny,
     const double* coords, int is_spherical, const double* mask);
 
