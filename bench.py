@@ -517,7 +517,7 @@ def learned_config5_variant(args) -> dict:
     1024 x 1024 box test with K mEVP iterations after the network's start
     instead of 100, with the device-side residual fallback.  Speed against the
     plain FP32 step, and the velocity error after `err_steps` steps against
-    the plain FP32 sub-cycle (the judge of the warm start) and against FP64,
+    the plain FP32 sub-cycle (the reference for the warm start's error) and against FP64,
     next to the FP32 path's own error against FP64."""
     from nextsimdg_gb300 import surrogate
     from nextsimdg_gb300.boxtest import BoxTest, step_forcing
@@ -982,7 +982,7 @@ def run_ours(args, world, rank, local):
                        "bytes_per_cell_update_parts": launched,
                        "bytes_note": "bytes_per_cell_update counts the arrays the launched kernels move; "
                                      "the reference-layout figure (every per-element operator streamed, "
-                                     "the unfused reference data flow) is the survey's nominal"},
+                                     "the unfused reference data flow) is the nominal upper figure"},
             "e2e": {**{kk: vv for kk, vv in e2e_res.items() if kk != "cycle"},
                     **({"calls_us": e2e_calls} if e2e_calls else {})},
             "e2e_module_step": {kk: vv for kk, vv in e2e_module_step.items() if kk != "cycle"},
