@@ -19,7 +19,10 @@ mEVP iterations (strain, stress, divergence, momentum, boundaries).
          update, then getDG0Data of h, A, u, v and the ice-ocean stress),
          13 C-ABI calls per step, wall clock, host<->device copies inside.
          e2e_module_step: the same cycle as one nsdg_kernel_module_step
-         call per step (what the GPUMEVPDynamics module makes).
+         call per step (what the GPUMEVPDynamics module makes);
+         e2e_pageable / e2e_module_step_pageable: the same with the
+         pageable arrays a model holds (moved by a kernel that reads and
+         writes them directly where the GPU allows it).
   variants.plain_fp64     the FP64 path (the reference's arithmetic) on the
                           same grid, with its own roofline;
   variants.learned_fp32   the learned warm start as configured for it:
@@ -911,6 +914,9 @@ def run_ours(args, world, rank, local):
     e2e_res = e2e_cycle(k, box, args, world, pinned=True)
     e2e_module_step = e2e_cycle(k, box, args, world, pinned=True, batched=True)
     e2e_pageable = e2e_cycle(k, box, args, world, pinned=False)
+    # what the module adapters do with a model's (pageable) arrays: one
+    # module-step call per step
+    e2e_module_pageable = e2e_cycle(k, box, args, world, pinned=False, batched=True)
     e2e_device_forcing = e2e_cycle(k, box, args, world, pinned=True, device_forcing=True)
     e2e_calls = e2e_call_breakdown(k, e2e_res["cycle"], args.warmup, args.steps) if args.e2e_calls else None
 
@@ -919,6 +925,7 @@ def run_ours(args, world, rank, local):
     launched = launched_bytes_per_cell_update(box, prec, (k.stress_variant()[0] or "fp64") if prec else "fp64",
                                               tiled_transport=tiled)
     transport = transport_record(k, N, ms_max / args.steps)
+    k_host_direct = k.host_direct()
     k.close()
 
     variants = {}
@@ -987,6 +994,8 @@ def run_ours(args, world, rank, local):
                     **({"calls_us": e2e_calls} if e2e_calls else {})},
             "e2e_module_step": {kk: vv for kk, vv in e2e_module_step.items() if kk != "cycle"},
             "e2e_pageable": {kk: vv for kk, vv in e2e_pageable.items() if kk != "cycle"},
+            "e2e_module_step_pageable": {**{kk: vv for kk, vv in e2e_module_pageable.items() if kk != "cycle"},
+                                         "host_direct": k_host_direct},
             "e2e_device_forcing": {kk: vv for kk, vv in e2e_device_forcing.items() if kk != "cycle"},
             "gpu_launches": launches * args.steps,
             "roofline": roof,

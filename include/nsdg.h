@@ -245,6 +245,14 @@ int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch);
  * from the coefficients, *offdiag = the largest off-diagonal entry of an
  * element's M^{-1} relative to its diagonal (-1 when not evaluated). */
 int nsdg_kernel_transport_variant(nsdg_kernel* k, int* tiled, double* cell_mismatch, double* offdiag);
+/* Whether host arrays that are not page-locked move by a kernel that reads
+ * or writes them directly (*direct = 1: the GPU accesses pageable host
+ * memory, as on Grace, at the CPU-GPU link's rate; a copy from pageable
+ * memory is staged through a driver buffer and runs at about half of it).
+ * set_data, get_dg0 and module_step use it for such arrays; page-locked
+ * arrays keep the copy engine.  NSDG_HOST_DIRECT=0 before initialise turns
+ * it off.  No reference counterpart. */
+int nsdg_kernel_host_direct(nsdg_kernel* k, int* direct);
 /* The evaluation of P/(8 alpha Delta) in the parallelogram stress kernel:
  * 0 CUDA's rsqrt(double), 1 and 2 one FP64 Newton step from an FP32 seed
  * (2, the default: conversions on the integer pipe), 3 the same step in

@@ -116,6 +116,7 @@ SIGNATURES = [
     ("nsdg_kernel_launches_per_update", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_kernel_stress_variant", c_int, [c_void_p, POINTER(c_int), POINTER(c_double)]),
     ("nsdg_kernel_transport_variant", c_int, [c_void_p, POINTER(c_int), POINTER(c_double), POINTER(c_double)]),
+    ("nsdg_kernel_host_direct", c_int, [c_void_p, POINTER(c_int)]),
     ("nsdg_kernel_module_step", c_int, [c_void_p, POINTER(FieldIn), c_size_t, c_double, c_double,
                                         POINTER(FieldOut), c_size_t]),
     ("nsdg_kernel_viscosity_form", c_int, [c_void_p, POINTER(c_int)]),

@@ -323,7 +323,22 @@ struct nsdg_kernel {
     int enqueueConversion(const SetTarget& t, const double* staging, size_t nComp);
     // the cell averages of a field into host memory `out`: projections and
     // the copy enqueued on `stream` (a stored field is copied at once)
-    int enqueueReadout(const std::string& s, double* out);
+    int enqueueReadout(const std::string& s, double* out, HostMoves* batch = nullptr);
+    // the GPU reads and writes pageable host memory directly (Grace: address
+    // translation over the CPU-GPU link; NSDG_HOST_DIRECT=0 turns it off):
+    // host arrays that are not page-locked then move by a kernel, which runs
+    // at the link's rate, instead of a copy staged through a driver buffer
+    bool hostDirect = false;
+    static bool isPageable(const void* p)
+    {
+        cudaPointerAttributes a {};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeUnregistered;
+    }
+    bool moveByKernel(const void* p) const { return hostDirect && isPageable(p); }
 };
 
 int nsdg_kernel::checkDeviceError()
@@ -745,6 +760,14 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         const int r = chooseStress32();
         if (r)
             return r;
+    }
+    {
+        int dev = 0, pageableAccess = 0;
+        const char* hd = std::getenv("NSDG_HOST_DIRECT");
+        hostDirect = cudaGetDevice(&dev) == cudaSuccess
+            && cudaDeviceGetAttribute(&pageableAccess, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess
+            && pageableAccess == 1 && !(hd && std::strcmp(hd, "0") == 0);
+        cudaGetLastError();
     }
     ready = true;
     return ok();
@@ -1552,8 +1575,17 @@ int nsdg_kernel_set_data(nsdg_kernel* k, const char* name, const double* data, s
     double* const staging = slot ? k->stage2 : k->staging;
     int r = cu(cudaStreamWaitEvent(k->copyStream, k->converted[slot], 0), "set_data wait");
     if (r) return r;
-    r = cu(cudaMemcpyAsync(staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, k->copyStream),
-        "set_data copy");
+    if (k->moveByKernel(data)) {
+        HostMoves m;
+        m.src[0] = data;
+        m.dst[0] = staging;
+        m.n[0] = N * n_comp;
+        m.count = 1;
+        r = cu(launchHostMove(k->copyStream, m), "set_data move");
+    } else {
+        r = cu(cudaMemcpyAsync(staging, data, N * n_comp * sizeof(double), cudaMemcpyHostToDevice, k->copyStream),
+            "set_data copy");
+    }
     if (r) return r;
     r = cu(cudaEventRecord(k->copied, k->copyStream), "set_data event");
     if (r) {
@@ -1599,7 +1631,7 @@ int nsdg_kernel_synchronize(nsdg_kernel* k)
     return r ? r : k->ok();
 }
 
-int nsdg_kernel::enqueueReadout(const std::string& s, double* out)
+int nsdg_kernel::enqueueReadout(const std::string& s, double* out, HostMoves* batch)
 {
     const bool bbm = rheology == NSDG_RHEOLOGY_BBM;
     const double* src = nullptr;
@@ -1644,8 +1676,27 @@ int nsdg_kernel::enqueueReadout(const std::string& s, double* out)
             out[i] = it->second[i * dg];
         return NSDG_OK;
     }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(out, src, N * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) {
+        if (moveByKernel(out)) {
+            // into a pageable host array: a kernel writes it (batched with
+            // the call's other read-outs when the caller collects them)
+            if (batch && batch->count < kHostMoves) {
+                batch->src[batch->count] = src;
+                batch->dst[batch->count] = out;
+                batch->n[batch->count] = N;
+                ++batch->count;
+            } else {
+                HostMoves m;
+                m.src[0] = src;
+                m.dst[0] = out;
+                m.n[0] = N;
+                m.count = 1;
+                e = launchHostMove(stream, m);
+            }
+        } else {
+            e = cudaMemcpyAsync(out, src, N * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        }
+    }
     return e == cudaSuccess ? NSDG_OK : fail(NSDG_ERR_CUDA, std::string("get_dg0: ") + cudaGetErrorString(e));
 }
 
@@ -1721,16 +1772,29 @@ int nsdg_kernel_module_step(nsdg_kernel* k, const nsdg_field_in* in, size_t n_in
     }
     int r = NSDG_OK;
     size_t off = 0;
+    HostMoves inMoves; // pageable inputs, moved by one kernel
     for (size_t i = 0; i < n_in && r == NSDG_OK; ++i) {
         if (!targets[i].cg && !targets[i].dg) {
             k->storeField(in[i].name, in[i].data, in[i].n_comp);
             continue;
         }
-        r = cu(cudaMemcpyAsync(k->moduleStage + off, in[i].data, N * in[i].n_comp * sizeof(double),
-                   cudaMemcpyHostToDevice, k->copyStream),
-            "module_step copy");
+        if (k->moveByKernel(in[i].data)) {
+            inMoves.src[inMoves.count] = in[i].data;
+            inMoves.dst[inMoves.count] = k->moduleStage + off;
+            inMoves.n[inMoves.count] = N * in[i].n_comp;
+            if (++inMoves.count == kHostMoves) {
+                r = cu(launchHostMove(k->copyStream, inMoves), "module_step move");
+                inMoves = HostMoves();
+            }
+        } else {
+            r = cu(cudaMemcpyAsync(k->moduleStage + off, in[i].data, N * in[i].n_comp * sizeof(double),
+                       cudaMemcpyHostToDevice, k->copyStream),
+                "module_step copy");
+        }
         off += N * in[i].n_comp;
     }
+    if (r == NSDG_OK && inMoves.count)
+        r = cu(launchHostMove(k->copyStream, inMoves), "module_step move");
     if (r == NSDG_OK)
         r = cu(cudaEventRecord(k->copied, k->copyStream), "module_step event");
     if (r == NSDG_OK)
@@ -1748,8 +1812,11 @@ int nsdg_kernel_module_step(nsdg_kernel* k, const nsdg_field_in* in, size_t n_in
     }
     if (r == NSDG_OK)
         r = k->launchStep(dt);
+    HostMoves outMoves; // pageable outputs, written by one kernel
     for (size_t j = 0; j < n_out && r == NSDG_OK; ++j)
-        r = k->enqueueReadout(out[j].name, out[j].data);
+        r = k->enqueueReadout(out[j].name, out[j].data, &outMoves);
+    if (r == NSDG_OK && outMoves.count)
+        r = cu(launchHostMove(k->stream, outMoves), "module_step move");
     const int rs = k->checkDeviceError(); // waits for the copies out as well
     if (r)
         return r;
@@ -2080,6 +2147,16 @@ int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch)
         return k->fail(NSDG_ERR_BAD_ARG, "stress_variant: kernel not initialised");
     *kind = k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP ? k->stressKind : -1;
     *mismatch = k->affWorst;
+    return k->ok();
+}
+
+int nsdg_kernel_host_direct(nsdg_kernel* k, int* direct)
+{
+    if (!k || !direct)
+        return NSDG_ERR_BAD_ARG;
+    if (!k->ready)
+        return k->fail(NSDG_ERR_BAD_ARG, "host_direct: kernel not initialised");
+    *direct = k->hostDirect ? 1 : 0;
     return k->ok();
 }
 

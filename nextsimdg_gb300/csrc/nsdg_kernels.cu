@@ -3379,6 +3379,43 @@ cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
     return cudaGetLastError();
 }
 
+// Up to kHostMoves arrays moved by one grid-stride kernel: on a GPU that
+// reads and writes pageable host memory directly (Grace: address translation
+// over the CPU-GPU link), one kernel over all of a call's host arrays moves
+// them at the link's rate, where a copy from or to pageable memory is staged
+// through a driver buffer.
+__global__ void __launch_bounds__(256) kHostMove(HostMoves m)
+{
+    unsigned long long total = 0;
+    for (int f = 0; f < m.count; ++f)
+        total += m.n[f];
+    for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < total; i += gridDim.x * 256ull) {
+        unsigned long long off = i;
+        int f = 0;
+        while (f < m.count - 1 && off >= m.n[f]) {
+            off -= m.n[f];
+            ++f;
+        }
+        m.dst[f][off] = m.src[f][off];
+    }
+}
+
+cudaError_t launchHostMove(cudaStream_t s, const HostMoves& m)
+{
+    if (m.count <= 0)
+        return cudaSuccess;
+    if (m.count > kHostMoves)
+        return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return e;
+    kHostMove<<<static_cast<unsigned>(4 * sms), 256, 0, s>>>(m);
+    return cudaGetLastError();
+}
+
 cudaError_t launchAosToSoa(cudaStream_t s, size_t N, int nin, int dg, const double* aos, double* soa)
 {
     kAosToSoa<<<blocksFor(N), kBlock, 0, s>>>(N, nin, dg, aos, soa);

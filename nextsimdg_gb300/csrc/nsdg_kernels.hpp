@@ -450,6 +450,16 @@ cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
 // host ModelArray layout (AoS, nin comps) -> device SoA with `dg` comps,
 // following DGModelArray::ma2dg (zero, then all or component 0 only).
 cudaError_t launchAosToSoa(cudaStream_t s, size_t N, int nin, int dg, const double* aos, double* soa);
+// Moves of whole arrays (dst[i][0 .. n[i]) = src[i][0 .. n[i])) in one kernel,
+// for host arrays on a GPU that accesses pageable host memory directly.
+constexpr int kHostMoves = 8;
+struct HostMoves {
+    const double* src[kHostMoves] = {};
+    double* dst[kHostMoves] = {};
+    unsigned long long n[kHostMoves] = {};
+    int count = 0;
+};
+cudaError_t launchHostMove(cudaStream_t s, const HostMoves& m);
 // device SoA -> AoS with `nout` comps (all, or component 0 only)
 cudaError_t launchSoaToAos(cudaStream_t s, size_t N, int dg, int nout, const double* soa, double* aos);
 // Tools::MeanValue: writes partial sums per block into `partials` and the

@@ -338,6 +338,14 @@ class _KernelBase:
         self._check(self._l.nsdg_kernel_transport_variant(self._h, byref(t), byref(cm), byref(od)))
         return ("tiled" if t.value else "element"), cm.value, od.value
 
+    def host_direct(self) -> bool:
+        """Whether pageable host arrays move by a kernel that reads or writes
+        them directly (nsdg_kernel_host_direct; NSDG_HOST_DIRECT=0 turns it
+        off)."""
+        d = c_int()
+        self._check(self._l.nsdg_kernel_host_direct(self._h, byref(d)))
+        return bool(d.value)
+
     def viscosity_form(self) -> int:
         """The parallelogram stress kernel's evaluation of P/(8 alpha Delta)
         (nsdg_kernel_viscosity_form: 2, the default, the FP64 Newton step;

@@ -729,6 +729,39 @@ def test_largest_grid_within_oracle_sensitivity(gpu, oracle):
         g.close()
 
 
+def test_host_arrays_moved_by_kernel_match_copies(gpu, monkeypatch):
+    """Pageable host arrays (numpy) moved by the direct-access kernel
+    (set_data, get_dg0 and module_step; on a GPU that reads pageable host
+    memory) give bitwise the results of the copy-engine path
+    (NSDG_HOST_DIRECT=0), and page-locked arrays keep the copies."""
+    box = BoxTest(40, 36)
+    prm = dict(alpha=300.0, beta=300.0, n_steps=100)
+    d = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    monkeypatch.setenv("NSDG_HOST_DIRECT", "0")
+    c = _make(MEVPDynamicsKernel, box, 6, None, precision=1, **prm)
+    monkeypatch.delenv("NSDG_HOST_DIRECT")
+    assert not c.host_direct()
+    print("direct host access:", d.host_direct())
+    outs = ["hice", "cice", "u", "v", "uiostress", "viostress"]
+    for s in range(3):
+        uw, vw = box.wind(s * box.dt)
+        for k in (d, c):
+            k.setData("uwind", uw)
+            k.setData("vwind", vw)
+            k.update(s * box.dt, box.dt)
+        for n in outs:
+            np.testing.assert_array_equal(d.getDG0Data(n), c.getDG0Data(n), err_msg=f"step {s}: {n}")
+    for s in range(3, 5):
+        uw, vw = box.wind(s * box.dt)
+        inputs = {"uwind": uw, "vwind": vw, "hice": d.getDG0Data("hice"), "cice": d.getDG0Data("cice")}
+        a = d.module_step(s * box.dt, box.dt, inputs, outs)
+        b = c.module_step(s * box.dt, box.dt, inputs, outs)
+        for n in outs:
+            np.testing.assert_array_equal(a[n], b[n], err_msg=f"module step {s}: {n}")
+    d.close()
+    c.close()
+
+
 @pytest.mark.parametrize("rheology,precision", [("mevp", 0), ("mevp", 1), ("bbm", 0)])
 def test_module_step_matches_separate_calls(gpu, rheology, precision):
     """nsdg_kernel_module_step (the module step in one call: the inputs,
