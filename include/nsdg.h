@@ -231,9 +231,12 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
 /* Which mixed-precision mEVP stress kernel the updates use: *kind 0 =
  * operators by global loads, 1 = operator tiles by TMA, 2 = parallelogram
  * coefficients (chosen by timing at initialise; NSDG_STRESS_KERNEL =
- * global|tma|affine fixes it); *mismatch = the largest relative difference,
- * in FP64, between the exact operators and those rebuilt from parallelogram
- * coefficients (-1 when not evaluated, e.g. spherical or FP64 handles). */
+ * global|tma|affine fixes it); for a mixed-precision BBM handle 2 = the
+ * parallelogram BBM stress kernel, 0 = per-element operators
+ * (NSDG_BBM_STRESS_KERNEL=general); *mismatch = the largest relative
+ * difference, in FP64, between the exact operators and those rebuilt from
+ * parallelogram coefficients (-1 when not evaluated, e.g. spherical or FP64
+ * handles). */
 int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch);
 /* Which transport stage the updates use: *tiled 1 = the parallelogram-mesh
  * kernel (mixed-precision mEVP on a Cartesian parallelogram mesh without

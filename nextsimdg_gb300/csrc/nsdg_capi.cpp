@@ -476,6 +476,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         add(Ncg, 8);                                        // inverse lumped mass {hi, lo}
     }
     if (P.precision == NSDG_PRECISION_MIXED && bbm) {
+        add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
         add(ops.gx.size(), 4); add(ops.gy.size(), 4); add(ops.w.size(), 4); add(ops.wdam.size(), 4);
         add(ops.d1.size(), 4); add(ops.d2.size(), 4); add(ops.cellX8.size(), 4); add(ops.cellY8.size(), 4);
         if (mesh.spherical) {
@@ -657,6 +658,33 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         bbm32.dm = mesh.spherical ? upf(ops.dm) : nullptr;
         cellX8_32 = upf(ops.cellX8);
         cellY8_32 = upf(ops.cellY8);
+        // parallelogram meshes: 5 coefficients per element and the unit
+        // square's operators replace the per-element ones in the stress
+        // kernel (NSDG_BBM_STRESS_KERNEL=general keeps those)
+        const char* bk = std::getenv("NSDG_BBM_STRESS_KERNEL");
+        if (!mesh.spherical && !(bk && std::strcmp(bk, "general") == 0)) {
+            AffineStressOps aff;
+            AffineBbmOps abb;
+            const size_t ld = ops32Ld(N);
+            const bool okS = buildAffineStressOps(mesh, ops, ld, 1e-9, aff);
+            const bool okB = okS && buildAffineBbmOps(mesh, ops, 1e-9, abb);
+            affWorst = std::max(aff.worst, abb.worst);
+            if (okS && okB) {
+                float* coef = arena.take<float>(aff.coef.size());
+                if (!coef)
+                    e = cudaErrorMemoryAllocation;
+                else if (e == cudaSuccess)
+                    e = cudaMemcpy(coef, aff.coef.data(), aff.coef.size() * sizeof(float), cudaMemcpyHostToDevice);
+                if (e == cudaSuccess)
+                    e = uploadAffineReference(aff.ref);
+                if (e == cudaSuccess)
+                    e = uploadAffineBbmReference(abb.w, abb.wdam, dg, abb.dxi, abb.deta);
+                if (e == cudaSuccess) {
+                    bbm32.coef = coef;
+                    bbm32.ld = ld;
+                }
+            }
+        }
     }
     if (mixed() && !bbm) {
         {
@@ -2145,7 +2173,12 @@ int nsdg_kernel_stress_variant(nsdg_kernel* k, int* kind, double* mismatch)
         return NSDG_ERR_BAD_ARG;
     if (!k->ready)
         return k->fail(NSDG_ERR_BAD_ARG, "stress_variant: kernel not initialised");
-    *kind = k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP ? k->stressKind : -1;
+    if (k->mixed() && k->rheology == NSDG_RHEOLOGY_MEVP)
+        *kind = k->stressKind;
+    else if (k->mixed())
+        *kind = k->bbm32.coef ? 2 : 0; // BBM: the parallelogram kernel or the per-element operators
+    else
+        *kind = -1;
     *mismatch = k->affWorst;
     return k->ok();
 }

@@ -491,6 +491,56 @@ bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, d
     return out.worst <= tol;
 }
 
+bool buildAffineBbmOps(const HostMesh& m, const ElementOps& ops, double tol, AffineBbmOps& out, unsigned threads)
+{
+    const size_t N = m.nelements();
+    const int dg = ops.dg;
+    if (m.spherical || N == 0 || ops.w.size() != 72 * N || ops.wdam.size() != size_t(dg) * 9 * N
+        || ops.d1.size() != 72 * N || ops.d2.size() != 72 * N || dg * 9 > 72)
+        return false;
+    HostMesh u;
+    u.nx = u.ny = 1;
+    u.vx = { 0.0, 1.0, 0.0, 1.0 };
+    u.vy = { 0.0, 0.0, 1.0, 1.0 };
+    u.ice = { 1 };
+    ElementOps uo;
+    buildElementOps(u, dg, true, uo, 1);
+    for (int r = 0; r < 72; ++r) {
+        out.w[r] = uo.w[r];
+        out.dxi[r] = uo.d1[r];  // on the unit square c0 = 1, c1 = 0
+        out.deta[r] = uo.d2[r]; // and c2 = 0, c3 = 1
+    }
+    for (int r = 0; r < dg * 9; ++r)
+        out.wdam[r] = uo.wdam[r];
+    std::mutex mu;
+    out.worst = 0;
+    parallelFor(N, threads, [&](size_t lo, size_t hi) {
+        double worst = 0;
+        Geom g;
+        auto rel = [&](const std::vector<double>& exact, size_t rows, auto rebuilt, size_t e) {
+            double mx = 0, diff = 0;
+            for (size_t r = 0; r < rows; ++r) {
+                const double x = exact[r * N + e];
+                mx = std::max(mx, std::fabs(x));
+                diff = std::max(diff, std::fabs(x - rebuilt(r)));
+            }
+            return mx > 0 ? diff / mx : 0.0;
+        };
+        for (size_t e = lo; e < hi; ++e) {
+            geometry(m, e, 3, g);
+            const int qc = 4;
+            const double c[4] = { g.deta[1][qc], -g.dxi[1][qc], -g.deta[0][qc], g.dxi[0][qc] };
+            worst = std::max(worst, rel(ops.w, 72, [&](size_t r) { return out.w[r]; }, e));
+            worst = std::max(worst, rel(ops.wdam, size_t(dg) * 9, [&](size_t r) { return out.wdam[r]; }, e));
+            worst = std::max(worst, rel(ops.d1, 72, [&](size_t r) { return c[0] * out.dxi[r] + c[1] * out.deta[r]; }, e));
+            worst = std::max(worst, rel(ops.d2, 72, [&](size_t r) { return c[2] * out.dxi[r] + c[3] * out.deta[r]; }, e));
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        out.worst = std::max(out.worst, worst);
+    });
+    return out.worst <= tol;
+}
+
 bool buildAffineTransportOps(const HostMesh& m, const ElementOps& ops, double tol, double offDiagTol,
     AffineTransportOps& out, unsigned threads)
 {

@@ -142,6 +142,24 @@ struct AffineStressOps {
 bool buildAffineStressOps(const HostMesh& m, const ElementOps& ops, size_t ld, double tol,
     AffineStressOps& out, unsigned threads = 0);
 
+// Parallelogram meshes, BBM: the stress projection iMJwPSI (8 x 9) and the
+// damage projection (DG x 9) do not depend on J (M = J M_ref), and the
+// divergence operators are divS1 = c0 D_xi + c1 D_eta, divS2 = c2 D_xi +
+// c3 D_eta with D_xi[j][k] = sum_q w_q dphi_j/dxi(q) psi_k(q) (and D_eta) on
+// the unit square and c the coefficients above.
+struct AffineBbmOps {
+    double w[72] {};    // iMJwPSI [k][q]
+    double wdam[72] {}; // damage projection [k][q], k < dg
+    double dxi[72] {};  // D_xi [j][k]
+    double deta[72] {}; // D_eta [j][k]
+    double worst = 0;   // max relative mismatch of the rebuilt operators (FP64)
+};
+// Fills `out` and returns true if the mesh is Cartesian, `ops` has the BBM
+// operators, and every element's w, wdam, divS1 and divS2 rebuilt from the
+// unit square's and its coefficients match `ops` within `tol`.
+bool buildAffineBbmOps(const HostMesh& m, const ElementOps& ops, double tol, AffineBbmOps& out,
+    unsigned threads = 0);
+
 // Parallelogram meshes, transport: the cell operators of DGTransport
 // (J dT^{-T} grad psi_i w_q, ParametricMap.cpp:13-66) are
 //   cellX = c0 U_xi + c1 U_eta,   cellY = c2 U_xi + c3 U_eta

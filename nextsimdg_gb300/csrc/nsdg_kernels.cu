@@ -2465,13 +2465,33 @@ template <typename T> struct BbmOps {
     const double* hsize;
     const T* gm; // spherical metric terms (null on Cartesian meshes)
     const T* dm;
+    const float* coef = nullptr; // [5][ld] parallelogram coefficients (AFF kernels)
+    size_t ld = 0;
 };
+
+// The unit square's BBM operators for the parallelogram-mesh kernel (with
+// cAff's strain operators): iMJwPSI [k][q], the damage projection [k][q],
+// D_xi and D_eta [j][k] (divS1 = c0 D_xi + c1 D_eta, divS2 = c2 D_xi +
+// c3 D_eta)
+struct BbmAffTables {
+    float w[72];
+    float wdam[72];
+    float dxi[72];
+    float deta[72];
+};
+__constant__ BbmAffTables cBbmAff;
 
 // BBM stress, damage and divergence for one element.  T = double is the
 // reference's arithmetic; T = float is the mixed-precision kernel (FP32
 // operators and arithmetic, including exp/pow/sqrt; the stress, damage and
 // divergence are stored FP64 for the FP64 transport of the stress fields).
-template <int DG, typename T>
+// AFF (T = float on a parallelogram mesh): the strain from the unit
+// square's operators and the element's coefficients c (as the mEVP
+// parallelogram kernel), iMJwPSI and the damage projection from constant
+// memory, the divergence as D_xi (c0 s_a + c2 s_b) + D_eta (c1 s_a + c3 s_b):
+// 5 coefficients per element instead of 2 x 81 + 72 + 9 DG + 2 x 72
+// operator entries.
+template <int DG, typename T, bool AFF = false>
 __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, const double* __restrict__ u,
     const double* __restrict__ v, const double* __restrict__ h, const double* __restrict__ a,
     double* __restrict__ damage, double* __restrict__ s11, double* __restrict__ s12,
@@ -2505,6 +2525,12 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         c12[k] = static_cast<T>(s12[k * N + e]);
         c22[k] = static_cast<T>(s22[k * N + e]);
     }
+    float cf[5] = { 0.f, 0.f, 0.f, 0.f, 0.f };
+    if constexpr (AFF) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            cf[k] = o.coef[k * o.ld + e];
+    }
     const T dt = static_cast<T>(p.dt);
     const T nu0 = static_cast<T>(p.nu0);
     const T hi = static_cast<T>(o.hsize[e]);
@@ -2530,16 +2556,32 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         const T aG = fmin(fmax(as, T(0)), T(1));
         T dG = fmin(fmax(ds, T(1e-12)), T(1));
         T ex = T(0), ey = T(0), exv = T(0), eyu = T(0);
+        if constexpr (AFF) {
+            float ux = 0.f, ue = 0.f, vx = 0.f, ve = 0.f;
 #pragma unroll
-        for (int j = 0; j < 9; ++j) {
-            const T gxq = o.gx[(q * 9 + j) * N + e];
-            const T gyq = o.gy[(q * 9 + j) * N + e];
-            ex = fma(gxq, ul[j], ex);
-            ey = fma(gyq, vl[j], ey);
-            exv = fma(gxq, vl[j], exv);
-            eyu = fma(gyq, ul[j], eyu);
+            for (int j = 0; j < 9; ++j) {
+                const float gx = cAff[0][q * 9 + j], ge = cAff[1][q * 9 + j];
+                ux = fmaf(gx, ul[j], ux);
+                ue = fmaf(ge, ul[j], ue);
+                vx = fmaf(gx, vl[j], vx);
+                ve = fmaf(ge, vl[j], ve);
+            }
+            ex = cf[4] * fmaf(cf[0], ux, cf[1] * ue);
+            ey = cf[4] * fmaf(cf[2], vx, cf[3] * ve);
+            exv = cf[4] * fmaf(cf[0], vx, cf[1] * ve);
+            eyu = cf[4] * fmaf(cf[2], ux, cf[3] * ue);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const T gxq = o.gx[(q * 9 + j) * N + e];
+                const T gyq = o.gy[(q * 9 + j) * N + e];
+                ex = fma(gxq, ul[j], ex);
+                ey = fma(gyq, vl[j], ey);
+                exv = fma(gxq, vl[j], exv);
+                eyu = fma(gyq, ul[j], eyu);
+            }
         }
-        if (o.gm) { // spherical: e11 -= iMM v, e12 += iMM u / 2 (CGDynamicsKernel.cpp:331-334)
+        if (!AFF && o.gm) { // spherical: e11 -= iMM v, e12 += iMM u / 2 (CGDynamicsKernel.cpp:331-334)
             T mu = T(0), mv = T(0);
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
@@ -2606,14 +2648,14 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         g22 -= g22 * relax;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const T wk = o.w[(k * 9 + q) * N + e];
+            const T wk = AFF ? T(cBbmAff.w[k * 9 + q]) : o.w[(k * 9 + q) * N + e];
             n11[k] = fma(wk, g11, n11[k]);
             n12[k] = fma(wk, g12, n12[k]);
             n22[k] = fma(wk, g22, n22[k]);
         }
 #pragma unroll
         for (int k = 0; k < DG; ++k)
-            nd[k] = fma(o.wdam[(k * 9 + q) * N + e], dG, nd[k]);
+            nd[k] = fma(AFF ? T(cBbmAff.wdam[k * 9 + q]) : o.wdam[(k * 9 + q) * N + e], dG, nd[k]);
     }
     bool finite = true;
 #pragma unroll
@@ -2628,6 +2670,33 @@ __global__ void __launch_bounds__(kBlock) kBbmStress(DevMesh m, BbmOps<T> o, con
         damage[k * N + e] = nd[k];
     if (!finite)
         atomicOr(err, DEV_ERR_NONFINITE_STRESS);
+    if constexpr (AFF) {
+        // divS1 n11 + divS2 n12 = D_xi (c0 n11 + c2 n12) + D_eta (c1 n11 + c3 n12),
+        // divS1 n12 + divS2 n22 likewise
+        T ax[8], bx[8], ay[8], by[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            ax[k] = fmaf(cf[0], n11[k], cf[2] * n12[k]);
+            bx[k] = fmaf(cf[1], n11[k], cf[3] * n12[k]);
+            ay[k] = fmaf(cf[0], n12[k], cf[2] * n22[k]);
+            by[k] = fmaf(cf[1], n12[k], cf[3] * n22[k]);
+        }
+#pragma unroll 1
+        for (int j = 0; j < 9; ++j) {
+            T tx = T(0), ty = T(0);
+            if (ice) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float dxi = cBbmAff.dxi[j * 8 + k], deta = cBbmAff.deta[j * 8 + k];
+                    tx = fmaf(dxi, ax[k], fmaf(deta, bx[k], tx));
+                    ty = fmaf(dxi, ay[k], fmaf(deta, by[k], ty));
+                }
+            }
+            contrib[j * N + e] = tx;
+            contrib[(9 + j) * N + e] = ty;
+        }
+        return;
+    }
 #pragma unroll 1
     for (int j = 0; j < 9; ++j) {
         T tx = T(0), ty = T(0);
@@ -3148,6 +3217,20 @@ cudaError_t launchMevpStress32Tma(cudaStream_t s, const DevMesh& m, const Stress
     return cudaLaunchKernelEx(&cfg, kMevpStress32Tma<false>, maps.g, maps.a, m, u, v, Pg, hP, tdiv, p, err);
 }
 
+cudaError_t uploadAffineBbmReference(const double* w, const double* wdam, int dg, const double* dxi,
+    const double* deta)
+{
+    BbmAffTables t {};
+    for (int r = 0; r < 72; ++r) {
+        t.w[r] = static_cast<float>(w[r]);
+        t.dxi[r] = static_cast<float>(dxi[r]);
+        t.deta[r] = static_cast<float>(deta[r]);
+    }
+    for (int r = 0; r < dg * 9 && r < 72; ++r)
+        t.wdam[r] = static_cast<float>(wdam[r]);
+    return cudaMemcpyToSymbol(cBbmAff, &t, sizeof(t));
+}
+
 cudaError_t uploadAffineReference(const double ref[4][81])
 {
     float h[4][81];
@@ -3349,6 +3432,18 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
     double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32)
 {
     const unsigned g = blocksFor(m.N);
+    if (o32 && o32->coef) {
+        BbmOps<float> of { o32->gx, o32->gy, o32->w, o32->wdam, o32->d1, o32->d2, o.hsize, o32->gm, o32->dm };
+        of.coef = o32->coef;
+        of.ld = o32->ld;
+        switch (dg) {
+        case 1: kBbmStress<1, float, true><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        case 3: kBbmStress<3, float, true><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        case 6: kBbmStress<6, float, true><<<g, kBlock, 0, s>>>(m, of, u, v, h, a, damage, s11, s12, s22, contrib, p, err); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     if (o32) {
         const BbmOps<float> of { o32->gx, o32->gy, o32->w, o32->wdam, o32->d1, o32->d2, o.hsize, o32->gm, o32->dm };
         switch (dg) {

@@ -438,7 +438,14 @@ struct BbmOps32 {
     const float* d2;
     const float* gm; // spherical only
     const float* dm; // spherical only
+    // parallelogram meshes: [5][ld] coefficients; the stress kernel then takes
+    // the unit square's operators (uploadAffineReference,
+    // uploadAffineBbmReference) instead of the per-element ones above
+    const float* coef = nullptr;
+    size_t ld = 0;
 };
+cudaError_t uploadAffineBbmReference(const double* w, const double* wdam, int dg, const double* dxi,
+    const double* deta);
 cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, int dg, const double* u,
     const double* v, const double* h, const double* a, double* damage, double* s11, double* s12,
     double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32 = nullptr);

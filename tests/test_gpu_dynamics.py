@@ -502,6 +502,40 @@ def test_bbm_mixed_precision_close_to_oracle(gpu, oracle, n, steps):
     assert err["hice"] <= 1e-6 and err["cice"] <= 1e-6, err
     assert err["damage"] <= 1e-5, err
     assert np.abs(o.getDG0Data("u")).max() > 1e-3
+    kind, mismatch = g.stress_variant()  # the box takes the parallelogram BBM kernel
+    assert kind == "affine" and 0 <= mismatch <= 1e-9, (kind, mismatch)
+
+
+def test_bbm_parallelogram_kernel_matches_per_element_operators(gpu, monkeypatch):
+    """The mixed BBM stress kernel on a parallelogram mesh (5 coefficients
+    per element, the unit square's strain, projection and divergence
+    operators in constant memory) against the same kernel streaming each
+    element's FP32 operators (NSDG_BBM_STRESS_KERNEL=general), on a sheared
+    grid with land holes: FP32 rounding of the operators only (velocity
+    1e-6 m/s, damage 1e-6 RMS after three steps)."""
+    box = BoxTest(33, 20)
+    c = box.coords().copy()
+    c[:, 0] += 0.3 * c[:, 1]  # sheared: still parallelograms
+    box.coords = lambda c=c: c
+    m = box.mask()
+    m[5, 7] = m[12, 20] = m[3, 30] = 0.0
+    box.mask = lambda m=m: m
+    prm = dict(n_steps=50)
+    a = _make(BBMDynamicsKernel, box, 6, None, precision=1, **prm)
+    monkeypatch.setenv("NSDG_BBM_STRESS_KERNEL", "general")
+    b = _make(BBMDynamicsKernel, box, 6, None, precision=1, **prm)
+    monkeypatch.delenv("NSDG_BBM_STRESS_KERNEL")
+    assert a.stress_variant()[0] == "affine" and b.stress_variant()[0] == "global"
+    for k in (a, b):
+        k.setData("damage", box.damage())
+    _advance(a, box, 3)
+    _advance(b, box, 3)
+    rms = lambda x, y: float(np.sqrt(np.mean((x - y) ** 2)))  # noqa: E731
+    for f, bar in (("u", 1e-6), ("v", 1e-6), ("hice", 1e-7), ("cice", 1e-7), ("damage", 1e-6)):
+        assert rms(a.getDG0Data(f), b.getDG0Data(f)) <= bar, f
+    assert np.abs(b.getDG0Data("u")).max() > 1e-4
+    a.close()
+    b.close()
 
 
 def test_mixed_precision_snapshot_and_reproducible(gpu):
