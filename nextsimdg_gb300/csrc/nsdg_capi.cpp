@@ -122,6 +122,10 @@ struct nsdg_kernel {
     float* jwA32 = nullptr; // FP32 J w at the advection Gauss points (mixed-precision CG2DG)
     float2* invmHL = nullptr; // inverse lumped CG2 mass as {hi, lo} floats (mixed precision)
     BbmOps32 bbm32 {};        // FP32 BBM operators (mixed precision BBM)
+    // mixed BBM: the node terms fixed through the elastic sub-steps (FP32,
+    // formed by the step's node preparation)
+    BbmNodeConst32 bbmConst { nullptr, nullptr };
+    bool bbmK0 = false;
     float *cellX8_32 = nullptr, *cellY8_32 = nullptr; // FP32 DG8 stress-transport operators
     // which FP32 stress kernel the updates use (chosen by timing at
     // initialise): 0 operators by global loads, 1 operator tiles by TMA,
@@ -477,6 +481,7 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
     }
     if (P.precision == NSDG_PRECISION_MIXED && bbm) {
         add(5 * ops32Ld(N), 4);                   // parallelogram coefficients
+        add(4 * Ncg, 4); add(4 * Ncg, 4);         // the node constants of the sub-steps
         add(ops.gx.size(), 4); add(ops.gy.size(), 4); add(ops.w.size(), 4); add(ops.wdam.size(), 4);
         add(ops.d1.size(), 4); add(ops.d2.size(), 4); add(ops.cellX8.size(), 4); add(ops.cellY8.size(), 4);
         if (mesh.spherical) {
@@ -658,6 +663,11 @@ int nsdg_kernel::initialise(size_t nx, size_t ny, const double* coords, int sphe
         bbm32.dm = mesh.spherical ? upf(ops.dm) : nullptr;
         cellX8_32 = upf(ops.cellX8);
         cellY8_32 = upf(ops.cellY8);
+        bbmConst.k0 = arena.take<float4>(Ncg);
+        bbmConst.k1 = arena.take<float4>(Ncg);
+        if (!bbmConst.k0 || !bbmConst.k1)
+            e = cudaErrorMemoryAllocation;
+        bbmK0 = bbmConst.k0 && bbmConst.k1;
         // parallelogram meshes: 5 coefficients per element and the unit
         // square's operators replace the per-element ones in the stress
         // kernel (NSDG_BBM_STRESS_KERNEL=general keeps those)
@@ -998,11 +1008,12 @@ int nsdg_kernel::enqueuePhases(cudaStream_t s, double dt, int phases, int& launc
             P.exponent_relaxation_sigma, P.exponent_compression_factor, P.tan_phi, P.compr_strength, P.C_lab };
         bbmPowModes(bp);
         BbmNodeState st { u, v, avgU, avgV, cgH, cgA, uo, vo, ua, va, uGrad, vGrad };
-        LCH(launchBbmPrepNodes(s, dm, st));
+        const BbmNodeConst32* bc = (mixed() && bbmK0) ? &bbmConst : nullptr;
+        LCH(launchBbmPrepNodes(s, dm, st, &bp, bc));
         for (int it = 0; it < nS; ++it) {
             LCH(launchBbmStress(s, dm, dops, dg, u, v, hice, cice, damage, s11, s12, s22, contrib, bp, derr,
                 mixed() ? &bbm32 : nullptr));
-            LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr, mixed() ? invmHL : nullptr));
+            LCH(launchBbmMomentum(s, dm, dops, st, contrib, bp, derr, mixed() ? invmHL : nullptr, bc));
         }
     }
 #undef LCH
@@ -2108,7 +2119,7 @@ int nsdg_kernel_time_kernel(nsdg_kernel* k, int kernel_id, int reps, float* mean
             if (!bbm && k->mixed())
                 return launchMevpMomentum32(k->stream, k->dm, k->st32, k->tdiv32, mp, k->derr);
             return bbm ? launchBbmMomentum(k->stream, k->dm, k->dops, bs, k->contrib, bp, k->derr,
-                             k->mixed() ? k->invmHL : nullptr)
+                             k->mixed() ? k->invmHL : nullptr, (k->mixed() && k->bbmK0) ? &k->bbmConst : nullptr)
                        : launchMevpMomentum(k->stream, k->dm, k->dops, st, k->contrib, mp, k->derr);
         case 3:
         case 4:

@@ -2430,15 +2430,77 @@ __global__ void kWidenVelocity(size_t n, const float* __restrict__ u32, const fl
 // ===========================================================================
 // BBM (BBMStressUpdateStep.hpp:31-195, BrittleCGDynamicsKernel.hpp:206-254)
 // ===========================================================================
-__global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState st)
+__global__ void __launch_bounds__(kBlock) kBbmPrepNodes(size_t n, BbmNodeState st, BbmParams p,
+    BbmNodeConst32 c)
 {
     const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
     if (i >= n)
         return;
-    st.cgA[i] = fmax(fmin(st.cgA[i], 1.0), 1.e-4);
-    st.cgH[i] = fmax(st.cgH[i], 1.e-4);
+    const double Ad = fmax(fmin(st.cgA[i], 1.0), 1.e-4);
+    const double Hd = fmax(st.cgH[i], 1.e-4);
+    st.cgA[i] = Ad;
+    st.cgH[i] = Hd;
     st.avgU[i] = 0.0;
     st.avgV[i] = 0.0;
+    if (c.k0) {
+        // the FP32 node kernel's sub-step-invariant terms, formed as it forms them
+        const float H = static_cast<float>(Hd), A = static_cast<float>(Ad);
+        const float dt = static_cast<float>(p.dt), rho = static_cast<float>(p.rho_ice);
+        const float ua = static_cast<float>(st.ua[i]), va = static_cast<float>(st.va[i]);
+        const float dragAtm = A * static_cast<float>(p.F_atm) * hypotf(ua, va);
+        const float rhoHg = rho * H * static_cast<float>(p.gravity);
+        c.k0[i] = make_float4(dt / (rho * H), A * static_cast<float>(p.F_ocean), static_cast<float>(st.uo[i]),
+            static_cast<float>(st.vo[i]));
+        c.k1[i] = make_float4(dragAtm * ua, dragAtm * va, rhoHg * static_cast<float>(st.uGrad[i]),
+            rhoHg * static_cast<float>(st.vGrad[i]));
+    }
+}
+
+// The mixed-precision BBM node update from the step's FP32 node constants
+// (kBbmPrepNodes): per sub-step only the velocity, the gathered divergence
+// and the running averages are read.
+__global__ void __launch_bounds__(kBlock) kBbmMomentum32(DevMesh m, BbmNodeState st, BbmNodeConst32 c,
+    const double* __restrict__ contrib, BbmParams p, int* __restrict__ err, const float2* __restrict__ invmHL)
+{
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= m.Ncg)
+        return;
+    const int s2 = 2 * m.nx + 1;
+    const int i2 = static_cast<int>(static_cast<unsigned>(i) % static_cast<unsigned>(s2)), j2 = static_cast<int>(static_cast<unsigned>(i) / static_cast<unsigned>(s2));
+    const bool dir = m.cg2Dir[i] != 0;
+    const float4 k0 = c.k0[i], k1 = c.k1[i];
+    const float2 im = invmHL[i];
+    double dSx = 0.0, dSy = 0.0;
+    if (!dir)
+        gatherDivergence(m, i2, j2, contrib, dSx, dSy);
+    const float dt = static_cast<float>(p.dt);
+    const float cosA = static_cast<float>(p.cosA), sinA = static_cast<float>(p.sinA);
+    const float dteOverMass = k0.x, AFo = k0.y, uo = k0.z, vo = k0.w;
+    const float uIce = static_cast<float>(st.u[i]), vIce = static_cast<float>(st.v[i]);
+    const float cPrime = AFo * hypotf(uo - uIce, vo - vIce);
+    const float alpha = 1.f + dteOverMass * (cPrime * cosA);
+    const float beta = dt * static_cast<float>(p.fc) + dteOverMass * cPrime * sinA;
+    const float rDenom = 1.f / (alpha * alpha + beta * beta);
+    const float tauX = k1.x + cPrime * (uo * cosA - vo * sinA);
+    const float tauY = k1.y + cPrime * (vo * cosA + uo * sinA);
+    const float fx = static_cast<float>(dSx), fy = static_cast<float>(dSy);
+    const float gradX = fmaf(fx, im.y, fx * im.x) - k1.z;
+    const float gradY = fmaf(fy, im.y, fy * im.x) - k1.w;
+    float un = alpha * uIce + beta * vIce + dteOverMass * (alpha * (gradX + tauX) + beta * (gradY + tauY));
+    un *= rDenom;
+    float vn = alpha * vIce - beta * uIce + dteOverMass * (alpha * (gradY + tauY) + beta * (gradX + tauX));
+    vn *= rDenom;
+    if (!isfinite(un) || !isfinite(vn))
+        atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
+    const double invSteps = 1.0 / p.nSteps;
+    st.avgU[i] += static_cast<double>(un) * invSteps;
+    st.avgV[i] += static_cast<double>(vn) * invSteps;
+    if (dir) {
+        un = 0.f;
+        vn = 0.f;
+    }
+    st.u[i] = un;
+    st.v[i] = vn;
 }
 
 // x^y for x >= 0: by multiplication when y is a small integer (mode 1), times
@@ -3421,9 +3483,11 @@ cudaError_t launchIceOceanStress(cudaStream_t s, size_t n, int brittle, const do
     return cudaGetLastError();
 }
 
-cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st)
+cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st, const BbmParams* p,
+    const BbmNodeConst32* c)
 {
-    kBbmPrepNodes<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st);
+    const BbmNodeConst32 none { nullptr, nullptr };
+    kBbmPrepNodes<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m.Ncg, st, p ? *p : BbmParams {}, (c && p) ? *c : none);
     return cudaGetLastError();
 }
 
@@ -3465,9 +3529,11 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
 }
 
 cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o, const BbmNodeState& st,
-    const double* contrib, const BbmParams& p, int* err, const float2* invmHL)
+    const double* contrib, const BbmParams& p, int* err, const float2* invmHL, const BbmNodeConst32* c)
 {
-    if (invmHL)
+    if (invmHL && c && c->k0)
+        kBbmMomentum32<<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, st, *c, contrib, p, err, invmHL);
+    else if (invmHL)
         kBbmMomentum<float><<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err, invmHL);
     else
         kBbmMomentum<double><<<blocksFor(m.Ncg), kBlock, 0, s>>>(m, o, st, contrib, p, err, nullptr);

@@ -425,7 +425,17 @@ struct BbmNodeState {
     const double* uGrad;
     const double* vGrad;
 };
-cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st);
+// Mixed-precision BBM: the node terms that stay fixed through the elastic
+// sub-steps, in FP32, formed once per step by the preparation kernel:
+// k0 = (dt_sub / (rho H), A F_ocean, u_ocean, v_ocean), k1 = (the wind
+// stress tau_atm,x, tau_atm,y, rho H g dX_ssh, rho H g dY_ssh).
+struct BbmNodeConst32 {
+    float4* k0;
+    float4* k1;
+};
+// c (mixed precision, with p): also forms the FP32 node constants.
+cudaError_t launchBbmPrepNodes(cudaStream_t s, const DevMesh& m, const BbmNodeState& st,
+    const BbmParams* p = nullptr, const BbmNodeConst32* c = nullptr);
 // Per-step Gauss-point constants of the BBM update from h and A:
 // 0 hG, 1 expC, 2 Pmax, 3 elasticity, 4 Dunit_factor / dt ... (9 x 5 per element)
 // FP32 copies of the BBM element operators (mixed precision)
@@ -451,7 +461,7 @@ cudaError_t launchBbmStress(cudaStream_t s, const DevMesh& m, const DevOps& o, i
     double* s22, double* contrib, const BbmParams& p, int* err, const BbmOps32* o32 = nullptr);
 cudaError_t launchBbmMomentum(cudaStream_t s, const DevMesh& m, const DevOps& o,
     const BbmNodeState& st, const double* contrib, const BbmParams& p, int* err,
-    const float2* invmHL = nullptr);
+    const float2* invmHL = nullptr, const BbmNodeConst32* c = nullptr);
 
 // --- layout conversion, reductions ---------------------------------------
 // host ModelArray layout (AoS, nin comps) -> device SoA with `dg` comps,
