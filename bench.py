@@ -1125,16 +1125,25 @@ def run_ensemble(args):
 
 
 def run_profile(args):
-    """Setup plus warm-up and K device-resident steps, nothing else."""
+    """Setup plus warm-up and K device-resident steps, nothing else
+    (--rheology bbm: the BBM box test with the elastic sub-steps the grid
+    needs)."""
     from nextsimdg_gb300.boxtest import BoxTest
-    from nextsimdg_gb300.dynamics import MEVPDynamicsKernel
+    from nextsimdg_gb300.dynamics import BBMDynamicsKernel, MEVPDynamicsKernel
 
     box = BoxTest(args.nx)
-    k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS,
-                           precision=1 if args.precision == "mixed" else 0)
+    prec = 1 if args.precision == "mixed" else 0
+    if args.rheology == "bbm":
+        dx = box.L / box.nx
+        sub = max(NSTEPS, int(math.ceil(DT / (0.5 * dx / math.sqrt(5.9467e8 / 900.0)))))
+        k = BBMDynamicsKernel(dg_comp=DG, n_steps=int(math.ceil(sub / 50.0)) * 50, precision=prec)
+    else:
+        k = MEVPDynamicsKernel(dg_comp=DG, alpha=ALPHA, beta=BETA, n_steps=NSTEPS, precision=prec)
     k.initialise(box.coords(), False, box.mask())
     for name, arr in box.initial_fields().items():
         k.setData(name, arr)
+    if args.rheology == "bbm":
+        k.setData("damage", box.damage())
     for s in range(args.warmup + args.steps):
         k.update(s * DT, DT)
     k.synchronize()
@@ -1445,6 +1454,7 @@ def main():
                     help="one line per benchmark configuration: the oracle (all threads, one thread) beside the GPU")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident steps (for ncu captures): no e2e, no baselines")
+    ap.add_argument("--rheology", default="mevp", choices=["mevp", "bbm"], help="the rheology of --profile")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()

@@ -2473,17 +2473,17 @@ __global__ void __launch_bounds__(kBlock) kBbmMomentum32(DevMesh m, BbmNodeState
     double dSx = 0.0, dSy = 0.0;
     if (!dir)
         gatherDivergence(m, i2, j2, contrib, dSx, dSy);
-    const float dt = static_cast<float>(p.dt);
-    const float cosA = static_cast<float>(p.cosA), sinA = static_cast<float>(p.sinA);
+    const float dt = narrowAny(p.dt);
+    const float cosA = narrowAny(p.cosA), sinA = narrowAny(p.sinA);
     const float dteOverMass = k0.x, AFo = k0.y, uo = k0.z, vo = k0.w;
-    const float uIce = static_cast<float>(st.u[i]), vIce = static_cast<float>(st.v[i]);
+    const float uIce = narrowAny(st.u[i]), vIce = narrowAny(st.v[i]);
     const float cPrime = AFo * hypotf(uo - uIce, vo - vIce);
     const float alpha = 1.f + dteOverMass * (cPrime * cosA);
-    const float beta = dt * static_cast<float>(p.fc) + dteOverMass * cPrime * sinA;
+    const float beta = dt * narrowAny(p.fc) + dteOverMass * cPrime * sinA;
     const float rDenom = 1.f / (alpha * alpha + beta * beta);
     const float tauX = k1.x + cPrime * (uo * cosA - vo * sinA);
     const float tauY = k1.y + cPrime * (vo * cosA + uo * sinA);
-    const float fx = static_cast<float>(dSx), fy = static_cast<float>(dSy);
+    const float fx = narrowAny(dSx), fy = narrowAny(dSy);
     const float gradX = fmaf(fx, im.y, fx * im.x) - k1.z;
     const float gradY = fmaf(fy, im.y, fy * im.x) - k1.w;
     float un = alpha * uIce + beta * vIce + dteOverMass * (alpha * (gradX + tauX) + beta * (gradY + tauY));
@@ -2492,15 +2492,14 @@ __global__ void __launch_bounds__(kBlock) kBbmMomentum32(DevMesh m, BbmNodeState
     vn *= rDenom;
     if (!isfinite(un) || !isfinite(vn))
         atomicOr(err, DEV_ERR_NONFINITE_VELOCITY);
-    const double invSteps = 1.0 / p.nSteps;
-    st.avgU[i] += static_cast<double>(un) * invSteps;
-    st.avgV[i] += static_cast<double>(vn) * invSteps;
+    st.avgU[i] += widenAny(un) * p.invNSteps;
+    st.avgV[i] += widenAny(vn) * p.invNSteps;
     if (dir) {
         un = 0.f;
         vn = 0.f;
     }
-    st.u[i] = un;
-    st.v[i] = vn;
+    st.u[i] = widenAny(un);
+    st.v[i] = widenAny(vn);
 }
 
 // x^y for x >= 0: by multiplication when y is a small integer (mode 1), times
@@ -2546,7 +2545,9 @@ __constant__ BbmAffTables cBbmAff;
 // BBM stress, damage and divergence for one element.  T = double is the
 // reference's arithmetic; T = float is the mixed-precision kernel (FP32
 // operators and arithmetic, including exp/pow/sqrt; the stress, damage and
-// divergence are stored FP64 for the FP64 transport of the stress fields).
+// divergence are stored FP64 for the FP64 transport of the stress fields;
+// the conversions stay on the conversion unit: on the integer pipe, as in the
+// other mixed kernels, this kernel measured 9 % slower).
 // AFF (T = float on a parallelogram mesh): the strain from the unit
 // square's operators and the element's coefficients c (as the mEVP
 // parallelogram kernel), iMJwPSI and the damage projection from constant

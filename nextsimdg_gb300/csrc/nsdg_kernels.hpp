@@ -388,10 +388,12 @@ struct BbmParams {
     // how the kernels evaluate d^(n-1) (relaxation) and h^(m+1) (compression):
     // mode 1 = integer power k by multiplication, 2 = x^k sqrt(x), 0 = pow()
     int powRmode = 0, powRk = 0, powCmode = 0, powCk = 0;
+    double invNSteps = 0; // 1 / nSteps (set by bbmPowModes)
 };
 // Sets the power modes of p from its exponents (integers and half-integers up to 8).
 inline void bbmPowModes(BbmParams& p)
 {
+    p.invNSteps = 1.0 / p.nSteps;
     auto classify = [](double y, int& mode, int& k) {
         mode = 0;
         k = 0;
