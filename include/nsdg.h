@@ -429,6 +429,14 @@ int nsdg_kernel_warm_stats(nsdg_kernel* k, nsdg_warm_stats* out);
  * Mixed-precision handles use the parallelogram stress kernel when it is at
  * most 1e-9. */
 int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords, int dg_comp, double* mismatch);
+/* Host only (no GPU): every check that admits the parallelogram kernels, as
+ * out[4]: 0 the mEVP stress operators' mismatch (as above), 1 the transport
+ * cell operators rebuilt from the coefficients, 2 the largest off-diagonal of
+ * an element's M^{-1} relative to its diagonal, 3 the BBM projection and
+ * divergence operators rebuilt from the unit square's; FP64, relative.
+ * Mixed-precision handles take the tiled transport when 1 <= 1e-9 and
+ * 2 <= 1e-12, the parallelogram BBM kernel when 0 and 3 <= 1e-9. */
+int nsdg_mesh_parallelogram_checks(size_t nx, size_t ny, const double* coords, int dg_comp, double* out);
 
 /* The closed (Dirichlet) element sides a handle derives from its mask at
  * initialise (ParametricMesh::landmaskFromModelArray, dirichletFromMask,

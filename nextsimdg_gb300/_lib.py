@@ -165,6 +165,7 @@ SIGNATURES = [
     ("nsdg_selftest_viscosity_ff", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_selftest_viscosity_checked", c_int, [c_size_t, c_void_p, c_void_p, c_double, c_void_p]),
     ("nsdg_mesh_parallelogram_mismatch", c_int, [c_size_t, c_size_t, c_void_p, c_int, POINTER(c_double)]),
+    ("nsdg_mesh_parallelogram_checks", c_int, [c_size_t, c_size_t, c_void_p, c_int, c_void_p]),
     ("nsdg_mesh_dirichlet", c_int, [c_size_t, c_size_t, c_void_p, POINTER(c_size_t), c_void_p, c_size_t]),
     ("nsdg_mean_value_noalloc", c_int, [c_int, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("nsdg_ice_growth_default_params", None, [c_void_p]),

@@ -2953,6 +2953,38 @@ int nsdg_mesh_parallelogram_mismatch(size_t nx, size_t ny, const double* coords,
     return NSDG_OK;
 }
 
+int nsdg_mesh_parallelogram_checks(size_t nx, size_t ny, const double* coords, int dg_comp, double* out)
+{
+    if (!coords || !out || nx < 1 || ny < 1 || (dg_comp != 1 && dg_comp != 3 && dg_comp != 6))
+        return NSDG_ERR_BAD_ARG;
+    HostMesh m;
+    m.nx = nx;
+    m.ny = ny;
+    const size_t nn = (nx + 1) * (ny + 1);
+    m.vx.resize(nn);
+    m.vy.resize(nn);
+    for (size_t i = 0; i < nn; ++i) {
+        m.vx[i] = coords[2 * i];
+        m.vy[i] = coords[2 * i + 1];
+        if (!std::isfinite(m.vx[i]) || !std::isfinite(m.vy[i]))
+            return NSDG_ERR_BAD_ARG;
+    }
+    m.ice.assign(nx * ny, 1);
+    ElementOps ops;
+    buildElementOps(m, dg_comp, true, ops);
+    AffineStressOps aff;
+    buildAffineStressOps(m, ops, m.nelements(), 0.0, aff);
+    AffineTransportOps atr;
+    buildAffineTransportOps(m, ops, 0.0, 0.0, atr);
+    AffineBbmOps abb;
+    buildAffineBbmOps(m, ops, 0.0, abb);
+    out[0] = aff.worst;
+    out[1] = atr.worstCell;
+    out[2] = atr.worstOffDiag;
+    out[3] = abb.worst;
+    return NSDG_OK;
+}
+
 int nsdg_mesh_dirichlet(size_t nx, size_t ny, const double* mask, size_t* counts, size_t* ids, size_t capacity)
 {
     if (!mask || !counts || nx < 1 || ny < 1 || (capacity > 0 && !ids))

@@ -68,6 +68,24 @@ def parallelogram_mismatch(coords, nx: int, ny: int, dg_comp: int = 6) -> float:
     return out.value
 
 
+def parallelogram_checks(coords, nx: int, ny: int, dg_comp: int = 6) -> dict:
+    """Host only: every check that admits the parallelogram kernels
+    (nsdg_mesh_parallelogram_checks): the relative FP64 mismatch of the mEVP
+    stress operators, of the transport cell operators and of the BBM
+    operators rebuilt from the coefficients, and M^{-1}'s relative
+    off-diagonal."""
+    lib = _lib.load()
+    c = _f64(coords)
+    if c.size != 2 * (nx + 1) * (ny + 1):
+        raise ValueError("coords must hold (nx+1)(ny+1) vertices x 2")
+    out = np.zeros(4)
+    st = lib.nsdg_mesh_parallelogram_checks(nx, ny, _ptr(c), dg_comp, _ptr(out))
+    if st != _lib.NSDG_OK:
+        raise NsdgError(st, "parallelogram_checks failed")
+    return {"stress": float(out[0]), "transport_cell": float(out[1]), "minv_offdiag": float(out[2]),
+            "bbm": float(out[3])}
+
+
 def mesh_dirichlet(mask, nx: int, ny: int) -> list:
     """Host only: the closed (Dirichlet) element sides a handle derives from
     its mask at initialise, as four ascending arrays of element ids (bottom,

@@ -98,6 +98,31 @@ def test_parallelogram_mismatch_on_the_host(nsdg_lib):
         parallelogram_mismatch(sheared, n, n, 2)
 
 
+def test_parallelogram_checks_on_the_host(nsdg_lib):
+    """Host only: the checks behind the tiled transport and the parallelogram
+    BBM kernel.  On box and sheared meshes the transport cell operators and
+    the BBM projection and divergence operators rebuilt from the unit
+    square's match the exact ones to FP64 rounding and M^{-1} is diagonal (the
+    Legendre basis, constant J); a distorted mesh fails each check, as
+    expected."""
+    from nextsimdg_gb300.boxtest import BoxTest
+    from nextsimdg_gb300.dynamics import parallelogram_checks, parallelogram_mismatch
+    n = 12
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1))
+    sheared = np.stack([(1000.0 * i + 300.0 * j).ravel(), (-200.0 * i + 900.0 * j).ravel()], axis=1)
+    for coords, nx, ny in ((BoxTest(9, 14).coords(), 9, 14), (sheared, n, n)):
+        for dg in (1, 3, 6):
+            c = parallelogram_checks(coords, nx, ny, dg)
+            assert c["stress"] < 1e-12 and c["transport_cell"] < 1e-12, c
+            assert c["minv_offdiag"] < 1e-13 and c["bbm"] < 1e-12, c
+            assert c["stress"] == parallelogram_mismatch(coords, nx, ny, dg)
+    rng = np.random.default_rng(4)
+    distorted = sheared + rng.normal(0.0, 30.0, sheared.shape)
+    c = parallelogram_checks(distorted, n, n, 6)
+    assert c["stress"] > 1e-3 and c["transport_cell"] > 1e-3 and c["bbm"] > 1e-3, c
+    assert c["minv_offdiag"] > 1e-6, c  # a general quadrilateral's mass matrix is not diagonal
+
+
 def test_ice_growth_create_validates_arguments(nsdg_lib):
     """Host-side checks of the column-thermodynamics handle (no GPU call is
     made before they pass); the defaults equal the oracle's."""
