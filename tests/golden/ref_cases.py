@@ -41,6 +41,14 @@ CASES = {
     # spherical meshes (coordinates in radians, DynamicsKernel.hpp:44-75)
     "mevp_sph_dg3_a1500_20x16": dict(rheology=0, dg=3, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
     "mevp_sph_dg6_a1500_20x16": dict(rheology=0, dg=6, alpha=1500.0, nx=20, ny=16, steps=3, sub=100, sphere=True),
+    # degenerate grids and masks: two rows, two columns, one ice cell in land,
+    # a checkerboard of ice and land (every ice cell's edges closed)
+    "mevp_dg6_a300_9x2": dict(rheology=0, dg=6, alpha=300.0, nx=9, ny=2, steps=3, sub=100),
+    "mevp_dg3_a300_2x7": dict(rheology=0, dg=3, alpha=300.0, nx=2, ny=7, steps=3, sub=100),
+    "mevp_dg6_a300_7x6_one": dict(rheology=0, dg=6, alpha=300.0, nx=7, ny=6, steps=3, sub=100, mask="one"),
+    "mevp_dg6_a300_33x3_checker": dict(rheology=0, dg=6, alpha=300.0, nx=33, ny=3, steps=3, sub=100,
+                                       mask="checker"),
+    "bbm_dg6_10x8_checker": dict(rheology=1, dg=6, alpha=1500.0, nx=10, ny=8, steps=2, sub=50, mask="checker"),
 }
 
 
@@ -98,6 +106,13 @@ def box(case: dict):
         rng = np.random.default_rng(5)
         for _ in range(12):
             m[rng.integers(1, case["ny"] - 1), rng.integers(1, case["nx"] - 1)] = 0.0
+        b.mask = lambda m=m: m
+    if case.get("mask"):
+        m = np.zeros((case["ny"], case["nx"]))
+        if case["mask"] == "one":
+            m[case["ny"] // 2, case["nx"] // 2] = 1.0
+        else:  # checkerboard
+            m[(np.add.outer(np.arange(case["ny"]), np.arange(case["nx"])) % 2) == 0] = 1.0
         b.mask = lambda m=m: m
     return b
 

@@ -49,6 +49,33 @@ def test_fp64_matches_reference(gpu, ref_goldens, name, stress, monkeypatch):
     assert max(worst.values()) <= TOL, worst
 
 
+DEGENERATE = ["mevp_dg6_a300_9x2", "mevp_dg3_a300_2x7", "mevp_dg6_a300_7x6_one", "mevp_dg6_a300_33x3_checker",
+              "bbm_dg6_10x8_checker"]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", DEGENERATE)
+def test_degenerate_cases_match_reference(gpu, ref_goldens, name, precision):
+    """Two-row and two-column grids, one ice cell in land, a checkerboard of
+    ice and land (mEVP and BBM) against the reference build: FP64 within
+    1e-10 of every read-out; mixed precision within its stated tolerance."""
+    cases, data = ref_goldens
+    case = cases.CASES[name]
+    k = _kernel(case, precision)
+    got = cases.readouts(cases.run(k, case), case)
+    k.close()
+    ref = data[name]
+    if precision == 0:
+        worst = cases.compare(got, ref)
+        assert max(worst.values()) <= TOL, worst
+    else:
+        rms = lambda a: float(np.sqrt(np.mean(a * a)))  # noqa: E731
+        du = rms(np.hypot(got["dg0_u"] - ref["dg0_u"], got["dg0_v"] - ref["dg0_v"]))
+        dh = rms(got["dg0_hice"] - ref["dg0_hice"])
+        da = rms(got["dg0_cice"] - ref["dg0_cice"])
+        assert du <= 1e-5 and dh <= 1e-6 and da <= 1e-6, (du, dh, da)
+
+
 @pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg6_a1500_32x32", "mevp_dg6_a300_64x64",
                                   "mevp_dg3_a1500_64x64"])
 def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, name):
