@@ -19,7 +19,7 @@ import numpy as np
 from nextsimdg_gb300.boxtest import BoxTest
 
 # name: rheology (0 mEVP, 1 BBM), DG components, alpha = beta, grid, model
-# steps, sub-cycle count, land holes, read-out mode
+# steps, sub-cycle count, land holes, mask, vertex displacement, read-out mode
 CASES = {
     "mevp_dg6_a300_12x12": dict(rheology=0, dg=6, alpha=300.0, nx=12, ny=12, steps=3, sub=100),
     "mevp_dg3_a300_17x18": dict(rheology=0, dg=3, alpha=300.0, nx=17, ny=18, steps=3, sub=100),
@@ -49,6 +49,14 @@ CASES = {
     "mevp_dg6_a300_33x3_checker": dict(rheology=0, dg=6, alpha=300.0, nx=33, ny=3, steps=3, sub=100,
                                        mask="checker"),
     "bbm_dg6_10x8_checker": dict(rheology=1, dg=6, alpha=1500.0, nx=10, ny=8, steps=2, sub=50, mask="checker"),
+    # general quadrilaterals: the box's vertices displaced as in the
+    # reference's distorted advection mesh (Advection_test.cpp:213-217), so the
+    # Jacobian varies inside each element and no operator is affine
+    "mevp_dg6_a300_20x18_distorted": dict(rheology=0, dg=6, alpha=300.0, nx=20, ny=18, steps=3, sub=100,
+                                          distort=0.05),
+    "mevp_dg3_a1500_16x16_distorted": dict(rheology=0, dg=3, alpha=1500.0, nx=16, ny=16, steps=3, sub=100,
+                                           distort=0.05),
+    "bbm_dg6_14x12_distorted": dict(rheology=1, dg=6, alpha=1500.0, nx=14, ny=12, steps=2, sub=50, distort=0.05),
 }
 
 
@@ -95,7 +103,7 @@ DG0_NAMES = ("hice", "cice", "u", "v", "uiostress", "viostress")
 def box(case: dict):
     if case.get("sphere"):
         return SphereCase(case["nx"], case["ny"])
-    b = BoxTest(case["nx"], case["ny"])
+    b = BoxTest(case["nx"], case["ny"], distort=case.get("distort", 0.0))
     if case.get("ssh"):
         # a tilted, wavy sea surface of the given amplitude (m)
         X, Y = np.meshgrid((np.arange(b.nx) + 0.5) / b.nx, (np.arange(b.ny) + 0.5) / b.ny)

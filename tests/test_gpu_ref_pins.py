@@ -76,6 +76,19 @@ def test_degenerate_cases_match_reference(gpu, ref_goldens, name, precision):
         assert du <= 1e-5 and dh <= 1e-6 and da <= 1e-6, (du, dh, da)
 
 
+DISTORTED = ["mevp_dg6_a300_20x18_distorted", "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted"]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", DISTORTED)
+def test_general_quadrilaterals_match_reference(gpu, ref_goldens, name, precision):
+    """General quadrilaterals (the box's vertices displaced as in the
+    reference's distorted advection mesh) against the reference build: the
+    per-element operator kernels of both paths, FP64 within 1e-10 of every
+    read-out, mixed precision within its stated tolerance."""
+    test_degenerate_cases_match_reference(gpu, ref_goldens, name, precision)
+
+
 @pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg6_a1500_32x32", "mevp_dg6_a300_64x64",
                                   "mevp_dg3_a1500_64x64"])
 def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, name):

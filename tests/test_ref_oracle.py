@@ -45,7 +45,7 @@ def test_reference_build_reproduces_transport_goldens(goldens):
 
 
 SMALL = ["mevp_dg6_a300_12x12", "mevp_dg1_a300_16x16", "bbm_dg3_16x12", "mevp_sph_dg3_a1500_20x16",
-         "mevp_dg6_a300_33x3_checker", "bbm_dg6_10x8_checker"]
+         "mevp_dg6_a300_33x3_checker", "bbm_dg6_10x8_checker", "bbm_dg6_14x12_distorted"]
 
 
 @needs_ref
@@ -66,7 +66,8 @@ def test_fixture_is_the_reference_output(ref_goldens, name):
                                   "mevp_dg6_a1500_256x256", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_16x14_ssh",
                                   "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16", "mevp_dg6_a300_9x2",
                                   "mevp_dg3_a300_2x7", "mevp_dg6_a300_7x6_one", "mevp_dg6_a300_33x3_checker",
-                                  "bbm_dg6_10x8_checker"])
+                                  "bbm_dg6_10x8_checker", "mevp_dg6_a300_20x18_distorted",
+                                  "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted"])
 def test_restatement_matches_reference(oracle, ref_goldens, name):
     """oracle/nsdg_oracle.cpp against the reference's own results: every
     read-out (h, A, damage in all DG components; u, v and the ice-ocean
