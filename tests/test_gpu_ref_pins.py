@@ -90,7 +90,10 @@ def test_general_quadrilaterals_match_reference(gpu, ref_goldens, name, precisio
 
 
 @pytest.mark.parametrize("name", ["mevp_dg6_a300_12x12", "mevp_dg6_a1500_32x32", "mevp_dg6_a300_64x64",
-                                  "mevp_dg3_a1500_64x64"])
+                                  "mevp_dg3_a1500_64x64", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16",
+                                  "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_14x14",
+                                  "bbm_dg3_16x12", "bbm_dg6_16x14_ssh", "mevp_sph_dg3_a1500_20x16",
+                                  "mevp_sph_dg6_a1500_20x16"])
 def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, name):
     """Mixed precision (FP32 bulk; FP64 conservation sums, inverse mass
     matrices, Delta and viscosity) against the reference's FP64 results."""
@@ -104,4 +107,5 @@ def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, 
     dh = rms(k.getDG0Data("hice") - ref["dg0_hice"])
     da = rms(k.getDG0Data("cice") - ref["dg0_cice"])
     k.close()
+    print(f"{name} mixed vs reference: velocity RMS {du:.2e} m/s, h RMS {dh:.2e} m, A RMS {da:.2e}")
     assert du <= 1e-5 and dh <= 1e-6 and da <= 1e-6, (du, dh, da)
