@@ -19,7 +19,8 @@ TOL = 1e-10
 ALL = ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16", "mevp_dg6_a1500_32x32",
        "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64", "mevp_dg3_a1500_64x64", "bbm_dg6_14x14",
        "bbm_dg3_16x12", "mevp_dg6_a1500_256x256", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_16x14_ssh",
-       "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16"]
+       "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16", "mevp_dg6_a300_20x18_distorted",
+       "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted"]
 
 
 def _kernel(case, precision):
