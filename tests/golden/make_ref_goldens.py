@@ -47,7 +47,7 @@ def main() -> None:
     arrays = {}
     for name, case in ref_cases.CASES.items():
         t0 = time.time()
-        k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], case["alpha"], case["sub"])
+        k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], ref_cases.beta(case), case["sub"])
         ref_cases.run(k, case)
         for key, a in ref_cases.readouts(k, case).items():
             arrays[f"{name}/{key}"] = np.asarray(a, dtype=np.float64)

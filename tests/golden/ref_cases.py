@@ -18,7 +18,7 @@ import numpy as np
 
 from nextsimdg_gb300.boxtest import BoxTest
 
-# name: rheology (0 mEVP, 1 BBM), DG components, alpha = beta, grid, model
+# name: rheology (0 mEVP, 1 BBM), DG components, alpha (= beta unless set), grid, model
 # steps, sub-cycle count, land holes, mask, vertex displacement, read-out mode
 CASES = {
     "mevp_dg6_a300_12x12": dict(rheology=0, dg=6, alpha=300.0, nx=12, ny=12, steps=3, sub=100),
@@ -57,7 +57,16 @@ CASES = {
     "mevp_dg3_a1500_16x16_distorted": dict(rheology=0, dg=3, alpha=1500.0, nx=16, ny=16, steps=3, sub=100,
                                            distort=0.05),
     "bbm_dg6_14x12_distorted": dict(rheology=1, dg=6, alpha=1500.0, nx=14, ny=12, steps=2, sub=50, distort=0.05),
+    # unequal mEVP relaxation constants (alpha for the stress, beta for the
+    # velocity): a swap of the two shows here and in no case above
+    "mevp_dg6_a300_b1500_18x16": dict(rheology=0, dg=6, alpha=300.0, beta=1500.0, nx=18, ny=16, steps=3, sub=100),
+    "mevp_dg3_a1500_b300_16x18": dict(rheology=0, dg=3, alpha=1500.0, beta=300.0, nx=16, ny=18, steps=3, sub=100),
 }
+
+
+def beta(case: dict) -> float:
+    """The case's mEVP beta (equal to alpha unless the case sets it)."""
+    return case.get("beta", case["alpha"])
 
 
 class SphereCase:

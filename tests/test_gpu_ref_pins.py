@@ -20,14 +20,15 @@ ALL = ["mevp_dg6_a300_12x12", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16", "mev
        "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a300_64x64", "mevp_dg3_a1500_64x64", "bbm_dg6_14x14",
        "bbm_dg3_16x12", "mevp_dg6_a1500_256x256", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_16x14_ssh",
        "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16", "mevp_dg6_a300_20x18_distorted",
-       "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted"]
+       "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted", "mevp_dg6_a300_b1500_18x16",
+       "mevp_dg3_a1500_b300_16x18"]
 
 
 def _kernel(case, precision):
     if case["rheology"] == 1:
         return BBMDynamicsKernel(dg_comp=case["dg"], n_steps=case["sub"], precision=precision)
-    return MEVPDynamicsKernel(dg_comp=case["dg"], alpha=case["alpha"], beta=case["alpha"], n_steps=case["sub"],
-                              precision=precision)
+    return MEVPDynamicsKernel(dg_comp=case["dg"], alpha=case["alpha"], beta=case.get("beta", case["alpha"]),
+                              n_steps=case["sub"], precision=precision)
 
 
 @pytest.mark.parametrize("stress", ["fma", "pairs", "pairs_tma"])
@@ -94,7 +95,8 @@ def test_general_quadrilaterals_match_reference(gpu, ref_goldens, name, precisio
                                   "mevp_dg3_a1500_64x64", "mevp_dg3_a300_17x18", "mevp_dg1_a300_16x16",
                                   "mevp_dg6_a1500_20x15_holes", "mevp_dg6_a1500_24x20_ssh", "bbm_dg6_14x14",
                                   "bbm_dg3_16x12", "bbm_dg6_16x14_ssh", "mevp_sph_dg3_a1500_20x16",
-                                  "mevp_sph_dg6_a1500_20x16"])
+                                  "mevp_sph_dg6_a1500_20x16", "mevp_dg6_a300_b1500_18x16",
+                                  "mevp_dg3_a1500_b300_16x18"])
 def test_mixed_precision_within_stated_tolerance_of_reference(gpu, ref_goldens, name):
     """Mixed precision (FP32 bulk; FP64 conservation sums, inverse mass
     matrices, Delta and viscosity) against the reference's FP64 results."""

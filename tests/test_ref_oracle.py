@@ -45,7 +45,8 @@ def test_reference_build_reproduces_transport_goldens(goldens):
 
 
 SMALL = ["mevp_dg6_a300_12x12", "mevp_dg1_a300_16x16", "bbm_dg3_16x12", "mevp_sph_dg3_a1500_20x16",
-         "mevp_dg6_a300_33x3_checker", "bbm_dg6_10x8_checker", "bbm_dg6_14x12_distorted"]
+         "mevp_dg6_a300_33x3_checker", "bbm_dg6_10x8_checker", "bbm_dg6_14x12_distorted",
+         "mevp_dg6_a300_b1500_18x16"]
 
 
 @needs_ref
@@ -54,7 +55,7 @@ def test_fixture_is_the_reference_output(ref_goldens, name):
     """The stored fixture is what the reference build computes now."""
     cases, data = ref_goldens
     case = cases.CASES[name]
-    k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], case["alpha"], case["sub"])
+    k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], cases.beta(case), case["sub"])
     got = cases.readouts(cases.run(k, case), case)
     for key, want in data[name].items():
         np.testing.assert_array_equal(got[key], want, err_msg=key)
@@ -67,7 +68,8 @@ def test_fixture_is_the_reference_output(ref_goldens, name):
                                   "mevp_sph_dg3_a1500_20x16", "mevp_sph_dg6_a1500_20x16", "mevp_dg6_a300_9x2",
                                   "mevp_dg3_a300_2x7", "mevp_dg6_a300_7x6_one", "mevp_dg6_a300_33x3_checker",
                                   "bbm_dg6_10x8_checker", "mevp_dg6_a300_20x18_distorted",
-                                  "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted"])
+                                  "mevp_dg3_a1500_16x16_distorted", "bbm_dg6_14x12_distorted",
+                                  "mevp_dg6_a300_b1500_18x16", "mevp_dg3_a1500_b300_16x18"])
 def test_restatement_matches_reference(oracle, ref_goldens, name):
     """oracle/nsdg_oracle.cpp against the reference's own results: every
     read-out (h, A, damage in all DG components; u, v and the ice-ocean
@@ -77,7 +79,7 @@ def test_restatement_matches_reference(oracle, ref_goldens, name):
     step 8 (alpha = beta = 1500)."""
     cases, data = ref_goldens
     case = cases.CASES[name]
-    k = oracle.OracleKernel(case["rheology"], case["dg"], alpha=case["alpha"], beta=case["alpha"],
+    k = oracle.OracleKernel(case["rheology"], case["dg"], alpha=case["alpha"], beta=cases.beta(case),
                             n_steps=case["sub"])
     got = cases.readouts(cases.run(k, case), case)
     worst = cases.compare(got, data[name])
@@ -131,7 +133,7 @@ def test_reference_ssh_cases_single_threaded(ref_goldens, name):
     try:
         runs = []
         for _ in range(2):
-            k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], case["alpha"], case["sub"])
+            k = pyref.RefKernel(case["rheology"], case["dg"], case["alpha"], cases.beta(case), case["sub"])
             runs.append(cases.readouts(cases.run(k, case), case))
             k.close()
     finally:
