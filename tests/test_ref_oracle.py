@@ -8,7 +8,8 @@ reference's transport tests and the stored fixture; everywhere, the C++
 restatement (oracle/nsdg_oracle.cpp) must reproduce the fixture
 (tests/golden/ref_dynamics.npz, made by tests/golden/make_ref_goldens.py):
 full mEVP and BBM model steps on box tests, 12 x 12 to 256 x 256, DG 1/3/6,
-alpha = beta = 300 and 1500, land holes, at 1e-10 relative.
+alpha and beta of 300 and 1500, land holes, degenerate grids and masks,
+general quadrilaterals and spherical patches, at 1e-10 relative.
 """
 import sys
 from pathlib import Path
@@ -141,3 +142,23 @@ def test_reference_ssh_cases_single_threaded(ref_goldens, name):
     for key, want in data[name].items():
         np.testing.assert_array_equal(runs[0][key], runs[1][key], err_msg=key)
         np.testing.assert_array_equal(runs[0][key], want, err_msg=key)
+
+
+def test_every_case_the_gpu_pins_name_has_a_fixture(ref_goldens):
+    """Each case named by the GPU pin tests (tests/test_gpu_ref_pins.py) is
+    defined in ref_cases.py and stored in the fixture, and each stored case
+    has its read-outs: a misspelt or missing case fails here, on the CPU,
+    rather than only where a GPU runs those tests."""
+    import test_gpu_ref_pins as pins
+    cases, data = ref_goldens
+    named = set(pins.ALL) | set(pins.DEGENERATE) | set(pins.DISTORTED)
+    for fn in (v for k, v in vars(pins).items() if k.startswith("test_")):
+        for mark in getattr(fn, "pytestmark", []):
+            if mark.name == "parametrize" and mark.args[0] == "name":
+                named |= set(mark.args[1])
+    assert named, "no cases found"
+    missing = sorted(n for n in named if n not in cases.CASES or n not in data)
+    assert not missing, missing
+    assert set(data) == set(cases.CASES), set(data) ^ set(cases.CASES)
+    for name in named:
+        assert {"dg0_hice", "dg0_cice", "dg0_u", "dg0_v"} <= set(data[name]), name
