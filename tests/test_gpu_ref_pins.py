@@ -2,8 +2,9 @@
 
 The fixture tests/golden/ref_dynamics.npz holds the read-outs of the
 reference's dynamics code (its unmodified sources built with the project's
-Eigen subset, oracle/_ref) on the box-test and spherical cases of
-tests/golden/ref_cases.py.  The FP64 path must match every read-out within
+Eigen subset, oracle/_ref) on the cases of tests/golden/ref_cases.py: box
+tests with land holes, sea-surface height, unequal alpha and beta,
+degenerate grids and masks, general quadrilaterals, and spherical patches.  The FP64 path must match every read-out within
 1e-10 of the reference's magnitude; the mixed-precision path within its
 stated tolerance (velocity RMS <= 1e-5 m/s, h and A RMS <= 1e-6).
 """
