@@ -61,6 +61,9 @@ CASES = {
     # velocity): a swap of the two shows here and in no case above
     "mevp_dg6_a300_b1500_18x16": dict(rheology=0, dg=6, alpha=300.0, beta=1500.0, nx=18, ny=16, steps=3, sub=100),
     "mevp_dg3_a1500_b300_16x18": dict(rheology=0, dg=3, alpha=1500.0, beta=300.0, nx=16, ny=18, steps=3, sub=100),
+    # BBM over six steps on a larger grid (damage down to 0.05): the
+    # reference's own response to h x (1 + 1e-14) stays near 2e-14 here
+    "bbm_dg3_40x40_6steps": dict(rheology=1, dg=3, alpha=1500.0, nx=40, ny=40, steps=6, sub=50),
 }
 
 
